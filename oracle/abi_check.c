@@ -1,0 +1,61 @@
+/*
+ * Prints the size and field offsets of every struct of the node contract.
+ * Compiled twice (oracle/Makefile `abi`): once against the reference's own
+ * headers (src/types.h, expr.h, group_agg.h, join.h, filter.h, project.h)
+ * and once against include/vectra_abi.h.  tests/test_abi_layout.py requires
+ * identical output; tests/golden/abi_layout.txt holds the reference's copy
+ * so the check also runs where the reference checkout is absent.
+ * TEST INFRASTRUCTURE ONLY.
+ */
+#include <stdio.h>
+#include <stddef.h>
+
+#ifdef USE_REF_HEADERS
+#include "types.h"
+#include "expr.h"
+#include "agg_ops.h"
+#include "group_agg.h"
+#include "join.h"
+#include "filter.h"
+#include "project.h"
+typedef JoinNode JoinPrefixT;
+#else
+#include "vectra_abi.h"
+typedef JoinNodePrefix JoinPrefixT;
+#endif
+
+#define S(T) printf("sizeof %s %zu\n", #T, sizeof(T))
+#define O(T, f) printf("offsetof %s.%s %zu\n", #T, #f, offsetof(T, f))
+
+int main(void) {
+    S(VecArray); O(VecArray, type); O(VecArray, length); O(VecArray, validity);
+    O(VecArray, owns_data); O(VecArray, buf.i64); O(VecArray, buf.str.offsets);
+    O(VecArray, buf.str.data); O(VecArray, buf.str.data_len);
+    S(VecBatch); O(VecBatch, n_rows); O(VecBatch, n_cols); O(VecBatch, col_names);
+    O(VecBatch, columns); O(VecBatch, sel); O(VecBatch, sel_n);
+    S(VecSchema); O(VecSchema, n_cols); O(VecSchema, col_names);
+    O(VecSchema, col_types); O(VecSchema, col_annotations);
+    S(VecNode); O(VecNode, next_batch); O(VecNode, free_node);
+    O(VecNode, output_schema); O(VecNode, kind);
+    S(VecExpr); O(VecExpr, kind); O(VecExpr, result_type); O(VecExpr, col_name);
+    O(VecExpr, lit_i64); O(VecExpr, lit_dbl); O(VecExpr, lit_bln);
+    O(VecExpr, lit_str); O(VecExpr, op); O(VecExpr, op2); O(VecExpr, left);
+    O(VecExpr, right); O(VecExpr, operand); O(VecExpr, cond);
+    O(VecExpr, then_expr); O(VecExpr, else_expr); O(VecExpr, cast_to);
+    S(AggSpec); O(AggSpec, output_name); O(AggSpec, kind); O(AggSpec, input_col);
+    O(AggSpec, na_rm);
+    S(GroupAggNode); O(GroupAggNode, child); O(GroupAggNode, n_keys);
+    O(GroupAggNode, key_names); O(GroupAggNode, n_aggs);
+    O(GroupAggNode, agg_specs); O(GroupAggNode, done); O(GroupAggNode, use_sorted);
+    S(JoinKey); O(JoinKey, left_col); O(JoinKey, right_col);
+    O(JoinPrefixT, left); O(JoinPrefixT, right); O(JoinPrefixT, kind);
+    O(JoinPrefixT, n_keys); O(JoinPrefixT, keys); O(JoinPrefixT, suffix_x);
+    O(JoinPrefixT, suffix_y);
+    S(FilterNode); O(FilterNode, child); O(FilterNode, predicate);
+    S(ProjEntry); O(ProjEntry, output_name); O(ProjEntry, expr);
+    S(ProjectNode); O(ProjectNode, child); O(ProjectNode, n_entries);
+    O(ProjectNode, entries);
+    printf("enum VEC_STRING %d EXPR_GREPL %d AGG_MAX %d JOIN_ANTI %d\n",
+           (int)VEC_STRING, (int)EXPR_GREPL, (int)AGG_MAX, (int)JOIN_ANTI);
+    return 0;
+}

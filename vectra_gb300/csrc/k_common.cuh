@@ -1,0 +1,234 @@
+// k_common.cuh -- device helpers shared by libvgpu's kernels (sm_103a).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "vgpu_internal.h"
+
+#define VG_DEV __device__ __forceinline__
+
+// number of kernels this library has launched (reported by the benchmark)
+extern "C" unsigned long long vg_launch_counter;
+
+// ---------------------------------------------------------------------
+// validity bits and column loads
+// ---------------------------------------------------------------------
+
+VG_DEV bool vg_valid(const VgCol &c, int64_t r) {
+    return c.valid == nullptr || ((__ldg(c.valid + (r >> 5)) >> (r & 31)) & 1u);
+}
+
+// 64-bit payload of a column value: int64 as is, double as its bit
+// pattern, bool as 0/1.
+VG_DEV uint64_t vg_load_bits(const VgCol &c, int64_t r) {
+    if (c.type == VEC_BOOL) return (uint64_t)__ldg((const unsigned char *)c.data + r);
+    return (uint64_t)__ldg((const unsigned long long *)c.data + r);
+}
+
+VG_DEV double vg_bits_to_f64(uint64_t b) { return __longlong_as_double((long long)b); }
+VG_DEV uint64_t vg_f64_to_bits(double d) { return (uint64_t)__double_as_longlong(d); }
+
+// Order-preserving integer image of a double's bit pattern: for non-NaN x,y
+// x < y  <=>  ord(x) < ord(y) (as signed int64), with -0 just below +0.
+VG_DEV int64_t vg_ord(uint64_t bits) {
+    int64_t s = (int64_t)bits;
+    return s >= 0 ? s : (int64_t)(bits ^ 0x7FFFFFFFFFFFFFFFull);
+}
+VG_DEV uint64_t vg_unord(int64_t o) {
+    return o >= 0 ? (uint64_t)o : ((uint64_t)o ^ 0x7FFFFFFFFFFFFFFFull);
+}
+VG_DEV bool vg_is_nan_bits(uint64_t b) {
+    return (b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+}
+
+// Exact int64 -> double conversion with round-to-nearest-even (the C
+// conversion the reference applies when it coerces int64 to double).
+VG_DEV double vg_i2f(int64_t v) { return __ll2double_rn((long long)v); }
+
+// ---------------------------------------------------------------------
+// hashing (internal to the device tables; any good mixer will do since
+// group / join membership depends only on key equality)
+// ---------------------------------------------------------------------
+
+VG_DEV uint64_t vg_mix64(uint64_t x) {
+    // splitmix64 finaliser (Steele, Lea, Flood 2014)
+    x ^= x >> 30; x *= 0xBF58476D1CE4E5B9ull;
+    x ^= x >> 27; x *= 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    return x;
+}
+
+// Key words are normalised so that equal keys have equal words:
+// doubles fold -0 onto +0.  NaN is kept as is; equality treats NaN as
+// unequal to everything (double ==), handled by vg_key_word_eq.
+VG_DEV uint64_t vg_norm_key(uint64_t bits, int type) {
+    if (type == VEC_DOUBLE && bits == 0x8000000000000000ull) return 0;
+    return bits;
+}
+VG_DEV bool vg_key_word_eq(uint64_t a, uint64_t b, int type) {
+    if (type == VEC_DOUBLE && vg_is_nan_bits(a)) return false;
+    return a == b;
+}
+
+VG_DEV uint64_t hash_keys(const uint64_t *k, int nk, uint32_t nm) {
+    uint64_t h = 0x9E3779B97F4A7C15ull ^ nm;
+    for (int i = 0; i < nk; i++) h = vg_mix64(h ^ k[i]) + (uint64_t)i;
+    return vg_mix64(h);
+}
+
+// Join table lookup: keys are normalised words of the common key types.
+VG_DEV bool jt_lookup(const VgJoinTable &jt, const uint64_t *k, int32_t &start, int32_t &count) {
+    uint64_t h = hash_keys(k, jt.n_keys, 0);
+    const int64_t mask = jt.cap - 1;
+    int64_t slot = (int64_t)(h & (uint64_t)mask);
+    for (int64_t probe = 0; probe < jt.cap; probe++) {
+        uint32_t st = __ldg(jt.state + slot);
+        if (st == 0) return false;
+        bool eq = true;
+        for (int i = 0; i < jt.n_keys && eq; i++)
+            eq = __ldg((const unsigned long long *)jt.keys + (int64_t)i * jt.cap + slot) == k[i];
+        if (eq) {
+            start = __ldg(jt.start + slot);
+            count = __ldg(jt.count + slot);
+            return true;
+        }
+        slot = (slot + 1) & mask;
+    }
+    return false;
+}
+
+// build row of match m of a lookup (rows == NULL: unique keys, start is the row)
+VG_DEV int64_t jt_row(const VgJoinTable &jt, int32_t start, int32_t m) {
+    return jt.rows ? (int64_t)__ldg(jt.rows + start + m) : (int64_t)start;
+}
+
+// ---------------------------------------------------------------------
+// exact double summation: fixed-point digit words
+// ---------------------------------------------------------------------
+//
+// A finite double is m * 2^(sh-1074) with sh = max(E,1)-1 in [0, 2045] and
+// m < 2^53.  In units of 2^-1074 it is m << sh, which spans at most three
+// 32-bit digits starting at digit lo = sh/32.  Digits are accumulated as
+// signed 64-bit words (32 bits of headroom each), so a group can take 2^31
+// additions per word before any carry handling is needed; the finish
+// step propagates carries and rounds once (round half to even).
+
+struct VgDigits {
+    int lo;            // first digit index, -1 for zero / non-finite
+    int64_t d0, d1, d2; // signed digit contributions
+    uint32_t special;  // bit2 NaN, bit3 +inf, bit4 -inf
+};
+
+VG_DEV VgDigits vg_split_double(uint64_t bits) {
+    VgDigits r;
+    uint32_t e = (uint32_t)((bits >> 52) & 0x7FF);
+    uint64_t f = bits & 0x000FFFFFFFFFFFFFull;
+    bool neg = (bits >> 63) != 0;
+    r.special = 0;
+    r.d0 = r.d1 = r.d2 = 0;
+    if (e == 0x7FF) {
+        r.lo = -1;
+        r.special = f ? 4u : (neg ? 16u : 8u);
+        return r;
+    }
+    uint64_t m = e ? (f | (1ull << 52)) : f;
+    if (m == 0) { r.lo = -1; return r; }
+    uint32_t sh = e ? e - 1 : 0;
+    uint32_t off = sh & 31;
+    r.lo = (int)(sh >> 5);
+    uint64_t low = m << off;
+    uint64_t high = off > 11 ? (m >> (64 - off)) : 0;
+    int64_t a0 = (int64_t)(low & 0xFFFFFFFFull);
+    int64_t a1 = (int64_t)(low >> 32);
+    int64_t a2 = (int64_t)high;
+    if (neg) { a0 = -a0; a1 = -a1; a2 = -a2; }
+    r.d0 = a0; r.d1 = a1; r.d2 = a2;
+    return r;
+}
+
+// Round the digit words (value = sum w[i] * 2^(32 i) units of 2^-1074,
+// n words) to the nearest double, ties to even.
+VG_DEV double vg_digits_to_double(const int64_t *w, int n, uint32_t special) {
+    if (special & 4u) return __longlong_as_double(0x7FF8000000000000ll);
+    if ((special & 8u) && (special & 16u)) return __longlong_as_double(0x7FF8000000000000ll);
+    if (special & 8u) return __longlong_as_double(0x7FF0000000000000ll);
+    if (special & 16u) return __longlong_as_double((long long)0xFFF0000000000000ull);
+    // propagate carries into 32-bit digits
+    uint32_t dig[VG_LACC_WORDS + 2];
+    int64_t carry = 0;
+    for (int i = 0; i < n; i++) {
+        int64_t v = w[i] + carry;
+        dig[i] = (uint32_t)(v & 0xFFFFFFFFll);
+        carry = v >> 32;          // arithmetic shift
+    }
+    // remaining carry: sign-extend into two more digits
+    dig[n] = (uint32_t)(carry & 0xFFFFFFFFll);
+    dig[n + 1] = (uint32_t)((carry >> 32) & 0xFFFFFFFFll);
+    int nd = n + 2;
+    bool neg = carry < 0;
+    if (neg) {   // two's complement negate
+        uint64_t c = 1;
+        for (int i = 0; i < nd; i++) {
+            uint64_t v = (uint64_t)(uint32_t)~dig[i] + c;
+            dig[i] = (uint32_t)v;
+            c = v >> 32;
+        }
+    }
+    int top = nd - 1;
+    while (top >= 0 && dig[top] == 0) top--;
+    if (top < 0) return 0.0;
+    int lz = __clz(dig[top]);
+    int p = top * 32 + (31 - lz);      // index of the leading one bit
+    if (p >= 2098 + 64) {              // far beyond the double range
+        return __longlong_as_double((long long)((neg ? 0xFFF0000000000000ull : 0x7FF0000000000000ull)));
+    }
+    uint64_t mant;
+    int exp_field;
+    if (p <= 52) {
+        // exact: M < 2^53 units of 2^-1074
+        uint64_t M = (uint64_t)dig[0] | ((top >= 1 ? (uint64_t)dig[1] : 0) << 32);
+        if (M < (1ull << 52)) { mant = M; exp_field = 0; }
+        else { mant = M & ((1ull << 52) - 1); exp_field = 1; }
+    } else {
+        // gather the 64 bits below and including bit p into `hi`
+        int s = p - 63;                // bit index of hi's lsb (may be negative)
+        uint64_t hi = 0;
+        bool sticky = false;
+        for (int i = 0; i < nd; i++) {
+            int b0 = i * 32;           // digit i covers bits [b0, b0+32)
+            if (b0 + 32 <= s) { if (dig[i]) sticky = true; continue; }
+            if (b0 > p) break;
+            uint64_t d = dig[i];
+            int shift = b0 - s;        // position of digit's lsb within hi
+            if (shift >= 0) hi |= d << shift;
+            else {
+                hi |= d >> (-shift);
+                if (d & ((1ull << (-shift)) - 1)) sticky = true;
+            }
+        }
+        // hi has the leading one at bit 63: keep 53 bits, round on the rest
+        uint64_t keep = hi >> 11;
+        uint64_t rest = hi & 0x7FF;
+        bool round_bit = (rest >> 10) & 1;
+        bool rest_sticky = sticky || (rest & 0x3FF);
+        if (round_bit && (rest_sticky || (keep & 1))) keep++;
+        int pp = p;
+        if (keep >> 53) { keep >>= 1; pp++; }
+        exp_field = pp - 51;
+        if (exp_field >= 2047)
+            return __longlong_as_double((long long)((neg ? 0xFFF0000000000000ull : 0x7FF0000000000000ull)));
+        mant = keep & ((1ull << 52) - 1);
+    }
+    uint64_t bits = ((uint64_t)exp_field << 52) | mant;
+    if (neg) bits |= 0x8000000000000000ull;
+    return __longlong_as_double((long long)bits);
+}
+
+// ---------------------------------------------------------------------
+// bounded waits
+// ---------------------------------------------------------------------
+
+#define VG_SPIN_LIMIT (1 << 22)
+#define VG_ERR_WAIT   1u
+#define VG_ERR_FULL   2u
+#define VG_ERR_PROG   4u

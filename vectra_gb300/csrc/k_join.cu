@@ -1,0 +1,379 @@
+// k_join.cu -- hash-join build and probe on sm_103a.
+//
+// Replaces the reference's JoinHT (src/join.c:23-150), join_build
+// (src/join.c:156-220) and join_probe_one (src/join.c:262-480):
+//  * build: one device pass inserts every non-NA build key into an
+//    open-addressing table (CAS-claimed slots, one slot per distinct key)
+//    and counts rows per key; if any key repeats, a stable radix sort of
+//    (slot, build row) lays each key's rows out in ascending row order, so
+//    the probe can emit them in the reference's descending order (its chains
+//    are built by head insertion, src/join.c:55-56);
+//  * probe: count -> exclusive scan -> emit (probe row, build row) pairs in
+//    the reference's output order: probe rows in order, matches in
+//    descending build row, then (LEFT/FULL) the unmatched probe rows of the
+//    batch (src/join.c:438-450).  SEMI/ANTI emit a selection vector.
+
+#include <cstdio>
+#include <cstring>
+#include "k_common.cuh"
+
+extern "C" {
+size_t vgk_sort_pairs_scratch(int64_t n);
+int vgk_sort_pairs(uint64_t *keys, int32_t *vals, int64_t n, int key_bits, void *scratch,
+                   size_t scratch_bytes, vg_stream_t s);
+const char *vgk_sort_last_error(void);
+size_t vgk_scan_scratch(int64_t n);
+int vgk_exclusive_scan(const int32_t *in, int64_t n, int64_t *out, int64_t *d_total, void *scratch,
+                       size_t scratch_bytes, vg_stream_t s);
+}
+
+namespace {
+
+char g_err[256];
+int check(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) {
+        snprintf(g_err, sizeof(g_err), "%s: %s", what, cudaGetErrorString(e));
+        return -1;
+    }
+    return 0;
+}
+size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+int grid_for(int64_t n, int threads) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    int64_t want = (n + threads - 1) / threads;
+    int64_t cap = (int64_t)sms * 16;
+    if (want > cap) want = cap;
+    if (want < 1) want = 1;
+    return (int)want;
+}
+
+struct KeyArgs {
+    int n_keys;
+    int32_t conv[VG_MAX_KEYS];
+    int32_t types[VG_MAX_KEYS];
+    VgCol cols[VG_MAX_KEYS];
+};
+
+// normalised key words of row r; false if any key is NA or NaN (never matches)
+VG_DEV bool key_words(const KeyArgs &K, int64_t r, uint64_t *k) {
+    for (int i = 0; i < K.n_keys; i++) {
+        const VgCol &c = K.cols[i];
+        if (!vg_valid(c, r)) return false;
+        uint64_t b = vg_load_bits(c, r);
+        if (K.conv[i]) b = vg_f64_to_bits(vg_i2f((int64_t)b));
+        if (K.types[i] == VEC_DOUBLE && vg_is_nan_bits(b)) return false;
+        k[i] = vg_norm_key(b, K.types[i]);
+    }
+    return true;
+}
+
+__global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < jt.cap; i += stride) {
+        jt.state[i] = 0;
+        jt.count[i] = 0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x < 4) counters[threadIdx.x] = 0;
+}
+
+// counters: [0] distinct keys, [1] max rows per key, [2] error bits
+__global__ void jt_insert_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t *rslot,
+                                 uint32_t *counters) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t mask = jt.cap - 1;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        uint64_t k[VG_MAX_KEYS];
+        if (!key_words(K, r, k)) { rslot[r] = -1; continue; }
+        uint64_t h = hash_keys(k, K.n_keys, 0);
+        int64_t slot = (int64_t)(h & (uint64_t)mask);
+        int64_t found = -1;
+        for (int64_t probe = 0; probe < jt.cap && found < 0; probe++) {
+            uint32_t st = *(volatile uint32_t *)(jt.state + slot);
+            if (st == 0) {
+                uint32_t prev = atomicCAS(jt.state + slot, 0u, 1u);
+                if (prev == 0u) {
+                    for (int i = 0; i < K.n_keys; i++) jt.keys[(int64_t)i * jt.cap + slot] = k[i];
+                    __threadfence();
+                    atomicExch(jt.state + slot, 2u);
+                    atomicAdd(counters + 0, 1u);
+                    found = slot;
+                    break;
+                }
+                st = prev;
+            }
+            int spins = 0;
+            while (st == 1u) {
+                if (++spins > VG_SPIN_LIMIT) { atomicOr(counters + 2, VG_ERR_WAIT); break; }
+                __nanosleep(32);
+                st = *(volatile uint32_t *)(jt.state + slot);
+            }
+            if (st != 2u) break;
+            __threadfence();
+            bool eq = true;
+            for (int i = 0; i < K.n_keys && eq; i++)
+                eq = *(volatile uint64_t *)(jt.keys + (int64_t)i * jt.cap + slot) == k[i];
+            if (eq) { found = slot; break; }
+            slot = (slot + 1) & mask;
+        }
+        if (found < 0) { atomicOr(counters + 2, VG_ERR_FULL); rslot[r] = -1; continue; }
+        int32_t old = atomicAdd(jt.count + found, 1);
+        atomicMax(counters + 1, (uint32_t)(old + 1));
+        if (old == 0) jt.start[found] = (int32_t)r;   // final when keys are unique
+        rslot[r] = (int32_t)found;
+    }
+}
+
+__global__ void pair_keys_kernel(const int32_t *rslot, int64_t n, int64_t cap, uint64_t *keys,
+                                 int32_t *vals) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        int32_t s = rslot[r];
+        keys[r] = s < 0 ? (uint64_t)cap : (uint64_t)s;   // NA rows sort last
+        vals[r] = (int32_t)r;
+    }
+}
+
+__global__ void seg_start_kernel(const uint64_t *keys, int64_t n, int64_t cap, int32_t *start) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint64_t k = keys[i];
+        if (k >= (uint64_t)cap) continue;
+        if (i == 0 || keys[i - 1] != k) start[k] = (int32_t)i;
+    }
+}
+
+// ---------------------------------------------------------------------
+// probe
+// ---------------------------------------------------------------------
+__global__ void probe_count_kernel(VgJoinTable jt, KeyArgs K, int64_t n_logical, const int32_t *sel,
+                                   int kind, int32_t *cnt, int32_t *start, int32_t *flag) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; li < n_logical; li += stride) {
+        int64_t p = sel ? (int64_t)sel[li] : li;
+        uint64_t k[VG_MAX_KEYS];
+        int32_t s0 = 0, c = 0;
+        if (key_words(K, p, k) && jt_lookup(jt, k, s0, c)) {}
+        else c = 0;
+        start[li] = s0;
+        switch (kind) {
+        case JOIN_SEMI: cnt[li] = 0; flag[li] = c > 0; break;
+        case JOIN_ANTI: cnt[li] = 0; flag[li] = c == 0; break;
+        case JOIN_INNER: cnt[li] = c; flag[li] = 0; break;
+        default: cnt[li] = c; flag[li] = c == 0; break;   // LEFT / FULL
+        }
+    }
+}
+
+__global__ void probe_emit_kernel(VgJoinTable jt, int64_t n_logical, const int32_t *sel, int kind,
+                                  const int32_t *cnt, const int32_t *start, const int32_t *flag,
+                                  const int64_t *off, const int64_t *off2, const int64_t *totals,
+                                  int32_t *out_probe, int32_t *out_build, uint32_t *build_matched) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t matched_total = totals[0];
+    for (int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; li < n_logical; li += stride) {
+        int32_t p = sel ? sel[li] : (int32_t)li;
+        int32_t c = cnt[li];
+        if (c > 0) {
+            int64_t o = off[li];
+            int32_t s0 = start[li];
+            for (int32_t m = 0; m < c; m++) {
+                // descending build row: the last of the ascending list first
+                int64_t br = jt_row(jt, s0, c - 1 - m);
+                out_probe[o + m] = p;
+                out_build[o + m] = (int32_t)br;
+                if (build_matched) atomicOr(build_matched + (br >> 5), 1u << (br & 31));
+            }
+        }
+        if (flag[li]) {
+            int64_t o = (kind == JOIN_SEMI || kind == JOIN_ANTI) ? off2[li] : matched_total + off2[li];
+            out_probe[o] = p;
+            if (out_build) out_build[o] = -1;
+        }
+    }
+}
+
+__global__ void unmatched_flags_kernel(const uint32_t *matched, int64_t n, int32_t *flag) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        flag[i] = !((matched[i >> 5] >> (i & 31)) & 1u);
+}
+
+__global__ void scatter_flags_kernel(const int32_t *flag, const int64_t *off, int64_t n, int32_t *out) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        if (flag[i]) out[off[i]] = (int32_t)i;
+}
+
+struct ProbeScratch {
+    int32_t *cnt, *start, *flag;
+    int64_t *off, *off2, *totals;
+    void *scan;
+    size_t scan_bytes;
+};
+
+bool carve_probe(void *base, size_t bytes, int64_t n, ProbeScratch &ps) {
+    char *p = (char *)base;
+    size_t o = 0;
+    ps.cnt = (int32_t *)(p + o); o += a256((size_t)n * 4);
+    ps.start = (int32_t *)(p + o); o += a256((size_t)n * 4);
+    ps.flag = (int32_t *)(p + o); o += a256((size_t)n * 4);
+    ps.off = (int64_t *)(p + o); o += a256((size_t)n * 8);
+    ps.off2 = (int64_t *)(p + o); o += a256((size_t)n * 8);
+    ps.totals = (int64_t *)(p + o); o += 256;
+    ps.scan = p + o;
+    ps.scan_bytes = vgk_scan_scratch(n);
+    o += a256(ps.scan_bytes);
+    return o <= bytes;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *vgk_join_last_error(void) { return g_err; }
+
+int64_t vgk_join_cap(int64_t n_build) {
+    int64_t cap = 64;
+    while (cap * 3 < n_build * 4) cap <<= 1;   // load factor <= 3/4
+    return cap;
+}
+
+size_t vgk_join_build_scratch_bytes(int64_t n_build) {
+    int64_t n = n_build > 0 ? n_build : 1;
+    return a256((size_t)n * 4) + a256((size_t)n * 8) + vgk_sort_pairs_scratch(n) + 256;
+}
+
+// jt->cap, state, keys, start, count, rows (n_build entries) are allocated by
+// the caller; on return jt->rows is NULL when every key is unique.
+int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t *key_conv,
+                   int64_t n_build, void *d_scratch, size_t scratch_bytes, int64_t *h_distinct,
+                   int64_t *h_maxdup, vg_stream_t s) {
+    cudaStream_t st = (cudaStream_t)s;
+    if (scratch_bytes < vgk_join_build_scratch_bytes(n_build)) {
+        snprintf(g_err, sizeof(g_err), "join build scratch too small");
+        return -1;
+    }
+    int64_t n = n_build > 0 ? n_build : 1;
+    char *p = (char *)d_scratch;
+    int32_t *rslot = (int32_t *)p; p += a256((size_t)n * 4);
+    uint64_t *pkeys = (uint64_t *)p; p += a256((size_t)n * 8);
+    void *sort_scratch = p; p += vgk_sort_pairs_scratch(n);
+    uint32_t *counters = (uint32_t *)p;
+    KeyArgs K;
+    memset(&K, 0, sizeof(K));
+    K.n_keys = n_keys;
+    for (int i = 0; i < n_keys; i++) {
+        K.cols[i] = keys[i];
+        K.conv[i] = key_conv[i];
+        K.types[i] = jt->key_types[i];
+    }
+    { jt_init_kernel<<<grid_for(jt->cap, 256), 256, 0, st>>>(*jt, counters); vg_launch_counter++; }
+    if (n_build > 0)
+        { jt_insert_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(*jt, K, n_build, rslot, counters); vg_launch_counter++; }
+    uint32_t hc[4] = {0, 0, 0, 0};
+    cudaMemcpyAsync(hc, counters, 16, cudaMemcpyDeviceToHost, st);
+    if (check(cudaStreamSynchronize(st), "join build")) return -1;
+    if (hc[2]) {
+        snprintf(g_err, sizeof(g_err), "join build: table overflow or wait expired (code %u)", hc[2]);
+        return -1;
+    }
+    *h_distinct = hc[0];
+    *h_maxdup = hc[1];
+    if (hc[1] <= 1) {
+        jt->rows = nullptr;    // start[slot] is the build row itself
+        return 0;
+    }
+    // duplicates: stable sort of (slot, row) lays out each key's rows in
+    // ascending row order
+    int bits = 1;
+    while (((int64_t)1 << bits) <= jt->cap) bits++;
+    { pair_keys_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(rslot, n_build, jt->cap, pkeys, jt->rows); vg_launch_counter++; }
+    if (vgk_sort_pairs(pkeys, jt->rows, n_build, bits, sort_scratch, vgk_sort_pairs_scratch(n), s)) {
+        snprintf(g_err, sizeof(g_err), "%s", vgk_sort_last_error());
+        return -1;
+    }
+    { seg_start_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(pkeys, n_build, jt->cap, jt->start); vg_launch_counter++; }
+    return check(cudaGetLastError(), "join build sort");
+}
+
+size_t vgk_join_probe_scratch_bytes(int64_t n_logical) {
+    int64_t n = n_logical > 0 ? n_logical : 1;
+    return a256((size_t)n * 4) * 3 + a256((size_t)n * 8) * 2 + 256 + a256(vgk_scan_scratch(n));
+}
+
+// Counts the output rows of one probe batch.  The per-row state stays in
+// the scratch for vgk_join_probe_emit.
+int vgk_join_probe_count(const VgJoinTable *jt, const VgCol *pkeys, int n_keys, const int32_t *key_conv,
+                         int64_t n_rows, const int32_t *d_sel, int64_t sel_n, int kind,
+                         void *d_scratch, size_t scratch_bytes, int64_t *h_total, vg_stream_t s) {
+    cudaStream_t st = (cudaStream_t)s;
+    int64_t n = d_sel ? sel_n : n_rows;
+    ProbeScratch ps;
+    if (!carve_probe(d_scratch, scratch_bytes, n > 0 ? n : 1, ps)) {
+        snprintf(g_err, sizeof(g_err), "probe scratch too small");
+        return -1;
+    }
+    if (n <= 0) { *h_total = 0; return 0; }
+    KeyArgs K;
+    memset(&K, 0, sizeof(K));
+    K.n_keys = n_keys;
+    for (int i = 0; i < n_keys; i++) {
+        K.cols[i] = pkeys[i];
+        K.conv[i] = key_conv[i];
+        K.types[i] = jt->key_types[i];
+    }
+    { probe_count_kernel<<<grid_for(n, 256), 256, 0, st>>>(*jt, K, n, d_sel, kind, ps.cnt, ps.start, ps.flag); vg_launch_counter++; }
+    if (vgk_exclusive_scan(ps.cnt, n, ps.off, ps.totals + 0, ps.scan, ps.scan_bytes, s)) return -1;
+    if (vgk_exclusive_scan(ps.flag, n, ps.off2, ps.totals + 1, ps.scan, ps.scan_bytes, s)) return -1;
+    int64_t t[2] = {0, 0};
+    cudaMemcpyAsync(t, ps.totals, 16, cudaMemcpyDeviceToHost, st);
+    if (check(cudaStreamSynchronize(st), "probe count")) return -1;
+    *h_total = t[0] + t[1];
+    return 0;
+}
+
+int vgk_join_probe_emit(const VgJoinTable *jt, int64_t n_rows, const int32_t *d_sel, int64_t sel_n,
+                        int kind, void *d_scratch, size_t scratch_bytes, int32_t *d_out_probe,
+                        int32_t *d_out_build, uint32_t *d_build_matched, vg_stream_t s) {
+    cudaStream_t st = (cudaStream_t)s;
+    int64_t n = d_sel ? sel_n : n_rows;
+    if (n <= 0) return 0;
+    ProbeScratch ps;
+    if (!carve_probe(d_scratch, scratch_bytes, n, ps)) {
+        snprintf(g_err, sizeof(g_err), "probe scratch too small");
+        return -1;
+    }
+    { probe_emit_kernel<<<grid_for(n, 256), 256, 0, st>>>(*jt, n, d_sel, kind, ps.cnt, ps.start, ps.flag,
+                                                         ps.off, ps.off2, ps.totals, d_out_probe,
+                                                         d_out_build, d_build_matched); vg_launch_counter++; }
+    return check(cudaGetLastError(), "probe emit");
+}
+
+// FULL join: build rows never matched, in ascending order.
+int vgk_join_unmatched_build(const uint32_t *d_matched, int64_t n_build, int32_t *d_out, int64_t *h_n,
+                             void *d_scratch, size_t scratch_bytes, vg_stream_t s) {
+    cudaStream_t st = (cudaStream_t)s;
+    if (n_build <= 0) { *h_n = 0; return 0; }
+    ProbeScratch ps;
+    if (!carve_probe(d_scratch, scratch_bytes, n_build, ps)) {
+        snprintf(g_err, sizeof(g_err), "unmatched scratch too small");
+        return -1;
+    }
+    { unmatched_flags_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(d_matched, n_build, ps.flag); vg_launch_counter++; }
+    if (vgk_exclusive_scan(ps.flag, n_build, ps.off, ps.totals, ps.scan, ps.scan_bytes, s)) return -1;
+    { scatter_flags_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(ps.flag, ps.off, n_build, d_out); vg_launch_counter++; }
+    int64_t t = 0;
+    cudaMemcpyAsync(&t, ps.totals, 8, cudaMemcpyDeviceToHost, st);
+    if (check(cudaStreamSynchronize(st), "unmatched build")) return -1;
+    *h_n = t;
+    return 0;
+}
+
+}  // extern "C"

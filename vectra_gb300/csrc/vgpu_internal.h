@@ -1,0 +1,339 @@
+/*
+ * vgpu_internal.h -- the contract between libvgpu's C11 host layer
+ * (nodes, plan compilation, memory) and its sm_103a CUDA kernels.
+ *
+ * Plain C structs only: the host side fills them, the .cu side launches
+ * kernels with them passed by value.
+ */
+#ifndef VGPU_INTERNAL_H
+#define VGPU_INTERNAL_H
+
+#include <stdint.h>
+#include <stddef.h>
+#include "vectra_abi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *vg_stream_t;
+
+/* ------------------------------------------------------------------ */
+/* device column views                                                 */
+/* ------------------------------------------------------------------ */
+
+/* One column resident in device memory.  data: 8-byte values for int64 and
+ * double, one byte per row for bool.  valid: the column's validity bitmap
+ * read as little-endian 32-bit words (bit i%32 of word i/32 == bit i%8 of
+ * byte i/8 of the host bitmap); NULL means every row is valid. */
+typedef struct {
+    int32_t type;              /* VecType */
+    int32_t pad;
+    const void *data;
+    const uint32_t *valid;
+} VgCol;
+
+#define VG_MAX_COLS   24
+#define VG_MAX_TERMS  12
+#define VG_MAX_KEYS   4
+#define VG_MAX_ACCS   12
+#define VG_MAX_INSNS  48
+
+/* ------------------------------------------------------------------ */
+/* predicates                                                          */
+/* ------------------------------------------------------------------ */
+
+/* A conjunction of column-vs-constant terms, each folded on the host into
+ * an inclusive range in the column's integer domain (int64 value, bool
+ * byte, or the order-preserving integer image of a double).  A row is kept
+ * iff every term keeps it; NA rows of a compared column are dropped, which
+ * is what Kleene AND followed by `valid && true` does (src/filter.c:20). */
+enum {
+    VG_TERM_RANGE = 0,       /* keep iff valid && lo <= v <= hi            */
+    VG_TERM_NOT_RANGE = 1,   /* keep iff valid && !(lo <= v <= hi)         */
+    VG_TERM_IS_NA = 2,       /* keep iff !valid                            */
+    VG_TERM_NOT_NA = 3,      /* keep iff valid                             */
+    VG_TERM_NONE = 4         /* keep nothing (FALSE or NA literal)         */
+};
+enum { VG_DOM_INT64 = 0, VG_DOM_DOUBLE = 1, VG_DOM_BOOL = 2 };
+
+typedef struct {
+    int32_t col;             /* index into the launch's column table */
+    int32_t kind;            /* VG_TERM_* */
+    int32_t domain;          /* VG_DOM_* */
+    int32_t nan_keep;        /* double domain: keep a valid NaN row? */
+    int64_t lo, hi;
+} VgTerm;
+
+typedef struct {
+    int32_t n_terms;
+    int32_t pad;
+    VgTerm term[VG_MAX_TERMS];
+} VgPred;
+
+/* ------------------------------------------------------------------ */
+/* general expressions (postfix programs)                              */
+/* ------------------------------------------------------------------ */
+
+/* Stack machine over (64-bit payload, valid) cells.  Each instruction
+ * leaves a value of a statically known type; coercions are explicit. */
+enum {
+    VI_COL_I64 = 1,   /* push column a as int64            */
+    VI_COL_F64,       /* push column a as double           */
+    VI_COL_BOOL,      /* push column a as bool (0/1)       */
+    VI_LIT_I64,       /* push imm                          */
+    VI_LIT_F64,       /* push imm (bit pattern of double)  */
+    VI_LIT_BOOL,      /* push imm (0/1)                    */
+    VI_LIT_NA,        /* push NA                           */
+    VI_I2F,           /* top: int64 -> double              */
+    VI_ARITH_I64,     /* a = op char                       */
+    VI_ARITH_F64,
+    VI_CMP_I64,       /* a = cmp code (VG_CMP_*)           */
+    VI_CMP_F64,
+    VI_AND,
+    VI_OR,
+    VI_NOT,
+    VI_IS_NA,
+    VI_NEG_I64,
+    VI_NEG_F64
+};
+enum { VG_CMP_EQ = 0, VG_CMP_NE, VG_CMP_LT, VG_CMP_LE, VG_CMP_GT, VG_CMP_GE };
+
+typedef struct {
+    int32_t op;
+    int32_t a;
+    int64_t imm;
+} VgInsn;
+
+typedef struct {
+    int32_t n;
+    int32_t result_type;     /* VecType of the value left on the stack */
+    int32_t max_depth;
+    int32_t pad;
+    VgInsn insn[VG_MAX_INSNS];
+} VgProg;
+
+/* ------------------------------------------------------------------ */
+/* values read by fused kernels                                        */
+/* ------------------------------------------------------------------ */
+
+/* An operand is a column of the probe (or only) side, a column of the
+ * build side of a join (NA for unmatched LEFT rows), or a constant. */
+enum { VG_SIDE_PROBE = 0, VG_SIDE_BUILD = 1, VG_SIDE_LIT = 2, VG_SIDE_NA = 3 };
+
+typedef struct {
+    int32_t side;
+    int32_t col;
+    int32_t type;            /* VecType of the operand */
+    int32_t pad;
+    int64_t lit;             /* literal payload (int64 or double bits) */
+} VgOperand;
+
+/* value = a, or (a op b) with the reference's arithmetic rules
+ * (src/scalar_ops.c:11-66): computed in `type` (int64 or double) after
+ * coercing both operands; int64 division/modulo by zero is NA. */
+typedef struct {
+    int32_t op;              /* 0 = plain operand, else '+','-','*','/','%' */
+    int32_t type;            /* result VecType */
+    VgOperand a, b;
+} VgValue;
+
+/* ------------------------------------------------------------------ */
+/* grouped aggregation                                                 */
+/* ------------------------------------------------------------------ */
+
+/* Accumulator classes; aggregate outputs are derived from them at finish
+ * (every output is double, src/group_agg.c:658-661). */
+enum {
+    VG_ACC_COUNT_ALL = 0,    /* n()                                      */
+    VG_ACC_COUNT_VALID,      /* count of non-NA values                   */
+    VG_ACC_SUM_I64,          /* int64 / bool sum (wrapping), count, NA   */
+    VG_ACC_SUM_F64,          /* exact fixed-point double sum, count, NA  */
+    VG_ACC_MIN_I64,
+    VG_ACC_MAX_I64,
+    VG_ACC_MIN_F64,          /* on the ordered-integer image             */
+    VG_ACC_MAX_F64,
+    VG_ACC_NA_ONLY           /* min/max of bool: only NA poisoning       */
+};
+
+typedef struct {
+    int32_t cls;             /* VG_ACC_* */
+    int32_t na_rm;
+    VgValue in;
+} VgAccSpec;
+
+/* Global group table.  Slots are claimed with a CAS on state
+ * (0 empty, 1 being written, 2 ready); keys are normalised 64-bit words
+ * (double -0 folded to +0) plus a per-slot NA mask. */
+#define VG_LACC_WORDS 66     /* 32-bit digits of a full-range double sum */
+
+typedef struct {
+    int64_t   cap;           /* power of two */
+    uint32_t *state;
+    uint32_t *nullmask;
+    uint64_t *keys;          /* [VG_MAX_KEYS][cap] */
+    uint64_t *first_row;     /* min global row id of each group */
+    /* per accumulator (index a): */
+    uint64_t *cnt[VG_MAX_ACCS];    /* count (valid values, or all rows) */
+    int64_t  *val[VG_MAX_ACCS];    /* int64 sum / min / max, or ordered image */
+    uint32_t *flags[VG_MAX_ACCS];  /* bit0 has_na, bit1 has_value, bit2 NaN, bit3 +inf, bit4 -inf */
+    int64_t  *lacc[VG_MAX_ACCS];   /* [cap][VG_LACC_WORDS] digit words */
+    uint32_t *n_used;        /* number of occupied slots */
+    uint32_t *err;           /* error word: nonzero = a bounded wait expired / table full */
+} VgGroupTable;
+
+/* Join hash table over the build side (keys unique per slot; rows of a key
+ * listed in ascending build-row order in rows[start .. start+count)). */
+typedef struct {
+    int64_t   cap;           /* power of two */
+    int32_t   n_keys;
+    int32_t   key_types[VG_MAX_KEYS];
+    uint32_t *state;
+    uint64_t *keys;          /* [n_keys][cap] */
+    int32_t  *start;
+    int32_t  *count;
+    int32_t  *rows;          /* n_build entries */
+    int64_t   n_build;
+    uint32_t *err;
+} VgJoinTable;
+
+/* One fused aggregation launch over a batch of rows:
+ *   rows -> [predicate] -> [join probe, per match] -> group keys / values
+ *   -> per-CTA shared-memory cache -> global group table. */
+typedef struct {
+    int64_t n_rows;              /* physical rows of the probe batch */
+    const int32_t *sel;          /* optional selection vector (device) */
+    int64_t sel_n;
+    int64_t row_base;            /* global id of physical row 0 */
+    int32_t n_pcols, n_bcols;
+    VgCol pcols[VG_MAX_COLS];
+    VgCol bcols[VG_MAX_COLS];
+    VgPred pred;
+    /* join */
+    int32_t has_join;
+    int32_t join_kind;           /* JOIN_INNER or JOIN_LEFT */
+    int32_t n_jkeys;
+    int32_t jkey_col[VG_MAX_KEYS];   /* probe columns */
+    int32_t jkey_conv[VG_MAX_KEYS];  /* 1: probe int64/bool -> double to match a double build key */
+    VgJoinTable jt;
+    /* grouping */
+    int32_t n_keys;
+    int32_t n_accs;
+    VgValue key[VG_MAX_KEYS];
+    VgAccSpec acc[VG_MAX_ACCS];
+    int32_t track_first;         /* record first-seen row per group */
+    int32_t cache_slots;         /* power of two, 0 = no shared-memory cache */
+    VgGroupTable gt;
+    /* When the global table is full, work is spilled instead of dropped:
+     * rows as (logical row, match << 8 | (acc + 1)) pairs (acc + 1 == 0:
+     * every accumulator), shared-cache entries in a cache-layout area with
+     * stride spill_cache_cap.  The host grows the table and replays both. */
+    int64_t  *spill_rows;
+    uint32_t *spill_rows_n;
+    int64_t   spill_rows_cap;
+    char     *spill_cache;
+    uint32_t *spill_cache_n;
+    int64_t   spill_cache_cap;
+    const int64_t *replay;       /* replay list (pairs as above) or NULL */
+    int64_t   replay_n;
+    int64_t   batch_idx;         /* probe batch number (join ordering key) */
+} VgAggLaunch;
+
+/* ------------------------------------------------------------------ */
+/* kernel entry points (implemented in the .cu files)                  */
+/* ------------------------------------------------------------------ */
+
+int  vgk_num_sms(void);
+const char *vgk_last_cuda_error(void);
+
+/* filter: keep mask + selection vector over logical rows */
+int vgk_filter_pred(const VgCol *cols, int n_cols, const VgPred *pred,
+                    int64_t n_rows, const int32_t *d_sel_in, int64_t sel_n,
+                    int32_t *d_sel_out, int64_t *h_count, void *d_scratch,
+                    size_t scratch_bytes, vg_stream_t s);
+int vgk_filter_prog(const VgCol *cols, int n_cols, const VgProg *prog,
+                    int64_t n_rows, const int32_t *d_sel_in, int64_t sel_n,
+                    int32_t *d_sel_out, int64_t *h_count, void *d_scratch,
+                    size_t scratch_bytes, vg_stream_t s);
+size_t vgk_filter_scratch_bytes(int64_t n_logical);
+
+/* evaluate a program over logical rows into a dense output column */
+int vgk_eval_prog(const VgCol *cols, int n_cols, const VgProg *prog,
+                  int64_t n_rows, const int32_t *d_sel, int64_t sel_n,
+                  void *d_out, uint32_t *d_out_valid, vg_stream_t s);
+
+/* gather logical rows of a column into dense output (values + validity) */
+int vgk_gather(const VgCol *col, const int32_t *d_idx, int64_t n_out,
+               int null_if_negative, void *d_out, uint32_t *d_out_valid,
+               vg_stream_t s);
+
+/* group table */
+int vgk_group_table_init(VgGroupTable *gt, int n_keys, const int32_t *acc_cls,
+                         int n_accs, vg_stream_t s);
+int vgk_agg_launch(const VgAggLaunch *L, vg_stream_t s);
+size_t vgk_agg_smem_bytes(const VgAggLaunch *L);
+/* per occupied slot: compact slot ids (in slot order) into d_slots */
+int vgk_group_table_compact(const VgGroupTable *gt, int32_t *d_slots,
+                            uint32_t *h_n, vg_stream_t s);
+/* results for the listed slots: keys + one double column per output */
+typedef struct {
+    int32_t acc;             /* accumulator index */
+    int32_t finish;          /* AggKind of the output */
+    int32_t in_type;         /* VecType of the aggregated input */
+    int32_t na_rm;
+} VgFinish;
+int vgk_group_finish(const VgGroupTable *gt, int n_keys, const int32_t *key_types,
+                     const int32_t *d_slots, int64_t n_groups,
+                     const VgFinish *fin, int n_out,
+                     uint64_t **d_key_out, uint32_t **d_key_valid,
+                     double **d_out, uint32_t **d_out_valid,
+                     uint32_t *d_warn, vg_stream_t s);
+/* order slots: mode 0 = keys ascending (NA last), 1 = first-seen row */
+int vgk_order_groups(const VgGroupTable *gt, int n_keys, const int32_t *key_types,
+                     int32_t *d_slots, int64_t n_groups, int mode,
+                     void *d_scratch, size_t scratch_bytes, vg_stream_t s);
+size_t vgk_order_scratch_bytes(int64_t n_groups);
+
+/* join */
+int64_t vgk_join_cap(int64_t n_build);
+size_t vgk_join_build_scratch_bytes(int64_t n_build);
+int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t *key_conv,
+                   int64_t n_build, void *d_scratch, size_t scratch_bytes, int64_t *h_distinct,
+                   int64_t *h_maxdup, vg_stream_t s);
+size_t vgk_join_probe_scratch_bytes(int64_t n_logical);
+int vgk_join_probe_count(const VgJoinTable *jt, const VgCol *pkeys, int n_keys, const int32_t *key_conv,
+                         int64_t n_rows, const int32_t *d_sel, int64_t sel_n, int kind,
+                         void *d_scratch, size_t scratch_bytes, int64_t *h_total, vg_stream_t s);
+int vgk_join_probe_emit(const VgJoinTable *jt, int64_t n_rows, const int32_t *d_sel, int64_t sel_n,
+                        int kind, void *d_scratch, size_t scratch_bytes, int32_t *d_out_probe,
+                        int32_t *d_out_build, uint32_t *d_build_matched, vg_stream_t s);
+int vgk_join_unmatched_build(const uint32_t *d_matched, int64_t n_build, int32_t *d_out, int64_t *h_n,
+                             void *d_scratch, size_t scratch_bytes, vg_stream_t s);
+const char *vgk_join_last_error(void);
+
+/* sort / scan building blocks */
+size_t vgk_sort_pairs_scratch(int64_t n);
+int vgk_sort_pairs(uint64_t *keys, int32_t *vals, int64_t n, int key_bits, void *scratch,
+                   size_t scratch_bytes, vg_stream_t s);
+const char *vgk_sort_last_error(void);
+size_t vgk_scan_scratch(int64_t n);
+int vgk_exclusive_scan(const int32_t *in, int64_t n, int64_t *out, int64_t *d_total, void *scratch,
+                       size_t scratch_bytes, vg_stream_t s);
+
+/* aggregation extras */
+const char *vgk_agg_last_error(void);
+size_t vgk_lacc_bytes(int64_t cap);
+/* replay shared-cache entries spilled by vgk_agg_launch (n of them) */
+int vgk_agg_merge_spilled_cache(const VgAggLaunch *L, int64_t n, vg_stream_t s);
+/* move every group of `from` into the empty, larger table `to` */
+int vgk_group_table_rehash(const VgGroupTable *from, const VgGroupTable *to, int n_keys,
+                           const int32_t *key_types, const int32_t *acc_cls, int n_accs,
+                           vg_stream_t s);
+/* bytes of spilled cache entries per entry (cache layout, one slot) */
+size_t vgk_agg_cache_bytes(const VgAggLaunch *L, int64_t slots);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
