@@ -1,0 +1,444 @@
+"""Benchmark of the hash-join + aggregate workload on one GB300.
+
+Workload (the reference's second configuration, synthetic, seed 0):
+  fact 100,000,000 rows: key int64 Zipf(s=1.1) over ids 1..10,000,000,
+                         value double LogNormal(0,1) with 2% NA
+  dim   10,000,000 rows: id int64 (a permutation of 1..10M), category int64
+                         uniform [0,256), weight double U(0,1)
+  left_join(fact, dim, by = c(key = "id")) |> group_by(category) |>
+      summarise(s = sum(value * weight), n = n())
+built through the node C API exactly as the R front end builds it (join ->
+hidden projection `.vectra_tmp_s = value * weight` -> group-agg with a
+temp_dir, i.e. key-ordered output).
+
+One step = one whole query.  value: rows/s with the columns resident in HBM
+(device table sources); e2e: the same query fed from page-locked host
+buffers, host->device copies and the result read-back inside the step.
+roofline: the fused probe + aggregate kernel, algorithmic bytes (the fact
+columns it reads, in the reference's layout) over its CUDA-event duration.
+cpu_baseline: this repository's CPU restatement of the reference path
+(single-threaded like the reference engine) on a 1/20-scale sample.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_FACT = 100_000_000
+N_DIM = 10_000_000
+N_CAT = 256
+ZIPF_S = 1.1
+SAMPLE_DIV = 20          # CPU baseline: 1/20-scale fact and dim
+WORKLOAD = ("hash join + aggregate: fact 100M (key int64 Zipf s=1.1 over 10M ids, value f64 "
+            "LogNormal(0,1), 2% NA) left_join dim 10M (unique id, category int64 U[0,256), weight "
+            "f64 U(0,1)) |> group_by(category) |> summarise(sum(value*weight), n())")
+METRIC = "rows/s (fact + dim input rows per second, whole query)"
+
+
+def algorithmic_bytes(n_fact, n_dim):
+    """Every referenced column once in the reference's layout (8 B values +
+    ceil(N/8) B validity), plus the 256-group output."""
+    vb = lambda n: (n + 7) // 8
+    fact = 2 * (8 * n_fact + vb(n_fact))
+    dim = 3 * (8 * n_dim + vb(n_dim))
+    out = 3 * (8 * N_CAT + vb(N_CAT))
+    return fact, dim, out
+
+
+# ---------------------------------------------------------------------------
+# data
+# ---------------------------------------------------------------------------
+
+def gen_tables(torch, n_fact, n_dim, seed, device):
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    ranks = torch.arange(1, n_dim + 1, device=device, dtype=torch.float64)
+    w = ranks.pow(-ZIPF_S)
+    cdf = torch.cumsum(w, 0)
+    cdf /= cdf[-1].clone()
+    fact = {}
+    keys = torch.empty(n_fact, dtype=torch.int64, device=device)
+    vals = torch.empty(n_fact, dtype=torch.float64, device=device)
+    valid = torch.empty(n_fact, dtype=torch.bool, device=device)
+    chunk = 1 << 25
+    for lo in range(0, n_fact, chunk):
+        hi = min(n_fact, lo + chunk)
+        u = torch.rand(hi - lo, dtype=torch.float64, device=device, generator=g)
+        keys[lo:hi] = torch.searchsorted(cdf, u).clamp_(max=n_dim - 1) + 1
+        vals[lo:hi] = torch.randn(hi - lo, dtype=torch.float64, device=device, generator=g).exp_()
+        valid[lo:hi] = torch.rand(hi - lo, device=device, generator=g) >= 0.02
+    vals[~valid] = 0.0
+    fact["key"] = (keys, None)
+    fact["value"] = (vals, valid)
+    dim = {
+        "id": (torch.randperm(n_dim, device=device, generator=g).to(torch.int64) + 1, None),
+        "category": (torch.randint(0, N_CAT, (n_dim,), device=device, generator=g, dtype=torch.int64), None),
+        "weight": (torch.rand(n_dim, dtype=torch.float64, device=device, generator=g), None),
+    }
+    return fact, dim
+
+
+def pack_validity(torch, mask):
+    """Reference bitmap (bit i%8 of byte i/8) of a bool tensor, padded to 4 bytes."""
+    n = mask.numel()
+    nb = ((n + 31) // 32) * 4
+    m = torch.zeros(nb * 8, dtype=torch.uint8, device=mask.device)
+    m[:n] = mask.to(torch.uint8)
+    wts = torch.tensor([1, 2, 4, 8, 16, 32, 64, 128], dtype=torch.uint8, device=mask.device)
+    return (m.view(-1, 8) * wts).sum(dim=1, dtype=torch.uint8)
+
+
+def columns_with_validity(torch, table):
+    """name -> (values, validity bytes): every column carries a bitmap, as
+    engine-allocated arrays do (src/array.c:14-16)."""
+    out = {}
+    for name, (v, valid) in table.items():
+        if valid is None:
+            valid = torch.ones(v.numel(), dtype=torch.bool, device=v.device)
+        out[name] = (v.contiguous(), pack_validity(torch, valid))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def source_from_ptrs(lib, cols, n_rows, batch_rows, flags):
+    names = list(cols.keys())
+    k = len(names)
+    data = (C.c_void_p * k)(*[cols[n][0].data_ptr() for n in names])
+    val = (C.c_void_p * k)(*[cols[n][1].data_ptr() for n in names])
+    types = (C.c_int * k)(*[1 if cols[n][0].dtype.is_floating_point else 0 for n in names])
+    cn = (C.c_char_p * k)(*[n.encode() for n in names])
+    lib.vgpu_table_source_create.restype = C.c_void_p
+    lib.vgpu_table_source_create.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_int64, C.c_int64, C.c_int]
+    p = lib.vgpu_table_source_create(k, cn, types, data, val, n_rows, batch_rows, flags)
+    if not p:
+        raise RuntimeError(lib.vgpu_last_error().decode())
+    return p
+
+
+def run_query(eng, fact_src, dim_src, temp_dir="tmp"):
+    from vectra_gb300.plan import Tbl, col
+    out = (Tbl(eng, fact_src).left_join(Tbl(eng, dim_src), {"key": "id"})
+           .group_by("category")
+           .summarise(temp_dir=temp_dir, s=("sum", col("value") * col("weight")), n=("n",))
+           .collect())
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(tempfile.gettempdir(), "vgpu_clocks_%d.csv" % os.getpid())
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.3)
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the fused kernel from the committed ncu
+    summary (a `traffic_bytes_per_launch:` line), if present."""
+    p = os.path.join(ROOT, "profiles", "agg_probe_c2_fused.md")
+    try:
+        for line in open(p):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip().split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def gpu_arm(args, rank, world):
+    import torch
+    import vectra_gb300
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    eng = vectra_gb300.engine(dev.index)
+    lib = eng.lib
+    stream = torch.cuda.current_stream(dev)
+    lib.vgpu_set_stream(C.c_void_p(stream.cuda_stream))
+    lib.vgpu_profile_enable.argtypes = [C.c_int]
+    lib.vgpu_profile_ms.restype = C.c_double
+    lib.vgpu_profile_ms.argtypes = [C.c_int, C.POINTER(C.c_ulonglong)]
+
+    fact, dim = gen_tables(torch, N_FACT, N_DIM, seed=0, device=dev)
+    fcols = columns_with_validity(torch, fact)
+    dcols = columns_with_validity(torch, dim)
+    torch.cuda.synchronize()
+
+    def dev_step():
+        fs = source_from_ptrs(lib, fcols, N_FACT, N_FACT, 2)
+        ds = source_from_ptrs(lib, dcols, N_DIM, N_DIM, 2)
+        return run_query(eng, fs, ds)
+
+    # correctness on the full size: n per group is exact and the group sums
+    # must equal an independent (torch, FP64) evaluation to 1e-12
+    out = dev_step()
+    check_full(torch, out, fact, dim)
+
+    def timed(step, k, w):
+        for _ in range(w):
+            step()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        l0 = lib.vgpu_kernel_launches()
+        lib.vgpu_profile_reset()
+        lib.vgpu_profile_enable(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(k):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        lib.vgpu_profile_enable(0)
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+            torch.distributed.barrier()
+        return ms / k, wall / k, lib.vgpu_kernel_launches() - l0
+
+    with ClockSampler(dev.index) as clk:
+        ms_step, wall_step, launches = timed(dev_step, args.steps, args.warmup)
+    clocks = clk.summary()
+    n_l = C.c_ulonglong(0)
+    agg_ms = lib.vgpu_profile_ms(0, C.byref(n_l))
+    agg_launches = max(1, n_l.value)
+    build_n = C.c_ulonglong(0)
+    build_ms = lib.vgpu_profile_ms(2, C.byref(build_n))
+
+    # e2e: page-locked host copies of the same columns
+    hf = {k: (v.cpu().pin_memory(), m.cpu().pin_memory()) for k, (v, m) in fcols.items()}
+    hd = {k: (v.cpu().pin_memory(), m.cpu().pin_memory()) for k, (v, m) in dcols.items()}
+    e2e_batch = 1 << 24
+
+    def host_step():
+        fs = source_from_ptrs(lib, hf, N_FACT, e2e_batch, 1)
+        ds = source_from_ptrs(lib, hd, N_DIM, N_DIM, 1)
+        return run_query(eng, fs, ds)
+
+    out2 = host_step()
+    same_result(out, out2)
+    e2e_ms, e2e_wall, _ = timed(host_step, max(1, min(args.steps, 5)), 1)
+
+    rows = N_FACT + N_DIM
+    fact_b, dim_b, out_b = algorithmic_bytes(N_FACT, N_DIM)
+    h2d = sum(v.numel() * v.element_size() + m.numel() for v, m in list(hf.values()) + list(hd.values()))
+    d2h = 3 * 8 * N_CAT
+    peak, peak_kind = measured_peak()
+    kernel_ms = agg_ms / agg_launches
+    achieved = fact_b / (kernel_ms * 1e-3) / 1e9
+    value = rows * world / (ms_step * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic (seeded torch generator, seed 0)",
+        "config": {"workload": WORKLOAD, "fact_rows": N_FACT, "dim_rows": N_DIM, "groups": N_CAT,
+                   "inputs": "device-resident, larger than L2 (1.87 GB)", "parallelism": "replicas",
+                   "output_order": "ascending category (temp_dir given, as from R)"},
+        "hbm_gbs_whole_query": (fact_b + dim_b + out_b) / (ms_step * 1e-3) / 1e9,
+        "roofline": {"bound": "hbm", "kernel": "fused left-join probe + project + group-agg (agg_kernel)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_launch": fact_b,
+                     "kernel_ms": kernel_ms, "traffic": profile_traffic()},
+        "join_build_ms": build_ms / max(1, build_n.value),
+        "e2e": {"value": rows * world / (e2e_ms * 1e-3), "unit": "rows/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "node C API, page-locked host table sources, 16M-row fact batches"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(torch, repeats=1)
+    return line
+
+
+def check_full(torch, out, fact, dim):
+    keys, _ = fact["key"]
+    vals, valid = fact["value"]
+    ids = dim["id"][0]
+    pos = torch.empty(N_DIM + 1, dtype=torch.int64, device=ids.device)
+    pos[ids] = torch.arange(N_DIM, device=ids.device)
+    p = pos[keys]
+    cat = dim["category"][0][p]
+    w = dim["weight"][0][p]
+    n = torch.bincount(cat, minlength=N_CAT).cpu().numpy()
+    prod = torch.where(valid, vals * w, torch.zeros_like(vals))
+    s = torch.zeros(N_CAT, dtype=torch.float64, device=ids.device).index_add_(0, cat, prod).cpu().numpy()
+    has_na = torch.zeros(N_CAT, dtype=torch.int64, device=ids.device).index_add_(
+        0, cat, (~valid).to(torch.int64)).cpu().numpy()
+    import numpy as np
+    assert list(out["category"][0]) == list(range(N_CAT)), "groups not in key order"
+    assert np.array_equal(out["n"][0], n.astype(np.float64)), "n() mismatch"
+    sv, sm = out["s"]
+    assert np.array_equal(sm, has_na == 0), "NA poisoning mismatch"
+    if sm.any():
+        rel = np.abs(sv[sm] - s[sm]) / np.abs(s[sm])
+        assert rel.max() <= 1e-12, rel.max()
+
+
+def same_result(a, b):
+    import numpy as np
+    for k in a:
+        assert np.array_equal(a[k][1], b[k][1]), k
+        assert np.array_equal(a[k][0][a[k][1]], b[k][0][b[k][1]]), k
+
+
+# ---------------------------------------------------------------------------
+# CPU arm: the reference path restated in C (oracle/), single-threaded
+# ---------------------------------------------------------------------------
+
+def sample_tables(n_fact, n_dim, seed):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    ranks = np.arange(1, n_dim + 1, dtype=np.float64)
+    cdf = np.cumsum(ranks ** -ZIPF_S)
+    cdf /= cdf[-1]
+    keys = np.minimum(np.searchsorted(cdf, rng.random(n_fact)), n_dim - 1) + 1
+    vals = rng.lognormal(0, 1, n_fact)
+    valid = rng.random(n_fact) >= 0.02
+    vals[~valid] = 0.0
+    fact = {"key": keys.astype(np.int64), "value": (vals, valid)}
+    dim = {"id": (rng.permutation(n_dim) + 1).astype(np.int64),
+           "category": rng.integers(0, N_CAT, n_dim).astype(np.int64),
+           "weight": rng.random(n_dim)}
+    return fact, dim
+
+
+def cpu_baseline(torch=None, repeats=1):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from engines import OracleEngine, ref_available, RefEngine
+    from vectra_gb300.plan import tbl, col
+    kind = "port"
+    E = OracleEngine()
+    nf, nd = N_FACT // SAMPLE_DIV, N_DIM // SAMPLE_DIV
+    fact, dim = sample_tables(nf, nd, seed=0)
+    best = None
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        (tbl(E, fact, batch_rows=100_000).left_join(tbl(E, dim, batch_rows=100_000), {"key": "id"})
+         .group_by("category").summarise(temp_dir=E.tmp, s=("sum", col("value") * col("weight")), n=("n",))
+         .collect())
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return {"value": (nf + nd) / best, "unit": "rows/s", "cores": 1, "kind": kind,
+            "sample": "1/%d-scale query (fact %d x dim %d rows, 100k-row batches, same distributions), "
+                      "R-default sort-based group-agg; the engine is single-threaded" % (SAMPLE_DIV, nf, nd),
+            "seconds": best}
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return None
+    for _ in range(args.warmup):
+        cpu_baseline()
+    vals = []
+    for _ in range(args.steps):
+        vals.append(cpu_baseline())
+    v = statistics.median([x["value"] for x in vals])
+    cb = dict(vals[0])
+    cb["value"] = v
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "rows/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median([x["seconds"] for x in vals]),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64+f64",
+            "data": "synthetic (numpy generator, seed 0)",
+            "config": {"workload": WORKLOAD, "parallelism": "single-threaded CPU engine"},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "rows/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "gpu":
+        import torch
+        torch.distributed.init_process_group("nccl")
+    if args.impl == "reference":
+        line = reference_arm(args, rank, world)
+    else:
+        line = gpu_arm(args, rank, world)
+    if rank == 0 and line is not None:
+        print(json.dumps(line))
+    if world > 1 and args.impl == "gpu":
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,121 @@
+/*
+ * vgpu.h -- libvgpu: GB300 (sm_103a) operator nodes for vectra's columnar
+ * execution path: predicate evaluation into selection vectors, hash grouped
+ * aggregation, hash-join build and probe, and the arithmetic projections
+ * that feed them.
+ *
+ * DROP-IN BOUNDARY.  The four constructors below have exactly the names,
+ * signatures, ownership rules and output schemas of the reference's node
+ * constructors, so linking libvgpu in place of src/filter.c, src/project.c,
+ * src/group_agg.c and src/join.c hands every plan the R front end and the
+ * optimizer build to the GPU.  The nodes they return keep the reference's
+ * struct prefixes and `kind` strings (include/vectra_abi.h), which the
+ * optimizer and explain() read through casts.
+ *
+ * Batches crossing the boundary are host memory owned by the receiver and
+ * released with free(), as in the reference.  Columns stay resident on the
+ * device inside a chain of libvgpu nodes: a group-agg node over a filter,
+ * a projection and/or a join runs the whole chain as one fused kernel.
+ *
+ * Errors: every failure releases the node's device state and then calls
+ * vectra_error() (src/error.c), which does not return.  Without the
+ * reference engine linked in, libvgpu's own vectra_error reports through
+ * the vgpu_guard_* entry points below.  Nothing falls back to the CPU: an
+ * input the GPU path does not support (string keys, string expressions) is
+ * an explicit error.
+ */
+#ifndef VGPU_H
+#define VGPU_H
+
+#include "vectra_abi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- drop-in node constructors -------------------------------------- */
+
+/* replaces src/filter.h:14 (FilterNode *filter_node_create) */
+FilterNode *filter_node_create(VecNode *child, VecExpr *predicate);
+
+/* replaces src/project.h:23 (ProjectNode *project_node_create) */
+ProjectNode *project_node_create(VecNode *child, int n_entries,
+                                 ProjEntry *entries);
+
+/* replaces src/group_agg.h:28-31 (GroupAggNode *group_agg_node_create).
+ * temp_dir != NULL with n_keys > 0 emits groups in ascending key order with
+ * NA last (what the reference's sort path produces); otherwise groups come
+ * in first-seen order (the reference's hash path).  No spill directory is
+ * used: group state lives in device memory. */
+GroupAggNode *group_agg_node_create(VecNode *child, int n_keys,
+                                    char **key_names, int n_aggs,
+                                    AggSpec *agg_specs, const char *temp_dir);
+
+/* replaces src/join.h:76-78 (JoinNode *join_node_create) */
+JoinNode *join_node_create(VecNode *left, VecNode *right, JoinKind kind,
+                           int n_keys, JoinKey *keys,
+                           const char *suffix_x, const char *suffix_y);
+
+/* ---- data sources (no reference counterpart beyond ScanNode's role) -- */
+
+#define VGPU_SRC_COPY    0   /* copy the host columns at creation          */
+#define VGPU_SRC_BORROW  1   /* borrow host columns (caller keeps them)     */
+#define VGPU_SRC_DEVICE  2   /* borrow device-resident columns              */
+
+/* A table as a source node, emitting batches of batch_rows rows (a multiple
+ * of 32).  data[c]: n_rows int64 / double values or bool bytes;
+ * validity[c]: the reference bitmap (bit i%8 of byte i/8), NULL = all
+ * valid.  With VGPU_SRC_DEVICE both are device pointers and libvgpu nodes
+ * read the batches in place; any other consumer gets host copies.  With
+ * VGPU_SRC_BORROW from page-locked memory, libvgpu nodes copy each batch to
+ * the device asynchronously. */
+VecNode *vgpu_table_source_create(int n_cols, const char *const *names,
+                                  const int *types, const void *const *data,
+                                  const uint8_t *const *validity,
+                                  int64_t n_rows, int64_t batch_rows,
+                                  int flags);
+
+/* ---- runtime --------------------------------------------------------- */
+
+int         vgpu_init(int device);          /* 0 on success */
+const char *vgpu_last_error(void);
+/* The CUDA stream (cudaStream_t) libvgpu launches on; NULL = its own. */
+void        vgpu_set_stream(void *cuda_stream);
+void       *vgpu_get_stream(void);
+int         vgpu_synchronize(void);
+/* Kernels launched by libvgpu since load. */
+unsigned long long vgpu_kernel_launches(void);
+/* Warnings the reference would raise through Rf_warning (all-NA min/max
+ * with na.rm), counted since load. */
+long        vgpu_warning_count(void);
+
+/* Optional kernel timing: CUDA events recorded on the launching stream
+ * around each kernel class (VGPU_PROF_*), read back in milliseconds. */
+#define VGPU_PROF_AGG         0   /* fused filter / probe / group-agg kernel */
+#define VGPU_PROF_FILTER      1   /* filter into a selection vector */
+#define VGPU_PROF_JOIN_BUILD  2   /* hash-join build insert */
+#define VGPU_PROF_JOIN_PROBE  3   /* hash-join probe count */
+#define VGPU_PROF_FINISH      4   /* group results */
+void   vgpu_profile_enable(int on);
+void   vgpu_profile_reset(void);
+double vgpu_profile_ms(int kernel_class, unsigned long long *launches);
+
+/* ---- guarded entry points for callers without an R error handler ----- */
+/* Each returns NULL (and sets vgpu_last_error) where the unguarded call
+ * would raise vectra_error. */
+VecBatch     *vgpu_guard_next_batch(VecNode *node);
+FilterNode   *vgpu_guard_filter(VecNode *child, VecExpr *predicate);
+ProjectNode  *vgpu_guard_project(VecNode *child, int n, ProjEntry *entries);
+GroupAggNode *vgpu_guard_group_agg(VecNode *child, int n_keys, char **key_names,
+                                   int n_aggs, AggSpec *specs,
+                                   const char *temp_dir);
+JoinNode     *vgpu_guard_join(VecNode *left, VecNode *right, JoinKind kind,
+                              int n_keys, JoinKey *keys, const char *suffix_x,
+                              const char *suffix_y);
+void          vgpu_batch_free(VecBatch *batch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VGPU_H */

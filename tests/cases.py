@@ -1,0 +1,316 @@
+"""Parity cases for the filter / group-agg / join path.
+
+Each case is a function (engine) -> list of batches ({name: (values,
+valid)}), built with the plan verbs, so the same case runs on the reference
+engine, the CPU oracle and libvgpu.  The first group restates the
+reference's own testthat cases (tests/testthat/test-filter.R,
+test-groupby.R, test-agg.R, test-joins.R, test-full-join.R,
+test-optimize.R); the rest are seeded random tables with NA, ragged batch
+sizes and selection vectors.
+"""
+import numpy as np
+
+from vectra_gb300.plan import tbl, col, lit, is_na
+
+NA = None
+
+
+def vals(x, dtype=None):
+    """(values, valid) from a list with None as NA."""
+    valid = np.array([v is not None for v in x], dtype=bool)
+    if dtype is None:
+        dtype = np.float64 if any(isinstance(v, float) for v in x) else np.int64
+    fill = [0 if v is None else v for v in x]
+    return np.array(fill, dtype=dtype), valid
+
+
+def T(**cols):
+    out = {}
+    for k, v in cols.items():
+        out[k] = vals(v) if isinstance(v, list) else v
+    return out
+
+
+# ---------------------------------------------------------------------------
+# restated reference tests
+# ---------------------------------------------------------------------------
+
+def f_simple(E):          # test-filter.R:1-11
+    t = T(x=[1.0, 2.0, 3.0, 4.0, 5.0], y=[10, 20, 30, 40, 50])
+    return tbl(E, t).filter(col("x") > 2.0).batches()
+
+
+def f_equality(E):        # test-filter.R:13-20
+    t = T(x=[1, 2, 3, 2, 1])
+    return tbl(E, t).filter(col("x").eq(2.0)).batches()
+
+
+def f_and_or_not(E):      # test-filter.R:22-47
+    t = T(x=[1.0, 2.0, 3.0, 4.0, 5.0], y=[5.0, 4.0, 3.0, 2.0, 1.0])
+    a = tbl(E, t).filter((col("x") > 1.0) & (col("y") > 1.0)).batches()
+    b = tbl(E, t).filter((col("x") < 2.0) | (col("y") < 2.0)).batches()
+    c = tbl(E, t).filter(~(col("x") > 3.0)).batches()
+    return a + b + c
+
+
+def f_na_dropped(E):      # test-filter.R:58-69
+    t = T(x=[1.0, NA, 3.0, NA, 5.0])
+    return tbl(E, t).filter(col("x") > 2.0).batches()
+
+
+def f_is_na(E):           # test-filter.R:49-56
+    t = T(x=[1.0, NA, 3.0], y=[1, 2, 3])
+    return tbl(E, t).filter(is_na(col("x"))).batches() + tbl(E, t).filter(~is_na(col("x"))).batches()
+
+
+def f_kleene(E):          # NA & FALSE = FALSE, NA | TRUE = TRUE (src/scalar_ops.c:168-181)
+    t = T(a=[1.0, NA, 3.0, NA, 0.0, 2.0], b=[NA, 1.0, NA, 0.0, NA, 2.0])
+    x = tbl(E, t).filter((col("a") > 1.0) | (col("b") > 0.5)).batches()
+    y = tbl(E, t).filter(~((col("a") > 1.0) & (col("b") > 0.5))).batches()
+    return x + y
+
+
+def f_double_filter(E):   # test-filter.R:89-97
+    t = T(x=list(range(1, 21)), y=[float(i % 7) for i in range(20)])
+    return tbl(E, t, batch_rows=8).filter(col("x") > 5).filter(col("y") < 4.0).batches()
+
+
+def f_empty(E):           # test-filter.R:163-173
+    t = T(x=[1.0, 2.0, 3.0])
+    return tbl(E, t).filter(col("x") > 100.0).batches()
+
+
+def f_general_expr(E):    # column-vs-column and arithmetic predicates
+    t = T(x=[1.0, 5.0, NA, 7.0, 2.0, 9.0], y=[2, 3, 4, NA, 1, 9])
+    a = tbl(E, t).filter(col("x") > col("y")).batches()
+    b = tbl(E, t).filter((col("x") + col("y")) >= 8.0).batches()
+    c = tbl(E, t).filter((col("y") % 2).eq(1) | is_na(col("x"))).batches()
+    return a + b + c
+
+
+def f_int_vs_double_literal(E):   # int64 column compared with a double (src/scalar_ops.c:110-142)
+    big = 2 ** 53
+    t = T(v=[big - 2, big - 1, big, big + 1, big + 2, big + 3, -5, 0, 7])
+    out = []
+    for op in (">", ">=", "<", "<=", "==", "!="):
+        e = col("v")._cmp(op, float(big + 1))
+        out += tbl(E, t).filter(e).batches()
+    out += tbl(E, t).filter(col("v") > 2.5).batches()
+    out += tbl(E, t).filter(col("v") <= -4.5).batches()
+    return out
+
+
+def g_basic(E, temp_dir):          # test-groupby.R:1-46
+    t = T(g=[1, 2, 1, 2, 1], x=[1.0, 2.0, 3.0, 4.0, 5.0])
+    return tbl(E, t).group_by("g").summarise(temp_dir=temp_dir, n=("n",), s=("sum", "x"), m=("mean", "x"),
+                                            lo=("min", "x"), hi=("max", "x")).batches()
+
+
+def g_na_key(E, temp_dir):         # test-groupby.R:48-59
+    t = T(g=[1, NA, 1, NA, 2], x=[1.0, 2.0, 3.0, 4.0, 5.0])
+    return tbl(E, t).group_by("g").summarise(temp_dir=temp_dir, s=("sum", "x"), n=("n",)).batches()
+
+
+def g_multi_key(E, temp_dir):      # test-groupby.R:61-72
+    t = T(a=[1, 1, 2, 2, 1, NA], b=[1.0, 2.0, 1.0, 1.0, 1.0, 2.0], x=[1, 2, 3, 4, 5, 6])
+    return tbl(E, t).group_by("a", "b").summarise(temp_dir=temp_dir, s=("sum", "x"), n=("n",)).batches()
+
+
+def g_na_semantics(E, temp_dir):   # test-agg.R:3-127, test-groupby.R:74-99
+    t = T(g=[1, 1, 2, 2, 3, 3], x=[1.0, NA, NA, NA, 4.0, 5.0], y=[1, NA, NA, NA, 7, 9])
+    return tbl(E, t).group_by("g").summarise(
+        temp_dir=temp_dir, s=("sum", "x"), m=("mean", "x"), lo=("min", "x"), hi=("max", "x"),
+        sr=("sum", "x", True), mr=("mean", "x", True), lor=("min", "x", True), hir=("max", "x", True),
+        si=("sum", "y"), sir=("sum", "y", True), mir=("mean", "y", True), loi=("min", "y", True),
+        hii=("max", "y", True), n=("n",), c=("count", "x")).batches()
+
+
+def g_int_sum_double(E, temp_dir):  # test-agg.R:131-139
+    t = T(g=[1, 1, 2], y=[2 ** 40, 3, -7])
+    return tbl(E, t).group_by("g").summarise(temp_dir=temp_dir, s=("sum", "y"), m=("mean", "y")).batches()
+
+
+def g_resize_200(E, temp_dir):      # test-groupby.R:101-131 (200 groups over 2000 rows)
+    rng = np.random.default_rng(101)
+    g = rng.integers(0, 200, 2000)
+    x = rng.normal(0, 1, 2000)
+    t = {"g": g, "x": x}
+    return tbl(E, t, batch_rows=256).group_by("g").summarise(temp_dir=temp_dir, s=("sum", "x"),
+                                                              m=("mean", "x"), n=("n",)).batches()
+
+
+def g_filter_then_group(E, temp_dir):   # test-groupby.R:133-149, test-filter.R:247-284
+    t = T(g=[1, 2, 1, 2, 3, 3, 1], x=[1.0, 5.0, 3.0, 7.0, 2.0, 9.0, NA])
+    return (tbl(E, t, batch_rows=32).filter(col("x") > 2.0).group_by("g")
+            .summarise(temp_dir=temp_dir, s=("sum", "x"), n=("n",)).batches())
+
+
+def g_ungrouped(E, temp_dir):       # summarise without group_by (hash path, one group)
+    t = T(x=[1.0, 2.0, NA, 4.0])
+    a = tbl(E, t).group_by().summarise(temp_dir=temp_dir, s=("sum", "x", True), n=("n",)).batches()
+    b = tbl(E, T(x=[1.0])).filter(col("x") > 5.0).group_by().summarise(temp_dir=temp_dir, n=("n",)).batches()
+    return a + b
+
+
+def g_nested_expr(E, temp_dir):     # test-optimize.R:73-96: sum(x + y) via a hidden projection
+    t = T(g=[1, 1, 2, 2], x=[1.0, 2.0, 3.0, NA], y=[10.0, 20.0, 30.0, 40.0])
+    return tbl(E, t).group_by("g").summarise(temp_dir=temp_dir, s=("sum", col("x") + col("y")),
+                                            p=("sum", col("x") * col("y"), True)).batches()
+
+
+def g_bool_and_double_keys(E, temp_dir):
+    t = T(b=vals([1, 0, 1, None, 0, 1], np.uint8), d=[0.5, -0.0, 0.0, 2.5, NA, 0.5], x=[1, 2, 3, 4, 5, 6])
+    a = tbl(E, t).group_by("b").summarise(temp_dir=temp_dir, s=("sum", "x"), lo=("min", "b"), n=("n",)).batches()
+    return a
+
+
+def j_inner_left_semi_anti(E):      # test-joins.R:12-56
+    l = T(id=[1, 2, 3, 4], x=[10.0, 20.0, 30.0, 40.0])
+    r = T(id=[2, 3, 5], y=[200.0, 300.0, 500.0])
+    out = []
+    out += tbl(E, l).inner_join(tbl(E, r), "id").batches()
+    out += tbl(E, l).left_join(tbl(E, r), "id").batches()
+    out += tbl(E, l).semi_join(tbl(E, r), "id").batches()
+    out += tbl(E, l).anti_join(tbl(E, r), "id").batches()
+    return out
+
+
+def j_duplicates(E):                # test-joins.R:84-95 (fan-out, descending build order)
+    l = T(k=[1, 2, 1, 3], x=[1.0, 2.0, 3.0, 4.0])
+    r = T(k=[1, 1, 2, 1, 4], y=[10.0, 11.0, 20.0, 12.0, 40.0])
+    return (tbl(E, l).inner_join(tbl(E, r), "k").batches() +
+            tbl(E, l).left_join(tbl(E, r), "k").batches())
+
+
+def j_na_keys(E):                   # test-joins.R:97-120
+    l = T(k=[1, NA, 3, NA], x=[1.0, 2.0, 3.0, 4.0])
+    r = T(k=[NA, 1, 3, NA], y=[10.0, 11.0, 13.0, 14.0])
+    out = []
+    for kind in ("inner_join", "left_join", "semi_join", "anti_join"):
+        out += getattr(tbl(E, l), kind)(tbl(E, r), "k").batches()
+    return out
+
+
+def j_suffix(E):                    # test-joins.R:122-133
+    l = T(id=[1, 2], v=[1.0, 2.0])
+    r = T(id=[1, 2], v=[10.0, 20.0])
+    return tbl(E, l).inner_join(tbl(E, r), "id").batches()
+
+
+def j_coerce(E):                    # test-joins.R:220-272
+    l = T(id=[1, 2, 3], x=[10.0, 20.0, 30.0])
+    r = T(id=[1.0, 2.0, 4.0], y=[100.0, 200.0, 400.0])
+    a = tbl(E, l).inner_join(tbl(E, r), "id").batches()
+    l2 = T(a=[1.0, 2.0], b=[10, 20], x=[1.0, 2.0])
+    r2 = T(a=[1.0, 2.0], b=[10.0, 20.0], y=[3.0, 4.0])
+    b = tbl(E, l2).inner_join(tbl(E, r2), ["a", "b"]).batches()
+    return a + b
+
+
+def j_streaming(E):                 # test-joins.R:314-409 (batch_size = 10)
+    rng = np.random.default_rng(314)
+    l = {"k": rng.integers(0, 30, 95), "x": rng.normal(0, 1, 95)}
+    r = {"k": rng.integers(0, 40, 50), "y": rng.normal(0, 1, 50)}
+    out = []
+    for kind in ("inner_join", "left_join", "semi_join", "anti_join"):
+        out += getattr(tbl(E, l, batch_rows=10), kind)(tbl(E, r, batch_rows=10), "k").batches()
+    return out
+
+
+def j_after_filter(E):              # test-joins.R:411-423
+    l = T(id=[1, 2, 3, 4, 5], x=[1.0, 2.0, 3.0, 4.0, 5.0])
+    r = T(id=[2, 4, 5], y=[20.0, 40.0, 50.0])
+    return tbl(E, l).filter(col("x") > 2.0).inner_join(tbl(E, r), "id").batches()
+
+
+def j_full(E):                      # test-full-join.R:3-72
+    l = T(id=[1, 2, 3], x=[1.0, 2.0, 3.0])
+    r = T(id=[2, 3, 4, 5], y=[20.0, 30.0, 40.0, 50.0])
+    return tbl(E, l).full_join(tbl(E, r), "id").batches()
+
+
+def ja_join_agg(E, temp_dir):       # the benchmark plan, small: left_join then sum(value * weight)
+    rng = np.random.default_rng(7)
+    nf, nd = 5000, 300
+    ids = rng.permutation(nd) + 1
+    fact = {"key": (rng.integers(1, nd + 40, nf), rng.random(nf) > 0.01),
+            "value": (rng.lognormal(0, 1, nf), rng.random(nf) > 0.02)}
+    dim = {"id": ids, "category": rng.integers(0, 16, nd), "weight": rng.random(nd)}
+    a = (tbl(E, fact, batch_rows=1024).left_join(tbl(E, dim, batch_rows=128), {"key": "id"})
+         .group_by("category").summarise(temp_dir=temp_dir, s=("sum", col("value") * col("weight")),
+                                          sr=("sum", col("value") * col("weight"), True), n=("n",)).batches())
+    return a
+
+
+# ---------------------------------------------------------------------------
+# seeded random cases
+# ---------------------------------------------------------------------------
+
+def random_table(seed, n, n_groups=50, na=0.05):
+    rng = np.random.default_rng(seed)
+    return {
+        "k": (rng.integers(0, n_groups, n), rng.random(n) > na),
+        "d": (rng.normal(0, 100, n), rng.random(n) > na),
+        "i": (rng.integers(-1000, 1000, n), rng.random(n) > na),
+        "b": (rng.integers(0, 2, n).astype(np.uint8), rng.random(n) > na),
+    }
+
+
+def r_filter(E, seed, n, batch_rows, sel_mode):
+    t = random_table(seed, n)
+    pred = (col("d") > -20.0) & (col("i") <= 500) & ~(col("b").eq(True))
+    return tbl(E, t, batch_rows=batch_rows, sel_mode=sel_mode).filter(pred).batches()
+
+
+def r_group(E, seed, n, batch_rows, sel_mode, temp_dir):
+    t = random_table(seed, n)
+    return (tbl(E, t, batch_rows=batch_rows, sel_mode=sel_mode).filter(col("d") > -150.0)
+            .group_by("k").summarise(temp_dir=temp_dir, n=("n",), si=("sum", "i"), mi=("mean", "i", True),
+                                     lo=("min", "i"), hi=("max", "d", True), c=("count", "d"),
+                                     sd=("sum", "d", True)).batches())
+
+
+def r_join(E, seed, n, batch_rows, kind):
+    rng = np.random.default_rng(seed)
+    l = {"k": (rng.integers(0, 60, n), rng.random(n) > 0.05), "x": rng.normal(0, 1, n)}
+    r = {"k": (rng.integers(0, 80, 70), rng.random(70) > 0.05), "y": rng.normal(0, 1, 70),
+         "z": rng.integers(0, 5, 70)}
+    return getattr(tbl(E, l, batch_rows=batch_rows), kind)(tbl(E, r, batch_rows=32), "k").batches()
+
+
+FILTER_CASES = [f_simple, f_equality, f_and_or_not, f_na_dropped, f_is_na, f_kleene, f_double_filter,
+                f_empty, f_general_expr, f_int_vs_double_literal]
+GROUP_CASES = [g_basic, g_na_key, g_multi_key, g_na_semantics, g_int_sum_double, g_resize_200,
+               g_filter_then_group, g_ungrouped, g_nested_expr, g_bool_and_double_keys, ja_join_agg]
+JOIN_CASES = [j_inner_left_semi_anti, j_duplicates, j_na_keys, j_suffix, j_coerce, j_streaming,
+              j_after_filter, j_full]
+
+# sizes chosen to hit warp / block edges: empty, 1, 31, 32, 33, 65, multi-block
+RAGGED = [(0, 32), (1, 32), (31, 32), (32, 32), (33, 32), (65, 64), (1000, 96), (20000, 4096)]
+
+
+# ---------------------------------------------------------------------------
+# comparison
+# ---------------------------------------------------------------------------
+
+def same_batches(a, b, rtol=0.0, tol_cols=()):
+    """Batch lists equal: names, row counts, validity, and values where
+    valid (bit-exact unless the column is listed in tol_cols)."""
+    assert len(a) == len(b), "batch count %d != %d" % (len(a), len(b))
+    for bi, (x, y) in enumerate(zip(a, b)):
+        assert list(x.keys()) == list(y.keys()), (bi, list(x.keys()), list(y.keys()))
+        for name in x:
+            va, ma = x[name]
+            vb, mb = y[name]
+            assert len(va) == len(vb), (bi, name, len(va), len(vb))
+            assert np.array_equal(ma, mb), (bi, name, "validity", ma, mb)
+            va, vb = va[ma], vb[mb]
+            if va.dtype == object:
+                assert list(va) == list(vb), (bi, name)
+            elif name in tol_cols and va.dtype == np.float64:
+                both_nan = np.isnan(va) & np.isnan(vb)
+                close = np.isclose(va, vb, rtol=rtol, atol=0) | both_nan | (va == vb)
+                assert close.all(), (bi, name, va[~close], vb[~close])
+            else:
+                eq = (va == vb) | (np.isnan(va) & np.isnan(vb) if va.dtype == np.float64 else False)
+                assert np.all(eq), (bi, name, va[~eq], vb[~eq])

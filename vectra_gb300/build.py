@@ -1,0 +1,86 @@
+"""Builds libvgpu.so in-tree: the sm_103a kernels (nvcc) and the C11 host
+layer (gcc), linked into one shared library next to this file.
+
+    python -m vectra_gb300.build        # or vectra_gb300.build.build()
+
+No CMake, no torch extension machinery: a handful of translation units
+compiled in parallel, then one link step.
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libvgpu.so")
+
+CU_SOURCES = ["k_filter.cu", "k_agg.cu", "k_sort.cu", "k_join.cu", "k_prof.cu"]
+C_SOURCES = ["runtime.c", "compile.c", "source.c", "node_filter.c",
+             "node_project.c", "node_agg.c", "node_join.c"]
+
+GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
+
+
+def _nvcc():
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    p = os.path.join(cuda, "bin", "nvcc")
+    return p if os.path.exists(p) else (shutil.which("nvcc") or "nvcc")
+
+
+def _cuda_include():
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    return os.path.join(cuda, "include")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n%s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return r
+
+
+def _stale(obj, srcs):
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def build(verbose=False):
+    """Compiles what changed and links libvgpu.so.  Returns its path."""
+    os.makedirs(BUILD, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
+    jobs = []
+    objs = []
+    for f in CU_SOURCES:
+        src = os.path.join(CSRC, f)
+        obj = os.path.join(BUILD, f + ".o")
+        objs.append(obj)
+        if _stale(obj, [src] + headers):
+            jobs.append([_nvcc(), GENCODE, "-O3", "-lineinfo", "-std=c++17",
+                         "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE, "-c", src, "-o", obj])
+    for f in C_SOURCES:
+        src = os.path.join(CSRC, f)
+        obj = os.path.join(BUILD, f + ".o")
+        objs.append(obj)
+        if _stale(obj, [src] + headers):
+            jobs.append(["gcc", "-std=gnu11", "-O2", "-g", "-fPIC", "-Wall", "-Wno-unused-function",
+                         "-I", CSRC, "-I", INCLUDE, "-I", _cuda_include(), "-c", src, "-o", obj])
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        for r in ex.map(_run, jobs):
+            if verbose and (r.stdout or r.stderr):
+                sys.stderr.write(r.stdout + r.stderr)
+    if jobs or not os.path.exists(LIB):
+        tmp = LIB + ".tmp"
+        _run([_nvcc(), GENCODE, "-shared", "-o", tmp] + objs + ["-cudart", "static"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

@@ -486,9 +486,11 @@ agg_kernel(const VgAggLaunch *__restrict__ Lp, int64_t n_logical) {
     const VgAggLaunch &L = *Lp;
     const int S = L.cache_slots;
     CacheLayout cl;
+    __shared__ int cache_used;   // occupied cache slots; a nearly full cache stops taking new keys
     if (kCache) {
         cl = cache_layout(L, S);
         for (int i = threadIdx.x; i < S; i += blockDim.x) init_cache_slot(L, sm, cl, S, i);
+        if (threadIdx.x == 0) cache_used = 0;
         __syncthreads();
     }
     int32_t ktypes[VG_MAX_KEYS];
@@ -543,9 +545,9 @@ agg_kernel(const VgAggLaunch *__restrict__ Lp, int64_t n_logical) {
                     uint64_t rank = matched ? (uint64_t)(mcount - 1 - m) : 0;
                     if (rank > 0x7FF) rank = 0x7FF;
                     order = ((uint64_t)L.batch_idx << 44) | ((uint64_t)(matched ? 0 : 1) << 43) |
-                            ((uint64_t)(pr & 0xFFFFFFFF) << 11) | rank;
+                            ((uint64_t)(li & 0xFFFFFFFF) << 11) | rank;
                 } else {
-                    order = (uint64_t)(L.row_base + pr);
+                    order = (uint64_t)(L.row_base + li);   // logical position in the stream
                 }
             }
             uint64_t h = hash_keys(k, L.n_keys, nm);
@@ -560,15 +562,18 @@ agg_kernel(const VgAggLaunch *__restrict__ Lp, int64_t n_logical) {
                 uint64_t *sk = (uint64_t *)(sm + cl.keys);
                 int slot = (int)(h & (uint64_t)(S - 1));
                 int found = -1;
-                for (int probe = 0; probe < 16; probe++) {
+                const bool may_insert = *(volatile int *)&cache_used < (S * 3) / 4;
+                for (int probe = 0; probe < (may_insert ? 16 : 4); probe++) {
                     uint32_t s0 = *(volatile uint32_t *)(st + slot);
                     if (s0 == 0) {
+                        if (!may_insert) break;
                         uint32_t prev = atomicCAS(st + slot, 0u, 1u);
                         if (prev == 0u) {
                             for (int i = 0; i < L.n_keys; i++) sk[(int64_t)i * S + slot] = k[i];
                             snm[slot] = nm;
                             __threadfence_block();
                             atomicExch(st + slot, 2u);
+                            atomicAdd(&cache_used, 1);
                             found = slot;
                             break;
                         }
@@ -956,6 +961,7 @@ int vgk_agg_launch(const VgAggLaunch *L, vg_stream_t s) {
         k<<<grid, kThreads, smem, st>>>((const VgAggLaunch *)dL, n_logical);             \
         vg_launch_counter++;                                                            \
     } while (0)
+    vg_prof_begin(VG_PROF_AGG, st);
     if (pred) {
         if (join) { if (cache) VG_LAUNCH(true, true, true); else VG_LAUNCH(true, true, false); }
         else { if (cache) VG_LAUNCH(true, false, true); else VG_LAUNCH(true, false, false); }
@@ -964,6 +970,7 @@ int vgk_agg_launch(const VgAggLaunch *L, vg_stream_t s) {
         else { if (cache) VG_LAUNCH(false, false, true); else VG_LAUNCH(false, false, false); }
     }
 #undef VG_LAUNCH
+    vg_prof_end(VG_PROF_AGG, st);
     cudaFreeAsync(dL, st);
     return check(cudaGetLastError(), "agg launch");
 }
@@ -1042,7 +1049,9 @@ int vgk_group_finish(const VgGroupTable *gt, int n_keys, const int32_t *key_type
     void *dF = nullptr;
     if (check(cudaMallocAsync(&dF, sizeof(F), st), "finish args")) return -1;
     cudaMemcpyAsync(dF, &F, sizeof(F), cudaMemcpyHostToDevice, st);
+    vg_prof_begin(VG_PROF_FINISH, st);
     { finish_kernel<<<grid_for(n_groups, 128), 128, 0, st>>>((const FinishArgs *)dF); vg_launch_counter++; }
+    vg_prof_end(VG_PROF_FINISH, st);
     cudaFreeAsync(dF, st);
     return check(cudaGetLastError(), "finish");
 }

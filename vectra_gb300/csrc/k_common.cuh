@@ -10,6 +10,16 @@
 // number of kernels this library has launched (reported by the benchmark)
 extern "C" unsigned long long vg_launch_counter;
 
+// optional event timing per kernel class (k_prof.cu); classes as in vgpu.h
+#define VG_PROF_CLASSES 8
+#define VG_PROF_AGG 0
+#define VG_PROF_FILTER 1
+#define VG_PROF_JOIN_BUILD 2
+#define VG_PROF_JOIN_PROBE 3
+#define VG_PROF_FINISH 4
+void vg_prof_begin(int cls, cudaStream_t s);
+void vg_prof_end(int cls, cudaStream_t s);
+
 // ---------------------------------------------------------------------
 // validity bits and column loads
 // ---------------------------------------------------------------------
@@ -229,6 +239,6 @@ VG_DEV double vg_digits_to_double(const int64_t *w, int n, uint32_t special) {
 // ---------------------------------------------------------------------
 
 #define VG_SPIN_LIMIT (1 << 22)
-#define VG_ERR_WAIT   1u
-#define VG_ERR_FULL   2u
-#define VG_ERR_PROG   4u
+
+
+

@@ -339,6 +339,19 @@ __global__ void gather_kernel(VgCol c, const int32_t *idx, int64_t n_out, int nu
     }
 }
 
+__global__ void gather_into_kernel(VgCol c, const int32_t *idx, int64_t n, void *out,
+                                   uint32_t *out_valid, int64_t row0) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        int64_t p = idx ? (int64_t)idx[j] : j;
+        bool ok = vg_valid(c, p);
+        int64_t d = row0 + j;
+        if (c.type == VEC_BOOL) ((uint8_t *)out)[d] = ok ? __ldg((const uint8_t *)c.data + p) : 0;
+        else ((uint64_t *)out)[d] = ok ? vg_load_bits(c, p) : 0;
+        if (ok) atomicOr(out_valid + (d >> 5), 1u << (d & 31));
+    }
+}
+
 char g_err_msg[256];
 
 int check(cudaError_t e, const char *what) {
@@ -397,11 +410,13 @@ int run_filter(const void *args, size_t args_bytes, int64_t n_logical, const int
     int n_blocks = (int)((n_logical + kRowsPerBlock - 1) / kRowsPerBlock);
     if (check(cudaMemcpyAsync(fs.args, args, args_bytes, cudaMemcpyHostToDevice, s), "filter args")) return -1;
     if (check(cudaMemsetAsync(fs.err, 0, 4, s), "filter err")) return -1;
+    vg_prof_begin(VG_PROF_FILTER, s);
     { keep_words_kernel<kUseProg><<<n_blocks, kThreads, 0, s>>>(
         (const PredArgs *)fs.args, (const ProgArgs *)fs.args, n_logical, d_sel_in,
         fs.words, fs.counts, fs.err); vg_launch_counter++; }
     { compact_kernel<<<n_blocks, kThreads, 0, s>>>(n_logical, d_sel_in, fs.words, fs.counts,
                                                  n_blocks, d_sel_out, fs.total); vg_launch_counter++; }
+    vg_prof_end(VG_PROF_FILTER, s);
     int64_t tot = 0;
     uint32_t err = 0;
     if (check(cudaMemcpyAsync(&tot, fs.total, 8, cudaMemcpyDeviceToHost, s), "filter count")) return -1;
@@ -492,6 +507,14 @@ int vgk_gather(const VgCol *col, const int32_t *d_idx, int64_t n_out, int null_i
     { gather_kernel<<<grid_for(n_out, 256), 256, 0, st>>>(*col, d_idx, n_out, null_if_negative,
                                                          d_out, d_out_valid); vg_launch_counter++; }
     return check(cudaGetLastError(), "gather");
+}
+
+int vgk_gather_into(const VgCol *col, const int32_t *d_idx, int64_t n, void *d_out,
+                    uint32_t *d_out_valid, int64_t row0, vg_stream_t s) {
+    if (n <= 0) return 0;
+    cudaStream_t st = (cudaStream_t)s;
+    { gather_into_kernel<<<grid_for(n, 256), 256, 0, st>>>(*col, d_idx, n, d_out, d_out_valid, row0); vg_launch_counter++; }
+    return check(cudaGetLastError(), "gather into");
 }
 
 }  // extern "C"

@@ -275,8 +275,9 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         K.types[i] = jt->key_types[i];
     }
     { jt_init_kernel<<<grid_for(jt->cap, 256), 256, 0, st>>>(*jt, counters); vg_launch_counter++; }
-    if (n_build > 0)
+    vg_prof_begin(VG_PROF_JOIN_BUILD, st);
         { jt_insert_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(*jt, K, n_build, rslot, counters); vg_launch_counter++; }
+        vg_prof_end(VG_PROF_JOIN_BUILD, st);
     uint32_t hc[4] = {0, 0, 0, 0};
     cudaMemcpyAsync(hc, counters, 16, cudaMemcpyDeviceToHost, st);
     if (check(cudaStreamSynchronize(st), "join build")) return -1;
@@ -329,7 +330,9 @@ int vgk_join_probe_count(const VgJoinTable *jt, const VgCol *pkeys, int n_keys, 
         K.conv[i] = key_conv[i];
         K.types[i] = jt->key_types[i];
     }
+    vg_prof_begin(VG_PROF_JOIN_PROBE, st);
     { probe_count_kernel<<<grid_for(n, 256), 256, 0, st>>>(*jt, K, n, d_sel, kind, ps.cnt, ps.start, ps.flag); vg_launch_counter++; }
+    vg_prof_end(VG_PROF_JOIN_PROBE, st);
     if (vgk_exclusive_scan(ps.cnt, n, ps.off, ps.totals + 0, ps.scan, ps.scan_bytes, s)) return -1;
     if (vgk_exclusive_scan(ps.flag, n, ps.off2, ps.totals + 1, ps.scan, ps.scan_bytes, s)) return -1;
     int64_t t[2] = {0, 0};

@@ -1,0 +1,411 @@
+/*
+ * node_join.c -- JoinNode on the GPU (replaces src/join.c).
+ *
+ * Same state machine as the reference (src/join.c:569-599): BUILD pulls the
+ * whole right side (applying any sel, src/join.c:166-182) into device
+ * columns and builds the hash table; PROBE turns each left batch into one
+ * output batch (skipping empty ones); FINALIZE (FULL joins) emits the build
+ * rows nothing matched, 65536 at a time (src/join.c:487-551).
+ *
+ * Keys are compared after the reference's coercion: the build key takes the
+ * common type of both sides and the probe key is converted to it
+ * (src/join.c:190-205, 270-293).  NA (and NaN) keys never match
+ * (src/join.c:85).
+ *
+ * Output batches are host memory, columns ordered left ++ right non-key with
+ * the reference's suffix rule; SEMI/ANTI return the probe batch itself with
+ * a selection vector of the kept rows.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "vg_host.h"
+
+typedef struct {
+    JoinNodePrefix jn;        /* reference prefix: base, left, right, kind, n_keys, keys, suffixes */
+    int state;                /* 0 build, 1 probe, 2 finalize, 3 done */
+    int built;
+    VgJoinBuilt B;
+    int64_t n_build;
+    int32_t key_type[VG_MAX_KEYS];
+    int32_t conv_build[VG_MAX_KEYS];
+    void *build_block;        /* device build columns */
+    void *table_block;        /* device hash table */
+    int *r_nonkey;
+    int r_nonkey_n;
+    uint32_t *d_matched;      /* FULL: build rows matched so far */
+    int32_t *d_unmatched;
+    int64_t n_unmatched, fin_cursor;
+    int64_t batch_idx;
+} VgJoin;
+
+static VecBatch *join_next(VecNode *self);
+
+int vg_is_join(const VecNode *n) { return n && n->next_batch == join_next; }
+VecNode *vg_join_left(VecNode *n) { return ((VgJoin *)n)->jn.left; }
+int vg_join_kind(VecNode *n) { return ((VgJoin *)n)->jn.kind; }
+
+int vg_join_resolve(VecNode *n, const char *name, int *side, int *col) {
+    VgJoin *j = (VgJoin *)n;
+    int i = vg_schema_find(&j->jn.base.output_schema, name);
+    if (i < 0) return 0;
+    int nl = j->jn.left->output_schema.n_cols;
+    if (i < nl) { *side = 0; *col = i; }
+    else { *side = 1; *col = j->r_nonkey[i - nl]; }
+    return 1;
+}
+
+static int common_type(int a, int b) {
+    if (a == b) return a;
+    if (a == VEC_DOUBLE || b == VEC_DOUBLE) return VEC_DOUBLE;
+    if (a == VEC_INT64 || b == VEC_INT64) return VEC_INT64;
+    return VEC_BOOL;
+}
+
+static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+static size_t elem(int t) { return t == VEC_BOOL ? 1 : 8; }
+
+/* BUILD: materialise the right side on the device, then the hash table */
+static void join_build(VgJoin *j) {
+    if (j->built) return;
+    const VecSchema *rs = &j->jn.right->output_schema;
+    int nr = rs->n_cols;
+    uint8_t *need = (uint8_t *)vg_xcalloc((size_t)(nr ? nr : 1), 1);
+    for (int k = 0; k < j->jn.n_keys; k++) need[j->jn.keys[k].right_col] = 1;
+    for (int q = 0; q < j->r_nonkey_n; q++) {
+        int c = j->r_nonkey[q];
+        if (rs->col_types[c] == VEC_STRING)
+            vg_fail("string column '%s' is not supported by the GPU join", rs->col_names[c]);
+        need[c] = 1;
+    }
+    /* pull every batch, keeping them on the device until the total is known */
+    int cap = 16, nb = 0;
+    VgDBatch *bs = (VgDBatch *)vg_xcalloc((size_t)cap, sizeof(VgDBatch));
+    int64_t total = 0;
+    for (;;) {
+        if (nb == cap) {
+            cap *= 2;
+            bs = (VgDBatch *)realloc(bs, (size_t)cap * sizeof(VgDBatch));
+            if (!bs) vg_fail("host allocation failed");
+        }
+        if (!vg_pull(j->jn.right, need, 0, &bs[nb])) break;
+        total += bs[nb].d_sel ? bs[nb].sel_n : bs[nb].n_rows;
+        nb++;
+    }
+    j->n_build = total;
+    j->B.n_bcols = nr;
+    j->B.bcols = (VgCol *)vg_xcalloc((size_t)(nr ? nr : 1), sizeof(VgCol));
+    /* dense device copy of the logical rows (one gather per batch) */
+    size_t wbytes = (size_t)((total + 31) / 32) * 4 + 8;
+    size_t bytes = 0;
+    for (int c = 0; c < nr; c++)
+        if (need[c]) bytes += a256((size_t)total * elem(rs->col_types[c]) + 8) + a256(wbytes);
+    char *blk = (char *)vg_dmalloc(bytes ? bytes : 256);
+    j->build_block = blk;
+    size_t off = 0;
+    for (int c = 0; c < nr; c++) {
+        j->B.bcols[c].type = rs->col_types[c];
+        if (!need[c]) continue;
+        char *dv = blk + off;
+        off += a256((size_t)total * elem(rs->col_types[c]) + 8);
+        uint32_t *dm = (uint32_t *)(blk + off);
+        off += a256(wbytes);
+        vg_dmemset(dm, 0, wbytes);
+        int64_t at = 0;
+        for (int b = 0; b < nb; b++) {
+            int64_t n = bs[b].d_sel ? bs[b].sel_n : bs[b].n_rows;
+            if (n == 0) continue;
+            vg_check_rc(vgk_gather_into(&bs[b].cols[c], bs[b].d_sel, n, dv, dm, at, vg_stream()),
+                        "join build gather");
+            at += n;
+        }
+        j->B.bcols[c].data = dv;
+        j->B.bcols[c].valid = dm;
+    }
+    for (int b = 0; b < nb; b++) vg_dbatch_release(&bs[b]);
+    free(bs);
+    free(need);
+
+    /* hash table */
+    int nk = j->jn.n_keys;
+    int64_t tcap = vgk_join_cap(total);
+    size_t tb = a256((size_t)tcap * 4) * 3 + a256((size_t)tcap * 8 * (size_t)nk) + a256((size_t)(total > 0 ? total : 1) * 4) + 256;
+    char *t = (char *)vg_dmalloc(tb);
+    j->table_block = t;
+    VgJoinTable *jt = &j->B.jt;
+    memset(jt, 0, sizeof(*jt));
+    jt->cap = tcap;
+    jt->n_keys = nk;
+    for (int k = 0; k < nk; k++) jt->key_types[k] = j->key_type[k];
+    size_t o = 0;
+    jt->state = (uint32_t *)(t + o); o += a256((size_t)tcap * 4);
+    jt->start = (int32_t *)(t + o); o += a256((size_t)tcap * 4);
+    jt->count = (int32_t *)(t + o); o += a256((size_t)tcap * 4);
+    jt->keys = (uint64_t *)(t + o); o += a256((size_t)tcap * 8 * (size_t)nk);
+    jt->rows = (int32_t *)(t + o); o += a256((size_t)(total > 0 ? total : 1) * 4);
+    jt->err = (uint32_t *)(t + o);
+    jt->n_build = total;
+    VgCol kc[VG_MAX_KEYS];
+    for (int k = 0; k < nk; k++) kc[k] = j->B.bcols[j->jn.keys[k].right_col];
+    size_t sb = vgk_join_build_scratch_bytes(total);
+    void *scratch = vg_dmalloc(sb);
+    int64_t distinct = 0, maxdup = 0;
+    int rc = vgk_join_build(jt, kc, nk, j->conv_build, total, scratch, sb, &distinct, &maxdup, vg_stream());
+    vg_dfree(scratch);
+    vg_check_rc(rc, "join build");
+    if (j->jn.kind == JOIN_FULL) {
+        size_t mb = (size_t)((total + 31) / 32) * 4 + 8;
+        j->d_matched = (uint32_t *)vg_dmalloc(mb);
+        vg_dmemset(j->d_matched, 0, mb);
+    }
+    j->built = 1;
+}
+
+const VgJoinBuilt *vg_join_build_now(VecNode *n) {
+    VgJoin *j = (VgJoin *)n;
+    join_build(j);
+    return &j->B;
+}
+
+/* one probe batch -> one output batch (NULL if empty) */
+static VecBatch *probe_one(VgJoin *j) {
+    const VecSchema *ls = &j->jn.left->output_schema;
+    int nl = ls->n_cols, nk = j->jn.n_keys;
+    int semi = (j->jn.kind == JOIN_SEMI || j->jn.kind == JOIN_ANTI);
+    uint8_t *need = (uint8_t *)vg_xcalloc((size_t)(nl ? nl : 1), 1);
+    for (int k = 0; k < nk; k++) need[j->jn.keys[k].left_col] = 1;
+    if (!semi) {
+        for (int c = 0; c < nl; c++) {
+            if (ls->col_types[c] == VEC_STRING)
+                vg_fail("string column '%s' is not supported by the GPU join", ls->col_names[c]);
+            need[c] = 1;
+        }
+    }
+    for (;;) {
+        VgDBatch db;
+        if (!vg_pull(j->jn.left, need, semi, &db)) { free(need); return NULL; }
+        j->batch_idx++;
+        int64_t n = db.d_sel ? db.sel_n : db.n_rows;
+        VgCol pk[VG_MAX_KEYS];
+        for (int k = 0; k < nk; k++) pk[k] = db.cols[j->jn.keys[k].left_col];
+        size_t sb = vgk_join_probe_scratch_bytes(n);
+        void *scratch = vg_dmalloc(sb);
+        int64_t total = 0;
+        int rc = vgk_join_probe_count(&j->B.jt, pk, nk, j->B.conv, db.n_rows, db.d_sel, db.sel_n,
+                                      j->jn.kind, scratch, sb, &total, vg_stream());
+        if (rc) { vg_dfree(scratch); vg_dbatch_release(&db); vg_check_rc(rc, "join probe"); }
+        if (total == 0) { vg_dfree(scratch); vg_dbatch_release(&db); continue; }
+        int32_t *pairs = (int32_t *)vg_dmalloc((size_t)total * 8 + 16);
+        int32_t *op = pairs, *ob = semi ? NULL : pairs + total;
+        rc = vgk_join_probe_emit(&j->B.jt, db.n_rows, db.d_sel, db.sel_n, j->jn.kind, scratch, sb, op, ob,
+                                 j->d_matched, vg_stream());
+        vg_dfree(scratch);
+        if (rc) { vg_dfree(pairs); vg_dbatch_release(&db); vg_check_rc(rc, "join emit"); }
+        VecBatch *out;
+        if (semi) {
+            /* the probe batch itself, with the kept rows as its selection */
+            out = db.host;
+            int32_t *sel = (int32_t *)vg_xmalloc((size_t)total * 4);
+            vg_d2h(sel, op, (size_t)total * 4);
+            vg_sync();
+            free(out->sel);
+            out->sel = sel;
+            out->sel_n = (int32_t)total;
+            db.host = NULL;
+        } else {
+            int oc = j->jn.base.output_schema.n_cols;
+            out = vg_batch_alloc(oc, total);
+            size_t wb = (size_t)((total + 31) / 32) * 4;
+            size_t per = a256((size_t)total * 8) + a256(wb);
+            char *blk = (char *)vg_dmalloc(per * (size_t)oc + 256);
+            for (int c = 0; c < oc; c++) {
+                char *dv = blk + per * (size_t)c;
+                uint32_t *dm = (uint32_t *)(dv + a256((size_t)total * 8));
+                const VgCol *src;
+                const int32_t *idx;
+                if (c < nl) { src = &db.cols[c]; idx = op; }
+                else { src = &j->B.bcols[j->r_nonkey[c - nl]]; idx = ob; }
+                vg_check_rc(vgk_gather(src, idx, total, 1, dv, dm, vg_stream()), "join gather");
+                out->columns[c] = vg_download_column(src->type, dv, dm, total);
+                out->col_names[c] = vg_xstrdup(j->jn.base.output_schema.col_names[c]);
+            }
+            vg_sync();
+            vg_dfree(blk);
+        }
+        vg_dfree(pairs);
+        vg_dbatch_release(&db);
+        free(need);
+        return out;
+    }
+}
+
+static VecBatch *finalize_one(VgJoin *j) {
+    if (!j->d_unmatched) {
+        j->d_unmatched = (int32_t *)vg_dmalloc((size_t)(j->n_build > 0 ? j->n_build : 1) * 4);
+        size_t sb = vgk_join_probe_scratch_bytes(j->n_build);
+        void *scratch = vg_dmalloc(sb);
+        int rc = vgk_join_unmatched_build(j->d_matched, j->n_build, j->d_unmatched, &j->n_unmatched, scratch, sb,
+                                          vg_stream());
+        vg_dfree(scratch);
+        vg_check_rc(rc, "join finalize");
+        j->fin_cursor = 0;
+    }
+    int64_t left = j->n_unmatched - j->fin_cursor;
+    if (left <= 0) return NULL;
+    int64_t n = left < 65536 ? left : 65536;
+    const int32_t *idx = j->d_unmatched + j->fin_cursor;
+    j->fin_cursor += n;
+    const VecSchema *ls = &j->jn.left->output_schema;
+    int nl = ls->n_cols, oc = j->jn.base.output_schema.n_cols;
+    VecBatch *out = vg_batch_alloc(oc, n);
+    size_t wb = (size_t)((n + 31) / 32) * 4;
+    size_t per = a256((size_t)n * 8) + a256(wb);
+    char *blk = (char *)vg_dmalloc(per * (size_t)oc + 256);
+    for (int c = 0; c < oc; c++) {
+        char *dv = blk + per * (size_t)c;
+        uint32_t *dm = (uint32_t *)(dv + a256((size_t)n * 8));
+        out->col_names[c] = vg_xstrdup(j->jn.base.output_schema.col_names[c]);
+        if (c < nl) {
+            int rk = -1;
+            for (int k = 0; k < j->jn.n_keys; k++)
+                if (j->jn.keys[k].left_col == c) { rk = j->jn.keys[k].right_col; break; }
+            if (rk < 0) {   /* non-key left column: NA */
+                VecArray a;
+                memset(&a, 0, sizeof(a));
+                a.type = ls->col_types[c];
+                a.length = n;
+                a.owns_data = 1;
+                a.validity = (uint8_t *)vg_xcalloc((size_t)vg_vbytes(n), 1);
+                a.buf.i64 = (int64_t *)vg_xcalloc((size_t)n * elem(a.type) + 1, 1);
+                out->columns[c] = a;
+                continue;
+            }
+            vg_check_rc(vgk_gather(&j->B.bcols[rk], idx, n, 0, dv, dm, vg_stream()), "join finalize gather");
+            out->columns[c] = vg_download_column(ls->col_types[c], dv, dm, n);
+        } else {
+            const VgCol *src = &j->B.bcols[j->r_nonkey[c - nl]];
+            vg_check_rc(vgk_gather(src, idx, n, 0, dv, dm, vg_stream()), "join finalize gather");
+            out->columns[c] = vg_download_column(src->type, dv, dm, n);
+        }
+    }
+    vg_sync();
+    vg_dfree(blk);
+    return out;
+}
+
+static VecBatch *join_next(VecNode *self) {
+    VgJoin *j = (VgJoin *)self;
+    if (j->state == 0) { join_build(j); j->state = 1; }
+    if (j->state == 1) {
+        VecBatch *b = probe_one(j);
+        if (b) return b;
+        j->state = (j->jn.kind == JOIN_FULL) ? 2 : 3;
+    }
+    if (j->state == 2) {
+        VecBatch *b = finalize_one(j);
+        if (b) return b;
+        j->state = 3;
+    }
+    return NULL;
+}
+
+static void join_free(VecNode *self) {
+    VgJoin *j = (VgJoin *)self;
+    j->jn.left->free_node(j->jn.left);
+    j->jn.right->free_node(j->jn.right);
+    free(j->jn.keys);
+    free(j->jn.suffix_x);
+    free(j->jn.suffix_y);
+    free(j->r_nonkey);
+    free(j->B.bcols);
+    vg_dfree(j->build_block);
+    vg_dfree(j->table_block);
+    vg_dfree(j->d_matched);
+    vg_dfree(j->d_unmatched);
+    vg_schema_free(&j->jn.base.output_schema);
+    free(j);
+}
+
+static const char *type_name(int t) {
+    switch (t) {
+    case VEC_INT64: return "int64";
+    case VEC_DOUBLE: return "double";
+    case VEC_BOOL: return "bool";
+    default: return "string";
+    }
+}
+
+JoinNode *join_node_create(VecNode *left, VecNode *right, JoinKind kind, int n_keys, JoinKey *keys,
+                           const char *suffix_x, const char *suffix_y) {
+    static const char *kind_names[] = {"inner_join", "left_join", "full_join", "semi_join", "anti_join"};
+    vg_ensure_init();
+    const VecSchema *ls = &left->output_schema, *rs = &right->output_schema;
+    if (n_keys < 1 || n_keys > VG_MAX_KEYS) vg_fail("GPU join supports 1 to %d key columns", VG_MAX_KEYS);
+    for (int k = 0; k < n_keys; k++) {
+        int lt = ls->col_types[keys[k].left_col], rt = rs->col_types[keys[k].right_col];
+        if (lt != rt && (lt == VEC_STRING || rt == VEC_STRING))
+            vg_fail("%s key type mismatch: x.%s (%s) vs y.%s (%s)", kind_names[kind],
+                    ls->col_names[keys[k].left_col], type_name(lt), rs->col_names[keys[k].right_col],
+                    type_name(rt));
+        if (lt == VEC_STRING)
+            vg_fail("string join keys are not supported by the GPU join (%s)", ls->col_names[keys[k].left_col]);
+        if (kind == JOIN_FULL && lt != rt)
+            vg_fail("full_join with key columns of different types (x.%s %s, y.%s %s) is not supported by the GPU join",
+                    ls->col_names[keys[k].left_col], type_name(lt), rs->col_names[keys[k].right_col], type_name(rt));
+    }
+    VgJoin *j = (VgJoin *)vg_xcalloc(1, sizeof(VgJoin));
+    j->jn.left = left;
+    j->jn.right = right;
+    j->jn.kind = kind;
+    j->jn.n_keys = n_keys;
+    j->jn.keys = keys;
+    j->jn.suffix_x = vg_xstrdup(suffix_x);
+    j->jn.suffix_y = vg_xstrdup(suffix_y);
+    j->B.n_keys = n_keys;
+    j->B.kind = kind;
+    for (int k = 0; k < n_keys; k++) {
+        int lt = ls->col_types[keys[k].left_col], rt = rs->col_types[keys[k].right_col];
+        int c = common_type(lt, rt);
+        j->key_type[k] = c;
+        j->conv_build[k] = (rt != c && c == VEC_DOUBLE);
+        j->B.conv[k] = (lt != c && c == VEC_DOUBLE);
+        j->B.lkey[k] = keys[k].left_col;
+    }
+    /* output schema (src/join.c:703-784) */
+    int *is_rkey = (int *)vg_xcalloc((size_t)(rs->n_cols ? rs->n_cols : 1), sizeof(int));
+    for (int k = 0; k < n_keys; k++) is_rkey[keys[k].right_col] = 1;
+    j->r_nonkey = (int *)vg_xcalloc((size_t)(rs->n_cols ? rs->n_cols : 1), sizeof(int));
+    if (kind == JOIN_INNER || kind == JOIN_LEFT || kind == JOIN_FULL)
+        for (int c = 0; c < rs->n_cols; c++)
+            if (!is_rkey[c]) j->r_nonkey[j->r_nonkey_n++] = c;
+    int on = ls->n_cols + j->r_nonkey_n;
+    char **names = (char **)vg_xcalloc((size_t)(on ? on : 1), sizeof(char *));
+    VecType *types = (VecType *)vg_xcalloc((size_t)(on ? on : 1), sizeof(VecType));
+    for (int i = 0; i < ls->n_cols; i++) { names[i] = vg_xstrdup(ls->col_names[i]); types[i] = ls->col_types[i]; }
+    for (int q = 0; q < j->r_nonkey_n; q++) {
+        int c = j->r_nonkey[q];
+        const char *rn = rs->col_names[c];
+        int coll = vg_schema_find(ls, rn);
+        if (coll >= 0) {
+            size_t l1 = strlen(rn) + strlen(suffix_y) + 1;
+            names[ls->n_cols + q] = (char *)vg_xmalloc(l1);
+            snprintf(names[ls->n_cols + q], l1, "%s%s", rn, suffix_y);
+            size_t l2 = strlen(ls->col_names[coll]) + strlen(suffix_x) + 1;
+            free(names[coll]);
+            names[coll] = (char *)vg_xmalloc(l2);
+            snprintf(names[coll], l2, "%s%s", ls->col_names[coll], suffix_x);
+        } else {
+            names[ls->n_cols + q] = vg_xstrdup(rn);
+        }
+        types[ls->n_cols + q] = rs->col_types[c];
+    }
+    j->jn.base.output_schema = vg_schema_make(on, names, types);
+    for (int i = 0; i < on; i++) free(names[i]);
+    free(names);
+    free(types);
+    free(is_rkey);
+    j->jn.base.next_batch = join_next;
+    j->jn.base.free_node = join_free;
+    j->jn.base.kind = "JoinNode";
+    return (JoinNode *)&j->jn;
+}

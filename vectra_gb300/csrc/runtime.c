@@ -1,0 +1,389 @@
+/*
+ * runtime.c -- libvgpu runtime: errors, device memory and stream, host
+ * batch helpers, and moving batches between host and device.
+ */
+#define _GNU_SOURCE
+#include <setjmp.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <cuda_runtime_api.h>
+
+#include "vg_host.h"
+
+extern unsigned long long vg_launch_counter;
+
+/* ------------------------------------------------------------------ */
+/* errors                                                              */
+/* ------------------------------------------------------------------ */
+
+static char g_msg[1024];
+static jmp_buf *g_jmp = NULL;
+static long g_warnings = 0;
+
+const char *vgpu_last_error(void) { return g_msg; }
+long vgpu_warning_count(void) { return g_warnings; }
+void vg_warn_count(long n) { g_warnings += n; }
+unsigned long long vgpu_kernel_launches(void) { return vg_launch_counter; }
+
+/* The reference engine's error entry point (src/error.c:4-11).  When libvgpu
+ * is linked into the vectra package, the engine's own definition (which
+ * raises an R error) takes precedence over this weak one. */
+__attribute__((weak)) void vectra_error(const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    snprintf(g_msg, sizeof(g_msg), "%s", buf);
+    if (g_jmp) longjmp(*g_jmp, 1);
+    fprintf(stderr, "libvgpu: %s\n", g_msg);
+    abort();
+}
+
+void vg_fail(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_msg, sizeof(g_msg), fmt, ap);
+    va_end(ap);
+    vectra_error("%s", g_msg);
+    abort();   /* vectra_error does not return */
+}
+
+const char *vgk_last_cuda_error(void);
+const char *vgk_agg_last_error(void);
+const char *vgk_join_last_error(void);
+const char *vgk_sort_last_error(void);
+
+void vg_check_rc(int rc, const char *what) {
+    if (rc == 0) return;
+    const char *m = vgk_last_cuda_error();
+    if (!m || !*m) m = vgk_agg_last_error();
+    if (!m || !*m) m = vgk_join_last_error();
+    if (!m || !*m) m = vgk_sort_last_error();
+    vg_fail("%s failed: %s", what, (m && *m) ? m : "unknown device error");
+}
+
+/* ------------------------------------------------------------------ */
+/* device, stream, memory                                              */
+/* ------------------------------------------------------------------ */
+
+static int g_inited = 0;
+static cudaStream_t g_own_stream = NULL;
+static cudaStream_t g_user_stream = NULL;
+static int g_use_user = 0;
+
+int vgpu_init(int device) {
+    if (g_inited) return 0;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+        snprintf(g_msg, sizeof(g_msg), "libvgpu: no CUDA device available");
+        return -1;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) {
+        snprintf(g_msg, sizeof(g_msg), "libvgpu: cannot select device %d", device);
+        return -1;
+    }
+    struct cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, device) == cudaSuccess && p.major < 10) {
+        snprintf(g_msg, sizeof(g_msg), "libvgpu: device %d is sm_%d%d; sm_103 required",
+                 device, p.major, p.minor);
+        return -1;
+    }
+    if (cudaStreamCreateWithFlags(&g_own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        snprintf(g_msg, sizeof(g_msg), "libvgpu: stream creation failed");
+        return -1;
+    }
+    /* keep freed device memory cached in the default pool */
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    g_inited = 1;
+    return 0;
+}
+
+void vg_ensure_init(void) {
+    if (!g_inited && vgpu_init(0) != 0) vg_fail("%s", g_msg);
+}
+
+void vgpu_set_stream(void *s) {
+    g_user_stream = (cudaStream_t)s;
+    g_use_user = (s != NULL);
+}
+
+void *vgpu_get_stream(void) { return (void *)vg_stream(); }
+
+vg_stream_t vg_stream(void) {
+    vg_ensure_init();
+    return (vg_stream_t)(g_use_user ? g_user_stream : g_own_stream);
+}
+
+int vgpu_synchronize(void) {
+    if (!g_inited) return 0;
+    return cudaStreamSynchronize((cudaStream_t)vg_stream()) == cudaSuccess ? 0 : -1;
+}
+
+void *vg_dmalloc(size_t bytes) {
+    void *p = NULL;
+    if (bytes == 0) bytes = 256;
+    cudaError_t e = cudaMallocAsync(&p, bytes, (cudaStream_t)vg_stream());
+    if (e != cudaSuccess) vg_fail("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    return p;
+}
+
+void vg_dfree(void *p) {
+    if (p) cudaFreeAsync(p, (cudaStream_t)vg_stream());
+}
+
+void vg_h2d(void *dst, const void *src, size_t bytes) {
+    if (!bytes) return;
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)vg_stream());
+    if (e != cudaSuccess) vg_fail("host to device copy failed: %s", cudaGetErrorString(e));
+}
+
+void vg_d2h(void *dst, const void *src, size_t bytes) {
+    if (!bytes) return;
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)vg_stream());
+    if (e != cudaSuccess) vg_fail("device to host copy failed: %s", cudaGetErrorString(e));
+}
+
+void vg_dmemset(void *dst, int v, size_t bytes) {
+    if (!bytes) return;
+    cudaError_t e = cudaMemsetAsync(dst, v, bytes, (cudaStream_t)vg_stream());
+    if (e != cudaSuccess) vg_fail("device memset failed: %s", cudaGetErrorString(e));
+}
+
+void vg_sync(void) {
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)vg_stream());
+    if (e != cudaSuccess) vg_fail("device execution failed: %s", cudaGetErrorString(e));
+}
+
+/* ------------------------------------------------------------------ */
+/* host memory, batches, schemas                                       */
+/* ------------------------------------------------------------------ */
+
+void *vg_xmalloc(size_t n) {
+    void *p = malloc(n ? n : 1);
+    if (!p) vg_fail("host allocation of %zu bytes failed", n);
+    return p;
+}
+void *vg_xcalloc(size_t n, size_t s) {
+    void *p = calloc(n ? n : 1, s ? s : 1);
+    if (!p) vg_fail("host allocation failed");
+    return p;
+}
+char *vg_xstrdup(const char *s) {
+    size_t n = strlen(s) + 1;
+    char *p = (char *)vg_xmalloc(n);
+    memcpy(p, s, n);
+    return p;
+}
+
+VecBatch *vg_batch_alloc(int n_cols, int64_t n_rows) {
+    VecBatch *b = (VecBatch *)vg_xcalloc(1, sizeof(VecBatch));
+    b->n_cols = n_cols;
+    b->n_rows = n_rows;
+    b->columns = (VecArray *)vg_xcalloc((size_t)n_cols, sizeof(VecArray));
+    b->col_names = (char **)vg_xcalloc((size_t)n_cols, sizeof(char *));
+    return b;
+}
+
+/* frees a batch exactly as the reference's vec_batch_free does
+ * (src/batch.c:19-29, src/array.c:41-58) */
+void vg_batch_free(VecBatch *b) {
+    if (!b) return;
+    for (int i = 0; i < b->n_cols; i++) {
+        VecArray *a = &b->columns[i];
+        free(a->validity);
+        switch (a->type) {
+        case VEC_INT64: free(a->buf.i64); break;
+        case VEC_DOUBLE: free(a->buf.dbl); break;
+        case VEC_BOOL: free(a->buf.bln); break;
+        case VEC_STRING:
+            free(a->buf.str.offsets);
+            if (a->owns_data) free(a->buf.str.data);
+            break;
+        }
+        free(b->col_names[i]);
+    }
+    free(b->columns);
+    free(b->col_names);
+    free(b->sel);
+    free(b);
+}
+
+void vgpu_batch_free(VecBatch *b) { vg_batch_free(b); }
+
+VecSchema vg_schema_make(int n, char *const *names, const VecType *types) {
+    VecSchema s;
+    s.n_cols = n;
+    s.col_names = (char **)vg_xcalloc((size_t)n, sizeof(char *));
+    s.col_types = (VecType *)vg_xcalloc((size_t)n, sizeof(VecType));
+    s.col_annotations = (char **)vg_xcalloc((size_t)n, sizeof(char *));
+    for (int i = 0; i < n; i++) {
+        s.col_names[i] = vg_xstrdup(names[i]);
+        s.col_types[i] = types[i];
+    }
+    return s;
+}
+
+VecSchema vg_schema_copy(const VecSchema *src) {
+    VecSchema s = vg_schema_make(src->n_cols, src->col_names, src->col_types);
+    for (int i = 0; i < src->n_cols; i++)
+        if (src->col_annotations && src->col_annotations[i])
+            s.col_annotations[i] = vg_xstrdup(src->col_annotations[i]);
+    return s;
+}
+
+void vg_schema_free(VecSchema *s) {
+    for (int i = 0; i < s->n_cols; i++) {
+        free(s->col_names[i]);
+        if (s->col_annotations) free(s->col_annotations[i]);
+    }
+    free(s->col_names);
+    free(s->col_types);
+    free(s->col_annotations);
+    memset(s, 0, sizeof(*s));
+}
+
+int vg_schema_find(const VecSchema *s, const char *name) {
+    for (int i = 0; i < s->n_cols; i++)
+        if (strcmp(s->col_names[i], name) == 0) return i;
+    return -1;
+}
+
+/* ------------------------------------------------------------------ */
+/* host <-> device batches                                             */
+/* ------------------------------------------------------------------ */
+
+static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static size_t value_bytes(int type, int64_t n) {
+    return (size_t)n * (type == VEC_BOOL ? 1 : 8);
+}
+static size_t valid_bytes_dev(int64_t n) { return (size_t)((n + 31) / 32) * 4; }
+
+int vg_pull(VecNode *child, const uint8_t *need, int keep_host, VgDBatch *out) {
+    memset(out, 0, sizeof(*out));
+    if (vg_is_table_source(child) && !keep_host) return vg_source_pull(child, need, out);
+    VecBatch *b = child->next_batch(child);
+    if (!b) return 0;
+    int64_t n = b->n_rows;
+    out->n_rows = n;
+    out->n_cols = b->n_cols;
+    out->cols = (VgCol *)vg_xcalloc((size_t)b->n_cols, sizeof(VgCol));
+    size_t total = 0;
+    for (int c = 0; c < b->n_cols; c++) {
+        if (!need || !need[c]) continue;
+        if (b->columns[c].type == VEC_STRING)
+            vg_fail("string column '%s' is not supported by the GPU path", b->col_names[c]);
+        total += a256(value_bytes(b->columns[c].type, n)) + a256(valid_bytes_dev(n));
+    }
+    if (b->sel) total += a256((size_t)b->sel_n * 4);
+    char *blk = total ? (char *)vg_dmalloc(total) : NULL;
+    out->block = blk;
+    size_t off = 0;
+    for (int c = 0; c < b->n_cols; c++) {
+        VecArray *a = &b->columns[c];
+        out->cols[c].type = a->type;
+        if (!need || !need[c]) continue;
+        char *dv = blk + off;
+        off += a256(value_bytes(a->type, n));
+        vg_h2d(dv, a->type == VEC_BOOL ? (void *)a->buf.bln : (void *)a->buf.i64, value_bytes(a->type, n));
+        out->cols[c].data = dv;
+        if (a->validity) {
+            char *dm = blk + off;
+            off += a256(valid_bytes_dev(n));
+            if (vg_vbytes(n) & 3) vg_dmemset(dm + (vg_vbytes(n) & ~(int64_t)3), 0, 4);
+            vg_h2d(dm, a->validity, (size_t)vg_vbytes(n));
+            out->cols[c].valid = (const uint32_t *)dm;
+        } else {
+            off += a256(valid_bytes_dev(n));
+        }
+    }
+    if (b->sel) {
+        int32_t *ds = (int32_t *)(blk + off);
+        vg_h2d(ds, b->sel, (size_t)b->sel_n * 4);
+        out->d_sel = ds;
+        out->sel_n = b->sel_n;
+    }
+    if (keep_host) {
+        out->host = b;
+    } else {
+        vg_sync();
+        vg_batch_free(b);
+    }
+    return 1;
+}
+
+void vg_dbatch_release(VgDBatch *b) {
+    if (b->block) vg_dfree(b->block);
+    if (b->host) vg_batch_free(b->host);
+    free(b->cols);
+    memset(b, 0, sizeof(*b));
+}
+
+VecArray vg_download_column(int type, const void *d_data, const uint32_t *d_valid, int64_t n) {
+    VecArray a;
+    memset(&a, 0, sizeof(a));
+    a.type = (VecType)type;
+    a.length = n;
+    a.owns_data = 1;
+    a.validity = (uint8_t *)vg_xcalloc((size_t)vg_vbytes(n), 1);
+    size_t vb = value_bytes(type, n);
+    void *dst = vg_xcalloc(vb ? vb : 1, 1);
+    if (type == VEC_BOOL) a.buf.bln = (uint8_t *)dst;
+    else a.buf.i64 = (int64_t *)dst;
+    if (n > 0) {
+        vg_d2h(dst, d_data, vb);
+        if (d_valid) vg_d2h(a.validity, d_valid, (size_t)vg_vbytes(n));
+        else memset(a.validity, 0xFF, (size_t)vg_vbytes(n));
+    }
+    return a;
+}
+
+/* ------------------------------------------------------------------ */
+/* guarded entry points                                                */
+/* ------------------------------------------------------------------ */
+
+#define GUARD_BEGIN(T)                                        \
+    jmp_buf jb; jmp_buf *prev = g_jmp; g_msg[0] = 0;          \
+    if (setjmp(jb)) { g_jmp = prev; return (T)NULL; }         \
+    g_jmp = &jb;
+#define GUARD_END g_jmp = prev;
+
+VecBatch *vgpu_guard_next_batch(VecNode *node) {
+    GUARD_BEGIN(VecBatch *)
+    VecBatch *b = node->next_batch(node);
+    GUARD_END
+    return b;
+}
+FilterNode *vgpu_guard_filter(VecNode *child, VecExpr *pred) {
+    GUARD_BEGIN(FilterNode *)
+    FilterNode *r = filter_node_create(child, pred);
+    GUARD_END
+    return r;
+}
+ProjectNode *vgpu_guard_project(VecNode *child, int n, ProjEntry *entries) {
+    GUARD_BEGIN(ProjectNode *)
+    ProjectNode *r = project_node_create(child, n, entries);
+    GUARD_END
+    return r;
+}
+GroupAggNode *vgpu_guard_group_agg(VecNode *child, int n_keys, char **key_names, int n_aggs,
+                                   AggSpec *specs, const char *temp_dir) {
+    GUARD_BEGIN(GroupAggNode *)
+    GroupAggNode *r = group_agg_node_create(child, n_keys, key_names, n_aggs, specs, temp_dir);
+    GUARD_END
+    return r;
+}
+JoinNode *vgpu_guard_join(VecNode *l, VecNode *r, JoinKind kind, int n_keys, JoinKey *keys,
+                          const char *sx, const char *sy) {
+    GUARD_BEGIN(JoinNode *)
+    JoinNode *j = join_node_create(l, r, kind, n_keys, keys, sx, sy);
+    GUARD_END
+    return j;
+}

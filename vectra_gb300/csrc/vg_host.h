@@ -1,0 +1,126 @@
+/*
+ * vg_host.h -- internal declarations of libvgpu's C11 host layer.
+ */
+#ifndef VG_HOST_H
+#define VG_HOST_H
+
+#include <stdint.h>
+#include <stddef.h>
+#include "vgpu.h"
+#include "vgpu_internal.h"
+
+/* ---- errors ---- */
+/* Records the message and raises it through vectra_error (no return). */
+void vg_fail(const char *fmt, ...);
+void vg_warn_count(long n);
+/* Fails with the last kernel-side message if rc != 0. */
+void vg_check_rc(int rc, const char *what);
+
+/* ---- device memory / stream ---- */
+void vg_ensure_init(void);
+vg_stream_t vg_stream(void);
+void *vg_dmalloc(size_t bytes);          /* stream-ordered, fails loudly */
+void vg_dfree(void *p);
+void vg_h2d(void *dst, const void *src, size_t bytes);
+void vg_d2h(void *dst, const void *src, size_t bytes);
+void vg_dmemset(void *dst, int v, size_t bytes);
+void vg_sync(void);
+
+/* ---- host batches ---- */
+void *vg_xmalloc(size_t n);
+void *vg_xcalloc(size_t n, size_t s);
+char *vg_xstrdup(const char *s);
+VecBatch *vg_batch_alloc(int n_cols, int64_t n_rows);
+void vg_batch_free(VecBatch *b);
+VecSchema vg_schema_make(int n, char *const *names, const VecType *types);
+VecSchema vg_schema_copy(const VecSchema *s);
+void vg_schema_free(VecSchema *s);
+int vg_schema_find(const VecSchema *s, const char *name);
+static inline int64_t vg_vbytes(int64_t n) { return (n + 7) / 8; }
+
+/* ---- device batches ---- */
+/* A batch whose needed columns are resident on the device. */
+typedef struct {
+    int64_t n_rows;            /* physical rows */
+    int n_cols;
+    VgCol *cols;               /* n_cols entries; data == NULL if not present */
+    const int32_t *d_sel;      /* device selection vector or NULL */
+    int64_t sel_n;
+    VecBatch *host;            /* the host batch it came from (owned) or NULL */
+    void *block;               /* device allocation holding uploaded data */
+    int64_t row_base;          /* stream position of physical row 0 */
+} VgDBatch;
+
+/* Pulls the next batch of `child` with the columns flagged in need[]
+ * resident on the device.  Returns 0 at end of stream.  keep_host: keep the
+ * host batch in out->host (otherwise it is freed after the upload). */
+int vg_pull(VecNode *child, const uint8_t *need, int keep_host, VgDBatch *out);
+void vg_dbatch_release(VgDBatch *b);
+
+/* Device column -> newly malloc'd host VecArray of n values. */
+VecArray vg_download_column(int type, const void *d_data, const uint32_t *d_valid, int64_t n);
+
+/* ---- table source (source.c) ---- */
+int vg_is_table_source(const VecNode *n);
+int vg_source_pull(VecNode *n, const uint8_t *need, VgDBatch *out);
+
+/* ---- expression compilation (compile.c) ---- */
+/* Column lookup: returns the index of `name` in the launch's column table
+ * (uploading it on demand) or -1 if unknown. */
+typedef int (*vg_colmap_fn)(void *ctx, const char *name, int *type);
+/* 1 if expr is a conjunction of column-vs-constant terms (filled into out),
+ * 0 if it needs the general program, -1 on error (message set). */
+int vg_compile_pred(const VecExpr *e, vg_colmap_fn map, void *ctx, VgPred *out);
+/* general program; returns 0 or -1 (message set) */
+int vg_compile_prog(const VecExpr *e, vg_colmap_fn map, void *ctx, VgProg *out);
+/* a value for fused kernels: a column, a literal, or a binary arithmetic of
+ * those; returns 1 if representable, 0 if not, -1 on error. */
+int vg_compile_value(const VecExpr *e, vg_colmap_fn map, void *ctx, int side, VgValue *out);
+const char *vg_compile_error(void);
+/* reference type of an expression (src/r_bridge.c parse rules) */
+int vg_expr_type(const VecExpr *e);
+/* frees an expression tree allocated with malloc (src/expr.c:16-27) */
+void vg_expr_free(VecExpr *e);
+/* 1 if the expression mentions column `name` */
+int vg_expr_refs(const VecExpr *e, const char *name);
+
+/* ---- compact column tables for kernels (at most VG_MAX_COLS) ---- */
+typedef struct { int n; int idx[VG_MAX_COLS]; } VgColSet;
+/* index of column i in the set, adding it if new; -1 if the set is full */
+static inline int vg_colset_add(VgColSet *s, int i) {
+    for (int j = 0; j < s->n; j++) if (s->idx[j] == i) return j;
+    if (s->n >= VG_MAX_COLS) return -1;
+    s->idx[s->n] = i;
+    return s->n++;
+}
+
+/* ---- node identification ---- */
+int vg_is_filter(const VecNode *n);
+int vg_is_project(const VecNode *n);
+int vg_is_join(const VecNode *n);
+
+/* filter internals used by fusion */
+const VgPred *vg_filter_cnf(VecNode *n, VecNode **child_out, const VgColSet **set);
+/* project internals: the expression producing column `name`, or NULL if it
+ * is a pass-through (then *pass_name is the child column name) */
+int vg_project_lookup(VecNode *n, const char *name, const VecExpr **expr, const char **pass_name);
+VecNode *vg_project_child(VecNode *n);
+
+/* join internals used by the fused aggregation */
+typedef struct {
+    VgJoinTable jt;
+    int n_keys;
+    int32_t lkey[VG_MAX_KEYS];       /* probe-side key columns */
+    int32_t conv[VG_MAX_KEYS];       /* probe key int/bool -> double */
+    VgCol *bcols;                    /* device build columns (all right columns) */
+    int n_bcols;
+    int kind;
+} VgJoinBuilt;
+const VgJoinBuilt *vg_join_build_now(VecNode *n);
+VecNode *vg_join_left(VecNode *n);
+int vg_join_kind(VecNode *n);
+/* resolves an output column name of the join: side 0 = left column index,
+ * side 1 = right column index; returns 0 if not found */
+int vg_join_resolve(VecNode *n, const char *name, int *side, int *col);
+
+#endif

@@ -167,6 +167,11 @@ typedef struct {
  * (double -0 folded to +0) plus a per-slot NA mask. */
 #define VG_LACC_WORDS 66     /* 32-bit digits of a full-range double sum */
 
+/* kernel error bits (group / join tables) */
+#define VG_ERR_WAIT   1u     /* a bounded wait expired */
+#define VG_ERR_FULL   2u     /* a table or spill list was full */
+#define VG_ERR_PROG   4u     /* malformed expression program */
+
 typedef struct {
     int64_t   cap;           /* power of two */
     uint32_t *state;
@@ -266,6 +271,11 @@ int vgk_eval_prog(const VgCol *cols, int n_cols, const VgProg *prog,
 int vgk_gather(const VgCol *col, const int32_t *d_idx, int64_t n_out,
                int null_if_negative, void *d_out, uint32_t *d_out_valid,
                vg_stream_t s);
+
+/* gather n values into rows [row0, row0+n) of an existing column whose
+ * validity words are zeroed beforehand (any row0; bits are OR-ed in) */
+int vgk_gather_into(const VgCol *col, const int32_t *d_idx, int64_t n, void *d_out,
+                    uint32_t *d_out_valid, int64_t row0, vg_stream_t s);
 
 /* group table */
 int vgk_group_table_init(VgGroupTable *gt, int n_keys, const int32_t *acc_cls,
