@@ -25,6 +25,7 @@ void vg_prof_end(int cls, cudaStream_t s);
 // ---------------------------------------------------------------------
 
 VG_DEV bool vg_valid(const VgCol &c, int64_t r) {
+    r += c.voff;
     return c.valid == nullptr || ((__ldg(c.valid + (r >> 5)) >> (r & 31)) & 1u);
 }
 

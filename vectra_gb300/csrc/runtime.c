@@ -42,6 +42,13 @@ __attribute__((weak)) void vectra_error(const char *fmt, ...) {
     abort();
 }
 
+void vg_set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_msg, sizeof(g_msg), fmt, ap);
+    va_end(ap);
+}
+
 void vg_fail(const char *fmt, ...) {
     va_list ap;
     va_start(ap, fmt);

@@ -27,6 +27,19 @@ int vg_is_table_source(const VecNode *n) { return n && n->next_batch == source_n
 
 static size_t elem(int type) { return type == VEC_BOOL ? 1 : 8; }
 
+/* dst bits [0, n) = src bits [off, off + n) (reference bitmap order) */
+static void copy_bits(uint8_t *dst, const uint8_t *src, int64_t off, int64_t n) {
+    if ((off & 7) == 0) {
+        memcpy(dst, src + off / 8, (size_t)vg_vbytes(n));
+        return;
+    }
+    memset(dst, 0, (size_t)vg_vbytes(n));
+    for (int64_t i = 0; i < n; i++) {
+        int64_t s = off + i;
+        if ((src[s >> 3] >> (s & 7)) & 1) dst[i >> 3] |= (uint8_t)(1u << (i & 7));
+    }
+}
+
 static VecBatch *source_next(VecNode *self) {
     VgSource *s = (VgSource *)self;
     if (s->cursor >= s->n_rows) return NULL;
@@ -44,14 +57,21 @@ static VecBatch *source_next(VecNode *self) {
         void *v = vg_xcalloc((size_t)n * elem(a.type) + 1, 1);
         if (a.type == VEC_BOOL) a.buf.bln = (uint8_t *)v; else a.buf.i64 = (int64_t *)v;
         const char *src = (const char *)s->data[c] + (size_t)lo * elem(a.type);
-        const uint8_t *vsrc = s->validity[c] ? s->validity[c] + lo / 8 : NULL;
+        const uint8_t *vsrc = s->validity[c];
         if (s->flags & VGPU_SRC_DEVICE) {
             vg_d2h(v, src, (size_t)n * elem(a.type));
-            if (vsrc) vg_d2h(a.validity, vsrc, (size_t)vg_vbytes(n));
+            if (vsrc) {
+                int64_t b0 = lo / 8, nb = (lo + n + 7) / 8 - b0;
+                uint8_t *tmp = (uint8_t *)vg_xmalloc((size_t)nb);
+                vg_d2h(tmp, vsrc + b0, (size_t)nb);
+                vg_sync();
+                copy_bits(a.validity, tmp, lo & 7, n);
+                free(tmp);
+            }
             vg_sync();
         } else {
             memcpy(v, src, (size_t)n * elem(a.type));
-            if (vsrc) memcpy(a.validity, vsrc, (size_t)vg_vbytes(n));
+            if (vsrc) copy_bits(a.validity, vsrc, lo, n);
         }
         if (!vsrc) memset(a.validity, 0xFF, (size_t)vg_vbytes(n));
         /* bits past the last row stay clear */
@@ -74,10 +94,13 @@ int vg_source_pull(VecNode *n, const uint8_t *need, VgDBatch *out) {
     out->row_base = lo;
     out->cols = (VgCol *)vg_xcalloc((size_t)s->n_cols, sizeof(VgCol));
     if (s->flags & VGPU_SRC_DEVICE) {
+        /* in place; validity bitmaps are 4-byte aligned, row lo sits at bit
+         * lo%32 of word lo/32 */
         for (int c = 0; c < s->n_cols; c++) {
             out->cols[c].type = s->types[c];
             out->cols[c].data = (const char *)s->data[c] + (size_t)lo * elem(s->types[c]);
-            out->cols[c].valid = s->validity[c] ? (const uint32_t *)(s->validity[c] + lo / 8) : NULL;
+            out->cols[c].valid = s->validity[c] ? (const uint32_t *)(s->validity[c] + (lo >> 5) * 4) : NULL;
+            out->cols[c].voff = (int32_t)(lo & 31);
         }
         return 1;
     }
@@ -85,7 +108,7 @@ int vg_source_pull(VecNode *n, const uint8_t *need, VgDBatch *out) {
     for (int c = 0; c < s->n_cols; c++)
         if (!need || need[c])
             total += (((size_t)rows * elem(s->types[c]) + 255) & ~(size_t)255) +
-                     ((((size_t)(rows + 31) / 32) * 4 + 255) & ~(size_t)255);
+                     ((((size_t)(rows + 31) / 32) * 4 + 4 + 255) & ~(size_t)255);
     char *blk = total ? (char *)vg_dmalloc(total) : NULL;
     out->block = blk;
     size_t off = 0;
@@ -97,13 +120,18 @@ int vg_source_pull(VecNode *n, const uint8_t *need, VgDBatch *out) {
         off += (vb + 255) & ~(size_t)255;
         vg_h2d(dv, (const char *)s->data[c] + (size_t)lo * elem(s->types[c]), vb);
         out->cols[c].data = dv;
-        size_t wb = ((size_t)(rows + 31) / 32) * 4;
+        size_t wb = ((size_t)(rows + 31) / 32) * 4 + 4;
         char *dm = blk + off;
         off += (wb + 255) & ~(size_t)255;
         if (s->validity[c]) {
-            if (vg_vbytes(rows) & 3) vg_dmemset(dm + (vg_vbytes(rows) & ~(int64_t)3), 0, 4);
-            vg_h2d(dm, s->validity[c] + lo / 8, (size_t)vg_vbytes(rows));
+            /* the bytes holding rows [lo, lo+rows), starting at the 4-byte
+             * word of row lo; never past the end of the host bitmap */
+            int64_t b0 = (lo >> 5) * 4;
+            int64_t b1 = (lo + rows + 7) / 8;
+            vg_dmemset(dm, 0, wb);
+            vg_h2d(dm, s->validity[c] + b0, (size_t)(b1 - b0));
             out->cols[c].valid = (const uint32_t *)dm;
+            out->cols[c].voff = (int32_t)(lo & 31);
         }
     }
     return 1;
@@ -127,8 +155,14 @@ static void source_free(VecNode *self) {
 VecNode *vgpu_table_source_create(int n_cols, const char *const *names, const int *types,
                                   const void *const *data, const uint8_t *const *validity,
                                   int64_t n_rows, int64_t batch_rows, int flags) {
-    if (batch_rows <= 0) batch_rows = n_rows > 0 ? n_rows : 32;
-    if (batch_rows % 32) vg_fail("table source: batch_rows must be a multiple of 32");
+    if (batch_rows <= 0) batch_rows = n_rows > 0 ? n_rows : 1;
+    if (n_cols <= 0 || n_rows < 0) { vg_set_error("table source: bad shape"); return NULL; }
+    for (int c = 0; c < n_cols; c++) {
+        if (types[c] != VEC_INT64 && types[c] != VEC_DOUBLE && types[c] != VEC_BOOL) {
+            vg_set_error("table source: column '%s' has a type the GPU path does not support", names[c]);
+            return NULL;
+        }
+    }
     VgSource *s = (VgSource *)vg_xcalloc(1, sizeof(VgSource));
     s->n_cols = n_cols;
     s->flags = flags;
@@ -139,7 +173,6 @@ VecNode *vgpu_table_source_create(int n_cols, const char *const *names, const in
     s->types = (int *)vg_xcalloc((size_t)n_cols, sizeof(int));
     VecType *ts = (VecType *)vg_xcalloc((size_t)n_cols, sizeof(VecType));
     for (int c = 0; c < n_cols; c++) {
-        if (types[c] == VEC_STRING) vg_fail("table source: string columns are not supported");
         s->types[c] = types[c];
         ts[c] = (VecType)types[c];
         if (flags & (VGPU_SRC_BORROW | VGPU_SRC_DEVICE)) {

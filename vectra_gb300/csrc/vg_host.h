@@ -13,6 +13,8 @@
 /* Records the message and raises it through vectra_error (no return). */
 void vg_fail(const char *fmt, ...);
 void vg_warn_count(long n);
+/* Records a message for vgpu_last_error() without raising. */
+void vg_set_error(const char *fmt, ...);
 /* Fails with the last kernel-side message if rc != 0. */
 void vg_check_rc(int rc, const char *what);
 

@@ -28,7 +28,7 @@ typedef struct CUstream_st *vg_stream_t;
  * byte i/8 of the host bitmap); NULL means every row is valid. */
 typedef struct {
     int32_t type;              /* VecType */
-    int32_t pad;
+    int32_t voff;              /* bit offset of row 0 within valid[0] (0..31) */
     const void *data;
     const uint32_t *valid;
 } VgCol;
