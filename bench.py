@@ -275,6 +275,10 @@ def gpu_arm(args, rank, world):
     build_n = C.c_ulonglong(0)
     build_ms = lib.vgpu_profile_ms(2, C.byref(build_n))
 
+    if args.no_e2e:
+        line = {"metric": METRIC, "ms_per_step": ms_step, "kernel_ms": agg_ms / agg_launches,
+                "scale": args.scale, "gpu_launches": launches}
+        return line
     # e2e: page-locked host copies of the same columns
     hf = {k: (v.cpu().pin_memory(), m.cpu().pin_memory()) for k, (v, m) in fcols.items()}
     hd = {k: (v.cpu().pin_memory(), m.cpu().pin_memory()) for k, (v, m) in dcols.items()}
@@ -422,8 +426,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) measurement")
+    ap.add_argument("--scale", type=int, default=1,
+                    help="divide both table sizes (small cases for profiling only; not a bench line)")
     args = ap.parse_args()
-    args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
+    if args.scale > 1:
+        global N_FACT, N_DIM
+        N_FACT //= args.scale
+        N_DIM //= args.scale
+    elif args.impl == "gpu":
+        args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1 and args.impl == "gpu":

@@ -288,7 +288,8 @@ static int pred_rec(const VecExpr *e, vg_colmap_fn map, void *ctx, VgPred *out, 
         int ci = map(ctx, c->col_name, &ty);
         if (ci < 0) return cerr("column not found: %s", c->col_name);
         if (ty == VEC_STRING) return 0;
-        fold_term(ty, lit_type(l), l->lit_i64, l->lit_dbl, code, t);
+        fold_term(ty, lit_type(l), l->kind == EXPR_LIT_BOOL ? (int64_t)(l->lit_bln != 0) : l->lit_i64,
+                  l->lit_dbl, code, t);
         t->col = ci;
         if (negate) {   /* Kleene NOT keeps NA as NA */
             switch (t->kind) {

@@ -1,4 +1,4 @@
-// k_agg.cu -- hash grouped aggregation on sm_103a, fused with the filter
+// k_groupby.cu -- hash grouped aggregation on sm_103a, fused with the filter
 // and, for joins feeding an aggregate, with the hash-join probe.
 //
 // Replaces the reference's per-row loop hash -> find_or_insert ->
@@ -15,6 +15,10 @@
 //    every double sum and mean is the correctly rounded result;
 //  * counts, integer sums (two's complement wrap, like the reference's
 //    int64 arithmetic), min and max are exact integer atomics.
+//
+// The launch description lives in the constant bank (__grid_constant__) and
+// the shared-memory layout is computed once per CTA, so the per-row path
+// keeps everything in registers.
 
 #include <cstdio>
 #include <cstring>
@@ -34,33 +38,89 @@ int check(cudaError_t e, const char *what) {
 constexpr int kWin = 6;               // window digits per double sum
 constexpr int kBaseUnset = 0x7FFFFFFF;
 constexpr int kThreads = 512;
-
-// ---------------------------------------------------------------------
-// accumulator state layout.  One layout description serves the shared
-// cache (per CTA) and the global table; `stride` is the slot count.
-// ---------------------------------------------------------------------
-struct AccPtrs {
-    uint64_t *cnt;      // count
-    int64_t *val;       // int sum / min / max / ordered double image
-    uint32_t *flags;
-    int32_t *base;      // window base digit (double sums)
-    int64_t *win;       // [kWin][stride] window digits
-    double *fs, *fc;    // compensated fallback sum (global table only)
-};
+constexpr int kCacheProbes = 16;
+constexpr int kGlobalProbes = 512;    // a longer probe means the table is too full: spill
 
 VG_DEV bool acc_is_min(int cls) { return cls == VG_ACC_MIN_I64 || cls == VG_ACC_MIN_F64; }
 VG_DEV bool acc_is_max(int cls) { return cls == VG_ACC_MAX_I64 || cls == VG_ACC_MAX_F64; }
+__host__ __device__ inline bool has_val(int cls) {
+    return cls == VG_ACC_SUM_I64 || cls == VG_ACC_MIN_I64 || cls == VG_ACC_MAX_I64 ||
+           cls == VG_ACC_MIN_F64 || cls == VG_ACC_MAX_F64;
+}
 
 // values flowing into accumulators
 struct InVal { uint64_t bits; bool ok; };
 
 // ---------------------------------------------------------------------
+// accumulator state of one table (shared cache, spill area or global)
+// ---------------------------------------------------------------------
+struct AccPtrs {
+    uint64_t *cnt;      // count
+    int64_t *val;       // int sum / min / max / ordered double image
+    uint32_t *flags;    // bit0 has_na, bit1 has_value, bit2 NaN, bit3 +inf, bit4 -inf
+    int32_t *base;      // window base digit (double sums)
+    int64_t *win;       // [kWin][stride] window digits
+    double *fs, *fc;    // compensated fallback sum (global table only)
+};
+
+// Layout of a cache-format area with `slots` slots (struct of arrays).
+struct Lay {
+    uint64_t state, nm, keys, first, total;
+    uint64_t cnt[VG_MAX_ACCS], val[VG_MAX_ACCS], flags[VG_MAX_ACCS], base[VG_MAX_ACCS], win[VG_MAX_ACCS];
+};
+
+__host__ __device__ inline uint64_t al8(uint64_t x) { return (x + 7) & ~(uint64_t)7; }
+
+__host__ __device__ inline void make_lay(const VgAggLaunch &L, uint64_t S, Lay &c) {
+    uint64_t off = 0;
+    c.state = off; off = al8(off + 4 * S);
+    c.nm = off; off = al8(off + 4 * S);
+    c.keys = off; off = al8(off + 8 * S * (uint64_t)L.n_keys);
+    c.first = off; off = al8(off + (L.track_first ? 8 * S : 0));
+    for (int a = 0; a < L.n_accs; a++) {
+        int cls = L.acc[a].cls;
+        c.cnt[a] = off; off = al8(off + 8 * S);
+        c.val[a] = off; off = al8(off + (has_val(cls) ? 8 * S : 0));
+        c.flags[a] = off; off = al8(off + 4 * S);
+        c.base[a] = off; off = al8(off + (cls == VG_ACC_SUM_F64 ? 4 * S : 0));
+        c.win[a] = off; off = al8(off + (cls == VG_ACC_SUM_F64 ? 8 * S * kWin : 0));
+    }
+    c.total = off;
+}
+
+VG_DEV AccPtrs lay_ptrs(char *base, const Lay &c, int a) {
+    AccPtrs p;
+    p.cnt = (uint64_t *)(base + c.cnt[a]);
+    p.val = (int64_t *)(base + c.val[a]);
+    p.flags = (uint32_t *)(base + c.flags[a]);
+    p.base = (int32_t *)(base + c.base[a]);
+    p.win = (int64_t *)(base + c.win[a]);
+    p.fs = p.fc = nullptr;
+    return p;
+}
+
+// Double-sum state of the global table lives in lacc[a]:
+//   [0, cap) int32 bases (in the first cap int64 words), then the window
+//   digits [kWin][cap], then fs[cap], fc[cap].
+VG_DEV AccPtrs global_ptrs(const VgGroupTable &gt, int a) {
+    AccPtrs p;
+    p.cnt = gt.cnt[a];
+    p.val = gt.val[a];
+    p.flags = gt.flags[a];
+    int64_t *l = gt.lacc[a];
+    p.base = (int32_t *)l;
+    p.win = l + gt.cap;
+    p.fs = (double *)(l + gt.cap * (1 + kWin));
+    p.fc = p.fs + gt.cap;
+    return p;
+}
+
+// ---------------------------------------------------------------------
 // exact window accumulation
 // ---------------------------------------------------------------------
-// Adds the digits of d into the window of slot s.  Returns false when the
+// Adds the digits of d into the window of a slot.  Returns false when the
 // value falls outside the window (the caller then uses a wider store).
-template <typename BaseT>
-VG_DEV bool win_add(BaseT *base_p, int64_t *win, int64_t stride, const VgDigits &d) {
+VG_DEV bool win_add(int32_t *base_p, int64_t *win, int64_t stride, const VgDigits &d) {
     int b = *(volatile int *)base_p;
     if (b == kBaseUnset) {
         int want = d.lo - 2;
@@ -90,81 +150,30 @@ VG_DEV void fallback_add(double *s, double *c, double x) {
     if (e != 0.0) atomicAdd(c, e);
 }
 
-// ---------------------------------------------------------------------
-// global table lookup / insert
-// ---------------------------------------------------------------------
-
-VG_DEV bool keys_equal_at(const uint64_t *tk, int64_t stride, int64_t slot, const uint64_t *k,
-                          int nk, const int32_t *types, uint32_t tnm, uint32_t nm) {
-    if (tnm != nm) return false;
-    for (int i = 0; i < nk; i++) {
-        if ((nm >> i) & 1u) continue;   // both NA in this component
-        uint64_t a = *(volatile const uint64_t *)(tk + (int64_t)i * stride + slot);
-        if (!vg_key_word_eq(a, k[i], types[i])) return false;
-    }
-    return true;
-}
-
-// Returns the slot or -1 (table full / wait expired; err is set).
-VG_DEV int64_t gt_find_insert(const VgGroupTable &gt, const uint64_t *k, int nk,
-                              const int32_t *types, uint32_t nm, uint64_t h) {
-    const int64_t mask = gt.cap - 1;
-    int64_t slot = (int64_t)(h & (uint64_t)mask);
-    for (int64_t probe = 0; probe < gt.cap; probe++) {
-        uint32_t st = *(volatile uint32_t *)(gt.state + slot);
-        if (st == 0) {
-            uint32_t prev = atomicCAS(gt.state + slot, 0u, 1u);
-            if (prev == 0u) {
-                for (int i = 0; i < nk; i++) gt.keys[(int64_t)i * gt.cap + slot] = k[i];
-                gt.nullmask[slot] = nm;
-                __threadfence();
-                atomicExch(gt.state + slot, 2u);
-                atomicAdd(gt.n_used, 1u);
-                return slot;
-            }
-            st = prev;
-        }
-        int spins = 0;
-        while (st == 1u) {
-            if (++spins > VG_SPIN_LIMIT) { atomicOr(gt.err, VG_ERR_WAIT); return -1; }
-            __nanosleep(32);
-            st = *(volatile uint32_t *)(gt.state + slot);
-        }
-        __threadfence();
-        uint32_t tnm = *(volatile uint32_t *)(gt.nullmask + slot);
-        if (keys_equal_at(gt.keys, gt.cap, slot, k, nk, types, tnm, nm)) return slot;
-        slot = (slot + 1) & mask;
-    }
-    atomicOr(gt.err, VG_ERR_FULL);
-    return -1;
-}
-
-// ---------------------------------------------------------------------
-// applying one input value to accumulator a of a slot
-// ---------------------------------------------------------------------
 VG_DEV void set_flags(uint32_t *f, uint32_t bits) {
     uint32_t cur = *(volatile uint32_t *)f;
     if ((cur & bits) != bits) atomicOr(f, bits);
 }
 
-// generic (shared or global) update; `global` selects the fallback path
+// One input value into accumulator A of a slot.  kGlobal selects the
+// global table's fallback for values outside the window; in a cache the
+// update is refused instead (returns false) and retried globally.
 template <bool kGlobal>
-VG_DEV bool acc_update(const VgAccSpec &A, const AccPtrs &P, int64_t stride, int64_t slot,
-                       InVal x, int in_type) {
-    switch (A.cls) {
-    case VG_ACC_COUNT_ALL:
+VG_DEV bool acc_update(const VgAccSpec &A, const AccPtrs &P, int64_t stride, int64_t slot, InVal x) {
+    const int cls = A.cls;
+    if (cls == VG_ACC_COUNT_ALL) {
         atomicAdd((unsigned long long *)(P.cnt + slot), 1ull);
         return true;
-    case VG_ACC_COUNT_VALID:
+    }
+    if (cls == VG_ACC_COUNT_VALID) {
         if (x.ok) atomicAdd((unsigned long long *)(P.cnt + slot), 1ull);
         return true;
-    default: break;
     }
     if (!x.ok) {
         if (!A.na_rm) set_flags(P.flags + slot, 1u);
         return true;
     }
-    switch (A.cls) {
+    switch (cls) {
     case VG_ACC_SUM_I64:
         atomicAdd((unsigned long long *)(P.cnt + slot), 1ull);
         atomicAdd((unsigned long long *)(P.val + slot), (unsigned long long)x.bits);
@@ -173,7 +182,7 @@ VG_DEV bool acc_update(const VgAccSpec &A, const AccPtrs &P, int64_t stride, int
         VgDigits d = vg_split_double(x.bits);
         if (d.special) set_flags(P.flags + slot, d.special);
         else if (d.lo >= 0 && !win_add(P.base + slot, P.win + slot, stride, d)) {
-            if (!kGlobal) return false;   // caller retries on the global table
+            if (!kGlobal) return false;
             fallback_add(P.fs + slot, P.fc + slot, vg_bits_to_f64(x.bits));
         }
         atomicAdd((unsigned long long *)(P.cnt + slot), 1ull);
@@ -190,79 +199,84 @@ VG_DEV bool acc_update(const VgAccSpec &A, const AccPtrs &P, int64_t stride, int
     case VG_ACC_MIN_F64:
     case VG_ACC_MAX_F64:
         if (vg_is_nan_bits(x.bits)) { set_flags(P.flags + slot, 2u | 4u); return true; }
-        if (A.cls == VG_ACC_MIN_F64) atomicMin((long long *)(P.val + slot), (long long)vg_ord(x.bits));
+        if (cls == VG_ACC_MIN_F64) atomicMin((long long *)(P.val + slot), (long long)vg_ord(x.bits));
         else atomicMax((long long *)(P.val + slot), (long long)vg_ord(x.bits));
         set_flags(P.flags + slot, 2u);
         return true;
-    default:   // VG_ACC_NA_ONLY
+    default:   // VG_ACC_NA_ONLY: only NA poisoning (bool min / max)
         return true;
     }
 }
 
 // ---------------------------------------------------------------------
-// shared-memory cache layout
+// keys
 // ---------------------------------------------------------------------
-struct CacheLayout {
-    size_t state, nullmask, keys, first, total;
-    size_t cnt[VG_MAX_ACCS], val[VG_MAX_ACCS], flags[VG_MAX_ACCS], base[VG_MAX_ACCS], win[VG_MAX_ACCS];
-};
+struct Keys { uint64_t w[VG_MAX_KEYS]; };
+struct KeyTypes { int32_t t[VG_MAX_KEYS]; };
 
-__host__ __device__ inline size_t al8(size_t x) { return (x + 7) & ~(size_t)7; }
+VG_DEV uint64_t hash_k(const Keys &k, int nk, uint32_t nm) {
+    uint64_t h = 0x9E3779B97F4A7C15ull ^ nm;
+#pragma unroll
+    for (int i = 0; i < VG_MAX_KEYS; i++)
+        if (i < nk) h = vg_mix64(h ^ k.w[i]) + (uint64_t)i;
+    return vg_mix64(h);
+}
 
-__host__ __device__ inline CacheLayout cache_layout(const VgAggLaunch &L, int64_t slots) {
-    CacheLayout c;
-    size_t S = (size_t)slots, off = 0;
-    c.state = off; off = al8(off + 4 * S);
-    c.nullmask = off; off = al8(off + 4 * S);
-    c.keys = off; off = al8(off + 8 * S * (size_t)L.n_keys);
-    c.first = off; off = al8(off + (L.track_first ? 8 * S : 0));
-    for (int a = 0; a < L.n_accs; a++) {
-        int cls = L.acc[a].cls;
-        c.cnt[a] = off; off = al8(off + 8 * S);
-        c.val[a] = off; off = al8(off + ((cls == VG_ACC_SUM_I64 || cls == VG_ACC_MIN_I64 ||
-                                          cls == VG_ACC_MAX_I64 || cls == VG_ACC_MIN_F64 ||
-                                          cls == VG_ACC_MAX_F64) ? 8 * S : 0));
-        c.flags[a] = off; off = al8(off + 4 * S);
-        c.base[a] = off; off = al8(off + (cls == VG_ACC_SUM_F64 ? 4 * S : 0));
-        c.win[a] = off; off = al8(off + (cls == VG_ACC_SUM_F64 ? 8 * S * kWin : 0));
+VG_DEV bool keys_eq(const uint64_t *tk, int64_t stride, int64_t slot, const Keys &k, int nk,
+                    const KeyTypes &kt, uint32_t tnm, uint32_t nm) {
+    if (tnm != nm) return false;
+#pragma unroll
+    for (int i = 0; i < VG_MAX_KEYS; i++) {
+        if (i >= nk) break;
+        if ((nm >> i) & 1u) continue;   // both NA in this component
+        uint64_t a = *(volatile const uint64_t *)(tk + (int64_t)i * stride + slot);
+        if (!vg_key_word_eq(a, k.w[i], kt.t[i])) return false;
     }
-    c.total = off;
-    return c;
+    return true;
 }
 
-VG_DEV AccPtrs cache_ptrs(char *sm, const CacheLayout &c, int a) {
-    AccPtrs p;
-    p.cnt = (uint64_t *)(sm + c.cnt[a]);
-    p.val = (int64_t *)(sm + c.val[a]);
-    p.flags = (uint32_t *)(sm + c.flags[a]);
-    p.base = (int32_t *)(sm + c.base[a]);
-    p.win = (int64_t *)(sm + c.win[a]);
-    p.fs = p.fc = nullptr;
-    return p;
-}
-
-VG_DEV AccPtrs global_ptrs(const VgGroupTable &gt, int a) {
-    AccPtrs p;
-    p.cnt = gt.cnt[a];
-    p.val = gt.val[a];
-    p.flags = gt.flags[a];
-    // double-sum state of the global table lives in lacc[a]:
-    //   [0, cap)            int32 base (as int64 words for alignment)
-    //   [cap, cap*(1+kWin)) window digits
-    //   then fs[cap], fc[cap]
-    int64_t *l = gt.lacc[a];
-    p.base = (int32_t *)l;                         // uses the first cap int32s
-    p.win = l + gt.cap;
-    p.fs = (double *)(l + gt.cap * (1 + kWin));
-    p.fc = p.fs + gt.cap;
-    return p;
+// Global table: returns the slot, or -1 when the table is too full (the
+// caller spills and the host grows the table) or a bounded wait expired
+// (err set).
+VG_DEV int64_t gt_find_insert(const VgGroupTable &gt, const Keys &k, int nk, const KeyTypes &kt,
+                              uint32_t nm, uint64_t h) {
+    const int64_t mask = gt.cap - 1;
+    int64_t slot = (int64_t)(h & (uint64_t)mask);
+    const int64_t max_probe = gt.cap < kGlobalProbes ? gt.cap : kGlobalProbes;
+    for (int64_t probe = 0; probe < max_probe; probe++) {
+        uint32_t st = *(volatile uint32_t *)(gt.state + slot);
+        if (st == 0) {
+            uint32_t prev = atomicCAS(gt.state + slot, 0u, 1u);
+            if (prev == 0u) {
+#pragma unroll
+                for (int i = 0; i < VG_MAX_KEYS; i++)
+                    if (i < nk) gt.keys[(int64_t)i * gt.cap + slot] = k.w[i];
+                gt.nullmask[slot] = nm;
+                __threadfence();
+                atomicExch(gt.state + slot, 2u);
+                atomicAdd(gt.n_used, 1u);
+                return slot;
+            }
+            st = prev;
+        }
+        int spins = 0;
+        while (st == 1u) {
+            if (++spins > VG_SPIN_LIMIT) { atomicOr(gt.err, VG_ERR_WAIT); return -1; }
+            __nanosleep(32);
+            st = *(volatile uint32_t *)(gt.state + slot);
+        }
+        __threadfence();
+        uint32_t tnm = *(volatile uint32_t *)(gt.nullmask + slot);
+        if (keys_eq(gt.keys, gt.cap, slot, k, nk, kt, tnm, nm)) return slot;
+        slot = (slot + 1) & mask;
+    }
+    return -1;
 }
 
 // ---------------------------------------------------------------------
-// reading operands and values
+// operands, values, predicate terms, join probe
 // ---------------------------------------------------------------------
-VG_DEV InVal load_operand(const VgOperand &o, const VgCol *pc, const VgCol *bc, int64_t pr,
-                          int64_t br) {
+VG_DEV InVal load_operand(const VgOperand &o, const VgCol *pc, const VgCol *bc, int64_t pr, int64_t br) {
     InVal v;
     switch (o.side) {
     case VG_SIDE_PROBE: {
@@ -330,7 +344,6 @@ VG_DEV InVal eval_value(const VgValue &V, const VgCol *pc, const VgCol *bc, int6
     return r;
 }
 
-// predicate terms (same semantics as the filter kernel)
 VG_DEV bool term_keep(const VgTerm &t, const VgCol *cols, int64_t p) {
     if (t.kind == VG_TERM_NONE) return false;
     const VgCol &c = cols[t.col];
@@ -350,11 +363,10 @@ VG_DEV bool term_keep(const VgTerm &t, const VgCol *cols, int64_t p) {
     return t.kind == VG_TERM_RANGE ? in : !in;
 }
 
-// ---------------------------------------------------------------------
-// join probe helpers
-// ---------------------------------------------------------------------
 VG_DEV bool probe_key_words(const VgAggLaunch &L, int64_t pr, uint64_t *k) {
-    for (int i = 0; i < L.n_jkeys; i++) {
+#pragma unroll
+    for (int i = 0; i < VG_MAX_KEYS; i++) {
+        if (i >= L.n_jkeys) break;
         const VgCol &c = L.pcols[L.jkey_col[i]];
         if (!vg_valid(c, pr)) return false;            // NA never matches
         uint64_t b = vg_load_bits(c, pr);
@@ -367,52 +379,33 @@ VG_DEV bool probe_key_words(const VgAggLaunch &L, int64_t pr, uint64_t *k) {
 }
 
 // ---------------------------------------------------------------------
-// the fused aggregation kernel
+// cache entry merge / spill (shared by the kernel tail and the replay)
 // ---------------------------------------------------------------------
 
-// Records spilled work; false if the spill list itself is full.
-VG_DEV bool spill_row(const VgAggLaunch &L, int64_t li, int32_t m, int acc) {
-    uint32_t i = atomicAdd(L.spill_rows_n, 1u);
-    if ((int64_t)i >= L.spill_rows_cap) { atomicOr(L.gt.err, VG_ERR_FULL); return false; }
-    L.spill_rows[2 * (int64_t)i] = li;
-    L.spill_rows[2 * (int64_t)i + 1] = ((int64_t)m << 8) | (int64_t)(acc + 1);
-    return true;
+// Merges cache-layout entry i (area `base`, layout c, stride S) into the
+// global table.  Returns false if the global table had no room.
+VG_DEV KeyTypes key_types(const VgAggLaunch &L) {
+    KeyTypes kt;
+#pragma unroll
+    for (int i = 0; i < VG_MAX_KEYS; i++) kt.t[i] = i < L.n_keys ? L.key[i].type : 0;
+    return kt;
 }
 
-VG_DEV void init_cache_slot(const VgAggLaunch &L, char *base, const CacheLayout &cl, int64_t S, int64_t i) {
-    ((uint32_t *)(base + cl.state))[i] = 0;
-    if (L.track_first) ((uint64_t *)(base + cl.first))[i] = ~0ull;
-    for (int a = 0; a < L.n_accs; a++) {
-        AccPtrs p = cache_ptrs(base, cl, a);
-        p.cnt[i] = 0;
-        p.flags[i] = 0;
-        int cls = L.acc[a].cls;
-        if (cls == VG_ACC_SUM_I64) p.val[i] = 0;
-        else if (acc_is_min(cls)) p.val[i] = 0x7FFFFFFFFFFFFFFFll;
-        else if (acc_is_max(cls)) p.val[i] = (int64_t)0x8000000000000000ull;
-        if (cls == VG_ACC_SUM_F64) {
-            p.base[i] = kBaseUnset;
-            for (int w = 0; w < kWin; w++) p.win[(int64_t)w * S + i] = 0;
-        }
-    }
-}
-
-// Merges cache-layout entry i (of an area with stride S) into the global
-// table.  Returns false if the global table had no room.
-VG_DEV bool merge_entry(const VgAggLaunch &L, char *base, const CacheLayout &cl, int64_t S, int64_t i,
-                        const int32_t *ktypes) {
-    uint64_t k[VG_MAX_KEYS];
-    const uint64_t *sk = (const uint64_t *)(base + cl.keys);
-    for (int j = 0; j < L.n_keys; j++) k[j] = sk[(int64_t)j * S + i];
-    uint32_t nm = ((const uint32_t *)(base + cl.nullmask))[i];
-    uint64_t h = hash_keys(k, L.n_keys, nm);
-    int64_t g = gt_find_insert(L.gt, k, L.n_keys, ktypes, nm, h);
+VG_DEV bool merge_entry(const VgAggLaunch &L, char *base, const Lay &c, int64_t S, int64_t i) {
+    const KeyTypes kt = key_types(L);
+    Keys k;
+    const uint64_t *sk = (const uint64_t *)(base + c.keys);
+#pragma unroll
+    for (int j = 0; j < VG_MAX_KEYS; j++) k.w[j] = j < L.n_keys ? sk[(int64_t)j * S + i] : 0;
+    uint32_t nm = ((const uint32_t *)(base + c.nm))[i];
+    uint64_t h = hash_k(k, L.n_keys, nm);
+    int64_t g = gt_find_insert(L.gt, k, L.n_keys, kt, nm, h);
     if (g < 0) return false;
     if (L.track_first)
-        atomicMin((unsigned long long *)(L.gt.first_row + g), ((unsigned long long *)(base + cl.first))[i]);
+        atomicMin((unsigned long long *)(L.gt.first_row + g), ((unsigned long long *)(base + c.first))[i]);
     for (int a = 0; a < L.n_accs; a++) {
         const int cls = L.acc[a].cls;
-        AccPtrs sp = cache_ptrs(base, cl, a);
+        AccPtrs sp = lay_ptrs(base, c, a);
         AccPtrs gp = global_ptrs(L.gt, a);
         if (sp.cnt[i]) atomicAdd((unsigned long long *)(gp.cnt + g), (unsigned long long)sp.cnt[i]);
         uint32_t f = sp.flags[i];
@@ -426,8 +419,8 @@ VG_DEV bool merge_entry(const VgAggLaunch &L, char *base, const CacheLayout &cl,
         } else if (cls == VG_ACC_SUM_F64) {
             int bs = sp.base[i];
             if (bs == kBaseUnset) continue;
-            // place each digit word into the global window; words that do
-            // not fit go through the compensated fallback, split into two
+            // each digit word goes into the global window; words that do not
+            // fit go through the compensated fallback, split into two
             // exactly representable halves
             int bg = *(volatile int *)(gp.base + g);
             if (bg == kBaseUnset) {
@@ -454,24 +447,23 @@ VG_DEV bool merge_entry(const VgAggLaunch &L, char *base, const CacheLayout &cl,
 }
 
 // Copies cache entry i into the spill area (same layout, stride spill cap).
-VG_DEV void spill_entry(const VgAggLaunch &L, const char *sm, const CacheLayout &cl, int64_t S, int64_t i,
-                        const CacheLayout &sl) {
+VG_DEV void spill_entry(const VgAggLaunch &L, char *sm, const Lay &c, int64_t S, int64_t i, const Lay &sl) {
     uint32_t j = atomicAdd(L.spill_cache_n, 1u);
-    if ((int64_t)j >= L.spill_cache_cap) { atomicOr(L.gt.err, VG_ERR_FULL); return; }
+    if ((int64_t)j >= L.spill_cache_cap) { atomicOr(L.gt.err, VG_ERR_SPILL); return; }
     const int64_t T = L.spill_cache_cap;
     char *d = L.spill_cache;
     ((uint32_t *)(d + sl.state))[j] = 2u;
-    ((uint32_t *)(d + sl.nullmask))[j] = ((const uint32_t *)(sm + cl.nullmask))[i];
+    ((uint32_t *)(d + sl.nm))[j] = ((const uint32_t *)(sm + c.nm))[i];
     for (int k = 0; k < L.n_keys; k++)
-        ((uint64_t *)(d + sl.keys))[(int64_t)k * T + j] = ((const uint64_t *)(sm + cl.keys))[(int64_t)k * S + i];
-    if (L.track_first) ((uint64_t *)(d + sl.first))[j] = ((const uint64_t *)(sm + cl.first))[i];
+        ((uint64_t *)(d + sl.keys))[(int64_t)k * T + j] = ((const uint64_t *)(sm + c.keys))[(int64_t)k * S + i];
+    if (L.track_first) ((uint64_t *)(d + sl.first))[j] = ((const uint64_t *)(sm + c.first))[i];
     for (int a = 0; a < L.n_accs; a++) {
-        AccPtrs sp = cache_ptrs((char *)sm, cl, a);
-        AccPtrs dp = cache_ptrs(d, sl, a);
+        AccPtrs sp = lay_ptrs(sm, c, a);
+        AccPtrs dp = lay_ptrs(d, sl, a);
         dp.cnt[j] = sp.cnt[i];
         dp.flags[j] = sp.flags[i];
         int cls = L.acc[a].cls;
-        if (cls == VG_ACC_SUM_I64 || acc_is_min(cls) || acc_is_max(cls)) dp.val[j] = sp.val[i];
+        if (has_val(cls)) dp.val[j] = sp.val[i];
         if (cls == VG_ACC_SUM_F64) {
             dp.base[j] = sp.base[i];
             for (int w = 0; w < kWin; w++) dp.win[(int64_t)w * T + j] = sp.win[(int64_t)w * S + i];
@@ -479,23 +471,51 @@ VG_DEV void spill_entry(const VgAggLaunch &L, const char *sm, const CacheLayout 
     }
 }
 
+VG_DEV void init_slot(const VgAggLaunch &L, char *base, const Lay &c, int64_t S, int64_t i) {
+    ((uint32_t *)(base + c.state))[i] = 0;
+    if (L.track_first) ((uint64_t *)(base + c.first))[i] = ~0ull;
+    for (int a = 0; a < L.n_accs; a++) {
+        AccPtrs p = lay_ptrs(base, c, a);
+        p.cnt[i] = 0;
+        p.flags[i] = 0;
+        int cls = L.acc[a].cls;
+        if (cls == VG_ACC_SUM_I64) p.val[i] = 0;
+        else if (acc_is_min(cls)) p.val[i] = 0x7FFFFFFFFFFFFFFFll;
+        else if (acc_is_max(cls)) p.val[i] = (int64_t)0x8000000000000000ull;
+        if (cls == VG_ACC_SUM_F64) {
+            p.base[i] = kBaseUnset;
+            for (int w = 0; w < kWin; w++) p.win[(int64_t)w * S + i] = 0;
+        }
+    }
+}
+
+VG_DEV bool spill_row(const VgAggLaunch &L, int64_t li, int32_t m, int acc) {
+    uint32_t i = atomicAdd(L.spill_rows_n, 1u);
+    if ((int64_t)i >= L.spill_rows_cap) { atomicOr(L.gt.err, VG_ERR_SPILL); return false; }
+    L.spill_rows[2 * (int64_t)i] = li;
+    L.spill_rows[2 * (int64_t)i + 1] = ((int64_t)m << 8) | (int64_t)(acc + 1);
+    return true;
+}
+
+// ---------------------------------------------------------------------
+// the fused aggregation kernel
+// ---------------------------------------------------------------------
 template <bool kPred, bool kJoin, bool kCache>
-__global__ void __launch_bounds__(kThreads)
-agg_kernel(const VgAggLaunch *__restrict__ Lp, int64_t n_logical) {
+__global__ void __launch_bounds__(kThreads, 2)
+agg_kernel(const __grid_constant__ VgAggLaunch L, int64_t n_logical) {
     extern __shared__ __align__(16) char sm[];
-    const VgAggLaunch &L = *Lp;
-    const int S = L.cache_slots;
-    CacheLayout cl;
+    __shared__ Lay cl;
     __shared__ int cache_used;   // occupied cache slots; a nearly full cache stops taking new keys
+    const int S = L.cache_slots;
+    const int nk = L.n_keys;
     if (kCache) {
-        cl = cache_layout(L, S);
-        for (int i = threadIdx.x; i < S; i += blockDim.x) init_cache_slot(L, sm, cl, S, i);
-        if (threadIdx.x == 0) cache_used = 0;
+        if (threadIdx.x == 0) { make_lay(L, S, cl); cache_used = 0; }
+        __syncthreads();
+        for (int i = threadIdx.x; i < S; i += blockDim.x) init_slot(L, sm, cl, S, i);
         __syncthreads();
     }
-    int32_t ktypes[VG_MAX_KEYS];
-    for (int i = 0; i < VG_MAX_KEYS; i++) ktypes[i] = i < L.n_keys ? L.key[i].type : 0;
     const bool replay = L.replay != nullptr;
+    const KeyTypes kt = key_types(L);
 
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < n_logical; it += stride) {
@@ -529,13 +549,16 @@ agg_kernel(const VgAggLaunch *__restrict__ Lp, int64_t n_logical) {
         for (int32_t m = m_lo; m < m_hi; m++) {
             int64_t br = -1;
             if (kJoin && matched) br = jt_row(L.jt, mstart, m);
-            // group key words
-            uint64_t k[VG_MAX_KEYS];
+            Keys k;
             uint32_t nm = 0;
-            for (int i = 0; i < L.n_keys; i++) {
-                InVal v = eval_value(L.key[i], L.pcols, L.bcols, pr, br);
-                if (!v.ok) { nm |= 1u << i; k[i] = 0; }
-                else k[i] = vg_norm_key(v.bits, ktypes[i]);
+#pragma unroll
+            for (int i = 0; i < VG_MAX_KEYS; i++) {
+                k.w[i] = 0;
+                if (i < nk) {
+                    InVal v = eval_value(L.key[i], L.pcols, L.bcols, pr, br);
+                    if (!v.ok) nm |= 1u << i;
+                    else k.w[i] = vg_norm_key(v.bits, L.key[i].type);
+                }
             }
             uint64_t order = 0;
             if (L.track_first) {
@@ -550,26 +573,23 @@ agg_kernel(const VgAggLaunch *__restrict__ Lp, int64_t n_logical) {
                     order = (uint64_t)(L.row_base + li);   // logical position in the stream
                 }
             }
-            uint64_t h = hash_keys(k, L.n_keys, nm);
-            InVal vals[VG_MAX_ACCS];
-            for (int a = 0; a < L.n_accs; a++)
-                vals[a] = (L.acc[a].cls == VG_ACC_COUNT_ALL) ? InVal{0, true}
-                                                             : eval_value(L.acc[a].in, L.pcols, L.bcols, pr, br);
-            bool done = false;
+            const uint64_t h = hash_k(k, nk, nm);
+            int found = -1;
             if (kCache) {
                 uint32_t *st = (uint32_t *)(sm + cl.state);
-                uint32_t *snm = (uint32_t *)(sm + cl.nullmask);
+                uint32_t *snm = (uint32_t *)(sm + cl.nm);
                 uint64_t *sk = (uint64_t *)(sm + cl.keys);
                 int slot = (int)(h & (uint64_t)(S - 1));
-                int found = -1;
                 const bool may_insert = *(volatile int *)&cache_used < (S * 3) / 4;
-                for (int probe = 0; probe < (may_insert ? 16 : 4); probe++) {
+                for (int probe = 0; probe < (may_insert ? kCacheProbes : 4); probe++) {
                     uint32_t s0 = *(volatile uint32_t *)(st + slot);
                     if (s0 == 0) {
                         if (!may_insert) break;
                         uint32_t prev = atomicCAS(st + slot, 0u, 1u);
                         if (prev == 0u) {
-                            for (int i = 0; i < L.n_keys; i++) sk[(int64_t)i * S + slot] = k[i];
+#pragma unroll
+                            for (int i = 0; i < VG_MAX_KEYS; i++)
+                                if (i < nk) sk[(int64_t)i * S + slot] = k.w[i];
                             snm[slot] = nm;
                             __threadfence_block();
                             atomicExch(st + slot, 2u);
@@ -586,57 +606,63 @@ agg_kernel(const VgAggLaunch *__restrict__ Lp, int64_t n_logical) {
                     }
                     if (s0 != 2u) break;
                     __threadfence_block();
-                    if (keys_equal_at(sk, S, slot, k, L.n_keys, ktypes, *(volatile uint32_t *)(snm + slot), nm)) {
+                    if (keys_eq(sk, S, slot, k, nk, kt, *(volatile uint32_t *)(snm + slot), nm)) {
                         found = slot;
                         break;
                     }
                     slot = (slot + 1) & (S - 1);
                 }
-                if (found >= 0) {
-                    done = true;
-                    if (L.track_first)
-                        atomicMin((unsigned long long *)(sm + cl.first) + found, (unsigned long long)order);
-                    for (int a = 0; a < L.n_accs; a++) {
-                        if (acc_update<false>(L.acc[a], cache_ptrs(sm, cl, a), S, found, vals[a], 0)) continue;
-                        // value outside the shared window: this update goes
-                        // to the global table
-                        int64_t g = gt_find_insert(L.gt, k, L.n_keys, ktypes, nm, h);
-                        if (g >= 0) acc_update<true>(L.acc[a], global_ptrs(L.gt, a), L.gt.cap, g, vals[a], 0);
-                        else spill_row(L, li, m, a);
-                    }
-                }
             }
-            if (!done) {
-                int64_t g = gt_find_insert(L.gt, k, L.n_keys, ktypes, nm, h);
+            if (found >= 0) {
+                if (L.track_first)
+                    atomicMin((unsigned long long *)(sm + cl.first) + found, (unsigned long long)order);
+                for (int a = 0; a < L.n_accs; a++) {
+                    const VgAccSpec &A = L.acc[a];
+                    InVal v = (A.cls == VG_ACC_COUNT_ALL) ? InVal{0, true}
+                                                          : eval_value(A.in, L.pcols, L.bcols, pr, br);
+                    if (acc_update<false>(A, lay_ptrs(sm, cl, a), S, found, v)) continue;
+                    // value outside the shared window: this update goes to
+                    // the global table
+                    int64_t g = gt_find_insert(L.gt, k, nk, kt, nm, h);
+                    if (g >= 0) acc_update<true>(A, global_ptrs(L.gt, a), L.gt.cap, g, v);
+                    else spill_row(L, li, m, a);
+                }
+            } else {
+                int64_t g = gt_find_insert(L.gt, k, nk, kt, nm, h);
                 if (g < 0) { spill_row(L, li, m, only_acc); continue; }
                 if (L.track_first && only_acc < 0)
                     atomicMin((unsigned long long *)(L.gt.first_row + g), (unsigned long long)order);
-                for (int a = 0; a < L.n_accs; a++)
-                    if (only_acc < 0 || only_acc == a)
-                        acc_update<true>(L.acc[a], global_ptrs(L.gt, a), L.gt.cap, g, vals[a], 0);
+                for (int a = 0; a < L.n_accs; a++) {
+                    if (only_acc >= 0 && only_acc != a) continue;
+                    const VgAccSpec &A = L.acc[a];
+                    InVal v = (A.cls == VG_ACC_COUNT_ALL) ? InVal{0, true}
+                                                          : eval_value(A.in, L.pcols, L.bcols, pr, br);
+                    acc_update<true>(A, global_ptrs(L.gt, a), L.gt.cap, g, v);
+                }
             }
         }
     }
 
     if (!kCache) return;
     __syncthreads();
+    __shared__ Lay sl;
+    if (threadIdx.x == 0) make_lay(L, (uint64_t)L.spill_cache_cap, sl);
+    __syncthreads();
     const uint32_t *st = (const uint32_t *)(sm + cl.state);
-    CacheLayout sl = cache_layout(L, L.spill_cache_cap);
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
         if (st[i] != 2u) continue;
-        if (!merge_entry(L, sm, cl, S, i, ktypes)) spill_entry(L, sm, cl, S, i, sl);
+        if (!merge_entry(L, sm, cl, S, i)) spill_entry(L, sm, cl, S, i, sl);
     }
 }
 
 // merges spilled cache entries (after the table has been grown)
-__global__ void merge_spilled_kernel(const VgAggLaunch *__restrict__ Lp, int64_t n) {
-    const VgAggLaunch &L = *Lp;
-    int32_t ktypes[VG_MAX_KEYS];
-    for (int i = 0; i < VG_MAX_KEYS; i++) ktypes[i] = i < L.n_keys ? L.key[i].type : 0;
-    CacheLayout sl = cache_layout(L, L.spill_cache_cap);
+__global__ void merge_spilled_kernel(const __grid_constant__ VgAggLaunch L, int64_t n) {
+    __shared__ Lay sl;
+    if (threadIdx.x == 0) make_lay(L, (uint64_t)L.spill_cache_cap, sl);
+    __syncthreads();
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-        if (!merge_entry(L, L.spill_cache, sl, L.spill_cache_cap, i, ktypes)) atomicOr(L.gt.err, VG_ERR_FULL);
+        if (!merge_entry(L, L.spill_cache, sl, L.spill_cache_cap, i)) atomicOr(L.gt.err, VG_ERR_FULL);
 }
 
 // moves every occupied slot of `from` into the empty table `to`
@@ -647,22 +673,26 @@ struct RehashArgs {
     int32_t cls[VG_MAX_ACCS];
 };
 
-__global__ void rehash_kernel(const RehashArgs *__restrict__ R) {
-    const VgGroupTable &F = R->from, &T = R->to;
+__global__ void rehash_kernel(const __grid_constant__ RehashArgs R) {
+    const VgGroupTable &F = R.from, &T = R.to;
+    KeyTypes kt;
+#pragma unroll
+    for (int j = 0; j < VG_MAX_KEYS; j++) kt.t[j] = R.key_types[j];
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < F.cap; i += stride) {
         if (F.state[i] != 2u) continue;
-        uint64_t k[VG_MAX_KEYS];
-        for (int j = 0; j < R->n_keys; j++) k[j] = F.keys[(int64_t)j * F.cap + i];
+        Keys k;
+#pragma unroll
+        for (int j = 0; j < VG_MAX_KEYS; j++) k.w[j] = j < R.n_keys ? F.keys[(int64_t)j * F.cap + i] : 0;
         uint32_t nm = F.nullmask[i];
-        int64_t g = gt_find_insert(T, k, R->n_keys, R->key_types, nm, hash_keys(k, R->n_keys, nm));
-        if (g < 0) continue;
+        int64_t g = gt_find_insert(T, k, R.n_keys, kt, nm, hash_k(k, R.n_keys, nm));
+        if (g < 0) { atomicOr(T.err, VG_ERR_FULL); continue; }
         T.first_row[g] = F.first_row[i];
-        for (int a = 0; a < R->n_accs; a++) {
+        for (int a = 0; a < R.n_accs; a++) {
             T.cnt[a][g] = F.cnt[a][i];
             T.flags[a][g] = F.flags[a][i];
             T.val[a][g] = F.val[a][i];
-            if (R->cls[a] == VG_ACC_SUM_F64) {
+            if (R.cls[a] == VG_ACC_SUM_F64) {
                 AccPtrs fp = global_ptrs(F, a), tp = global_ptrs(T, a);
                 tp.base[g] = fp.base[i];
                 for (int w = 0; w < kWin; w++) tp.win[(int64_t)w * T.cap + g] = fp.win[(int64_t)w * F.cap + i];
@@ -720,13 +750,13 @@ struct FinishArgs {
     int n_keys;
     int32_t key_types[VG_MAX_KEYS];
     int n_out;
-    VgFinish fin[VG_MAX_ACCS * 2];
+    VgFinish fin[VG_MAX_OUTS];
     const int32_t *slots;
     int64_t n_groups;
     uint64_t *key_out[VG_MAX_KEYS];
     uint32_t *key_valid[VG_MAX_KEYS];
-    double *out[VG_MAX_ACCS * 2];
-    uint32_t *out_valid[VG_MAX_ACCS * 2];
+    double *out[VG_MAX_OUTS];
+    uint32_t *out_valid[VG_MAX_OUTS];
     uint32_t *warn;
 };
 
@@ -914,11 +944,15 @@ const char *vgk_agg_last_error(void) { return g_err; }
 
 size_t vgk_agg_smem_bytes(const VgAggLaunch *L) {
     if (L->cache_slots <= 0) return 0;
-    return cache_layout(*L, L->cache_slots).total;
+    Lay c;
+    make_lay(*L, (uint64_t)L->cache_slots, c);
+    return c.total;
 }
 
 size_t vgk_agg_cache_bytes(const VgAggLaunch *L, int64_t slots) {
-    return cache_layout(*L, slots).total;
+    Lay c;
+    make_lay(*L, (uint64_t)slots, c);
+    return c.total;
 }
 
 int vgk_group_table_init(VgGroupTable *gt, int n_keys, const int32_t *acc_cls, int n_accs,
@@ -942,9 +976,6 @@ int vgk_agg_launch(const VgAggLaunch *L, vg_stream_t s) {
     cudaStream_t st = (cudaStream_t)s;
     int64_t n_logical = L->replay ? L->replay_n : (L->sel ? L->sel_n : L->n_rows);
     if (n_logical <= 0) return 0;
-    void *dL = nullptr;
-    if (check(cudaMallocAsync(&dL, sizeof(VgAggLaunch), st), "agg args")) return -1;
-    if (check(cudaMemcpyAsync(dL, L, sizeof(VgAggLaunch), cudaMemcpyHostToDevice, st), "agg args")) return -1;
     bool cache = L->cache_slots > 0 && !L->replay;
     size_t smem = cache ? vgk_agg_smem_bytes(L) : 0;
     bool pred = L->pred.n_terms > 0, join = L->has_join != 0;
@@ -958,7 +989,7 @@ int vgk_agg_launch(const VgAggLaunch *L, vg_stream_t s) {
         auto k = agg_kernel<P, J, C>;                                                   \
         if (smem > 48 * 1024)                                                           \
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        k<<<grid, kThreads, smem, st>>>((const VgAggLaunch *)dL, n_logical);             \
+        k<<<grid, kThreads, smem, st>>>(*L, n_logical);                                  \
         vg_launch_counter++;                                                            \
     } while (0)
     vg_prof_begin(VG_PROF_AGG, st);
@@ -971,19 +1002,14 @@ int vgk_agg_launch(const VgAggLaunch *L, vg_stream_t s) {
     }
 #undef VG_LAUNCH
     vg_prof_end(VG_PROF_AGG, st);
-    cudaFreeAsync(dL, st);
     return check(cudaGetLastError(), "agg launch");
 }
 
 int vgk_agg_merge_spilled_cache(const VgAggLaunch *L, int64_t n, vg_stream_t s) {
     if (n <= 0) return 0;
     cudaStream_t st = (cudaStream_t)s;
-    void *dL = nullptr;
-    if (check(cudaMallocAsync(&dL, sizeof(VgAggLaunch), st), "merge args")) return -1;
-    cudaMemcpyAsync(dL, L, sizeof(VgAggLaunch), cudaMemcpyHostToDevice, st);
-    merge_spilled_kernel<<<grid_for(n, 256), 256, 0, st>>>((const VgAggLaunch *)dL, n);
+    merge_spilled_kernel<<<grid_for(n, 256), 256, 0, st>>>(*L, n);
     vg_launch_counter++;
-    cudaFreeAsync(dL, st);
     return check(cudaGetLastError(), "merge spilled");
 }
 
@@ -998,12 +1024,8 @@ int vgk_group_table_rehash(const VgGroupTable *from, const VgGroupTable *to, int
     R.n_accs = n_accs;
     for (int k = 0; k < n_keys; k++) R.key_types[k] = key_types[k];
     for (int a = 0; a < n_accs; a++) R.cls[a] = acc_cls[a];
-    void *dR = nullptr;
-    if (check(cudaMallocAsync(&dR, sizeof(R), st), "rehash args")) return -1;
-    cudaMemcpyAsync(dR, &R, sizeof(R), cudaMemcpyHostToDevice, st);
-    rehash_kernel<<<grid_for(from->cap, 256), 256, 0, st>>>((const RehashArgs *)dR);
+    rehash_kernel<<<grid_for(from->cap, 256), 256, 0, st>>>(R);
     vg_launch_counter++;
-    cudaFreeAsync(dR, st);
     return check(cudaGetLastError(), "rehash");
 }
 
@@ -1023,7 +1045,7 @@ int vgk_group_finish(const VgGroupTable *gt, int n_keys, const int32_t *key_type
                      uint64_t **d_key_out, uint32_t **d_key_valid, double **d_out,
                      uint32_t **d_out_valid, uint32_t *d_warn, vg_stream_t s) {
     if (n_groups <= 0) return 0;
-    if (n_out > VG_MAX_ACCS * 2 || n_keys > VG_MAX_KEYS) {
+    if (n_out > VG_MAX_OUTS || n_keys > VG_MAX_KEYS) {
         snprintf(g_err, sizeof(g_err), "finish: too many outputs");
         return -1;
     }

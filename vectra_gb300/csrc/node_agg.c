@@ -47,7 +47,7 @@ typedef struct {
     VgValue key[VG_MAX_KEYS];
     int32_t key_type[VG_MAX_KEYS];
     VgAccSpec acc[VG_MAX_ACCS];
-    VgFinish fin[VG_MAX_ACCS];
+    VgFinish fin[VG_MAX_OUTS];
     int fail;                 /* resolution failed: not fusable */
 } Plan;
 
@@ -342,12 +342,22 @@ static void run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_log
         vg_d2h(&used, T->gt.n_used, 4);
         vg_sync();
         if (err & (VG_ERR_WAIT | VG_ERR_PROG)) vg_fail("group-agg kernel error (code %u)", err);
-        if (err & VG_ERR_FULL) {
-            /* the spill lists themselves overflowed: nothing was lost that
-             * we cannot recover only if nothing spilled; give up loudly */
+        if (err & (VG_ERR_FULL | VG_ERR_SPILL))
             vg_fail("group-agg: spill capacity exceeded (%u rows, %u entries)", c[0], c[1]);
+        if (c[0] == 0 && c[1] == 0) {
+            /* keep the load factor at or below 1/2 for the next batch */
+            if ((int64_t)used * 2 > T->gt.cap) {
+                Table T2;
+                table_alloc(&T2, P, pow2_at_least(4 * (int64_t)used));
+                int32_t cls[VG_MAX_ACCS];
+                for (int a = 0; a < P->n_accs; a++) cls[a] = P->acc[a].cls;
+                vg_check_rc(vgk_group_table_rehash(&T->gt, &T2.gt, P->n_keys, P->key_type, cls, P->n_accs,
+                                                   vg_stream()), "group table rehash");
+                vg_dfree(T->block);
+                *T = T2;
+            }
+            break;
         }
-        if (c[0] == 0 && c[1] == 0) break;
         /* grow the table, move the groups, then replay what spilled */
         int64_t ncap = pow2_at_least(2 * ((int64_t)used + c[0] + c[1]) + 1024);
         Table T2;
@@ -395,8 +405,8 @@ static VecBatch *emit_result(VgAgg *A, Plan *P, Table *T) {
     char *blk = (char *)vg_dmalloc(per * (size_t)(n_out ? n_out : 1) + 256);
     uint64_t *kout[VG_MAX_KEYS];
     uint32_t *kval[VG_MAX_KEYS];
-    double *aout[VG_MAX_ACCS];
-    uint32_t *aval[VG_MAX_ACCS];
+    double *aout[VG_MAX_OUTS];
+    uint32_t *aval[VG_MAX_OUTS];
     for (int k = 0; k < ga->n_keys; k++) {
         kout[k] = (uint64_t *)(blk + per * (size_t)k);
         kval[k] = (uint32_t *)((char *)kout[k] + a256((size_t)ng * 8 + 8));
@@ -532,7 +542,7 @@ GroupAggNode *group_agg_node_create(VecNode *child, int n_keys, char **key_names
                                     AggSpec *agg_specs, const char *temp_dir) {
     vg_ensure_init();
     if (n_keys > VG_MAX_KEYS) vg_fail("GPU group-agg supports at most %d key columns", VG_MAX_KEYS);
-    if (n_aggs > VG_MAX_ACCS) vg_fail("GPU group-agg supports at most %d aggregates", VG_MAX_ACCS);
+    if (n_aggs > VG_MAX_OUTS) vg_fail("GPU group-agg supports at most %d aggregates", VG_MAX_OUTS);
     const VecSchema *cs = &child->output_schema;
     for (int k = 0; k < n_keys; k++) {
         int idx = vg_schema_find(cs, key_names[k]);

@@ -36,7 +36,8 @@ typedef struct {
 #define VG_MAX_COLS   24
 #define VG_MAX_TERMS  12
 #define VG_MAX_KEYS   4
-#define VG_MAX_ACCS   12
+#define VG_MAX_ACCS   12   /* distinct accumulators per group-agg */
+#define VG_MAX_OUTS   32   /* aggregate outputs per group-agg */
 #define VG_MAX_INSNS  48
 
 /* ------------------------------------------------------------------ */
@@ -171,6 +172,7 @@ typedef struct {
 #define VG_ERR_WAIT   1u     /* a bounded wait expired */
 #define VG_ERR_FULL   2u     /* a table or spill list was full */
 #define VG_ERR_PROG   4u     /* malformed expression program */
+#define VG_ERR_SPILL  8u     /* a spill list overflowed */
 
 typedef struct {
     int64_t   cap;           /* power of two */
