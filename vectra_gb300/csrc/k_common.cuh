@@ -87,11 +87,37 @@ VG_DEV uint64_t hash_keys(const uint64_t *k, int nk, uint32_t nm) {
     return vg_mix64(h);
 }
 
+// one 16-byte slot read through the read-only path
+VG_DEV VgJSlot jt_slot(const VgJSlot *p) {
+    ulonglong2 v = __ldg((const ulonglong2 *)p);
+    VgJSlot s;
+    s.key = v.x;
+    s.start = (int32_t)(uint32_t)v.y;
+    s.count = (int32_t)(uint32_t)(v.y >> 32);
+    return s;
+}
+
 // Join table lookup: keys are normalised words of the common key types.
 VG_DEV bool jt_lookup(const VgJoinTable &jt, const uint64_t *k, int32_t &start, int32_t &count) {
     uint64_t h = hash_keys(k, jt.n_keys, 0);
     const int64_t mask = jt.cap - 1;
     int64_t slot = (int64_t)(h & (uint64_t)mask);
+    if (jt.slots) {
+        if (k[0] == VG_JEMPTY) {
+            VgJSlot e = jt_slot(jt.slots + jt.cap);
+            if (e.count <= 0) return false;
+            start = e.start;
+            count = e.count;
+            return true;
+        }
+        for (int64_t probe = 0; probe < jt.cap; probe++) {
+            VgJSlot e = jt_slot(jt.slots + slot);
+            if (e.key == k[0]) { start = e.start; count = e.count; return true; }
+            if (e.key == VG_JEMPTY) return false;
+            slot = (slot + 1) & mask;
+        }
+        return false;
+    }
     for (int64_t probe = 0; probe < jt.cap; probe++) {
         uint32_t st = __ldg(jt.state + slot);
         if (st == 0) return false;

@@ -79,7 +79,7 @@ __host__ __device__ inline void make_lay(const VgAggLaunch &L, uint64_t S, Lay &
     c.first = off; off = al8(off + (L.track_first ? 8 * S : 0));
     for (int a = 0; a < L.n_accs; a++) {
         int cls = L.acc[a].cls;
-        c.cnt[a] = off; off = al8(off + 8 * S);
+        c.cnt[a] = off; off = al8(off + 4 * S);
         c.val[a] = off; off = al8(off + (has_val(cls) ? 8 * S : 0));
         c.flags[a] = off; off = al8(off + 4 * S);
         c.base[a] = off; off = al8(off + (cls == VG_ACC_SUM_F64 ? 4 * S : 0));
@@ -88,15 +88,47 @@ __host__ __device__ inline void make_lay(const VgAggLaunch &L, uint64_t S, Lay &
     c.total = off;
 }
 
-VG_DEV AccPtrs lay_ptrs(char *base, const Lay &c, int a) {
-    AccPtrs p;
-    p.cnt = (uint64_t *)(base + c.cnt[a]);
-    p.val = (int64_t *)(base + c.val[a]);
+// Cache-format state (shared-memory cache and spill area).  Shared memory
+// has fast native 32-bit atomics but emulates 64-bit adds, so 64-bit
+// quantities are kept as (u32 lo, i32 hi) word pairs: value = hi * 2^32 + lo,
+// with carries / borrows of lo applied to hi, which is exact.
+struct CPtrs {
+    uint32_t *cnt;      // count
+    uint32_t *vlo;      // int sum, low words (val pair) ...
+    int32_t *vhi;       // ... and high words; min/max use the pair as one int64
+    int64_t *val64;
+    uint32_t *flags;
+    int32_t *base;
+    uint32_t *wlo;      // [kWin][S] window digits, low words
+    int32_t *whi;       // [kWin][S] window digits, high words
+};
+
+VG_DEV CPtrs cptrs(char *base, const Lay &c, int a, int64_t S) {
+    CPtrs p;
+    p.cnt = (uint32_t *)(base + c.cnt[a]);
+    p.vlo = (uint32_t *)(base + c.val[a]);
+    p.vhi = (int32_t *)(base + c.val[a] + 4 * S);
+    p.val64 = (int64_t *)(base + c.val[a]);
     p.flags = (uint32_t *)(base + c.flags[a]);
     p.base = (int32_t *)(base + c.base[a]);
-    p.win = (int64_t *)(base + c.win[a]);
-    p.fs = p.fc = nullptr;
+    p.wlo = (uint32_t *)(base + c.win[a]);
+    p.whi = (int32_t *)(base + c.win[a] + 4 * S * kWin);
     return p;
+}
+
+// adds a signed 64-bit value to a (lo, hi) pair with 32-bit atomics
+VG_DEV void pair_add(uint32_t *lo, int32_t *hi, int64_t v) {
+    uint32_t vl = (uint32_t)(uint64_t)v;
+    int32_t vh = (int32_t)(v >> 32);      // v = vh * 2^32 + vl
+    if (vl) {
+        uint32_t old = atomicAdd(lo, vl);
+        if ((uint32_t)(old + vl) < old) vh += 1;   // carry out of the low word
+    }
+    if (vh) atomicAdd(hi, vh);
+}
+
+VG_DEV int64_t pair_get(const uint32_t *lo, const int32_t *hi) {
+    return (int64_t)(((uint64_t)(int64_t)*hi << 32) + (uint64_t)*lo);
 }
 
 // Double-sum state of the global table lives in lacc[a]:
@@ -153,6 +185,68 @@ VG_DEV void fallback_add(double *s, double *c, double x) {
 VG_DEV void set_flags(uint32_t *f, uint32_t bits) {
     uint32_t cur = *(volatile uint32_t *)f;
     if ((cur & bits) != bits) atomicOr(f, bits);
+}
+
+// Window add for the cache: digits into (lo, hi) pairs.  False when the
+// value falls outside the window.
+VG_DEV bool cwin_add(int32_t *base_p, uint32_t *wlo, int32_t *whi, int64_t S, const VgDigits &d) {
+    int b = *(volatile int *)base_p;
+    if (b == kBaseUnset) {
+        int want = d.lo - 2;
+        if (want < 0) want = 0;
+        if (want > VG_LACC_WORDS - kWin) want = VG_LACC_WORDS - kWin;
+        int prev = atomicCAS((int *)base_p, kBaseUnset, want);
+        b = (prev == kBaseUnset) ? want : prev;
+    }
+    int rel = d.lo - b;
+    int need = d.d2 ? 3 : 2;
+    if (rel < 0 || rel + need > kWin) return false;
+    if (d.d0) pair_add(wlo + (int64_t)rel * S, whi + (int64_t)rel * S, d.d0);
+    if (d.d1) pair_add(wlo + (int64_t)(rel + 1) * S, whi + (int64_t)(rel + 1) * S, d.d1);
+    if (d.d2) pair_add(wlo + (int64_t)(rel + 2) * S, whi + (int64_t)(rel + 2) * S, d.d2);
+    return true;
+}
+
+// One input value into accumulator A of cache slot `slot`; false if the
+// value must go to the global table instead (outside the window).
+VG_DEV bool cache_update(const VgAccSpec &A, const CPtrs &P, int64_t S, int64_t slot, InVal x) {
+    const int cls = A.cls;
+    if (cls == VG_ACC_COUNT_ALL) { atomicAdd(P.cnt + slot, 1u); return true; }
+    if (cls == VG_ACC_COUNT_VALID) { if (x.ok) atomicAdd(P.cnt + slot, 1u); return true; }
+    if (!x.ok) {
+        if (!A.na_rm) set_flags(P.flags + slot, 1u);
+        return true;
+    }
+    switch (cls) {
+    case VG_ACC_SUM_I64:
+        atomicAdd(P.cnt + slot, 1u);
+        pair_add(P.vlo + slot, P.vhi + slot, (int64_t)x.bits);
+        return true;
+    case VG_ACC_SUM_F64: {
+        VgDigits d = vg_split_double(x.bits);
+        if (d.special) set_flags(P.flags + slot, d.special);
+        else if (d.lo >= 0 && !cwin_add(P.base + slot, P.wlo + slot, P.whi + slot, S, d)) return false;
+        atomicAdd(P.cnt + slot, 1u);
+        return true;
+    }
+    case VG_ACC_MIN_I64:
+        atomicMin((long long *)(P.val64 + slot), (long long)x.bits);
+        set_flags(P.flags + slot, 2u);
+        return true;
+    case VG_ACC_MAX_I64:
+        atomicMax((long long *)(P.val64 + slot), (long long)x.bits);
+        set_flags(P.flags + slot, 2u);
+        return true;
+    case VG_ACC_MIN_F64:
+    case VG_ACC_MAX_F64:
+        if (vg_is_nan_bits(x.bits)) { set_flags(P.flags + slot, 2u | 4u); return true; }
+        if (cls == VG_ACC_MIN_F64) atomicMin((long long *)(P.val64 + slot), (long long)vg_ord(x.bits));
+        else atomicMax((long long *)(P.val64 + slot), (long long)vg_ord(x.bits));
+        set_flags(P.flags + slot, 2u);
+        return true;
+    default:
+        return true;
+    }
 }
 
 // One input value into accumulator A of a slot.  kGlobal selects the
@@ -405,17 +499,18 @@ VG_DEV bool merge_entry(const VgAggLaunch &L, char *base, const Lay &c, int64_t 
         atomicMin((unsigned long long *)(L.gt.first_row + g), ((unsigned long long *)(base + c.first))[i]);
     for (int a = 0; a < L.n_accs; a++) {
         const int cls = L.acc[a].cls;
-        AccPtrs sp = lay_ptrs(base, c, a);
+        CPtrs sp = cptrs(base, c, a, S);
         AccPtrs gp = global_ptrs(L.gt, a);
         if (sp.cnt[i]) atomicAdd((unsigned long long *)(gp.cnt + g), (unsigned long long)sp.cnt[i]);
         uint32_t f = sp.flags[i];
         if (f) atomicOr(gp.flags + g, f);
         if (cls == VG_ACC_SUM_I64) {
-            if (sp.val[i]) atomicAdd((unsigned long long *)(gp.val + g), (unsigned long long)sp.val[i]);
+            int64_t v = pair_get(sp.vlo + i, sp.vhi + i);
+            if (v) atomicAdd((unsigned long long *)(gp.val + g), (unsigned long long)v);
         } else if (acc_is_min(cls)) {
-            if (f & 2u) atomicMin((long long *)(gp.val + g), (long long)sp.val[i]);
+            if (f & 2u) atomicMin((long long *)(gp.val + g), (long long)sp.val64[i]);
         } else if (acc_is_max(cls)) {
-            if (f & 2u) atomicMax((long long *)(gp.val + g), (long long)sp.val[i]);
+            if (f & 2u) atomicMax((long long *)(gp.val + g), (long long)sp.val64[i]);
         } else if (cls == VG_ACC_SUM_F64) {
             int bs = sp.base[i];
             if (bs == kBaseUnset) continue;
@@ -428,7 +523,7 @@ VG_DEV bool merge_entry(const VgAggLaunch &L, char *base, const Lay &c, int64_t 
                 bg = (prev == kBaseUnset) ? bs : prev;
             }
             for (int w = 0; w < kWin; w++) {
-                int64_t v = sp.win[(int64_t)w * S + i];
+                int64_t v = pair_get(sp.wlo + (int64_t)w * S + i, sp.whi + (int64_t)w * S + i);
                 if (!v) continue;
                 int rel = bs + w - bg;
                 if (rel >= 0 && rel < kWin) {
@@ -458,15 +553,19 @@ VG_DEV void spill_entry(const VgAggLaunch &L, char *sm, const Lay &c, int64_t S,
         ((uint64_t *)(d + sl.keys))[(int64_t)k * T + j] = ((const uint64_t *)(sm + c.keys))[(int64_t)k * S + i];
     if (L.track_first) ((uint64_t *)(d + sl.first))[j] = ((const uint64_t *)(sm + c.first))[i];
     for (int a = 0; a < L.n_accs; a++) {
-        AccPtrs sp = lay_ptrs(sm, c, a);
-        AccPtrs dp = lay_ptrs(d, sl, a);
+        CPtrs sp = cptrs(sm, c, a, S);
+        CPtrs dp = cptrs(d, sl, a, T);
         dp.cnt[j] = sp.cnt[i];
         dp.flags[j] = sp.flags[i];
         int cls = L.acc[a].cls;
-        if (has_val(cls)) dp.val[j] = sp.val[i];
+        if (cls == VG_ACC_SUM_I64) { dp.vlo[j] = sp.vlo[i]; dp.vhi[j] = sp.vhi[i]; }
+        else if (has_val(cls)) dp.val64[j] = sp.val64[i];
         if (cls == VG_ACC_SUM_F64) {
             dp.base[j] = sp.base[i];
-            for (int w = 0; w < kWin; w++) dp.win[(int64_t)w * T + j] = sp.win[(int64_t)w * S + i];
+            for (int w = 0; w < kWin; w++) {
+                dp.wlo[(int64_t)w * T + j] = sp.wlo[(int64_t)w * S + i];
+                dp.whi[(int64_t)w * T + j] = sp.whi[(int64_t)w * S + i];
+            }
         }
     }
 }
@@ -475,16 +574,16 @@ VG_DEV void init_slot(const VgAggLaunch &L, char *base, const Lay &c, int64_t S,
     ((uint32_t *)(base + c.state))[i] = 0;
     if (L.track_first) ((uint64_t *)(base + c.first))[i] = ~0ull;
     for (int a = 0; a < L.n_accs; a++) {
-        AccPtrs p = lay_ptrs(base, c, a);
+        CPtrs p = cptrs(base, c, a, S);
         p.cnt[i] = 0;
         p.flags[i] = 0;
         int cls = L.acc[a].cls;
-        if (cls == VG_ACC_SUM_I64) p.val[i] = 0;
-        else if (acc_is_min(cls)) p.val[i] = 0x7FFFFFFFFFFFFFFFll;
-        else if (acc_is_max(cls)) p.val[i] = (int64_t)0x8000000000000000ull;
+        if (cls == VG_ACC_SUM_I64) { p.vlo[i] = 0; p.vhi[i] = 0; }
+        else if (acc_is_min(cls)) p.val64[i] = 0x7FFFFFFFFFFFFFFFll;
+        else if (acc_is_max(cls)) p.val64[i] = (int64_t)0x8000000000000000ull;
         if (cls == VG_ACC_SUM_F64) {
             p.base[i] = kBaseUnset;
-            for (int w = 0; w < kWin; w++) p.win[(int64_t)w * S + i] = 0;
+            for (int w = 0; w < kWin; w++) { p.wlo[(int64_t)w * S + i] = 0; p.whi[(int64_t)w * S + i] = 0; }
         }
     }
 }
@@ -620,7 +719,7 @@ agg_kernel(const __grid_constant__ VgAggLaunch L, int64_t n_logical) {
                     const VgAccSpec &A = L.acc[a];
                     InVal v = (A.cls == VG_ACC_COUNT_ALL) ? InVal{0, true}
                                                           : eval_value(A.in, L.pcols, L.bcols, pr, br);
-                    if (acc_update<false>(A, lay_ptrs(sm, cl, a), S, found, v)) continue;
+                    if (cache_update(A, cptrs(sm, cl, a, S), S, found, v)) continue;
                     // value outside the shared window: this update goes to
                     // the global table
                     int64_t g = gt_find_insert(L.gt, k, nk, kt, nm, h);

@@ -1,13 +1,16 @@
-// k_join.cu -- hash-join build and probe on sm_103a.
+// k_hashjoin.cu -- hash-join build and probe on sm_103a.
 //
 // Replaces the reference's JoinHT (src/join.c:23-150), join_build
 // (src/join.c:156-220) and join_probe_one (src/join.c:262-480):
 //  * build: one device pass inserts every non-NA build key into an
-//    open-addressing table (CAS-claimed slots, one slot per distinct key)
-//    and counts rows per key; if any key repeats, a stable radix sort of
-//    (slot, build row) lays each key's rows out in ascending row order, so
-//    the probe can emit them in the reference's descending order (its chains
-//    are built by head insertion, src/join.c:55-56);
+//    open-addressing table with one slot per distinct key and counts rows
+//    per key.  Single-key tables claim 16-byte {key, start, count} slots
+//    with one 64-bit CAS on the key (no locks, no fences; one sector per
+//    probe); composite keys use per-slot locks.  If any key repeats, a
+//    stable radix sort of (slot, build row) lays each key's rows out in
+//    ascending row order, so the probe can emit them in the reference's
+//    descending order (its chains are built by head insertion,
+//    src/join.c:55-56);
 //  * probe: count -> exclusive scan -> emit (probe row, build row) pairs in
 //    the reference's output order: probe rows in order, matches in
 //    descending build row, then (LEFT/FULL) the unmatched probe rows of the
@@ -63,7 +66,9 @@ struct KeyArgs {
 
 // normalised key words of row r; false if any key is NA or NaN (never matches)
 VG_DEV bool key_words(const KeyArgs &K, int64_t r, uint64_t *k) {
-    for (int i = 0; i < K.n_keys; i++) {
+#pragma unroll
+    for (int i = 0; i < VG_MAX_KEYS; i++) {
+        if (i >= K.n_keys) break;
         const VgCol &c = K.cols[i];
         if (!vg_valid(c, r)) return false;
         uint64_t b = vg_load_bits(c, r);
@@ -74,58 +79,97 @@ VG_DEV bool key_words(const KeyArgs &K, int64_t r, uint64_t *k) {
     return true;
 }
 
+VG_DEV int32_t *jt_start_ptr(const VgJoinTable &jt, int64_t slot) {
+    return jt.slots ? &jt.slots[slot].start : jt.start + slot;
+}
+VG_DEV int32_t *jt_count_ptr(const VgJoinTable &jt, int64_t slot) {
+    return jt.slots ? &jt.slots[slot].count : jt.count + slot;
+}
+
 __global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters) {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < jt.cap; i += stride) {
-        jt.state[i] = 0;
-        jt.count[i] = 0;
+    const int64_t n = jt.slots ? jt.cap + 1 : jt.cap;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (jt.slots) {
+            jt.slots[i].key = VG_JEMPTY;
+            jt.slots[i].start = 0;
+            jt.slots[i].count = 0;
+        } else {
+            jt.state[i] = 0;
+            jt.count[i] = 0;
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x < 4) counters[threadIdx.x] = 0;
+}
+
+// single key: claim a slot with one CAS on its key word
+VG_DEV int64_t insert_single(const VgJoinTable &jt, uint64_t k, uint32_t *counters) {
+    if (k == VG_JEMPTY) return jt.cap;      // the marker value has its own slot
+    const int64_t mask = jt.cap - 1;
+    int64_t slot = (int64_t)(hash_keys(&k, 1, 0) & (uint64_t)mask);
+    for (int64_t probe = 0; probe < jt.cap; probe++) {
+        unsigned long long *kp = (unsigned long long *)&jt.slots[slot].key;
+        unsigned long long cur = *(volatile unsigned long long *)kp;
+        if (cur == k) return slot;
+        if (cur == VG_JEMPTY) {
+            unsigned long long prev = atomicCAS(kp, VG_JEMPTY, k);
+            if (prev == VG_JEMPTY || prev == k) return slot;
+        }
+        slot = (slot + 1) & mask;
+    }
+    atomicOr(counters + 2, VG_ERR_FULL);
+    return -1;
+}
+
+// composite keys: per-slot lock (0 empty, 1 being written, 2 ready)
+VG_DEV int64_t insert_multi(const VgJoinTable &jt, const uint64_t *k, int nk, uint32_t *counters) {
+    const int64_t mask = jt.cap - 1;
+    int64_t slot = (int64_t)(hash_keys(k, nk, 0) & (uint64_t)mask);
+    for (int64_t probe = 0; probe < jt.cap; probe++) {
+        uint32_t st = *(volatile uint32_t *)(jt.state + slot);
+        if (st == 0) {
+            uint32_t prev = atomicCAS(jt.state + slot, 0u, 1u);
+            if (prev == 0u) {
+                for (int i = 0; i < nk; i++) jt.keys[(int64_t)i * jt.cap + slot] = k[i];
+                __threadfence();
+                atomicExch(jt.state + slot, 2u);
+                return slot;
+            }
+            st = prev;
+        }
+        int spins = 0;
+        while (st == 1u) {
+            if (++spins > VG_SPIN_LIMIT) { atomicOr(counters + 2, VG_ERR_WAIT); return -1; }
+            __nanosleep(32);
+            st = *(volatile uint32_t *)(jt.state + slot);
+        }
+        __threadfence();
+        bool eq = true;
+        for (int i = 0; i < nk && eq; i++)
+            eq = *(volatile uint64_t *)(jt.keys + (int64_t)i * jt.cap + slot) == k[i];
+        if (eq) return slot;
+        slot = (slot + 1) & mask;
+    }
+    atomicOr(counters + 2, VG_ERR_FULL);
+    return -1;
 }
 
 // counters: [0] distinct keys, [1] max rows per key, [2] error bits
 __global__ void jt_insert_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t *rslot,
                                  uint32_t *counters) {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int64_t mask = jt.cap - 1;
     for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
         uint64_t k[VG_MAX_KEYS];
         if (!key_words(K, r, k)) { rslot[r] = -1; continue; }
-        uint64_t h = hash_keys(k, K.n_keys, 0);
-        int64_t slot = (int64_t)(h & (uint64_t)mask);
-        int64_t found = -1;
-        for (int64_t probe = 0; probe < jt.cap && found < 0; probe++) {
-            uint32_t st = *(volatile uint32_t *)(jt.state + slot);
-            if (st == 0) {
-                uint32_t prev = atomicCAS(jt.state + slot, 0u, 1u);
-                if (prev == 0u) {
-                    for (int i = 0; i < K.n_keys; i++) jt.keys[(int64_t)i * jt.cap + slot] = k[i];
-                    __threadfence();
-                    atomicExch(jt.state + slot, 2u);
-                    atomicAdd(counters + 0, 1u);
-                    found = slot;
-                    break;
-                }
-                st = prev;
-            }
-            int spins = 0;
-            while (st == 1u) {
-                if (++spins > VG_SPIN_LIMIT) { atomicOr(counters + 2, VG_ERR_WAIT); break; }
-                __nanosleep(32);
-                st = *(volatile uint32_t *)(jt.state + slot);
-            }
-            if (st != 2u) break;
-            __threadfence();
-            bool eq = true;
-            for (int i = 0; i < K.n_keys && eq; i++)
-                eq = *(volatile uint64_t *)(jt.keys + (int64_t)i * jt.cap + slot) == k[i];
-            if (eq) { found = slot; break; }
-            slot = (slot + 1) & mask;
+        int64_t found = jt.slots ? insert_single(jt, k[0], counters) : insert_multi(jt, k, K.n_keys, counters);
+        if (found < 0) { rslot[r] = -1; continue; }
+        int32_t old = atomicAdd(jt_count_ptr(jt, found), 1);
+        if (old == 0) {
+            atomicAdd(counters + 0, 1u);
+            *jt_start_ptr(jt, found) = (int32_t)r;   // final when keys are unique
+        } else {
+            atomicMax(counters + 1, (uint32_t)(old + 1));
         }
-        if (found < 0) { atomicOr(counters + 2, VG_ERR_FULL); rslot[r] = -1; continue; }
-        int32_t old = atomicAdd(jt.count + found, 1);
-        atomicMax(counters + 1, (uint32_t)(old + 1));
-        if (old == 0) jt.start[found] = (int32_t)r;   // final when keys are unique
         rslot[r] = (int32_t)found;
     }
 }
@@ -135,17 +179,17 @@ __global__ void pair_keys_kernel(const int32_t *rslot, int64_t n, int64_t cap, u
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
         int32_t s = rslot[r];
-        keys[r] = s < 0 ? (uint64_t)cap : (uint64_t)s;   // NA rows sort last
+        keys[r] = s < 0 ? (uint64_t)cap + 1 : (uint64_t)s;   // NA rows sort last
         vals[r] = (int32_t)r;
     }
 }
 
-__global__ void seg_start_kernel(const uint64_t *keys, int64_t n, int64_t cap, int32_t *start) {
+__global__ void seg_start_kernel(VgJoinTable jt, const uint64_t *keys, int64_t n, int64_t nslots) {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         uint64_t k = keys[i];
-        if (k >= (uint64_t)cap) continue;
-        if (i == 0 || keys[i - 1] != k) start[k] = (int32_t)i;
+        if (k >= (uint64_t)nslots) continue;
+        if (i == 0 || keys[i - 1] != k) *jt_start_ptr(jt, (int64_t)k) = (int32_t)i;
     }
 }
 
@@ -274,7 +318,7 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         K.conv[i] = key_conv[i];
         K.types[i] = jt->key_types[i];
     }
-    { jt_init_kernel<<<grid_for(jt->cap, 256), 256, 0, st>>>(*jt, counters); vg_launch_counter++; }
+    { jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters); vg_launch_counter++; }
     vg_prof_begin(VG_PROF_JOIN_BUILD, st);
         { jt_insert_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(*jt, K, n_build, rslot, counters); vg_launch_counter++; }
         vg_prof_end(VG_PROF_JOIN_BUILD, st);
@@ -294,13 +338,13 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
     // duplicates: stable sort of (slot, row) lays out each key's rows in
     // ascending row order
     int bits = 1;
-    while (((int64_t)1 << bits) <= jt->cap) bits++;
+    while (((int64_t)1 << bits) <= jt->cap + 1) bits++;
     { pair_keys_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(rslot, n_build, jt->cap, pkeys, jt->rows); vg_launch_counter++; }
     if (vgk_sort_pairs(pkeys, jt->rows, n_build, bits, sort_scratch, vgk_sort_pairs_scratch(n), s)) {
         snprintf(g_err, sizeof(g_err), "%s", vgk_sort_last_error());
         return -1;
     }
-    { seg_start_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(pkeys, n_build, jt->cap, jt->start); vg_launch_counter++; }
+    { seg_start_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(*jt, pkeys, n_build, jt->slots ? jt->cap + 1 : jt->cap); vg_launch_counter++; }
     return check(cudaGetLastError(), "join build sort");
 }
 

@@ -115,8 +115,12 @@ static void join_build(VgJoin *j) {
         for (int b = 0; b < nb; b++) {
             int64_t n = bs[b].d_sel ? bs[b].sel_n : bs[b].n_rows;
             if (n == 0) continue;
-            vg_check_rc(vgk_gather_into(&bs[b].cols[c], bs[b].d_sel, n, dv, dm, at, vg_stream()),
-                        "join build gather");
+            if ((at & 31) == 0)   /* word-aligned: whole validity words per warp */
+                vg_check_rc(vgk_gather(&bs[b].cols[c], bs[b].d_sel, n, 0, dv + (size_t)at * elem(rs->col_types[c]),
+                                       dm + at / 32, vg_stream()), "join build gather");
+            else
+                vg_check_rc(vgk_gather_into(&bs[b].cols[c], bs[b].d_sel, n, dv, dm, at, vg_stream()),
+                            "join build gather");
             at += n;
         }
         j->B.bcols[c].data = dv;
@@ -129,7 +133,9 @@ static void join_build(VgJoin *j) {
     /* hash table */
     int nk = j->jn.n_keys;
     int64_t tcap = vgk_join_cap(total);
-    size_t tb = a256((size_t)tcap * 4) * 3 + a256((size_t)tcap * 8 * (size_t)nk) + a256((size_t)(total > 0 ? total : 1) * 4) + 256;
+    size_t rows_b = a256((size_t)(total > 0 ? total : 1) * 4);
+    size_t tb = (nk == 1) ? a256((size_t)(tcap + 1) * sizeof(VgJSlot)) + rows_b + 256
+                          : a256((size_t)tcap * 4) * 3 + a256((size_t)tcap * 8 * (size_t)nk) + rows_b + 256;
     char *t = (char *)vg_dmalloc(tb);
     j->table_block = t;
     VgJoinTable *jt = &j->B.jt;
@@ -138,11 +144,16 @@ static void join_build(VgJoin *j) {
     jt->n_keys = nk;
     for (int k = 0; k < nk; k++) jt->key_types[k] = j->key_type[k];
     size_t o = 0;
-    jt->state = (uint32_t *)(t + o); o += a256((size_t)tcap * 4);
-    jt->start = (int32_t *)(t + o); o += a256((size_t)tcap * 4);
-    jt->count = (int32_t *)(t + o); o += a256((size_t)tcap * 4);
-    jt->keys = (uint64_t *)(t + o); o += a256((size_t)tcap * 8 * (size_t)nk);
-    jt->rows = (int32_t *)(t + o); o += a256((size_t)(total > 0 ? total : 1) * 4);
+    if (nk == 1) {
+        /* one 16-byte {key, start, count} slot per key, claimed lock-free */
+        jt->slots = (VgJSlot *)(t + o); o += a256((size_t)(tcap + 1) * sizeof(VgJSlot));
+    } else {
+        jt->state = (uint32_t *)(t + o); o += a256((size_t)tcap * 4);
+        jt->start = (int32_t *)(t + o); o += a256((size_t)tcap * 4);
+        jt->count = (int32_t *)(t + o); o += a256((size_t)tcap * 4);
+        jt->keys = (uint64_t *)(t + o); o += a256((size_t)tcap * 8 * (size_t)nk);
+    }
+    jt->rows = (int32_t *)(t + o); o += rows_b;
     jt->err = (uint32_t *)(t + o);
     jt->n_build = total;
     VgCol kc[VG_MAX_KEYS];

@@ -191,15 +191,26 @@ typedef struct {
 
 /* Join hash table over the build side (keys unique per slot; rows of a key
  * listed in ascending build-row order in rows[start .. start+count)). */
+/* Single-key join slot: one 16-byte sector per probe.  key == VG_JEMPTY
+ * marks a free slot; the one key equal to that marker (if any) lives in
+ * the extra slot at index cap. */
+typedef struct {
+    uint64_t key;
+    int32_t  start;
+    int32_t  count;
+} VgJSlot;
+#define VG_JEMPTY 0x8000000000000000ull
+
 typedef struct {
     int64_t   cap;           /* power of two */
     int32_t   n_keys;
     int32_t   key_types[VG_MAX_KEYS];
-    uint32_t *state;
-    uint64_t *keys;          /* [n_keys][cap] */
-    int32_t  *start;
-    int32_t  *count;
-    int32_t  *rows;          /* n_build entries */
+    VgJSlot  *slots;         /* single-key tables: cap + 1 slots */
+    uint32_t *state;         /* composite-key tables: slot locks ... */
+    uint64_t *keys;          /* ... [n_keys][cap] key words ... */
+    int32_t  *start;         /* ... first position in rows ... */
+    int32_t  *count;         /* ... rows with this key */
+    int32_t  *rows;          /* n_build entries, or NULL when keys are unique */
     int64_t   n_build;
     uint32_t *err;
 } VgJoinTable;
