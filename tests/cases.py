@@ -242,6 +242,26 @@ def ja_join_agg(E, temp_dir):       # the benchmark plan, small: left_join then 
     return a
 
 
+def ja_dense_keys(E, temp_dir):     # join + aggregate keyed on a small-range build-side column
+    rng = np.random.default_rng(17)
+    nf, nd = 7001, 257
+    ids = rng.permutation(nd) + 1
+    fact = {"key": (rng.integers(1, nd + 30, nf), rng.random(nf) > 0.02),
+            "value": (rng.normal(0, 10, nf), rng.random(nf) > 0.03),
+            "q": rng.integers(-5, 5, nf)}
+    dims = [{"id": ids, "grp": (rng.integers(-40, -20, nd), rng.random(nd) > 0.1), "weight": rng.random(nd)},
+            {"id": ids, "grp": (rng.integers(0, 3, nd), np.zeros(nd, bool)), "weight": rng.random(nd)}]
+    out = []
+    for dim in dims:
+        for kind in ("left_join", "inner_join"):
+            out += (getattr(tbl(E, fact, batch_rows=2000).filter(col("q") > -3), kind)(
+                        tbl(E, dim, batch_rows=100), {"key": "id"})
+                    .group_by("grp").summarise(temp_dir=temp_dir, s=("sum", "value"),
+                                               m=("mean", col("value") * col("weight"), True),
+                                               lo=("min", "q"), n=("n",)).batches())
+    return out
+
+
 # ---------------------------------------------------------------------------
 # seeded random cases
 # ---------------------------------------------------------------------------
@@ -281,7 +301,8 @@ def r_join(E, seed, n, batch_rows, kind):
 FILTER_CASES = [f_simple, f_equality, f_and_or_not, f_na_dropped, f_is_na, f_kleene, f_double_filter,
                 f_empty, f_general_expr, f_int_vs_double_literal]
 GROUP_CASES = [g_basic, g_na_key, g_multi_key, g_na_semantics, g_int_sum_double, g_resize_200,
-               g_filter_then_group, g_ungrouped, g_nested_expr, g_bool_and_double_keys, ja_join_agg]
+               g_filter_then_group, g_ungrouped, g_nested_expr, g_bool_and_double_keys, ja_join_agg,
+               ja_dense_keys]
 JOIN_CASES = [j_inner_left_semi_anti, j_duplicates, j_na_keys, j_suffix, j_coerce, j_streaming,
               j_after_filter, j_full]
 

@@ -18,7 +18,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvgpu.so")
 
-CU_SOURCES = ["k_filter.cu", "k_groupby.cu", "k_sort.cu", "k_hashjoin.cu", "k_prof.cu"]
+CU_SOURCES = ["k_groupby_fastj.cu", "k_groupby_fast.cu", "k_groupby.cu", "k_filter.cu", "k_sort.cu", "k_hashjoin.cu",
+              "k_prof.cu"]
 C_SOURCES = ["runtime.c", "compile.c", "source.c", "node_filter.c",
              "node_project.c", "node_agg.c", "node_join.c"]
 

@@ -397,6 +397,40 @@ bool carve(void *base, size_t bytes, int64_t n_logical, size_t args_bytes, Filte
     return off <= bytes;
 }
 
+
+// min, max and number of the valid values of an int64 column:
+// out[0] = min, out[1] = max, out[2] = count (out preset by minmax_init_kernel)
+__global__ void minmax_init_kernel(long long *out) {
+    out[0] = 0x7FFFFFFFFFFFFFFFll;
+    out[1] = (long long)0x8000000000000000ull;
+    out[2] = 0;
+}
+
+__global__ void minmax_i64_kernel(VgCol c, int64_t n, long long *out) {
+    long long lo = 0x7FFFFFFFFFFFFFFFll, hi = (long long)0x8000000000000000ull, cnt = 0;
+    const long long *v = (const long long *)c.data;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        if (!vg_valid(c, r)) continue;
+        long long x = v[r];
+        lo = x < lo ? x : lo;
+        hi = x > hi ? x : hi;
+        cnt++;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        long long l2 = __shfl_xor_sync(0xFFFFFFFFu, lo, o);
+        long long h2 = __shfl_xor_sync(0xFFFFFFFFu, hi, o);
+        cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, o);
+        lo = l2 < lo ? l2 : lo;
+        hi = h2 > hi ? h2 : hi;
+    }
+    if ((threadIdx.x & 31) == 0 && cnt > 0) {
+        atomicMin(out + 0, lo);
+        atomicMax(out + 1, hi);
+        atomicAdd((unsigned long long *)out + 2, (unsigned long long)cnt);
+    }
+}
+
 template <bool kUseProg>
 int run_filter(const void *args, size_t args_bytes, int64_t n_logical, const int32_t *d_sel_in,
                int32_t *d_sel_out, int64_t *h_count, void *d_scratch, size_t scratch_bytes,
@@ -515,6 +549,14 @@ int vgk_gather_into(const VgCol *col, const int32_t *d_idx, int64_t n, void *d_o
     cudaStream_t st = (cudaStream_t)s;
     { gather_into_kernel<<<grid_for(n, 256), 256, 0, st>>>(*col, d_idx, n, d_out, d_out_valid, row0); vg_launch_counter++; }
     return check(cudaGetLastError(), "gather into");
+}
+
+int vgk_col_minmax_i64(const VgCol *col, int64_t n, int64_t *d_out, int64_t *h_out, vg_stream_t s) {
+    cudaStream_t st = (cudaStream_t)s;
+    { minmax_init_kernel<<<1, 1, 0, st>>>((long long *)d_out); vg_launch_counter++; }
+    if (n > 0) { minmax_i64_kernel<<<grid_for(n, 256), 256, 0, st>>>(*col, n, (long long *)d_out); vg_launch_counter++; }
+    if (check(cudaMemcpyAsync(h_out, d_out, 24, cudaMemcpyDeviceToHost, st), "column min/max")) return -1;
+    return check(cudaStreamSynchronize(st), "column min/max");
 }
 
 }  // extern "C"

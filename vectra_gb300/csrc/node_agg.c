@@ -494,6 +494,34 @@ static VecBatch *agg_next(VecNode *self) {
     for (int a = 0; a < P.n_accs; a++) L->acc[a] = P.acc[a];
     L->track_first = (!A->sorted && P.n_keys > 0);
     L->cache_slots = cache_slots_for(L);
+    /* sum accumulators whose row counts no output reads (no mean) */
+    for (int a = 0; a < P.n_accs; a++) {
+        if (P.acc[a].cls != VG_ACC_SUM_F64 && P.acc[a].cls != VG_ACC_SUM_I64) continue;
+        int counted = 0;
+        for (int o = 0; o < P.n_out; o++)
+            if (P.fin[o].acc == a && P.fin[o].finish != AGG_SUM) counted = 1;
+        if (!counted) L->skip_count_mask |= 1u << a;
+    }
+    /* one int64 group key read straight from a build-side column: if the
+     * build side's values span fewer slots than the cache holds, every
+     * group has a fixed cache slot (key - min; NA in the last one) */
+    if (B && P.n_keys == 1 && L->cache_slots > 0 && P.key[0].op == 0 &&
+        P.key[0].a.side == VG_SIDE_BUILD && P.key[0].a.type == VEC_INT64) {
+        int64_t mm[3];
+        int64_t *d = (int64_t *)vg_dmalloc(256);
+        vg_check_rc(vgk_col_minmax_i64(&L->bcols[P.key[0].a.col], B->jt.n_build, d, mm, vg_stream()),
+                    "build key range");
+        vg_dfree(d);
+        if (mm[2] == 0) {
+            L->dense = 1;
+            L->dense_n = 0;
+            L->dense_min = 0;
+        } else if ((uint64_t)mm[1] - (uint64_t)mm[0] < (uint64_t)(L->cache_slots - 1)) {
+            L->dense = 1;
+            L->dense_n = (int32_t)(mm[1] - mm[0] + 1);
+            L->dense_min = mm[0];
+        }
+    }
 
     Table T;
     table_alloc(&T, &P, 8192);

@@ -255,6 +255,14 @@ typedef struct {
     const int64_t *replay;       /* replay list (pairs as above) or NULL */
     int64_t   replay_n;
     int64_t   batch_idx;         /* probe batch number (join ordering key) */
+    /* Direct-mapped cache for a single int64 key known to lie in
+     * [dense_min, dense_min + dense_n) (a build-side attribute): cache slot
+     * = key - dense_min, slot dense_n holds the NA key.  0 = hashed cache. */
+    int32_t   dense;
+    int32_t   dense_n;
+    int64_t   dense_min;
+    /* Accumulators whose count no output reads (a SUM without MEAN). */
+    uint32_t  skip_count_mask;
 } VgAggLaunch;
 
 /* ------------------------------------------------------------------ */
@@ -289,6 +297,10 @@ int vgk_gather(const VgCol *col, const int32_t *d_idx, int64_t n_out,
  * validity words are zeroed beforehand (any row0; bits are OR-ed in) */
 int vgk_gather_into(const VgCol *col, const int32_t *d_idx, int64_t n, void *d_out,
                     uint32_t *d_out_valid, int64_t row0, vg_stream_t s);
+
+/* min (out[0]), max (out[1]) and count (out[2]) of the valid values of an
+ * int64 column of n rows; d_out: 24 bytes of device scratch, h_out: host */
+int vgk_col_minmax_i64(const VgCol *col, int64_t n, int64_t *d_out, int64_t *h_out, vg_stream_t s);
 
 /* group table */
 int vgk_group_table_init(VgGroupTable *gt, int n_keys, const int32_t *acc_cls,
