@@ -14,8 +14,9 @@ temp_dir, i.e. key-ordered output).
 One step = one whole query.  value: rows/s with the columns resident in HBM
 (device table sources); e2e: the same query fed from page-locked host
 buffers, host->device copies and the result read-back inside the step.
-roofline: the fused probe + aggregate kernel, algorithmic bytes (the fact
-columns it reads, in the reference's layout) over its CUDA-event duration.
+roofline: the fused probe + aggregate kernel, algorithmic bytes (the
+columns it reads, once each in the reference's layout: fact key and value,
+dim category and weight) over its CUDA-event duration.
 cpu_baseline: this repository's CPU restatement of the reference path
 (single-threaded like the reference engine) on a 1/20-scale sample.
 
@@ -299,7 +300,10 @@ def gpu_arm(args, rank, world):
     d2h = 3 * 8 * N_CAT
     peak, peak_kind = measured_peak()
     kernel_ms = agg_ms / agg_launches
-    achieved = fact_b / (kernel_ms * 1e-3) / 1e9
+    # the fused kernel reads the fact columns and two of the three dim columns
+    # (the join build reads the third, id)
+    kernel_b = fact_b + dim_b * 2 // 3
+    achieved = kernel_b / (kernel_ms * 1e-3) / 1e9
     value = rows * world / (ms_step * 1e-3)
     line = {
         "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
@@ -309,9 +313,9 @@ def gpu_arm(args, rank, world):
                    "inputs": "device-resident, larger than L2 (1.87 GB)", "parallelism": "replicas",
                    "output_order": "ascending category (temp_dir given, as from R)"},
         "hbm_gbs_whole_query": (fact_b + dim_b + out_b) / (ms_step * 1e-3) / 1e9,
-        "roofline": {"bound": "hbm", "kernel": "fused left-join probe + project + group-agg (agg_kernel)",
+        "roofline": {"bound": "hbm", "kernel": "fused left-join probe + project + group-agg (agg_fast_kernel)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "algorithmic_bytes_per_launch": fact_b,
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_launch": kernel_b,
                      "kernel_ms": kernel_ms, "traffic": profile_traffic()},
         "join_build_ms": build_ms / max(1, build_n.value),
         "e2e": {"value": rows * world / (e2e_ms * 1e-3), "unit": "rows/s", "ms_per_step": e2e_ms,
