@@ -114,6 +114,39 @@ JoinNode     *vgpu_guard_join(VecNode *left, VecNode *right, JoinKind kind,
                               const char *suffix_y);
 void          vgpu_batch_free(VecBatch *batch);
 
+/* ---- allocation-free filter (no counterpart in the reference) -------- */
+/* For callers that may not allocate device memory during a query: a host
+ * whose device memory is fully reserved by another framework's pool, a
+ * latency-bound serving loop that must never wait on the allocator, or an
+ * embedding with a fixed memory budget.  Every other entry point allocates
+ * its working space (stream-ordered, from the device's default pool).
+ *
+ * Writes the ascending indices of the rows of n_rows device-resident rows
+ * that satisfy `predicate` (filter_node_create's semantics: NA and NaN
+ * comparisons drop the row) to d_sel_out (device, room for n_rows int32),
+ * and their number to *n_selected.  d_data[c]: device int64 / double
+ * values or bool bytes; d_validity[c]: device bitmap in the reference
+ * layout, 4-byte aligned and padded to whole 32-bit words, NULL = all valid
+ * (d_validity itself may be NULL).  Runs on the vgpu_set_stream stream if
+ * one is set, else libvgpu's own stream if the library is initialised,
+ * else the legacy default stream, and synchronises that stream before it
+ * returns.  Returns 0, or -1 with vgpu_last_error set: more than
+ * VGPU_STATIC_MAX_ROWS rows, more than 24 columns, a string column or an
+ * unsupported predicate.
+ *
+ * Working space is one fixed device array of 1 MiB + 64 KiB compiled into
+ * libvgpu; nothing in it needs to be zero beforehand (each call writes
+ * what it reads).  Because that array is shared, calls must not overlap:
+ * two calls at once, from two threads or on two streams, race on it.  The
+ * first call on each device looks up the array's address
+ * (cudaGetSymbolAddress) -- make one call before capturing a stream. */
+#define VGPU_STATIC_MAX_ROWS 8388608LL
+int vgpu_filter_select_static(int n_cols, const char *const *names,
+                              const int *types, const void *const *d_data,
+                              const void *const *d_validity, int64_t n_rows,
+                              const VecExpr *predicate, int32_t *d_sel_out,
+                              int64_t *n_selected);
+
 #ifdef __cplusplus
 }
 #endif

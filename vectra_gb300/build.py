@@ -1,7 +1,9 @@
 """Builds libvgpu.so in-tree: the sm_103a kernels (nvcc) and the C11 host
 layer (gcc), linked into one shared library next to this file.
 
-    python -m vectra_gb300.build        # or vectra_gb300.build.build()
+    python -m vectra_gb300.build             # or vectra_gb300.build.build()
+    python -m vectra_gb300.build --archive   # also libvgpu.a, for linking the
+                                             # nodes into the vectra package
 
 No CMake, no torch extension machinery: a handful of translation units
 compiled in parallel, then one link step.
@@ -17,11 +19,12 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvgpu.so")
+ARCHIVE = os.path.join(HERE, "libvgpu.a")
 
-CU_SOURCES = ["k_groupby_fastj.cu", "k_groupby_fast.cu", "k_groupby.cu", "k_filter.cu", "k_sort.cu", "k_hashjoin.cu",
-              "k_prof.cu"]
+CU_SOURCES = ["k_groupby_fastj.cu", "k_groupby_fast.cu", "k_groupby.cu", "k_filter.cu", "k_sort.cu",
+              "k_hashjoin.cu", "k_prof.cu", "k_static.cu"]
 C_SOURCES = ["runtime.c", "compile.c", "source.c", "node_filter.c",
-             "node_project.c", "node_agg.c", "node_join.c"]
+             "node_project.c", "node_agg.c", "node_join.c", "noalloc.c"]
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -51,8 +54,9 @@ def _stale(obj, srcs):
     return any(os.path.getmtime(s) > t for s in srcs)
 
 
-def build(verbose=False):
-    """Compiles what changed and links libvgpu.so.  Returns its path."""
+def build(verbose=False, archive=False):
+    """Compiles what changed and links libvgpu.so (and, with archive=True,
+    a static libvgpu.a of the same objects).  Returns the .so path."""
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
@@ -80,8 +84,12 @@ def build(verbose=False):
         tmp = LIB + ".tmp"
         _run([_nvcc(), GENCODE, "-shared", "-o", tmp] + objs + ["-cudart", "static"])
         os.replace(tmp, LIB)
+    if archive:
+        if os.path.exists(ARCHIVE):
+            os.remove(ARCHIVE)
+        _run(["ar", "rcs", ARCHIVE] + objs)
     return LIB
 
 
 if __name__ == "__main__":
-    print(build(verbose=True))
+    print(build(verbose=True, archive="--archive" in sys.argv[1:]))

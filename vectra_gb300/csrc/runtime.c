@@ -128,6 +128,14 @@ vg_stream_t vg_stream(void) {
     return (vg_stream_t)(g_use_user ? g_user_stream : g_own_stream);
 }
 
+/* The stream for work that must not initialise the library (the
+ * allocation-free entry point): the caller's stream if one was set, else
+ * the library's own once it exists, else the legacy default stream. */
+vg_stream_t vg_stream_noinit(void) {
+    if (g_use_user) return (vg_stream_t)g_user_stream;
+    return g_inited ? (vg_stream_t)g_own_stream : (vg_stream_t)0;
+}
+
 int vgpu_synchronize(void) {
     if (!g_inited) return 0;
     return cudaStreamSynchronize((cudaStream_t)vg_stream()) == cudaSuccess ? 0 : -1;

@@ -21,6 +21,7 @@ void vg_check_rc(int rc, const char *what);
 /* ---- device memory / stream ---- */
 void vg_ensure_init(void);
 vg_stream_t vg_stream(void);
+vg_stream_t vg_stream_noinit(void);
 void *vg_dmalloc(size_t bytes);          /* stream-ordered, fails loudly */
 void vg_dfree(void *p);
 void vg_h2d(void *dst, const void *src, size_t bytes);
