@@ -23,8 +23,12 @@
 #ifndef VGPU_VECTRA_ABI_H
 #define VGPU_VECTRA_ABI_H
 
+#ifdef __CUDACC_RTC__
+#include "vg_rtc_types.h"   /* run-time compiled device code: no libc headers */
+#else
 #include <stdint.h>
 #include <stddef.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {

@@ -7,6 +7,8 @@ semantics.  Double sums and means: libvgpu returns the correctly rounded
 sum, the oracle (like the reference) a left-to-right sum, so those columns
 are compared with a relative tolerance of 1e-12; test_exact_sums checks the
 GPU against an exactly rounded oracle with no tolerance at all."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -124,6 +126,15 @@ def test_join_agg_exact(G):
         assert out["category"][0][g] == g
         assert out["n"][0][g] == m.sum()
         assert out["s"][0][g] == exact_sum_products(fv[m], ww[m])
+
+
+def test_specialised_kernel_ran(G):
+    """The group cases above ran through the run-time specialised kernel."""
+    import vectra_gb300
+    lib = vectra_gb300.load()
+    lib.vgk_jit_compiles.restype = C.c_ulonglong
+    cases.ja_join_agg(G, "tmp")
+    assert lib.vgk_jit_compiles() > 0
 
 
 def test_unsupported_is_an_error(G):

@@ -1,0 +1,21 @@
+"""The run-time specialised aggregation kernel: representative plan shapes
+are generated and compiled for sm_103a with NVRTC (no device needed), with
+no register spills at the default launch shape."""
+import ctypes as C
+import re
+
+import pytest
+
+
+@pytest.mark.parametrize("shape", [0, 1, 2], ids=["join_dense_sum", "filter_sel_mean", "two_keys_all_accs"])
+def test_generated_kernel_compiles(shape):
+    import vectra_gb300
+    lib = vectra_gb300.load()
+    lib.vgk_jit_error.restype = C.c_char_p
+    regs = C.c_int(-1)
+    rc = lib.vgpu_jit_selftest(shape, C.byref(regs))
+    log = lib.vgk_jit_error().decode()
+    assert rc == 0, log
+    assert 0 < regs.value <= 64, log
+    spills = re.findall(r"(\d+) bytes spill stores", log)
+    assert spills and all(int(x) == 0 for x in spills), log

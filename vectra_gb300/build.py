@@ -21,8 +21,12 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvgpu.so")
 ARCHIVE = os.path.join(HERE, "libvgpu.a")
 
-CU_SOURCES = ["k_groupby_fastj.cu", "k_groupby_fast.cu", "k_groupby.cu", "k_filter.cu", "k_sort.cu",
-              "k_hashjoin.cu", "k_prof.cu", "k_static.cu"]
+CU_SOURCES = ["k_groupby_fastj.cu", "k_groupby_fast.cu", "k_groupby.cu", "jit_agg.cu", "k_filter.cu",
+              "k_sort.cu", "k_hashjoin.cu", "k_prof.cu", "k_static.cu"]
+# headers the run-time compiler needs, embedded into jit_agg.cu's object
+JIT_HEADERS = [("vg_rtc_types.h", CSRC), ("vectra_abi.h", INCLUDE), ("vgpu_internal.h", CSRC),
+               ("k_common.cuh", CSRC), ("k_groupby_dev.cuh", CSRC), ("k_jit_lib.cuh", CSRC),
+               ("k_jit_kernel.cuh", CSRC)]
 C_SOURCES = ["runtime.c", "compile.c", "source.c", "node_filter.c",
              "node_project.c", "node_agg.c", "node_join.c", "noalloc.c"]
 
@@ -54,10 +58,30 @@ def _stale(obj, srcs):
     return any(os.path.getmtime(s) > t for s in srcs)
 
 
+def _write_jit_headers():
+    """vg_jit_headers.inc: the device headers as string literals, for NVRTC."""
+    names, srcs = [], []
+    for name, d in JIT_HEADERS:
+        text = open(os.path.join(d, name)).read()
+        if ")VGJH\"" in text:
+            raise RuntimeError("%s contains the raw-string delimiter" % name)
+        names.append('"%s"' % name)
+        srcs.append('R"VGJH(%s)VGJH"' % text)
+    out = ("// generated by build.py from the device headers; do not edit\n"
+           "static const char *const kJitHeaderNames[] = {%s};\n"
+           "static const char *const kJitHeaderSources[] = {\n%s};\n"
+           "static const int kJitHeaderCount = %d;\n") % (", ".join(names), ",\n".join(srcs), len(names))
+    path = os.path.join(BUILD, "vg_jit_headers.inc")
+    if not os.path.exists(path) or open(path).read() != out:
+        with open(path, "w") as f:
+            f.write(out)
+
+
 def build(verbose=False, archive=False):
     """Compiles what changed and links libvgpu.so (and, with archive=True,
     a static libvgpu.a of the same objects).  Returns the .so path."""
     os.makedirs(BUILD, exist_ok=True)
+    _write_jit_headers()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     jobs = []
@@ -68,7 +92,7 @@ def build(verbose=False, archive=False):
         objs.append(obj)
         if _stale(obj, [src] + headers):
             jobs.append([_nvcc(), GENCODE, "-O3", "-lineinfo", "-std=c++17",
-                         "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE, "-c", src, "-o", obj])
+                         "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE, "-I", BUILD, "-c", src, "-o", obj])
     for f in C_SOURCES:
         src = os.path.join(CSRC, f)
         obj = os.path.join(BUILD, f + ".o")
@@ -82,7 +106,9 @@ def build(verbose=False, archive=False):
                 sys.stderr.write(r.stdout + r.stderr)
     if jobs or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
-        _run([_nvcc(), GENCODE, "-shared", "-o", tmp] + objs + ["-cudart", "static"])
+        cuda_lib = os.path.join(os.path.dirname(_cuda_include()), "lib64")
+        _run([_nvcc(), GENCODE, "-shared", "-o", tmp] + objs +
+             ["-cudart", "static", "-L", cuda_lib, "-lnvrtc", "-Xlinker", "-rpath=" + cuda_lib])
         os.replace(tmp, LIB)
     if archive:
         if os.path.exists(ARCHIVE):

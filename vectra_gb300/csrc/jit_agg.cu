@@ -1,0 +1,479 @@
+// jit_agg.cu -- run-time specialisation of the fused aggregation kernel.
+//
+// For each plan shape (the columns read and their types, the predicate's
+// term shapes, the join key, the group keys, the aggregate inputs and
+// classes, the cache size) this file writes a few dozen lines of CUDA that
+// fix those choices at compile time, compiles them together with
+// k_jit_lib.cuh / k_jit_kernel.cuh for sm_103a with NVRTC, loads the cubin
+// with the runtime's library API and caches the kernel by its source text.
+// Values that change between executions of one plan shape (column
+// pointers, predicate bounds, tables, the dense key range) stay in the
+// launch description, so re-running a plan reuses the compiled kernel.
+//
+// Host code only (no kernels of its own); the headers NVRTC needs are
+// embedded at build time (vg_jit_headers.inc, written by build.py).
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include <nvrtc.h>
+
+#include "k_groupby_dev.cuh"
+#include "vg_jit_headers.inc"   // kJitHeaderNames[], kJitHeaderSources[], kJitHeaderCount
+
+namespace {
+
+// Launch shape: threads per CTA, CTAs per SM the register budget is set
+// for, rows per thread.  VGPU_JIT_SHAPE="rows,threads,ctas" overrides it
+// (tuning runs).
+struct Shape { int rows = 2, threads = 512, ctas = 2; };
+
+const Shape &shape() {
+    static Shape sh;
+    static bool init = false;
+    if (!init) {
+        const char *e = getenv("VGPU_JIT_SHAPE");
+        int r, t, c;
+        if (e && sscanf(e, "%d,%d,%d", &r, &t, &c) == 3 && (r == 2 || r == 4) && t >= 64 && t <= 1024 &&
+            (t & 31) == 0 && c >= 1 && c <= 8)
+            sh.rows = r, sh.threads = t, sh.ctas = c;
+        init = true;
+    }
+    return sh;
+}
+
+char g_jit_err[2048];
+
+struct JitKernel {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t kernel = nullptr;
+    int smem_set = 0;
+};
+
+std::mutex g_mu;
+std::unordered_map<std::string, JitKernel> g_cache;
+unsigned long long g_compiles = 0;
+
+void fmt(std::string &s, const char *f, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, f);
+    vsnprintf(buf, sizeof(buf), f, ap);
+    va_end(ap);
+    s += buf;
+}
+
+std::string operand(const VgOperand &o) {
+    std::string s;
+    switch (o.side) {
+    case VG_SIDE_PROBE:
+        fmt(s, "InVal{X.p[%d][j], ((X.pok[%d] >> j) & 1u) != 0}", o.col, o.col);
+        break;
+    case VG_SIDE_BUILD:
+        fmt(s, "InVal{X.b[%d][j], ((X.bok[%d] >> j) & 1u) != 0}", o.col, o.col);
+        break;
+    case VG_SIDE_LIT:
+        fmt(s, "InVal{0x%llxull, true}", (unsigned long long)o.lit);
+        break;
+    default:
+        s = "InVal{0ull, false}";
+    }
+    return s;
+}
+
+std::string value(const VgValue &v) {
+    if (v.op == 0) return operand(v.a);
+    std::string s;
+    fmt(s, "vgj::arith<%d, %d, %d, %d>(%s, %s)", v.op, v.type, v.a.type, v.b.type, operand(v.a).c_str(),
+        operand(v.b).c_str());
+    return s;
+}
+
+int next_pow2(int x) {
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *vgk_jit_error(void) { return g_jit_err; }
+unsigned long long vgk_jit_compiles(void) { return g_compiles; }
+
+// Shapes the specialised kernel covers: no replay, single-key joins with
+// unique build keys (slot table), a shared-memory cache.
+int vgk_agg_jit_ok(const VgAggLaunch *L) {
+    if (getenv("VGPU_NO_JIT")) return 0;
+    if (L->replay || L->cache_slots <= 0) return 0;
+    if (L->has_join && (L->n_jkeys != 1 || !L->jt.slots || L->jt.rows)) return 0;
+    if (L->has_join && L->join_kind != JOIN_INNER && L->join_kind != JOIN_LEFT) return 0;
+    if (L->dense && (L->n_keys != 1 || L->dense_n + 1 > L->cache_slots)) return 0;
+    return 1;
+}
+
+// Cache slots the specialised kernel uses: the dense range (rounded up to a
+// power of two) when the keys are known, else the plan's cache size.
+int vgk_agg_jit_slots(const VgAggLaunch *L) {
+    if (L->dense) {
+        int s = next_pow2(L->dense_n + 1);
+        return s < 256 ? 256 : (s > L->cache_slots ? L->cache_slots : s);
+    }
+    return L->cache_slots;
+}
+
+// The plan-specific source for L with S cache slots.
+int vgk_agg_jit_source(const VgAggLaunch *L, int S, char *out, size_t out_bytes);
+
+}  // extern "C"
+
+namespace {
+
+std::string gen_source(const VgAggLaunch &L, int S, bool vec) {
+    VgAggLaunch T = L;
+    T.cache_slots = S;
+    Lay c;
+    make_lay(T, (uint64_t)S, c);
+    std::string s;
+    s += "// generated by jit_agg.cu\n";
+    fmt(s, "#define VGJ_R %d\n#define VGJ_NPC %d\n#define VGJ_NBC %d\n", shape().rows, L.n_pcols,
+        L.has_join ? L.n_bcols : 0);
+    s += "#include \"k_jit_lib.cuh\"\n";
+    fmt(s, "#define VGJ_THREADS %d\n#define VGJ_MINB %d\n#define VGJ_S %d\n", shape().threads, shape().ctas, S);
+    fmt(s, "#define VGJ_SEL %d\n#define VGJ_VEC %d\n", L.sel ? 1 : 0, vec ? 1 : 0);
+    fmt(s, "#define VGJ_PRED %d\n#define VGJ_JOIN %d\n", L.pred.n_terms > 0 ? 1 : 0, L.has_join ? 1 : 0);
+    if (L.has_join)
+        fmt(s, "#define VGJ_JKIND %d\n#define VGJ_JCOL %d\n#define VGJ_JCONV %d\n#define VGJ_JKT %d\n",
+            L.join_kind, L.jkey_col[0], L.jkey_conv[0], L.jt.key_types[0]);
+    fmt(s, "#define VGJ_NK %d\n#define VGJ_DENSE %d\n#define VGJ_TRACK %d\n", L.n_keys, L.dense ? 1 : 0,
+        L.track_first ? 1 : 0);
+    fmt(s, "#define VGJ_OFF_STATE %lluu\n#define VGJ_OFF_NM %lluu\n#define VGJ_OFF_KEYS %lluu\n"
+           "#define VGJ_OFF_FIRST %lluu\n",
+        (unsigned long long)c.state, (unsigned long long)c.nm, (unsigned long long)c.keys,
+        (unsigned long long)c.first);
+    s += "using namespace vgj;\n";
+
+    // probe columns
+    s += "VG_DEV void vgj_load_probe(const VgAggLaunch &L, Rows &X, int64_t r0, int nv, bool vec, "
+         "const int64_t (&phys)[R], uint32_t want) {\n";
+    for (int i = 0; i < L.n_pcols; i++) {
+        if (L.sel)
+            fmt(s, "    load_rows<%d>(L.pcols[%d], phys, want, X.p[%d], X.pok[%d]);\n", L.pcols[i].type, i, i, i);
+        else
+            fmt(s, "    load_dense<%d>(L.pcols[%d], r0, nv, vec, X.p[%d], X.pok[%d]);\n", L.pcols[i].type, i, i, i);
+    }
+    s += "    (void)L; (void)X; (void)r0; (void)nv; (void)vec; (void)phys; (void)want;\n}\n";
+
+    // predicate
+    s += "VG_DEV uint32_t vgj_pred(const VgAggLaunch &L, const Rows &X) {\n    uint32_t m = 0xFFFFFFFFu;\n";
+    for (int t = 0; t < L.pred.n_terms; t++) {
+        const VgTerm &tm = L.pred.term[t];
+        fmt(s, "    m &= term_mask<%d, %d, %d, %d, %d>(L, X);\n", tm.kind, tm.kind == VG_TERM_NONE ? 0 : tm.col,
+            tm.domain, tm.nan_keep ? 1 : 0, t);
+    }
+    s += "    (void)L; (void)X;\n    return m;\n}\n";
+
+    // build columns
+    s += "VG_DEV void vgj_load_build(const VgAggLaunch &L, Rows &X, const int64_t (&brow)[R], uint32_t want) {\n";
+    if (L.has_join)
+        for (int i = 0; i < L.n_bcols; i++)
+            fmt(s, "    load_rows<%d>(L.bcols[%d], brow, want, X.b[%d], X.bok[%d]);\n", L.bcols[i].type, i, i, i);
+    s += "    (void)L; (void)X; (void)brow; (void)want;\n}\n";
+
+    // group keys
+    s += "VG_DEV void vgj_keys(const Rows &X, int j, Keys &k, uint32_t &nm) {\n";
+    for (int i = 0; i < L.n_keys; i++)
+        fmt(s, "    { InVal v = %s; if (v.ok) k.w[%d] = vg_norm_key(v.bits, %d); else nm |= %uu; }\n",
+            value(L.key[i]).c_str(), i, L.key[i].type, 1u << i);
+    s += "    (void)X; (void)j; (void)k; (void)nm;\n}\n";
+
+    // cache updates
+    s += "VG_DEV uint32_t vgj_cache_update(char *sm, int slot, const Rows &X, int j) {\n    uint32_t fail = 0;\n";
+    for (int a = 0; a < L.n_accs; a++) {
+        const VgAccSpec &A = L.acc[a];
+        const int count = (L.skip_count_mask >> a) & 1u ? 0 : 1;
+        std::string v = A.cls == VG_ACC_COUNT_ALL ? std::string("InVal{0ull, true}") : value(A.in);
+        fmt(s, "    if (!cache_acc<%d, %d, %d, %lluu, %lluu, %lluu, %lluu, %lluu, %d>(sm, slot, %s)) fail |= %uu;\n",
+            A.cls, A.na_rm ? 1 : 0, count, (unsigned long long)c.cnt[a], (unsigned long long)c.val[a],
+            (unsigned long long)c.flags[a], (unsigned long long)c.base[a], (unsigned long long)c.win[a], S,
+            v.c_str(), 1u << a);
+    }
+    s += "    (void)sm; (void)slot; (void)X; (void)j;\n    return fail;\n}\n";
+
+    // global-table updates of the accumulators in `which`
+    s += "VG_DEV void vgj_global_update(const VgAggLaunch &L, int64_t g, const Rows &X, int j, uint32_t which) {\n";
+    for (int a = 0; a < L.n_accs; a++) {
+        const VgAccSpec &A = L.acc[a];
+        std::string v = A.cls == VG_ACC_COUNT_ALL ? std::string("InVal{0ull, true}") : value(A.in);
+        fmt(s, "    if (which & %uu) acc_update<true>(L.acc[%d], global_ptrs(L.gt, %d), L.gt.cap, g, %s);\n", 1u << a,
+            a, a, v.c_str());
+    }
+    s += "    (void)L; (void)g; (void)X; (void)j; (void)which;\n}\n";
+
+    // spill of single accumulators (global table full)
+    s += "VG_DEV void vgj_spill(const VgAggLaunch &L, int64_t li, uint32_t which) {\n";
+    for (int a = 0; a < L.n_accs; a++) fmt(s, "    if (which & %uu) spill_row(L, li, 0, %d);\n", 1u << a, a);
+    s += "    (void)L; (void)li; (void)which;\n}\n";
+
+    s += "#include \"k_jit_kernel.cuh\"\n";
+    return s;
+}
+
+int compile(const std::string &src, JitKernel &out) {
+    nvrtcProgram prog;
+    nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "vg_jit_agg.cu", kJitHeaderCount, kJitHeaderSources,
+                                       kJitHeaderNames);
+    if (r != NVRTC_SUCCESS) {
+        snprintf(g_jit_err, sizeof(g_jit_err), "nvrtcCreateProgram: %s", nvrtcGetErrorString(r));
+        return -1;
+    }
+    const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--generate-line-info"};
+    r = nvrtcCompileProgram(prog, 3, opts);
+    if (r != NVRTC_SUCCESS) {
+        size_t n = 0;
+        nvrtcGetProgramLogSize(prog, &n);
+        std::vector<char> log(n + 1, 0);
+        nvrtcGetProgramLog(prog, log.data());
+        snprintf(g_jit_err, sizeof(g_jit_err), "NVRTC: %s\n%.1800s", nvrtcGetErrorString(r), log.data());
+        nvrtcDestroyProgram(&prog);
+        return -1;
+    }
+    size_t n = 0;
+    nvrtcGetCUBINSize(prog, &n);
+    std::vector<char> cubin(n);
+    nvrtcGetCUBIN(prog, cubin.data());
+    nvrtcDestroyProgram(&prog);
+    g_compiles++;
+    cudaError_t e = cudaLibraryLoadData(&out.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if (e != cudaSuccess) {
+        snprintf(g_jit_err, sizeof(g_jit_err), "cudaLibraryLoadData: %s", cudaGetErrorString(e));
+        return -1;
+    }
+    e = cudaLibraryGetKernel(&out.kernel, out.lib, "vg_jit_agg");
+    if (e != cudaSuccess) {
+        snprintf(g_jit_err, sizeof(g_jit_err), "cudaLibraryGetKernel: %s", cudaGetErrorString(e));
+        return -1;
+    }
+    return 0;
+}
+
+bool vec_ok(const VgAggLaunch &L) {
+    if (L.sel) return false;
+    for (int c = 0; c < L.n_pcols; c++) {
+        const uintptr_t p = (uintptr_t)L.pcols[c].data;
+        if (L.pcols[c].type == VEC_BOOL ? (p & 3) : (p & 15)) return false;
+    }
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vgk_agg_jit_source(const VgAggLaunch *L, int S, char *out, size_t out_bytes) {
+    std::string s = gen_source(*L, S, vec_ok(*L));
+    if (s.size() + 1 > out_bytes) return (int)(s.size() + 1);
+    memcpy(out, s.c_str(), s.size() + 1);
+    return 0;
+}
+
+// Compiles the kernel for L without launching it (no device needed):
+// 0 on success, -1 with vgk_jit_error() set.
+int vgk_agg_jit_compile_only(const VgAggLaunch *L, int *regs_out) {
+    const int S = vgk_agg_jit_slots(L);
+    std::string src = gen_source(*L, S, vec_ok(*L));
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, src.c_str(), "vg_jit_agg.cu", kJitHeaderCount, kJitHeaderSources,
+                           kJitHeaderNames) != NVRTC_SUCCESS)
+        return -1;
+    const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--ptxas-options=-v"};
+    nvrtcResult r = nvrtcCompileProgram(prog, 3, opts);
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    std::vector<char> log(n + 1, 0);
+    nvrtcGetProgramLog(prog, log.data());
+    snprintf(g_jit_err, sizeof(g_jit_err), "%s%.1900s", r == NVRTC_SUCCESS ? "" : "NVRTC failed:\n", log.data());
+    nvrtcDestroyProgram(&prog);
+    if (regs_out) {
+        const char *p = strstr(log.data(), "Used ");
+        *regs_out = p ? atoi(p + 5) : -1;
+    }
+    return r == NVRTC_SUCCESS ? 0 : -1;
+}
+
+// Launches the specialised kernel over n_logical rows: 1 launched, 0 the
+// plan shape is not covered (nothing launched), -1 error (message in
+// vgk_jit_error()).
+int vgk_agg_launch_jit(const VgAggLaunch *L, int64_t n_logical, vg_stream_t s) {
+    if (!vgk_agg_jit_ok(L)) return 0;
+    const int S = vgk_agg_jit_slots(L);
+    const bool vec = vec_ok(*L);
+    std::string src = gen_source(*L, S, vec);
+    JitKernel *jk;
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        auto it = g_cache.find(src);
+        if (it == g_cache.end()) {
+            JitKernel k;
+            if (compile(src, k) != 0) return -1;
+            it = g_cache.emplace(src, k).first;
+        }
+        jk = &it->second;
+    }
+    VgAggLaunch T = *L;
+    T.cache_slots = S;
+    Lay c;
+    make_lay(T, (uint64_t)S, c);
+    const int smem = (int)c.total;
+    if (jk->smem_set < smem) {
+        cudaError_t e = cudaFuncSetAttribute((const void *)jk->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             smem);
+        if (e != cudaSuccess) {
+            snprintf(g_jit_err, sizeof(g_jit_err), "jit smem attribute: %s", cudaGetErrorString(e));
+            return -1;
+        }
+        jk->smem_set = smem;
+    }
+    const int sms = vgk_num_sms();
+    const Shape &sh = shape();
+    const int64_t per = (int64_t)sh.rows * sh.threads;
+    const int64_t tiles = (n_logical + per - 1) / per;
+    const int64_t cap = (int64_t)sms * (sh.ctas < 2 ? sh.ctas : 2);   // the spill area holds 2 caches per SM
+    const int grid = (int)(tiles < cap ? (tiles < 1 ? 1 : tiles) : cap);
+    cudaStream_t st = (cudaStream_t)s;
+    int64_t n = n_logical;
+    void *args[] = {(void *)&T, (void *)&n};
+    vg_prof_begin(VG_PROF_AGG, st);
+    cudaError_t e = cudaLaunchKernel((const void *)jk->kernel, dim3(grid), dim3(sh.threads), args, (size_t)smem, st);
+    vg_launch_counter++;
+    vg_prof_end(VG_PROF_AGG, st);
+    if (e != cudaSuccess) {
+        snprintf(g_jit_err, sizeof(g_jit_err), "jit agg launch: %s", cudaGetErrorString(e));
+        return -1;
+    }
+    return 1;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------
+// self-test: generates and compiles representative plan shapes (no device
+// needed).  Shape 0: left join + value*weight sum + n() keyed on a dense
+// build-side attribute; 1: filter (double and int64 ranges) + mean + n()
+// over a selection vector; 2: two keys (int64, double), bool column, int64
+// division, min / max / integer sum / count / bool min, first-seen order.
+// Returns 0 and the kernel's register count, or -1 (vgk_jit_error()).
+// ---------------------------------------------------------------------
+namespace {
+
+VgOperand op_col(int side, int col, int type) {
+    VgOperand o;
+    memset(&o, 0, sizeof(o));
+    o.side = side;
+    o.col = col;
+    o.type = type;
+    return o;
+}
+
+VgValue val_plain(VgOperand a) {
+    VgValue v;
+    memset(&v, 0, sizeof(v));
+    v.op = 0;
+    v.type = a.type;
+    v.a = a;
+    return v;
+}
+
+VgValue val_op(int op, int type, VgOperand a, VgOperand b) {
+    VgValue v;
+    memset(&v, 0, sizeof(v));
+    v.op = op;
+    v.type = type;
+    v.a = a;
+    v.b = b;
+    return v;
+}
+
+}  // namespace
+
+extern "C" int vgpu_jit_selftest(int shape, int *regs) {
+    static VgAggLaunch L;
+    memset(&L, 0, sizeof(L));
+    static double dummy[4];
+    L.cache_slots = 1024;
+    if (shape == 0) {
+        L.n_pcols = 2;
+        L.pcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
+        L.pcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};
+        L.n_bcols = 2;
+        L.bcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
+        L.bcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};
+        L.has_join = 1;
+        L.join_kind = JOIN_LEFT;
+        L.n_jkeys = 1;
+        L.jkey_col[0] = 0;
+        L.jt.cap = 64;
+        L.jt.n_keys = 1;
+        L.jt.key_types[0] = VEC_INT64;
+        L.jt.slots = (VgJSlot *)dummy;
+        L.n_keys = 1;
+        L.key[0] = val_plain(op_col(VG_SIDE_BUILD, 0, VEC_INT64));
+        L.n_accs = 2;
+        L.acc[0].cls = VG_ACC_SUM_F64;
+        L.acc[0].in = val_op('*', VEC_DOUBLE, op_col(VG_SIDE_PROBE, 1, VEC_DOUBLE), op_col(VG_SIDE_BUILD, 1, VEC_DOUBLE));
+        L.acc[1].cls = VG_ACC_COUNT_ALL;
+        L.skip_count_mask = 1u;
+        L.dense = 1;
+        L.dense_n = 256;
+    } else if (shape == 1) {
+        static int32_t sel[4];
+        L.sel = sel;
+        L.n_pcols = 3;
+        L.pcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
+        L.pcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};
+        L.pcols[2] = VgCol{VEC_INT64, 0, dummy, nullptr};
+        L.pred.n_terms = 2;
+        L.pred.term[0] = VgTerm{1, VG_TERM_RANGE, VG_DOM_DOUBLE, 0, 0, 0};
+        L.pred.term[1] = VgTerm{2, VG_TERM_NOT_RANGE, VG_DOM_INT64, 0, 0, 0};
+        L.n_keys = 1;
+        L.key[0] = val_plain(op_col(VG_SIDE_PROBE, 0, VEC_INT64));
+        L.n_accs = 2;
+        L.acc[0].cls = VG_ACC_SUM_F64;
+        L.acc[0].in = val_plain(op_col(VG_SIDE_PROBE, 1, VEC_DOUBLE));
+        L.acc[1].cls = VG_ACC_COUNT_ALL;
+    } else if (shape == 2) {
+        L.n_pcols = 4;
+        L.pcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
+        L.pcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};
+        L.pcols[2] = VgCol{VEC_BOOL, 0, dummy, nullptr};
+        L.pcols[3] = VgCol{VEC_INT64, 0, dummy, nullptr};
+        L.n_keys = 2;
+        L.key[0] = val_plain(op_col(VG_SIDE_PROBE, 0, VEC_INT64));
+        L.key[1] = val_plain(op_col(VG_SIDE_PROBE, 1, VEC_DOUBLE));
+        L.n_accs = 5;
+        L.acc[0].cls = VG_ACC_MIN_I64;
+        L.acc[0].in = val_op('/', VEC_INT64, op_col(VG_SIDE_PROBE, 3, VEC_INT64), op_col(VG_SIDE_PROBE, 0, VEC_INT64));
+        L.acc[1].cls = VG_ACC_MAX_F64;
+        L.acc[1].na_rm = 1;
+        L.acc[1].in = val_plain(op_col(VG_SIDE_PROBE, 1, VEC_DOUBLE));
+        L.acc[2].cls = VG_ACC_SUM_I64;
+        L.acc[2].in = val_op('%', VEC_INT64, op_col(VG_SIDE_PROBE, 3, VEC_INT64), op_col(VG_SIDE_LIT, 0, VEC_INT64));
+        L.acc[2].in.b.lit = 7;
+        L.acc[3].cls = VG_ACC_COUNT_VALID;
+        L.acc[3].in = val_plain(op_col(VG_SIDE_PROBE, 1, VEC_DOUBLE));
+        L.acc[4].cls = VG_ACC_NA_ONLY;
+        L.acc[4].in = val_plain(op_col(VG_SIDE_PROBE, 2, VEC_BOOL));
+        L.track_first = 1;
+    } else {
+        snprintf(g_jit_err, sizeof(g_jit_err), "no such self-test shape %d", shape);
+        return -1;
+    }
+    return vgk_agg_jit_compile_only(&L, regs);
+}

@@ -1,12 +1,17 @@
 // k_common.cuh -- device helpers shared by libvgpu's kernels (sm_103a).
 #pragma once
 
+#ifdef __CUDACC_RTC__
+#include "vg_rtc_types.h"
+#else
 #include <cstdint>
 #include <cuda_runtime.h>
+#endif
 #include "vgpu_internal.h"
 
 #define VG_DEV __device__ __forceinline__
 
+#ifndef __CUDACC_RTC__
 // number of kernels this library has launched (reported by the benchmark)
 extern "C" unsigned long long vg_launch_counter;
 
@@ -19,6 +24,7 @@ extern "C" unsigned long long vg_launch_counter;
 #define VG_PROF_FINISH 4
 void vg_prof_begin(int cls, cudaStream_t s);
 void vg_prof_end(int cls, cudaStream_t s);
+#endif
 
 // ---------------------------------------------------------------------
 // validity bits and column loads

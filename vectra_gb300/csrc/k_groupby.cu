@@ -492,6 +492,12 @@ int vgk_agg_launch(const VgAggLaunch *L, vg_stream_t s) {
     cudaStream_t st = (cudaStream_t)s;
     int64_t n_logical = L->replay ? L->replay_n : (L->sel ? L->sel_n : L->n_rows);
     if (n_logical <= 0) return 0;
+    int jrc = vgk_agg_launch_jit(L, n_logical, s);
+    if (jrc == 1) return 0;
+    if (jrc < 0) {
+        snprintf(g_err, sizeof(g_err), "%s", vgk_jit_error());
+        return -1;
+    }
     if (vgk_agg_fast_ok(L)) return vgk_agg_launch_fast(L, n_logical, s);
     bool cache = L->cache_slots > 0 && !L->replay;
     size_t smem = cache ? vgk_agg_smem_bytes(L) : 0;

@@ -22,12 +22,15 @@
 // keeps everything in registers.
 
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cstdio>
 #include <cstring>
+#endif
 #include "k_common.cuh"
 
 namespace {
 
+#ifndef __CUDACC_RTC__
 char g_err[256];
 int check(cudaError_t e, const char *what) {
     if (e != cudaSuccess) {
@@ -36,6 +39,7 @@ int check(cudaError_t e, const char *what) {
     }
     return 0;
 }
+#endif
 
 constexpr int kWin = 6;               // window digits per double sum
 constexpr int kBaseUnset = 0x7FFFFFFF;

@@ -1,0 +1,171 @@
+// k_jit_kernel.cuh -- the run-time specialised fused aggregation kernel.
+//
+// Included by the NVRTC source that jit_agg.cu generates for one plan,
+// after k_jit_lib.cuh and the plan's hooks:
+//   vgj_load_probe, vgj_pred, vgj_load_build, vgj_keys, vgj_cache_update,
+//   vgj_global_update, vgj_spill
+// and the VGJ_* constants.  One thread owns R consecutive logical rows per
+// step: it issues every column load for them first, then the R join
+// probes together, then the build-row loads, then the cache updates, so a
+// warp keeps many independent memory requests in flight.  The CTA's groups
+// live in a shared-memory cache (hashed, or dense when the group key is a
+// build-side attribute with a small known range) and are merged into the
+// global table when the CTA finishes; groups that do not fit in the cache,
+// and digit-window overflows, update the global table directly; rows that
+// find the global table full are spilled for a replay after it grows.
+
+#pragma once
+
+extern "C" __global__ void __launch_bounds__(VGJ_THREADS, VGJ_MINB)
+vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
+    using namespace vgj;
+    extern __shared__ __align__(16) char sm[];
+    __shared__ Lay cl;
+    __shared__ int cache_used;
+    constexpr int S = VGJ_S;
+    if (threadIdx.x == 0) {
+        make_lay(L, S, cl);
+        cache_used = 0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < S; i += blockDim.x) init_slot(L, sm, cl, S, i);
+#if VGJ_DENSE
+    {
+        uint64_t *sk = (uint64_t *)(sm + VGJ_OFF_KEYS);
+        uint32_t *snm = (uint32_t *)(sm + VGJ_OFF_NM);
+        for (int i = threadIdx.x; i <= L.dense_n; i += blockDim.x) {
+            sk[i] = i < L.dense_n ? (uint64_t)(L.dense_min + i) : 0;
+            snm[i] = i < L.dense_n ? 0u : 1u;
+        }
+    }
+#endif
+    __syncthreads();
+    uint32_t *st = (uint32_t *)(sm + VGJ_OFF_STATE);
+    const KeyTypes kt = key_types(L);
+
+    const int64_t tile = (int64_t)R * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * tile; base < n_rows; base += (int64_t)gridDim.x * tile) {
+        const int64_t r0 = base + (int64_t)R * threadIdx.x;
+        if (r0 >= n_rows) continue;
+        const int nv = (int)(n_rows - r0 < R ? n_rows - r0 : R);
+        const uint32_t all = (1u << nv) - 1u;
+        int64_t phys[R];
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+#if VGJ_SEL
+            phys[j] = j < nv ? (int64_t)__ldg(L.sel + r0 + j) : 0;
+#else
+            phys[j] = r0 + j;
+#endif
+        }
+        Rows X;
+        vgj_load_probe(L, X, r0, nv, VGJ_VEC && nv == R, phys, all);
+        uint32_t live = all;
+#if VGJ_PRED
+        live &= vgj_pred(L, X);
+#endif
+#if VGJ_JOIN
+        int64_t brow[R];
+        uint32_t matched = 0;
+        {
+            uint64_t kw[R];
+            int64_t slot[R];
+            uint32_t need = 0;
+            const int64_t mask = L.jt.cap - 1;
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                brow[j] = -1;
+                kw[j] = 0;
+                slot[j] = 0;
+                if (!((live >> j) & 1u)) continue;
+                if (!((X.pok[VGJ_JCOL] >> j) & 1u)) continue;           // NA never matches
+                uint64_t b = X.p[VGJ_JCOL][j];
+                if (VGJ_JCONV) b = vg_f64_to_bits(vg_i2f((int64_t)b));
+                if (VGJ_JKT == VEC_DOUBLE && vg_is_nan_bits(b)) continue;
+                kw[j] = vg_norm_key(b, VGJ_JKT);
+                slot[j] = (int64_t)(hash_keys(&kw[j], 1, 0) & (uint64_t)mask);
+                need |= 1u << j;
+            }
+            VgJSlot e[R];
+#pragma unroll
+            for (int j = 0; j < R; j++)
+                if ((need >> j) & 1u) e[j] = jt_slot(L.jt.slots + (kw[j] == VG_JEMPTY ? L.jt.cap : slot[j]));
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                if (!((need >> j) & 1u)) continue;
+                if (kw[j] == VG_JEMPTY) {
+                    if (e[j].count > 0) { brow[j] = e[j].start; matched |= 1u << j; }
+                    continue;
+                }
+                int64_t s = slot[j];
+                for (int64_t probe = 0; probe < L.jt.cap; probe++) {
+                    if (e[j].key == kw[j]) { brow[j] = e[j].start; matched |= 1u << j; break; }
+                    if (e[j].key == VG_JEMPTY) break;
+                    s = (s + 1) & mask;
+                    e[j] = jt_slot(L.jt.slots + s);
+                }
+            }
+            if (VGJ_JKIND != JOIN_LEFT) live &= matched;
+        }
+        vgj_load_build(L, X, brow, live & matched);
+#endif
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            if (!((live >> j) & 1u)) continue;
+            const int64_t li = r0 + j;
+            Keys k;
+#pragma unroll
+            for (int i = 0; i < VG_MAX_KEYS; i++) k.w[i] = 0;
+            uint32_t nm = 0;
+            vgj_keys(X, j, k, nm);
+            int found;
+#if VGJ_DENSE
+            (void)cache_used;
+            found = nm ? L.dense_n : (int)((int64_t)k.w[0] - L.dense_min);
+            if (st[found] != 2u) st[found] = 2u;      // first touch marks the slot live
+#else
+            {
+                int err = 0;
+                found = cache_find<S, VGJ_NK>(sm, VGJ_OFF_STATE, VGJ_OFF_NM, VGJ_OFF_KEYS, &cache_used, k, nm,
+                                              kt, &err);
+                if (err) atomicOr(L.gt.err, VG_ERR_WAIT);
+            }
+#endif
+#if VGJ_TRACK
+#if VGJ_JOIN
+            const uint64_t order = ((uint64_t)L.batch_idx << 44) | ((uint64_t)(((matched >> j) & 1u) ? 0 : 1) << 43) |
+                                   ((uint64_t)(li & 0xFFFFFFFF) << 11);
+#else
+            const uint64_t order = (uint64_t)(L.row_base + li);
+#endif
+#endif
+            if (found >= 0) {
+#if VGJ_TRACK
+                atomicMin((unsigned long long *)(sm + VGJ_OFF_FIRST) + found, (unsigned long long)order);
+#endif
+                const uint32_t fail = vgj_cache_update(sm, found, X, j);
+                if (fail) {
+                    const int64_t g = gt_find_insert(L.gt, k, VGJ_NK, kt, nm, hash_k(k, VGJ_NK, nm));
+                    if (g >= 0) vgj_global_update(L, g, X, j, fail);
+                    else vgj_spill(L, li, fail);
+                }
+            } else {
+                const int64_t g = gt_find_insert(L.gt, k, VGJ_NK, kt, nm, hash_k(k, VGJ_NK, nm));
+                if (g < 0) { spill_row(L, li, 0, -1); continue; }
+#if VGJ_TRACK
+                atomicMin((unsigned long long *)(L.gt.first_row + g), (unsigned long long)order);
+#endif
+                vgj_global_update(L, g, X, j, 0xFFFFFFFFu);
+            }
+        }
+    }
+
+    __syncthreads();
+    __shared__ Lay sl;
+    if (threadIdx.x == 0) make_lay(L, (uint64_t)L.spill_cache_cap, sl);
+    __syncthreads();
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+        if (st[i] != 2u) continue;
+        if (!merge_entry(L, sm, cl, S, i)) spill_entry(L, sm, cl, S, i, sl);
+    }
+}

@@ -1,0 +1,255 @@
+// k_jit_lib.cuh -- device building blocks of the run-time specialised fused
+// aggregation kernel (compiled by NVRTC together with the plan-specific
+// definitions that jit_agg.cu generates, then k_jit_kernel.cuh).
+//
+// The generated part fixes at compile time everything the general kernel
+// decides per row: which columns are read and their types, the predicate's
+// term shapes, the join key, every group key and aggregate input
+// expression, every accumulator's class and the shared-memory layout.  What
+// stays a run-time value (column pointers, predicate bounds, table
+// pointers, the dense key range) is read from the launch description in
+// the constant bank.  Semantics are those of agg_kernel (k_groupby.cu),
+// which in turn follow src/group_agg.c:155-281, src/agg_ops.c:93-158 and
+// src/scalar_ops.c:11-66.
+//
+// Needs, defined before inclusion: VGJ_NPC, VGJ_NBC (probe / build columns
+// read), VGJ_R (rows per thread).
+
+#pragma once
+#include "k_groupby_dev.cuh"
+
+namespace vgj {
+
+constexpr int R = VGJ_R;
+constexpr int kNP = VGJ_NPC > 0 ? VGJ_NPC : 1;
+constexpr int kNB = VGJ_NBC > 0 ? VGJ_NBC : 1;
+
+// The rows one thread works on: values (raw 64-bit patterns) and validity
+// bits of the probe columns and, after the join, of the build columns.
+struct Rows {
+    uint64_t p[kNP][R];
+    uint32_t pok[kNP];
+    uint64_t b[kNB][R];
+    uint32_t bok[kNB];
+};
+
+// R validity bits of rows r..r+R-1 (r + voff aligned to R).
+VG_DEV uint32_t valid_bits(const VgCol &c, int64_t r) {
+    if (c.valid == nullptr) return (1u << R) - 1u;
+    const int64_t b = r + c.voff;
+    const uint32_t w = __ldg(c.valid + (b >> 5));
+    return (w >> (int)(b & 31)) & ((1u << R) - 1u);
+}
+
+// Loads rows r0..r0+nv-1 of a probe column.  vec: r0 + R <= rows and the
+// column's data and validity offsets allow whole vector loads.
+template <int TYPE>
+VG_DEV void load_dense(const VgCol &c, int64_t r0, int nv, bool vec, uint64_t (&v)[R], uint32_t &ok) {
+    if (TYPE == VEC_BOOL) {
+        const unsigned char *d = (const unsigned char *)c.data + r0;
+        if (vec && R == 4) {
+            uint32_t w = __ldg((const unsigned int *)d);
+#pragma unroll
+            for (int j = 0; j < R; j++) v[j] = (w >> (8 * j)) & 0xFFu;
+        } else {
+#pragma unroll
+            for (int j = 0; j < R; j++) v[j] = j < nv ? (uint64_t)__ldg(d + j) : 0;
+        }
+    } else {
+        const unsigned long long *d = (const unsigned long long *)c.data + r0;
+        if (vec) {
+#pragma unroll
+            for (int j = 0; j < R; j += 2) {
+                ulonglong2 a = __ldg((const ulonglong2 *)(d + j));
+                v[j] = a.x;
+                v[j + 1] = a.y;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < R; j++) v[j] = j < nv ? (uint64_t)__ldg(d + j) : 0;
+        }
+    }
+    if (vec && ((r0 + c.voff) & (R - 1)) == 0) {
+        ok = valid_bits(c, r0);
+    } else {
+        uint32_t m = 0;
+#pragma unroll
+        for (int j = 0; j < R; j++)
+            if (j < nv && vg_valid(c, r0 + j)) m |= 1u << j;
+        ok = m;
+    }
+}
+
+// Loads the rows phys[0..nv) of a column (selection vector or build rows;
+// entries < 0 are absent and read as NA).
+template <int TYPE>
+VG_DEV void load_rows(const VgCol &c, const int64_t (&phys)[R], uint32_t want, uint64_t (&v)[R], uint32_t &ok) {
+    uint32_t m = 0;
+#pragma unroll
+    for (int j = 0; j < R; j++) {
+        v[j] = 0;
+        if (!((want >> j) & 1u)) continue;
+        const int64_t r = phys[j];
+        if (TYPE == VEC_BOOL) v[j] = (uint64_t)__ldg((const unsigned char *)c.data + r);
+        else v[j] = (uint64_t)__ldg((const unsigned long long *)c.data + r);
+        if (vg_valid(c, r)) m |= 1u << j;
+    }
+    ok = m;
+}
+
+// value = a op b in result type T (src/scalar_ops.c:11-66): operands
+// coerced to T first; int64 division / modulo by zero is NA.
+template <int OP, int T, int TA, int TB>
+VG_DEV InVal arith(InVal a, InVal b) {
+    InVal r;
+    r.ok = a.ok && b.ok;
+    r.bits = 0;
+    if (!r.ok) return r;
+    if (T == VEC_DOUBLE) {
+        const double x = vg_bits_to_f64(TA == VEC_DOUBLE ? a.bits : vg_f64_to_bits(vg_i2f((int64_t)a.bits)));
+        const double y = vg_bits_to_f64(TB == VEC_DOUBLE ? b.bits : vg_f64_to_bits(vg_i2f((int64_t)b.bits)));
+        double z;
+        if (OP == '+') z = __dadd_rn(x, y);
+        else if (OP == '-') z = __dsub_rn(x, y);
+        else if (OP == '*') z = __dmul_rn(x, y);   // one rounding, never fused
+        else if (OP == '/') z = __ddiv_rn(x, y);
+        else z = fmod(x, y);
+        r.bits = vg_f64_to_bits(z);
+    } else {
+        const int64_t x = (int64_t)a.bits, y = (int64_t)b.bits;
+        const uint64_t ux = (uint64_t)x, uy = (uint64_t)y;
+        if (OP == '+') r.bits = ux + uy;
+        else if (OP == '-') r.bits = ux - uy;
+        else if (OP == '*') r.bits = ux * uy;
+        else if (OP == '/') {
+            if (y == 0) r.ok = false;
+            else r.bits = (y == -1) ? (0 - ux) : (uint64_t)(x / y);
+        } else {
+            if (y == 0) r.ok = false;
+            else r.bits = (y == -1) ? 0 : (uint64_t)(x % y);
+        }
+    }
+    return r;
+}
+
+// Keep mask of the R rows for predicate term T (kind, column and domain
+// fixed; bounds read from the launch description).
+template <int KIND, int COL, int DOM, int NAN_KEEP, int T>
+VG_DEV uint32_t term_mask(const VgAggLaunch &L, const Rows &X) {
+    uint32_t m = 0;
+    const uint32_t ok = X.pok[COL];
+#pragma unroll
+    for (int j = 0; j < R; j++) {
+        const bool v = (ok >> j) & 1u;
+        bool keep;
+        if (KIND == VG_TERM_NONE) keep = false;
+        else if (KIND == VG_TERM_IS_NA) keep = !v;
+        else if (KIND == VG_TERM_NOT_NA) keep = v;
+        else if (!v) keep = false;
+        else {
+            const uint64_t bits = X.p[COL][j];
+            int64_t x;
+            bool nan = false;
+            if (DOM == VG_DOM_DOUBLE) {
+                nan = vg_is_nan_bits(bits);
+                x = vg_ord(bits);
+            } else {
+                x = (int64_t)bits;
+            }
+            if (nan) keep = NAN_KEEP != 0;
+            else {
+                const bool in = (x >= L.pred.term[T].lo) && (x <= L.pred.term[T].hi);
+                keep = KIND == VG_TERM_RANGE ? in : !in;
+            }
+        }
+        if (keep) m |= 1u << j;
+    }
+    return m;
+}
+
+// Accumulator update in the shared cache at compile-time layout offsets.
+// False: the value falls outside the cache's digit window (the caller
+// then updates the global table).
+template <int CLS, int NA_RM, int COUNT, uint32_t OCNT, uint32_t OVAL, uint32_t OFLAGS, uint32_t OBASE,
+          uint32_t OWIN, int S>
+VG_DEV bool cache_acc(char *sm, int slot, InVal x) {
+    uint32_t *cnt = (uint32_t *)(sm + OCNT) + slot;
+    uint32_t *flags = (uint32_t *)(sm + OFLAGS) + slot;
+    if (CLS == VG_ACC_COUNT_ALL) { atomicAdd(cnt, 1u); return true; }
+    if (CLS == VG_ACC_COUNT_VALID) { if (x.ok) atomicAdd(cnt, 1u); return true; }
+    if (!x.ok) {
+        if (!NA_RM) set_flags(flags, 1u);
+        return true;
+    }
+    if (CLS == VG_ACC_SUM_I64) {
+        if (COUNT) atomicAdd(cnt, 1u);
+        pair_add((uint32_t *)(sm + OVAL) + slot, (int32_t *)(sm + OVAL + 4 * S) + slot, (int64_t)x.bits);
+        return true;
+    }
+    if (CLS == VG_ACC_SUM_F64) {
+        const VgDigits d = vg_split_double(x.bits);
+        if (d.special) set_flags(flags, d.special);
+        else if (d.lo >= 0 && !cwin_add((int32_t *)(sm + OBASE) + slot, (uint32_t *)(sm + OWIN) + slot,
+                                        (int32_t *)(sm + OWIN + 4 * S * kWin) + slot, S, d))
+            return false;
+        if (COUNT) atomicAdd(cnt, 1u);
+        return true;
+    }
+    long long *v64 = (long long *)(sm + OVAL) + slot;
+    if (CLS == VG_ACC_MIN_I64 || CLS == VG_ACC_MAX_I64) {
+        if (CLS == VG_ACC_MIN_I64) atomicMin(v64, (long long)x.bits);
+        else atomicMax(v64, (long long)x.bits);
+        set_flags(flags, 2u);
+        return true;
+    }
+    if (CLS == VG_ACC_MIN_F64 || CLS == VG_ACC_MAX_F64) {
+        if (vg_is_nan_bits(x.bits)) { set_flags(flags, 2u | 4u); return true; }
+        if (CLS == VG_ACC_MIN_F64) atomicMin(v64, (long long)vg_ord(x.bits));
+        else atomicMax(v64, (long long)vg_ord(x.bits));
+        set_flags(flags, 2u);
+        return true;
+    }
+    return true;   // VG_ACC_NA_ONLY
+}
+
+// Finds or claims the cache slot of a key (open addressing, bounded
+// probes; new keys only while the cache is under 3/4 full).  -1: not cached.
+template <int S, int NK>
+VG_DEV int cache_find(char *sm, uint32_t OSTATE, uint32_t ONM, uint32_t OKEYS, int *cache_used,
+                      const Keys &k, uint32_t nm, const KeyTypes &kt, int *err) {
+    uint32_t *st = (uint32_t *)(sm + OSTATE);
+    uint32_t *snm = (uint32_t *)(sm + ONM);
+    uint64_t *sk = (uint64_t *)(sm + OKEYS);
+    const uint64_t h = hash_k(k, NK, nm);
+    int slot = (int)(h & (uint64_t)(S - 1));
+    const bool may_insert = *(volatile int *)cache_used < (S * 3) / 4;
+    for (int probe = 0; probe < (may_insert ? kCacheProbes : 4); probe++) {
+        uint32_t s0 = *(volatile uint32_t *)(st + slot);
+        if (s0 == 0) {
+            if (!may_insert) return -1;
+            const uint32_t prev = atomicCAS(st + slot, 0u, 1u);
+            if (prev == 0u) {
+#pragma unroll
+                for (int i = 0; i < NK; i++) sk[(int64_t)i * S + slot] = k.w[i];
+                snm[slot] = nm;
+                __threadfence_block();
+                atomicExch(st + slot, 2u);
+                atomicAdd(cache_used, 1);
+                return slot;
+            }
+            s0 = prev;
+        }
+        int spins = 0;
+        while (s0 == 1u) {
+            if (++spins > VG_SPIN_LIMIT) { *err = 1; return -1; }
+            s0 = *(volatile uint32_t *)(st + slot);
+        }
+        if (s0 != 2u) return -1;
+        __threadfence_block();
+        if (keys_eq(sk, S, slot, k, NK, kt, *(volatile uint32_t *)(snm + slot), nm)) return slot;
+        slot = (slot + 1) & (S - 1);
+    }
+    return -1;
+}
+
+}  // namespace vgj

@@ -8,8 +8,12 @@
 #ifndef VGPU_INTERNAL_H
 #define VGPU_INTERNAL_H
 
+#ifdef __CUDACC_RTC__
+#include "vg_rtc_types.h"
+#else
 #include <stdint.h>
 #include <stddef.h>
+#endif
 #include "vectra_abi.h"
 
 #ifdef __cplusplus
@@ -269,6 +273,7 @@ typedef struct {
 /* kernel entry points (implemented in the .cu files)                  */
 /* ------------------------------------------------------------------ */
 
+#ifndef __CUDACC_RTC__
 int  vgk_num_sms(void);
 const char *vgk_last_cuda_error(void);
 
@@ -366,6 +371,17 @@ int vgk_group_table_rehash(const VgGroupTable *from, const VgGroupTable *to, int
                            vg_stream_t s);
 /* bytes of spilled cache entries per entry (cache layout, one slot) */
 size_t vgk_agg_cache_bytes(const VgAggLaunch *L, int64_t slots);
+
+/* run-time specialised aggregation kernel (jit_agg.cu): launch returns 1
+ * if launched, 0 if the plan shape is not covered, -1 on error */
+int vgk_agg_launch_jit(const VgAggLaunch *L, int64_t n_logical, vg_stream_t s);
+int vgk_agg_jit_ok(const VgAggLaunch *L);
+int vgk_agg_jit_slots(const VgAggLaunch *L);
+int vgk_agg_jit_compile_only(const VgAggLaunch *L, int *regs_out);
+int vgk_agg_jit_source(const VgAggLaunch *L, int S, char *out, size_t out_bytes);
+const char *vgk_jit_error(void);
+unsigned long long vgk_jit_compiles(void);
+#endif  /* !__CUDACC_RTC__ */
 
 #ifdef __cplusplus
 }
