@@ -148,7 +148,8 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec) {
     s += "#include \"k_jit_lib.cuh\"\n";
     fmt(s, "#define VGJ_THREADS %d\n#define VGJ_MINB %d\n#define VGJ_S %d\n", shape().threads, shape().ctas, S);
     fmt(s, "#define VGJ_SEL %d\n#define VGJ_VEC %d\n", L.sel ? 1 : 0, vec ? 1 : 0);
-    fmt(s, "#define VGJ_PRED %d\n#define VGJ_JOIN %d\n", L.pred.n_terms > 0 ? 1 : 0, L.has_join ? 1 : 0);
+    fmt(s, "#define VGJ_PRED %d\n#define VGJ_JOIN %d\n#define VGJ_PAY %d\n", L.pred.n_terms > 0 ? 1 : 0,
+        L.has_join ? 1 : 0, (L.has_join && L.jpay && L.jpay_n == L.n_bcols && L.n_bcols >= 1) ? 1 : 0);
     if (L.has_join)
         fmt(s, "#define VGJ_JKIND %d\n#define VGJ_JCOL %d\n#define VGJ_JCONV %d\n#define VGJ_JKT %d\n",
             L.join_kind, L.jkey_col[0], L.jkey_conv[0], L.jt.key_types[0]);
@@ -366,9 +367,10 @@ int vgk_agg_launch_jit(const VgAggLaunch *L, int64_t n_logical, vg_stream_t s) {
 // ---------------------------------------------------------------------
 // self-test: generates and compiles representative plan shapes (no device
 // needed).  Shape 0: left join + value*weight sum + n() keyed on a dense
-// build-side attribute; 1: filter (double and int64 ranges) + mean + n()
+// build-side attribute (payload copy); 1: filter (double and int64 ranges) + mean + n()
 // over a selection vector; 2: two keys (int64, double), bool column, int64
-// division, min / max / integer sum / count / bool min, first-seen order.
+// division, min / max / integer sum / count / bool min, first-seen order;
+// 3: inner join on a coerced double key, build columns gathered by row.
 // Returns 0 and the kernel's register count, or -1 (vgk_jit_error()).
 // ---------------------------------------------------------------------
 namespace {
@@ -432,6 +434,8 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
         L.skip_count_mask = 1u;
         L.dense = 1;
         L.dense_n = 256;
+        L.jpay = (const VgJPay *)dummy;
+        L.jpay_n = 2;
     } else if (shape == 1) {
         static int32_t sel[4];
         L.sel = sel;
@@ -470,6 +474,33 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
         L.acc[3].in = val_plain(op_col(VG_SIDE_PROBE, 1, VEC_DOUBLE));
         L.acc[4].cls = VG_ACC_NA_ONLY;
         L.acc[4].in = val_plain(op_col(VG_SIDE_PROBE, 2, VEC_BOOL));
+        L.track_first = 1;
+    } else if (shape == 3) {
+        // inner join, build columns gathered by row (no payload copy), hashed cache
+        L.n_pcols = 2;
+        L.pcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
+        L.pcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};
+        L.n_bcols = 3;
+        L.bcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
+        L.bcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};
+        L.bcols[2] = VgCol{VEC_BOOL, 0, dummy, nullptr};
+        L.has_join = 1;
+        L.join_kind = JOIN_INNER;
+        L.n_jkeys = 1;
+        L.jkey_col[0] = 0;
+        L.jkey_conv[0] = 1;
+        L.jt.cap = 64;
+        L.jt.n_keys = 1;
+        L.jt.key_types[0] = VEC_DOUBLE;
+        L.jt.slots = (VgJSlot *)dummy;
+        L.n_keys = 2;
+        L.key[0] = val_plain(op_col(VG_SIDE_BUILD, 0, VEC_INT64));
+        L.key[1] = val_plain(op_col(VG_SIDE_BUILD, 2, VEC_BOOL));
+        L.n_accs = 2;
+        L.acc[0].cls = VG_ACC_SUM_F64;
+        L.acc[0].in = val_op('-', VEC_DOUBLE, op_col(VG_SIDE_PROBE, 1, VEC_DOUBLE), op_col(VG_SIDE_BUILD, 1, VEC_DOUBLE));
+        L.acc[1].cls = VG_ACC_MAX_I64;
+        L.acc[1].in = val_plain(op_col(VG_SIDE_BUILD, 0, VEC_INT64));
         L.track_first = 1;
     } else {
         snprintf(g_jit_err, sizeof(g_jit_err), "no such self-test shape %d", shape);

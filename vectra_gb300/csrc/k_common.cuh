@@ -93,6 +93,14 @@ VG_DEV uint64_t hash_keys(const uint64_t *k, int nk, uint32_t nm) {
     return vg_mix64(h);
 }
 
+// Slot hash of a join table key: one mixing round for the single-key
+// tables (the common case, paid once per probe row), the general key hash
+// for composite keys.
+VG_DEV uint64_t vg_jhash(const uint64_t *k, int nk) {
+    if (nk == 1) return vg_mix64(k[0] ^ 0x9E3779B97F4A7C15ull);
+    return hash_keys(k, nk, 0);
+}
+
 // one 16-byte slot read through the read-only path
 VG_DEV VgJSlot jt_slot(const VgJSlot *p) {
     ulonglong2 v = __ldg((const ulonglong2 *)p);
@@ -105,7 +113,7 @@ VG_DEV VgJSlot jt_slot(const VgJSlot *p) {
 
 // Join table lookup: keys are normalised words of the common key types.
 VG_DEV bool jt_lookup(const VgJoinTable &jt, const uint64_t *k, int32_t &start, int32_t &count) {
-    uint64_t h = hash_keys(k, jt.n_keys, 0);
+    uint64_t h = vg_jhash(k, jt.n_keys);
     const int64_t mask = jt.cap - 1;
     int64_t slot = (int64_t)(h & (uint64_t)mask);
     if (jt.slots) {

@@ -223,7 +223,7 @@ agg_fast_kernel(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
                 if (L.jkey_conv[0]) b = vg_f64_to_bits(vg_i2f((int64_t)b));
                 if (L.jt.key_types[0] == VEC_DOUBLE && vg_is_nan_bits(b)) continue;
                 kw[j] = vg_norm_key(b, L.jt.key_types[0]);
-                slot[j] = (int64_t)(hash_keys(&kw[j], 1, 0) & (uint64_t)mask);
+                slot[j] = (int64_t)(vg_jhash(&kw[j], 1) & (uint64_t)mask);
                 need |= 1u << j;
             }
             VgJSlot e[kFastRows];

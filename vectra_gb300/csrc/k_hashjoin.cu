@@ -106,7 +106,7 @@ __global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters) {
 VG_DEV int64_t insert_single(const VgJoinTable &jt, uint64_t k, uint32_t *counters) {
     if (k == VG_JEMPTY) return jt.cap;      // the marker value has its own slot
     const int64_t mask = jt.cap - 1;
-    int64_t slot = (int64_t)(hash_keys(&k, 1, 0) & (uint64_t)mask);
+    int64_t slot = (int64_t)(vg_jhash(&k, 1) & (uint64_t)mask);
     for (int64_t probe = 0; probe < jt.cap; probe++) {
         unsigned long long *kp = (unsigned long long *)&jt.slots[slot].key;
         unsigned long long cur = *(volatile unsigned long long *)kp;
@@ -124,7 +124,7 @@ VG_DEV int64_t insert_single(const VgJoinTable &jt, uint64_t k, uint32_t *counte
 // composite keys: per-slot lock (0 empty, 1 being written, 2 ready)
 VG_DEV int64_t insert_multi(const VgJoinTable &jt, const uint64_t *k, int nk, uint32_t *counters) {
     const int64_t mask = jt.cap - 1;
-    int64_t slot = (int64_t)(hash_keys(k, nk, 0) & (uint64_t)mask);
+    int64_t slot = (int64_t)(vg_jhash(k, nk) & (uint64_t)mask);
     for (int64_t probe = 0; probe < jt.cap; probe++) {
         uint32_t st = *(volatile uint32_t *)(jt.state + slot);
         if (st == 0) {
@@ -154,23 +154,66 @@ VG_DEV int64_t insert_multi(const VgJoinTable &jt, const uint64_t *k, int nk, ui
     return -1;
 }
 
-// counters: [0] distinct keys, [1] max rows per key, [2] error bits
+// counters: [0] distinct keys, [1] max rows per key, [2] error bits.
+// Every warp runs the same number of iterations (the row index is the
+// block's base plus the lane), so the per-warp counter updates can be
+// combined with full-warp votes: one atomic per warp instead of one per row.
 __global__ void jt_insert_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t *rslot,
                                  uint32_t *counters) {
-    int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-        uint64_t k[VG_MAX_KEYS];
-        if (!key_words(K, r, k)) { rslot[r] = -1; continue; }
-        int64_t found = jt.slots ? insert_single(jt, k[0], counters) : insert_multi(jt, k, K.n_keys, counters);
-        if (found < 0) { rslot[r] = -1; continue; }
-        int32_t old = atomicAdd(jt_count_ptr(jt, found), 1);
-        if (old == 0) {
-            atomicAdd(counters + 0, 1u);
-            *jt_start_ptr(jt, found) = (int32_t)r;   // final when keys are unique
-        } else {
-            atomicMax(counters + 1, (uint32_t)(old + 1));
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x; b < n; b += stride) {
+        const int64_t r = b + threadIdx.x;
+        bool first = false;
+        uint32_t dup = 0;
+        if (r < n) {
+            uint64_t k[VG_MAX_KEYS];
+            int64_t found = -1;
+            if (key_words(K, r, k))
+                found = jt.slots ? insert_single(jt, k[0], counters) : insert_multi(jt, k, K.n_keys, counters);
+            if (found >= 0) {
+                int32_t old = atomicAdd(jt_count_ptr(jt, found), 1);
+                if (old == 0) {
+                    first = true;
+                    *jt_start_ptr(jt, found) = (int32_t)r;   // final when keys are unique
+                } else {
+                    dup = (uint32_t)(old + 1);
+                }
+            }
+            rslot[r] = (int32_t)found;
         }
-        rslot[r] = (int32_t)found;
+        const unsigned nfirst = __popc(__ballot_sync(0xFFFFFFFFu, first));
+        const unsigned mx = __reduce_max_sync(0xFFFFFFFFu, dup);
+        if (lane == 0) {
+            if (nfirst) atomicAdd(counters + 0, nfirst);
+            if (mx) atomicMax(counters + 1, mx);
+        }
+    }
+}
+
+// Payload copy of the slot table: per slot the key, the build row and the
+// values and validity of up to two build columns of that row.
+__global__ void jt_pay_kernel(VgJoinTable jt, VgCol c0, VgCol c1, int n_cols, VgJPay *pay) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s <= jt.cap; s += stride) {
+        const VgJSlot e = jt_slot(jt.slots + s);
+        uint64_t p0 = 0, p1 = 0;
+        uint32_t meta = 0;
+        if (e.count > 0 && (s == jt.cap || e.key != VG_JEMPTY)) {
+            const int64_t r = e.start;
+            meta = 1u;
+            if (n_cols > 0) {
+                p0 = vg_load_bits(c0, r);
+                if (vg_valid(c0, r)) meta |= 2u;
+            }
+            if (n_cols > 1) {
+                p1 = vg_load_bits(c1, r);
+                if (vg_valid(c1, r)) meta |= 4u;
+            }
+        }
+        ulonglong2 *o = (ulonglong2 *)(pay + s);
+        o[0] = make_ulonglong2(e.key, (unsigned long long)(uint32_t)e.start | ((unsigned long long)meta << 32));
+        o[1] = make_ulonglong2(p0, p1);
     }
 }
 
@@ -421,6 +464,20 @@ int vgk_join_unmatched_build(const uint32_t *d_matched, int64_t n_build, int32_t
     if (check(cudaStreamSynchronize(st), "unmatched build")) return -1;
     *h_n = t;
     return 0;
+}
+
+int vgk_join_payload(const VgJoinTable *jt, const VgCol *cols, int n_cols, VgJPay *pay, vg_stream_t s) {
+    if (!jt->slots || n_cols < 0 || n_cols > 2) {
+        snprintf(g_err, sizeof(g_err), "join payload: unsupported table");
+        return -1;
+    }
+    cudaStream_t st = (cudaStream_t)s;
+    VgCol none;
+    memset(&none, 0, sizeof(none));
+    { jt_pay_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, n_cols > 0 ? cols[0] : none,
+                                                             n_cols > 1 ? cols[1] : none, n_cols, pay);
+      vg_launch_counter++; }
+    return check(cudaGetLastError(), "join payload");
 }
 
 }  // extern "C"

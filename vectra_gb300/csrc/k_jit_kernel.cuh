@@ -83,9 +83,52 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
                 if (VGJ_JCONV) b = vg_f64_to_bits(vg_i2f((int64_t)b));
                 if (VGJ_JKT == VEC_DOUBLE && vg_is_nan_bits(b)) continue;
                 kw[j] = vg_norm_key(b, VGJ_JKT);
-                slot[j] = (int64_t)(hash_keys(&kw[j], 1, 0) & (uint64_t)mask);
+                slot[j] = (int64_t)(vg_jhash(&kw[j], 1) & (uint64_t)mask);
                 need |= 1u << j;
             }
+#if VGJ_PAY
+            // payload copy: key, build row, validity and up to two build
+            // columns in one 32-byte sector per probe
+            ulonglong2 ea[R], eb[R];
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                if (!((need >> j) & 1u)) continue;
+                const VgJPay *q = L.jpay + (kw[j] == VG_JEMPTY ? L.jt.cap : slot[j]);
+                ea[j] = __ldg((const ulonglong2 *)q);
+                eb[j] = __ldg((const ulonglong2 *)q + 1);
+            }
+#pragma unroll
+            for (int i = 0; i < kNB; i++) X.bok[i] = 0;
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                if (!((need >> j) & 1u)) continue;
+                bool hit = false;
+                if (kw[j] == VG_JEMPTY) {
+                    hit = ((ea[j].y >> 32) & 1u) != 0;
+                } else {
+                    int64_t s = slot[j];
+                    for (int64_t probe = 0; probe < L.jt.cap; probe++) {
+                        if (ea[j].x == kw[j]) { hit = true; break; }
+                        if (ea[j].x == VG_JEMPTY) break;
+                        s = (s + 1) & mask;
+                        const VgJPay *q = L.jpay + s;
+                        ea[j] = __ldg((const ulonglong2 *)q);
+                        eb[j] = __ldg((const ulonglong2 *)q + 1);
+                    }
+                }
+                if (hit) {
+                    const uint32_t meta = (uint32_t)(ea[j].y >> 32);
+                    brow[j] = (int64_t)(int32_t)(uint32_t)ea[j].y;
+                    matched |= 1u << j;
+                    X.b[0][j] = eb[j].x;
+                    X.bok[0] |= ((meta >> 1) & 1u) << j;
+                    if (kNB > 1) {
+                        X.b[kNB > 1 ? 1 : 0][j] = eb[j].y;
+                        X.bok[kNB > 1 ? 1 : 0] |= ((meta >> 2) & 1u) << j;
+                    }
+                }
+            }
+#else
             VgJSlot e[R];
 #pragma unroll
             for (int j = 0; j < R; j++)
@@ -105,9 +148,14 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
                     e[j] = jt_slot(L.jt.slots + s);
                 }
             }
+#endif
             if (VGJ_JKIND != JOIN_LEFT) live &= matched;
         }
+#if !VGJ_PAY
         vgj_load_build(L, X, brow, live & matched);
+#else
+        (void)brow;
+#endif
 #endif
 #pragma unroll
         for (int j = 0; j < R; j++) {

@@ -522,6 +522,15 @@ static VecBatch *agg_next(VecNode *self) {
             L->dense_min = mm[0];
         }
     }
+    /* the run-time specialised kernel reads up to two build columns from a
+     * payload copy of the join table: one sector per probe row */
+    VgJPay *jpay = NULL;
+    if (B && L->jt.slots && !L->jt.rows && L->n_bcols >= 1 && L->n_bcols <= 2 && vgk_agg_jit_ok(L)) {
+        jpay = (VgJPay *)vg_dmalloc((size_t)(L->jt.cap + 1) * sizeof(VgJPay));
+        vg_check_rc(vgk_join_payload(&L->jt, L->bcols, L->n_bcols, jpay, vg_stream()), "join payload");
+        L->jpay = jpay;
+        L->jpay_n = L->n_bcols;
+    }
 
     Table T;
     table_alloc(&T, &P, 8192);
@@ -543,6 +552,7 @@ static VecBatch *agg_next(VecNode *self) {
         batch_idx++;
     }
     VecBatch *res = emit_result(A, &P, &T);
+    vg_dfree(jpay);
     vg_dfree(T.block);
     vg_dfree(S.rows);
     vg_dfree(S.cache);

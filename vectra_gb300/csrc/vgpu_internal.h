@@ -193,6 +193,17 @@ typedef struct {
     uint32_t *err;           /* error word: nonzero = a bounded wait expired / table full */
 } VgGroupTable;
 
+/* Build-row payload inlined into a copy of a single-key join table's
+ * slots (same capacity and slot positions): one 32-byte sector per probe
+ * gives the key, the build row and up to two build columns with their
+ * validity.  Built only for unique build keys. */
+typedef struct {
+    uint64_t key;
+    int32_t  start;          /* build row */
+    uint32_t meta;           /* bit0: key present; bit 1+c: payload column c valid */
+    uint64_t p[2];
+} VgJPay;
+
 /* Join hash table over the build side (keys unique per slot; rows of a key
  * listed in ascending build-row order in rows[start .. start+count)). */
 /* Single-key join slot: one 16-byte sector per probe.  key == VG_JEMPTY
@@ -267,6 +278,11 @@ typedef struct {
     int64_t   dense_min;
     /* Accumulators whose count no output reads (a SUM without MEAN). */
     uint32_t  skip_count_mask;
+    /* Optional payload copy of the join table holding bcols[0..jpay_n)
+     * (read by the run-time specialised kernel). */
+    const VgJPay *jpay;
+    int32_t   jpay_n;
+    int32_t   pad_jpay;
 } VgAggLaunch;
 
 /* ------------------------------------------------------------------ */
@@ -371,6 +387,10 @@ int vgk_group_table_rehash(const VgGroupTable *from, const VgGroupTable *to, int
                            vg_stream_t s);
 /* bytes of spilled cache entries per entry (cache layout, one slot) */
 size_t vgk_agg_cache_bytes(const VgAggLaunch *L, int64_t slots);
+
+/* payload copy of a unique-key single-key join table: bcols[0..n) of the
+ * build rows, (cap + 1) entries */
+int vgk_join_payload(const VgJoinTable *jt, const VgCol *cols, int n_cols, VgJPay *pay, vg_stream_t s);
 
 /* run-time specialised aggregation kernel (jit_agg.cu): launch returns 1
  * if launched, 0 if the plan shape is not covered, -1 on error */
