@@ -242,6 +242,22 @@ def ja_join_agg(E, temp_dir):       # the benchmark plan, small: left_join then 
     return a
 
 
+def ja_join_agg_sparse(E, temp_dir):   # the benchmark plan with scattered ids (hashed join table)
+    rng = np.random.default_rng(8)
+    nf, nd = 4000, 250
+    ids = (rng.permutation(nd) + 1) * 7_000_003 - 2_000_000_000
+    fk = ids[rng.integers(0, nd, nf)]
+    fk[rng.random(nf) < 0.05] += 1                      # some probe keys match nothing
+    fact = {"key": (fk, rng.random(nf) > 0.01), "value": (rng.lognormal(0, 1, nf), rng.random(nf) > 0.02)}
+    dim = {"id": ids, "category": rng.integers(0, 16, nd), "weight": rng.random(nd)}
+    out = []
+    for kind in ("left_join", "inner_join"):
+        out += (getattr(tbl(E, fact, batch_rows=1024), kind)(tbl(E, dim, batch_rows=128), {"key": "id"})
+                .group_by("category").summarise(temp_dir=temp_dir, s=("sum", col("value") * col("weight")),
+                                                n=("n",)).batches())
+    return out
+
+
 def ja_dense_keys(E, temp_dir):     # join + aggregate keyed on a small-range build-side column
     rng = np.random.default_rng(17)
     nf, nd = 7001, 257
@@ -290,10 +306,12 @@ def r_group(E, seed, n, batch_rows, sel_mode, temp_dir):
                                      sd=("sum", "d", True)).batches())
 
 
-def r_join(E, seed, n, batch_rows, kind):
+def r_join(E, seed, n, batch_rows, kind, spread=1):
+    """spread > 1 scatters the key values far apart (a hashed join table
+    instead of the direct-addressed one small key ranges get)."""
     rng = np.random.default_rng(seed)
-    l = {"k": (rng.integers(0, 60, n), rng.random(n) > 0.05), "x": rng.normal(0, 1, n)}
-    r = {"k": (rng.integers(0, 80, 70), rng.random(70) > 0.05), "y": rng.normal(0, 1, 70),
+    l = {"k": (rng.integers(0, 60, n) * spread, rng.random(n) > 0.05), "x": rng.normal(0, 1, n)}
+    r = {"k": (rng.integers(0, 80, 70) * spread, rng.random(70) > 0.05), "y": rng.normal(0, 1, 70),
          "z": rng.integers(0, 5, 70)}
     return getattr(tbl(E, l, batch_rows=batch_rows), kind)(tbl(E, r, batch_rows=32), "k").batches()
 
@@ -302,7 +320,7 @@ FILTER_CASES = [f_simple, f_equality, f_and_or_not, f_na_dropped, f_is_na, f_kle
                 f_empty, f_general_expr, f_int_vs_double_literal]
 GROUP_CASES = [g_basic, g_na_key, g_multi_key, g_na_semantics, g_int_sum_double, g_resize_200,
                g_filter_then_group, g_ungrouped, g_nested_expr, g_bool_and_double_keys, ja_join_agg,
-               ja_dense_keys]
+               ja_dense_keys, ja_join_agg_sparse]
 JOIN_CASES = [j_inner_left_semi_anti, j_duplicates, j_na_keys, j_suffix, j_coerce, j_streaming,
               j_after_filter, j_full]
 

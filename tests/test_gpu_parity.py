@@ -60,6 +60,14 @@ def test_random_join(kind, n, batch, G, oracle):
     cases.same_batches(cases.r_join(G, n + 3, n, batch, kind), cases.r_join(oracle, n + 3, n, batch, kind))
 
 
+@pytest.mark.parametrize("kind", ["inner_join", "left_join", "semi_join", "anti_join", "full_join"])
+@pytest.mark.parametrize("n,batch", [(33, 32), (5000, 1024)])
+def test_random_join_sparse_keys(kind, n, batch, G, oracle):
+    """Keys spread over a wide range: hashed join tables."""
+    sp = 1_000_003
+    cases.same_batches(cases.r_join(G, n + 5, n, batch, kind, sp), cases.r_join(oracle, n + 5, n, batch, kind, sp))
+
+
 def test_high_cardinality_groups(G, oracle):
     """More groups than any shared-memory cache: exercises the global table,
     spill and growth (rehash) paths."""

@@ -7,8 +7,8 @@ import re
 import pytest
 
 
-@pytest.mark.parametrize("shape", [0, 1, 2, 3], ids=["join_payload_dense_sum", "filter_sel_mean", "two_keys_all_accs",
-                                          "inner_join_gather"])
+@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4], ids=["join_direct_payload", "filter_sel_mean", "two_keys_all_accs",
+                                             "inner_join_gather", "join_hashed_payload"])
 def test_generated_kernel_compiles(shape):
     import vectra_gb300
     lib = vectra_gb300.load()

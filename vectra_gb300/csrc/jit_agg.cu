@@ -151,8 +151,9 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec) {
     fmt(s, "#define VGJ_PRED %d\n#define VGJ_JOIN %d\n#define VGJ_PAY %d\n", L.pred.n_terms > 0 ? 1 : 0,
         L.has_join ? 1 : 0, (L.has_join && L.jpay && L.jpay_n == L.n_bcols && L.n_bcols >= 1) ? 1 : 0);
     if (L.has_join)
-        fmt(s, "#define VGJ_JKIND %d\n#define VGJ_JCOL %d\n#define VGJ_JCONV %d\n#define VGJ_JKT %d\n",
-            L.join_kind, L.jkey_col[0], L.jkey_conv[0], L.jt.key_types[0]);
+        fmt(s, "#define VGJ_JKIND %d\n#define VGJ_JCOL %d\n#define VGJ_JCONV %d\n#define VGJ_JKT %d\n"
+               "#define VGJ_JDIRECT %d\n",
+            L.join_kind, L.jkey_col[0], L.jkey_conv[0], L.jt.key_types[0], L.jt.direct ? 1 : 0);
     fmt(s, "#define VGJ_NK %d\n#define VGJ_DENSE %d\n#define VGJ_TRACK %d\n", L.n_keys, L.dense ? 1 : 0,
         L.track_first ? 1 : 0);
     fmt(s, "#define VGJ_OFF_STATE %lluu\n#define VGJ_OFF_NM %lluu\n#define VGJ_OFF_KEYS %lluu\n"
@@ -367,10 +368,11 @@ int vgk_agg_launch_jit(const VgAggLaunch *L, int64_t n_logical, vg_stream_t s) {
 // ---------------------------------------------------------------------
 // self-test: generates and compiles representative plan shapes (no device
 // needed).  Shape 0: left join + value*weight sum + n() keyed on a dense
-// build-side attribute (payload copy); 1: filter (double and int64 ranges) + mean + n()
+// build-side attribute (direct-addressed payload copy); 1: filter (double and int64 ranges) + mean + n()
 // over a selection vector; 2: two keys (int64, double), bool column, int64
 // division, min / max / integer sum / count / bool min, first-seen order;
-// 3: inner join on a coerced double key, build columns gathered by row.
+// 3: inner join on a coerced double key, build columns gathered by row;
+// 4: shape 0 on a hashed join table.
 // Returns 0 and the kernel's register count, or -1 (vgk_jit_error()).
 // ---------------------------------------------------------------------
 namespace {
@@ -410,7 +412,7 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
     memset(&L, 0, sizeof(L));
     static double dummy[4];
     L.cache_slots = 1024;
-    if (shape == 0) {
+    if (shape == 0 || shape == 4) {
         L.n_pcols = 2;
         L.pcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
         L.pcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};
@@ -436,6 +438,8 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
         L.dense_n = 256;
         L.jpay = (const VgJPay *)dummy;
         L.jpay_n = 2;
+        L.jt.direct = shape == 0;   // shape 4: hashed table, linear-probing chain
+        L.jt.dmin = 1;
     } else if (shape == 1) {
         static int32_t sel[4];
         L.sel = sel;

@@ -111,8 +111,23 @@ VG_DEV VgJSlot jt_slot(const VgJSlot *p) {
     return s;
 }
 
+// Direct-addressed slot of key k, or -1 when k lies outside the table's range.
+VG_DEV int64_t jt_direct_slot(const VgJoinTable &jt, uint64_t k) {
+    const uint64_t d = k - (uint64_t)jt.dmin;
+    return d < (uint64_t)jt.cap ? (int64_t)d : -1;
+}
+
 // Join table lookup: keys are normalised words of the common key types.
 VG_DEV bool jt_lookup(const VgJoinTable &jt, const uint64_t *k, int32_t &start, int32_t &count) {
+    if (jt.direct) {
+        const int64_t d = jt_direct_slot(jt, k[0]);
+        if (d < 0) return false;
+        VgJSlot e = jt_slot(jt.slots + d);
+        if (e.count <= 0) return false;
+        start = e.start;
+        count = e.count;
+        return true;
+    }
     uint64_t h = vg_jhash(k, jt.n_keys);
     const int64_t mask = jt.cap - 1;
     int64_t slot = (int64_t)(h & (uint64_t)mask);

@@ -368,7 +368,7 @@ int vgk_agg_fast_ok(const VgAggLaunch *L) {
         if (L->pcols[c].type == VEC_BOOL) return 0;
         if (((uintptr_t)L->pcols[c].data) & 15) return 0;
     }
-    if (L->has_join && (L->n_jkeys != 1 || !L->jt.slots || L->jt.rows)) return 0;
+    if (L->has_join && (L->n_jkeys != 1 || !L->jt.slots || L->jt.rows || L->jt.direct)) return 0;
     if (L->dense && (L->n_keys != 1 || L->dense_n + 1 > L->cache_slots)) return 0;
     return 1;
 }

@@ -102,8 +102,15 @@ __global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters) {
     if (blockIdx.x == 0 && threadIdx.x < 4) counters[threadIdx.x] = 0;
 }
 
-// single key: claim a slot with one CAS on its key word
+// single key: claim a slot with one CAS on its key word (direct tables:
+// the key's own slot; the host sized the range from the build keys)
 VG_DEV int64_t insert_single(const VgJoinTable &jt, uint64_t k, uint32_t *counters) {
+    if (jt.direct) {
+        const int64_t d = jt_direct_slot(jt, k);
+        if (d < 0) { atomicOr(counters + 2, VG_ERR_FULL); return -1; }
+        jt.slots[d].key = k;                // every writer stores the same word
+        return d;
+    }
     if (k == VG_JEMPTY) return jt.cap;      // the marker value has its own slot
     const int64_t mask = jt.cap - 1;
     int64_t slot = (int64_t)(vg_jhash(&k, 1) & (uint64_t)mask);
@@ -199,7 +206,7 @@ __global__ void jt_pay_kernel(VgJoinTable jt, VgCol c0, VgCol c1, int n_cols, Vg
         const VgJSlot e = jt_slot(jt.slots + s);
         uint64_t p0 = 0, p1 = 0;
         uint32_t meta = 0;
-        if (e.count > 0 && (s == jt.cap || e.key != VG_JEMPTY)) {
+        if (e.count > 0 && (jt.direct || s == jt.cap || e.key != VG_JEMPTY)) {
             const int64_t r = e.start;
             meta = 1u;
             if (n_cols > 0) {

@@ -65,6 +65,7 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
         live &= vgj_pred(L, X);
 #endif
 #if VGJ_JOIN
+        // join probe: the R rows' slot reads are issued together
         int64_t brow[R];
         uint32_t matched = 0;
         {
@@ -83,7 +84,12 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
                 if (VGJ_JCONV) b = vg_f64_to_bits(vg_i2f((int64_t)b));
                 if (VGJ_JKT == VEC_DOUBLE && vg_is_nan_bits(b)) continue;
                 kw[j] = vg_norm_key(b, VGJ_JKT);
-                slot[j] = (int64_t)(vg_jhash(&kw[j], 1) & (uint64_t)mask);
+#if VGJ_JDIRECT
+                slot[j] = jt_direct_slot(L.jt, kw[j]);
+                if (slot[j] < 0) continue;                           // outside the key range: no match
+#else
+                slot[j] = kw[j] == VG_JEMPTY ? L.jt.cap : (int64_t)(vg_jhash(&kw[j], 1) & (uint64_t)mask);
+#endif
                 need |= 1u << j;
             }
 #if VGJ_PAY
@@ -93,7 +99,7 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
 #pragma unroll
             for (int j = 0; j < R; j++) {
                 if (!((need >> j) & 1u)) continue;
-                const VgJPay *q = L.jpay + (kw[j] == VG_JEMPTY ? L.jt.cap : slot[j]);
+                const VgJPay *q = L.jpay + slot[j];
                 ea[j] = __ldg((const ulonglong2 *)q);
                 eb[j] = __ldg((const ulonglong2 *)q + 1);
             }
@@ -102,10 +108,11 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
 #pragma unroll
             for (int j = 0; j < R; j++) {
                 if (!((need >> j) & 1u)) continue;
-                bool hit = false;
-                if (kw[j] == VG_JEMPTY) {
+                bool hit;
+                if (VGJ_JDIRECT || kw[j] == VG_JEMPTY) {
                     hit = ((ea[j].y >> 32) & 1u) != 0;
                 } else {
+                    hit = false;
                     int64_t s = slot[j];
                     for (int64_t probe = 0; probe < L.jt.cap; probe++) {
                         if (ea[j].x == kw[j]) { hit = true; break; }
@@ -132,11 +139,11 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
             VgJSlot e[R];
 #pragma unroll
             for (int j = 0; j < R; j++)
-                if ((need >> j) & 1u) e[j] = jt_slot(L.jt.slots + (kw[j] == VG_JEMPTY ? L.jt.cap : slot[j]));
+                if ((need >> j) & 1u) e[j] = jt_slot(L.jt.slots + slot[j]);
 #pragma unroll
             for (int j = 0; j < R; j++) {
                 if (!((need >> j) & 1u)) continue;
-                if (kw[j] == VG_JEMPTY) {
+                if (VGJ_JDIRECT || kw[j] == VG_JEMPTY) {
                     if (e[j].count > 0) { brow[j] = e[j].start; matched |= 1u << j; }
                     continue;
                 }
@@ -149,6 +156,7 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
                 }
             }
 #endif
+            (void)mask;
             if (VGJ_JKIND != JOIN_LEFT) live &= matched;
         }
 #if !VGJ_PAY

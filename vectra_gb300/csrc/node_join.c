@@ -130,9 +130,26 @@ static void join_build(VgJoin *j) {
     free(bs);
     free(need);
 
-    /* hash table */
+    /* hash table, or a direct-addressed one when the only key is an int64
+     * column whose values span at most twice the build rows (dense ids) */
     int nk = j->jn.n_keys;
-    int64_t tcap = vgk_join_cap(total);
+    VgCol kc[VG_MAX_KEYS];
+    for (int k = 0; k < nk; k++) kc[k] = j->B.bcols[j->jn.keys[k].right_col];
+    int direct = 0;
+    int64_t dmin = 0, drange = 0;
+    if (nk == 1 && j->key_type[0] == VEC_INT64 && kc[0].type == VEC_INT64 && total > 0) {
+        int64_t mm[3];
+        int64_t *d = (int64_t *)vg_dmalloc(256);
+        vg_check_rc(vgk_col_minmax_i64(&kc[0], total, d, mm, vg_stream()), "join key range");
+        vg_dfree(d);
+        uint64_t limit = (uint64_t)(2 * total > 65536 ? 2 * total : 65536);
+        if (mm[2] > 0 && (uint64_t)mm[1] - (uint64_t)mm[0] < limit) {
+            direct = 1;
+            dmin = mm[0];
+            drange = (int64_t)((uint64_t)mm[1] - (uint64_t)mm[0]) + 1;
+        }
+    }
+    int64_t tcap = direct ? drange : vgk_join_cap(total);
     size_t rows_b = a256((size_t)(total > 0 ? total : 1) * 4);
     size_t tb = (nk == 1) ? a256((size_t)(tcap + 1) * sizeof(VgJSlot)) + rows_b + 256
                           : a256((size_t)tcap * 4) * 3 + a256((size_t)tcap * 8 * (size_t)nk) + rows_b + 256;
@@ -141,6 +158,8 @@ static void join_build(VgJoin *j) {
     VgJoinTable *jt = &j->B.jt;
     memset(jt, 0, sizeof(*jt));
     jt->cap = tcap;
+    jt->direct = direct;
+    jt->dmin = dmin;
     jt->n_keys = nk;
     for (int k = 0; k < nk; k++) jt->key_types[k] = j->key_type[k];
     size_t o = 0;
@@ -156,8 +175,6 @@ static void join_build(VgJoin *j) {
     jt->rows = (int32_t *)(t + o); o += rows_b;
     jt->err = (uint32_t *)(t + o);
     jt->n_build = total;
-    VgCol kc[VG_MAX_KEYS];
-    for (int k = 0; k < nk; k++) kc[k] = j->B.bcols[j->jn.keys[k].right_col];
     size_t sb = vgk_join_build_scratch_bytes(total);
     void *scratch = vg_dmalloc(sb);
     int64_t distinct = 0, maxdup = 0;

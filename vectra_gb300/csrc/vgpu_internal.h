@@ -217,9 +217,16 @@ typedef struct {
 #define VG_JEMPTY 0x8000000000000000ull
 
 typedef struct {
-    int64_t   cap;           /* power of two */
+    int64_t   cap;           /* power of two (hashed) or the key range (direct) */
     int32_t   n_keys;
     int32_t   key_types[VG_MAX_KEYS];
+    /* Direct addressing for one int64 key whose build values span a range
+     * comparable to the build row count (surrogate / dense ids): the slot
+     * of key k is k - dmin for k in [dmin, dmin + cap), no hashing, one
+     * slot read per probe, presence = count > 0. */
+    int32_t   direct;
+    int32_t   pad_direct;
+    int64_t   dmin;
     VgJSlot  *slots;         /* single-key tables: cap + 1 slots */
     uint32_t *state;         /* composite-key tables: slot locks ... */
     uint64_t *keys;          /* ... [n_keys][cap] key words ... */
