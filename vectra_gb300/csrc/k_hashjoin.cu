@@ -224,6 +224,69 @@ __global__ void jt_pay_kernel(VgJoinTable jt, VgCol c0, VgCol c1, int n_cols, Vg
     }
 }
 
+// Direct tables: every build row writes its key's own slot; the counts are
+// non-returning adds, and the distinct / duplicate counters come from a
+// pass over the slots afterwards (jt_count_kernel).  With duplicates the
+// start written here is replaced by the sorted layout (seg_start_kernel).
+__global__ void jt_insert_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t *rslot,
+                                        uint32_t *counters) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    uint64_t k[VG_MAX_KEYS];
+    int64_t d = -1;
+    if (key_words(K, r, k)) {
+        d = jt_direct_slot(jt, k[0]);
+        if (d < 0) {
+            atomicOr(counters + 2, VG_ERR_FULL);
+        } else {
+            jt.slots[d].key = k[0];
+            jt.slots[d].start = (int32_t)r;
+            atomicAdd(&jt.slots[d].count, 1);
+        }
+    }
+    rslot[r] = (int32_t)d;
+}
+
+__global__ void jt_count_kernel(VgJoinTable jt, uint32_t *counters) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x; b < jt.cap; b += stride) {
+        const int64_t s = b + threadIdx.x;
+        const int32_t c = s < jt.cap ? jt.slots[s].count : 0;
+        const unsigned nd = __popc(__ballot_sync(0xFFFFFFFFu, c > 0));
+        const unsigned mx = __reduce_max_sync(0xFFFFFFFFu, (unsigned)c);
+        if (lane == 0) {
+            if (nd) atomicAdd(counters + 0, nd);
+            if (mx > 1) atomicMax(counters + 1, mx);
+        }
+    }
+}
+
+// Payload copy of a direct table in build-row order: column reads are
+// coalesced, each row writes its key's whole 32-byte entry (the entries
+// start zeroed: absent keys read as not present).
+__global__ void jt_pay_direct_kernel(VgJoinTable jt, VgCol key, VgCol c0, VgCol c1, int n_cols, VgJPay *pay) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= jt.n_build) return;
+    if (!vg_valid(key, r)) return;
+    const uint64_t k = vg_load_bits(key, r);
+    const int64_t d = jt_direct_slot(jt, k);
+    if (d < 0) return;
+    uint64_t p0 = 0, p1 = 0;
+    uint32_t meta = 1u;
+    if (n_cols > 0) {
+        p0 = vg_load_bits(c0, r);
+        if (vg_valid(c0, r)) meta |= 2u;
+    }
+    if (n_cols > 1) {
+        p1 = vg_load_bits(c1, r);
+        if (vg_valid(c1, r)) meta |= 4u;
+    }
+    ulonglong2 *o = (ulonglong2 *)(pay + d);
+    o[0] = make_ulonglong2(k, (unsigned long long)(uint32_t)r | ((unsigned long long)meta << 32));
+    o[1] = make_ulonglong2(p0, p1);
+}
+
 __global__ void pair_keys_kernel(const int32_t *rslot, int64_t n, int64_t cap, uint64_t *keys,
                                  int32_t *vals) {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -370,8 +433,18 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
     }
     { jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters); vg_launch_counter++; }
     vg_prof_begin(VG_PROF_JOIN_BUILD, st);
-        { jt_insert_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(*jt, K, n_build, rslot, counters); vg_launch_counter++; }
-        vg_prof_end(VG_PROF_JOIN_BUILD, st);
+    if (jt->direct) {
+        if (n_build > 0) {
+            jt_insert_direct_kernel<<<(unsigned)((n_build + 255) / 256), 256, 0, st>>>(*jt, K, n_build, rslot,
+                                                                                  counters);
+            vg_launch_counter++;
+        }
+        { jt_count_kernel<<<grid_for(jt->cap, 256), 256, 0, st>>>(*jt, counters); vg_launch_counter++; }
+    } else {
+        jt_insert_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(*jt, K, n_build, rslot, counters);
+        vg_launch_counter++;
+    }
+    vg_prof_end(VG_PROF_JOIN_BUILD, st);
     uint32_t hc[4] = {0, 0, 0, 0};
     cudaMemcpyAsync(hc, counters, 16, cudaMemcpyDeviceToHost, st);
     if (check(cudaStreamSynchronize(st), "join build")) return -1;
@@ -473,7 +546,8 @@ int vgk_join_unmatched_build(const uint32_t *d_matched, int64_t n_build, int32_t
     return 0;
 }
 
-int vgk_join_payload(const VgJoinTable *jt, const VgCol *cols, int n_cols, VgJPay *pay, vg_stream_t s) {
+int vgk_join_payload(const VgJoinTable *jt, const VgCol *key, const VgCol *cols, int n_cols, VgJPay *pay,
+                     vg_stream_t s) {
     if (!jt->slots || n_cols < 0 || n_cols > 2) {
         snprintf(g_err, sizeof(g_err), "join payload: unsupported table");
         return -1;
@@ -481,6 +555,15 @@ int vgk_join_payload(const VgJoinTable *jt, const VgCol *cols, int n_cols, VgJPa
     cudaStream_t st = (cudaStream_t)s;
     VgCol none;
     memset(&none, 0, sizeof(none));
+    if (jt->direct && key) {
+        if (check(cudaMemsetAsync(pay, 0, (size_t)(jt->cap + 1) * sizeof(VgJPay), st), "join payload")) return -1;
+        if (jt->n_build > 0) {
+            jt_pay_direct_kernel<<<(unsigned)((jt->n_build + 255) / 256), 256, 0, st>>>(
+                *jt, *key, n_cols > 0 ? cols[0] : none, n_cols > 1 ? cols[1] : none, n_cols, pay);
+            vg_launch_counter++;
+        }
+        return check(cudaGetLastError(), "join payload");
+    }
     { jt_pay_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, n_cols > 0 ? cols[0] : none,
                                                              n_cols > 1 ? cols[1] : none, n_cols, pay);
       vg_launch_counter++; }

@@ -527,7 +527,8 @@ static VecBatch *agg_next(VecNode *self) {
     VgJPay *jpay = NULL;
     if (B && L->jt.slots && !L->jt.rows && L->n_bcols >= 1 && L->n_bcols <= 2 && vgk_agg_jit_ok(L)) {
         jpay = (VgJPay *)vg_dmalloc((size_t)(L->jt.cap + 1) * sizeof(VgJPay));
-        vg_check_rc(vgk_join_payload(&L->jt, L->bcols, L->n_bcols, jpay, vg_stream()), "join payload");
+        vg_check_rc(vgk_join_payload(&L->jt, &B->bcols[B->rkey[0]], L->bcols, L->n_bcols, jpay, vg_stream()),
+                    "join payload");
         L->jpay = jpay;
         L->jpay_n = L->n_bcols;
     }

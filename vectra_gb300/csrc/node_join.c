@@ -30,6 +30,8 @@ typedef struct {
     int32_t key_type[VG_MAX_KEYS];
     int32_t conv_build[VG_MAX_KEYS];
     void *build_block;        /* device build columns */
+    VgDBatch kept;            /* the one build batch, used in place */
+    int has_kept;
     void *table_block;        /* device hash table */
     int *r_nonkey;
     int r_nonkey_n;
@@ -95,15 +97,26 @@ static void join_build(VgJoin *j) {
     j->n_build = total;
     j->B.n_bcols = nr;
     j->B.bcols = (VgCol *)vg_xcalloc((size_t)(nr ? nr : 1), sizeof(VgCol));
-    /* dense device copy of the logical rows (one gather per batch) */
+    if (nb == 1 && !bs[0].d_sel) {
+        /* one batch without a selection: its device columns are the build
+         * columns as they are (kept until the node is freed) */
+        for (int c = 0; c < nr; c++) {
+            j->B.bcols[c].type = rs->col_types[c];
+            if (need[c]) j->B.bcols[c] = bs[0].cols[c];
+        }
+        j->kept = bs[0];
+        j->has_kept = 1;
+        nb = 0;
+    }
+    /* otherwise a dense device copy of the logical rows (one gather per batch) */
     size_t wbytes = (size_t)((total + 31) / 32) * 4 + 8;
     size_t bytes = 0;
-    for (int c = 0; c < nr; c++)
+    for (int c = 0; c < nr && !j->has_kept; c++)
         if (need[c]) bytes += a256((size_t)total * elem(rs->col_types[c]) + 8) + a256(wbytes);
-    char *blk = (char *)vg_dmalloc(bytes ? bytes : 256);
+    char *blk = j->has_kept ? NULL : (char *)vg_dmalloc(bytes ? bytes : 256);
     j->build_block = blk;
     size_t off = 0;
-    for (int c = 0; c < nr; c++) {
+    for (int c = 0; c < nr && !j->has_kept; c++) {
         j->B.bcols[c].type = rs->col_types[c];
         if (!need[c]) continue;
         char *dv = blk + off;
@@ -347,6 +360,7 @@ static void join_free(VecNode *self) {
     free(j->r_nonkey);
     free(j->B.bcols);
     vg_dfree(j->build_block);
+    if (j->has_kept) vg_dbatch_release(&j->kept);
     vg_dfree(j->table_block);
     vg_dfree(j->d_matched);
     vg_dfree(j->d_unmatched);
@@ -398,6 +412,7 @@ JoinNode *join_node_create(VecNode *left, VecNode *right, JoinKind kind, int n_k
         j->conv_build[k] = (rt != c && c == VEC_DOUBLE);
         j->B.conv[k] = (lt != c && c == VEC_DOUBLE);
         j->B.lkey[k] = keys[k].left_col;
+        j->B.rkey[k] = keys[k].right_col;
     }
     /* output schema (src/join.c:703-784) */
     int *is_rkey = (int *)vg_xcalloc((size_t)(rs->n_cols ? rs->n_cols : 1), sizeof(int));

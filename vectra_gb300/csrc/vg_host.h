@@ -114,6 +114,7 @@ typedef struct {
     VgJoinTable jt;
     int n_keys;
     int32_t lkey[VG_MAX_KEYS];       /* probe-side key columns */
+    int32_t rkey[VG_MAX_KEYS];       /* build-side key columns (index into bcols) */
     int32_t conv[VG_MAX_KEYS];       /* probe key int/bool -> double */
     VgCol *bcols;                    /* device build columns (all right columns) */
     int n_bcols;

@@ -395,9 +395,11 @@ int vgk_group_table_rehash(const VgGroupTable *from, const VgGroupTable *to, int
 /* bytes of spilled cache entries per entry (cache layout, one slot) */
 size_t vgk_agg_cache_bytes(const VgAggLaunch *L, int64_t slots);
 
-/* payload copy of a unique-key single-key join table: bcols[0..n) of the
- * build rows, (cap + 1) entries */
-int vgk_join_payload(const VgJoinTable *jt, const VgCol *cols, int n_cols, VgJPay *pay, vg_stream_t s);
+/* payload copy of a unique-key single-key join table: cols[0..n) of the
+ * build rows, (cap + 1) entries; key: the build key column (direct tables
+ * are filled in build-row order from it) */
+int vgk_join_payload(const VgJoinTable *jt, const VgCol *key, const VgCol *cols, int n_cols, VgJPay *pay,
+                     vg_stream_t s);
 
 /* run-time specialised aggregation kernel (jit_agg.cu): launch returns 1
  * if launched, 0 if the plan shape is not covered, -1 on error */
