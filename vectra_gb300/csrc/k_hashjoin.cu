@@ -248,17 +248,26 @@ __global__ void jt_insert_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, in
 }
 
 __global__ void jt_count_kernel(VgJoinTable jt, uint32_t *counters) {
+    __shared__ unsigned s_nd, s_mx;
+    if (threadIdx.x == 0) { s_nd = 0; s_mx = 0; }
+    __syncthreads();
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int lane = threadIdx.x & 31;
-    for (int64_t b = (int64_t)blockIdx.x * blockDim.x; b < jt.cap; b += stride) {
-        const int64_t s = b + threadIdx.x;
-        const int32_t c = s < jt.cap ? jt.slots[s].count : 0;
-        const unsigned nd = __popc(__ballot_sync(0xFFFFFFFFu, c > 0));
-        const unsigned mx = __reduce_max_sync(0xFFFFFFFFu, (unsigned)c);
-        if (lane == 0) {
-            if (nd) atomicAdd(counters + 0, nd);
-            if (mx > 1) atomicMax(counters + 1, mx);
-        }
+    unsigned nd = 0, mx = 0;
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < jt.cap; s += stride) {
+        const int32_t c = jt.slots[s].count;
+        nd += c > 0;
+        mx = (unsigned)c > mx ? (unsigned)c : mx;
+    }
+    nd = __reduce_add_sync(0xFFFFFFFFu, nd);
+    mx = __reduce_max_sync(0xFFFFFFFFu, mx);
+    if ((threadIdx.x & 31) == 0) {
+        if (nd) atomicAdd(&s_nd, nd);
+        if (mx) atomicMax(&s_mx, mx);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_nd) atomicAdd(counters + 0, s_nd);
+        if (s_mx > 1) atomicMax(counters + 1, s_mx);
     }
 }
 
