@@ -32,7 +32,7 @@ namespace {
 // Launch shape: threads per CTA, CTAs per SM the register budget is set
 // for, rows per thread.  VGPU_JIT_SHAPE="rows,threads,ctas" overrides it
 // (tuning runs).
-struct Shape { int rows = 2, threads = 512, ctas = 2; };
+struct Shape { int rows = 2, threads = 1024, ctas = 1; };
 
 const Shape &shape() {
     static Shape sh;
