@@ -61,6 +61,10 @@ JoinNode *join_node_create(VecNode *left, VecNode *right, JoinKind kind,
 #define VGPU_SRC_COPY    0   /* copy the host columns at creation          */
 #define VGPU_SRC_BORROW  1   /* borrow host columns (caller keeps them)     */
 #define VGPU_SRC_DEVICE  2   /* borrow device-resident columns              */
+#define VGPU_SRC_MAPPED  4   /* borrow page-locked host columns that libvgpu
+                                kernels read in place (cudaHostAlloc /
+                                cudaHostRegister memory; over NVLink-C2C on
+                                Grace systems) -- no staging copy            */
 
 /* A table as a source node, emitting batches of batch_rows rows (a multiple
  * of 32).  data[c]: n_rows int64 / double values or bool bytes;
@@ -68,7 +72,10 @@ JoinNode *join_node_create(VecNode *left, VecNode *right, JoinKind kind,
  * valid.  With VGPU_SRC_DEVICE both are device pointers and libvgpu nodes
  * read the batches in place; any other consumer gets host copies.  With
  * VGPU_SRC_BORROW from page-locked memory, libvgpu nodes copy each batch to
- * the device asynchronously. */
+ * the device asynchronously.  With VGPU_SRC_MAPPED, data and validity must
+ * be memory the device can address; each validity bitmap 4-byte aligned
+ * and padded to whole 32-bit words (as for VGPU_SRC_DEVICE); creation fails
+ * (NULL, vgpu_last_error) otherwise. */
 VecNode *vgpu_table_source_create(int n_cols, const char *const *names,
                                   const int *types, const void *const *data,
                                   const uint8_t *const *validity,

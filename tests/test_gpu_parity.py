@@ -153,3 +153,70 @@ def test_unsupported_is_an_error(G):
     src = make_oracle_source({"s": np.array(["a", "b"], dtype=object), "x": np.array([1.0, 2.0])})
     with pytest.raises(EngineError):
         Tbl(G, src).group_by("s").summarise(n=("n",)).batches()
+
+
+def test_mapped_host_source(G, oracle):
+    """VGPU_SRC_MAPPED: page-locked host columns read in place by the
+    kernels give the same result as the copied path; unpinned memory is
+    refused at creation."""
+    torch = pytest.importorskip("torch")
+    from vectra_gb300 import abi
+    from vectra_gb300.plan import Tbl, tbl, col
+    rng = np.random.default_rng(21)
+    nf, nd = 50_000, 700
+    ids = rng.permutation(nd) + 1
+    fact = {"key": rng.integers(1, nd + 20, nf), "value": rng.lognormal(0, 1, nf)}
+    dim = {"id": ids, "category": rng.integers(0, 9, nd), "weight": rng.random(nd)}
+    fvalid = rng.random(nf) > 0.03
+
+    def pinned(a):
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        return t
+
+    def padded_bits(mask):
+        bits = abi.validity_from_mask(mask)
+        out = np.zeros(((len(bits) + 3) // 4) * 4, np.uint8)
+        out[:len(bits)] = bits
+        return out
+
+    keep = []
+
+    def mapped(table, n, valid=None):
+        cols = {}
+        for name, v in table.items():
+            tv = pinned(v)
+            tm = pinned(padded_bits(valid)) if (valid is not None and name == "value") else None
+            keep.extend([tv, tm])
+            cols[name] = (tv.data_ptr(), tm.data_ptr() if tm is not None else 0,
+                          abi.VEC_DOUBLE if v.dtype == np.float64 else abi.VEC_INT64, n)
+        names = list(cols)
+        data = (C.c_void_p * len(names))(*[cols[k][0] for k in names])
+        val = (C.c_void_p * len(names))(*[cols[k][1] or None for k in names])
+        types = (C.c_int * len(names))(*[cols[k][2] for k in names])
+        cn = (C.c_char_p * len(names))(*[k.encode() for k in names])
+        p = G.lib.vgpu_table_source_create(len(names), cn, types, data, val, n, 8192, 4)
+        return G.check(p, "mapped source")
+
+    def query(fsrc, dsrc):
+        return (Tbl(G, fsrc).left_join(Tbl(G, dsrc), {"key": "id"}).group_by("category")
+                .summarise(temp_dir="tmp", s=("sum", col("value") * col("weight")), n=("n",)).collect())
+
+    got = query(mapped(fact, nf, fvalid), mapped(dim, nd))
+    f2 = dict(fact)
+    f2["value"] = (fact["value"], fvalid)
+    want = (tbl(oracle, f2, batch_rows=8192).left_join(tbl(oracle, dim), {"key": "id"}).group_by("category")
+            .summarise(temp_dir=oracle.tmp, s=("sum", col("value") * col("weight")), n=("n",)).collect())
+    for k in want:
+        assert np.array_equal(got[k][1], want[k][1]), k
+        m = want[k][1]
+        if k == "s":
+            np.testing.assert_allclose(got[k][0][m], want[k][0][m], rtol=RTOL)
+        else:
+            assert np.array_equal(got[k][0][m], want[k][0][m]), k
+    # ordinary (pageable) host memory is refused for in-place reads
+    plain = np.arange(10, dtype=np.int64)
+    cn = (C.c_char_p * 1)(b"k")
+    p = G.lib.vgpu_table_source_create(1, cn, (C.c_int * 1)(abi.VEC_INT64), (C.c_void_p * 1)(plain.ctypes.data),
+                                       None, 10, 32, 4)
+    assert not p
+    assert b"page-locked" in G.lib.vgpu_last_error()

@@ -97,8 +97,8 @@ static void join_build(VgJoin *j) {
     j->n_build = total;
     j->B.n_bcols = nr;
     j->B.bcols = (VgCol *)vg_xcalloc((size_t)(nr ? nr : 1), sizeof(VgCol));
-    if (nb == 1 && !bs[0].d_sel) {
-        /* one batch without a selection: its device columns are the build
+    if (nb == 1 && !bs[0].d_sel && !bs[0].in_host) {
+        /* one device batch without a selection: its columns are the build
          * columns as they are (kept until the node is freed) */
         for (int c = 0; c < nr; c++) {
             j->B.bcols[c].type = rs->col_types[c];

@@ -2,12 +2,14 @@
  * source.c -- a table as a source node.  For any consumer it behaves like
  * the reference's ScanNode (src/scan.c:107-127): each next_batch returns a
  * malloc-owned copy of the next batch_rows rows.  libvgpu nodes instead pull
- * batches straight onto the device: in place for device-resident tables,
- * by asynchronous copies for host tables.
+ * batches straight onto the device: in place for device-resident tables
+ * and for mapped page-locked host tables (the kernels read host memory),
+ * by asynchronous copies for other host tables.
  */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <cuda_runtime_api.h>
 #include "vg_host.h"
 
 typedef struct {
@@ -93,9 +95,10 @@ int vg_source_pull(VecNode *n, const uint8_t *need, VgDBatch *out) {
     out->n_cols = s->n_cols;
     out->row_base = lo;
     out->cols = (VgCol *)vg_xcalloc((size_t)s->n_cols, sizeof(VgCol));
-    if (s->flags & VGPU_SRC_DEVICE) {
+    if (s->flags & (VGPU_SRC_DEVICE | VGPU_SRC_MAPPED)) {
         /* in place; validity bitmaps are 4-byte aligned, row lo sits at bit
          * lo%32 of word lo/32 */
+        out->in_host = (s->flags & VGPU_SRC_MAPPED) != 0;
         for (int c = 0; c < s->n_cols; c++) {
             out->cols[c].type = s->types[c];
             out->cols[c].data = (const char *)s->data[c] + (size_t)lo * elem(s->types[c]);
@@ -139,7 +142,7 @@ int vg_source_pull(VecNode *n, const uint8_t *need, VgDBatch *out) {
 
 static void source_free(VecNode *self) {
     VgSource *s = (VgSource *)self;
-    if (!(s->flags & (VGPU_SRC_BORROW | VGPU_SRC_DEVICE))) {
+    if (!(s->flags & (VGPU_SRC_BORROW | VGPU_SRC_DEVICE | VGPU_SRC_MAPPED))) {
         for (int c = 0; c < s->n_cols; c++) {
             free(s->data[c]);
             free(s->validity[c]);
@@ -163,6 +166,28 @@ VecNode *vgpu_table_source_create(int n_cols, const char *const *names, const in
             return NULL;
         }
     }
+    if (flags & VGPU_SRC_MAPPED) {
+        /* every buffer must be host memory the device addresses directly */
+        for (int c = 0; c < n_cols; c++) {
+            const void *bufs[2] = {data[c], validity ? validity[c] : NULL};
+            for (int b = 0; b < 2; b++) {
+                if (!bufs[b]) continue;
+                struct cudaPointerAttributes a;
+                memset(&a, 0, sizeof(a));
+                if (cudaPointerGetAttributes(&a, bufs[b]) != cudaSuccess || a.type != cudaMemoryTypeHost ||
+                    a.devicePointer != bufs[b]) {
+                    cudaGetLastError();
+                    vg_set_error("table source: column '%s' is not page-locked host memory the device can "
+                                 "address in place", names[c]);
+                    return NULL;
+                }
+                if (b == 1 && ((uintptr_t)bufs[b] & 3)) {
+                    vg_set_error("table source: validity of column '%s' is not 4-byte aligned", names[c]);
+                    return NULL;
+                }
+            }
+        }
+    }
     VgSource *s = (VgSource *)vg_xcalloc(1, sizeof(VgSource));
     s->n_cols = n_cols;
     s->flags = flags;
@@ -175,7 +200,7 @@ VecNode *vgpu_table_source_create(int n_cols, const char *const *names, const in
     for (int c = 0; c < n_cols; c++) {
         s->types[c] = types[c];
         ts[c] = (VecType)types[c];
-        if (flags & (VGPU_SRC_BORROW | VGPU_SRC_DEVICE)) {
+        if (flags & (VGPU_SRC_BORROW | VGPU_SRC_DEVICE | VGPU_SRC_MAPPED)) {
             s->data[c] = (void *)data[c];
             s->validity[c] = validity ? (uint8_t *)validity[c] : NULL;
         } else {

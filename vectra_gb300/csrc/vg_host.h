@@ -52,6 +52,7 @@ typedef struct {
     VecBatch *host;            /* the host batch it came from (owned) or NULL */
     void *block;               /* device allocation holding uploaded data */
     int64_t row_base;          /* stream position of physical row 0 */
+    int in_host;               /* columns are page-locked host memory read in place */
 } VgDBatch;
 
 /* Pulls the next batch of `child` with the columns flagged in need[]
