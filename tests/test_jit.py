@@ -20,3 +20,12 @@ def test_generated_kernel_compiles(shape):
     assert 0 < regs.value <= 64, log
     spills = re.findall(r"(\d+) bytes spill stores", log)
     assert spills and all(int(x) == 0 for x in spills), log
+
+
+def test_digit_split_32bit_matches_64bit():
+    """The specialised kernel's 32-bit digit split of a double equals the
+    64-bit split every other path uses (edge patterns + 4M random ones)."""
+    import vectra_gb300
+    lib = vectra_gb300.load()
+    lib.vgk_digits_selftest.restype = C.c_longlong
+    assert lib.vgk_digits_selftest(C.c_longlong(4_000_000), C.c_ulonglong(0x9E3779B97F4A7C15)) == 0

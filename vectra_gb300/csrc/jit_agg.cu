@@ -512,3 +512,35 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
     }
     return vgk_agg_jit_compile_only(&L, regs);
 }
+
+// Host check of the 32-bit digit split against the 64-bit one on n bit
+// patterns (edge cases first, then a xorshift sequence from seed):
+// returns the number of mismatches.
+extern "C" long long vgk_digits_selftest(long long n, unsigned long long seed) {
+    const uint64_t edge[] = {0ull, 0x8000000000000000ull, 1ull, 0x8000000000000001ull, 0x000FFFFFFFFFFFFFull,
+                             0x0010000000000000ull, 0x3FF0000000000000ull, 0xBFF0000000000000ull,
+                             0x7FEFFFFFFFFFFFFFull, 0xFFEFFFFFFFFFFFFFull, 0x7FF0000000000000ull,
+                             0xFFF0000000000000ull, 0x7FF8000000000000ull, 0x7FF0000000000001ull,
+                             0x4330000000000000ull, 0x433FFFFFFFFFFFFFull, 0x0000000100000000ull};
+    long long bad = 0;
+    uint64_t x = seed | 1;
+    for (long long i = 0; i < n; i++) {
+        uint64_t b;
+        if (i < (long long)(sizeof(edge) / sizeof(edge[0]))) {
+            b = edge[i];
+        } else {
+            x ^= x << 13; x ^= x >> 7; x ^= x << 17;
+            b = x;
+        }
+        const VgDigits r = vg_split_double(b);
+        const VgDigits32 q = vg_split_double32(b);
+        if (r.special != q.special) { bad++; continue; }
+        if (r.special) continue;
+        if ((r.lo < 0) != (q.zero != 0)) { bad++; continue; }
+        if (r.lo < 0) continue;
+        const int64_t s = q.neg ? -1 : 1;
+        if (r.lo != q.word || r.d0 != s * (int64_t)q.d0 || r.d1 != s * (int64_t)q.d1 || r.d2 != s * (int64_t)q.d2)
+            bad++;
+    }
+    return bad;
+}

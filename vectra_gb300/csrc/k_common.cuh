@@ -185,7 +185,7 @@ struct VgDigits {
     uint32_t special;  // bit2 NaN, bit3 +inf, bit4 -inf
 };
 
-VG_DEV VgDigits vg_split_double(uint64_t bits) {
+__host__ __device__ inline VgDigits vg_split_double(uint64_t bits) {
     VgDigits r;
     uint32_t e = (uint32_t)((bits >> 52) & 0x7FF);
     uint64_t f = bits & 0x000FFFFFFFFFFFFFull;
@@ -209,6 +209,43 @@ VG_DEV VgDigits vg_split_double(uint64_t bits) {
     int64_t a2 = (int64_t)high;
     if (neg) { a0 = -a0; a1 = -a1; a2 = -a2; }
     r.d0 = a0; r.d1 = a1; r.d2 = a2;
+    return r;
+}
+
+// The same split in 32-bit arithmetic, as magnitudes and a sign: the
+// digits of |x| are d0, d1, d2 (unsigned) at digit index `word`.  zero:
+// x is +-0 (nothing to add); special: as in VgDigits.
+struct VgDigits32 {
+    int word;
+    uint32_t d0, d1, d2;
+    uint32_t neg;
+    uint32_t special;
+    uint32_t zero;
+};
+
+__host__ __device__ inline VgDigits32 vg_split_double32(uint64_t bits) {
+    VgDigits32 r;
+    const uint32_t hi = (uint32_t)(bits >> 32), lo = (uint32_t)bits;
+    const uint32_t e = (hi >> 20) & 0x7FFu;
+    const uint32_t fh = hi & 0xFFFFFu;
+    r.neg = hi >> 31;
+    r.special = 0;
+    r.zero = 0;
+    r.word = 0;
+    r.d0 = r.d1 = r.d2 = 0;
+    if (e == 0x7FFu) {
+        r.special = (fh | lo) ? 4u : (r.neg ? 16u : 8u);
+        return r;
+    }
+    const uint32_t mh = fh | (e ? 0x100000u : 0u);
+    if ((mh | lo) == 0) { r.zero = 1; return r; }
+    const uint32_t sh = e ? e - 1 : 0;
+    const uint32_t off = sh & 31u;
+    r.word = (int)(sh >> 5);
+    // (mh:lo) << off spread over three 32-bit digits
+    r.d0 = lo << off;
+    r.d1 = off ? (mh << off) | (lo >> (32 - off)) : mh;
+    r.d2 = off ? mh >> (32 - off) : 0u;
     return r;
 }
 

@@ -167,6 +167,46 @@ VG_DEV uint32_t term_mask(const VgAggLaunch &L, const Rows &X) {
     return m;
 }
 
+// One digit magnitude into a cache (lo, hi) word pair: add, or subtract for
+// a negative summand, with the carry / borrow of the low word applied to
+// the high word (exact; one atomic unless the low word wraps).
+VG_DEV void digit_add(uint32_t *lo, int32_t *hi, uint32_t d, uint32_t neg) {
+    if (!d) return;
+    if (!neg) {
+        const uint32_t old = atomicAdd(lo, d);
+        if (old + d < old) atomicAdd(hi, 1);
+    } else {
+        const uint32_t old = atomicSub(lo, d);
+        if (old < d) atomicAdd(hi, -1);
+    }
+}
+
+// A double into a cache slot's digit window (same representation as
+// cwin_add, in 32-bit arithmetic).  False: outside the window.
+template <int S>
+VG_DEV bool cache_sum_f64(char *sm, uint32_t OBASE, uint32_t OWIN, uint32_t *flags, int slot, uint64_t bits) {
+    const VgDigits32 d = vg_split_double32(bits);
+    if (d.special) { set_flags(flags, d.special); return true; }
+    if (d.zero) return true;
+    int32_t *bp = (int32_t *)(sm + OBASE) + slot;
+    int b = *(volatile int *)bp;
+    if (b == kBaseUnset) {
+        int want = d.word - 2;
+        if (want < 0) want = 0;
+        if (want > VG_LACC_WORDS - kWin) want = VG_LACC_WORDS - kWin;
+        const int prev = atomicCAS((int *)bp, kBaseUnset, want);
+        b = (prev == kBaseUnset) ? want : prev;
+    }
+    const int rel = d.word - b;
+    if (rel < 0 || rel + (d.d2 ? 3 : 2) > kWin) return false;
+    uint32_t *wl = (uint32_t *)(sm + OWIN) + slot + rel * S;
+    int32_t *wh = (int32_t *)(sm + OWIN + 4 * S * kWin) + slot + rel * S;
+    digit_add(wl, wh, d.d0, d.neg);
+    digit_add(wl + S, wh + S, d.d1, d.neg);
+    digit_add(wl + 2 * S, wh + 2 * S, d.d2, d.neg);
+    return true;
+}
+
 // Accumulator update in the shared cache at compile-time layout offsets.
 // False: the value falls outside the cache's digit window (the caller
 // then updates the global table).
@@ -187,11 +227,7 @@ VG_DEV bool cache_acc(char *sm, int slot, InVal x) {
         return true;
     }
     if (CLS == VG_ACC_SUM_F64) {
-        const VgDigits d = vg_split_double(x.bits);
-        if (d.special) set_flags(flags, d.special);
-        else if (d.lo >= 0 && !cwin_add((int32_t *)(sm + OBASE) + slot, (uint32_t *)(sm + OWIN) + slot,
-                                        (int32_t *)(sm + OWIN + 4 * S * kWin) + slot, S, d))
-            return false;
+        if (!cache_sum_f64<S>(sm, OBASE, OWIN, flags, slot, x.bits)) return false;
         if (COUNT) atomicAdd(cnt, 1u);
         return true;
     }
