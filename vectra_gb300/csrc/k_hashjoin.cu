@@ -86,10 +86,22 @@ VG_DEV int32_t *jt_count_ptr(const VgJoinTable &jt, int64_t slot) {
     return jt.slots ? &jt.slots[slot].count : jt.count + slot;
 }
 
-__global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters) {
+// Payload columns written by the build itself (direct tables).
+struct PayArgs {
+    VgCol c0, c1;
+    int n_cols;
+    VgJPay *pay;             // NULL: none requested
+};
+
+__global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters, VgJPay *pay) {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n = jt.slots ? jt.cap + 1 : jt.cap;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (pay) {
+            ulonglong2 *o = (ulonglong2 *)(pay + i);
+            o[0] = make_ulonglong2(0ull, 0ull);
+            o[1] = make_ulonglong2(0ull, 0ull);
+        }
         if (jt.slots) {
             jt.slots[i].key = VG_JEMPTY;
             jt.slots[i].start = 0;
@@ -229,7 +241,7 @@ __global__ void jt_pay_kernel(VgJoinTable jt, VgCol c0, VgCol c1, int n_cols, Vg
 // pass over the slots afterwards (jt_count_kernel).  With duplicates the
 // start written here is replaced by the sorted layout (seg_start_kernel).
 __global__ void jt_insert_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t *rslot,
-                                        uint32_t *counters) {
+                                        uint32_t *counters, PayArgs P) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     uint64_t k[VG_MAX_KEYS];
@@ -242,6 +254,22 @@ __global__ void jt_insert_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, in
             jt.slots[d].key = k[0];
             jt.slots[d].start = (int32_t)r;
             atomicAdd(&jt.slots[d].count, 1);
+            if (P.pay) {
+                // the payload entry of this key (meaningful when keys are unique)
+                uint64_t p0 = 0, p1 = 0;
+                uint32_t meta = 1u;
+                if (P.n_cols > 0) {
+                    p0 = vg_load_bits(P.c0, r);
+                    if (vg_valid(P.c0, r)) meta |= 2u;
+                }
+                if (P.n_cols > 1) {
+                    p1 = vg_load_bits(P.c1, r);
+                    if (vg_valid(P.c1, r)) meta |= 4u;
+                }
+                ulonglong2 *o = (ulonglong2 *)(P.pay + d);
+                o[0] = make_ulonglong2(k[0], (unsigned long long)(uint32_t)r | ((unsigned long long)meta << 32));
+                o[1] = make_ulonglong2(p0, p1);
+            }
         }
     }
     rslot[r] = (int32_t)d;
@@ -420,7 +448,7 @@ size_t vgk_join_build_scratch_bytes(int64_t n_build) {
 // the caller; on return jt->rows is NULL when every key is unique.
 int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t *key_conv,
                    int64_t n_build, void *d_scratch, size_t scratch_bytes, int64_t *h_distinct,
-                   int64_t *h_maxdup, vg_stream_t s) {
+                   int64_t *h_maxdup, const VgCol *pay_cols, int n_pay, VgJPay *pay, vg_stream_t s) {
     cudaStream_t st = (cudaStream_t)s;
     if (scratch_bytes < vgk_join_build_scratch_bytes(n_build)) {
         snprintf(g_err, sizeof(g_err), "join build scratch too small");
@@ -440,12 +468,20 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         K.conv[i] = key_conv[i];
         K.types[i] = jt->key_types[i];
     }
-    { jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters); vg_launch_counter++; }
+    PayArgs P;
+    memset(&P, 0, sizeof(P));
+    if (pay && jt->direct && jt->slots && n_pay >= 0 && n_pay <= 2) {
+        P.pay = pay;
+        P.n_cols = n_pay;
+        if (n_pay > 0) P.c0 = pay_cols[0];
+        if (n_pay > 1) P.c1 = pay_cols[1];
+    }
+    { jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters, P.pay); vg_launch_counter++; }
     vg_prof_begin(VG_PROF_JOIN_BUILD, st);
     if (jt->direct) {
         if (n_build > 0) {
             jt_insert_direct_kernel<<<(unsigned)((n_build + 255) / 256), 256, 0, st>>>(*jt, K, n_build, rslot,
-                                                                                  counters);
+                                                                                  counters, P);
             vg_launch_counter++;
         }
         { jt_count_kernel<<<grid_for(jt->cap, 256), 256, 0, st>>>(*jt, counters); vg_launch_counter++; }
@@ -465,6 +501,8 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
     *h_maxdup = hc[1];
     if (hc[1] <= 1) {
         jt->rows = nullptr;    // start[slot] is the build row itself
+        // hashed tables: the payload copy from the finished slots
+        if (pay && !P.pay && jt->slots) return vgk_join_payload(jt, nullptr, pay_cols, n_pay, pay, s);
         return 0;
     }
     // duplicates: stable sort of (slot, row) lays out each key's rows in

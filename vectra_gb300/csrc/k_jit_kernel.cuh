@@ -178,7 +178,7 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
 #if VGJ_DENSE
             (void)cache_used;
             found = nm ? L.dense_n : (int)((int64_t)k.w[0] - L.dense_min);
-            if (st[found] != 2u) st[found] = 2u;      // first touch marks the slot live
+            st[found] = 2u;                           // every touch marks the slot live (same value)
 #else
             {
                 int err = 0;

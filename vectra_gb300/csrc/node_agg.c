@@ -77,12 +77,11 @@ static int resolve_operand(Plan *P, VecNode *at, const char *name, VgOperand *o)
             VecNode *l = vg_join_left(at);
             return resolve_operand(P, l, l->output_schema.col_names[col], o);
         }
-        const VgJoinBuilt *B = vg_join_build_now(at);
         int j = vg_colset_add(&P->bset, col);
         if (j < 0) return 0;
         o->side = VG_SIDE_BUILD;
         o->col = j;
-        o->type = B->bcols[col].type;
+        o->type = vg_join_right_type(at, col);
         return o->type != VEC_STRING;
     }
     if (at == P->filter) {
@@ -468,7 +467,12 @@ static VecBatch *agg_next(VecNode *self) {
     }
     const VgJoinBuilt *B = NULL;
     if (P.join) {
-        B = vg_join_build_now(P.join);
+        /* up to two build columns travel in a payload copy of the join
+         * table (one sector per probe row in the specialised kernel) */
+        const VgJPay *pay = NULL;
+        B = vg_join_build_payload(P.join, P.bset.idx, P.bset.n, &pay);
+        L->jpay = pay;
+        L->jpay_n = pay ? P.bset.n : 0;
         L->has_join = 1;
         L->join_kind = vg_join_kind(P.join);
         L->n_jkeys = B->n_keys;
@@ -522,18 +526,12 @@ static VecBatch *agg_next(VecNode *self) {
             L->dense_min = mm[0];
         }
     }
-    /* the run-time specialised kernel reads up to two build columns from a
-     * payload copy of the join table: one sector per probe row */
-    VgJPay *jpay = NULL;
-    if (B && L->jt.slots && !L->jt.rows && L->n_bcols >= 1 && L->n_bcols <= 2 && vgk_agg_jit_ok(L)) {
-        jpay = (VgJPay *)vg_dmalloc((size_t)(L->jt.cap + 1) * sizeof(VgJPay));
-        vg_check_rc(vgk_join_payload(&L->jt, &B->bcols[B->rkey[0]], L->bcols, L->n_bcols, jpay, vg_stream()),
-                    "join payload");
-        L->jpay = jpay;
-        L->jpay_n = L->n_bcols;
-    }
-
-    Table T;
+        /* up to two build columns travel in a payload copy of the join
+         * table (one sector per probe row in the specialised kernel) */
+        const VgJPay *pay = NULL;
+        B = vg_join_build_payload(P.join, P.bset.idx, P.bset.n, &pay);
+        L->jpay = pay;
+        L->jpay_n = pay ? P.bset.n : 0;    Table T;
     table_alloc(&T, &P, 8192);
     Spill S;
     memset(&S, 0, sizeof(S));
@@ -553,7 +551,6 @@ static VecBatch *agg_next(VecNode *self) {
         batch_idx++;
     }
     VecBatch *res = emit_result(A, &P, &T);
-    vg_dfree(jpay);
     vg_dfree(T.block);
     vg_dfree(S.rows);
     vg_dfree(S.cache);

@@ -32,6 +32,9 @@ typedef struct {
     void *build_block;        /* device build columns */
     VgDBatch kept;            /* the one build batch, used in place */
     int has_kept;
+    VgJPay *pay;              /* payload copy requested by a fused aggregation */
+    int pay_n;
+    int32_t pay_col[2];
     void *table_block;        /* device hash table */
     int *r_nonkey;
     int r_nonkey_n;
@@ -67,7 +70,9 @@ static int common_type(int a, int b) {
 static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 static size_t elem(int t) { return t == VEC_BOOL ? 1 : 8; }
 
-/* BUILD: materialise the right side on the device, then the hash table */
+/* BUILD: materialise the right side on the device, then the hash table
+ * (and, when a fused aggregation asked for it, the payload copy of up to
+ * two right columns: pay_n / pay_col set before the build) */
 static void join_build(VgJoin *j) {
     if (j->built) return;
     const VecSchema *rs = &j->jn.right->output_schema;
@@ -188,10 +193,17 @@ static void join_build(VgJoin *j) {
     jt->rows = (int32_t *)(t + o); o += rows_b;
     jt->err = (uint32_t *)(t + o);
     jt->n_build = total;
+    VgCol pc[2];
+    memset(pc, 0, sizeof(pc));
+    if (j->pay_n > 0 && nk == 1) {
+        for (int q = 0; q < j->pay_n; q++) pc[q] = j->B.bcols[j->pay_col[q]];
+        j->pay = (VgJPay *)vg_dmalloc((size_t)(tcap + 1) * sizeof(VgJPay));
+    }
     size_t sb = vgk_join_build_scratch_bytes(total);
     void *scratch = vg_dmalloc(sb);
     int64_t distinct = 0, maxdup = 0;
-    int rc = vgk_join_build(jt, kc, nk, j->conv_build, total, scratch, sb, &distinct, &maxdup, vg_stream());
+    int rc = vgk_join_build(jt, kc, nk, j->conv_build, total, scratch, sb, &distinct, &maxdup, pc,
+                            j->pay ? j->pay_n : 0, j->pay, vg_stream());
     vg_dfree(scratch);
     vg_check_rc(rc, "join build");
     if (j->jn.kind == JOIN_FULL) {
@@ -206,6 +218,26 @@ const VgJoinBuilt *vg_join_build_now(VecNode *n) {
     VgJoin *j = (VgJoin *)n;
     join_build(j);
     return &j->B;
+}
+
+const VgJoinBuilt *vg_join_build_payload(VecNode *n, const int32_t *cols, int n_cols, const VgJPay **pay) {
+    VgJoin *j = (VgJoin *)n;
+    *pay = NULL;
+    if (!j->built && n_cols >= 1 && n_cols <= 2) {
+        j->pay_n = n_cols;
+        for (int q = 0; q < n_cols; q++) j->pay_col[q] = cols[q];
+    }
+    join_build(j);
+    /* usable only for unique single keys built with the same columns */
+    if (j->pay && !j->B.jt.rows && j->pay_n == n_cols &&
+        (n_cols < 1 || j->pay_col[0] == cols[0]) && (n_cols < 2 || j->pay_col[1] == cols[1]))
+        *pay = j->pay;
+    return &j->B;
+}
+
+int vg_join_right_type(VecNode *n, int col) {
+    VgJoin *j = (VgJoin *)n;
+    return j->jn.right->output_schema.col_types[col];
 }
 
 /* one probe batch -> one output batch (NULL if empty) */
@@ -361,6 +393,7 @@ static void join_free(VecNode *self) {
     free(j->B.bcols);
     vg_dfree(j->build_block);
     if (j->has_kept) vg_dbatch_release(&j->kept);
+    vg_dfree(j->pay);
     vg_dfree(j->table_block);
     vg_dfree(j->d_matched);
     vg_dfree(j->d_unmatched);

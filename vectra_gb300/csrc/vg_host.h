@@ -122,6 +122,11 @@ typedef struct {
     int kind;
 } VgJoinBuilt;
 const VgJoinBuilt *vg_join_build_now(VecNode *n);
+/* builds with a payload copy of right columns cols[0..n_cols) (n_cols <= 2);
+ * *pay = the copy, or NULL when it does not apply (duplicate or composite
+ * keys, table already built) */
+const VgJoinBuilt *vg_join_build_payload(VecNode *n, const int32_t *cols, int n_cols, const VgJPay **pay);
+int vg_join_right_type(VecNode *n, int col);
 VecNode *vg_join_left(VecNode *n);
 int vg_join_kind(VecNode *n);
 /* resolves an output column name of the join: side 0 = left column index,
