@@ -526,12 +526,8 @@ static VecBatch *agg_next(VecNode *self) {
             L->dense_min = mm[0];
         }
     }
-        /* up to two build columns travel in a payload copy of the join
-         * table (one sector per probe row in the specialised kernel) */
-        const VgJPay *pay = NULL;
-        B = vg_join_build_payload(P.join, P.bset.idx, P.bset.n, &pay);
-        L->jpay = pay;
-        L->jpay_n = pay ? P.bset.n : 0;    Table T;
+
+    Table T;
     table_alloc(&T, &P, 8192);
     Spill S;
     memset(&S, 0, sizeof(S));
