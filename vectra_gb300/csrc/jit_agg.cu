@@ -29,20 +29,21 @@
 
 namespace {
 
-// Launch shape: threads per CTA, CTAs per SM the register budget is set
-// for, rows per thread.  VGPU_JIT_SHAPE="rows,threads,ctas" overrides it
-// (tuning runs).
-struct Shape { int rows = 2, threads = 1024, ctas = 1; };
+// Launch shape: rows per thread, threads per CTA, CTAs per SM the register
+// budget is set for, and whether the next rows' loads are issued before the
+// current rows are processed.  VGPU_JIT_SHAPE="rows,threads,ctas[,pipe]"
+// overrides it (tuning runs).
+struct Shape { int rows = 2, threads = 1024, ctas = 1, pipe = 1; };
 
 const Shape &shape() {
     static Shape sh;
     static bool init = false;
     if (!init) {
         const char *e = getenv("VGPU_JIT_SHAPE");
-        int r, t, c;
-        if (e && sscanf(e, "%d,%d,%d", &r, &t, &c) == 3 && (r == 2 || r == 4) && t >= 64 && t <= 1024 &&
-            (t & 31) == 0 && c >= 1 && c <= 8)
-            sh.rows = r, sh.threads = t, sh.ctas = c;
+        int r, t, c, p = 1;
+        if (e && sscanf(e, "%d,%d,%d,%d", &r, &t, &c, &p) >= 3 && (r == 2 || r == 4) && t >= 64 && t <= 1024 &&
+            (t & 31) == 0 && c >= 1 && c <= 8 && (p == 0 || p == 1))
+            sh.rows = r, sh.threads = t, sh.ctas = c, sh.pipe = p;
         init = true;
     }
     return sh;
@@ -147,7 +148,8 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec) {
         L.has_join ? L.n_bcols : 0);
     s += "#include \"k_jit_lib.cuh\"\n";
     fmt(s, "#define VGJ_THREADS %d\n#define VGJ_MINB %d\n#define VGJ_S %d\n", shape().threads, shape().ctas, S);
-    fmt(s, "#define VGJ_SEL %d\n#define VGJ_VEC %d\n", L.sel ? 1 : 0, vec ? 1 : 0);
+    fmt(s, "#define VGJ_SEL %d\n#define VGJ_VEC %d\n#define VGJ_PIPE %d\n", L.sel ? 1 : 0, vec ? 1 : 0,
+        (!L.sel && shape().pipe) ? 1 : 0);
     fmt(s, "#define VGJ_PRED %d\n#define VGJ_JOIN %d\n#define VGJ_PAY %d\n", L.pred.n_terms > 0 ? 1 : 0,
         L.has_join ? 1 : 0, (L.has_join && L.jpay && L.jpay_n == L.n_bcols && L.n_bcols >= 1) ? 1 : 0);
     if (L.has_join)

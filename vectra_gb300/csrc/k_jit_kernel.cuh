@@ -44,7 +44,23 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
     const KeyTypes kt = key_types(L);
 
     const int64_t tile = (int64_t)R * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * tile; base < n_rows; base += (int64_t)gridDim.x * tile) {
+    const int64_t step = (int64_t)gridDim.x * tile;
+#if VGJ_PIPE
+    // software pipeline: the probe columns of a thread's next rows are
+    // loaded before its current rows are processed
+    Rows Xn;
+    {
+        const int64_t r0n = (int64_t)blockIdx.x * tile + (int64_t)R * threadIdx.x;
+        if (r0n < n_rows) {
+            const int nvn = (int)(n_rows - r0n < R ? n_rows - r0n : R);
+            int64_t physn[R];
+#pragma unroll
+            for (int j = 0; j < R; j++) physn[j] = r0n + j;
+            vgj_load_probe(L, Xn, r0n, nvn, VGJ_VEC && nvn == R, physn, (1u << nvn) - 1u);
+        }
+    }
+#endif
+    for (int64_t base = (int64_t)blockIdx.x * tile; base < n_rows; base += step) {
         const int64_t r0 = base + (int64_t)R * threadIdx.x;
         if (r0 >= n_rows) continue;
         const int nv = (int)(n_rows - r0 < R ? n_rows - r0 : R);
@@ -59,7 +75,21 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
 #endif
         }
         Rows X;
+#if VGJ_PIPE
+        X = Xn;
+        {
+            const int64_t r0n = r0 + step;
+            if (r0n < n_rows) {
+                const int nvn = (int)(n_rows - r0n < R ? n_rows - r0n : R);
+                int64_t physn[R];
+#pragma unroll
+                for (int j = 0; j < R; j++) physn[j] = r0n + j;
+                vgj_load_probe(L, Xn, r0n, nvn, VGJ_VEC && nvn == R, physn, (1u << nvn) - 1u);
+            }
+        }
+#else
         vgj_load_probe(L, X, r0, nv, VGJ_VEC && nv == R, phys, all);
+#endif
         uint32_t live = all;
 #if VGJ_PRED
         live &= vgj_pred(L, X);
