@@ -1,6 +1,7 @@
 """The run-time specialised aggregation kernel: representative plan shapes
 are generated and compiled for sm_103a with NVRTC (no device needed), with
-no register spills at the default launch shape."""
+no register spills (a plan that would spill at 1024 threads per CTA is
+compiled for fewer threads)."""
 import ctypes as C
 import re
 
@@ -17,7 +18,7 @@ def test_generated_kernel_compiles(shape):
     rc = lib.vgpu_jit_selftest(shape, C.byref(regs))
     log = lib.vgk_jit_error().decode()
     assert rc == 0, log
-    assert 0 < regs.value <= 64, log
+    assert 0 < regs.value <= 128, log
     spills = re.findall(r"(\d+) bytes spill stores", log)
     assert spills and all(int(x) == 0 for x in spills), log
 

@@ -55,6 +55,7 @@ struct JitKernel {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t kernel = nullptr;
     int smem_set = 0;
+    Shape shape;             // the launch shape it was compiled for
 };
 
 std::mutex g_mu;
@@ -137,19 +138,19 @@ int vgk_agg_jit_source(const VgAggLaunch *L, int S, char *out, size_t out_bytes)
 
 namespace {
 
-std::string gen_source(const VgAggLaunch &L, int S, bool vec) {
+std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
     VgAggLaunch T = L;
     T.cache_slots = S;
     Lay c;
     make_lay(T, (uint64_t)S, c);
     std::string s;
     s += "// generated by jit_agg.cu\n";
-    fmt(s, "#define VGJ_R %d\n#define VGJ_NPC %d\n#define VGJ_NBC %d\n", shape().rows, L.n_pcols,
+    fmt(s, "#define VGJ_R %d\n#define VGJ_NPC %d\n#define VGJ_NBC %d\n", sh.rows, L.n_pcols,
         L.has_join ? L.n_bcols : 0);
     s += "#include \"k_jit_lib.cuh\"\n";
-    fmt(s, "#define VGJ_THREADS %d\n#define VGJ_MINB %d\n#define VGJ_S %d\n", shape().threads, shape().ctas, S);
+    fmt(s, "#define VGJ_THREADS %d\n#define VGJ_MINB %d\n#define VGJ_S %d\n", sh.threads, sh.ctas, S);
     fmt(s, "#define VGJ_SEL %d\n#define VGJ_VEC %d\n#define VGJ_PIPE %d\n", L.sel ? 1 : 0, vec ? 1 : 0,
-        (!L.sel && shape().pipe) ? 1 : 0);
+        (!L.sel && sh.pipe) ? 1 : 0);
     fmt(s, "#define VGJ_PRED %d\n#define VGJ_JOIN %d\n#define VGJ_PAY %d\n", L.pred.n_terms > 0 ? 1 : 0,
         L.has_join ? 1 : 0, (L.has_join && L.jpay && L.jpay_n == L.n_bcols && L.n_bcols >= 1) ? 1 : 0);
     if (L.has_join)
@@ -230,7 +231,9 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec) {
     return s;
 }
 
-int compile(const std::string &src, JitKernel &out) {
+// NVRTC: source -> cubin.  *spill: bytes of register spill stores ptxas
+// reported; *log_out (optional): the compile log.
+int nvrtc_cubin(const std::string &src, std::vector<char> &cubin, int *spill, std::string *log_out) {
     nvrtcProgram prog;
     nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "vg_jit_agg.cu", kJitHeaderCount, kJitHeaderSources,
                                        kJitHeaderNames);
@@ -238,23 +241,52 @@ int compile(const std::string &src, JitKernel &out) {
         snprintf(g_jit_err, sizeof(g_jit_err), "nvrtcCreateProgram: %s", nvrtcGetErrorString(r));
         return -1;
     }
-    const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--generate-line-info"};
-    r = nvrtcCompileProgram(prog, 3, opts);
+    const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--generate-line-info", "--ptxas-options=-v"};
+    r = nvrtcCompileProgram(prog, 4, opts);
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    std::vector<char> log(n + 1, 0);
+    nvrtcGetProgramLog(prog, log.data());
+    if (log_out) *log_out = log.data();
     if (r != NVRTC_SUCCESS) {
-        size_t n = 0;
-        nvrtcGetProgramLogSize(prog, &n);
-        std::vector<char> log(n + 1, 0);
-        nvrtcGetProgramLog(prog, log.data());
         snprintf(g_jit_err, sizeof(g_jit_err), "NVRTC: %s\n%.1800s", nvrtcGetErrorString(r), log.data());
         nvrtcDestroyProgram(&prog);
         return -1;
     }
-    size_t n = 0;
+    const char *sp = strstr(log.data(), "bytes spill stores");
+    int spills = 0;
+    if (sp) {
+        const char *q = sp;
+        while (q > log.data() && q[-1] == ' ') q--;
+        while (q > log.data() && q[-1] >= '0' && q[-1] <= '9') q--;
+        spills = atoi(q);
+    }
+    *spill = spills;
     nvrtcGetCUBINSize(prog, &n);
-    std::vector<char> cubin(n);
+    cubin.resize(n);
     nvrtcGetCUBIN(prog, cubin.data());
     nvrtcDestroyProgram(&prog);
     g_compiles++;
+    return 0;
+}
+
+// Compiles the plan at the preferred launch shape; if ptxas had to spill
+// registers there, at half the threads per CTA (twice the registers per
+// thread), down to 256.  out.shape records the shape compiled for.
+int compile_plan(const VgAggLaunch &L, int S, bool vec, std::vector<char> &cubin, Shape &used,
+                 std::string *log_out) {
+    Shape sh = shape();
+    for (;;) {
+        int spill = 0;
+        if (nvrtc_cubin(gen_source(L, S, vec, sh), cubin, &spill, log_out) != 0) return -1;
+        if (spill == 0 || sh.threads <= 256) break;
+        sh.threads /= 2;
+    }
+    used = sh;
+    return 0;
+}
+
+int load_kernel(const std::vector<char> &cubin, JitKernel &out) {
     cudaError_t e = cudaLibraryLoadData(&out.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
     if (e != cudaSuccess) {
         snprintf(g_jit_err, sizeof(g_jit_err), "cudaLibraryLoadData: %s", cudaGetErrorString(e));
@@ -282,7 +314,7 @@ bool vec_ok(const VgAggLaunch &L) {
 extern "C" {
 
 int vgk_agg_jit_source(const VgAggLaunch *L, int S, char *out, size_t out_bytes) {
-    std::string s = gen_source(*L, S, vec_ok(*L));
+    std::string s = gen_source(*L, S, vec_ok(*L), shape());
     if (s.size() + 1 > out_bytes) return (int)(s.size() + 1);
     memcpy(out, s.c_str(), s.size() + 1);
     return 0;
@@ -292,24 +324,17 @@ int vgk_agg_jit_source(const VgAggLaunch *L, int S, char *out, size_t out_bytes)
 // 0 on success, -1 with vgk_jit_error() set.
 int vgk_agg_jit_compile_only(const VgAggLaunch *L, int *regs_out) {
     const int S = vgk_agg_jit_slots(L);
-    std::string src = gen_source(*L, S, vec_ok(*L));
-    nvrtcProgram prog;
-    if (nvrtcCreateProgram(&prog, src.c_str(), "vg_jit_agg.cu", kJitHeaderCount, kJitHeaderSources,
-                           kJitHeaderNames) != NVRTC_SUCCESS)
-        return -1;
-    const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--ptxas-options=-v"};
-    nvrtcResult r = nvrtcCompileProgram(prog, 3, opts);
-    size_t n = 0;
-    nvrtcGetProgramLogSize(prog, &n);
-    std::vector<char> log(n + 1, 0);
-    nvrtcGetProgramLog(prog, log.data());
-    snprintf(g_jit_err, sizeof(g_jit_err), "%s%.1900s", r == NVRTC_SUCCESS ? "" : "NVRTC failed:\n", log.data());
-    nvrtcDestroyProgram(&prog);
+    std::vector<char> cubin;
+    Shape used;
+    std::string log;
+    const int rc = compile_plan(*L, S, vec_ok(*L), cubin, used, &log);
+    snprintf(g_jit_err, sizeof(g_jit_err), "%sthreads per CTA: %d\n%.1800s", rc == 0 ? "" : "NVRTC failed:\n",
+             used.threads, log.c_str());
     if (regs_out) {
-        const char *p = strstr(log.data(), "Used ");
+        const char *p = strstr(log.c_str(), "Used ");
         *regs_out = p ? atoi(p + 5) : -1;
     }
-    return r == NVRTC_SUCCESS ? 0 : -1;
+    return rc;
 }
 
 // Launches the specialised kernel over n_logical rows: 1 launched, 0 the
@@ -319,14 +344,16 @@ int vgk_agg_launch_jit(const VgAggLaunch *L, int64_t n_logical, vg_stream_t s) {
     if (!vgk_agg_jit_ok(L)) return 0;
     const int S = vgk_agg_jit_slots(L);
     const bool vec = vec_ok(*L);
-    std::string src = gen_source(*L, S, vec);
+    std::string src = gen_source(*L, S, vec, shape());
     JitKernel *jk;
     {
         std::lock_guard<std::mutex> lock(g_mu);
         auto it = g_cache.find(src);
         if (it == g_cache.end()) {
             JitKernel k;
-            if (compile(src, k) != 0) return -1;
+            std::vector<char> cubin;
+            if (compile_plan(*L, S, vec, cubin, k.shape, nullptr) != 0) return -1;
+            if (load_kernel(cubin, k) != 0) return -1;
             it = g_cache.emplace(src, k).first;
         }
         jk = &it->second;
@@ -346,7 +373,7 @@ int vgk_agg_launch_jit(const VgAggLaunch *L, int64_t n_logical, vg_stream_t s) {
         jk->smem_set = smem;
     }
     const int sms = vgk_num_sms();
-    const Shape &sh = shape();
+    const Shape &sh = jk->shape;
     const int64_t per = (int64_t)sh.rows * sh.threads;
     const int64_t tiles = (n_logical + per - 1) / per;
     const int64_t cap = (int64_t)sms * (sh.ctas < 2 ? sh.ctas : 2);   // the spill area holds 2 caches per SM

@@ -16,6 +16,20 @@
 
 #pragma once
 
+// First-seen order code of logical row li (hash-path output order): probe
+// batch, then matched rows before the batch's unmatched LEFT rows, then the
+// row (join), or the row's stream position.
+VG_DEV uint64_t vgj_order(const VgAggLaunch &L, int64_t li, uint32_t matched, int j) {
+#if VGJ_JOIN
+    return ((uint64_t)L.batch_idx << 44) | ((uint64_t)(((matched >> j) & 1u) ? 0 : 1) << 43) |
+           ((uint64_t)(li & 0xFFFFFFFF) << 11);
+#else
+    (void)matched;
+    (void)j;
+    return (uint64_t)(L.row_base + li);
+#endif
+}
+
 extern "C" __global__ void __launch_bounds__(VGJ_THREADS, VGJ_MINB)
 vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
     using namespace vgj;
@@ -94,10 +108,10 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
 #if VGJ_PRED
         live &= vgj_pred(L, X);
 #endif
+        uint32_t matched = 0;
 #if VGJ_JOIN
         // join probe: the R rows' slot reads are issued together
         int64_t brow[R];
-        uint32_t matched = 0;
         {
             uint64_t kw[R];
             int64_t slot[R];
@@ -195,10 +209,16 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
         (void)brow;
 #endif
 #endif
+        // Cache updates.  Rows that need the global table (a hashed-cache
+        // miss, or a value outside a cache digit window) are only marked
+        // here and handled together afterwards, so the per-row path has no
+        // rarely-taken branches around global atomics.
+        uint32_t rare = 0, miss = 0;
+        uint32_t failm[R];
 #pragma unroll
         for (int j = 0; j < R; j++) {
+            failm[j] = 0;
             if (!((live >> j) & 1u)) continue;
-            const int64_t li = r0 + j;
             Keys k;
 #pragma unroll
             for (int i = 0; i < VG_MAX_KEYS; i++) k.w[i] = 0;
@@ -216,32 +236,38 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
                                               kt, &err);
                 if (err) atomicOr(L.gt.err, VG_ERR_WAIT);
             }
+            if (found < 0) {
+                miss |= 1u << j;
+                continue;
+            }
 #endif
 #if VGJ_TRACK
-#if VGJ_JOIN
-            const uint64_t order = ((uint64_t)L.batch_idx << 44) | ((uint64_t)(((matched >> j) & 1u) ? 0 : 1) << 43) |
-                                   ((uint64_t)(li & 0xFFFFFFFF) << 11);
-#else
-            const uint64_t order = (uint64_t)(L.row_base + li);
+            atomicMin((unsigned long long *)(sm + VGJ_OFF_FIRST) + found, (unsigned long long)vgj_order(L, r0 + j, matched, j));
 #endif
-#endif
-            if (found >= 0) {
-#if VGJ_TRACK
-                atomicMin((unsigned long long *)(sm + VGJ_OFF_FIRST) + found, (unsigned long long)order);
-#endif
-                const uint32_t fail = vgj_cache_update(sm, found, X, j);
-                if (fail) {
-                    const int64_t g = gt_find_insert(L.gt, k, VGJ_NK, kt, nm, hash_k(k, VGJ_NK, nm));
-                    if (g >= 0) vgj_global_update(L, g, X, j, fail);
-                    else vgj_spill(L, li, fail);
-                }
-            } else {
+            failm[j] = vgj_cache_update(sm, found, X, j);
+            if (failm[j]) rare |= 1u << j;
+        }
+        if (rare | miss) {
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                const bool m = (miss >> j) & 1u;
+                if (!m && !((rare >> j) & 1u)) continue;
+                const int64_t li = r0 + j;
+                Keys k;
+#pragma unroll
+                for (int i = 0; i < VG_MAX_KEYS; i++) k.w[i] = 0;
+                uint32_t nm = 0;
+                vgj_keys(X, j, k, nm);
                 const int64_t g = gt_find_insert(L.gt, k, VGJ_NK, kt, nm, hash_k(k, VGJ_NK, nm));
-                if (g < 0) { spill_row(L, li, 0, -1); continue; }
+                if (g < 0) {
+                    if (m) spill_row(L, li, 0, -1);
+                    else vgj_spill(L, li, failm[j]);
+                    continue;
+                }
 #if VGJ_TRACK
-                atomicMin((unsigned long long *)(L.gt.first_row + g), (unsigned long long)order);
+                if (m) atomicMin((unsigned long long *)(L.gt.first_row + g), (unsigned long long)vgj_order(L, li, matched, j));
 #endif
-                vgj_global_update(L, g, X, j, 0xFFFFFFFFu);
+                vgj_global_update(L, g, X, j, m ? 0xFFFFFFFFu : failm[j]);
             }
         }
     }

@@ -167,22 +167,11 @@ VG_DEV uint32_t term_mask(const VgAggLaunch &L, const Rows &X) {
     return m;
 }
 
-// One digit magnitude into a cache (lo, hi) word pair: add, or subtract for
-// a negative summand, with the carry / borrow of the low word applied to
-// the high word (exact; one atomic unless the low word wraps).
-VG_DEV void digit_add(uint32_t *lo, int32_t *hi, uint32_t d, uint32_t neg) {
-    if (!d) return;
-    if (!neg) {
-        const uint32_t old = atomicAdd(lo, d);
-        if (old + d < old) atomicAdd(hi, 1);
-    } else {
-        const uint32_t old = atomicSub(lo, d);
-        if (old < d) atomicAdd(hi, -1);
-    }
-}
-
 // A double into a cache slot's digit window (same representation as
-// cwin_add, in 32-bit arithmetic).  False: outside the window.
+// cwin_add, in 32-bit arithmetic): each digit magnitude is added to (or,
+// for a negative summand, subtracted from) the low word of its (lo, hi)
+// pair; the carries / borrows, rare, are applied to the high words after.
+// False: outside the window.
 template <int S>
 VG_DEV bool cache_sum_f64(char *sm, uint32_t OBASE, uint32_t OWIN, uint32_t *flags, int slot, uint64_t bits) {
     const VgDigits32 d = vg_split_double32(bits);
@@ -201,9 +190,23 @@ VG_DEV bool cache_sum_f64(char *sm, uint32_t OBASE, uint32_t OWIN, uint32_t *fla
     if (rel < 0 || rel + (d.d2 ? 3 : 2) > kWin) return false;
     uint32_t *wl = (uint32_t *)(sm + OWIN) + slot + rel * S;
     int32_t *wh = (int32_t *)(sm + OWIN + 4 * S * kWin) + slot + rel * S;
-    digit_add(wl, wh, d.d0, d.neg);
-    digit_add(wl + S, wh + S, d.d1, d.neg);
-    digit_add(wl + 2 * S, wh + 2 * S, d.d2, d.neg);
+    // adding 2^32 - d to a low word subtracts d from it
+    const uint32_t a0 = d.neg ? 0u - d.d0 : d.d0;
+    const uint32_t a1 = d.neg ? 0u - d.d1 : d.d1;
+    const uint32_t a2 = d.neg ? 0u - d.d2 : d.d2;
+    const uint32_t o0 = atomicAdd(wl, a0);
+    const uint32_t o1 = atomicAdd(wl + S, a1);
+    const uint32_t o2 = a2 ? atomicAdd(wl + 2 * S, a2) : 0u;
+    // carry out of an add: the sum wrapped; borrow of a subtract: old < d
+    const bool c0 = d.neg ? (o0 < d.d0) : (o0 + a0 < o0);
+    const bool c1 = d.neg ? (o1 < d.d1) : (o1 + a1 < o1);
+    const bool c2 = d.neg ? (o2 < d.d2) : (o2 + a2 < o2);
+    if (c0 | c1 | c2) {
+        const int32_t adj = d.neg ? -1 : 1;
+        if (c0) atomicAdd(wh, adj);
+        if (c1) atomicAdd(wh + S, adj);
+        if (c2 && a2) atomicAdd(wh + 2 * S, adj);
+    }
     return true;
 }
 
