@@ -258,6 +258,20 @@ def ja_join_agg_sparse(E, temp_dir):   # the benchmark plan with scattered ids (
     return out
 
 
+def ja_dup_build_keys(E, temp_dir):  # join + aggregate where some build keys repeat (many matches per row)
+    rng = np.random.default_rng(9)
+    nf, nd = 3000, 400
+    ids = rng.integers(1, 300, nd)                      # ~100 repeated ids
+    fact = {"key": (rng.integers(1, 320, nf), rng.random(nf) > 0.02), "value": rng.lognormal(0, 1, nf)}
+    dim = {"id": ids, "category": rng.integers(0, 12, nd), "weight": (rng.random(nd), rng.random(nd) > 0.05)}
+    out = []
+    for kind in ("left_join", "inner_join"):
+        out += (getattr(tbl(E, fact, batch_rows=1024), kind)(tbl(E, dim, batch_rows=128), {"key": "id"})
+                .group_by("category").summarise(temp_dir=temp_dir, s=("sum", col("value") * col("weight")),
+                                                n=("n",)).batches())
+    return out
+
+
 def ja_dense_keys(E, temp_dir):     # join + aggregate keyed on a small-range build-side column
     rng = np.random.default_rng(17)
     nf, nd = 7001, 257
@@ -320,7 +334,7 @@ FILTER_CASES = [f_simple, f_equality, f_and_or_not, f_na_dropped, f_is_na, f_kle
                 f_empty, f_general_expr, f_int_vs_double_literal]
 GROUP_CASES = [g_basic, g_na_key, g_multi_key, g_na_semantics, g_int_sum_double, g_resize_200,
                g_filter_then_group, g_ungrouped, g_nested_expr, g_bool_and_double_keys, ja_join_agg,
-               ja_dense_keys, ja_join_agg_sparse]
+               ja_dense_keys, ja_join_agg_sparse, ja_dup_build_keys]
 JOIN_CASES = [j_inner_left_semi_anti, j_duplicates, j_na_keys, j_suffix, j_coerce, j_streaming,
               j_after_filter, j_full]
 

@@ -93,9 +93,16 @@ struct PayArgs {
     VgJPay *pay;             // NULL: none requested
 };
 
-__global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters, VgJPay *pay) {
+__global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters, VgJPay *pay, uint32_t *bits, long long *mm) {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n = jt.slots ? jt.cap + 1 : jt.cap;
+    if (bits)
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n + 31) / 32; i += stride) bits[i] = 0;
+    if (mm && blockIdx.x == 0 && threadIdx.x < 2) {
+        mm[3 * threadIdx.x + 0] = 0x7FFFFFFFFFFFFFFFll;
+        mm[3 * threadIdx.x + 1] = (long long)0x8000000000000000ull;
+        mm[3 * threadIdx.x + 2] = 0;
+    }
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         if (pay) {
             ulonglong2 *o = (ulonglong2 *)(pay + i);
@@ -275,6 +282,80 @@ __global__ void jt_insert_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, in
     rslot[r] = (int32_t)d;
 }
 
+// Direct tables with a payload copy, in one pass: each build row claims
+// its key's bit in a bitmap; the first claimant writes the whole slot {key,
+// row, 1} and the payload entry with plain stores (no per-slot atomics); a
+// second claimant flags a duplicate key (counters[3]), after which the
+// counting pass rebuilds the slots.  Also the min, max and count of the
+// valid values of int64 payload columns (mm, 3 words per column).
+__global__ void jt_claim_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t *rslot, uint32_t *counters,
+                                       uint32_t *bits, PayArgs P, long long *mm) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = r < n;
+    bool first = false, dup = false;
+    uint64_t p[2] = {0, 0};
+    uint32_t meta = 1u;
+    if (in) {
+        uint64_t k[VG_MAX_KEYS];
+        int64_t d = -1;
+        if (key_words(K, r, k)) {
+            d = jt_direct_slot(jt, k[0]);
+            if (d < 0) {
+                atomicOr(counters + 2, VG_ERR_FULL);
+            } else {
+                const uint32_t bit = 1u << (d & 31);
+                const uint32_t old = atomicOr(bits + (d >> 5), bit);
+                first = !(old & bit);
+                dup = !first;
+            }
+        }
+        if (P.n_cols > 0) {
+            p[0] = vg_load_bits(P.c0, r);
+            if (vg_valid(P.c0, r)) meta |= 2u;
+        }
+        if (P.n_cols > 1) {
+            p[1] = vg_load_bits(P.c1, r);
+            if (vg_valid(P.c1, r)) meta |= 4u;
+        }
+        if (first) {
+            ulonglong2 *sl = (ulonglong2 *)(jt.slots + d);
+            *sl = make_ulonglong2(k[0], (unsigned long long)(uint32_t)r | (1ull << 32));
+            ulonglong2 *o = (ulonglong2 *)(P.pay + d);
+            o[0] = make_ulonglong2(k[0], (unsigned long long)(uint32_t)r | ((unsigned long long)meta << 32));
+            o[1] = make_ulonglong2(p[0], p[1]);
+        }
+        rslot[r] = (int32_t)d;
+    }
+    const unsigned nfirst = __popc(__ballot_sync(0xFFFFFFFFu, first));
+    const bool anydup = __any_sync(0xFFFFFFFFu, dup);
+    if ((threadIdx.x & 31) == 0) {
+        if (nfirst) atomicAdd(counters + 0, nfirst);
+        if (anydup) atomicOr(counters + 3, 1u);
+    }
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        if (c >= P.n_cols) break;
+        const int type = c == 0 ? P.c0.type : P.c1.type;
+        if (type != VEC_INT64) continue;
+        const bool ok = in && ((meta >> (1 + c)) & 1u);
+        long long lo = ok ? (long long)p[c] : 0x7FFFFFFFFFFFFFFFll;
+        long long hi = ok ? (long long)p[c] : (long long)0x8000000000000000ull;
+        unsigned cnt = ok ? 1u : 0u;
+        for (int o = 16; o > 0; o >>= 1) {
+            const long long l2 = __shfl_xor_sync(0xFFFFFFFFu, lo, o);
+            const long long h2 = __shfl_xor_sync(0xFFFFFFFFu, hi, o);
+            cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, o);
+            lo = l2 < lo ? l2 : lo;
+            hi = h2 > hi ? h2 : hi;
+        }
+        if ((threadIdx.x & 31) == 0 && cnt) {
+            atomicMin(mm + 3 * c, lo);
+            atomicMax(mm + 3 * c + 1, hi);
+            atomicAdd((unsigned long long *)mm + 3 * c + 2, (unsigned long long)cnt);
+        }
+    }
+}
+
 __global__ void jt_count_kernel(VgJoinTable jt, uint32_t *counters) {
     __shared__ unsigned s_nd, s_mx;
     if (threadIdx.x == 0) { s_nd = 0; s_mx = 0; }
@@ -441,14 +522,18 @@ int64_t vgk_join_cap(int64_t n_build) {
 
 size_t vgk_join_build_scratch_bytes(int64_t n_build) {
     int64_t n = n_build > 0 ? n_build : 1;
-    return a256((size_t)n * 4) + a256((size_t)n * 8) + vgk_sort_pairs_scratch(n) + 256;
+    // + the claim bitmap of a direct table (range < max(2 n, 65536), see
+    // node_join.c) and the payload min / max words
+    const size_t bitmap = a256((size_t)((2 * n > 65536 ? 2 * n : 65536) + 64) / 8 + 8);
+    return a256((size_t)n * 4) + a256((size_t)n * 8) + vgk_sort_pairs_scratch(n) + 256 + bitmap + 256;
 }
 
 // jt->cap, state, keys, start, count, rows (n_build entries) are allocated by
 // the caller; on return jt->rows is NULL when every key is unique.
 int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t *key_conv,
                    int64_t n_build, void *d_scratch, size_t scratch_bytes, int64_t *h_distinct,
-                   int64_t *h_maxdup, const VgCol *pay_cols, int n_pay, VgJPay *pay, vg_stream_t s) {
+                   int64_t *h_maxdup, const VgCol *pay_cols, int n_pay, VgJPay *pay, int64_t *h_pay_mm,
+                   vg_stream_t s) {
     cudaStream_t st = (cudaStream_t)s;
     if (scratch_bytes < vgk_join_build_scratch_bytes(n_build)) {
         snprintf(g_err, sizeof(g_err), "join build scratch too small");
@@ -459,7 +544,11 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
     int32_t *rslot = (int32_t *)p; p += a256((size_t)n * 4);
     uint64_t *pkeys = (uint64_t *)p; p += a256((size_t)n * 8);
     void *sort_scratch = p; p += vgk_sort_pairs_scratch(n);
-    uint32_t *counters = (uint32_t *)p;
+    uint32_t *counters = (uint32_t *)p; p += 256;
+    long long *mm = (long long *)p; p += 256;
+    uint32_t *bits = (uint32_t *)p;
+    if (h_pay_mm)
+        for (int i = 0; i < 6; i++) h_pay_mm[i] = 0;
     KeyArgs K;
     memset(&K, 0, sizeof(K));
     K.n_keys = n_keys;
@@ -476,7 +565,38 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         if (n_pay > 0) P.c0 = pay_cols[0];
         if (n_pay > 1) P.c1 = pay_cols[1];
     }
-    { jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters, P.pay); vg_launch_counter++; }
+    if (P.pay) {
+        // direct table with a payload copy: one claim pass; the counting
+        // pass below runs only if a key repeats
+        jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters, P.pay, bits, mm);
+        vg_launch_counter++;
+        vg_prof_begin(VG_PROF_JOIN_BUILD, st);
+        if (n_build > 0) {
+            jt_claim_direct_kernel<<<(unsigned)((n_build + 255) / 256), 256, 0, st>>>(*jt, K, n_build, rslot,
+                                                                                 counters, bits, P, mm);
+            vg_launch_counter++;
+        }
+        vg_prof_end(VG_PROF_JOIN_BUILD, st);
+        uint32_t hc[4] = {0, 0, 0, 0};
+        long long hm[6];
+        cudaMemcpyAsync(hc, counters, 16, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(hm, mm, 48, cudaMemcpyDeviceToHost, st);
+        if (check(cudaStreamSynchronize(st), "join build")) return -1;
+        if (hc[2]) {
+            snprintf(g_err, sizeof(g_err), "join build: key outside the direct range (code %u)", hc[2]);
+            return -1;
+        }
+        if (h_pay_mm)
+            for (int i = 0; i < 6; i++) h_pay_mm[i] = hm[i];
+        if (!hc[3]) {
+            *h_distinct = hc[0];
+            *h_maxdup = 1;
+            jt->rows = nullptr;
+            return 0;
+        }
+        P.pay = nullptr;   // a key repeats: the payload does not apply; count the slots properly
+    }
+    { jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters, nullptr, nullptr, nullptr); vg_launch_counter++; }
     vg_prof_begin(VG_PROF_JOIN_BUILD, st);
     if (jt->direct) {
         if (n_build > 0) {
@@ -502,15 +622,15 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
     if (hc[1] <= 1) {
         jt->rows = nullptr;    // start[slot] is the build row itself
         // hashed tables: the payload copy from the finished slots
-        if (pay && !P.pay && jt->slots) return vgk_join_payload(jt, nullptr, pay_cols, n_pay, pay, s);
+        if (pay && !jt->direct && jt->slots) return vgk_join_payload(jt, nullptr, pay_cols, n_pay, pay, s);
         return 0;
     }
     // duplicates: stable sort of (slot, row) lays out each key's rows in
     // ascending row order
-    int bits = 1;
-    while (((int64_t)1 << bits) <= jt->cap + 1) bits++;
+    int key_bits = 1;
+    while (((int64_t)1 << key_bits) <= jt->cap + 1) key_bits++;
     { pair_keys_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(rslot, n_build, jt->cap, pkeys, jt->rows); vg_launch_counter++; }
-    if (vgk_sort_pairs(pkeys, jt->rows, n_build, bits, sort_scratch, vgk_sort_pairs_scratch(n), s)) {
+    if (vgk_sort_pairs(pkeys, jt->rows, n_build, key_bits, sort_scratch, vgk_sort_pairs_scratch(n), s)) {
         snprintf(g_err, sizeof(g_err), "%s", vgk_sort_last_error());
         return -1;
     }

@@ -512,10 +512,22 @@ static VecBatch *agg_next(VecNode *self) {
     if (B && P.n_keys == 1 && L->cache_slots > 0 && P.key[0].op == 0 &&
         P.key[0].a.side == VG_SIDE_BUILD && P.key[0].a.type == VEC_INT64) {
         int64_t mm[3];
-        int64_t *d = (int64_t *)vg_dmalloc(256);
-        vg_check_rc(vgk_col_minmax_i64(&L->bcols[P.key[0].a.col], B->jt.n_build, d, mm, vg_stream()),
-                    "build key range");
-        vg_dfree(d);
+        const int rcol = P.bset.idx[P.key[0].a.col];
+        int q = -1;
+        if (B->pay_mm_ok)
+            for (int i = 0; i < B->pay_n; i++)
+                if (B->pay_col[i] == rcol) q = i;
+        if (q >= 0) {
+            /* the join build's payload pass measured this column */
+            mm[0] = B->pay_mm[3 * q];
+            mm[1] = B->pay_mm[3 * q + 1];
+            mm[2] = B->pay_mm[3 * q + 2];
+        } else {
+            int64_t *d = (int64_t *)vg_dmalloc(256);
+            vg_check_rc(vgk_col_minmax_i64(&L->bcols[P.key[0].a.col], B->jt.n_build, d, mm, vg_stream()),
+                        "build key range");
+            vg_dfree(d);
+        }
         if (mm[2] == 0) {
             L->dense = 1;
             L->dense_n = 0;

@@ -203,7 +203,12 @@ static void join_build(VgJoin *j) {
     void *scratch = vg_dmalloc(sb);
     int64_t distinct = 0, maxdup = 0;
     int rc = vgk_join_build(jt, kc, nk, j->conv_build, total, scratch, sb, &distinct, &maxdup, pc,
-                            j->pay ? j->pay_n : 0, j->pay, vg_stream());
+                            j->pay ? j->pay_n : 0, j->pay, j->B.pay_mm, vg_stream());
+    if (j->pay) {
+        j->B.pay_n = j->pay_n;
+        for (int q = 0; q < j->pay_n; q++) j->B.pay_col[q] = j->pay_col[q];
+        j->B.pay_mm_ok = jt->direct;   /* the claim pass computed them */
+    }
     vg_dfree(scratch);
     vg_check_rc(rc, "join build");
     if (j->jn.kind == JOIN_FULL) {

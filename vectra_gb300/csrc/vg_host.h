@@ -120,6 +120,12 @@ typedef struct {
     VgCol *bcols;                    /* device build columns (all right columns) */
     int n_bcols;
     int kind;
+    /* payload copy columns (right column indices) and, when pay_mm_ok, the
+     * min / max / count of their valid values for int64 columns */
+    int pay_n;
+    int32_t pay_col[2];
+    int pay_mm_ok;
+    int64_t pay_mm[6];
 } VgJoinBuilt;
 const VgJoinBuilt *vg_join_build_now(VecNode *n);
 /* builds with a payload copy of right columns cols[0..n_cols) (n_cols <= 2);
