@@ -280,7 +280,7 @@ def gpu_arm(args, rank, world):
 
     if args.no_e2e:
         line = {"metric": METRIC, "ms_per_step": ms_step, "kernel_ms": agg_ms / agg_launches,
-                "scale": args.scale, "gpu_launches": launches}
+                "join_build_ms": build_ms / max(1, build_n.value), "scale": args.scale, "gpu_launches": launches}
         return line
     # e2e: page-locked host copies of the same columns
     hf = {k: (v.cpu().pin_memory(), m.cpu().pin_memory()) for k, (v, m) in fcols.items()}
