@@ -93,11 +93,11 @@ struct PayArgs {
     VgJPay *pay;             // NULL: none requested
 };
 
-__global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters, VgJPay *pay, uint32_t *bits, long long *mm) {
+// Empties the table (init_slots) and / or zeroes the payload copy; resets
+// the counters and the payload min / max words.
+__global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters, VgJPay *pay, int init_slots, long long *mm) {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n = jt.slots ? jt.cap + 1 : jt.cap;
-    if (bits)
-        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n + 31) / 32; i += stride) bits[i] = 0;
     if (mm && blockIdx.x == 0 && threadIdx.x < 2) {
         mm[3 * threadIdx.x + 0] = 0x7FFFFFFFFFFFFFFFll;
         mm[3 * threadIdx.x + 1] = (long long)0x8000000000000000ull;
@@ -109,6 +109,7 @@ __global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters, VgJPay *pay, 
             o[0] = make_ulonglong2(0ull, 0ull);
             o[1] = make_ulonglong2(0ull, 0ull);
         }
+        if (!init_slots) continue;
         if (jt.slots) {
             jt.slots[i].key = VG_JEMPTY;
             jt.slots[i].start = 0;
@@ -282,17 +283,16 @@ __global__ void jt_insert_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, in
     rslot[r] = (int32_t)d;
 }
 
-// Direct tables with a payload copy, in one pass: each build row claims
-// its key's bit in a bitmap; the first claimant writes the whole slot {key,
-// row, 1} and the payload entry with plain stores (no per-slot atomics); a
-// second claimant flags a duplicate key (counters[3]), after which the
-// counting pass rebuilds the slots.  Also the min, max and count of the
-// valid values of int64 payload columns (mm, 3 words per column).
-__global__ void jt_claim_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t *rslot, uint32_t *counters,
-                                       uint32_t *bits, PayArgs P, long long *mm) {
+// Direct tables with a payload copy.  Pass 1: every build row writes the
+// whole 32-byte payload entry of its key {key, row | meta << 32, p0, p1}
+// with plain stores (one sector per row, no atomics) and also reports the
+// min, max and count of the valid values of int64 payload columns (mm, 3
+// words per column).  If a key repeats, one of its rows' writes survives;
+// pass 2 (jt_pay_verify_kernel) finds that out.
+__global__ void jt_pay_rows_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t *rslot, uint32_t *counters,
+                                   PayArgs P, long long *mm) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = r < n;
-    bool first = false, dup = false;
     uint64_t p[2] = {0, 0};
     uint32_t meta = 1u;
     if (in) {
@@ -300,14 +300,7 @@ __global__ void jt_claim_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int
         int64_t d = -1;
         if (key_words(K, r, k)) {
             d = jt_direct_slot(jt, k[0]);
-            if (d < 0) {
-                atomicOr(counters + 2, VG_ERR_FULL);
-            } else {
-                const uint32_t bit = 1u << (d & 31);
-                const uint32_t old = atomicOr(bits + (d >> 5), bit);
-                first = !(old & bit);
-                dup = !first;
-            }
+            if (d < 0) atomicOr(counters + 2, VG_ERR_FULL);
         }
         if (P.n_cols > 0) {
             p[0] = vg_load_bits(P.c0, r);
@@ -317,20 +310,12 @@ __global__ void jt_claim_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int
             p[1] = vg_load_bits(P.c1, r);
             if (vg_valid(P.c1, r)) meta |= 4u;
         }
-        if (first) {
-            ulonglong2 *sl = (ulonglong2 *)(jt.slots + d);
-            *sl = make_ulonglong2(k[0], (unsigned long long)(uint32_t)r | (1ull << 32));
+        if (d >= 0) {
             ulonglong2 *o = (ulonglong2 *)(P.pay + d);
             o[0] = make_ulonglong2(k[0], (unsigned long long)(uint32_t)r | ((unsigned long long)meta << 32));
             o[1] = make_ulonglong2(p[0], p[1]);
         }
         rslot[r] = (int32_t)d;
-    }
-    const unsigned nfirst = __popc(__ballot_sync(0xFFFFFFFFu, first));
-    const bool anydup = __any_sync(0xFFFFFFFFu, dup);
-    if ((threadIdx.x & 31) == 0) {
-        if (nfirst) atomicAdd(counters + 0, nfirst);
-        if (anydup) atomicOr(counters + 3, 1u);
     }
 #pragma unroll
     for (int c = 0; c < 2; c++) {
@@ -353,6 +338,30 @@ __global__ void jt_claim_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int
             atomicMax(mm + 3 * c + 1, hi);
             atomicAdd((unsigned long long *)mm + 3 * c + 2, (unsigned long long)cnt);
         }
+    }
+}
+
+// Pass 2: a row whose entry names another row shares its key with that row
+// (counters[3] = 1: duplicates, the payload does not apply).
+__global__ void jt_pay_verify_kernel(const VgJPay *pay, int64_t n, const int32_t *rslot, uint32_t *counters) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool dup = false;
+    if (r < n) {
+        const int32_t d = rslot[r];
+        if (d >= 0) dup = (int32_t)(uint32_t)__ldg((const unsigned long long *)(pay + d) + 1) != (int32_t)r;
+    }
+    if (__any_sync(0xFFFFFFFFu, dup) && (threadIdx.x & 31) == 0) atomicOr(counters + 3, 1u);
+}
+
+// The slot table of a unique-key direct table from its payload copy, for
+// consumers that read slots (the general kernels, the join node's probe).
+__global__ void jt_slots_from_pay_kernel(VgJoinTable jt, const VgJPay *pay) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= jt.cap; i += stride) {
+        const ulonglong2 e = __ldg((const ulonglong2 *)(pay + i));
+        const bool present = ((e.y >> 32) & 1u) != 0;
+        *(ulonglong2 *)(jt.slots + i) =
+            make_ulonglong2(present ? e.x : VG_JEMPTY, (e.y & 0xFFFFFFFFull) | ((present ? 1ull : 0ull) << 32));
     }
 }
 
@@ -522,10 +531,8 @@ int64_t vgk_join_cap(int64_t n_build) {
 
 size_t vgk_join_build_scratch_bytes(int64_t n_build) {
     int64_t n = n_build > 0 ? n_build : 1;
-    // + the claim bitmap of a direct table (range < max(2 n, 65536), see
-    // node_join.c) and the payload min / max words
-    const size_t bitmap = a256((size_t)((2 * n > 65536 ? 2 * n : 65536) + 64) / 8 + 8);
-    return a256((size_t)n * 4) + a256((size_t)n * 8) + vgk_sort_pairs_scratch(n) + 256 + bitmap + 256;
+    // rows' slots, sort keys, sort scratch, counters, payload min / max words
+    return a256((size_t)n * 4) + a256((size_t)n * 8) + vgk_sort_pairs_scratch(n) + 256 + 256;
 }
 
 // jt->cap, state, keys, start, count, rows (n_build entries) are allocated by
@@ -533,7 +540,7 @@ size_t vgk_join_build_scratch_bytes(int64_t n_build) {
 int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t *key_conv,
                    int64_t n_build, void *d_scratch, size_t scratch_bytes, int64_t *h_distinct,
                    int64_t *h_maxdup, const VgCol *pay_cols, int n_pay, VgJPay *pay, int64_t *h_pay_mm,
-                   vg_stream_t s) {
+                   int *slots_ready, vg_stream_t s) {
     cudaStream_t st = (cudaStream_t)s;
     if (scratch_bytes < vgk_join_build_scratch_bytes(n_build)) {
         snprintf(g_err, sizeof(g_err), "join build scratch too small");
@@ -545,8 +552,7 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
     uint64_t *pkeys = (uint64_t *)p; p += a256((size_t)n * 8);
     void *sort_scratch = p; p += vgk_sort_pairs_scratch(n);
     uint32_t *counters = (uint32_t *)p; p += 256;
-    long long *mm = (long long *)p; p += 256;
-    uint32_t *bits = (uint32_t *)p;
+    long long *mm = (long long *)p;
     if (h_pay_mm)
         for (int i = 0; i < 6; i++) h_pay_mm[i] = 0;
     KeyArgs K;
@@ -565,16 +571,19 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         if (n_pay > 0) P.c0 = pay_cols[0];
         if (n_pay > 1) P.c1 = pay_cols[1];
     }
+    if (slots_ready) *slots_ready = 1;
     if (P.pay) {
-        // direct table with a payload copy: one claim pass; the counting
-        // pass below runs only if a key repeats
-        jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters, P.pay, bits, mm);
+        // direct table with a payload copy: rows write their entries, a
+        // check pass looks for repeated keys; the slot table is derived
+        // later, only if something reads it (vgk_join_slots_from_payload)
+        jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters, P.pay, 0, mm);
         vg_launch_counter++;
         vg_prof_begin(VG_PROF_JOIN_BUILD, st);
         if (n_build > 0) {
-            jt_claim_direct_kernel<<<(unsigned)((n_build + 255) / 256), 256, 0, st>>>(*jt, K, n_build, rslot,
-                                                                                 counters, bits, P, mm);
-            vg_launch_counter++;
+            const unsigned g = (unsigned)((n_build + 255) / 256);
+            jt_pay_rows_kernel<<<g, 256, 0, st>>>(*jt, K, n_build, rslot, counters, P, mm);
+            jt_pay_verify_kernel<<<g, 256, 0, st>>>(P.pay, n_build, rslot, counters);
+            vg_launch_counter += 2;
         }
         vg_prof_end(VG_PROF_JOIN_BUILD, st);
         uint32_t hc[4] = {0, 0, 0, 0};
@@ -589,14 +598,15 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         if (h_pay_mm)
             for (int i = 0; i < 6; i++) h_pay_mm[i] = hm[i];
         if (!hc[3]) {
-            *h_distinct = hc[0];
+            *h_distinct = -1;      // not counted on this path
             *h_maxdup = 1;
             jt->rows = nullptr;
+            if (slots_ready) *slots_ready = 0;
             return 0;
         }
-        P.pay = nullptr;   // a key repeats: the payload does not apply; count the slots properly
+        P.pay = nullptr;   // a key repeats: the payload does not apply; build the slots by counting
     }
-    { jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters, nullptr, nullptr, nullptr); vg_launch_counter++; }
+    { jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters, nullptr, 1, nullptr); vg_launch_counter++; }
     vg_prof_begin(VG_PROF_JOIN_BUILD, st);
     if (jt->direct) {
         if (n_build > 0) {
@@ -735,6 +745,13 @@ int vgk_join_payload(const VgJoinTable *jt, const VgCol *key, const VgCol *cols,
                                                              n_cols > 1 ? cols[1] : none, n_cols, pay);
       vg_launch_counter++; }
     return check(cudaGetLastError(), "join payload");
+}
+
+int vgk_join_slots_from_payload(const VgJoinTable *jt, const VgJPay *pay, vg_stream_t s) {
+    cudaStream_t st = (cudaStream_t)s;
+    jt_slots_from_pay_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, pay);
+    vg_launch_counter++;
+    return check(cudaGetLastError(), "join slots");
 }
 
 }  // extern "C"

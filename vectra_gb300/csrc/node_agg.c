@@ -370,6 +370,7 @@ static void run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_log
         L->gt = T->gt;
         if (c[1]) vg_check_rc(vgk_agg_merge_spilled_cache(L, c[1], vg_stream()), "group-agg merge");
         if (c[0]) {
+            if (P->join) vg_join_ensure_slots(P->join);   /* the replay kernel probes slots */
             L->replay = S->rows;
             L->replay_n = c[0];
             L->spill_rows_cap = 0;           /* a replay must not spill again */
@@ -537,6 +538,12 @@ static VecBatch *agg_next(VecNode *self) {
             L->dense_n = (int32_t)(mm[1] - mm[0] + 1);
             L->dense_min = mm[0];
         }
+    }
+
+    /* only the specialised kernel reads the payload copy instead of slots */
+    if (P.join && !(L->jpay && vgk_agg_jit_ok(L))) {
+        vg_join_ensure_slots(P.join);
+        L->jt = B->jt;
     }
 
     Table T;

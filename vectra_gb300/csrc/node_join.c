@@ -32,6 +32,7 @@ typedef struct {
     void *build_block;        /* device build columns */
     VgDBatch kept;            /* the one build batch, used in place */
     int has_kept;
+    int slots_ready;          /* the slot table is filled (else derive it from pay) */
     VgJPay *pay;              /* payload copy requested by a fused aggregation */
     int pay_n;
     int32_t pay_col[2];
@@ -203,7 +204,7 @@ static void join_build(VgJoin *j) {
     void *scratch = vg_dmalloc(sb);
     int64_t distinct = 0, maxdup = 0;
     int rc = vgk_join_build(jt, kc, nk, j->conv_build, total, scratch, sb, &distinct, &maxdup, pc,
-                            j->pay ? j->pay_n : 0, j->pay, j->B.pay_mm, vg_stream());
+                            j->pay ? j->pay_n : 0, j->pay, j->B.pay_mm, &j->slots_ready, vg_stream());
     if (j->pay) {
         j->B.pay_n = j->pay_n;
         for (int q = 0; q < j->pay_n; q++) j->B.pay_col[q] = j->pay_col[q];
@@ -240,6 +241,14 @@ const VgJoinBuilt *vg_join_build_payload(VecNode *n, const int32_t *cols, int n_
     return &j->B;
 }
 
+void vg_join_ensure_slots(VecNode *n) {
+    VgJoin *j = (VgJoin *)n;
+    join_build(j);
+    if (j->slots_ready) return;
+    vg_check_rc(vgk_join_slots_from_payload(&j->B.jt, j->pay, vg_stream()), "join slots");
+    j->slots_ready = 1;
+}
+
 int vg_join_right_type(VecNode *n, int col) {
     VgJoin *j = (VgJoin *)n;
     return j->jn.right->output_schema.col_types[col];
@@ -247,6 +256,7 @@ int vg_join_right_type(VecNode *n, int col) {
 
 /* one probe batch -> one output batch (NULL if empty) */
 static VecBatch *probe_one(VgJoin *j) {
+    vg_join_ensure_slots(&j->jn.base);
     const VecSchema *ls = &j->jn.left->output_schema;
     int nl = ls->n_cols, nk = j->jn.n_keys;
     int semi = (j->jn.kind == JOIN_SEMI || j->jn.kind == JOIN_ANTI);

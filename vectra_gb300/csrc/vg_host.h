@@ -133,6 +133,8 @@ const VgJoinBuilt *vg_join_build_now(VecNode *n);
  * keys, table already built) */
 const VgJoinBuilt *vg_join_build_payload(VecNode *n, const int32_t *cols, int n_cols, const VgJPay **pay);
 int vg_join_right_type(VecNode *n, int col);
+/* the join table's slots, filled (a build with a payload copy defers them) */
+void vg_join_ensure_slots(VecNode *n);
 VecNode *vg_join_left(VecNode *n);
 int vg_join_kind(VecNode *n);
 /* resolves an output column name of the join: side 0 = left column index,

@@ -363,11 +363,15 @@ size_t vgk_join_build_scratch_bytes(int64_t n_build);
 /* pay (optional, (cap + 1) entries): filled with the payload copy of
  * pay_cols[0..n_pay) when every key is unique (in the insert pass itself
  * for direct tables, which then also report min, max and count of the
- * valid values of int64 payload columns in h_pay_mm[3 c .. 3 c + 2]) */
+ * valid values of int64 payload columns in h_pay_mm[3 c .. 3 c + 2], and
+ * leave the slot table unfilled: *slots_ready == 0) */
 int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t *key_conv,
                    int64_t n_build, void *d_scratch, size_t scratch_bytes, int64_t *h_distinct,
                    int64_t *h_maxdup, const VgCol *pay_cols, int n_pay, VgJPay *pay, int64_t *h_pay_mm,
-                   vg_stream_t s);
+                   int *slots_ready, vg_stream_t s);
+/* fills the slot table of a unique-key direct table from its payload copy
+ * (a build that returned *slots_ready == 0) */
+int vgk_join_slots_from_payload(const VgJoinTable *jt, const VgJPay *pay, vg_stream_t s);
 size_t vgk_join_probe_scratch_bytes(int64_t n_logical);
 int vgk_join_probe_count(const VgJoinTable *jt, const VgCol *pkeys, int n_keys, const int32_t *key_conv,
                          int64_t n_rows, const int32_t *d_sel, int64_t sel_n, int kind,
