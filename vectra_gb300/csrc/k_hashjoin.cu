@@ -103,7 +103,7 @@ __global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters, VgJPay *pay, 
         mm[3 * threadIdx.x + 1] = (long long)0x8000000000000000ull;
         mm[3 * threadIdx.x + 2] = 0;
     }
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n && (pay || init_slots); i += stride) {
         if (pay) {
             ulonglong2 *o = (ulonglong2 *)(pay + i);
             o[0] = make_ulonglong2(0ull, 0ull);
@@ -283,18 +283,23 @@ __global__ void jt_insert_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, in
     rslot[r] = (int32_t)d;
 }
 
-// Direct tables with a payload copy.  Pass 1: every build row writes the
-// whole 32-byte payload entry of its key {key, row | meta << 32, p0, p1}
-// with plain stores (one sector per row, no atomics) and also reports the
-// min, max and count of the valid values of int64 payload columns (mm, 3
-// words per column).  If a key repeats, one of its rows' writes survives;
-// pass 2 (jt_pay_verify_kernel) finds that out.
-__global__ void jt_pay_rows_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t *rslot, uint32_t *counters,
-                                   PayArgs P, long long *mm) {
+// Direct tables with a payload copy, built without random writes to the
+// large tables.  Pass 1: every build row records itself in rowof[key - min]
+// (4 bytes per key: small enough to stay in L2) with the validity bits of
+// its two payload values in bits 29 and 30, and reports min, max and count
+// of the valid values of int64 payload columns (mm, 3 words per column).
+// If a key repeats, one of its rows survives; pass 2 finds that out.  Pass
+// 3 writes every payload entry in key order (coalesced), gathering the
+// payload values by row.
+constexpr int32_t kRowBits = 29;                       // build rows < 2^29
+constexpr uint32_t kRowMask = (1u << kRowBits) - 1u;
+
+__global__ void jt_rows_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t *rslot, uint32_t *counters,
+                                      PayArgs P, uint32_t *rowof, long long *mm) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = r < n;
     uint64_t p[2] = {0, 0};
-    uint32_t meta = 1u;
+    uint32_t vb = 0;                                   // validity of the payload values
     if (in) {
         uint64_t k[VG_MAX_KEYS];
         int64_t d = -1;
@@ -302,27 +307,19 @@ __global__ void jt_pay_rows_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t
             d = jt_direct_slot(jt, k[0]);
             if (d < 0) atomicOr(counters + 2, VG_ERR_FULL);
         }
-        if (P.n_cols > 0) {
-            p[0] = vg_load_bits(P.c0, r);
-            if (vg_valid(P.c0, r)) meta |= 2u;
-        }
-        if (P.n_cols > 1) {
-            p[1] = vg_load_bits(P.c1, r);
-            if (vg_valid(P.c1, r)) meta |= 4u;
-        }
-        if (d >= 0) {
-            ulonglong2 *o = (ulonglong2 *)(P.pay + d);
-            o[0] = make_ulonglong2(k[0], (unsigned long long)(uint32_t)r | ((unsigned long long)meta << 32));
-            o[1] = make_ulonglong2(p[0], p[1]);
-        }
+        if (P.n_cols > 0 && vg_valid(P.c0, r)) vb |= 1u;
+        if (P.n_cols > 1 && vg_valid(P.c1, r)) vb |= 2u;
+        if (d >= 0) rowof[d] = (uint32_t)r | (vb << kRowBits);
         rslot[r] = (int32_t)d;
+        if (P.n_cols > 0 && P.c0.type == VEC_INT64 && (vb & 1u)) p[0] = vg_load_bits(P.c0, r);
+        if (P.n_cols > 1 && P.c1.type == VEC_INT64 && (vb & 2u)) p[1] = vg_load_bits(P.c1, r);
     }
 #pragma unroll
     for (int c = 0; c < 2; c++) {
         if (c >= P.n_cols) break;
         const int type = c == 0 ? P.c0.type : P.c1.type;
         if (type != VEC_INT64) continue;
-        const bool ok = in && ((meta >> (1 + c)) & 1u);
+        const bool ok = in && ((vb >> c) & 1u);
         long long lo = ok ? (long long)p[c] : 0x7FFFFFFFFFFFFFFFll;
         long long hi = ok ? (long long)p[c] : (long long)0x8000000000000000ull;
         unsigned cnt = ok ? 1u : 0u;
@@ -341,16 +338,36 @@ __global__ void jt_pay_rows_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t
     }
 }
 
-// Pass 2: a row whose entry names another row shares its key with that row
+// Pass 2: a row whose key records another row shares its key with it
 // (counters[3] = 1: duplicates, the payload does not apply).
-__global__ void jt_pay_verify_kernel(const VgJPay *pay, int64_t n, const int32_t *rslot, uint32_t *counters) {
+__global__ void jt_rows_verify_kernel(const uint32_t *rowof, int64_t n, const int32_t *rslot, uint32_t *counters) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool dup = false;
     if (r < n) {
         const int32_t d = rslot[r];
-        if (d >= 0) dup = (int32_t)(uint32_t)__ldg((const unsigned long long *)(pay + d) + 1) != (int32_t)r;
+        if (d >= 0) dup = (__ldg(rowof + d) & kRowMask) != (uint32_t)r;
     }
     if (__any_sync(0xFFFFFFFFu, dup) && (threadIdx.x & 31) == 0) atomicOr(counters + 3, 1u);
+}
+
+// Pass 3: the payload entries in key order.
+__global__ void jt_pay_gather_kernel(VgJoinTable jt, const uint32_t *rowof, PayArgs P) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d <= jt.cap; d += stride) {
+        const uint32_t v = d < jt.cap ? __ldg(rowof + d) : 0xFFFFFFFFu;
+        ulonglong2 a = make_ulonglong2(0ull, 0ull), b = make_ulonglong2(0ull, 0ull);
+        if (v != 0xFFFFFFFFu) {
+            const int64_t r = v & kRowMask;
+            const uint32_t meta = 1u | (((v >> kRowBits) & 3u) << 1);
+            a = make_ulonglong2((uint64_t)jt.dmin + (uint64_t)d, (unsigned long long)(uint32_t)r |
+                                                                  ((unsigned long long)meta << 32));
+            if (P.n_cols > 0) b.x = vg_load_bits(P.c0, r);
+            if (P.n_cols > 1) b.y = vg_load_bits(P.c1, r);
+        }
+        ulonglong2 *o = (ulonglong2 *)(P.pay + d);
+        o[0] = a;
+        o[1] = b;
+    }
 }
 
 // The slot table of a unique-key direct table from its payload copy, for
@@ -531,8 +548,11 @@ int64_t vgk_join_cap(int64_t n_build) {
 
 size_t vgk_join_build_scratch_bytes(int64_t n_build) {
     int64_t n = n_build > 0 ? n_build : 1;
-    // rows' slots, sort keys, sort scratch, counters, payload min / max words
-    return a256((size_t)n * 4) + a256((size_t)n * 8) + vgk_sort_pairs_scratch(n) + 256 + 256;
+    // rows' slots, sort keys, sort scratch, counters, payload min / max
+    // words, and the row of each key of a direct table (whose range is
+    // below max(2 n, 65536), node_join.c)
+    const size_t rowof = a256((size_t)((2 * n > 65536 ? 2 * n : 65536) + 64) * 4);
+    return a256((size_t)n * 4) + a256((size_t)n * 8) + vgk_sort_pairs_scratch(n) + 256 + 256 + rowof;
 }
 
 // jt->cap, state, keys, start, count, rows (n_build entries) are allocated by
@@ -552,7 +572,7 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
     uint64_t *pkeys = (uint64_t *)p; p += a256((size_t)n * 8);
     void *sort_scratch = p; p += vgk_sort_pairs_scratch(n);
     uint32_t *counters = (uint32_t *)p; p += 256;
-    long long *mm = (long long *)p;
+    long long *mm = (long long *)p; p += 256;
     if (h_pay_mm)
         for (int i = 0; i < 6; i++) h_pay_mm[i] = 0;
     KeyArgs K;
@@ -572,19 +592,25 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         if (n_pay > 1) P.c1 = pay_cols[1];
     }
     if (slots_ready) *slots_ready = 1;
+    if (P.pay && n_build >= ((int64_t)1 << kRowBits)) P.pay = nullptr;   // too many rows for rowof: no payload
     if (P.pay) {
-        // direct table with a payload copy: rows write their entries, a
-        // check pass looks for repeated keys; the slot table is derived
-        // later, only if something reads it (vgk_join_slots_from_payload)
-        jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters, P.pay, 0, mm);
+        // direct table with a payload copy: rows record themselves per key,
+        // a check pass looks for repeated keys, then the payload is written
+        // in key order; the slot table is derived later, only if something
+        // reads it (vgk_join_slots_from_payload)
+        uint32_t *rowof = (uint32_t *)p;
+        jt_init_kernel<<<1, 32, 0, st>>>(*jt, counters, nullptr, 0, mm);
         vg_launch_counter++;
+        if (check(cudaMemsetAsync(rowof, 0xFF, (size_t)jt->cap * 4, st), "join build")) return -1;
         vg_prof_begin(VG_PROF_JOIN_BUILD, st);
         if (n_build > 0) {
             const unsigned g = (unsigned)((n_build + 255) / 256);
-            jt_pay_rows_kernel<<<g, 256, 0, st>>>(*jt, K, n_build, rslot, counters, P, mm);
-            jt_pay_verify_kernel<<<g, 256, 0, st>>>(P.pay, n_build, rslot, counters);
+            jt_rows_direct_kernel<<<g, 256, 0, st>>>(*jt, K, n_build, rslot, counters, P, rowof, mm);
+            jt_rows_verify_kernel<<<g, 256, 0, st>>>(rowof, n_build, rslot, counters);
             vg_launch_counter += 2;
         }
+        jt_pay_gather_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, rowof, P);
+        vg_launch_counter++;
         vg_prof_end(VG_PROF_JOIN_BUILD, st);
         uint32_t hc[4] = {0, 0, 0, 0};
         long long hm[6];
