@@ -424,10 +424,25 @@ __global__ void minmax_i64_kernel(VgCol c, int64_t n, long long *out) {
         lo = l2 < lo ? l2 : lo;
         hi = h2 > hi ? h2 : hi;
     }
+    // one combine per block: the three result words are single addresses
+    __shared__ long long s_lo, s_hi;
+    __shared__ unsigned long long s_cnt;
+    if (threadIdx.x == 0) {
+        s_lo = 0x7FFFFFFFFFFFFFFFll;
+        s_hi = (long long)0x8000000000000000ull;
+        s_cnt = 0;
+    }
+    __syncthreads();
     if ((threadIdx.x & 31) == 0 && cnt > 0) {
-        atomicMin(out + 0, lo);
-        atomicMax(out + 1, hi);
-        atomicAdd((unsigned long long *)out + 2, (unsigned long long)cnt);
+        atomicMin(&s_lo, lo);
+        atomicMax(&s_hi, hi);
+        atomicAdd(&s_cnt, (unsigned long long)cnt);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_cnt > 0) {
+        atomicMin(out + 0, s_lo);
+        atomicMax(out + 1, s_hi);
+        atomicAdd((unsigned long long *)out + 2, s_cnt);
     }
 }
 

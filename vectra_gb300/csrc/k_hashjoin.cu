@@ -296,45 +296,64 @@ constexpr uint32_t kRowMask = (1u << kRowBits) - 1u;
 
 __global__ void jt_rows_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t *rslot, uint32_t *counters,
                                       PayArgs P, uint32_t *rowof, long long *mm) {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in = r < n;
-    uint64_t p[2] = {0, 0};
-    uint32_t vb = 0;                                   // validity of the payload values
-    if (in) {
+    // per-thread min / max / count over a grid-stride range, then one
+    // combine per block (the statistic words are single addresses)
+    long long lo[2] = {0x7FFFFFFFFFFFFFFFll, 0x7FFFFFFFFFFFFFFFll};
+    long long hi[2] = {(long long)0x8000000000000000ull, (long long)0x8000000000000000ull};
+    unsigned long long cnt[2] = {0, 0};
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
         uint64_t k[VG_MAX_KEYS];
         int64_t d = -1;
         if (key_words(K, r, k)) {
             d = jt_direct_slot(jt, k[0]);
             if (d < 0) atomicOr(counters + 2, VG_ERR_FULL);
         }
+        uint32_t vb = 0;                               // validity of the payload values
         if (P.n_cols > 0 && vg_valid(P.c0, r)) vb |= 1u;
         if (P.n_cols > 1 && vg_valid(P.c1, r)) vb |= 2u;
         if (d >= 0) rowof[d] = (uint32_t)r | (vb << kRowBits);
         rslot[r] = (int32_t)d;
-        if (P.n_cols > 0 && P.c0.type == VEC_INT64 && (vb & 1u)) p[0] = vg_load_bits(P.c0, r);
-        if (P.n_cols > 1 && P.c1.type == VEC_INT64 && (vb & 2u)) p[1] = vg_load_bits(P.c1, r);
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            if (c >= P.n_cols || !((vb >> c) & 1u)) continue;
+            const VgCol &col = c == 0 ? P.c0 : P.c1;
+            if (col.type != VEC_INT64) continue;
+            const long long x = (long long)vg_load_bits(col, r);
+            lo[c] = x < lo[c] ? x : lo[c];
+            hi[c] = x > hi[c] ? x : hi[c];
+            cnt[c]++;
+        }
     }
+    __shared__ long long s_lo[2], s_hi[2];
+    __shared__ unsigned long long s_cnt[2];
+    if (threadIdx.x < 2) {
+        s_lo[threadIdx.x] = 0x7FFFFFFFFFFFFFFFll;
+        s_hi[threadIdx.x] = (long long)0x8000000000000000ull;
+        s_cnt[threadIdx.x] = 0;
+    }
+    __syncthreads();
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-        if (c >= P.n_cols) break;
-        const int type = c == 0 ? P.c0.type : P.c1.type;
-        if (type != VEC_INT64) continue;
-        const bool ok = in && ((vb >> c) & 1u);
-        long long lo = ok ? (long long)p[c] : 0x7FFFFFFFFFFFFFFFll;
-        long long hi = ok ? (long long)p[c] : (long long)0x8000000000000000ull;
-        unsigned cnt = ok ? 1u : 0u;
         for (int o = 16; o > 0; o >>= 1) {
-            const long long l2 = __shfl_xor_sync(0xFFFFFFFFu, lo, o);
-            const long long h2 = __shfl_xor_sync(0xFFFFFFFFu, hi, o);
-            cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, o);
-            lo = l2 < lo ? l2 : lo;
-            hi = h2 > hi ? h2 : hi;
+            const long long l2 = __shfl_xor_sync(0xFFFFFFFFu, lo[c], o);
+            const long long h2 = __shfl_xor_sync(0xFFFFFFFFu, hi[c], o);
+            cnt[c] += __shfl_xor_sync(0xFFFFFFFFu, cnt[c], o);
+            lo[c] = l2 < lo[c] ? l2 : lo[c];
+            hi[c] = h2 > hi[c] ? h2 : hi[c];
         }
-        if ((threadIdx.x & 31) == 0 && cnt) {
-            atomicMin(mm + 3 * c, lo);
-            atomicMax(mm + 3 * c + 1, hi);
-            atomicAdd((unsigned long long *)mm + 3 * c + 2, (unsigned long long)cnt);
+        if ((threadIdx.x & 31) == 0 && cnt[c]) {
+            atomicMin(s_lo + c, lo[c]);
+            atomicMax(s_hi + c, hi[c]);
+            atomicAdd(s_cnt + c, cnt[c]);
         }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 && threadIdx.x < P.n_cols && s_cnt[threadIdx.x]) {
+        const int c = threadIdx.x;
+        atomicMin(mm + 3 * c, s_lo[c]);
+        atomicMax(mm + 3 * c + 1, s_hi[c]);
+        atomicAdd((unsigned long long *)mm + 3 * c + 2, s_cnt[c]);
     }
 }
 
@@ -605,7 +624,8 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         vg_prof_begin(VG_PROF_JOIN_BUILD, st);
         if (n_build > 0) {
             const unsigned g = (unsigned)((n_build + 255) / 256);
-            jt_rows_direct_kernel<<<g, 256, 0, st>>>(*jt, K, n_build, rslot, counters, P, rowof, mm);
+            jt_rows_direct_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(*jt, K, n_build, rslot, counters, P,
+                                                                           rowof, mm);
             jt_rows_verify_kernel<<<g, 256, 0, st>>>(rowof, n_build, rslot, counters);
             vg_launch_counter += 2;
         }
