@@ -438,6 +438,67 @@ def reference_arm(args, rank, world):
                                         "d2h_bytes_per_step": 0}}
 
 
+def workload_arm(args):
+    """The reference's other configurations (not the headline line): the
+    query through the node C API over device-resident columns, its result
+    checked against torch, then timed with CUDA events."""
+    import torch
+    import vectra_gb300
+    from vectra_gb300 import workloads as W
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    eng = vectra_gb300.engine(dev.index)
+    lib = eng.lib
+    lib.vgpu_profile_enable.argtypes = [C.c_int]
+    lib.vgpu_profile_ms.restype = C.c_double
+    lib.vgpu_profile_ms.argtypes = [C.c_int, C.POINTER(C.c_ulonglong)]
+    if args.workload == "filter_group":
+        n = 10_000_000 // args.scale
+        cols = W.gen_filter_group(torch, n, 0, dev)
+        run = lambda: W.run_filter_group(eng, W.device_source(lib, cols, n)[0])
+        out = run()
+        kept = W.check_filter_group(torch, out, cols)
+        algo = W.filter_group_bytes(n)
+        desc = {"workload": "filter(temperature > 30, year >= 2020) |> group_by(station) |> "
+                            "summarise(avg = mean(temperature), n = n()) over 10M rows",
+                "rows": n, "rows_kept": kept, "groups": len(out["station"][0])}
+    else:
+        n, distinct = 200_000_000 // args.scale, 50_000_000 // args.scale
+        cols, raw = W.gen_high_card(torch, n, distinct, 0, dev)
+        run = lambda: W.run_high_card(eng, W.device_source(lib, cols, n)[0])
+        out = run()
+        groups = W.check_high_card(torch, out, cols, raw, distinct)
+        del raw
+        algo = W.high_card_bytes(n, groups)
+        desc = {"workload": "group_by(key) |> summarise(sum(x), mean(x), min(y), max(y), n()) over 200M rows, "
+                            "50M distinct int64 keys, 5% NA", "rows": n, "groups": groups + 1}
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        run()
+    torch.cuda.synchronize()
+    lib.vgpu_profile_reset()
+    lib.vgpu_profile_enable(1)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    lib.vgpu_profile_enable(0)
+    ms = e0.elapsed_time(e1) / args.steps
+    nl = C.c_ulonglong(0)
+    agg_ms = lib.vgpu_profile_ms(0, C.byref(nl))
+    peak, peak_kind = measured_peak()
+    return {"metric": "rows/s (input rows per second, whole query)", "value": n / (ms * 1e-3), "unit": "rows/s",
+            "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "config": desc, "data": "synthetic (seeded torch generator, seed 0)",
+            "algorithmic_bytes": algo, "hbm_gbs_whole_query": algo / (ms * 1e-3) / 1e9,
+            "frac_of_hbm_peak": algo / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
+            "agg_kernel_ms": agg_ms / max(1, args.steps * 1), "agg_launches": nl.value,
+            "result_checked": True}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -448,6 +509,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) measurement")
     ap.add_argument("--scale", type=int, default=1,
                     help="divide both table sizes (small cases for profiling only; not a bench line)")
+    ap.add_argument("--workload", default="join_agg", choices=["join_agg", "filter_group", "high_card"],
+                    help="join_agg: the headline line; the others measure the reference's other "
+                         "configurations (checked, not the headline)")
     args = ap.parse_args()
     if args.scale > 1:
         global N_FACT, N_DIM
@@ -462,6 +526,8 @@ def main():
         torch.distributed.init_process_group("nccl")
     if args.impl == "reference":
         line = reference_arm(args, rank, world)
+    elif args.workload != "join_agg":
+        line = workload_arm(args) if rank == 0 else None
     else:
         line = gpu_arm(args, rank, world)
     if rank == 0 and line is not None:

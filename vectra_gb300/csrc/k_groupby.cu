@@ -84,7 +84,7 @@ agg_kernel(const __grid_constant__ VgAggLaunch L, int64_t n_logical) {
                     uint64_t rank = matched ? (uint64_t)(mcount - 1 - m) : 0;
                     if (rank > 0x7FF) rank = 0x7FF;
                     order = ((uint64_t)L.batch_idx << 44) | ((uint64_t)(matched ? 0 : 1) << 43) |
-                            ((uint64_t)(li & 0xFFFFFFFF) << 11) | rank;
+                            ((uint64_t)((li + L.li_base) & 0xFFFFFFFF) << 11) | rank;
                 } else {
                     order = (uint64_t)(L.row_base + li);   // logical position in the stream
                 }

@@ -307,7 +307,7 @@ agg_fast_kernel(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
                 if (kJoin) {
                     bool m = (matched >> j) & 1u;
                     order = ((uint64_t)L.batch_idx << 44) | ((uint64_t)(m ? 0 : 1) << 43) |
-                            ((uint64_t)(li & 0xFFFFFFFF) << 11);
+                            ((uint64_t)((li + L.li_base) & 0xFFFFFFFF) << 11);
                 } else {
                     order = (uint64_t)(L.row_base + li);
                 }

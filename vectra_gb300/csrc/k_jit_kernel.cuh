@@ -22,7 +22,7 @@
 VG_DEV uint64_t vgj_order(const VgAggLaunch &L, int64_t li, uint32_t matched, int j) {
 #if VGJ_JOIN
     return ((uint64_t)L.batch_idx << 44) | ((uint64_t)(((matched >> j) & 1u) ? 0 : 1) << 43) |
-           ((uint64_t)(li & 0xFFFFFFFF) << 11);
+           ((uint64_t)((li + L.li_base) & 0xFFFFFFFF) << 11);
 #else
     (void)matched;
     (void)j;

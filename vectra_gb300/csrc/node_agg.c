@@ -279,6 +279,22 @@ static void table_alloc(Table *T, const Plan *P, int64_t cap) {
     vg_check_rc(vgk_group_table_init(g, P->n_keys, cls, P->n_accs, vg_stream()), "group table init");
 }
 
+/* rows per aggregation launch: the spill list holds up to 2^25 entries */
+static const int64_t kChunk = (int64_t)1 << 24;
+
+/* column view of rows [off, ...) of c */
+static VgCol vg_col_slice(const VgCol *c, int64_t off) {
+    VgCol o = *c;
+    if (off == 0 || !c->data) return o;
+    o.data = (const char *)c->data + (size_t)off * (c->type == VEC_BOOL ? 1 : 8);
+    if (c->valid) {
+        const int64_t b = (int64_t)c->voff + off;
+        o.valid = c->valid + (b >> 5);
+        o.voff = (int32_t)(b & 31);
+    }
+    return o;
+}
+
 static int64_t pow2_at_least(int64_t x) {
     int64_t c = 1024;
     while (c < x) c <<= 1;
@@ -553,14 +569,27 @@ static VecBatch *agg_next(VecNode *self) {
     VgDBatch db;
     int64_t batch_idx = 0, stream_pos = 0;
     while (vg_pull(P.src, need, 0, &db)) {
-        for (int j = 0; j < P.pset.n; j++) L->pcols[j] = db.cols[P.pset.idx[j]];
-        L->n_rows = db.n_rows;
-        L->sel = db.d_sel;
-        L->sel_n = db.sel_n;
         int64_t n_logical = db.d_sel ? db.sel_n : db.n_rows;
-        L->row_base = stream_pos;      /* logical position of the batch's first row */
         L->batch_idx = batch_idx;
-        if (n_logical > 0) run_batch(&P, &T, L, &S, n_logical);
+        /* launches of at most kChunk logical rows, so that everything one
+         * launch can spill fits the spill list (a batch of any size) */
+        for (int64_t off = 0; off < n_logical; off += kChunk) {
+            const int64_t n = n_logical - off < kChunk ? n_logical - off : kChunk;
+            if (db.d_sel) {
+                for (int j = 0; j < P.pset.n; j++) L->pcols[j] = db.cols[P.pset.idx[j]];
+                L->n_rows = db.n_rows;
+                L->sel = db.d_sel + off;
+                L->sel_n = n;
+            } else {
+                for (int j = 0; j < P.pset.n; j++) L->pcols[j] = vg_col_slice(&db.cols[P.pset.idx[j]], off);
+                L->n_rows = n;
+                L->sel = NULL;
+                L->sel_n = 0;
+            }
+            L->row_base = stream_pos + off;   /* logical position of the launch's first row */
+            L->li_base = off;
+            run_batch(&P, &T, L, &S, n);
+        }
         vg_dbatch_release(&db);
         stream_pos += n_logical;
         batch_idx++;

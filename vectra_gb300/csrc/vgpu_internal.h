@@ -277,6 +277,7 @@ typedef struct {
     const int64_t *replay;       /* replay list (pairs as above) or NULL */
     int64_t   replay_n;
     int64_t   batch_idx;         /* probe batch number (join ordering key) */
+    int64_t   li_base;           /* logical offset of this launch's rows within the probe batch */
     /* Direct-mapped cache for a single int64 key known to lie in
      * [dense_min, dense_min + dense_n) (a build-side attribute): cache slot
      * = key - dense_min, slot dense_n holds the NA key.  0 = hashed cache. */

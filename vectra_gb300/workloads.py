@@ -1,0 +1,164 @@
+"""Synthetic workloads of the reference's benchmark configurations beyond
+the join + aggregate headline, generated on the device with torch (seeded),
+with the queries built through the node C API and property checks of the
+results at full size.
+
+  filter_group  10M rows: station int64 U{0..999}, temperature f64
+                N(20, 10) with 1% NA, year int64 U{2000..2025};
+                filter(temperature > 30, year >= 2020) |> group_by(station)
+                |> summarise(avg = mean(temperature), n = n())
+  high_card     200M rows: key int64 over 50M distinct values (a bijective
+                scramble of U{0..50M-1}) with 5% NA, x f64 LogNormal(0, 2),
+                y int64 U{-1e6..1e6}; group_by(key) |> summarise(sum(x),
+                mean(x), min(y), max(y), n())
+"""
+import ctypes as C
+
+import numpy as np
+
+from .plan import Tbl, col
+
+
+def _validity(torch, mask):
+    n = mask.numel()
+    nb = ((n + 31) // 32) * 4
+    m = torch.zeros(nb * 8, dtype=torch.uint8, device=mask.device)
+    m[:n] = mask.to(torch.uint8)
+    w = torch.tensor([1, 2, 4, 8, 16, 32, 64, 128], dtype=torch.uint8, device=mask.device)
+    return (m.view(-1, 8) * w).sum(dim=1, dtype=torch.uint8)
+
+
+def device_source(lib, cols, n_rows, batch_rows=None):
+    """A VGPU_SRC_DEVICE table source over {name: (values, valid_mask or None)}."""
+    names = list(cols)
+    keep = []
+    data = (C.c_void_p * len(names))()
+    val = (C.c_void_p * len(names))()
+    types = (C.c_int * len(names))()
+    for i, n in enumerate(names):
+        v, m = cols[n]
+        data[i] = v.data_ptr()
+        types[i] = 1 if v.dtype.is_floating_point else 0
+        if m is not None:
+            import torch
+            bits = _validity(torch, m)
+            keep.append(bits)
+            val[i] = bits.data_ptr()
+        else:
+            val[i] = None
+    cn = (C.c_char_p * len(names))(*[n.encode() for n in names])
+    lib.vgpu_table_source_create.restype = C.c_void_p
+    p = lib.vgpu_table_source_create(len(names), cn, types, data, val, n_rows, batch_rows or n_rows, 2)
+    if not p:
+        raise RuntimeError(lib.vgpu_last_error().decode())
+    return p, keep
+
+
+# --------------------------------------------------------------------------
+# filter + group-by (10M rows)
+# --------------------------------------------------------------------------
+
+def gen_filter_group(torch, n, seed, device):
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    station = torch.randint(0, 1000, (n,), device=device, generator=g, dtype=torch.int64)
+    temp = torch.randn(n, dtype=torch.float64, device=device, generator=g) * 10.0 + 20.0
+    tvalid = torch.rand(n, device=device, generator=g) >= 0.01
+    temp[~tvalid] = 0.0
+    year = torch.randint(2000, 2026, (n,), device=device, generator=g, dtype=torch.int64)
+    return {"station": (station, None), "temperature": (temp, tvalid), "year": (year, None)}
+
+
+def run_filter_group(eng, src, temp_dir="tmp"):
+    return (Tbl(eng, src).filter((col("temperature") > 30.0) & (col("year") >= 2020.0))
+            .group_by("station").summarise(temp_dir=temp_dir, avg=("mean", "temperature"), n=("n",))
+            .collect())
+
+
+def check_filter_group(torch, out, cols):
+    st, _ = cols["station"]
+    t, tv = cols["temperature"]
+    y, _ = cols["year"]
+    keep = tv & (t > 30.0) & (y >= 2020)
+    cnt = torch.bincount(st[keep], minlength=1000)
+    s = torch.zeros(1000, dtype=torch.float64, device=st.device).index_add_(0, st[keep], t[keep])
+    present = (cnt > 0).cpu().numpy()
+    assert list(out["station"][0]) == list(np.nonzero(present)[0]), "groups"
+    assert np.array_equal(out["n"][0], cnt.cpu().numpy()[present].astype(np.float64)), "n()"
+    want = (s / cnt.clamp(min=1)).cpu().numpy()[present]
+    got = out["avg"][0]
+    assert np.all(np.abs(got - want) <= 1e-12 * np.abs(want)), "mean"
+    return int(keep.sum().item())
+
+
+def filter_group_bytes(n):
+    """Every referenced column once in the reference layout (3 columns)."""
+    return 3 * (8 * n + (n + 7) // 8)
+
+
+# --------------------------------------------------------------------------
+# high-cardinality group-by (200M rows, 50M distinct keys)
+# --------------------------------------------------------------------------
+
+SCRAMBLE = 0x9E3779B97F4A7C15 - (1 << 64)    # odd: multiplication is a bijection mod 2^64
+
+
+def gen_high_card(torch, n, distinct, seed, device):
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    raw = torch.randint(0, distinct, (n,), device=device, generator=g, dtype=torch.int64)
+    key = raw * SCRAMBLE                                  # wraps: distinct raw -> distinct key
+    kvalid = torch.rand(n, device=device, generator=g) >= 0.05
+    key[~kvalid] = 0
+    x = (torch.randn(n, dtype=torch.float64, device=device, generator=g) * 2.0).exp_()
+    y = torch.randint(-1_000_000, 1_000_001, (n,), device=device, generator=g, dtype=torch.int64)
+    return {"key": (key, kvalid), "x": (x, None), "y": (y, None)}, raw
+
+
+def run_high_card(eng, src, temp_dir="tmp"):
+    return (Tbl(eng, src).group_by("key")
+            .summarise(temp_dir=temp_dir, s=("sum", "x"), m=("mean", "x"), lo=("min", "y"), hi=("max", "y"),
+                       n=("n",)).collect())
+
+
+def _signed64(u):
+    return u - (1 << 64) if u >= (1 << 63) else u
+
+
+def check_high_card(torch, out, cols, raw, distinct):
+    """Every group against torch: the group count, ascending key order with
+    the NA group last, n(), sum and mean (relative 1e-12), min and max."""
+    key, kv = cols["key"]
+    x, _ = cols["x"]
+    y, _ = cols["y"]
+    dev = key.device
+    keys, kvalid = out["key"]
+    r = raw[kv]
+    cnt = torch.bincount(r, minlength=distinct)
+    n_na = int((~kv).sum().item())
+    n_groups = int((cnt > 0).sum().item())
+    assert len(keys) == n_groups + (1 if n_na else 0), ("groups", len(keys), n_groups)
+    if n_na:
+        assert not kvalid[-1] and out["n"][0][-1] == n_na, "NA group last"
+    tk = torch.from_numpy(np.ascontiguousarray(keys[:n_groups])).to(dev)
+    assert bool((tk[1:] > tk[:-1]).all()), "key order"
+    inv = tk * _signed64(pow(SCRAMBLE % (1 << 64), -1, 1 << 64))   # raw id of each output key
+    s = torch.zeros(distinct, dtype=torch.float64, device=dev).index_add_(0, r, x[kv])
+    big = torch.iinfo(torch.int64)
+    lo = torch.full((distinct,), big.max, dtype=torch.int64, device=dev).scatter_reduce_(0, r, y[kv], "amin")
+    hi = torch.full((distinct,), big.min, dtype=torch.int64, device=dev).scatter_reduce_(0, r, y[kv], "amax")
+    g = lambda name: torch.from_numpy(np.ascontiguousarray(out[name][0][:n_groups])).to(dev)
+    assert bool((cnt[inv].to(torch.float64) == g("n")).all()), "n()"
+    want = s[inv]
+    assert bool(((g("s") - want).abs() <= 1e-12 * want.abs()).all()), "sum"
+    wm = want / cnt[inv].to(torch.float64)
+    assert bool(((g("m") - wm).abs() <= 1e-12 * wm.abs()).all()), "mean"
+    assert bool((g("lo") == lo[inv].to(torch.float64)).all()), "min"
+    assert bool((g("hi") == hi[inv].to(torch.float64)).all()), "max"
+    return n_groups
+
+
+def high_card_bytes(n, n_groups):
+    """Inputs (3 columns) and outputs (key + 5 aggregates) once each."""
+    vb = lambda k: (k + 7) // 8
+    return 3 * 8 * n + vb(n) + 6 * (8 * n_groups + vb(n_groups))
