@@ -30,6 +30,14 @@ void vg_prof_end(int cls, cudaStream_t s);
 // validity bits and column loads
 // ---------------------------------------------------------------------
 
+// Load with acquire semantics at device scope: the writes a releasing
+// thread made before publishing this word are visible after it.
+VG_DEV uint32_t vg_ld_acquire(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 VG_DEV bool vg_valid(const VgCol &c, int64_t r) {
     r += c.voff;
     return c.valid == nullptr || ((__ldg(c.valid + (r >> 5)) >> (r & 31)) & 1u);

@@ -344,7 +344,10 @@ VG_DEV int64_t gt_find_insert(const VgGroupTable &gt, const Keys &k, int nk, con
     int64_t slot = (int64_t)(h & (uint64_t)mask);
     const int64_t max_probe = gt.cap < kGlobalProbes ? gt.cap : kGlobalProbes;
     for (int64_t probe = 0; probe < max_probe; probe++) {
-        uint32_t st = *(volatile uint32_t *)(gt.state + slot);
+        // state 2 is published after the key words (fence + exchange), so
+        // an acquire load of it orders the key reads below: no fence on the
+        // lookup path
+        uint32_t st = vg_ld_acquire(gt.state + slot);
         if (st == 0) {
             uint32_t prev = atomicCAS(gt.state + slot, 0u, 1u);
             if (prev == 0u) {
@@ -357,15 +360,14 @@ VG_DEV int64_t gt_find_insert(const VgGroupTable &gt, const Keys &k, int nk, con
                 atomicAdd(gt.n_used, 1u);
                 return slot;
             }
-            st = prev;
+            st = vg_ld_acquire(gt.state + slot);
         }
         int spins = 0;
         while (st == 1u) {
             if (++spins > VG_SPIN_LIMIT) { atomicOr(gt.err, VG_ERR_WAIT); return -1; }
             __nanosleep(32);
-            st = *(volatile uint32_t *)(gt.state + slot);
+            st = vg_ld_acquire(gt.state + slot);
         }
-        __threadfence();
         uint32_t tnm = *(volatile uint32_t *)(gt.nullmask + slot);
         if (keys_eq(gt.keys, gt.cap, slot, k, nk, kt, tnm, nm)) return slot;
         slot = (slot + 1) & mask;

@@ -153,7 +153,8 @@ VG_DEV int64_t insert_multi(const VgJoinTable &jt, const uint64_t *k, int nk, ui
     const int64_t mask = jt.cap - 1;
     int64_t slot = (int64_t)(vg_jhash(k, nk) & (uint64_t)mask);
     for (int64_t probe = 0; probe < jt.cap; probe++) {
-        uint32_t st = *(volatile uint32_t *)(jt.state + slot);
+        // acquire loads of the state order the key reads after state 2
+        uint32_t st = vg_ld_acquire(jt.state + slot);
         if (st == 0) {
             uint32_t prev = atomicCAS(jt.state + slot, 0u, 1u);
             if (prev == 0u) {
@@ -162,15 +163,14 @@ VG_DEV int64_t insert_multi(const VgJoinTable &jt, const uint64_t *k, int nk, ui
                 atomicExch(jt.state + slot, 2u);
                 return slot;
             }
-            st = prev;
+            st = vg_ld_acquire(jt.state + slot);
         }
         int spins = 0;
         while (st == 1u) {
             if (++spins > VG_SPIN_LIMIT) { atomicOr(counters + 2, VG_ERR_WAIT); return -1; }
             __nanosleep(32);
-            st = *(volatile uint32_t *)(jt.state + slot);
+            st = vg_ld_acquire(jt.state + slot);
         }
-        __threadfence();
         bool eq = true;
         for (int i = 0; i < nk && eq; i++)
             eq = *(volatile uint64_t *)(jt.keys + (int64_t)i * jt.cap + slot) == k[i];
