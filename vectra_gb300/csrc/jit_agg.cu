@@ -352,6 +352,15 @@ int vgk_agg_launch_jit(const VgAggLaunch *L, int64_t n_logical, vg_stream_t s) {
         if (it == g_cache.end()) {
             JitKernel k;
             std::vector<char> cubin;
+            // VGPU_JIT_DUMP=<file>: append each newly compiled plan's source
+            const char *dump = getenv("VGPU_JIT_DUMP");
+            if (dump) {
+                FILE *f = fopen(dump, "a");
+                if (f) {
+                    fputs(src.c_str(), f);
+                    fclose(f);
+                }
+            }
             if (compile_plan(*L, S, vec, cubin, k.shape, nullptr) != 0) return -1;
             if (load_kernel(cubin, k) != 0) return -1;
             it = g_cache.emplace(src, k).first;

@@ -279,8 +279,8 @@ static void table_alloc(Table *T, const Plan *P, int64_t cap) {
     vg_check_rc(vgk_group_table_init(g, P->n_keys, cls, P->n_accs, vg_stream()), "group table init");
 }
 
-/* rows per aggregation launch: the spill list holds up to 2^25 entries */
-static const int64_t kChunk = (int64_t)1 << 24;
+/* rows per aggregation launch (the spill list is sized for a launch) */
+static const int64_t kChunk = (int64_t)1 << 28;
 
 /* column view of rows [off, ...) of c */
 static VgCol vg_col_slice(const VgCol *c, int64_t off) {
@@ -326,7 +326,6 @@ static void run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_log
     int sms = vgk_num_sms();
     /* spill space for this launch */
     int64_t need_rows = n_logical + 65536;
-    if (need_rows > ((int64_t)1 << 25)) need_rows = (int64_t)1 << 25;
     if (!S->counters) S->counters = (uint32_t *)vg_dmalloc(256);
     if (S->rows_cap < need_rows) {
         vg_dfree(S->rows);
