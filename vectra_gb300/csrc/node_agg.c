@@ -279,8 +279,10 @@ static void table_alloc(Table *T, const Plan *P, int64_t cap) {
     vg_check_rc(vgk_group_table_init(g, P->n_keys, cls, P->n_accs, vg_stream()), "group table init");
 }
 
-/* rows per aggregation launch (the spill list is sized for a launch) */
-static const int64_t kChunk = (int64_t)1 << 28;
+/* Rows per aggregation launch while the group table is still growing; once
+ * a launch needed no growth, the rest of the batch goes in one launch (the
+ * spill list is sized for a launch). */
+static const int64_t kChunk = (int64_t)1 << 24;
 
 /* column view of rows [off, ...) of c */
 static VgCol vg_col_slice(const VgCol *c, int64_t off) {
@@ -322,7 +324,8 @@ static int cache_slots_for(const VgAggLaunch *L) {
     return 0;
 }
 
-static void run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_logical) {
+/* one launch over n_logical rows (+ growth and replay); 1 if the table grew */
+static int run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_logical) {
     int sms = vgk_num_sms();
     /* spill space for this launch */
     int64_t need_rows = n_logical + 65536;
@@ -369,8 +372,9 @@ static void run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_log
                                                    vg_stream()), "group table rehash");
                 vg_dfree(T->block);
                 *T = T2;
+                return 1;
             }
-            break;
+            return 0;
         }
         /* grow the table, move the groups, then replay what spilled */
         int64_t ncap = pow2_at_least(2 * ((int64_t)used + c[0] + c[1]) + 1024);
@@ -396,7 +400,7 @@ static void run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_log
         vg_d2h(&err, T->gt.err, 4);
         vg_sync();
         if (err) vg_fail("group-agg: table still full after growing (code %u)", err);
-        break;
+        return 1;
     }
 }
 
@@ -572,8 +576,10 @@ static VecBatch *agg_next(VecNode *self) {
         L->batch_idx = batch_idx;
         /* launches of at most kChunk logical rows, so that everything one
          * launch can spill fits the spill list (a batch of any size) */
-        for (int64_t off = 0; off < n_logical; off += kChunk) {
-            const int64_t n = n_logical - off < kChunk ? n_logical - off : kChunk;
+        int settled = 0;
+        for (int64_t off = 0, n = 0; off < n_logical; off += n) {
+            n = n_logical - off;
+            if (!settled && n > kChunk) n = kChunk;
             if (db.d_sel) {
                 for (int j = 0; j < P.pset.n; j++) L->pcols[j] = db.cols[P.pset.idx[j]];
                 L->n_rows = db.n_rows;
@@ -587,7 +593,7 @@ static VecBatch *agg_next(VecNode *self) {
             }
             L->row_base = stream_pos + off;   /* logical position of the launch's first row */
             L->li_base = off;
-            run_batch(&P, &T, L, &S, n);
+            settled = !run_batch(&P, &T, L, &S, n);
         }
         vg_dbatch_release(&db);
         stream_pos += n_logical;
