@@ -122,13 +122,26 @@ int vgk_agg_jit_ok(const VgAggLaunch *L) {
 }
 
 // Cache slots the specialised kernel uses: the dense range (rounded up to a
-// power of two) when the keys are known, else the plan's cache size.
+// power of two) when the keys are known, else up to twice the plan's cache
+// size while the layout fits the shared memory one CTA per SM can have
+// (the spill area holds two plan-size caches per SM).
 int vgk_agg_jit_slots(const VgAggLaunch *L) {
     if (L->dense) {
         int s = next_pow2(L->dense_n + 1);
         return s < 256 ? 256 : (s > L->cache_slots ? L->cache_slots : s);
     }
-    return L->cache_slots;
+    int S = L->cache_slots;
+    VgAggLaunch T = *L;
+    for (;;) {
+        const int S2 = 2 * S;
+        if (S2 > 2 * L->cache_slots) break;
+        T.cache_slots = S2;
+        Lay c;
+        make_lay(T, (uint64_t)S2, c);
+        if (c.total > 200 * 1024) break;
+        S = S2;
+    }
+    return S;
 }
 
 // The plan-specific source for L with S cache slots.

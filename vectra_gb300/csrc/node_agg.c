@@ -314,6 +314,12 @@ typedef struct {
     int64_t rows_cap, cache_cap;
 } Spill;
 
+/* The spill list is sized for a whole launch and kept between queries (the
+ * node API runs one query at a time), so a large batch does not allocate
+ * gigabytes per query. */
+static int64_t *g_spill_rows;
+static int64_t g_spill_rows_cap;
+
 static int cache_slots_for(const VgAggLaunch *L) {
     /* largest power of two <= 2048 whose shared layout fits in 96 KB */
     VgAggLaunch tmp = *L;
@@ -330,11 +336,13 @@ static int run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_logi
     /* spill space for this launch */
     int64_t need_rows = n_logical + 65536;
     if (!S->counters) S->counters = (uint32_t *)vg_dmalloc(256);
-    if (S->rows_cap < need_rows) {
-        vg_dfree(S->rows);
-        S->rows = (int64_t *)vg_dmalloc((size_t)need_rows * 16);
-        S->rows_cap = need_rows;
+    if (g_spill_rows_cap < need_rows) {
+        vg_dfree(g_spill_rows);
+        g_spill_rows = (int64_t *)vg_dmalloc((size_t)need_rows * 16);
+        g_spill_rows_cap = need_rows;
     }
+    S->rows = g_spill_rows;
+    S->rows_cap = g_spill_rows_cap;
     int64_t cc = (int64_t)sms * 2 * (L->cache_slots > 0 ? L->cache_slots : 1);
     if (L->cache_slots > 0 && S->cache_cap < cc) {
         vg_dfree(S->cache);
@@ -601,7 +609,6 @@ static VecBatch *agg_next(VecNode *self) {
     }
     VecBatch *res = emit_result(A, &P, &T);
     vg_dfree(T.block);
-    vg_dfree(S.rows);
     vg_dfree(S.cache);
     vg_dfree(S.counters);
     free(L);
