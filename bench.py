@@ -27,6 +27,8 @@ cpu_baseline: this repository's CPU restatement of the reference path
 import argparse
 import ctypes as C
 import json
+
+import numpy as np
 import os
 import statistics
 import subprocess
@@ -452,6 +454,8 @@ def workload_arm(args):
     lib.vgpu_profile_enable.argtypes = [C.c_int]
     lib.vgpu_profile_ms.restype = C.c_double
     lib.vgpu_profile_ms.argtypes = [C.c_int, C.POINTER(C.c_ulonglong)]
+    if args.workload == "query_set":
+        return query_set_arm(args, eng, lib, dev)
     if args.workload == "filter_group":
         n = 10_000_000 // args.scale
         cols = W.gen_filter_group(torch, n, 0, dev)
@@ -499,6 +503,78 @@ def workload_arm(args):
             "result_checked": True}
 
 
+def query_set_arm(args, eng, lib, dev):
+    """4096 small group-by / inner-join instances: queries per second as a
+    query set (one CUDA graph replay runs all of them) and through the plain
+    node path (one query after another, each its own launches) on a sample."""
+    import torch
+    from vectra_gb300 import workloads as W
+    from vectra_gb300.plan import Tbl
+    n_inst = 4096 // args.scale
+    qs = W.gen_query_set(torch, n_inst, 0, dev)
+    arr, outs, out_rows, keep = W.query_set_structs(torch, qs, dev)
+    lib.vgpu_queryset_prepare.restype = C.c_int
+    lib.vgpu_queryset_prepare.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
+    lib.vgpu_queryset_run.argtypes = [C.c_void_p]
+    lib.vgpu_queryset_free.argtypes = [C.c_void_p]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plan = C.c_void_p()
+    if lib.vgpu_queryset_prepare(arr, n_inst, C.byref(plan)) != 0:
+        raise RuntimeError(lib.vgpu_last_error().decode())
+    prep_s = time.perf_counter() - t0
+    if lib.vgpu_queryset_run(plan) != 0:
+        raise RuntimeError(lib.vgpu_last_error().decode())
+    rng = np.random.default_rng(2)
+    sample = rng.choice(n_inst, size=min(256, n_inst), replace=False)
+    W.check_query_set(torch, qs, outs, out_rows, sample)
+    for _ in range(args.warmup):
+        lib.vgpu_queryset_run(plan)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        lib.vgpu_queryset_run(plan)
+        times.append(time.perf_counter() - t0)
+    lib.vgpu_queryset_free(plan)
+    set_s = statistics.median(times)
+    # the plain path: every query through the node API on its own
+    off = np.concatenate([[0], np.cumsum(qs["rows"])])
+    boff = np.concatenate([[0], np.cumsum(qs["bcard"])])
+    plain = rng.choice(n_inst, size=min(128, n_inst), replace=False)
+
+    def one(i):
+        k = qs["key"][off[i]:off[i + 1]]
+        if qs["kind"][i] == W.SET_GROUP:
+            v = qs["value"][off[i]:off[i + 1]]
+            src, _ = W.device_source(lib, {"key": (k, None), "value": (v, None)}, len(k))
+            return Tbl(eng, src).group_by("key").summarise(temp_dir=None, s=("sum", "value"),
+                                                           m=("mean", "value"), n=("n",)).batches()
+        b = qs["bkey"][boff[i]:boff[i + 1]]
+        ps, _ = W.device_source(lib, {"key": (k, None)}, len(k))
+        bs, _ = W.device_source(lib, {"key": (b, None)}, len(b))
+        return Tbl(eng, ps).inner_join(Tbl(eng, bs), "key").batches()
+    for i in plain[:8]:
+        one(i)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in plain:
+        one(i)
+    torch.cuda.synchronize()
+    plain_s = (time.perf_counter() - t0) / len(plain)
+    rows = int(qs["rows"].sum() + qs["bcard"].sum())
+    return {"metric": "queries/s (query set of small group-by / inner-join instances)",
+            "value": n_inst / set_s, "unit": "queries/s", "ms_per_step": set_s * 1e3, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True,
+            "config": {"workload": "%d instances: rows LogNormal(median 20k, sigma 1.5) capped at 5M, group "
+                                   "cardinality log-uniform [1, 1e5], half group_by+summarise(sum, mean, n), half "
+                                   "inner_join (unique build keys, ~50%% probe match), int32-range / int64 keys, "
+                                   "values N(0,1)" % n_inst, "input_rows": rows},
+            "plain_path_queries_per_s": 1.0 / plain_s, "plain_path_sample": len(plain),
+            "speedup_vs_plain": (n_inst / set_s) * plain_s, "rows_per_s": rows / set_s,
+            "prepare_s": prep_s, "data": "synthetic (seeded numpy / torch generators, seed 0)",
+            "result_checked": "256 sampled instances against torch"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -509,7 +585,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) measurement")
     ap.add_argument("--scale", type=int, default=1,
                     help="divide both table sizes (small cases for profiling only; not a bench line)")
-    ap.add_argument("--workload", default="join_agg", choices=["join_agg", "filter_group", "high_card"],
+    ap.add_argument("--workload", default="join_agg", choices=["join_agg", "filter_group", "high_card", "query_set"],
                     help="join_agg: the headline line; the others measure the reference's other "
                          "configurations (checked, not the headline)")
     args = ap.parse_args()

@@ -121,6 +121,44 @@ JoinNode     *vgpu_guard_join(VecNode *left, VecNode *right, JoinKind kind,
                               const char *suffix_y);
 void          vgpu_batch_free(VecBatch *batch);
 
+/* ---- query sets: many small queries at once (no reference counterpart) */
+/* Many small independent queries run together: a plan prepared once
+ * captures persistent kernels over all of them in one CUDA graph, and
+ * every run replays it.  Two kinds, on one int64 key column (no NA):
+ *   VGPU_SET_GROUP  group_by(key) |> summarise(sum(value), mean(value),
+ *                   n()): one output row per distinct key (table order, not
+ *                   sorted), double sums correctly rounded;
+ *   VGPU_SET_JOIN   inner_join over unique build keys: the (probe row,
+ *                   build row) pairs in probe row order.
+ * All pointers are device memory the caller keeps alive while the plan
+ * exists; outputs are sized by the caller (group: max_groups rows, join: n
+ * rows) and *out_rows receives the output row count. */
+#define VGPU_SET_GROUP 0
+#define VGPU_SET_JOIN  1
+typedef struct {
+    int32_t kind;
+    int32_t pad;
+    int64_t n;                  /* group rows / probe rows */
+    const int64_t *key;         /* group keys / probe keys */
+    const double *value;        /* group values */
+    int64_t n_build;            /* join build rows */
+    const int64_t *build_key;   /* join build keys (unique) */
+    int64_t max_groups;         /* group: bound on distinct keys (output rows) */
+    int64_t *out_key;           /* group outputs */
+    double *out_sum;
+    double *out_mean;
+    int64_t *out_n;
+    int32_t *out_probe;         /* join outputs */
+    int32_t *out_build;
+    int64_t *out_rows;          /* output row count (device) */
+} VgpuSetQuery;
+/* 0 on success (*plan set), -1 with vgpu_last_error set. */
+int  vgpu_queryset_prepare(const VgpuSetQuery *queries, int n_queries, void **plan);
+/* Runs every query of the plan and waits: 0, or -1 (a table or output too
+ * small, repeated build keys) with vgpu_last_error set. */
+int  vgpu_queryset_run(void *plan);
+void vgpu_queryset_free(void *plan);
+
 /* ---- allocation-free filter (no counterpart in the reference) -------- */
 /* For callers that may not allocate device memory during a query: a host
  * whose device memory is fully reserved by another framework's pool, a

@@ -162,3 +162,128 @@ def high_card_bytes(n, n_groups):
     """Inputs (3 columns) and outputs (key + 5 aggregates) once each."""
     vb = lambda k: (k + 7) // 8
     return 3 * 8 * n + vb(n) + 6 * (8 * n_groups + vb(n_groups))
+
+
+# --------------------------------------------------------------------------
+# query sets: many small group-by / join instances (vgpu_queryset_*)
+# --------------------------------------------------------------------------
+
+SET_GROUP, SET_JOIN = 0, 1
+
+
+class SetQuery(C.Structure):
+    """Mirror of VgpuSetQuery (include/vgpu.h)."""
+    _fields_ = [("kind", C.c_int32), ("pad", C.c_int32), ("n", C.c_int64), ("key", C.c_void_p),
+                ("value", C.c_void_p), ("n_build", C.c_int64), ("build_key", C.c_void_p),
+                ("max_groups", C.c_int64), ("out_key", C.c_void_p), ("out_sum", C.c_void_p),
+                ("out_mean", C.c_void_p), ("out_n", C.c_void_p), ("out_probe", C.c_void_p),
+                ("out_build", C.c_void_p), ("out_rows", C.c_void_p)]
+
+
+def gen_query_set(torch, n_inst, seed, device, median_rows=20_000, sigma=1.5, cap_rows=5_000_000,
+                  max_card=100_000):
+    """n_inst instances: rows ~ LogNormal(ln median_rows, sigma) capped,
+    group cardinality log-uniform [1, max_card], half group_by + summarise
+    (sum, mean, n), half inner joins against `card` unique build keys with
+    probe keys uniform over [0, 2 card) (about half match); keys in the
+    int32 range for half the instances, scrambled over int64 for the rest;
+    values N(0, 1)."""
+    rng = np.random.default_rng(seed)
+    rows = np.clip(np.round(rng.lognormal(np.log(median_rows), sigma, n_inst)), 1, cap_rows).astype(np.int64)
+    card = np.clip(np.round(np.exp(rng.uniform(0.0, np.log(max_card), n_inst))), 1, max_card).astype(np.int64)
+    kind = rng.integers(0, 2, n_inst)
+    wide = rng.integers(0, 2, n_inst).astype(bool)
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    total = int(rows.sum())
+    # probe / group keys: uniform over [0, card) or [0, 2 card) per instance
+    span = np.where(kind == SET_GROUP, card, 2 * card)
+    span_t = torch.from_numpy(np.repeat(span, rows)).to(device)
+    key = (torch.rand(total, dtype=torch.float64, device=device, generator=g) * span_t).to(torch.int64)
+    key = torch.minimum(key, span_t - 1)
+    wide_t = torch.from_numpy(np.repeat(wide, rows)).to(device)
+    key = torch.where(wide_t, key * SCRAMBLE, key)
+    value = torch.randn(total, dtype=torch.float64, device=device, generator=g)
+    bcard = np.where(kind == SET_JOIN, card, 0)
+    btotal = int(bcard.sum())
+    bkey = torch.cat([torch.arange(int(c), device=device, dtype=torch.int64) for c in bcard if c > 0]) \
+        if btotal else torch.empty(0, dtype=torch.int64, device=device)
+    bwide = torch.from_numpy(np.repeat(wide, bcard)).to(device)
+    bkey = torch.where(bwide, bkey * SCRAMBLE, bkey)
+    return {"rows": rows, "card": card, "kind": kind, "wide": wide, "key": key, "value": value, "bkey": bkey,
+            "bcard": bcard}
+
+
+def query_set_structs(torch, qs, device):
+    """VgpuSetQuery array over the generated instances, with output buffers."""
+    n = len(qs["rows"])
+    arr = (SetQuery * n)()
+    keep = []
+    off = np.concatenate([[0], np.cumsum(qs["rows"])])
+    boff = np.concatenate([[0], np.cumsum(qs["bcard"])])
+    kp, vp, bp = qs["key"].data_ptr(), qs["value"].data_ptr(), qs["bkey"].data_ptr()
+    out_rows = torch.zeros(n, dtype=torch.int64, device=device)
+    keep.append(out_rows)
+    outs = []
+    for i in range(n):
+        q = arr[i]
+        q.kind = int(qs["kind"][i])
+        q.n = int(qs["rows"][i])
+        q.key = kp + 8 * int(off[i])
+        q.out_rows = out_rows.data_ptr() + 8 * i
+        if q.kind == SET_GROUP:
+            q.value = vp + 8 * int(off[i])
+            mg = int(min(qs["card"][i], qs["rows"][i]))
+            q.max_groups = mg
+            o = {"key": torch.empty(mg, dtype=torch.int64, device=device),
+                 "sum": torch.empty(mg, dtype=torch.float64, device=device),
+                 "mean": torch.empty(mg, dtype=torch.float64, device=device),
+                 "n": torch.empty(mg, dtype=torch.int64, device=device)}
+            q.out_key, q.out_sum = o["key"].data_ptr(), o["sum"].data_ptr()
+            q.out_mean, q.out_n = o["mean"].data_ptr(), o["n"].data_ptr()
+        else:
+            q.n_build = int(qs["bcard"][i])
+            q.build_key = bp + 8 * int(boff[i])
+            o = {"probe": torch.empty(max(1, q.n), dtype=torch.int32, device=device),
+                 "build": torch.empty(max(1, q.n), dtype=torch.int32, device=device)}
+            q.out_probe, q.out_build = o["probe"].data_ptr(), o["build"].data_ptr()
+        outs.append(o)
+    return arr, outs, out_rows, keep
+
+
+def check_query_set(torch, qs, outs, out_rows, idx):
+    """Instances idx against torch: group keys and n exactly, sums within
+    1e-12 of the sum of magnitudes (torch adds in arbitrary order), mean =
+    sum / n, as sets sorted by key; join pairs exactly, in probe order."""
+    off = np.concatenate([[0], np.cumsum(qs["rows"])])
+    boff = np.concatenate([[0], np.cumsum(qs["bcard"])])
+    nrow = out_rows.cpu().numpy()
+    for i in idx:
+        k = qs["key"][off[i]:off[i + 1]]
+        o = outs[i]
+        if qs["kind"][i] == SET_GROUP:
+            v = qs["value"][off[i]:off[i + 1]]
+            uk, inv = torch.unique(k, return_inverse=True)
+            cnt = torch.bincount(inv, minlength=len(uk))
+            s = torch.zeros(len(uk), dtype=torch.float64, device=k.device).index_add_(0, inv, v)
+            m = int(nrow[i])
+            assert m == len(uk), (i, m, len(uk))
+            order = torch.argsort(o["key"][:m])
+            assert bool((o["key"][:m][order] == uk).all()), i
+            assert bool((o["n"][:m][order] == cnt).all()), i
+            got = o["sum"][:m][order]
+            # torch sums in arbitrary order: bound by the sum of magnitudes
+            sa = torch.zeros(len(uk), dtype=torch.float64, device=k.device).index_add_(0, inv, v.abs())
+            assert bool(((got - s).abs() <= 1e-12 * sa).all()), i
+            mean = o["mean"][:m][order]
+            assert bool(((mean - got / cnt.double()).abs() <= 1e-15 * (got / cnt.double()).abs() + 1e-300).all()), i
+        else:
+            b = qs["bkey"][boff[i]:boff[i + 1]]
+            sb, perm = torch.sort(b)
+            pos = torch.searchsorted(sb, k).clamp(max=max(0, len(sb) - 1))
+            hit = (sb[pos] == k) if len(sb) else torch.zeros_like(k, dtype=torch.bool)
+            prow = torch.nonzero(hit).flatten().to(torch.int32)
+            brow = perm[pos[hit]].to(torch.int32)
+            m = int(nrow[i])
+            assert m == len(prow), (i, m, len(prow))
+            assert bool((o["probe"][:m] == prow).all()) and bool((o["build"][:m] == brow).all()), i
