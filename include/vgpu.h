@@ -159,6 +159,54 @@ int  vgpu_queryset_prepare(const VgpuSetQuery *queries, int n_queries, void **pl
 int  vgpu_queryset_run(void *plan);
 void vgpu_queryset_free(void *plan);
 
+/* ---- serving loop over resident tables (no reference counterpart) ---- */
+/* A server keeps tables resident (device pointers the caller keeps alive)
+ * and runs requests as they arrive: vgpu_server_poll admits queued
+ * requests in arrival order while their estimated memory fits the budget,
+ * launches the admitted ones as one wave on a free stream (waves on
+ * different streams overlap) and retires finished waves.  Kinds:
+ *   VGPU_SERVE_FILTER_SUM  rows with a valid val > threshold: count, exact sum
+ *   VGPU_SERVE_GROUP_SUM   group_by(key) |> summarise(sum(val, na.rm = TRUE),
+ *                          n()): NA keys form one group
+ *   VGPU_SERVE_SEMI / ANTI rows of `table` whose key has / has no match in
+ *                          `build_table` (NA keys never match), ascending
+ * Bitmaps use the reference layout, 4-byte aligned, padded to 32-bit words;
+ * NULL means all valid.  Results stay valid until vgpu_server_release. */
+#define VGPU_SERVE_FILTER_SUM 0
+#define VGPU_SERVE_GROUP_SUM  1
+#define VGPU_SERVE_SEMI       2
+#define VGPU_SERVE_ANTI       3
+typedef struct {
+    int32_t kind;
+    int32_t table;
+    int32_t build_table;
+    int32_t pad;
+    double  threshold;
+} VgpuServeQuery;
+typedef struct {
+    int64_t rows;                 /* filter: rows kept; group: groups; semi / anti: rows */
+    double  sum;                  /* filter: exact sum */
+    const int64_t *key;           /* group (device): keys ... */
+    const uint8_t *key_valid;     /* ... 0 for the NA group ... */
+    const double  *group_sum;     /* ... exact sums ... */
+    const int64_t *group_n;       /* ... n() */
+    const int32_t *sel;           /* semi / anti (device): selected rows */
+} VgpuServeResult;
+void   *vgpu_server_create(int n_streams, int64_t budget_bytes);
+int     vgpu_server_add_table(void *server, const int64_t *key, const uint8_t *key_valid,
+                              const double *val, const uint8_t *val_valid, int64_t n);
+int64_t vgpu_server_submit(void *server, const VgpuServeQuery *query);   /* request id, or -1 */
+int     vgpu_server_poll(void *server);          /* requests not yet done, or -1 */
+int     vgpu_server_done(void *server, int64_t id);
+int     vgpu_server_result(void *server, int64_t id, VgpuServeResult *result);
+void    vgpu_server_release(void *server, int64_t id);
+/* Builds a table's key set now (it is built at the first request that
+ * needs it otherwise): 0 or -1. */
+int     vgpu_server_warm(void *server, int table);
+void    vgpu_server_free(void *server);
+/* Copies bytes of device memory (a result) to host memory; 0 or -1. */
+int     vgpu_copy_to_host(void *dst_host, const void *src_device, int64_t bytes);
+
 /* ---- allocation-free filter (no counterpart in the reference) -------- */
 /* For callers that may not allocate device memory during a query: a host
  * whose device memory is fully reserved by another framework's pool, a

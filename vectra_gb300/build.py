@@ -22,7 +22,7 @@ LIB = os.path.join(HERE, "libvgpu.so")
 ARCHIVE = os.path.join(HERE, "libvgpu.a")
 
 CU_SOURCES = ["k_groupby_fastj.cu", "k_groupby_fast.cu", "k_groupby.cu", "jit_agg.cu", "k_filter.cu",
-              "k_sort.cu", "k_hashjoin.cu", "k_prof.cu", "k_static.cu", "k_batch.cu"]
+              "k_sort.cu", "k_hashjoin.cu", "k_prof.cu", "k_static.cu", "k_batch.cu", "k_serve.cu"]
 # headers the run-time compiler needs, embedded into jit_agg.cu's object
 JIT_HEADERS = [("vg_rtc_types.h", CSRC), ("vectra_abi.h", INCLUDE), ("vgpu_internal.h", CSRC),
                ("k_common.cuh", CSRC), ("k_groupby_dev.cuh", CSRC), ("k_jit_lib.cuh", CSRC),

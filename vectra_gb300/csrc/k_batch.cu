@@ -23,7 +23,7 @@
 #include <cstdio>
 #include <cstring>
 #include <vector>
-#include "k_groupby_dev.cuh"
+#include "k_set_dev.cuh"
 
 #include "vgpu.h"
 
@@ -31,24 +31,8 @@ namespace {
 
 constexpr int kSetThreads = 512;
 constexpr int64_t kChunk = 65536;
-constexpr uint64_t kEmpty = 0x8000000000000000ull;    // free slot marker; that key has its own slot
 
 int ck(cudaError_t e, const char *what) { return check(e, what); }
-
-// group table slot (array of structures: one group's state in two lines)
-struct GSlot {
-    unsigned long long key;
-    unsigned long long cnt;
-    int32_t base;             // digit window base, kBaseUnset until the first summand
-    uint32_t flags;           // bit2 NaN, bit3 +inf, bit4 -inf
-    long long win[kWin];      // digits of the exact sum (units of 2^-1074)
-    double fs, fc;            // compensated fallback for summands outside the window
-};
-
-struct JSlot {
-    unsigned long long key;
-    long long row;
-};
 
 struct Inst {                 // a query with its scratch
     VgpuSetQuery q;
@@ -76,8 +60,6 @@ struct Plan {
     cudaStream_t stream;
     int grid;
 };
-
-VG_DEV uint64_t bhash(uint64_t k) { return vg_mix64(k ^ 0x9E3779B97F4A7C15ull); }
 
 // ---------------------------------------------------------------------
 // phase 0: empty the tables
@@ -107,72 +89,6 @@ __global__ void __launch_bounds__(kSetThreads) set_init_kernel(const Inst *inst,
         }
         if (I.q.out_rows && threadIdx.x == 0) *I.q.out_rows = 0;
     }
-}
-
-// claims or finds key k's slot: index, or -1 when the table is full
-VG_DEV int64_t g_slot(GSlot *t, int64_t cap, uint64_t k) {
-    if (k == kEmpty) return cap;
-    const int64_t mask = cap - 1;
-    int64_t s = (int64_t)(bhash(k) & (uint64_t)mask);
-    for (int64_t p = 0; p < cap; p++) {
-        unsigned long long cur = *(volatile unsigned long long *)&t[s].key;
-        if (cur == k) return s;
-        if (cur == kEmpty) {
-            const unsigned long long prev = atomicCAS(&t[s].key, kEmpty, k);
-            if (prev == kEmpty || prev == k) return s;
-        }
-        s = (s + 1) & mask;
-    }
-    return -1;
-}
-
-// one double into slot g's exact sum
-VG_DEV void g_add(GSlot &g, uint64_t bits) {
-    const VgDigits d = vg_split_double(bits);
-    if (d.special) { atomicOr(&g.flags, d.special); return; }
-    if (d.lo < 0) return;
-    int b = *(volatile int *)&g.base;
-    if (b == kBaseUnset) {
-        int want = d.lo - 2;
-        if (want < 0) want = 0;
-        if (want > VG_LACC_WORDS - kWin) want = VG_LACC_WORDS - kWin;
-        const int prev = atomicCAS(&g.base, kBaseUnset, want);
-        b = (prev == kBaseUnset) ? want : prev;
-    }
-    const int rel = d.lo - b;
-    if (rel >= 0 && rel + (d.d2 ? 3 : 2) <= kWin) {
-        if (d.d0) atomicAdd((unsigned long long *)&g.win[rel], (unsigned long long)d.d0);
-        if (d.d1) atomicAdd((unsigned long long *)&g.win[rel + 1], (unsigned long long)d.d1);
-        if (d.d2) atomicAdd((unsigned long long *)&g.win[rel + 2], (unsigned long long)d.d2);
-    } else {
-        fallback_add(&g.fs, &g.fc, vg_bits_to_f64(bits));
-    }
-}
-
-// join slot of build key k (claimed); -1 when full
-VG_DEV int64_t j_insert(JSlot *t, int64_t cap, uint64_t k) {
-    if (k == kEmpty) return cap;
-    const int64_t mask = cap - 1;
-    int64_t s = (int64_t)(bhash(k) & (uint64_t)mask);
-    for (int64_t p = 0; p < cap; p++) {
-        const unsigned long long prev = atomicCAS(&t[s].key, kEmpty, k);
-        if (prev == kEmpty || prev == k) return s;
-        s = (s + 1) & mask;
-    }
-    return -1;
-}
-
-VG_DEV long long j_find(const JSlot *t, int64_t cap, uint64_t k) {
-    if (k == kEmpty) return __ldg(&t[cap].row);
-    const int64_t mask = cap - 1;
-    int64_t s = (int64_t)(bhash(k) & (uint64_t)mask);
-    for (int64_t p = 0; p < cap; p++) {
-        const unsigned long long cur = __ldg(&t[s].key);
-        if (cur == k) return __ldg(&t[s].row);
-        if (cur == kEmpty) return -1;
-        s = (s + 1) & mask;
-    }
-    return -1;
 }
 
 // ---------------------------------------------------------------------
@@ -211,26 +127,6 @@ __global__ void __launch_bounds__(kSetThreads) set_phase1_kernel(const Inst *ins
             }
         }
     }
-}
-
-// exact sum of a group slot, rounded once
-VG_DEV double g_sum(const GSlot &g) {
-    int64_t w[VG_LACC_WORDS];
-    for (int i = 0; i < VG_LACC_WORDS; i++) w[i] = 0;
-    if (g.base != kBaseUnset)
-        for (int i = 0; i < kWin; i++) w[g.base + i] += g.win[i];
-    uint32_t special = g.flags & (4u | 8u | 16u);
-    const double fb[2] = {g.fs, g.fc};
-    for (int j = 0; j < 2; j++) {
-        const VgDigits d = vg_split_double(vg_f64_to_bits(fb[j]));
-        special |= d.special;
-        if (d.lo >= 0) {
-            w[d.lo] += d.d0;
-            w[d.lo + 1] += d.d1;
-            if (d.lo + 2 < VG_LACC_WORDS) w[d.lo + 2] += d.d2;
-        }
-    }
-    return vg_digits_to_double(w, VG_LACC_WORDS, special);
 }
 
 // ---------------------------------------------------------------------

@@ -287,3 +287,122 @@ def check_query_set(torch, qs, outs, out_rows, idx):
             m = int(nrow[i])
             assert m == len(prow), (i, m, len(prow))
             assert bool((o["probe"][:m] == prow).all()) and bool((o["build"][:m] == brow).all()), i
+
+
+# --------------------------------------------------------------------------
+# serving: resident tables, a stream of filter / group / semi-anti requests
+# --------------------------------------------------------------------------
+
+SERVE_FILTER_SUM, SERVE_GROUP_SUM, SERVE_SEMI, SERVE_ANTI = 0, 1, 2, 3
+
+
+class ServeQuery(C.Structure):
+    """Mirror of VgpuServeQuery (include/vgpu.h)."""
+    _fields_ = [("kind", C.c_int32), ("table", C.c_int32), ("build_table", C.c_int32), ("pad", C.c_int32),
+                ("threshold", C.c_double)]
+
+
+class ServeResult(C.Structure):
+    """Mirror of VgpuServeResult (include/vgpu.h)."""
+    _fields_ = [("rows", C.c_int64), ("sum", C.c_double), ("key", C.c_void_p), ("key_valid", C.c_void_p),
+                ("group_sum", C.c_void_p), ("group_n", C.c_void_p), ("sel", C.c_void_p)]
+
+
+def bind_server(lib):
+    lib.vgpu_server_create.restype = C.c_void_p
+    lib.vgpu_server_create.argtypes = [C.c_int, C.c_int64]
+    lib.vgpu_server_add_table.restype = C.c_int
+    lib.vgpu_server_add_table.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+    lib.vgpu_server_submit.restype = C.c_int64
+    lib.vgpu_server_submit.argtypes = [C.c_void_p, C.POINTER(ServeQuery)]
+    lib.vgpu_server_poll.restype = C.c_int
+    lib.vgpu_server_poll.argtypes = [C.c_void_p]
+    lib.vgpu_server_done.restype = C.c_int
+    lib.vgpu_server_done.argtypes = [C.c_void_p, C.c_int64]
+    lib.vgpu_server_result.restype = C.c_int
+    lib.vgpu_server_result.argtypes = [C.c_void_p, C.c_int64, C.POINTER(ServeResult)]
+    lib.vgpu_server_release.argtypes = [C.c_void_p, C.c_int64]
+    lib.vgpu_server_free.argtypes = [C.c_void_p]
+    lib.vgpu_server_warm.restype = C.c_int
+    lib.vgpu_server_warm.argtypes = [C.c_void_p, C.c_int]
+    lib.vgpu_copy_to_host.restype = C.c_int
+    lib.vgpu_copy_to_host.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
+    return lib
+
+
+def gen_serve_tables(torch, sizes, seed, device, ids=10_000_000, zipf_s=1.0, na=0.03):
+    """Tables of the given row counts: key int64 Zipf(s) over 1..ids, val f64
+    LogNormal(0, 1), each with `na` NA in both columns (validity masks)."""
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    ranks = torch.arange(1, ids + 1, device=device, dtype=torch.float64)
+    cdf = torch.cumsum(ranks.pow(-zipf_s), 0)
+    cdf /= cdf[-1].clone()
+    tables = []
+    for n in sizes:
+        key = torch.searchsorted(cdf, torch.rand(n, dtype=torch.float64, device=device, generator=g)) + 1
+        key = key.clamp_(max=ids).to(torch.int64)
+        kv = torch.rand(n, device=device, generator=g) >= na
+        val = torch.randn(n, dtype=torch.float64, device=device, generator=g).exp_()
+        vv = torch.rand(n, device=device, generator=g) >= na
+        key[~kv] = 0
+        val[~vv] = 0.0
+        tables.append({"key": key, "kv": kv, "val": val, "vv": vv, "kbits": _validity(torch, kv),
+                       "vbits": _validity(torch, vv)})
+    return tables
+
+
+def server_with_tables(lib, tables, n_streams=4, budget=120 << 30):
+    srv = lib.vgpu_server_create(n_streams, budget)
+    if not srv:
+        raise RuntimeError(lib.vgpu_last_error().decode())
+    for t in tables:
+        r = lib.vgpu_server_add_table(srv, t["key"].data_ptr(), t["kbits"].data_ptr(), t["val"].data_ptr(),
+                                      t["vbits"].data_ptr(), t["key"].numel())
+        if r < 0:
+            raise RuntimeError(lib.vgpu_last_error().decode())
+    return srv
+
+
+def gen_requests(n, n_tables, seed):
+    """Equal thirds of filter (val > t, t ~ LogNormal quantiles), group-by
+    and semi / anti joins of table i against table j."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        q = ServeQuery()
+        third = rng.integers(0, 3)
+        q.table = int(rng.integers(0, n_tables))
+        if third == 0:
+            q.kind = SERVE_FILTER_SUM
+            q.threshold = float(np.exp(rng.normal(0, 1)))
+        elif third == 1:
+            q.kind = SERVE_GROUP_SUM
+        else:
+            q.kind = SERVE_SEMI if rng.integers(0, 2) == 0 else SERVE_ANTI
+            q.build_table = int(rng.integers(0, n_tables))
+        out.append(q)
+    return out
+
+
+def fetch_result(lib, srv, rid, kind):
+    """A finished request's result on the host (group rows sorted by key,
+    the NA group last)."""
+    r = ServeResult()
+    if lib.vgpu_server_result(srv, rid, C.byref(r)) != 0:
+        raise RuntimeError(lib.vgpu_last_error().decode())
+    if kind == SERVE_FILTER_SUM:
+        return (r.rows, r.sum)
+    n = r.rows
+
+    def col(ptr, dt):
+        a = np.empty(max(1, n), dt)
+        if n and lib.vgpu_copy_to_host(a.ctypes.data, ptr, n * a.itemsize) != 0:
+            raise RuntimeError(lib.vgpu_last_error().decode())
+        return a[:n]
+    if kind == SERVE_GROUP_SUM:
+        keys, kval = col(r.key, np.int64), col(r.key_valid, np.uint8)
+        sums, cnt = col(r.group_sum, np.float64), col(r.group_n, np.int64)
+        order = np.lexsort((keys, kval == 0))
+        return (keys[order], kval[order], sums[order], cnt[order])
+    return col(r.sel, np.int32)
