@@ -613,9 +613,14 @@ def serve_arm(args):
         lib.vgpu_server_free(srv)
         return dt
 
-    # warm-up: builds every table's key set once (they stay resident in a server)
+    def note(msg):
+        sys.stderr.write("serve: %s\n" % msg)
+        sys.stderr.flush()
+    t_start = time.perf_counter()
     saturate(4, reqs[: min(64, n_req)])
+    note("warm-up done at %.1f s" % (time.perf_counter() - t_start))
     sat_s = saturate(4, reqs)
+    note("saturated: %d requests in %.2f s" % (n_req, sat_s))
     # the plain path: one request at a time
     rng = np.random.default_rng(1)
     sample = [reqs[i] for i in rng.choice(n_req, size=min(256, n_req), replace=False)]
@@ -633,6 +638,7 @@ def serve_arm(args):
         lib.vgpu_server_release(srv, rid)
     plain_s = (time.perf_counter() - t0) / len(sample)
     lib.vgpu_server_free(srv)
+    note("plain path: %.2f ms per request" % (plain_s * 1e3))
     # open loop: Poisson arrivals at `rate`
     arrivals = np.cumsum(np.random.default_rng(2).exponential(1.0 / rate, n_req))
     srv = warmed(4)
