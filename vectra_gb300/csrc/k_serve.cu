@@ -29,6 +29,8 @@
 
 #include "vgpu.h"
 
+extern "C" int vgk_col_minmax_i64(const VgCol *col, int64_t n, int64_t *d_out, int64_t *h_out, vg_stream_t s);
+
 namespace {
 
 constexpr int kSrvThreads = 512;
@@ -41,8 +43,10 @@ struct Table {
     const long long *val;
     const uint32_t *val_valid;
     int64_t n;
-    JSlot *keyset;                 // distinct valid keys, built on first use as a build side
+    JSlot *keyset;                 // distinct valid keys, built on first use as a build side ...
     int64_t keyset_cap;
+    uint32_t *kbits;               // ... or, for keys within a range of at most 2^30, one bit per key
+    int64_t kmin, krange;
     int64_t distinct;              // distinct valid keys (after the key set is built), else -1
 };
 
@@ -74,7 +78,13 @@ struct WItem {
 
 VG_DEV bool bit(const uint32_t *v, int64_t r) { return v == nullptr || ((__ldg(v + (r >> 5)) >> (r & 31)) & 1u); }
 
-VG_DEV bool keyset_has(const JSlot *t, int64_t cap, uint64_t k) { return j_find(t, cap, k) >= 0; }
+VG_DEV bool keyset_has(const Table &B, uint64_t k) {
+    if (B.kbits) {
+        const uint64_t d = k - (uint64_t)B.kmin;
+        return d < (uint64_t)B.krange && ((__ldg(B.kbits + (d >> 5)) >> (d & 31)) & 1u);
+    }
+    return j_find(B.keyset, B.keyset_cap, k) >= 0;
+}
 
 // ---------------------------------------------------------------------
 // wave kernels
@@ -113,6 +123,7 @@ __global__ void __launch_bounds__(kSrvThreads) srv_init_kernel(const Req *req, i
 // phase 1: filter sums, group aggregation, semi / anti match counts
 __global__ void __launch_bounds__(kSrvThreads) srv_phase1_kernel(const Req *req, const WItem *items, int n_items,
                                                                  long long *chunk_cnt, uint32_t *ctr) {
+    extern __shared__ __align__(16) char dsm[];
     __shared__ int item;
     __shared__ unsigned long long s_cnt;
     for (;;) {
@@ -134,17 +145,38 @@ __global__ void __launch_bounds__(kSrvThreads) srv_phase1_kernel(const Req *req,
                 g_add(*R.acc, b);
             }
         } else if (R.kind == VGPU_SERVE_GROUP_SUM) {
+            // hot keys aggregate in the CTA's cache, the rest go straight to
+            // the request's table; the cache is merged at the end of the item
+            GCache &gc = *(GCache *)dsm;
+            gc_reset(gc);
+            __syncthreads();
             for (int64_t r = W.lo + threadIdx.x; r < W.hi; r += blockDim.x) {
-                const int64_t s = bit(T.key_valid, r) ? g_slot(R.gt, R.cap, (uint64_t)__ldg(T.key + r)) : R.cap + 1;
+                const bool kv = bit(T.key_valid, r);
+                const uint64_t k = kv ? (uint64_t)__ldg(T.key + r) : 0;
+                const bool vv = bit(T.val_valid, r);
+                const uint64_t v = vv ? (uint64_t)__ldg(T.val + r) : 0;
+                const int cs = kv ? gc_find(gc, k) : -1;
+                if (cs >= 0) {
+                    atomicAdd(&gc.cnt[cs], 1u);
+                    if (!vv || gc_sum(gc, cs, v)) continue;
+                }
+                const int64_t s = kv ? g_slot(R.gt, R.cap, k) : R.cap + 1;
                 if (s < 0) { atomicOr(ctr + 4, VG_ERR_FULL); continue; }
-                atomicAdd(&R.gt[s].cnt, 1ull);
-                if (bit(T.val_valid, r)) g_add(R.gt[s], (uint64_t)__ldg(T.val + r));
+                if (cs < 0) atomicAdd(&R.gt[s].cnt, 1ull);
+                if (vv) g_add(R.gt[s], v);
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < kGC; i += blockDim.x) {
+                if (gc.state[i] != 2u) continue;
+                const int64_t s = g_slot(R.gt, R.cap, gc.key[i]);
+                if (s < 0) { atomicOr(ctr + 4, VG_ERR_FULL); continue; }
+                gc_merge(gc, i, R.gt[s]);
             }
         } else {
             const bool semi = R.kind == VGPU_SERVE_SEMI;
             for (int64_t r = W.lo + threadIdx.x; r < W.hi; r += blockDim.x) {
                 const bool m = bit(T.key_valid, r) &&
-                               keyset_has(R.build.keyset, R.build.keyset_cap, (uint64_t)__ldg(T.key + r));
+                               keyset_has(R.build, (uint64_t)__ldg(T.key + r));
                 if (m == semi) c++;
             }
         }
@@ -204,7 +236,7 @@ __global__ void __launch_bounds__(kSrvThreads) srv_phase2_kernel(const Req *req,
                 bool keep = false;
                 if (r < W.hi) {
                     const bool m = bit(T.key_valid, r) &&
-                                   keyset_has(R.build.keyset, R.build.keyset_cap, (uint64_t)__ldg(T.key + r));
+                                   keyset_has(R.build, (uint64_t)__ldg(T.key + r));
                     keep = m == semi;
                 }
                 const unsigned bm = __ballot_sync(0xFFFFFFFFu, keep);
@@ -234,6 +266,23 @@ __global__ void srv_keyset_kernel(Table T, uint32_t *err) {
         if (s < 0) { atomicOr(err, VG_ERR_FULL); continue; }
         T.keyset[s].row = 1;                       // present (the marker key's slot included)
     }
+}
+
+__global__ void srv_keybits_kernel(Table T) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < T.n; r += stride) {
+        if (!bit(T.key_valid, r)) continue;
+        const uint64_t d = (uint64_t)__ldg(T.key + r) - (uint64_t)T.kmin;
+        if (d < (uint64_t)T.krange) atomicOr(T.kbits + (d >> 5), 1u << (d & 31));
+    }
+}
+
+__global__ void srv_keybits_count_kernel(const uint32_t *w, int64_t n_words, unsigned long long *n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    unsigned long long c = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_words; i += stride) c += __popc(w[i]);
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(n, c);
 }
 
 __global__ void srv_keyset_count_kernel(const JSlot *t, int64_t cap, unsigned long long *n) {
@@ -300,7 +349,40 @@ int64_t pow2_ge(int64_t x) {
 }
 
 int ensure_keyset(Server *S, Table &T) {
-    if (T.keyset) return 0;
+    if (T.keyset || T.kbits) return 0;
+    cudaStream_t bst = S->build_stream;
+    // dense key ranges: a bitmap (fits L2 for ranges up to ~10^9 bits)
+    if (T.n > 0) {
+        VgCol kc;
+        memset(&kc, 0, sizeof(kc));
+        kc.type = VEC_INT64;
+        kc.data = T.key;
+        kc.valid = T.key_valid;
+        int64_t mm[3];
+        if (vgk_col_minmax_i64(&kc, T.n, (int64_t *)(S->d_err + 8), mm, (vg_stream_t)bst) != 0)
+            return srv_fail(S, "server: %s", "key range failed");
+        const uint64_t span = (uint64_t)mm[1] - (uint64_t)mm[0];
+        if (mm[2] > 0 && span < ((uint64_t)1 << 30)) {
+            T.kmin = mm[0];
+            T.krange = (int64_t)span + 1;
+            const int64_t words = (T.krange + 31) / 32;
+            if (cudaMalloc(&T.kbits, (size_t)words * 4) != cudaSuccess)
+                return srv_fail(S, "server: %s", "no device memory for a key bitmap");
+            S->used += words * 4;
+            cudaMemsetAsync(T.kbits, 0, (size_t)words * 4, bst);
+            cudaMemsetAsync(S->d_err, 0, 16, bst);
+            srv_keybits_kernel<<<S->grid, 256, 0, bst>>>(T);
+            srv_keybits_count_kernel<<<S->grid, 256, 0, bst>>>(T.kbits, words, (unsigned long long *)(S->d_err + 2));
+            vg_launch_counter += 2;
+            uint32_t e[4] = {0, 0, 0, 0};
+            cudaMemcpyAsync(e, S->d_err, 16, cudaMemcpyDeviceToHost, bst);
+            if (cudaStreamSynchronize(bst) != cudaSuccess) return srv_fail(S, "server: %s", "key bitmap build failed");
+            unsigned long long d = 0;
+            memcpy(&d, e + 2, 8);
+            T.distinct = (int64_t)d;
+            return 0;
+        }
+    }
     T.keyset_cap = pow2_ge(2 * (T.n > 0 ? T.n : 1));
     if (cudaMalloc(&T.keyset, (size_t)(T.keyset_cap + 1) * sizeof(JSlot)) != cudaSuccess)
         return srv_fail(S, "server: %s", "no device memory for a join key set");
@@ -451,7 +533,7 @@ int launch(Server *S) {
         if (!it2.empty()) cudaMemcpyAsync(d_it2, it2.data(), sizeof(WItem) * it2.size(), cudaMemcpyHostToDevice, st);
         cudaMemsetAsync(d_ctr, 0, 32, st);
         srv_init_kernel<<<S->grid, kSrvThreads, 0, st>>>(d_req, (int)n);
-        srv_phase1_kernel<<<S->grid, kSrvThreads, 0, st>>>(d_req, d_it1, (int)it1.size(), d_cc, d_ctr);
+        srv_phase1_kernel<<<S->grid, kSrvThreads, sizeof(GCache), st>>>(d_req, d_it1, (int)it1.size(), d_cc, d_ctr);
         srv_phase2_kernel<<<S->grid, kSrvThreads, 0, st>>>(d_req, d_it2, (int)it2.size(), d_cc, d_ctr);
         vg_launch_counter += 3;
         // the small results (and the wave's error word) back to pinned host memory
@@ -485,7 +567,8 @@ void *vgpu_server_create(int n_streams, int64_t budget_bytes) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    S->grid = sms > 0 ? sms * (2048 / kSrvThreads) : 64;
+    S->grid = sms > 0 ? sms * 2 : 64;             // two CTAs per SM: two group caches fit
+    cudaFuncSetAttribute(srv_phase1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GCache));
     S->waves.resize((size_t)n_streams);
     for (auto &W : S->waves) {
         if (cudaStreamCreateWithFlags(&W.stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -618,8 +701,10 @@ void vgpu_server_free(void *srv) {
     }
     for (auto &kv : S->reqs)
         if (kv.second.mem) cudaFree(kv.second.mem);
-    for (auto &T : S->tables)
+    for (auto &T : S->tables) {
         if (T.keyset) cudaFree(T.keyset);
+        if (T.kbits) cudaFree(T.kbits);
+    }
     if (S->build_stream) cudaStreamDestroy(S->build_stream);
     if (S->d_err) cudaFree(S->d_err);
     delete S;

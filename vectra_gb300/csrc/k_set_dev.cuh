@@ -113,3 +113,124 @@ VG_DEV double g_sum(const GSlot &g) {
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------
+// per-CTA shared-memory group cache for one work item: hot keys aggregate
+// here (32-bit shared atomics) and reach their instance's table once per
+// item instead of once per row
+// ---------------------------------------------------------------------
+namespace {
+
+constexpr int kGC = 1024;                       // cache slots (power of two)
+
+struct GCache {
+    unsigned long long key[kGC];
+    uint32_t state[kGC];                         // 0 empty, 1 being claimed, 2 ready
+    uint32_t cnt[kGC];
+    int32_t base[kGC];
+    uint32_t flags[kGC];
+    uint32_t wlo[kWin][kGC];
+    int32_t whi[kWin][kGC];
+    int used;
+};
+
+VG_DEV void gc_reset(GCache &c) {
+    for (int i = threadIdx.x; i < kGC; i += blockDim.x) {
+        c.state[i] = 0;
+        c.cnt[i] = 0;
+        c.base[i] = kBaseUnset;
+        c.flags[i] = 0;
+#pragma unroll
+        for (int w = 0; w < kWin; w++) { c.wlo[w][i] = 0; c.whi[w][i] = 0; }
+    }
+    if (threadIdx.x == 0) c.used = 0;
+}
+
+// cache slot of key k, claimed if new and the cache is under 3/4 full; -1
+// when the key is not cached
+VG_DEV int gc_find(GCache &c, uint64_t k) {
+    int s = (int)(bhash(k) & (uint64_t)(kGC - 1));
+    const bool may_insert = *(volatile int *)&c.used < (kGC * 3) / 4;
+    for (int p = 0; p < 8; p++) {
+        uint32_t st = *(volatile uint32_t *)&c.state[s];
+        if (st == 0) {
+            if (!may_insert) return -1;
+            const uint32_t prev = atomicCAS(&c.state[s], 0u, 1u);
+            if (prev == 0u) {
+                c.key[s] = k;
+                __threadfence_block();
+                atomicExch(&c.state[s], 2u);
+                atomicAdd(&c.used, 1);
+                return s;
+            }
+            st = prev;
+        }
+        int spins = 0;
+        while (st == 1u) {
+            if (++spins > VG_SPIN_LIMIT) return -1;
+            st = *(volatile uint32_t *)&c.state[s];
+        }
+        __threadfence_block();
+        if (*(volatile unsigned long long *)&c.key[s] == k) return s;
+        s = (s + 1) & (kGC - 1);
+    }
+    return -1;
+}
+
+// a double into cache slot s's digit window; false: outside the window
+VG_DEV bool gc_sum(GCache &c, int s, uint64_t bits) {
+    const VgDigits32 d = vg_split_double32(bits);
+    if (d.special) { atomicOr(&c.flags[s], d.special); return true; }
+    if (d.zero) return true;
+    int b = *(volatile int *)&c.base[s];
+    if (b == kBaseUnset) {
+        int want = d.word - 2;
+        if (want < 0) want = 0;
+        if (want > VG_LACC_WORDS - kWin) want = VG_LACC_WORDS - kWin;
+        const int prev = atomicCAS(&c.base[s], kBaseUnset, want);
+        b = (prev == kBaseUnset) ? want : prev;
+    }
+    const int rel = d.word - b;
+    if (rel < 0 || rel + (d.d2 ? 3 : 2) > kWin) return false;
+    const uint32_t dd[3] = {d.d0, d.d1, d.d2};
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        if (!dd[i]) continue;
+        const uint32_t a = d.neg ? 0u - dd[i] : dd[i];
+        const uint32_t o = atomicAdd(&c.wlo[rel + i][s], a);
+        const bool carry = d.neg ? (o < dd[i]) : (o + a < o);
+        if (carry) atomicAdd(&c.whi[rel + i][s], d.neg ? -1 : 1);
+    }
+    return true;
+}
+
+// cache slot s into global slot g (count, flags, digits)
+VG_DEV void gc_merge(const GCache &c, int s, GSlot &g) {
+    if (c.cnt[s]) atomicAdd(&g.cnt, (unsigned long long)c.cnt[s]);
+    if (c.flags[s]) atomicOr(&g.flags, c.flags[s]);
+    const int bs = c.base[s];
+    if (bs == kBaseUnset) return;
+    int bg = *(volatile int *)&g.base;
+    if (bg == kBaseUnset) {
+        const int prev = atomicCAS(&g.base, kBaseUnset, bs);
+        bg = (prev == kBaseUnset) ? bs : prev;
+    }
+    for (int w = 0; w < kWin; w++) {
+        const int64_t v = (int64_t)(((uint64_t)(int64_t)c.whi[w][s] << 32) + (uint64_t)c.wlo[w][s]);
+        if (!v) continue;
+        const int rel = bs + w - bg;
+        if (rel >= 0 && rel < kWin) {
+            atomicAdd((unsigned long long *)&g.win[rel], (unsigned long long)v);
+        } else {
+            // outside the table's window: two exactly representable halves
+            // through the compensated fallback
+            const int e = 32 * (bs + w) - 1074;
+            const double hi = ldexp((double)(v >> 32), e + 32);
+            const double lo = ldexp((double)(v & 0xFFFFFFFFll), e);
+            if (hi != 0.0) fallback_add(&g.fs, &g.fc, hi);
+            if (lo != 0.0) fallback_add(&g.fs, &g.fc, lo);
+        }
+    }
+}
+
+}  // namespace
