@@ -604,12 +604,17 @@ def serve_arm(args):
     def saturate(n_streams, reqs):
         srv = warmed(n_streams)
         t0 = time.perf_counter()
-        ids = [lib.vgpu_server_submit(srv, q) for q in reqs]
-        while lib.vgpu_server_poll(srv) > 0:
-            pass
+        pending = set(lib.vgpu_server_submit(srv, q) for q in reqs)
+        deadline = time.perf_counter() + 300
+        while pending:                      # results released as they complete
+            if time.perf_counter() > deadline:
+                raise RuntimeError("serve: saturated run did not finish in 300 s")
+            if lib.vgpu_server_poll(srv) < 0:
+                raise RuntimeError(lib.vgpu_last_error().decode())
+            for rid in [r for r in pending if lib.vgpu_server_done(srv, r)]:
+                lib.vgpu_server_release(srv, rid)
+                pending.discard(rid)
         dt = time.perf_counter() - t0
-        for i in ids:
-            lib.vgpu_server_release(srv, i)
         lib.vgpu_server_free(srv)
         return dt
 
@@ -646,12 +651,16 @@ def serve_arm(args):
     pending = {}
     k = 0
     t0 = time.perf_counter()
+    deadline = time.perf_counter() + 300
     while k < n_req or pending:
+        if time.perf_counter() > deadline:
+            raise RuntimeError("serve: open loop did not finish in 300 s")
         now = time.perf_counter() - t0
         while k < n_req and arrivals[k] <= now:
             pending[lib.vgpu_server_submit(srv, reqs[k])] = k
             k += 1
-        lib.vgpu_server_poll(srv)
+        if lib.vgpu_server_poll(srv) < 0:
+            raise RuntimeError(lib.vgpu_last_error().decode())
         now = time.perf_counter() - t0
         for rid in [r for r in pending if lib.vgpu_server_done(srv, r)]:
             lat[pending.pop(rid)] = now            # completion time

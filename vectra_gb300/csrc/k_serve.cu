@@ -307,7 +307,9 @@ __global__ void srv_keyset_init_kernel(JSlot *t, int64_t cap) {
 struct Request {
     VgpuServeQuery q;
     int64_t id;
-    int64_t bytes;                 // admission estimate
+    int64_t bytes;                 // admission estimate (scratch + outputs)
+    int64_t scratch_bytes;         // the part returned when the request finishes
+    void *scratch;                 // group table (freed when the request finishes)
     int state;                     // 0 queued, 1 admitted, 2 running, 3 done
     void *mem;                     // outputs + scratch (device)
     Req dev;                       // kernel view (pointers into mem)
@@ -403,6 +405,13 @@ int ensure_keyset(Server *S, Table &T) {
 }
 
 // bytes a request holds while admitted (outputs and scratch)
+// group table bytes of a request (scratch, released when it finishes)
+int64_t scratch_estimate(Server *S, const VgpuServeQuery &q) {
+    if (q.kind != VGPU_SERVE_GROUP_SUM) return 0;
+    const Table &T = S->tables[(size_t)q.table];
+    return (pow2_ge(2 * (T.distinct + 1)) + 2) * (int64_t)sizeof(GSlot);
+}
+
 int64_t estimate(Server *S, const VgpuServeQuery &q) {
     const Table &T = S->tables[(size_t)q.table];
     switch (q.kind) {
@@ -427,6 +436,12 @@ int retire(Server *S) {
             R.h_kept = h[3 * i + 1];
             memcpy(&R.h_sum, &h[3 * i + 2], 8);
             R.state = 3;
+            if (R.scratch) {                    // the group table is no longer needed
+                cudaFreeAsync(R.scratch, W.stream);
+                R.scratch = nullptr;
+                S->used -= R.scratch_bytes;
+                R.bytes -= R.scratch_bytes;
+            }
         }
         cudaFreeAsync(W.meta, W.stream);
         W.meta = nullptr;
@@ -437,9 +452,15 @@ int retire(Server *S) {
 }
 
 void admit(Server *S) {
+    bool busy = !S->ready.empty();
+    for (auto &W : S->waves) busy = busy || W.busy;
     while (!S->queue.empty()) {
         Request &R = S->reqs[S->queue.front()];
-        if (S->used + R.bytes > S->budget && S->used > 0) break;   // a lone request always fits
+        // over the budget: wait for running work to return memory; with
+        // nothing running, admit anyway (results the client still holds must
+        // not stall the queue forever)
+        if (S->used + R.bytes > S->budget && busy) break;
+        busy = true;
         S->used += R.bytes;
         R.state = 1;
         S->ready.push_back(R.id);
@@ -470,7 +491,10 @@ int launch(Server *S) {
             if (D.kind == VGPU_SERVE_GROUP_SUM) {
                 D.cap = pow2_ge(2 * (T.distinct + 1));
                 D.max_groups = T.distinct + 1;
-                bytes += (size_t)(D.cap + 2) * sizeof(GSlot) + (size_t)D.max_groups * 25 + 1024;
+                bytes += (size_t)D.max_groups * 25 + 1024;
+                if (cudaMallocAsync(&R.scratch, (size_t)(D.cap + 2) * sizeof(GSlot), W->stream) != cudaSuccess)
+                    return srv_fail(S, "server: %s", "device allocation failed");
+                D.gt = (GSlot *)R.scratch;
             } else if (D.kind == VGPU_SERVE_FILTER_SUM) {
                 bytes += sizeof(GSlot) + 256;
             } else {
@@ -486,7 +510,6 @@ int launch(Server *S) {
             D.out_sum = (double *)(m + 16);
             char *p = m + 512;
             if (D.kind == VGPU_SERVE_GROUP_SUM) {
-                D.gt = (GSlot *)p; p += (D.cap + 2) * sizeof(GSlot);
                 D.out_sum = (double *)p; p += D.max_groups * 8;
                 D.out_key = (long long *)p; p += D.max_groups * 8;
                 D.out_n = (long long *)p; p += D.max_groups * 8;
@@ -625,6 +648,8 @@ int64_t vgpu_server_submit(void *srv, const VgpuServeQuery *q) {
     R.q = *q;
     R.id = S->next_id++;
     R.bytes = estimate(S, *q);
+    R.scratch_bytes = scratch_estimate(S, *q);
+    R.scratch = nullptr;
     R.state = 0;
     R.mem = nullptr;
     S->reqs[R.id] = R;
@@ -701,6 +726,8 @@ void vgpu_server_free(void *srv) {
     }
     for (auto &kv : S->reqs)
         if (kv.second.mem) cudaFree(kv.second.mem);
+    for (auto &kv : S->reqs)
+        if (kv.second.scratch) cudaFree(kv.second.scratch);
     for (auto &T : S->tables) {
         if (T.keyset) cudaFree(T.keyset);
         if (T.kbits) cudaFree(T.kbits);
