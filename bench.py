@@ -204,12 +204,12 @@ def measured_peak():
 
 
 def profile_traffic():
-    """DRAM bytes per launch of the fused kernel from the committed ncu
-    summary (a `traffic_bytes_per_launch:` line), if present."""
+    """DRAM bytes of the fused kernel per query from the committed ncu
+    summary (a `traffic_bytes_per_step:` line), if present."""
     p = os.path.join(ROOT, "profiles", "agg_probe_c2_fused.md")
     try:
         for line in open(p):
-            if line.strip().startswith("traffic_bytes_per_launch:"):
+            if line.strip().startswith("traffic_bytes_per_step:"):
                 return float(line.split(":", 1)[1].strip().split()[0])
     except OSError:
         pass
@@ -281,7 +281,8 @@ def gpu_arm(args, rank, world):
     build_ms = lib.vgpu_profile_ms(2, C.byref(build_n))
 
     if args.no_e2e:
-        line = {"metric": METRIC, "ms_per_step": ms_step, "kernel_ms": agg_ms / agg_launches,
+        line = {"metric": METRIC, "ms_per_step": ms_step, "kernel_ms": agg_ms / args.steps,
+                "kernel_launches_per_step": agg_launches / args.steps,
                 "join_build_ms": build_ms / max(1, build_n.value), "scale": args.scale, "gpu_launches": launches}
         return line
     # e2e: page-locked host copies of the same columns
@@ -314,7 +315,9 @@ def gpu_arm(args, rank, world):
     h2d = sum(v.numel() * v.element_size() + m.numel() for v, m in list(hf.values()) + list(hd.values()))
     d2h = 3 * 8 * N_CAT
     peak, peak_kind = measured_peak()
-    kernel_ms = agg_ms / agg_launches
+    # the fused kernel's time per query (a batch runs as one or more
+    # launches: 2^24 rows while the group table may still grow, then the rest)
+    kernel_ms = agg_ms / args.steps
     # the fused kernel reads the fact columns and two of the three dim columns
     # (the join build reads the third, id)
     kernel_b = fact_b + dim_b * 2 // 3
@@ -330,8 +333,9 @@ def gpu_arm(args, rank, world):
         "hbm_gbs_whole_query": (fact_b + dim_b + out_b) / (ms_step * 1e-3) / 1e9,
         "roofline": {"bound": "hbm", "kernel": "fused left-join probe + project + group-agg (agg_fast_kernel)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "algorithmic_bytes_per_launch": kernel_b,
-                     "kernel_ms": kernel_ms, "traffic": profile_traffic()},
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_step": kernel_b,
+                     "kernel_ms_per_step": kernel_ms, "kernel_launches_per_step": agg_launches / args.steps,
+                     "traffic": profile_traffic()},
         "join_build_ms": build_ms / max(1, build_n.value),
         "e2e": {"value": rows * world / (e2e_ms * 1e-3), "unit": "rows/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
