@@ -331,7 +331,7 @@ def gpu_arm(args, rank, world):
                    "inputs": "device-resident, larger than L2 (1.87 GB)", "parallelism": "replicas",
                    "output_order": "ascending category (temp_dir given, as from R)"},
         "hbm_gbs_whole_query": (fact_b + dim_b + out_b) / (ms_step * 1e-3) / 1e9,
-        "roofline": {"bound": "hbm", "kernel": "fused left-join probe + project + group-agg (agg_fast_kernel)",
+        "roofline": {"bound": "hbm", "kernel": "fused left-join probe + project + group-agg (vg_jit_agg, run-time specialised)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "algorithmic_bytes_per_step": kernel_b,
                      "kernel_ms_per_step": kernel_ms, "kernel_launches_per_step": agg_launches / args.steps,
