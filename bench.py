@@ -463,8 +463,8 @@ def workload_arm(args):
     if args.workload == "filter_group":
         n = 10_000_000 // args.scale
         cols = W.gen_filter_group(torch, n, 0, dev)
-        run = lambda: W.run_filter_group(eng, W.device_source(lib, cols, n)[0])
-        out = run()
+        run = lambda numpy=False: W.run_filter_group(eng, W.device_source(lib, cols, n)[0], numpy=numpy)
+        out = run(True)
         kept = W.check_filter_group(torch, out, cols)
         algo = W.filter_group_bytes(n)
         desc = {"workload": "filter(temperature > 30, year >= 2020) |> group_by(station) |> "
@@ -473,17 +473,20 @@ def workload_arm(args):
     else:
         n, distinct = 200_000_000 // args.scale, 50_000_000 // args.scale
         cols, raw = W.gen_high_card(torch, n, distinct, 0, dev)
-        run = lambda: W.run_high_card(eng, W.device_source(lib, cols, n)[0])
-        out = run()
+        run = lambda numpy=False: W.run_high_card(eng, W.device_source(lib, cols, n)[0], numpy=numpy)
+        out = run(True)
         groups = W.check_high_card(torch, out, cols, raw, distinct)
         del raw
         algo = W.high_card_bytes(n, groups)
         desc = {"workload": "group_by(key) |> summarise(sum(x), mean(x), min(y), max(y), n()) over 200M rows, "
                             "50M distinct int64 keys, 5% NA", "rows": n, "groups": groups + 1}
     torch.cuda.synchronize()
+    lib.vgpu_pagg_runs.restype = C.c_ulonglong
+    pagg_before = lib.vgpu_pagg_runs()
     for _ in range(args.warmup):
         run()
     torch.cuda.synchronize()
+    pagg_runs = lib.vgpu_pagg_runs() - pagg_before
     lib.vgpu_profile_reset()
     lib.vgpu_profile_enable(1)
     stream = torch.cuda.current_stream(dev)
@@ -497,6 +500,10 @@ def workload_arm(args):
     ms = e0.elapsed_time(e1) / args.steps
     nl = C.c_ulonglong(0)
     agg_ms = lib.vgpu_profile_ms(0, C.byref(nl))
+    n5 = C.c_ulonglong(0)
+    reduce_ms = lib.vgpu_profile_ms(5, C.byref(n5))
+    n4 = C.c_ulonglong(0)
+    finish_ms = lib.vgpu_profile_ms(4, C.byref(n4))
     peak, peak_kind = measured_peak()
     return {"metric": "rows/s (input rows per second, whole query)", "value": n / (ms * 1e-3), "unit": "rows/s",
             "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
@@ -504,7 +511,10 @@ def workload_arm(args):
             "algorithmic_bytes": algo, "hbm_gbs_whole_query": algo / (ms * 1e-3) / 1e9,
             "frac_of_hbm_peak": algo / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
             "agg_kernel_ms": agg_ms / max(1, args.steps * 1), "agg_launches": nl.value,
-            "result_checked": True}
+            "partitioned_path": bool(pagg_runs), "reduce_kernel_ms": reduce_ms / max(1, args.steps),
+            "finish_kernel_ms": finish_ms / max(1, args.steps), "result_checked": True,
+            "timed": "the node C API producing the host result batch (malloc-owned columns), without "
+                     "conversion to numpy"}
 
 
 def query_set_arm(args, eng, lib, dev):

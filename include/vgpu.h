@@ -95,6 +95,12 @@ unsigned long long vgpu_kernel_launches(void);
 /* Warnings the reference would raise through Rf_warning (all-NA min/max
  * with na.rm), counted since load. */
 long        vgpu_warning_count(void);
+/* Group-aggregations that took the partitioned path (many groups, one
+ * int64 key, key-ordered output), counted since load.  The path is chosen
+ * on the first input batch; environment: VGPU_PAGG=0 never, =1 whenever
+ * the plan allows it, VGPU_PAGG_MIN_ROWS / VGPU_PAGG_MIN_GROUPS the
+ * thresholds otherwise (4Mi rows, 256Ki estimated groups). */
+unsigned long long vgpu_pagg_runs(void);
 
 /* Optional kernel timing: CUDA events recorded on the launching stream
  * around each kernel class (VGPU_PROF_*), read back in milliseconds. */
@@ -103,6 +109,7 @@ long        vgpu_warning_count(void);
 #define VGPU_PROF_JOIN_BUILD  2   /* hash-join build insert */
 #define VGPU_PROF_JOIN_PROBE  3   /* hash-join probe count */
 #define VGPU_PROF_FINISH      4   /* group results */
+#define VGPU_PROF_PAGG        5   /* partitioned aggregation: bucket reducer */
 void   vgpu_profile_enable(int on);
 void   vgpu_profile_reset(void);
 double vgpu_profile_ms(int kernel_class, unsigned long long *launches);

@@ -8,8 +8,8 @@ import re
 import pytest
 
 
-@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4], ids=["join_direct_payload", "filter_sel_mean", "two_keys_all_accs",
-                                             "inner_join_gather", "join_hashed_payload"])
+@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4, 5], ids=["join_direct_payload", "filter_sel_mean", "two_keys_all_accs",
+                                                "inner_join_gather", "join_hashed_payload", "partition_records"])
 def test_generated_kernel_compiles(shape):
     import vectra_gb300
     lib = vectra_gb300.load()
@@ -30,3 +30,21 @@ def test_digit_split_32bit_matches_64bit():
     lib = vectra_gb300.load()
     lib.vgk_digits_selftest.restype = C.c_longlong
     assert lib.vgk_digits_selftest(C.c_longlong(4_000_000), C.c_ulonglong(0x9E3779B97F4A7C15)) == 0
+
+
+@pytest.mark.parametrize("shape", [0, 1], ids=["high_card_5_aggs", "every_acc_class"])
+def test_partition_reducer_compiles(shape):
+    """The partitioned aggregation's bucket reducer for representative
+    plans: compiles for 1024 threads per CTA within 64 registers (the
+    exact-sum finish keeps its 66-digit array on the stack; the per-record
+    path does not spill more than a few words)."""
+    import vectra_gb300
+    lib = vectra_gb300.load()
+    lib.vgk_jit_error.restype = C.c_char_p
+    regs = C.c_int(-1)
+    rc = lib.vgpu_pagg_selftest(shape, C.byref(regs))
+    log = lib.vgk_jit_error().decode()
+    assert rc == 0, log
+    assert 0 < regs.value <= 64, log
+    kernel = re.search(r"Function properties for vg_jit_pagg\s*\n.*?(\d+) bytes spill stores", log)
+    assert kernel and int(kernel.group(1)) <= 256, log

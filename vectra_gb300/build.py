@@ -22,11 +22,12 @@ LIB = os.path.join(HERE, "libvgpu.so")
 ARCHIVE = os.path.join(HERE, "libvgpu.a")
 
 CU_SOURCES = ["k_groupby_fastj.cu", "k_groupby_fast.cu", "k_groupby.cu", "jit_agg.cu", "k_filter.cu",
-              "k_sort.cu", "k_hashjoin.cu", "k_prof.cu", "k_static.cu", "k_batch.cu", "k_serve.cu"]
+              "k_sort.cu", "k_hashjoin.cu", "k_prof.cu", "k_static.cu", "k_batch.cu", "k_serve.cu",
+              "k_pagg.cu"]
 # headers the run-time compiler needs, embedded into jit_agg.cu's object
 JIT_HEADERS = [("vg_rtc_types.h", CSRC), ("vectra_abi.h", INCLUDE), ("vgpu_internal.h", CSRC),
                ("k_common.cuh", CSRC), ("k_groupby_dev.cuh", CSRC), ("k_jit_lib.cuh", CSRC),
-               ("k_jit_kernel.cuh", CSRC)]
+               ("k_jit_kernel.cuh", CSRC), ("k_jit_pagg.cuh", CSRC)]
 C_SOURCES = ["runtime.c", "compile.c", "source.c", "node_filter.c",
              "node_project.c", "node_agg.c", "node_join.c", "noalloc.c"]
 
@@ -108,7 +109,7 @@ def build(verbose=False, archive=False):
         tmp = LIB + ".tmp"
         cuda_lib = os.path.join(os.path.dirname(_cuda_include()), "lib64")
         _run([_nvcc(), GENCODE, "-shared", "-o", tmp] + objs +
-             ["-cudart", "static", "-L", cuda_lib, "-lnvrtc", "-Xlinker", "-rpath=" + cuda_lib])
+             ["-cudart", "static", "-L", cuda_lib, "-lnvrtc", "-lpthread", "-Xlinker", "-rpath=" + cuda_lib])
         os.replace(tmp, LIB)
     if archive:
         if os.path.exists(ARCHIVE):

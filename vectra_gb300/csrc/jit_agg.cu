@@ -49,6 +49,15 @@ const Shape &shape() {
     return sh;
 }
 
+// The shape a plan is compiled for: partition mode keeps four rows per
+// thread in flight (each row's record position is a global atomic whose
+// latency the other rows' hide).
+Shape plan_shape(const VgAggLaunch &L) {
+    Shape sh = shape();
+    if (L.part && !getenv("VGPU_JIT_SHAPE")) sh.rows = 4;
+    return sh;
+}
+
 char g_jit_err[2048];
 
 struct JitKernel {
@@ -103,6 +112,23 @@ int next_pow2(int x) {
     return p;
 }
 
+// Distinct aggregate input values of a plan (the values a partition record
+// carries): acc_val[a] = index of accumulator a's input, -1 for n().
+int record_values(const VgAggLaunch &L, int *acc_val, const VgValue **vals) {
+    int nv = 0;
+    for (int a = 0; a < L.n_accs; a++) {
+        acc_val[a] = -1;
+        if (L.acc[a].cls == VG_ACC_COUNT_ALL) continue;
+        for (int v = 0; v < nv; v++)
+            if (memcmp(vals[v], &L.acc[a].in, sizeof(VgValue)) == 0) acc_val[a] = v;
+        if (acc_val[a] < 0) {
+            vals[nv] = &L.acc[a].in;
+            acc_val[a] = nv++;
+        }
+    }
+    return nv;
+}
+
 }  // namespace
 
 extern "C" {
@@ -114,7 +140,11 @@ unsigned long long vgk_jit_compiles(void) { return g_compiles; }
 // unique build keys (slot table), a shared-memory cache.
 int vgk_agg_jit_ok(const VgAggLaunch *L) {
     if (getenv("VGPU_NO_JIT")) return 0;
-    if (L->replay || L->cache_slots <= 0) return 0;
+    if (L->part) {
+        if (L->replay || L->dense || L->n_keys != 1 || L->track_first) return 0;
+    } else if (L->replay || L->cache_slots <= 0) {
+        return 0;
+    }
     if (L->has_join && (L->n_jkeys != 1 || !L->jt.slots || L->jt.rows)) return 0;
     if (L->has_join && L->join_kind != JOIN_INNER && L->join_kind != JOIN_LEFT) return 0;
     if (L->dense && (L->n_keys != 1 || L->dense_n + 1 > L->cache_slots)) return 0;
@@ -126,6 +156,7 @@ int vgk_agg_jit_ok(const VgAggLaunch *L) {
 // size while the layout fits the shared memory one CTA per SM can have
 // (the spill area holds two plan-size caches per SM).
 int vgk_agg_jit_slots(const VgAggLaunch *L) {
+    if (L->part) return 32;                // the NA-key group, one slot per warp
     if (L->dense) {
         int s = next_pow2(L->dense_n + 1);
         return s < 256 ? 256 : (s > L->cache_slots ? L->cache_slots : s);
@@ -170,8 +201,8 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
         fmt(s, "#define VGJ_JKIND %d\n#define VGJ_JCOL %d\n#define VGJ_JCONV %d\n#define VGJ_JKT %d\n"
                "#define VGJ_JDIRECT %d\n",
             L.join_kind, L.jkey_col[0], L.jkey_conv[0], L.jt.key_types[0], L.jt.direct ? 1 : 0);
-    fmt(s, "#define VGJ_NK %d\n#define VGJ_DENSE %d\n#define VGJ_TRACK %d\n", L.n_keys, L.dense ? 1 : 0,
-        L.track_first ? 1 : 0);
+    fmt(s, "#define VGJ_NK %d\n#define VGJ_DENSE %d\n#define VGJ_TRACK %d\n#define VGJ_PART %d\n", L.n_keys,
+        L.dense ? 1 : 0, L.track_first ? 1 : 0, L.part ? 1 : 0);
     fmt(s, "#define VGJ_OFF_STATE %lluu\n#define VGJ_OFF_NM %lluu\n#define VGJ_OFF_KEYS %lluu\n"
            "#define VGJ_OFF_FIRST %lluu\n",
         (unsigned long long)c.state, (unsigned long long)c.nm, (unsigned long long)c.keys,
@@ -240,6 +271,37 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
     for (int a = 0; a < L.n_accs; a++) fmt(s, "    if (which & %uu) spill_row(L, li, 0, %d);\n", 1u << a, a);
     s += "    (void)L; (void)li; (void)which;\n}\n";
 
+    // partition mode: a row with a valid key becomes a record in its bucket
+    // (cursors padded to one per 128-byte line: VG_PAGG_CURSOR_STRIDE)
+    s += "VG_DEV unsigned long long vgj_reserve(const VgAggLaunch &L, uint64_t key) {\n";
+    if (L.part)
+        s += "    const uint64_t ow = key ^ 0x8000000000000000ull;\n"
+             "    const uint64_t d = ow < L.po.omin ? 0ull : ((ow - L.po.omin) >> L.po.shift);\n"
+             "    const uint32_t b = d >= (uint64_t)L.po.n_buckets ? (uint32_t)(L.po.n_buckets - 1) : (uint32_t)d;\n"
+             "    const unsigned long long pos = atomicAdd(L.po.cursor + (uint64_t)b * VG_PAGG_CURSOR_STRIDE, 1ull);\n"
+             "    return pos < __ldg(L.po.end + b) ? pos : ~0ull;\n";
+    else
+        s += "    (void)L; (void)key;\n    return ~0ull;\n";
+    s += "}\n";
+    s += "VG_DEV void vgj_write(const VgAggLaunch &L, unsigned long long pos, uint64_t key, const Rows &X, int j) {\n";
+    if (L.part) {
+        int acc_val[VG_MAX_ACCS];
+        const VgValue *vals[VG_MAX_ACCS];
+        const int nv = record_values(L, acc_val, vals);
+        const int rw = 2 + nv + (nv & 1);
+        s += "    if (pos == ~0ull) { atomicOr(L.po.err, VG_ERR_FULL); return; }\n";
+        for (int v = 0; v < nv; v++) fmt(s, "    const InVal v%d = %s;\n", v, value(*vals[v]).c_str());
+        s += "    uint64_t fl = 0;\n";
+        for (int v = 0; v < nv; v++) fmt(s, "    if (v%d.ok) fl |= %lluull;\n", v, 1ull << v);
+        fmt(s, "    ulonglong2 *r = (ulonglong2 *)(L.po.rec + pos * %dull);\n", rw);
+        s += "    r[0] = make_ulonglong2(key, fl);\n";
+        for (int v = 0; v < nv; v += 2) {
+            if (v + 1 < nv) fmt(s, "    r[%d] = make_ulonglong2(v%d.bits, v%d.bits);\n", 1 + v / 2, v, v + 1);
+            else fmt(s, "    r[%d] = make_ulonglong2(v%d.bits, 0ull);\n", 1 + v / 2, v);
+        }
+    }
+    s += "    (void)L; (void)pos; (void)key; (void)X; (void)j;\n}\n";
+
     s += "#include \"k_jit_kernel.cuh\"\n";
     return s;
 }
@@ -288,7 +350,7 @@ int nvrtc_cubin(const std::string &src, std::vector<char> &cubin, int *spill, st
 // thread), down to 256.  out.shape records the shape compiled for.
 int compile_plan(const VgAggLaunch &L, int S, bool vec, std::vector<char> &cubin, Shape &used,
                  std::string *log_out) {
-    Shape sh = shape();
+    Shape sh = plan_shape(L);
     for (;;) {
         int spill = 0;
         if (nvrtc_cubin(gen_source(L, S, vec, sh), cubin, &spill, log_out) != 0) return -1;
@@ -299,13 +361,13 @@ int compile_plan(const VgAggLaunch &L, int S, bool vec, std::vector<char> &cubin
     return 0;
 }
 
-int load_kernel(const std::vector<char> &cubin, JitKernel &out) {
+int load_kernel(const std::vector<char> &cubin, JitKernel &out, const char *name = "vg_jit_agg") {
     cudaError_t e = cudaLibraryLoadData(&out.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
     if (e != cudaSuccess) {
         snprintf(g_jit_err, sizeof(g_jit_err), "cudaLibraryLoadData: %s", cudaGetErrorString(e));
         return -1;
     }
-    e = cudaLibraryGetKernel(&out.kernel, out.lib, "vg_jit_agg");
+    e = cudaLibraryGetKernel(&out.kernel, out.lib, name);
     if (e != cudaSuccess) {
         snprintf(g_jit_err, sizeof(g_jit_err), "cudaLibraryGetKernel: %s", cudaGetErrorString(e));
         return -1;
@@ -327,7 +389,7 @@ bool vec_ok(const VgAggLaunch &L) {
 extern "C" {
 
 int vgk_agg_jit_source(const VgAggLaunch *L, int S, char *out, size_t out_bytes) {
-    std::string s = gen_source(*L, S, vec_ok(*L), shape());
+    std::string s = gen_source(*L, S, vec_ok(*L), plan_shape(*L));
     if (s.size() + 1 > out_bytes) return (int)(s.size() + 1);
     memcpy(out, s.c_str(), s.size() + 1);
     return 0;
@@ -357,7 +419,7 @@ int vgk_agg_launch_jit(const VgAggLaunch *L, int64_t n_logical, vg_stream_t s) {
     if (!vgk_agg_jit_ok(L)) return 0;
     const int S = vgk_agg_jit_slots(L);
     const bool vec = vec_ok(*L);
-    std::string src = gen_source(*L, S, vec, shape());
+    std::string src = gen_source(*L, S, vec, plan_shape(*L));
     JitKernel *jk;
     {
         std::lock_guard<std::mutex> lock(g_mu);
@@ -417,6 +479,236 @@ int vgk_agg_launch_jit(const VgAggLaunch *L, int64_t n_logical, vg_stream_t s) {
 }  // extern "C"
 
 // ---------------------------------------------------------------------
+// partitioned aggregation, second step: the bucket reducer (k_jit_pagg.cuh)
+// ---------------------------------------------------------------------
+namespace {
+
+// Shared-memory layout of the reducer for G groups and S hash slots:
+// only the arrays an accumulator class touches are allocated.
+struct PLay {
+    uint64_t hid, gkey, total;
+    uint64_t cnt[VG_MAX_ACCS], val[VG_MAX_ACCS], flags[VG_MAX_ACCS], base[VG_MAX_ACCS], win[VG_MAX_ACCS];
+};
+
+bool acc_counted(const VgAggLaunch &L, int a) {
+    const int cls = L.acc[a].cls;
+    if (cls == VG_ACC_COUNT_ALL || cls == VG_ACC_COUNT_VALID) return true;
+    if (cls == VG_ACC_SUM_I64 || cls == VG_ACC_SUM_F64) return !((L.skip_count_mask >> a) & 1u);
+    return false;
+}
+
+PLay pagg_lay(const VgAggLaunch &L, int G, int S) {
+    PLay c;
+    memset(&c, 0, sizeof(c));
+    uint64_t off = 0;
+    auto take = [&](uint64_t bytes) {
+        const uint64_t o = off;
+        off = (off + bytes + 15) & ~15ull;
+        return o;
+    };
+    c.hid = take(4ull * S);
+    c.gkey = take(8ull * G);
+    for (int a = 0; a < L.n_accs; a++) {
+        const int cls = L.acc[a].cls;
+        if (acc_counted(L, a)) c.cnt[a] = take(4ull * G);
+        if (cls == VG_ACC_SUM_I64 || acc_is_min(cls) || acc_is_max(cls)) c.val[a] = take(8ull * G);
+        if (cls != VG_ACC_COUNT_ALL && cls != VG_ACC_COUNT_VALID) c.flags[a] = take(4ull * G);
+        if (cls == VG_ACC_SUM_F64) {
+            c.base[a] = take(4ull * G);
+            c.win[a] = take(8ull * G * kWin);
+        }
+    }
+    c.total = off;
+    return c;
+}
+
+constexpr uint64_t kPaggSmem = 226 * 1024;   // dynamic shared memory of one reducer CTA
+
+int hash_slots(int G) { return next_pow2(2 * G); }
+
+std::string gen_pagg_source(const VgAggLaunch &L, const VgFinish *fin, int n_out, int G, int threads) {
+    const int S = hash_slots(G);
+    const PLay c = pagg_lay(L, G, S);
+    int acc_val[VG_MAX_ACCS];
+    const VgValue *vals[VG_MAX_ACCS];
+    const int nv = record_values(L, acc_val, vals);
+    const int rw = 2 + nv + (nv & 1);
+    std::string s;
+    s += "// generated by jit_agg.cu (partitioned aggregation, bucket reducer)\n";
+    s += "#define VGJ_R 2\n#define VGJ_NPC 1\n#define VGJ_NBC 1\n#include \"k_jit_lib.cuh\"\n";
+    fmt(s, "#define VGP_G %d\n#define VGP_S %d\n#define VGP_RW %d\n#define VGP_THREADS %d\n", G, S, rw, threads);
+    fmt(s, "#define VGP_OFF_HID %lluu\n#define VGP_OFF_GKEY %lluu\n", (unsigned long long)c.hid,
+        (unsigned long long)c.gkey);
+    s += "#include \"k_jit_pagg.cuh\"\n";
+
+    // initial accumulator state of a new group
+    s += "VG_DEV void vgp_init(char *sm, int g) {\n";
+    for (int a = 0; a < L.n_accs; a++) {
+        const int cls = L.acc[a].cls;
+        if (acc_counted(L, a)) fmt(s, "    ((uint32_t *)(sm + %lluu))[g] = 0u;\n", (unsigned long long)c.cnt[a]);
+        if (cls != VG_ACC_COUNT_ALL && cls != VG_ACC_COUNT_VALID)
+            fmt(s, "    ((uint32_t *)(sm + %lluu))[g] = 0u;\n", (unsigned long long)c.flags[a]);
+        if (cls == VG_ACC_SUM_I64)
+            fmt(s, "    ((uint32_t *)(sm + %lluu))[g] = 0u; ((int32_t *)(sm + %lluu))[g] = 0;\n",
+                (unsigned long long)c.val[a], (unsigned long long)(c.val[a] + 4ull * G));
+        else if (acc_is_min(cls))
+            fmt(s, "    ((int64_t *)(sm + %lluu))[g] = 0x7FFFFFFFFFFFFFFFll;\n", (unsigned long long)c.val[a]);
+        else if (acc_is_max(cls))
+            fmt(s, "    ((int64_t *)(sm + %lluu))[g] = (int64_t)0x8000000000000000ull;\n",
+                (unsigned long long)c.val[a]);
+        if (cls == VG_ACC_SUM_F64) {
+            fmt(s, "    ((int32_t *)(sm + %lluu))[g] = kBaseUnset;\n", (unsigned long long)c.base[a]);
+            fmt(s, "    for (int i = 0; i < 2 * kWin; i++) ((uint32_t *)(sm + %lluu))[i * %d + g] = 0u;\n",
+                (unsigned long long)c.win[a], G);
+        }
+    }
+    s += "    (void)sm; (void)g;\n}\n";
+
+    // one record into its group
+    s += "VG_DEV void vgp_acc(char *sm, int g, const uint64_t (&w)[VGP_RW], const VgPaggReduce &B, uint64_t fpos) {\n";
+    s += "    const uint64_t fl = w[1];\n";
+    for (int a = 0; a < L.n_accs; a++) {
+        const VgAccSpec &A = L.acc[a];
+        std::string x = acc_val[a] < 0 ? std::string("InVal{0ull, true}")
+                                       : std::string("InVal{w[") + std::to_string(2 + acc_val[a]) + "], ((fl >> " +
+                                             std::to_string(acc_val[a]) + ") & 1ull) != 0}";
+        const int count = acc_counted(L, a) ? 1 : 0;
+        fmt(s, "    { const InVal x = %s;\n", x.c_str());
+        fmt(s, "      if (!vgj::cache_acc<%d, %d, %d, %lluu, %lluu, %lluu, %lluu, %lluu, %d>(sm, g, x)) {\n", A.cls,
+            A.na_rm ? 1 : 0, count, (unsigned long long)c.cnt[a], (unsigned long long)c.val[a],
+            (unsigned long long)c.flags[a], (unsigned long long)c.base[a], (unsigned long long)c.win[a], G);
+        if (A.cls == VG_ACC_SUM_F64) {
+            fmt(s, "          vgp::sum_fallback(B.fs[%d] + fpos, B.fc[%d] + fpos, (uint32_t *)(sm + %lluu) + g, "
+                   "vg_bits_to_f64(x.bits), B.err);\n",
+                a, a, (unsigned long long)c.flags[a]);
+            if (count) fmt(s, "          atomicAdd((uint32_t *)(sm + %lluu) + g, 1u);\n", (unsigned long long)c.cnt[a]);
+        }
+        s += "      } }\n";
+    }
+    s += "    (void)sm; (void)g; (void)w; (void)B; (void)fpos; (void)fl;\n}\n";
+
+    // outputs of a group
+    s += "VG_DEV uint32_t vgp_finish(const char *sm, int g, const VgPaggReduce &B, uint64_t fpos, uint64_t opos) {\n";
+    s += "    uint32_t okb = 0;\n";
+    for (int o = 0; o < n_out; o++) {
+        const VgFinish &F = fin[o];
+        const int a = F.acc;
+        const int cls = L.acc[a].cls;
+        std::string fsp = cls == VG_ACC_SUM_F64 ? "B.fs[" + std::to_string(a) + "] + fpos" : std::string("nullptr");
+        std::string fcp = cls == VG_ACC_SUM_F64 ? "B.fc[" + std::to_string(a) + "] + fpos" : std::string("nullptr");
+        fmt(s, "    { bool ok; const double r = vgp::finish<%d, %d, %d, %lluu, %lluu, %lluu, %lluu, %lluu>(sm, g, %s, %s, "
+               "ok, B.warn);\n",
+            F.finish, cls, F.in_type, (unsigned long long)c.cnt[a], (unsigned long long)c.val[a],
+            (unsigned long long)c.flags[a], (unsigned long long)c.base[a], (unsigned long long)c.win[a], fsp.c_str(),
+            fcp.c_str());
+        fmt(s, "      B.st_out[%d][opos] = ok ? r : 0.0; if (ok) okb |= %uu; }\n", o, 1u << o);
+    }
+    s += "    (void)sm; (void)g; (void)B; (void)fpos; (void)opos;\n    return okb;\n}\n";
+    return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Groups one reducer CTA holds for this plan (0: the plan does not fit).
+int vgk_pagg_groups(const VgAggLaunch *L) {
+    for (int G = 4096; G >= 256; G -= 256) {
+        const PLay c = pagg_lay(*L, G, hash_slots(G));
+        if (c.total <= kPaggSmem) return G;
+    }
+    return 0;
+}
+
+// Record words of the plan's partition records.
+int vgk_pagg_record_words(const VgAggLaunch *L) {
+    int acc_val[VG_MAX_ACCS];
+    const VgValue *vals[VG_MAX_ACCS];
+    const int nv = record_values(*L, acc_val, vals);
+    return 2 + nv + (nv & 1);
+}
+
+int vgk_pagg_source(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, char *out, size_t out_bytes) {
+    std::string s = gen_pagg_source(*L, fin, n_out, G, 1024);
+    if (s.size() + 1 > out_bytes) return (int)(s.size() + 1);
+    memcpy(out, s.c_str(), s.size() + 1);
+    return 0;
+}
+
+// Compiles (cached) and launches the bucket reducer: one CTA per SM.
+// 0 on success, -1 with vgk_jit_error() set.
+int vgk_pagg_reduce(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, const VgPaggReduce *B,
+                    vg_stream_t s) {
+    if (getenv("VGPU_NO_JIT")) {
+        snprintf(g_jit_err, sizeof(g_jit_err), "partitioned aggregation needs the run-time compiler");
+        return -1;
+    }
+    int threads = 1024;
+    std::string src = gen_pagg_source(*L, fin, n_out, G, threads);
+    JitKernel *jk;
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        auto it = g_cache.find(src);
+        if (it == g_cache.end()) {
+            JitKernel k;
+            std::vector<char> cubin;
+            int spill = 0;
+            if (nvrtc_cubin(src, cubin, &spill, nullptr) != 0) return -1;
+            if (spill > 256) {
+                // fewer threads, more registers each
+                threads = 512;
+                if (nvrtc_cubin(gen_pagg_source(*L, fin, n_out, G, threads), cubin, &spill, nullptr) != 0) return -1;
+            }
+            k.shape.threads = threads;
+            if (load_kernel(cubin, k, "vg_jit_pagg") != 0) return -1;
+            it = g_cache.emplace(src, k).first;
+        }
+        jk = &it->second;
+    }
+    const int smem = (int)pagg_lay(*L, G, hash_slots(G)).total;
+    if (jk->smem_set < smem) {
+        cudaError_t e = cudaFuncSetAttribute((const void *)jk->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             smem);
+        if (e != cudaSuccess) {
+            snprintf(g_jit_err, sizeof(g_jit_err), "pagg smem attribute: %s", cudaGetErrorString(e));
+            return -1;
+        }
+        jk->smem_set = smem;
+    }
+    const int sms = vgk_num_sms();
+    const int grid = B->n_buckets < sms ? (B->n_buckets < 1 ? 1 : B->n_buckets) : sms;
+    cudaStream_t st = (cudaStream_t)s;
+    VgPaggReduce T = *B;
+    void *args[] = {(void *)&T};
+    vg_prof_begin(VG_PROF_PAGG, st);
+    cudaError_t e = cudaLaunchKernel((const void *)jk->kernel, dim3(grid), dim3(jk->shape.threads), args, (size_t)smem,
+                                     st);
+    vg_launch_counter++;
+    vg_prof_end(VG_PROF_PAGG, st);
+    if (e != cudaSuccess) {
+        snprintf(g_jit_err, sizeof(g_jit_err), "pagg reduce launch: %s", cudaGetErrorString(e));
+        return -1;
+    }
+    return 0;
+}
+
+// Compiles the reducer without launching it (no device needed).
+int vgk_pagg_compile_only(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, int *regs_out) {
+    std::vector<char> cubin;
+    int spill = 0;
+    std::string log;
+    const int rc = nvrtc_cubin(gen_pagg_source(*L, fin, n_out, G, 1024), cubin, &spill, &log);
+    snprintf(g_jit_err, sizeof(g_jit_err), "%s%.1800s", rc == 0 ? "" : "NVRTC failed:\n", log.c_str());
+    if (regs_out) {
+        const char *p = strstr(log.c_str(), "Used ");
+        *regs_out = p ? atoi(p + 5) : -1;
+    }
+    return rc;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------
 // self-test: generates and compiles representative plan shapes (no device
 // needed).  Shape 0: left join + value*weight sum + n() keyed on a dense
 // build-side attribute (direct-addressed payload copy); 1: filter (double and int64 ranges) + mean + n()
@@ -454,6 +746,53 @@ VgValue val_op(int op, int type, VgOperand a, VgOperand b) {
     v.a = a;
     v.b = b;
     return v;
+}
+
+// Plans of the partitioned-aggregation self-tests (partition mode set).
+void pagg_plan(VgAggLaunch &L, int variant) {
+    static double dummy[4];
+    memset(&L, 0, sizeof(L));
+    L.part = 1;
+    L.po.n_buckets = 2;
+    L.cache_slots = 32;
+    if (variant == 0) {
+        L.n_pcols = 3;
+        L.pcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
+        L.pcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};
+        L.pcols[2] = VgCol{VEC_INT64, 0, dummy, nullptr};
+        L.n_keys = 1;
+        L.key[0] = val_plain(op_col(VG_SIDE_PROBE, 0, VEC_INT64));
+        L.n_accs = 4;
+        L.acc[0].cls = VG_ACC_SUM_F64;
+        L.acc[0].in = val_plain(op_col(VG_SIDE_PROBE, 1, VEC_DOUBLE));
+        L.acc[1].cls = VG_ACC_MIN_I64;
+        L.acc[1].in = val_plain(op_col(VG_SIDE_PROBE, 2, VEC_INT64));
+        L.acc[2].cls = VG_ACC_MAX_I64;
+        L.acc[2].in = val_plain(op_col(VG_SIDE_PROBE, 2, VEC_INT64));
+        L.acc[3].cls = VG_ACC_COUNT_ALL;
+    } else {
+        L.n_pcols = 4;
+        L.pcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
+        L.pcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};
+        L.pcols[2] = VgCol{VEC_INT64, 0, dummy, nullptr};
+        L.pcols[3] = VgCol{VEC_BOOL, 0, dummy, nullptr};
+        L.pred.n_terms = 1;
+        L.pred.term[0] = VgTerm{1, VG_TERM_RANGE, VG_DOM_DOUBLE, 0, 0, 0};
+        L.n_keys = 1;
+        L.key[0] = val_plain(op_col(VG_SIDE_PROBE, 0, VEC_INT64));
+        L.n_accs = 5;
+        L.acc[0].cls = VG_ACC_SUM_I64;
+        L.acc[0].in = val_plain(op_col(VG_SIDE_PROBE, 2, VEC_INT64));
+        L.acc[1].cls = VG_ACC_MIN_F64;
+        L.acc[1].na_rm = 1;
+        L.acc[1].in = val_plain(op_col(VG_SIDE_PROBE, 1, VEC_DOUBLE));
+        L.acc[2].cls = VG_ACC_MAX_F64;
+        L.acc[2].in = val_op('*', VEC_DOUBLE, op_col(VG_SIDE_PROBE, 1, VEC_DOUBLE), op_col(VG_SIDE_PROBE, 2, VEC_INT64));
+        L.acc[3].cls = VG_ACC_COUNT_VALID;
+        L.acc[3].in = val_plain(op_col(VG_SIDE_PROBE, 1, VEC_DOUBLE));
+        L.acc[4].cls = VG_ACC_NA_ONLY;
+        L.acc[4].in = val_plain(op_col(VG_SIDE_PROBE, 3, VEC_BOOL));
+    }
 }
 
 }  // namespace
@@ -557,11 +896,52 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
         L.acc[1].cls = VG_ACC_MAX_I64;
         L.acc[1].in = val_plain(op_col(VG_SIDE_BUILD, 0, VEC_INT64));
         L.track_first = 1;
+    } else if (shape == 5) {
+        // partition mode of group_by(key) |> summarise(sum(x), mean(x), min(y), max(y), n())
+        pagg_plan(L, 0);
     } else {
         snprintf(g_jit_err, sizeof(g_jit_err), "no such self-test shape %d", shape);
         return -1;
     }
     return vgk_agg_jit_compile_only(&L, regs);
+}
+
+// Partitioned-aggregation reducer of representative plans (no device
+// needed): 0, the 5-aggregate high-cardinality plan; 1, every accumulator
+// class (int64 sum, double min / max with na.rm, count of valid values,
+// bool min) with a filter in front.  Returns 0 and the register count, or
+// -1 (vgk_jit_error()).
+extern "C" int vgpu_pagg_selftest(int shape, int *regs) {
+    static VgAggLaunch L;
+    VgFinish fin[VG_MAX_OUTS];
+    int n_out = 0;
+    memset(fin, 0, sizeof(fin));
+    if (shape == 0) {
+        pagg_plan(L, 0);
+        const int kinds[5] = {AGG_SUM, AGG_MEAN, AGG_MIN, AGG_MAX, AGG_COUNT_STAR};
+        const int accs[5] = {0, 0, 1, 2, 3};
+        const int types[5] = {VEC_DOUBLE, VEC_DOUBLE, VEC_INT64, VEC_INT64, VEC_INT64};
+        for (int o = 0; o < 5; o++) fin[o] = VgFinish{accs[o], kinds[o], types[o], 0};
+        n_out = 5;
+    } else if (shape == 1) {
+        pagg_plan(L, 1);
+        fin[0] = VgFinish{0, AGG_SUM, VEC_INT64, 0};
+        fin[1] = VgFinish{0, AGG_MEAN, VEC_INT64, 0};
+        fin[2] = VgFinish{1, AGG_MIN, VEC_DOUBLE, 1};
+        fin[3] = VgFinish{2, AGG_MAX, VEC_DOUBLE, 0};
+        fin[4] = VgFinish{3, AGG_COUNT, VEC_DOUBLE, 0};
+        fin[5] = VgFinish{4, AGG_MIN, VEC_BOOL, 0};
+        n_out = 6;
+    } else {
+        snprintf(g_jit_err, sizeof(g_jit_err), "no such self-test shape %d", shape);
+        return -1;
+    }
+    const int G = vgk_pagg_groups(&L);
+    if (G <= 0) {
+        snprintf(g_jit_err, sizeof(g_jit_err), "plan does not fit the reducer");
+        return -1;
+    }
+    return vgk_pagg_compile_only(&L, fin, n_out, G, regs);
 }
 
 // Host check of the 32-bit digit split against the 64-bit one on n bit

@@ -22,6 +22,7 @@ extern "C" unsigned long long vg_launch_counter;
 #define VG_PROF_JOIN_BUILD 2
 #define VG_PROF_JOIN_PROBE 3
 #define VG_PROF_FINISH 4
+#define VG_PROF_PAGG 5
 void vg_prof_begin(int cls, cudaStream_t s);
 void vg_prof_end(int cls, cudaStream_t s);
 #endif
@@ -328,6 +329,78 @@ VG_DEV double vg_digits_to_double(const int64_t *w, int n, uint32_t special) {
         exp_field = pp - 51;
         if (exp_field >= 2047)
             return __longlong_as_double((long long)((neg ? 0xFFF0000000000000ull : 0x7FF0000000000000ull)));
+        mant = keep & ((1ull << 52) - 1);
+    }
+    uint64_t bits = ((uint64_t)exp_field << 52) | mant;
+    if (neg) bits |= 0x8000000000000000ull;
+    return __longlong_as_double((long long)bits);
+}
+
+// The double nearest (ties to even) to six digit words w[0..6) at digit
+// index base (value = sum w[i] 2^(32 (base + i)) units of 2^-1074, no
+// special values): vg_digits_to_double's arithmetic on registers only, for
+// kernels whose shared memory leaves little L1 for a thread-local array.
+VG_DEV double vg_window6_to_double(const int64_t (&w)[6], int base) {
+    constexpr int kWin = 6;
+    uint32_t dig[kWin + 2];
+    int64_t carry = 0;
+#pragma unroll
+    for (int i = 0; i < kWin; i++) {
+        const int64_t v = w[i] + carry;
+        dig[i] = (uint32_t)(v & 0xFFFFFFFFll);
+        carry = v >> 32;
+    }
+    dig[kWin] = (uint32_t)(carry & 0xFFFFFFFFll);
+    dig[kWin + 1] = (uint32_t)((carry >> 32) & 0xFFFFFFFFll);
+    const bool neg = carry < 0;
+    if (neg) {
+        uint64_t c = 1;
+#pragma unroll
+        for (int i = 0; i < kWin + 2; i++) {
+            const uint64_t v = (uint64_t)(uint32_t)~dig[i] + c;
+            dig[i] = (uint32_t)v;
+            c = v >> 32;
+        }
+    }
+    uint64_t q[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) q[j] = (uint64_t)dig[2 * j] | ((uint64_t)dig[2 * j + 1] << 32);
+    int top = -1;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        if (q[j]) top = j;
+    if (top < 0) return 0.0;
+    uint64_t qt = 0, q1 = 0;
+    bool sticky = false;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        if (j == top) qt = q[j];
+        if (j == top - 1) q1 = q[j];
+        if (j < top - 1 && q[j]) sticky = true;
+    }
+    const int lz = __clzll((long long)qt);
+    const int p = base * 32 + top * 64 + (63 - lz);     // index of the leading one bit
+    const uint64_t inf = neg ? 0xFFF0000000000000ull : 0x7FF0000000000000ull;
+    if (p >= 2098 + 64) return __longlong_as_double((long long)inf);
+    uint64_t mant;
+    int exp_field;
+    if (p <= 52) {
+        // exact: fewer than 2^53 units of 2^-1074 (then base <= 1 and top == 0)
+        const uint64_t M = q[0] << (32 * base);
+        if (M < (1ull << 52)) { mant = M; exp_field = 0; }
+        else { mant = M & ((1ull << 52) - 1); exp_field = 1; }
+    } else {
+        const uint64_t hi = lz ? (qt << lz) | (q1 >> (64 - lz)) : qt;
+        if (lz ? (q1 << lz) != 0 : q1 != 0) sticky = true;
+        uint64_t keep = hi >> 11;
+        const uint64_t rest = hi & 0x7FF;
+        const bool round_bit = (rest >> 10) & 1;
+        const bool rest_sticky = sticky || (rest & 0x3FF);
+        if (round_bit && (rest_sticky || (keep & 1))) keep++;
+        int pp = p;
+        if (keep >> 53) { keep >>= 1; pp++; }
+        exp_field = pp - 51;
+        if (exp_field >= 2047) return __longlong_as_double((long long)inf);
         mant = keep & ((1ull << 52) - 1);
     }
     uint64_t bits = ((uint64_t)exp_field << 52) | mant;

@@ -297,6 +297,70 @@ VG_DEV double sum_f64_result(const VgGroupTable &gt, int a, int64_t g, uint32_t 
     return vg_digits_to_double(w, VG_LACC_WORDS, special);
 }
 
+// One output of group g (src/group_agg.c:240-281): counts, sums (NA if
+// any input was NA and not removed), means, min / max (+-Inf with a
+// warning for a group without values, as R's min/max).
+VG_DEV double group_result(const VgGroupTable &gt, const VgFinish &fi, int64_t g, bool &ok, uint32_t *warn) {
+    const int a = fi.acc;
+    const uint64_t cnt = gt.cnt[a][g];
+    const uint32_t fl = gt.flags[a][g];
+    const int64_t v = gt.val[a][g];
+    ok = true;
+    switch (fi.finish) {
+    case AGG_COUNT:
+    case AGG_COUNT_STAR:
+        return (double)cnt;   // exact below 2^53
+    case AGG_SUM:
+        if (fl & 1u) { ok = false; return 0.0; }
+        if (fi.in_type == VEC_DOUBLE) return sum_f64_result(gt, a, g, fl);
+        return vg_i2f(v);
+    case AGG_MEAN:
+        if (fl & 1u) { ok = false; return 0.0; }
+        if (cnt == 0) return __longlong_as_double(0x7FF8000000000000ll);
+        if (fi.in_type == VEC_DOUBLE) return __ddiv_rn(sum_f64_result(gt, a, g, fl), (double)cnt);
+        return __ddiv_rn(vg_i2f(v), (double)cnt);
+    default: {   // AGG_MIN, AGG_MAX
+        const bool is_min = fi.finish == AGG_MIN;
+        if (fl & 1u) { ok = false; return 0.0; }
+        if (!(fl & 2u)) {
+            atomicAdd(warn, 1u);
+            return is_min ? __longlong_as_double(0x7FF0000000000000ll)
+                          : __longlong_as_double((long long)0xFFF0000000000000ull);
+        }
+        if (fl & 4u) return __longlong_as_double(0x7FF8000000000000ll);
+        if (fi.in_type == VEC_DOUBLE) return vg_bits_to_f64(vg_unord(v));
+        return vg_i2f(v);
+    }
+    }
+}
+
+// The results of slot g written to one staging position (the NA-key
+// group of the partitioned aggregation).
+struct StageArgs {
+    VgGroupTable gt;
+    int n_out;
+    VgFinish fin[VG_MAX_OUTS];
+    int64_t slot;
+    uint64_t pos;
+    uint64_t *st_key;
+    uint32_t *st_ok;
+    double *st_out[VG_MAX_OUTS];
+    uint32_t *warn;
+};
+
+__global__ void stage_kernel(const __grid_constant__ StageArgs A) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    uint32_t okb = 0;
+    for (int o = 0; o < A.n_out; o++) {
+        bool ok = false;
+        const double r = group_result(A.gt, A.fin[o], A.slot, ok, A.warn);
+        A.st_out[o][A.pos] = ok ? r : 0.0;
+        if (ok) okb |= 1u << o;
+    }
+    A.st_key[A.pos] = 0;
+    A.st_ok[A.pos] = okb;
+}
+
 __global__ void finish_kernel(const FinishArgs *__restrict__ F) {
     const int lane = threadIdx.x & 31;
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -313,47 +377,9 @@ __global__ void finish_kernel(const FinishArgs *__restrict__ F) {
             if (lane == 0) F->key_valid[k][j >> 5] = m;
         }
         for (int o = 0; o < F->n_out; o++) {
-            const VgFinish &fi = F->fin[o];
             bool ok = false;
-            double r = 0.0;
             if (in) {
-                int a = fi.acc;
-                uint64_t cnt = gt.cnt[a][g];
-                uint32_t fl = gt.flags[a][g];
-                int64_t v = gt.val[a][g];
-                ok = true;
-                switch (fi.finish) {
-                case AGG_COUNT:
-                case AGG_COUNT_STAR:
-                    r = (double)cnt;   // exact below 2^53
-                    break;
-                case AGG_SUM:
-                    if (fl & 1u) { ok = false; break; }
-                    if (fi.in_type == VEC_DOUBLE) r = sum_f64_result(gt, a, g, fl);
-                    else r = vg_i2f(v);
-                    break;
-                case AGG_MEAN:
-                    if (fl & 1u) { ok = false; break; }
-                    if (cnt == 0) { r = __longlong_as_double(0x7FF8000000000000ll); break; }
-                    if (fi.in_type == VEC_DOUBLE) r = __ddiv_rn(sum_f64_result(gt, a, g, fl), (double)cnt);
-                    else r = __ddiv_rn(vg_i2f(v), (double)cnt);
-                    break;
-                case AGG_MIN:
-                case AGG_MAX: {
-                    bool is_min = fi.finish == AGG_MIN;
-                    if (fl & 1u) { ok = false; break; }
-                    if (!(fl & 2u)) {
-                        r = is_min ? __longlong_as_double(0x7FF0000000000000ll)
-                                   : __longlong_as_double((long long)0xFFF0000000000000ull);
-                        atomicAdd(F->warn, 1u);
-                        break;
-                    }
-                    if (fl & 4u) { r = __longlong_as_double(0x7FF8000000000000ll); break; }
-                    if (fi.in_type == VEC_DOUBLE) r = vg_bits_to_f64(vg_unord(v));
-                    else r = vg_i2f(v);
-                    break;
-                }
-                }
+                const double r = group_result(gt, F->fin[o], g, ok, F->warn);
                 F->out[o][j] = ok ? r : 0.0;
             }
             uint32_t m = __ballot_sync(0xFFFFFFFFu, in && ok);
@@ -554,6 +580,29 @@ int vgk_group_table_compact(const VgGroupTable *gt, int32_t *d_slots, uint32_t *
     cudaMemcpyAsync(h_n, dn, 4, cudaMemcpyDeviceToHost, st);
     cudaFreeAsync(dn, st);
     return check(cudaStreamSynchronize(st), "compact");
+}
+
+int vgk_group_stage(const VgGroupTable *gt, const VgFinish *fin, int n_out, int64_t slot, uint64_t *st_key,
+                    uint32_t *st_ok, double *const *st_out, uint64_t pos, uint32_t *d_warn, vg_stream_t s) {
+    if (n_out > VG_MAX_OUTS) {
+        snprintf(g_err, sizeof(g_err), "stage: too many outputs");
+        return -1;
+    }
+    StageArgs A;
+    memset(&A, 0, sizeof(A));
+    A.gt = *gt;
+    A.n_out = n_out;
+    for (int o = 0; o < n_out; o++) {
+        A.fin[o] = fin[o];
+        A.st_out[o] = st_out[o];
+    }
+    A.slot = slot;
+    A.pos = pos;
+    A.st_key = st_key;
+    A.st_ok = st_ok;
+    A.warn = d_warn;
+    { stage_kernel<<<1, 32, 0, (cudaStream_t)s>>>(A); vg_launch_counter++; }
+    return check(cudaGetLastError(), "stage");
 }
 
 int vgk_group_finish(const VgGroupTable *gt, int n_keys, const int32_t *key_types,

@@ -47,8 +47,8 @@ constexpr int kThreads = 512;
 constexpr int kCacheProbes = 16;
 constexpr int kGlobalProbes = 512;    // a longer probe means the table is too full: spill
 
-VG_DEV bool acc_is_min(int cls) { return cls == VG_ACC_MIN_I64 || cls == VG_ACC_MIN_F64; }
-VG_DEV bool acc_is_max(int cls) { return cls == VG_ACC_MAX_I64 || cls == VG_ACC_MAX_F64; }
+__host__ __device__ inline bool acc_is_min(int cls) { return cls == VG_ACC_MIN_I64 || cls == VG_ACC_MIN_F64; }
+__host__ __device__ inline bool acc_is_max(int cls) { return cls == VG_ACC_MAX_I64 || cls == VG_ACC_MAX_F64; }
 __host__ __device__ inline bool has_val(int cls) {
     return cls == VG_ACC_SUM_I64 || cls == VG_ACC_MIN_I64 || cls == VG_ACC_MAX_I64 ||
            cls == VG_ACC_MIN_F64 || cls == VG_ACC_MAX_F64;

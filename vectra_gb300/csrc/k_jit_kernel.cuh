@@ -13,6 +13,9 @@
 // global table when the CTA finishes; groups that do not fit in the cache,
 // and digit-window overflows, update the global table directly; rows that
 // find the global table full are spilled for a replay after it grows.
+// Partition mode (VGJ_PART, hooks vgj_reserve / vgj_write): rows with a valid key are
+// written as records into their key-range bucket instead; the cache then
+// holds the NA-key group alone, one slot per warp.
 
 #pragma once
 
@@ -50,6 +53,17 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
         for (int i = threadIdx.x; i <= L.dense_n; i += blockDim.x) {
             sk[i] = i < L.dense_n ? (uint64_t)(L.dense_min + i) : 0;
             snm[i] = i < L.dense_n ? 0u : 1u;
+        }
+    }
+#endif
+#if VGJ_PART
+    {
+        // partition mode: the cache holds the NA-key group only, one slot per warp
+        uint64_t *sk = (uint64_t *)(sm + VGJ_OFF_KEYS);
+        uint32_t *snm = (uint32_t *)(sm + VGJ_OFF_NM);
+        for (int i = threadIdx.x; i < S; i += blockDim.x) {
+            sk[i] = 0;
+            snm[i] = 1u;
         }
     }
 #endif
@@ -209,6 +223,35 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
         (void)brow;
 #endif
 #endif
+#if VGJ_PART
+        // Partition mode: the rows with a valid key claim their record
+        // positions first (all R cursor atomics in flight together), then
+        // write their records; the NA-key rows stay live for the cache.
+        {
+            unsigned long long pos[R];
+            uint64_t kk[R];
+            uint32_t emit = 0;
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                pos[j] = 0;
+                kk[j] = 0;
+                if (!((live >> j) & 1u)) continue;
+                Keys k;
+#pragma unroll
+                for (int i = 0; i < VG_MAX_KEYS; i++) k.w[i] = 0;
+                uint32_t nm = 0;
+                vgj_keys(X, j, k, nm);
+                if (nm) continue;
+                kk[j] = k.w[0];
+                pos[j] = vgj_reserve(L, kk[j]);
+                emit |= 1u << j;
+            }
+#pragma unroll
+            for (int j = 0; j < R; j++)
+                if ((emit >> j) & 1u) vgj_write(L, pos[j], kk[j], X, j);
+            live &= ~emit;
+        }
+#endif
         // Cache updates.  Rows that need the global table (a hashed-cache
         // miss, or a value outside a cache digit window) are only marked
         // here and handled together afterwards, so the per-row path has no
@@ -225,7 +268,11 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
             uint32_t nm = 0;
             vgj_keys(X, j, k, nm);
             int found;
-#if VGJ_DENSE
+#if VGJ_PART
+            (void)cache_used;
+            found = (int)(threadIdx.x >> 5);             // an NA-key row: the warp's slot
+            st[found] = 2u;
+#elif VGJ_DENSE
             (void)cache_used;
             found = nm ? L.dense_n : (int)((int64_t)k.w[0] - L.dense_min);
             st[found] = 2u;                           // every touch marks the slot live (same value)

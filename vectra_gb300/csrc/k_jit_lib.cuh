@@ -234,17 +234,22 @@ VG_DEV bool cache_acc(char *sm, int slot, InVal x) {
         if (COUNT) atomicAdd(cnt, 1u);
         return true;
     }
+    // 64-bit shared-memory min / max are compare-and-swap loops: only a
+    // value that improves on the current one (which only moves one way)
+    // takes the atomic
     long long *v64 = (long long *)(sm + OVAL) + slot;
     if (CLS == VG_ACC_MIN_I64 || CLS == VG_ACC_MAX_I64) {
-        if (CLS == VG_ACC_MIN_I64) atomicMin(v64, (long long)x.bits);
-        else atomicMax(v64, (long long)x.bits);
+        const long long v = (long long)x.bits, cur = *(volatile long long *)v64;
+        if (CLS == VG_ACC_MIN_I64) { if (v < cur) atomicMin(v64, v); }
+        else if (v > cur) atomicMax(v64, v);
         set_flags(flags, 2u);
         return true;
     }
     if (CLS == VG_ACC_MIN_F64 || CLS == VG_ACC_MAX_F64) {
         if (vg_is_nan_bits(x.bits)) { set_flags(flags, 2u | 4u); return true; }
-        if (CLS == VG_ACC_MIN_F64) atomicMin(v64, (long long)vg_ord(x.bits));
-        else atomicMax(v64, (long long)vg_ord(x.bits));
+        const long long v = (long long)vg_ord(x.bits), cur = *(volatile long long *)v64;
+        if (CLS == VG_ACC_MIN_F64) { if (v < cur) atomicMin(v64, v); }
+        else if (v > cur) atomicMax(v64, v);
         set_flags(flags, 2u);
         return true;
     }

@@ -1,0 +1,292 @@
+// k_jit_pagg.cuh -- second step of the partitioned aggregation: the
+// run-time specialised bucket reducer.
+//
+// The first step (vg_jit_agg in partition mode) has written every row with
+// a valid int64 group key as a record (key, validity bits, the plan's
+// distinct aggregate inputs) into the key-range bucket of its key; buckets
+// are contiguous key ranges, ascending.  Here one CTA takes one bucket at a
+// time, in bucket order from a ticket:
+//   1. every record's key is looked up in a shared-memory hash table that
+//      hands out dense group ids (the group's accumulators are initialised
+//      by the thread that claims the key), and the record's values update
+//      that group's accumulators with shared-memory atomics, in the same
+//      representation as the fused kernel's cache (exact double sums as
+//      32-bit digits in a window; a value outside the window goes to a
+//      compensated pair in global memory);
+//   2. the group ids are sorted by key (bitonic, in shared memory);
+//   3. each group's outputs are finished (the arithmetic of finish_kernel)
+//      and written, in key order, to the staging area at stage_off[b].
+// A bucket with more groups than one CTA holds is abandoned (ovf[b] = 1)
+// and split further by the host.  Semantics: src/group_agg.c:155-281 and
+// src/agg_ops.c:93-158, as for the other aggregation kernels.
+//
+// Included by the NVRTC source that jit_agg.cu generates, which defines
+// before inclusion VGP_G (groups per CTA), VGP_S (hash slots), VGP_RW (record words),
+// VGP_THREADS and the layout offsets VGP_OFF_HID / VGP_OFF_GKEY, and after
+// it the hooks vgp_init, vgp_acc and vgp_finish.
+
+#pragma once
+#include "k_groupby_dev.cuh"
+
+namespace vgp {
+
+constexpr uint32_t kEmptyId = 0xFFFFFFFFu;
+constexpr uint32_t kBusyId = 0xFFFFFFFEu;
+constexpr int G = VGP_G;
+constexpr int S = VGP_S;          // hash slots: a power of two >= 2 G (load <= 1/2)
+constexpr int RW = VGP_RW;
+
+// flags bits beyond those of the accumulators (bit0..4): the group's
+// compensated pair in global memory is being / has been initialised
+constexpr uint32_t kFbInit = 32u, kFbReady = 64u;
+
+// A double outside the group's digit window: compensated sum in global
+// memory at fpos (the group's staging position).  The first such value
+// of a group zeroes the pair; the others wait (bounded) until it has.
+VG_DEV void sum_fallback(double *fs, double *fc, uint32_t *flags, double x, uint32_t *err) {
+    const uint32_t old = atomicOr(flags, kFbInit);
+    if (!(old & kFbInit)) {
+        *fs = 0.0;
+        *fc = 0.0;
+        __threadfence();
+        atomicOr(flags, kFbReady);
+    } else {
+        int spins = 0;
+        while (!(*(volatile uint32_t *)flags & kFbReady)) {
+            if (++spins > VG_SPIN_LIMIT) { atomicOr(err, VG_ERR_WAIT); return; }
+        }
+        __threadfence();
+    }
+    fallback_add(fs, fc, x);
+}
+
+// Correctly rounded double sum of a group: window digits (lo, hi pairs,
+// stride G) plus, when the group used it, the compensated pair, all added
+// exactly and rounded once.
+__device__ __noinline__ double sum_wide(const int64_t (&win)[kWin], int b, uint32_t special, const double *fs,
+                                        const double *fc) {
+    int64_t w[VG_LACC_WORDS];
+    for (int i = 0; i < VG_LACC_WORDS; i++) w[i] = 0;
+    if (b != kBaseUnset)
+        for (int i = 0; i < kWin; i++) w[b + i] += win[i];
+    const double fb[2] = {*fs, *fc};
+    for (int j = 0; j < 2; j++) {
+        const VgDigits d = vg_split_double(vg_f64_to_bits(fb[j]));
+        special |= d.special;
+        if (d.lo >= 0) {
+            w[d.lo] += d.d0;
+            w[d.lo + 1] += d.d1;
+            if (d.lo + 2 < VG_LACC_WORDS) w[d.lo + 2] += d.d2;
+        }
+    }
+    return vg_digits_to_double(w, VG_LACC_WORDS, special);
+}
+
+VG_DEV double sum_result(const char *sm, uint32_t OBASE, uint32_t OWIN, int g, uint32_t flags, const double *fs,
+                         const double *fc) {
+    const int b = ((const int32_t *)(sm + OBASE))[g];
+    int64_t win[kWin];
+    const uint32_t *wl = (const uint32_t *)(sm + OWIN);
+    const int32_t *wh = (const int32_t *)(sm + OWIN + 4 * G * kWin);
+#pragma unroll
+    for (int i = 0; i < kWin; i++) win[i] = b != kBaseUnset ? pair_get(wl + i * G + g, wh + i * G + g) : 0;
+    const uint32_t special = flags & (4u | 8u | 16u);
+    if (flags & kFbReady) return sum_wide(win, b, special, fs, fc);
+    if ((special & 4u) || (special & 24u) == 24u) return __longlong_as_double(0x7FF8000000000000ll);
+    if (special & 8u) return __longlong_as_double(0x7FF0000000000000ll);
+    if (special & 16u) return __longlong_as_double((long long)0xFFF0000000000000ull);
+    if (b == kBaseUnset) return 0.0;
+    return vg_window6_to_double(win, b);
+}
+
+// One output of group g (finish_kernel's arithmetic on the shared state).
+template <int FIN, int CLS, int IN_TYPE, uint32_t OCNT, uint32_t OVAL, uint32_t OFLAGS, uint32_t OBASE, uint32_t OWIN>
+VG_DEV double finish(const char *sm, int g, const double *fs, const double *fc, bool &ok, uint32_t *warn) {
+    ok = true;
+    const uint32_t cnt = (CLS == VG_ACC_COUNT_ALL || CLS == VG_ACC_COUNT_VALID || FIN == AGG_MEAN ||
+                          FIN == AGG_COUNT || FIN == AGG_COUNT_STAR)
+                             ? ((const uint32_t *)(sm + OCNT))[g]
+                             : 0u;
+    if (FIN == AGG_COUNT || FIN == AGG_COUNT_STAR) return (double)cnt;
+    const uint32_t fl = ((const uint32_t *)(sm + OFLAGS))[g];
+    if (fl & 1u) { ok = false; return 0.0; }
+    if (FIN == AGG_SUM || FIN == AGG_MEAN) {
+        double s;
+        if (IN_TYPE == VEC_DOUBLE) {
+            s = sum_result(sm, OBASE, OWIN, g, fl, fs, fc);
+        } else {
+            s = vg_i2f(pair_get((const uint32_t *)(sm + OVAL) + g, (const int32_t *)(sm + OVAL + 4 * G) + g));
+        }
+        if (FIN == AGG_SUM) return s;
+        if (cnt == 0) return __longlong_as_double(0x7FF8000000000000ll);
+        return __ddiv_rn(s, (double)cnt);
+    }
+    // min / max
+    if (!(fl & 2u)) {
+        atomicAdd(warn, 1u);
+        return FIN == AGG_MIN ? __longlong_as_double(0x7FF0000000000000ll)
+                              : __longlong_as_double((long long)0xFFF0000000000000ull);
+    }
+    if (fl & 4u) return __longlong_as_double(0x7FF8000000000000ll);
+    const int64_t v = ((const int64_t *)(sm + OVAL))[g];
+    if (IN_TYPE == VEC_DOUBLE) return vg_bits_to_f64(vg_unord(v));
+    return vg_i2f(v);
+}
+
+// Group id of key (claiming one, and initialising its accumulators, if
+// the key is new); -1 when the CTA holds G groups already (the bucket
+// overflows) or a bounded wait expired (err set).
+VG_DEV int find(char *sm, uint64_t key, int *s_ng, int *s_ovf, uint32_t *err);
+
+}  // namespace vgp
+
+// hooks written by the generator
+VG_DEV void vgp_init(char *sm, int g);
+VG_DEV void vgp_acc(char *sm, int g, const uint64_t (&w)[VGP_RW], const VgPaggReduce &B, uint64_t fpos);
+VG_DEV uint32_t vgp_finish(const char *sm, int g, const VgPaggReduce &B, uint64_t fpos, uint64_t opos);
+
+namespace vgp {
+
+VG_DEV int find(char *sm, uint64_t key, int *s_ng, int *s_ovf, uint32_t *err) {
+    uint32_t *hid = (uint32_t *)(sm + VGP_OFF_HID);
+    uint64_t *gk = (uint64_t *)(sm + VGP_OFF_GKEY);
+    uint32_t s = (uint32_t)vg_mix64(key) & (uint32_t)(S - 1);
+    for (int probe = 0; probe < S; probe++) {
+        uint32_t v = *(volatile uint32_t *)(hid + s);
+        if (v == kEmptyId) {
+            const uint32_t prev = atomicCAS(hid + s, kEmptyId, kBusyId);
+            if (prev == kEmptyId) {
+                const int id = atomicAdd(s_ng, 1);
+                if (id >= G) {
+                    *(volatile int *)s_ovf = 1;          // the slot stays busy; the bucket is abandoned
+                    return -1;
+                }
+                gk[id] = key;
+                vgp_init(sm, id);
+                __threadfence_block();
+                atomicExch(hid + s, (uint32_t)id);
+                return id;
+            }
+            v = prev;
+        }
+        int spins = 0;
+        while (v == kBusyId) {
+            if (*(volatile int *)s_ovf) return -1;
+            if (++spins > VG_SPIN_LIMIT) {
+                atomicOr(err, VG_ERR_WAIT);
+                *(volatile int *)s_ovf = 1;
+                return -1;
+            }
+            v = *(volatile uint32_t *)(hid + s);
+        }
+        __threadfence_block();
+        if (*(volatile uint64_t *)(gk + v) == key) return (int)v;
+        s = (s + 1) & (uint32_t)(S - 1);
+    }
+    *(volatile int *)s_ovf = 1;
+    return -1;
+}
+
+}  // namespace vgp
+
+extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const __grid_constant__ VgPaggReduce B) {
+    using namespace vgp;
+    extern __shared__ __align__(16) char sm[];
+    __shared__ int s_bucket, s_ng, s_ovf;
+    uint32_t *hid = (uint32_t *)(sm + VGP_OFF_HID);
+    const uint64_t *gk = (const uint64_t *)(sm + VGP_OFF_GKEY);
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_bucket = (int)atomicAdd(B.ticket, 1u);
+            s_ng = 0;
+            s_ovf = 0;
+        }
+        for (int i = threadIdx.x; i < S; i += blockDim.x) hid[i] = kEmptyId;
+        __syncthreads();
+        const int b = s_bucket;
+        if (b >= B.n_buckets) break;
+        const uint64_t sbase = B.stage_off[b];
+        // 1. records -> groups (two records per thread in flight)
+        for (int r = 0; r < B.n_regions; r++) {
+            const uint64_t lo = B.roff[r][b];
+            const uint64_t e = B.rend[r][b], e2 = B.roff[r][b + 1];
+            const uint64_t hi = e < e2 ? e : e2;      // never past the bucket's range
+            const ulonglong2 *rec = (const ulonglong2 *)B.rec[r];
+            for (uint64_t p = lo + 2 * (uint64_t)threadIdx.x; p < hi; p += 2 * (uint64_t)blockDim.x) {
+                if (*(volatile int *)&s_ovf) break;
+                uint64_t w0[RW], w1[RW];
+                const bool two = p + 1 < hi;
+#pragma unroll
+                for (int i = 0; i < RW / 2; i++) {
+                    const ulonglong2 a = __ldcs(rec + (p * RW) / 2 + i);
+                    w0[2 * i] = a.x;
+                    w0[2 * i + 1] = a.y;
+                }
+                if (two) {
+#pragma unroll
+                    for (int i = 0; i < RW / 2; i++) {
+                        const ulonglong2 a = __ldcs(rec + ((p + 1) * RW) / 2 + i);
+                        w1[2 * i] = a.x;
+                        w1[2 * i + 1] = a.y;
+                    }
+                }
+                const int g0 = find(sm, w0[0], &s_ng, &s_ovf, B.err);
+                if (g0 < 0) break;
+                vgp_acc(sm, g0, w0, B, sbase + (uint64_t)g0);
+                if (two) {
+                    const int g1 = find(sm, w1[0], &s_ng, &s_ovf, B.err);
+                    if (g1 < 0) break;
+                    vgp_acc(sm, g1, w1, B, sbase + (uint64_t)g1);
+                }
+            }
+        }
+        __syncthreads();
+        if (s_ovf) {
+            if (threadIdx.x == 0) {
+                B.gc[b] = 0;
+                B.ovf[b] = 1;
+            }
+            __syncthreads();
+            continue;
+        }
+        // 2. group ids in key order (bitonic sort in the hash area)
+        const int n = s_ng;
+        int P2 = 1;
+        while (P2 < n) P2 <<= 1;
+        uint32_t *ord = hid;
+        for (int i = threadIdx.x; i < P2; i += blockDim.x) ord[i] = i < n ? (uint32_t)i : kEmptyId;
+        __syncthreads();
+        for (int size = 2; size <= P2; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int i = threadIdx.x; i < P2; i += blockDim.x) {
+                    const int j = i ^ stride;
+                    if (j <= i) continue;
+                    const uint32_t x = ord[i], y = ord[j];
+                    // padding sorts last; keys compare as signed int64
+                    bool gt;
+                    if (x == kEmptyId) gt = y != kEmptyId;
+                    else if (y == kEmptyId) gt = false;
+                    else gt = (int64_t)gk[x] > (int64_t)gk[y];
+                    const bool up = (i & size) == 0;
+                    if (gt == up) {
+                        ord[i] = y;
+                        ord[j] = x;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // 3. results in key order
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int g = (int)ord[i];
+            const uint64_t opos = sbase + (uint64_t)i;
+            B.st_key[opos] = gk[g];
+            B.st_ok[opos] = vgp_finish(sm, g, B, sbase + (uint64_t)g, opos);
+        }
+        if (threadIdx.x == 0) {
+            B.gc[b] = (uint32_t)n;
+            B.ovf[b] = 0;
+        }
+        __syncthreads();
+    }
+}

@@ -473,6 +473,425 @@ static VecBatch *emit_result(VgAgg *A, Plan *P, Table *T) {
     return res;
 }
 
+/* ------------------------------------------------------------------ */
+/* partitioned aggregation (many groups, one int64 key, key order)     */
+/* ------------------------------------------------------------------ */
+
+/* For key-ordered output of a single int64 key with very many groups, the
+ * group table does not fit on chip and every update would be a random
+ * atomic in HBM.  Instead (k_pagg.cu, k_jit_pagg.cuh):
+ *   1. the first batch's key column is sketched: distinct-key estimate D
+ *      and key range; buckets = 2^p contiguous key ranges with about 3/4 of
+ *      the groups one reducer CTA holds in each;
+ *   2. per batch: rows per bucket (hist), bucket ranges (scan), and the
+ *      fused kernel in partition mode writes each row with a valid key as
+ *      a record into its bucket (NA keys go to a one-group table);
+ *   3. the reducer aggregates every bucket in shared memory, orders its
+ *      groups by key and stages their results; buckets with too many
+ *      groups are split by their own key range (recursively);
+ *   4. the staged results are compacted into the output columns, NA group
+ *      last.
+ * Buckets ascend with the key, so the output needs no global sort. */
+
+typedef struct {
+    uint64_t *rec;
+    uint64_t *off;                 /* n_buckets + 1 */
+    unsigned long long *cursor;    /* record ends after the partition pass */
+} PRegion;
+
+typedef struct {
+    int G;                         /* groups per reducer CTA */
+    int rw;                        /* record words */
+    int nb;                        /* buckets */
+    int shift;
+    uint64_t omin;
+    int n_regions;
+    PRegion reg[VG_PAGG_MAX_REGIONS];
+    uint32_t *cnt;                 /* nb: rows per bucket (hist scratch) */
+    unsigned long long *pcur;      /* nb cursors of the partition pass, VG_PAGG_CURSOR_STRIDE apart */
+    uint32_t *err;
+    Table na;                      /* the NA-key group */
+    uint32_t *counters;            /* spill counters of the partition launch (never used) */
+    uint64_t rows;                 /* records written (upper bound) */
+    VgHostBufs *hb;                /* result columns, faulted in while the device works */
+} PAgg;
+
+static int env_int(const char *name, int dflt) {
+    const char *e = getenv(name);
+    return (e && *e) ? atoi(e) : dflt;
+}
+
+static int bitlen64(uint64_t x) {
+    int b = 0;
+    while (x) { b++; x >>= 1; }
+    return b;
+}
+
+/* Whether this aggregation takes the partitioned path; decided on the
+ * first batch.  VGPU_PAGG=0 never, =1 always when the plan allows it
+ * (tests); otherwise when the batch has at least VGPU_PAGG_MIN_ROWS
+ * logical rows and an estimated VGPU_PAGG_MIN_GROUPS distinct keys. */
+static PAgg *pagg_begin(VgAgg *A, Plan *P, VgAggLaunch *L, const VgDBatch *db) {
+    const int mode = env_int("VGPU_PAGG", -1);
+    if (mode == 0 || !A->sorted || P->n_keys != 1 || P->key[0].op != 0 || P->key[0].a.side != VG_SIDE_PROBE ||
+        P->key[0].a.type != VEC_INT64 || L->dense || L->track_first)
+        return NULL;
+    const int64_t n = db->d_sel ? db->sel_n : db->n_rows;
+    if (mode != 1 && n < (int64_t)env_int("VGPU_PAGG_MIN_ROWS", 1 << 22)) return NULL;
+    L->part = 1;
+    const int ok = vgk_agg_jit_ok(L);
+    const int G = ok ? vgk_pagg_groups(L) : 0;
+    L->part = 0;
+    if (!G) return NULL;
+    const VgCol *kc = &db->cols[P->pset.idx[P->key[0].a.col]];
+    uint32_t *regs = (uint32_t *)vg_dmalloc(4096 * 4 + 256);
+    unsigned long long *mm = (unsigned long long *)((char *)regs + 4096 * 4);
+    double d = 0.0;
+    uint64_t hmm[3];
+    vg_check_rc(vgk_pagg_sketch(kc, n, db->d_sel, regs, mm, &d, hmm, vg_stream()), "partitioned aggregation sketch");
+    vg_dfree(regs);
+    if (mode != 1 && d < (double)env_int("VGPU_PAGG_MIN_GROUPS", 1 << 18)) return NULL;
+    PAgg *pg = (PAgg *)vg_xcalloc(1, sizeof(PAgg));
+    pg->G = env_int("VGPU_PAGG_G", G);          /* a smaller G exercises the bucket split (tests) */
+    if (pg->G < 1 || pg->G > G) pg->G = G;
+    L->part = 1;
+    pg->rw = vgk_pagg_record_words(L);
+    L->part = 0;
+    /* buckets: about 3/4 of G groups each */
+    const double want = d / (0.75 * (double)pg->G);
+    int nb = 2;
+    while ((double)nb < want && nb < (1 << 20)) nb <<= 1;
+    if (env_int("VGPU_PAGG_BUCKETS", 0) > 1) nb = env_int("VGPU_PAGG_BUCKETS", 0);
+    pg->omin = hmm[2] ? hmm[0] : 0;
+    const int bits = hmm[2] ? bitlen64(hmm[1] - hmm[0]) : 0;
+    int lb = 0;
+    while ((1 << lb) < nb) lb++;
+    if (bits < lb) {            /* fewer distinct key values than buckets */
+        lb = bits > 0 ? bits : 1;
+        nb = 1 << lb;
+    }
+    pg->nb = nb;
+    pg->shift = bits > lb ? bits - lb : 0;
+    pg->cnt = (uint32_t *)vg_dmalloc((size_t)nb * 4 + 256);
+    pg->pcur = (unsigned long long *)vg_dmalloc((size_t)nb * VG_PAGG_CURSOR_STRIDE * 8 + 256);
+    pg->err = (uint32_t *)vg_dmalloc(256);
+    vg_dmemset(pg->err, 0, 4);
+    pg->counters = (uint32_t *)vg_dmalloc(256);
+    table_alloc(&pg->na, P, 1024);
+    /* the host result columns (key + outputs) for about the estimated
+     * number of groups: their fresh pages are faulted in by background
+     * threads during the device passes */
+    const double est = d * 1.04 + 4096.0;
+    if (est * 8.0 >= (double)(64 << 20) && est < 4e9)
+        pg->hb = vg_host_bufs_begin(1 + A->ga.n_aggs, (size_t)est * 8);
+    return pg;
+}
+
+/* Step 2 for one batch: its rows become records of a new region. */
+static void pagg_batch(PAgg *pg, Plan *P, VgAggLaunch *L, const VgDBatch *db, int64_t stream_pos, int64_t batch_idx) {
+    if (pg->n_regions == VG_PAGG_MAX_REGIONS)
+        vg_fail("partitioned aggregation: more than %d input batches", VG_PAGG_MAX_REGIONS);
+    const int64_t n = db->d_sel ? db->sel_n : db->n_rows;
+    const VgCol *kc = &db->cols[P->pset.idx[P->key[0].a.col]];
+    const int nb = pg->nb;
+    PRegion *R = &pg->reg[pg->n_regions++];
+    R->off = (uint64_t *)vg_dmalloc((size_t)(nb + 1) * 8 + 256);
+    R->cursor = (unsigned long long *)vg_dmalloc((size_t)nb * 8 + 256);
+    vg_check_rc(vgk_pagg_hist(kc, n, db->d_sel, pg->omin, pg->shift, nb, pg->cnt, vg_stream()),
+                "partitioned aggregation hist");
+    vg_check_rc(vgk_pagg_scan(pg->cnt, NULL, nb, R->off, pg->pcur, VG_PAGG_CURSOR_STRIDE, vg_stream()),
+                "partitioned aggregation scan");
+    uint64_t total = 0;
+    vg_d2h(&total, R->off + nb, 8);
+    vg_sync();
+    R->rec = (uint64_t *)vg_dmalloc((size_t)(total ? total : 1) * (size_t)pg->rw * 8 + 256);
+    pg->rows += total;
+
+    for (int j = 0; j < P->pset.n; j++) L->pcols[j] = db->cols[P->pset.idx[j]];
+    if (db->d_sel) {
+        L->n_rows = db->n_rows;
+        L->sel = db->d_sel;
+        L->sel_n = n;
+    } else {
+        L->n_rows = n;
+        L->sel = NULL;
+        L->sel_n = 0;
+    }
+    L->row_base = stream_pos;
+    L->li_base = 0;
+    L->batch_idx = batch_idx;
+    L->part = 1;
+    L->gt = pg->na.gt;
+    vg_dmemset(pg->counters, 0, 8);
+    L->spill_rows = NULL;
+    L->spill_rows_n = pg->counters;
+    L->spill_rows_cap = 0;
+    L->spill_cache = NULL;
+    L->spill_cache_n = pg->counters + 1;
+    L->spill_cache_cap = 0;
+    L->replay = NULL;
+    L->replay_n = 0;
+    L->po.rec = R->rec;
+    L->po.cursor = pg->pcur;
+    L->po.end = R->off + 1;
+    L->po.omin = pg->omin;
+    L->po.shift = pg->shift;
+    L->po.n_buckets = nb;
+    L->po.rec_words = pg->rw;
+    L->po.n_vals = pg->rw - 2;
+    L->po.err = pg->err;
+    if (n > 0) {
+        const int rc = vgk_agg_launch_jit(L, n, vg_stream());
+        if (rc <= 0) vg_fail("partitioned aggregation: %s", rc < 0 ? vgk_jit_error() : "plan not covered");
+    }
+    L->part = 0;
+    vg_check_rc(vgk_pagg_cursor_compact(pg->pcur, VG_PAGG_CURSOR_STRIDE, nb, R->cursor, vg_stream()),
+                "partitioned aggregation cursors");
+    uint32_t err[2] = {0, 0};
+    vg_d2h(&err[0], pg->err, 4);
+    vg_d2h(&err[1], pg->na.gt.err, 4);
+    vg_sync();
+    if (err[0] | err[1]) vg_fail("partitioned aggregation: partition kernel error (codes %u, %u)", err[0], err[1]);
+}
+
+typedef struct {
+    uint64_t *stage;               /* host leaf arrays (refinement) */
+    uint64_t *gc;
+    int64_t n, cap;
+} Leaves;
+
+static void leaves_push(Leaves *lv, uint64_t stage, uint64_t gc) {
+    if (lv->n == lv->cap) {
+        lv->cap = lv->cap ? 2 * lv->cap : 1024;
+        lv->stage = (uint64_t *)realloc(lv->stage, (size_t)lv->cap * 8);
+        lv->gc = (uint64_t *)realloc(lv->gc, (size_t)lv->cap * 8);
+        if (!lv->stage || !lv->gc) vg_fail("out of host memory");
+    }
+    lv->stage[lv->n] = stage;
+    lv->gc[lv->n] = gc;
+    lv->n++;
+}
+
+/* Runs the reducer over the buckets of R (staging positions stage_off) and
+ * appends the leaves in key order, splitting overflowing buckets. */
+static void pagg_reduce_level(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggReduce *B, int nb,
+                              const uint64_t *d_stage_off, Leaves *lv, int depth) {
+    uint32_t *gc = (uint32_t *)vg_dmalloc((size_t)nb * 8 + 256);
+    uint32_t *ovf = gc + nb;
+    unsigned int *ticket = (unsigned int *)vg_dmalloc(256);
+    vg_dmemset(ticket, 0, 4);
+    B->n_buckets = nb;
+    B->stage_off = d_stage_off;
+    B->gc = gc;
+    B->ovf = ovf;
+    B->ticket = ticket;
+    if (vgk_pagg_reduce(L, P->fin, P->n_out, pg->G, B, vg_stream()) != 0)
+        vg_fail("partitioned aggregation reduce: %s", vgk_jit_error());
+    uint32_t *h = (uint32_t *)vg_xcalloc((size_t)nb * 2, 4);
+    uint64_t *hs = (uint64_t *)vg_xcalloc((size_t)nb, 8);
+    uint32_t err = 0;
+    vg_d2h(h, gc, (size_t)nb * 8);
+    vg_d2h(hs, d_stage_off, (size_t)nb * 8);
+    vg_d2h(&err, B->err, 4);
+    vg_sync();
+    if (err) vg_fail("partitioned aggregation: reduce kernel error (code %u)", err);
+    vg_dfree(ticket);
+    for (int b = 0; b < nb; b++) {
+        if (!h[nb + b]) {
+            leaves_push(lv, hs[b], h[b]);
+            continue;
+        }
+        /* more groups than a CTA holds: split this bucket by its key range */
+        if (depth > 16) vg_fail("partitioned aggregation: bucket split did not converge");
+        uint64_t rows = 0;
+        for (int r = 0; r < B->n_regions; r++) {
+            uint64_t a = 0, e = 0;
+            vg_d2h(&a, B->roff[r] + b, 8);
+            vg_d2h(&e, B->rend[r] + b, 8);
+            vg_sync();
+            rows += e - a;
+        }
+        unsigned long long *mm = (unsigned long long *)vg_dmalloc(256);
+        uint64_t hmm[3];
+        vg_check_rc(vgk_pagg_rec_minmax(B, b, rows, mm, hmm, vg_stream()), "partitioned aggregation split range");
+        vg_dfree(mm);
+        const int bits = bitlen64(hmm[1] - hmm[0]);
+        if (bits == 0) vg_fail("partitioned aggregation: one key overflowed a bucket");
+        const int lb = bits < 8 ? bits : 8;
+        const int nb2 = 1 << lb;
+        const int shift2 = bits - lb;
+        uint32_t *cnt2 = (uint32_t *)vg_dmalloc((size_t)nb2 * 4 + 256);
+        uint64_t *off2 = (uint64_t *)vg_dmalloc((size_t)(nb2 + 1) * 8 + 256);
+        unsigned long long *cur2 = (unsigned long long *)vg_dmalloc((size_t)nb2 * 8 + 256);
+        uint64_t *rec2 = (uint64_t *)vg_dmalloc((size_t)(rows ? rows : 1) * (size_t)pg->rw * 8 + 256);
+        vg_check_rc(vgk_pagg_rec_split(B, b, rows, hmm[0], shift2, nb2, cnt2, off2, cur2, rec2, pg->err, vg_stream()),
+                    "partitioned aggregation split");
+        uint64_t *hoff = (uint64_t *)vg_xcalloc((size_t)nb2 + 1, 8);
+        vg_d2h(hoff, off2, (size_t)(nb2 + 1) * 8);
+        vg_d2h(&err, pg->err, 4);
+        vg_sync();
+        if (err) vg_fail("partitioned aggregation: split kernel error (code %u)", err);
+        for (int i = 0; i < nb2; i++) hoff[i] += hs[b];
+        uint64_t *st2 = (uint64_t *)vg_dmalloc((size_t)nb2 * 8 + 256);
+        vg_h2d(st2, hoff, (size_t)nb2 * 8);
+        VgPaggReduce B2 = *B;
+        B2.n_regions = 1;
+        for (int r = 1; r < VG_PAGG_MAX_REGIONS; r++) { B2.rec[r] = NULL; B2.roff[r] = NULL; B2.rend[r] = NULL; }
+        B2.rec[0] = rec2;
+        B2.roff[0] = off2;
+        B2.rend[0] = cur2;
+        pagg_reduce_level(pg, L, P, &B2, nb2, st2, lv, depth + 1);
+        vg_sync();
+        free(hoff);
+        vg_dfree(st2);
+        vg_dfree(rec2);
+        vg_dfree(cur2);
+        vg_dfree(off2);
+        vg_dfree(cnt2);
+    }
+    free(h);
+    free(hs);
+    vg_dfree(gc);
+}
+
+/* Steps 3 and 4: the result batch. */
+static VecBatch *pagg_end(PAgg *pg, VgAgg *A, Plan *P, VgAggLaunch *L) {
+    GroupAggNode *ga = &A->ga;
+    const int nb = pg->nb;
+    const int n_out = ga->n_aggs;
+    VgPaggReduce B;
+    memset(&B, 0, sizeof(B));
+    B.n_regions = pg->n_regions;
+    B.rec_words = pg->rw;
+    B.n_out = n_out;
+    for (int r = 0; r < pg->n_regions; r++) {
+        B.rec[r] = pg->reg[r].rec;
+        B.roff[r] = pg->reg[r].off;
+        B.rend[r] = pg->reg[r].cursor;
+    }
+    uint64_t *stage_off = (uint64_t *)vg_dmalloc((size_t)(nb + 1) * 8 + 256);
+    vg_check_rc(vgk_pagg_scan(NULL, &B, nb, stage_off, NULL, 1, vg_stream()), "partitioned aggregation stage scan");
+    uint64_t total = 0;
+    vg_d2h(&total, stage_off + nb, 8);
+    vg_sync();
+    /* staging: one position per record plus the NA group's */
+    const uint64_t cap = total + 1;
+    size_t bytes = a256(cap * 8) + a256(cap * 4) + (size_t)n_out * a256(cap * 8);
+    int n_fb = 0;
+    for (int a = 0; a < P->n_accs; a++)
+        if (P->acc[a].cls == VG_ACC_SUM_F64) n_fb++;
+    bytes += (size_t)n_fb * 2 * a256(cap * 8);
+    char *blk = (char *)vg_dmalloc(bytes + 256);
+    size_t o = 0;
+    B.st_key = (uint64_t *)(blk + o); o += a256(cap * 8);
+    B.st_ok = (uint32_t *)(blk + o); o += a256(cap * 4);
+    for (int j = 0; j < n_out; j++) { B.st_out[j] = (double *)(blk + o); o += a256(cap * 8); }
+    for (int a = 0; a < P->n_accs; a++) {
+        if (P->acc[a].cls != VG_ACC_SUM_F64) continue;
+        B.fs[a] = (double *)(blk + o); o += a256(cap * 8);
+        B.fc[a] = (double *)(blk + o); o += a256(cap * 8);
+    }
+    uint32_t *warn = (uint32_t *)vg_dmalloc(256);
+    vg_dmemset(warn, 0, 4);
+    B.warn = warn;
+    B.err = pg->err;
+
+    Leaves lv;
+    memset(&lv, 0, sizeof(lv));
+    pagg_reduce_level(pg, L, P, &B, nb, stage_off, &lv, 0);
+
+    /* the NA-key group */
+    uint32_t na_n = 0;
+    vg_d2h(&na_n, pg->na.gt.n_used, 4);
+    vg_sync();
+    int has_na = 0;
+    if (na_n) {
+        int32_t *slots = (int32_t *)vg_dmalloc((size_t)pg->na.gt.cap * 4 + 16);
+        uint32_t ns = 0;
+        vg_check_rc(vgk_group_table_compact(&pg->na.gt, slots, &ns, vg_stream()), "group compact");
+        int32_t slot = 0;
+        vg_d2h(&slot, slots, 4);
+        vg_sync();
+        vg_dfree(slots);
+        if (ns != 1) vg_fail("partitioned aggregation: NA group table holds %u groups", ns);
+        vg_check_rc(vgk_group_stage(&pg->na.gt, P->fin, n_out, slot, B.st_key, B.st_ok, B.st_out, total, warn,
+                                    vg_stream()),
+                    "NA group");
+        has_na = 1;
+    }
+
+    /* leaf offsets in the output */
+    int64_t ng = 0;
+    uint64_t *hout = (uint64_t *)vg_xcalloc((size_t)lv.n + 1, 8);
+    for (int64_t i = 0; i < lv.n; i++) {
+        hout[i] = (uint64_t)ng;
+        ng += (int64_t)lv.gc[i];
+    }
+    hout[lv.n] = (uint64_t)ng;
+    const int64_t n_groups = ng + has_na;
+    uint64_t *d_leaf = (uint64_t *)vg_dmalloc((size_t)(2 * lv.n + 1) * 8 + 256);
+    if (lv.n) vg_h2d(d_leaf, lv.stage, (size_t)lv.n * 8);
+    vg_h2d(d_leaf + lv.n, hout, (size_t)(lv.n + 1) * 8);
+
+    int n_cols = ga->n_keys + n_out;
+    VecBatch *res = vg_batch_alloc(n_cols, n_groups);
+    size_t wb = (size_t)((n_groups + 31) / 32) * 4;
+    size_t per = a256((size_t)n_groups * 8 + 8) + a256(wb + 8);
+    char *ob = (char *)vg_dmalloc(per * (size_t)n_cols + 256);
+    uint64_t *kout = (uint64_t *)ob;
+    uint32_t *kval = (uint32_t *)((char *)kout + a256((size_t)n_groups * 8 + 8));
+    double *aout[VG_MAX_OUTS];
+    uint32_t *aval[VG_MAX_OUTS];
+    for (int j = 0; j < n_out; j++) {
+        aout[j] = (double *)(ob + per * (size_t)(1 + j));
+        aval[j] = (uint32_t *)((char *)aout[j] + a256((size_t)n_groups * 8 + 8));
+    }
+    vg_check_rc(vgk_pagg_emit(lv.n, d_leaf, d_leaf + lv.n, n_groups, has_na, total, B.st_key, B.st_ok,
+                              (const double *const *)B.st_out, n_out, kout, kval, aout, aval, vg_stream()),
+                "partitioned aggregation emit");
+    vg_host_bufs_wait(pg->hb);
+    const size_t need = (size_t)n_groups * 8;
+    res->columns[0] = vg_download_column_into(VEC_INT64, kout, kval, n_groups, vg_host_bufs_take(pg->hb, 0, need));
+    res->col_names[0] = vg_xstrdup(ga->key_names[0]);
+    for (int j = 0; j < n_out; j++) {
+        res->columns[1 + j] =
+            vg_download_column_into(VEC_DOUBLE, aout[j], aval[j], n_groups, vg_host_bufs_take(pg->hb, 1 + j, need));
+        res->col_names[1 + j] = vg_xstrdup(ga->agg_specs[j].output_name);
+    }
+    uint32_t w = 0;
+    vg_d2h(&w, warn, 4);
+    vg_sync();
+    vg_warn_count((long)w);
+    vg_dfree(ob);
+    vg_dfree(d_leaf);
+    vg_dfree(warn);
+    vg_dfree(blk);
+    vg_dfree(stage_off);
+    free(hout);
+    free(lv.stage);
+    free(lv.gc);
+    return res;
+}
+
+static unsigned long long g_pagg_runs;
+unsigned long long vgpu_pagg_runs(void) { return g_pagg_runs; }
+
+static void pagg_free(PAgg *pg) {
+    if (!pg) return;
+    for (int r = 0; r < pg->n_regions; r++) {
+        vg_dfree(pg->reg[r].rec);
+        vg_dfree(pg->reg[r].off);
+        vg_dfree(pg->reg[r].cursor);
+    }
+    vg_dfree(pg->cnt);
+    vg_dfree(pg->pcur);
+    vg_dfree(pg->err);
+    vg_dfree(pg->counters);
+    vg_dfree(pg->na.block);
+    vg_host_bufs_free(pg->hb);
+    free(pg);
+}
+
 static VecBatch *agg_next(VecNode *self) {
     VgAgg *A = (VgAgg *)self;
     if (A->ga.done) return NULL;
@@ -579,8 +998,17 @@ static VecBatch *agg_next(VecNode *self) {
     memset(&S, 0, sizeof(S));
     VgDBatch db;
     int64_t batch_idx = 0, stream_pos = 0;
+    PAgg *pg = NULL;
     while (vg_pull(P.src, need, 0, &db)) {
         int64_t n_logical = db.d_sel ? db.sel_n : db.n_rows;
+        if (batch_idx == 0) pg = pagg_begin(A, &P, L, &db);
+        if (pg) {
+            pagg_batch(pg, &P, L, &db, stream_pos, batch_idx);
+            vg_dbatch_release(&db);
+            stream_pos += n_logical;
+            batch_idx++;
+            continue;
+        }
         L->batch_idx = batch_idx;
         /* launches of at most kChunk logical rows, so that everything one
          * launch can spill fits the spill list (a batch of any size) */
@@ -607,7 +1035,9 @@ static VecBatch *agg_next(VecNode *self) {
         stream_pos += n_logical;
         batch_idx++;
     }
-    VecBatch *res = emit_result(A, &P, &T);
+    VecBatch *res = pg ? pagg_end(pg, A, &P, L) : emit_result(A, &P, &T);
+    if (pg) g_pagg_runs++;
+    pagg_free(pg);
     vg_dfree(T.block);
     vg_dfree(S.cache);
     vg_dfree(S.counters);

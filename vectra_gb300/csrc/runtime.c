@@ -8,6 +8,8 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <pthread.h>
+#include <unistd.h>
 #include <cuda_runtime_api.h>
 
 #include "vg_host.h"
@@ -69,6 +71,8 @@ void vg_check_rc(int rc, const char *what) {
     if (!m || !*m) m = vgk_agg_last_error();
     if (!m || !*m) m = vgk_join_last_error();
     if (!m || !*m) m = vgk_sort_last_error();
+    if (!m || !*m) m = vgk_pagg_last_error();
+    if (!m || !*m) m = vgk_jit_error();
     vg_fail("%s failed: %s", what, (m && *m) ? m : "unknown device error");
 }
 
@@ -341,6 +345,147 @@ void vg_dbatch_release(VgDBatch *b) {
     memset(b, 0, sizeof(*b));
 }
 
+/* A large fresh host allocation costs the kernel's page zeroing on first
+ * touch (about 25 GB/s on one core), several times the copy from the
+ * device into touched pages; several threads fault the pages in first. */
+typedef struct {
+    volatile char *p;
+    size_t n, step;
+} Touch;
+
+static void *touch_pages(void *arg) {
+    Touch *t = (Touch *)arg;
+    for (size_t o = 0; o < t->n; o += t->step) t->p[o] = 0;
+    return NULL;
+}
+
+static void prefault(void *p, size_t n) {
+    enum { kMaxThreads = 8 };
+    if (n < ((size_t)64 << 20)) return;
+    long cpus = sysconf(_SC_NPROCESSORS_ONLN);
+    int nt = cpus >= 2 * kMaxThreads ? kMaxThreads : (int)(cpus > 1 ? cpus / 2 : 1);
+    if (nt < 2) return;
+    long pg = sysconf(_SC_PAGESIZE);
+    size_t step = pg > 4096 ? (size_t)pg : 4096;
+    size_t chunk = ((n / (size_t)nt) + step - 1) / step * step;
+    pthread_t th[kMaxThreads];
+    Touch t[kMaxThreads];
+    int started = 0;
+    for (int i = 0; i < nt; i++) {
+        size_t off = (size_t)i * chunk;
+        if (off >= n) break;
+        t[i].p = (volatile char *)p + off;
+        t[i].n = off + chunk <= n ? chunk : n - off;
+        t[i].step = step;
+        if (pthread_create(&th[i], NULL, touch_pages, &t[i]) != 0) {
+            touch_pages(&t[i]);
+            continue;
+        }
+        started |= 1 << i;
+    }
+    for (int i = 0; i < nt; i++)
+        if (started & (1 << i)) pthread_join(th[i], NULL);
+}
+
+/* Host buffers faulted in by background threads while the device works
+ * (a result whose size is estimated before it is computed). */
+typedef struct {
+    VgHostBufs *h;
+    size_t lo, hi;             /* the thread's share of every buffer */
+} Slice;
+
+struct VgHostBufs {
+    int n, nt;
+    size_t bytes;
+    void **buf;
+    pthread_t th[8];
+    Slice sl[8];
+    int started;
+};
+
+static void *touch_slices(void *arg) {
+    Slice *t = (Slice *)arg;
+    long pg = sysconf(_SC_PAGESIZE);
+    size_t step = pg > 4096 ? (size_t)pg : 4096;
+    for (int b = 0; b < t->h->n; b++)
+        for (size_t o = t->lo; o < t->hi; o += step) ((volatile char *)t->h->buf[b])[o] = 0;
+    return NULL;
+}
+
+VgHostBufs *vg_host_bufs_begin(int n, size_t bytes) {
+    VgHostBufs *h = (VgHostBufs *)vg_xcalloc(1, sizeof(VgHostBufs));
+    h->n = n;
+    h->bytes = bytes;
+    h->buf = (void **)vg_xcalloc((size_t)n, sizeof(void *));
+    for (int b = 0; b < n; b++) {
+        h->buf[b] = malloc(bytes ? bytes : 1);
+        if (!h->buf[b]) {
+            for (int c = 0; c < b; c++) free(h->buf[c]);
+            free(h->buf);
+            free(h);
+            return NULL;
+        }
+    }
+    long cpus = sysconf(_SC_NPROCESSORS_ONLN);
+    h->nt = cpus >= 16 ? 8 : (int)(cpus > 1 ? cpus / 2 : 1);
+    size_t chunk = (bytes + (size_t)h->nt - 1) / (size_t)h->nt;
+    chunk = (chunk + 65535) & ~(size_t)65535;
+    for (int i = 0; i < h->nt; i++) {
+        size_t lo = (size_t)i * chunk, hi = lo + chunk < bytes ? lo + chunk : bytes;
+        if (lo >= bytes) break;
+        h->sl[i].h = h;
+        h->sl[i].lo = lo;
+        h->sl[i].hi = hi;
+        if (pthread_create(&h->th[i], NULL, touch_slices, &h->sl[i]) == 0) h->started |= 1 << i;
+        else touch_slices(&h->sl[i]);
+    }
+    return h;
+}
+
+/* Waits for the touching threads; the buffers stay with h until taken. */
+void vg_host_bufs_wait(VgHostBufs *h) {
+    if (!h) return;
+    for (int i = 0; i < h->nt; i++)
+        if (h->started & (1 << i)) pthread_join(h->th[i], NULL);
+    h->started = 0;
+}
+
+void *vg_host_bufs_take(VgHostBufs *h, int b, size_t need) {
+    if (!h || b >= h->n || need > h->bytes || !h->buf[b]) return NULL;
+    void *p = h->buf[b];
+    h->buf[b] = NULL;
+    return p;
+}
+
+void vg_host_bufs_free(VgHostBufs *h) {
+    if (!h) return;
+    vg_host_bufs_wait(h);
+    for (int b = 0; b < h->n; b++) free(h->buf[b]);
+    free(h->buf);
+    free(h);
+}
+
+/* A column downloaded into dst (malloc-owned, at least value bytes of n
+ * rows), or into a fresh allocation when dst is NULL. */
+VecArray vg_download_column_into(int type, const void *d_data, const uint32_t *d_valid, int64_t n, void *dst) {
+    if (!dst) return vg_download_column(type, d_data, d_valid, n);
+    VecArray a;
+    memset(&a, 0, sizeof(a));
+    a.type = (VecType)type;
+    a.length = n;
+    a.owns_data = 1;
+    a.validity = (uint8_t *)vg_xcalloc((size_t)vg_vbytes(n), 1);
+    size_t vb = value_bytes(type, n);
+    if (type == VEC_BOOL) a.buf.bln = (uint8_t *)dst;
+    else a.buf.i64 = (int64_t *)dst;
+    if (n > 0) {
+        vg_d2h(dst, d_data, vb);
+        if (d_valid) vg_d2h(a.validity, d_valid, (size_t)vg_vbytes(n));
+        else memset(a.validity, 0xFF, (size_t)vg_vbytes(n));
+    }
+    return a;
+}
+
 VecArray vg_download_column(int type, const void *d_data, const uint32_t *d_valid, int64_t n) {
     VecArray a;
     memset(&a, 0, sizeof(a));
@@ -350,6 +495,7 @@ VecArray vg_download_column(int type, const void *d_data, const uint32_t *d_vali
     a.validity = (uint8_t *)vg_xcalloc((size_t)vg_vbytes(n), 1);
     size_t vb = value_bytes(type, n);
     void *dst = vg_xcalloc(vb ? vb : 1, 1);
+    prefault(dst, vb);
     if (type == VEC_BOOL) a.buf.bln = (uint8_t *)dst;
     else a.buf.i64 = (int64_t *)dst;
     if (n > 0) {

@@ -63,6 +63,13 @@ void vg_dbatch_release(VgDBatch *b);
 
 /* Device column -> newly malloc'd host VecArray of n values. */
 VecArray vg_download_column(int type, const void *d_data, const uint32_t *d_valid, int64_t n);
+VecArray vg_download_column_into(int type, const void *d_data, const uint32_t *d_valid, int64_t n, void *dst);
+/* n host buffers of `bytes` each, faulted in by background threads */
+typedef struct VgHostBufs VgHostBufs;
+VgHostBufs *vg_host_bufs_begin(int n, size_t bytes);
+void vg_host_bufs_wait(VgHostBufs *h);
+void *vg_host_bufs_take(VgHostBufs *h, int b, size_t need);   /* NULL: too small or taken */
+void vg_host_bufs_free(VgHostBufs *h);
 
 /* ---- table source (source.c) ---- */
 int vg_is_table_source(const VecNode *n);

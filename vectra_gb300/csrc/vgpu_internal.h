@@ -237,6 +237,57 @@ typedef struct {
     uint32_t *err;
 } VgJoinTable;
 
+/* Partitioned aggregation (many groups, one int64 key, key-ordered
+ * output): the fused kernel writes every row with a valid key as a record
+ * into the key-range bucket of its key, instead of updating a table.
+ * Record (rec_words 64-bit words): key, validity bits of the values, the
+ * plan's distinct aggregate input values.  Bucket of key k:
+ * min(n_buckets - 1, max(0, (k ^ 2^63) - omin) >> shift); bucket b's
+ * records go to [start[b], end[b]) through its cursor. */
+typedef struct {
+    uint64_t *rec;
+    unsigned long long *cursor;   /* per bucket (stride VG_PAGG_CURSOR_STRIDE): next record position */
+    const uint64_t *end;          /* per bucket: one past its last position */
+    uint64_t omin;
+    int32_t shift;
+    int32_t n_buckets;
+    int32_t rec_words;
+    int32_t n_vals;
+    uint32_t *err;                /* VG_ERR_FULL: a bucket range was exceeded */
+} VgPartOut;
+
+#define VG_PAGG_MAX_REGIONS 64
+/* the partition pass's bucket cursors are VgPartOut.cursor[b * stride]: one
+ * per 128-byte line, so cursor atomics of different buckets do not queue
+ * on the same line */
+#define VG_PAGG_CURSOR_STRIDE 16
+
+/* Second step of the partitioned aggregation: one CTA per bucket at a
+ * time (bucket order from a ticket) aggregates the bucket's records in
+ * shared memory, orders its groups by key and writes their results to
+ * the staging area at stage_off[b].  Records of bucket b in region r:
+ * [roff[r][b], rend[r][b]). */
+typedef struct {
+    int32_t n_regions;
+    int32_t n_buckets;
+    int32_t rec_words;
+    int32_t n_out;
+    const uint64_t *rec[VG_PAGG_MAX_REGIONS];
+    const uint64_t *roff[VG_PAGG_MAX_REGIONS];
+    const unsigned long long *rend[VG_PAGG_MAX_REGIONS];
+    const uint64_t *stage_off;
+    uint32_t *gc;                 /* per bucket: groups written */
+    uint32_t *ovf;                /* per bucket: 1 = more groups than one CTA holds (nothing written) */
+    unsigned int *ticket;
+    uint64_t *st_key;
+    uint32_t *st_ok;              /* bit o: output o is valid */
+    double *st_out[VG_MAX_OUTS];
+    double *fs[VG_MAX_ACCS];      /* compensated fallback of double sums, per staging position */
+    double *fc[VG_MAX_ACCS];
+    uint32_t *warn;
+    uint32_t *err;
+} VgPaggReduce;
+
 /* One fused aggregation launch over a batch of rows:
  *   rows -> [predicate] -> [join probe, per match] -> group keys / values
  *   -> per-CTA shared-memory cache -> global group table. */
@@ -290,7 +341,11 @@ typedef struct {
      * (read by the run-time specialised kernel). */
     const VgJPay *jpay;
     int32_t   jpay_n;
-    int32_t   pad_jpay;
+    /* 1: partitioned aggregation's first step (run-time specialised kernel
+     * only): rows with a valid key become records (po); NA-key rows update
+     * the group table gt, which holds the NA group alone. */
+    int32_t   part;
+    VgPartOut po;
 } VgAggLaunch;
 
 /* ------------------------------------------------------------------ */
@@ -420,6 +475,39 @@ int vgk_agg_jit_compile_only(const VgAggLaunch *L, int *regs_out);
 int vgk_agg_jit_source(const VgAggLaunch *L, int S, char *out, size_t out_bytes);
 const char *vgk_jit_error(void);
 unsigned long long vgk_jit_compiles(void);
+
+/* partitioned aggregation (k_pagg.cu, jit_agg.cu) */
+int vgk_pagg_groups(const VgAggLaunch *L);          /* groups per reducer CTA, 0 = does not fit */
+int vgk_pagg_record_words(const VgAggLaunch *L);
+int vgk_pagg_source(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, char *out, size_t out_bytes);
+int vgk_pagg_compile_only(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, int *regs_out);
+int vgk_pagg_reduce(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, const VgPaggReduce *B,
+                    vg_stream_t s);
+const char *vgk_pagg_last_error(void);
+/* distinct-key estimate and the order-word range (min, max, valid count)
+ * of an int64 key column; d_regs: 4096 words, d_mm: 3 words */
+int vgk_pagg_sketch(const VgCol *key, int64_t n, const int32_t *sel, uint32_t *d_regs, unsigned long long *d_mm,
+                    double *h_distinct, uint64_t *h_mm, vg_stream_t s);
+int vgk_pagg_hist(const VgCol *key, int64_t n, const int32_t *sel, uint64_t omin, int shift, int nb, uint32_t *d_cnt,
+                  vg_stream_t s);
+/* off[0..nb]: exclusive scan of d_cnt (or, d_cnt NULL, of the bucket sizes
+ * of the regions); d_cursor (optional): d_cursor[b * cursor_stride] = off[b] */
+int vgk_pagg_scan(const uint32_t *d_cnt, const VgPaggReduce *regions, int64_t nb, uint64_t *d_off,
+                  unsigned long long *d_cursor, int cursor_stride, vg_stream_t s);
+int vgk_pagg_cursor_compact(const unsigned long long *padded, int stride, int64_t nb, unsigned long long *dense,
+                            vg_stream_t s);
+int vgk_pagg_rec_minmax(const VgPaggReduce *R, int b, uint64_t rows, unsigned long long *d_mm, uint64_t *h_mm,
+                        vg_stream_t s);
+int vgk_pagg_rec_split(const VgPaggReduce *R, int b, uint64_t rows, uint64_t omin, int shift, int nb, uint32_t *d_cnt,
+                       uint64_t *d_off, unsigned long long *d_cursor, uint64_t *d_out, uint32_t *d_err,
+                       vg_stream_t s);
+int vgk_pagg_emit(int64_t n_leaves, const uint64_t *d_leaf_stage, const uint64_t *d_leaf_out, int64_t n_groups,
+                  int has_na, uint64_t na_stage, const uint64_t *st_key, const uint32_t *st_ok,
+                  const double *const *st_out, int n_out, uint64_t *key_out, uint32_t *key_valid, double **out,
+                  uint32_t **out_valid, vg_stream_t s);
+/* the results of one group-table slot written to staging position pos */
+int vgk_group_stage(const VgGroupTable *gt, const VgFinish *fin, int n_out, int64_t slot, uint64_t *st_key,
+                    uint32_t *st_ok, double *const *st_out, uint64_t pos, uint32_t *d_warn, vg_stream_t s);
 #endif  /* !__CUDACC_RTC__ */
 
 #ifdef __cplusplus

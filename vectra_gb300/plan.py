@@ -420,6 +420,24 @@ class Tbl:
             self.engine.free_node(node)
         return out
 
+    def run(self):
+        """Pulls every batch through the node API and frees it (the host
+        batches a C caller receives), without converting to numpy: the
+        number of logical rows produced."""
+        node = self._take()
+        rows = 0
+        try:
+            while True:
+                b = self.engine.next_batch(node)
+                if not b:
+                    break
+                bb = C.cast(b, C.POINTER(abi.VecBatch)).contents
+                rows += bb.sel_n if bb.sel else bb.n_rows
+                self.engine.free_batch(b)
+        finally:
+            self.engine.free_node(node)
+        return rows
+
     def collect(self):
         """All logical rows: {name: (values, valid)}."""
         bs = self.batches()

@@ -69,10 +69,10 @@ def gen_filter_group(torch, n, seed, device):
     return {"station": (station, None), "temperature": (temp, tvalid), "year": (year, None)}
 
 
-def run_filter_group(eng, src, temp_dir="tmp"):
-    return (Tbl(eng, src).filter((col("temperature") > 30.0) & (col("year") >= 2020.0))
-            .group_by("station").summarise(temp_dir=temp_dir, avg=("mean", "temperature"), n=("n",))
-            .collect())
+def run_filter_group(eng, src, temp_dir="tmp", numpy=True):
+    q = (Tbl(eng, src).filter((col("temperature") > 30.0) & (col("year") >= 2020.0))
+         .group_by("station").summarise(temp_dir=temp_dir, avg=("mean", "temperature"), n=("n",)))
+    return q.collect() if numpy else q.run()
 
 
 def check_filter_group(torch, out, cols):
@@ -115,10 +115,11 @@ def gen_high_card(torch, n, distinct, seed, device):
     return {"key": (key, kvalid), "x": (x, None), "y": (y, None)}, raw
 
 
-def run_high_card(eng, src, temp_dir="tmp"):
-    return (Tbl(eng, src).group_by("key")
-            .summarise(temp_dir=temp_dir, s=("sum", "x"), m=("mean", "x"), lo=("min", "y"), hi=("max", "y"),
-                       n=("n",)).collect())
+def run_high_card(eng, src, temp_dir="tmp", numpy=True):
+    q = (Tbl(eng, src).group_by("key")
+         .summarise(temp_dir=temp_dir, s=("sum", "x"), m=("mean", "x"), lo=("min", "y"), hi=("max", "y"),
+                    n=("n",)))
+    return q.collect() if numpy else q.run()
 
 
 def _signed64(u):
