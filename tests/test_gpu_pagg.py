@@ -122,9 +122,11 @@ def test_pagg_filter_every_class(G, oracle, force):
     check(G, oracle, q)
 
 
-def test_pagg_join_in_front(G, oracle, force):
-    """left_join to a dimension, then group_by the fact key: the join probe
-    runs in the partition pass."""
+@pytest.mark.parametrize("kind", ["left_join", "inner_join"])
+def test_pagg_join_in_front(kind, G, oracle, force):
+    """A join to a dimension, then group_by the fact key: the join probe
+    runs in the partition pass (an inner join leaves holes in the record
+    ranges of the rows it drops)."""
     from vectra_gb300.plan import tbl, col
     rng = np.random.default_rng(7)
     nf, nd = 120_000, 9_000
@@ -134,9 +136,23 @@ def test_pagg_join_in_front(G, oracle, force):
     dim = {"id": ids, "weight": rng.random(nd)}
 
     def q(E, td):
-        return (tbl(E, fact, batch_rows=50_000).left_join(tbl(E, dim, batch_rows=4096), {"key": "id"})
+        return (getattr(tbl(E, fact, batch_rows=50_000), kind)(tbl(E, dim, batch_rows=4096), {"key": "id"})
                 .group_by("key").summarise(temp_dir=td, s=("sum", col("value") * col("weight")),
                                            mx=("max", "weight"), n=("n",)).batches())
+    check(G, oracle, q)
+
+
+def test_pagg_global_cursors(G, oracle, force):
+    """Records placed through per-bucket global cursors (the mode for more
+    buckets than the partition kernel keeps counters for), with a filter."""
+    from vectra_gb300.plan import tbl, col
+    force.setenv("VGPU_PAGG_ATOMIC", "1")
+    t = high_card_table(9, 100_000, 30_000)
+
+    def q(E, td):
+        return (tbl(E, t, batch_rows=60_000).filter(col("y") > -500_000).group_by("k")
+                .summarise(temp_dir=td, s=("sum", "x"), m=("mean", "x"), lo=("min", "y"), hi=("max", "y"),
+                           n=("n",)).batches())
     check(G, oracle, q)
 
 

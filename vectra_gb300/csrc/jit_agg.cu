@@ -203,6 +203,10 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
             L.join_kind, L.jkey_col[0], L.jkey_conv[0], L.jt.key_types[0], L.jt.direct ? 1 : 0);
     fmt(s, "#define VGJ_NK %d\n#define VGJ_DENSE %d\n#define VGJ_TRACK %d\n#define VGJ_PART %d\n", L.n_keys,
         L.dense ? 1 : 0, L.track_first ? 1 : 0, L.part ? 1 : 0);
+    // per-CTA record ranges; holes when a filter or an inner join drops rows
+    fmt(s, "#define VGJ_PART_CTA %d\n#define VGJ_PART_HOLES %d\n#define VGJ_OFF_PCUR %lluu\n",
+        (L.part && L.po.cta_off) ? 1 : 0,
+        (L.pred.n_terms > 0 || (L.has_join && L.join_kind == JOIN_INNER)) ? 1 : 0, (unsigned long long)c.total);
     fmt(s, "#define VGJ_OFF_STATE %lluu\n#define VGJ_OFF_NM %lluu\n#define VGJ_OFF_KEYS %lluu\n"
            "#define VGJ_OFF_FIRST %lluu\n",
         (unsigned long long)c.state, (unsigned long long)c.nm, (unsigned long long)c.keys,
@@ -273,15 +277,19 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
 
     // partition mode: a row with a valid key becomes a record in its bucket
     // (cursors padded to one per 128-byte line: VG_PAGG_CURSOR_STRIDE)
-    s += "VG_DEV unsigned long long vgj_reserve(const VgAggLaunch &L, uint64_t key) {\n";
-    if (L.part)
+    s += "VG_DEV unsigned long long vgj_reserve(const VgAggLaunch &L, char *sm, uint64_t key) {\n";
+    if (L.part) {
         s += "    const uint64_t ow = key ^ 0x8000000000000000ull;\n"
              "    const uint64_t d = ow < L.po.omin ? 0ull : ((ow - L.po.omin) >> L.po.shift);\n"
-             "    const uint32_t b = d >= (uint64_t)L.po.n_buckets ? (uint32_t)(L.po.n_buckets - 1) : (uint32_t)d;\n"
-             "    const unsigned long long pos = atomicAdd(L.po.cursor + (uint64_t)b * VG_PAGG_CURSOR_STRIDE, 1ull);\n"
-             "    return pos < __ldg(L.po.end + b) ? pos : ~0ull;\n";
-    else
-        s += "    (void)L; (void)key;\n    return ~0ull;\n";
+             "    const uint32_t b = d >= (uint64_t)L.po.n_buckets ? (uint32_t)(L.po.n_buckets - 1) : (uint32_t)d;\n";
+        if (L.po.cta_off)
+            s += "    const unsigned long long pos = __ldg(L.po.start + b) + atomicAdd((uint32_t *)(sm + VGJ_OFF_PCUR) + b, 1u);\n";
+        else
+            s += "    const unsigned long long pos = atomicAdd(L.po.cursor + (uint64_t)b * VG_PAGG_CURSOR_STRIDE, 1ull);\n";
+        s += "    (void)sm;\n    return pos < __ldg(L.po.end + b) ? pos : ~0ull;\n";
+    } else {
+        s += "    (void)L; (void)sm; (void)key;\n    return ~0ull;\n";
+    }
     s += "}\n";
     s += "VG_DEV void vgj_write(const VgAggLaunch &L, unsigned long long pos, uint64_t key, const Rows &X, int j) {\n";
     if (L.part) {
@@ -375,6 +383,18 @@ int load_kernel(const std::vector<char> &cubin, JitKernel &out, const char *name
     return 0;
 }
 
+// Grid and rows per tile of a launch over n rows (CTA c processes tiles c,
+// c + grid, ...): at most two CTAs per SM (the spill area holds two caches
+// per SM).
+void launch_geometry(const Shape &sh, int64_t n, int *grid, int64_t *tile) {
+    const int sms = vgk_num_sms();
+    const int64_t per = (int64_t)sh.rows * sh.threads;
+    const int64_t tiles = (n + per - 1) / per;
+    const int64_t cap = (int64_t)sms * (sh.ctas < 2 ? sh.ctas : 2);
+    *grid = (int)(tiles < cap ? (tiles < 1 ? 1 : tiles) : cap);
+    *tile = per;
+}
+
 bool vec_ok(const VgAggLaunch &L) {
     if (L.sel) return false;
     for (int c = 0; c < L.n_pcols; c++) {
@@ -415,38 +435,62 @@ int vgk_agg_jit_compile_only(const VgAggLaunch *L, int *regs_out) {
 // Launches the specialised kernel over n_logical rows: 1 launched, 0 the
 // plan shape is not covered (nothing launched), -1 error (message in
 // vgk_jit_error()).
+}  // extern "C"
+
+namespace {
+
+// The compiled kernel of plan L (cached by its source), or null
+// (vgk_jit_error()).
+JitKernel *plan_kernel(const VgAggLaunch *L, int S, bool vec) {
+    std::string src = gen_source(*L, S, vec, plan_shape(*L));
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_cache.find(src);
+    if (it == g_cache.end()) {
+        JitKernel k;
+        std::vector<char> cubin;
+        // VGPU_JIT_DUMP=<file>: append each newly compiled plan's source
+        const char *dump = getenv("VGPU_JIT_DUMP");
+        if (dump) {
+            FILE *f = fopen(dump, "a");
+            if (f) {
+                fputs(src.c_str(), f);
+                fclose(f);
+            }
+        }
+        if (compile_plan(*L, S, vec, cubin, k.shape, nullptr) != 0) return nullptr;
+        if (load_kernel(cubin, k) != 0) return nullptr;
+        it = g_cache.emplace(src, k).first;
+    }
+    return &it->second;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vgk_agg_jit_geometry(const VgAggLaunch *L, int64_t n, int *grid, int64_t *tile) {
+    if (!vgk_agg_jit_ok(L)) {
+        snprintf(g_jit_err, sizeof(g_jit_err), "plan not covered by the specialised kernel");
+        return -1;
+    }
+    JitKernel *jk = plan_kernel(L, vgk_agg_jit_slots(L), vec_ok(*L));
+    if (!jk) return -1;
+    launch_geometry(jk->shape, n, grid, tile);
+    return 0;
+}
+
 int vgk_agg_launch_jit(const VgAggLaunch *L, int64_t n_logical, vg_stream_t s) {
     if (!vgk_agg_jit_ok(L)) return 0;
     const int S = vgk_agg_jit_slots(L);
     const bool vec = vec_ok(*L);
-    std::string src = gen_source(*L, S, vec, plan_shape(*L));
-    JitKernel *jk;
-    {
-        std::lock_guard<std::mutex> lock(g_mu);
-        auto it = g_cache.find(src);
-        if (it == g_cache.end()) {
-            JitKernel k;
-            std::vector<char> cubin;
-            // VGPU_JIT_DUMP=<file>: append each newly compiled plan's source
-            const char *dump = getenv("VGPU_JIT_DUMP");
-            if (dump) {
-                FILE *f = fopen(dump, "a");
-                if (f) {
-                    fputs(src.c_str(), f);
-                    fclose(f);
-                }
-            }
-            if (compile_plan(*L, S, vec, cubin, k.shape, nullptr) != 0) return -1;
-            if (load_kernel(cubin, k) != 0) return -1;
-            it = g_cache.emplace(src, k).first;
-        }
-        jk = &it->second;
-    }
+    JitKernel *jk = plan_kernel(L, S, vec);
+    if (!jk) return -1;
     VgAggLaunch T = *L;
     T.cache_slots = S;
     Lay c;
     make_lay(T, (uint64_t)S, c);
-    const int smem = (int)c.total;
+    int smem = (int)c.total;
+    if (L->part && L->po.cta_off) smem += 4 * L->po.n_buckets;      // per-CTA bucket counters
     if (jk->smem_set < smem) {
         cudaError_t e = cudaFuncSetAttribute((const void *)jk->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              smem);
@@ -456,12 +500,10 @@ int vgk_agg_launch_jit(const VgAggLaunch *L, int64_t n_logical, vg_stream_t s) {
         }
         jk->smem_set = smem;
     }
-    const int sms = vgk_num_sms();
+    int grid = 0;
+    int64_t per = 0;
+    launch_geometry(jk->shape, n_logical, &grid, &per);
     const Shape &sh = jk->shape;
-    const int64_t per = (int64_t)sh.rows * sh.threads;
-    const int64_t tiles = (n_logical + per - 1) / per;
-    const int64_t cap = (int64_t)sms * (sh.ctas < 2 ? sh.ctas : 2);   // the spill area holds 2 caches per SM
-    const int grid = (int)(tiles < cap ? (tiles < 1 ? 1 : tiles) : cap);
     cudaStream_t st = (cudaStream_t)s;
     int64_t n = n_logical;
     void *args[] = {(void *)&T, (void *)&n};
@@ -715,7 +757,9 @@ int vgk_pagg_compile_only(const VgAggLaunch *L, const VgFinish *fin, int n_out, 
 // over a selection vector; 2: two keys (int64, double), bool column, int64
 // division, min / max / integer sum / count / bool min, first-seen order;
 // 3: inner join on a coerced double key, build columns gathered by row;
-// 4: shape 0 on a hashed join table.
+// 4: shape 0 on a hashed join table; 5-7: partition mode (partitioned
+// aggregation's first step) with per-CTA ranges, behind a filter, with
+// global cursors.
 // Returns 0 and the kernel's register count, or -1 (vgk_jit_error()).
 // ---------------------------------------------------------------------
 namespace {
@@ -896,9 +940,11 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
         L.acc[1].cls = VG_ACC_MAX_I64;
         L.acc[1].in = val_plain(op_col(VG_SIDE_BUILD, 0, VEC_INT64));
         L.track_first = 1;
-    } else if (shape == 5) {
-        // partition mode of group_by(key) |> summarise(sum(x), mean(x), min(y), max(y), n())
-        pagg_plan(L, 0);
+    } else if (shape >= 5 && shape <= 7) {
+        // partition mode of group_by(key) |> summarise(sum(x), mean(x), min(y), max(y), n()): 5 per-CTA
+        // record ranges, 6 the same behind a filter (holes), 7 global cursors
+        pagg_plan(L, shape == 6 ? 1 : 0);
+        if (shape != 7) L.po.cta_off = (const uint64_t *)dummy;
     } else {
         snprintf(g_jit_err, sizeof(g_jit_err), "no such self-test shape %d", shape);
         return -1;

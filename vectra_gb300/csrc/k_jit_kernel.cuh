@@ -66,6 +66,14 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
             snm[i] = 1u;
         }
     }
+#if VGJ_PART_CTA
+    {
+        // this CTA's next position in each bucket, relative to the bucket's start
+        uint32_t *pc = (uint32_t *)(sm + VGJ_OFF_PCUR);
+        for (int i = threadIdx.x; i < L.po.n_buckets; i += blockDim.x)
+            pc[i] = (uint32_t)(L.po.cta_off[(int64_t)i * gridDim.x + blockIdx.x] - L.po.start[i]);
+    }
+#endif
 #endif
     __syncthreads();
     uint32_t *st = (uint32_t *)(sm + VGJ_OFF_STATE);
@@ -243,7 +251,7 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
                 vgj_keys(X, j, k, nm);
                 if (nm) continue;
                 kk[j] = k.w[0];
-                pos[j] = vgj_reserve(L, kk[j]);
+                pos[j] = vgj_reserve(L, sm, kk[j]);
                 emit |= 1u << j;
             }
 #pragma unroll
@@ -320,6 +328,19 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
     }
 
     __syncthreads();
+#if VGJ_PART_CTA && VGJ_PART_HOLES
+    {
+        // positions of this CTA's ranges that no row took (dropped rows)
+        const uint32_t *pc = (const uint32_t *)(sm + VGJ_OFF_PCUR);
+        for (int i = threadIdx.x; i < L.po.n_buckets; i += blockDim.x) {
+            const uint64_t e = L.po.cta_off[(int64_t)i * gridDim.x + blockIdx.x + 1];
+            for (uint64_t q = L.po.start[i] + pc[i]; q < e; q++) {
+                ulonglong2 *r = (ulonglong2 *)(L.po.rec + q * (uint64_t)L.po.rec_words);
+                r[0] = make_ulonglong2(0ull, VG_PAGG_HOLE);
+            }
+        }
+    }
+#endif
     __shared__ Lay sl;
     if (threadIdx.x == 0) make_lay(L, (uint64_t)L.spill_cache_cap, sl);
     __syncthreads();

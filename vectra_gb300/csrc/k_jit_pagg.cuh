@@ -13,7 +13,8 @@
 //      representation as the fused kernel's cache (exact double sums as
 //      32-bit digits in a window; a value outside the window goes to a
 //      compensated pair in global memory);
-//   2. the group ids are sorted by key (bitonic, in shared memory);
+//   2. the group ids are sorted by key (counting sort on the top bits of
+//      the key's offset in the bucket's range, in shared memory);
 //   3. each group's outputs are finished (the arithmetic of finish_kernel)
 //      and written, in key order, to the staging area at stage_off[b].
 // A bucket with more groups than one CTA holds is abandoned (ovf[b] = 1)
@@ -35,6 +36,47 @@ constexpr uint32_t kBusyId = 0xFFFFFFFEu;
 constexpr int G = VGP_G;
 constexpr int S = VGP_S;          // hash slots: a power of two >= 2 G (load <= 1/2)
 constexpr int RW = VGP_RW;
+// key-order bins of the reducer's sort: the hash area (S >= 2 G words)
+// holds the G ordered ids and then the bin counters
+constexpr int kBins = (S - G) >= 2048 ? 2048 : (S - G) >= 1024 ? 1024 : (S - G) >= 512 ? 512 : 256;
+constexpr int kBinBits = kBins == 2048 ? 11 : kBins == 1024 ? 10 : kBins == 512 ? 9 : 8;
+
+// In-place exclusive scan of v[0..n) by the whole CTA (n a multiple of
+// blockDim.x or smaller); wsum: 32 words of shared scratch.
+VG_DEV void block_exclusive_scan(uint32_t *v, int n, uint32_t *wsum) {
+    const int per = (n + (int)blockDim.x - 1) / (int)blockDim.x;
+    const int lo = threadIdx.x * per;
+    uint32_t t = 0;
+    for (int i = 0; i < per; i++)
+        if (lo + i < n) t += v[lo + i];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = t;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (int)(blockDim.x >> 5);
+        uint32_t w = lane < nw ? wsum[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nw) wsum[lane] = w;
+    }
+    __syncthreads();
+    uint32_t run = (warp ? wsum[warp - 1] : 0u) + x - t;
+    for (int i = 0; i < per; i++) {
+        if (lo + i < n) {
+            const uint32_t c = v[lo + i];
+            v[lo + i] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+}
 
 // flags bits beyond those of the accumulators (bit0..4): the group's
 // compensated pair in global memory is being / has been initialised
@@ -192,7 +234,8 @@ VG_DEV int find(char *sm, uint64_t key, int *s_ng, int *s_ovf, uint32_t *err) {
 extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const __grid_constant__ VgPaggReduce B) {
     using namespace vgp;
     extern __shared__ __align__(16) char sm[];
-    __shared__ int s_bucket, s_ng, s_ovf;
+    __shared__ int s_bucket, s_ng, s_ovf, s_crowded;
+    __shared__ uint32_t s_wsum[32];
     uint32_t *hid = (uint32_t *)(sm + VGP_OFF_HID);
     const uint64_t *gk = (const uint64_t *)(sm + VGP_OFF_GKEY);
     for (;;) {
@@ -230,10 +273,12 @@ extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const _
                         w1[2 * i + 1] = a.y;
                     }
                 }
-                const int g0 = find(sm, w0[0], &s_ng, &s_ovf, B.err);
-                if (g0 < 0) break;
-                vgp_acc(sm, g0, w0, B, sbase + (uint64_t)g0);
-                if (two) {
+                if (!(w0[1] & VG_PAGG_HOLE)) {                 // holes: positions no row took
+                    const int g0 = find(sm, w0[0], &s_ng, &s_ovf, B.err);
+                    if (g0 < 0) break;
+                    vgp_acc(sm, g0, w0, B, sbase + (uint64_t)g0);
+                }
+                if (two && !(w1[1] & VG_PAGG_HOLE)) {
                     const int g1 = find(sm, w1[0], &s_ng, &s_ovf, B.err);
                     if (g1 < 0) break;
                     vgp_acc(sm, g1, w1, B, sbase + (uint64_t)g1);
@@ -249,31 +294,71 @@ extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const _
             __syncthreads();
             continue;
         }
-        // 2. group ids in key order (bitonic sort in the hash area)
+        // 2. group ids in key order, in the hash area: a counting sort on
+        //    the top bits of each key's offset in the bucket's key range,
+        //    insertion sort within a bin; a bitonic sort if some bin is
+        //    crowded (keys outside the range the buckets were cut for)
         const int n = s_ng;
-        int P2 = 1;
-        while (P2 < n) P2 <<= 1;
         uint32_t *ord = hid;
-        for (int i = threadIdx.x; i < P2; i += blockDim.x) ord[i] = i < n ? (uint32_t)i : kEmptyId;
+        uint32_t *cnt = hid + G;                          // kBins counters after the ids
+        const uint64_t lo = B.omin + ((uint64_t)b << B.shift);
+        const int sh = B.shift > kBinBits ? B.shift - kBinBits : 0;
+        auto bin_of = [&](uint32_t g) -> int {
+            const uint64_t ow = gk[g] ^ 0x8000000000000000ull;
+            const uint64_t d = ow < lo ? 0ull : ((ow - lo) >> sh);
+            return d >= (uint64_t)kBins ? kBins - 1 : (int)d;
+        };
+        for (int i = threadIdx.x; i < kBins; i += blockDim.x) cnt[i] = 0;
+        if (threadIdx.x == 0) s_crowded = 0;
         __syncthreads();
-        for (int size = 2; size <= P2; size <<= 1) {
-            for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                for (int i = threadIdx.x; i < P2; i += blockDim.x) {
-                    const int j = i ^ stride;
-                    if (j <= i) continue;
-                    const uint32_t x = ord[i], y = ord[j];
-                    // padding sorts last; keys compare as signed int64
-                    bool gt;
-                    if (x == kEmptyId) gt = y != kEmptyId;
-                    else if (y == kEmptyId) gt = false;
-                    else gt = (int64_t)gk[x] > (int64_t)gk[y];
-                    const bool up = (i & size) == 0;
-                    if (gt == up) {
-                        ord[i] = y;
-                        ord[j] = x;
-                    }
+        for (int g = threadIdx.x; g < n; g += blockDim.x) atomicAdd(cnt + bin_of((uint32_t)g), 1u);
+        __syncthreads();
+        block_exclusive_scan(cnt, kBins, s_wsum);
+        for (int g = threadIdx.x; g < n; g += blockDim.x) ord[atomicAdd(cnt + bin_of((uint32_t)g), 1u)] = (uint32_t)g;
+        __syncthreads();
+        for (int i = threadIdx.x; i < kBins; i += blockDim.x) {
+            const int e = (int)cnt[i], st = i ? (int)cnt[i - 1] : 0;
+            if (e - st <= 1) continue;
+            if (e - st > 32) {
+                s_crowded = 1;
+                continue;
+            }
+            for (int x = st + 1; x < e; x++) {
+                const uint32_t v = ord[x];
+                const int64_t kv = (int64_t)gk[v];
+                int y = x - 1;
+                while (y >= st && (int64_t)gk[ord[y]] > kv) {
+                    ord[y + 1] = ord[y];
+                    y--;
                 }
-                __syncthreads();
+                ord[y + 1] = v;
+            }
+        }
+        __syncthreads();
+        if (s_crowded) {
+            int P2 = 1;
+            while (P2 < n) P2 <<= 1;
+            for (int i = threadIdx.x; i < P2; i += blockDim.x) ord[i] = i < n ? (uint32_t)i : kEmptyId;
+            __syncthreads();
+            for (int size = 2; size <= P2; size <<= 1) {
+                for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                    for (int i = threadIdx.x; i < P2; i += blockDim.x) {
+                        const int j = i ^ stride;
+                        if (j <= i) continue;
+                        const uint32_t x = ord[i], y = ord[j];
+                        // padding sorts last; keys compare as signed int64
+                        bool gt;
+                        if (x == kEmptyId) gt = y != kEmptyId;
+                        else if (y == kEmptyId) gt = false;
+                        else gt = (int64_t)gk[x] > (int64_t)gk[y];
+                        const bool up = (i & size) == 0;
+                        if (gt == up) {
+                            ord[i] = y;
+                            ord[j] = x;
+                        }
+                    }
+                    __syncthreads();
+                }
             }
         }
         // 3. results in key order

@@ -150,6 +150,88 @@ __global__ void __launch_bounds__(kThreads) hist_kernel(VgCol key, int64_t n, co
     }
 }
 
+// Valid keys per (bucket, CTA) over the fused kernel's tiles: CTA c counts
+// tiles c, c + gridDim.x, ... of `tile` logical rows, as that kernel's CTA
+// c processes them; m[b * gridDim.x + c].
+__global__ void __launch_bounds__(kThreads) hist_cta_kernel(VgCol key, int64_t n, const int32_t *sel, uint64_t omin,
+                                                            int shift, int nb, int64_t tile, uint32_t *m) {
+    extern __shared__ uint32_t h[];
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const uint64_t *d = (const uint64_t *)key.data;
+    const int64_t ntiles = (n + tile - 1) / tile;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t r1 = (t + 1) * tile < n ? (t + 1) * tile : n;
+        for (int64_t i = t * tile + threadIdx.x; i < r1; i += blockDim.x) {
+            const int64_t row = phys_row(sel, i);
+            if (!vg_valid(key, row)) continue;
+            atomicAdd(h + bucket_of(__ldg(d + row), omin, shift, nb), 1u);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) m[(int64_t)i * gridDim.x + blockIdx.x] = h[i];
+}
+
+// Exclusive scan of n u32 counts into u64 offsets (out[n] = total), in
+// three passes: chunk sums, their scan (one CTA), chunk scans.
+constexpr int kScanChunk = kThreads * 16;
+
+__global__ void __launch_bounds__(kThreads) scan_sums_kernel(const uint32_t *in, int64_t n, unsigned long long *sums) {
+    const int64_t lo = (int64_t)blockIdx.x * kScanChunk;
+    unsigned long long t = 0;
+    for (int64_t i = lo + threadIdx.x; i < lo + kScanChunk && i < n; i += blockDim.x) t += in[i];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
+    __shared__ unsigned long long w[32];
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long s = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += w[i];
+        sums[blockIdx.x] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) scan_chunks_kernel(const uint32_t *in, int64_t n,
+                                                               const unsigned long long *sums, int64_t n_chunks,
+                                                               uint64_t *out) {
+    __shared__ unsigned long long base, w[32];
+    if (threadIdx.x == 0) {
+        unsigned long long s = 0;
+        for (int64_t c = 0; c < blockIdx.x; c++) s += sums[c];   // few chunks: sums are L2-resident
+        base = s;
+        if (blockIdx.x == n_chunks - 1) out[n] = s + sums[blockIdx.x];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t lo = (int64_t)blockIdx.x * kScanChunk;
+    for (int64_t b0 = lo; b0 < lo + kScanChunk && b0 < n; b0 += blockDim.x) {
+        const int64_t i = b0 + threadIdx.x;
+        const unsigned long long v = i < n ? in[i] : 0ull;
+        unsigned long long x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) w[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            const int nw = (int)(blockDim.x >> 5);
+            unsigned long long y = lane < nw ? w[lane] : 0ull;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long z = __shfl_up_sync(0xFFFFFFFFu, y, o);
+                if (lane >= o) y += z;
+            }
+            if (lane < nw) w[lane] = y;
+        }
+        __syncthreads();
+        const unsigned long long excl = base + (warp ? w[warp - 1] : 0ull) + x - v;
+        if (i < n) out[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) base = excl + v;
+        __syncthreads();
+    }
+}
+
 // One CTA: off[b] = sum of cnt[0..b), off[nb] = total; cursor[b * cstride]
 // = off[b] (cursor optional).  cnt == nullptr: counts are rend[b] - roff[b] summed
 // over the regions of R (bucket sizes of a set of regions).
@@ -203,6 +285,7 @@ __global__ void __launch_bounds__(kThreads) rec_minmax_kernel(VgPaggReduce R, in
         const uint64_t a = R.roff[r][b], e = rec_end(R, r, b);
         const int64_t stride = (int64_t)gridDim.x * blockDim.x;
         for (uint64_t p = a + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < e; p += stride) {
+            if (__ldg(R.rec[r] + p * R.rec_words + 1) & VG_PAGG_HOLE) continue;
             const uint64_t ow = __ldg(R.rec[r] + p * R.rec_words) ^ 0x8000000000000000ull;
             lo = ow < lo ? ow : lo;
             hi = ow > hi ? ow : hi;
@@ -221,7 +304,8 @@ __global__ void __launch_bounds__(kThreads) rec_hist_kernel(VgPaggReduce R, int 
         const uint64_t a = R.roff[r][b], e = rec_end(R, r, b);
         const int64_t stride = (int64_t)gridDim.x * blockDim.x;
         for (uint64_t p = a + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < e; p += stride)
-            atomicAdd(h + bucket_of(__ldg(R.rec[r] + p * R.rec_words), omin, shift, nb), 1u);
+            if (!(__ldg(R.rec[r] + p * R.rec_words + 1) & VG_PAGG_HOLE))
+                atomicAdd(h + bucket_of(__ldg(R.rec[r] + p * R.rec_words), omin, shift, nb), 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nb; i += blockDim.x)
@@ -237,6 +321,7 @@ __global__ void __launch_bounds__(kThreads) rec_scatter_kernel(VgPaggReduce R, i
         const int64_t stride = (int64_t)gridDim.x * blockDim.x;
         for (uint64_t p = a + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < e; p += stride) {
             const uint64_t *src = R.rec[r] + p * rw;
+            if (__ldg(src + 1) & VG_PAGG_HOLE) continue;
             const uint32_t sb = bucket_of(__ldg(src), omin, shift, nb);
             const unsigned long long pos = atomicAdd(cursor + sb, 1ull);
             if (pos >= end[sb]) { atomicOr(err, VG_ERR_FULL); continue; }
@@ -405,6 +490,37 @@ int vgk_pagg_scan(const uint32_t *d_cnt, const VgPaggReduce *regions, int64_t nb
     scan_kernel<<<1, kThreads, 0, (cudaStream_t)s>>>(d_cnt, R, nb, d_off, d_cursor, cursor_stride);
     vg_launch_counter++;
     return check(cudaGetLastError(), "pagg scan");
+}
+
+int vgk_pagg_hist_cta(const VgCol *key, int64_t n, const int32_t *sel, uint64_t omin, int shift, int nb, int grid,
+                      int64_t tile, uint32_t *d_m, vg_stream_t s) {
+    if (nb > kHistSmemBuckets) {
+        snprintf(g_err, sizeof(g_err), "pagg hist: at most %d buckets per CTA", kHistSmemBuckets);
+        return -1;
+    }
+    static int attr_set = 0;
+    if (!attr_set) {
+        cudaFuncSetAttribute(hist_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kHistSmemBuckets * 4);
+        attr_set = 1;
+    }
+    hist_cta_kernel<<<grid, kThreads, (size_t)nb * 4, (cudaStream_t)s>>>(*key, n, sel, omin, shift, nb, tile, d_m);
+    vg_launch_counter++;
+    return check(cudaGetLastError(), "pagg hist per CTA");
+}
+
+// out[0..n]: exclusive scan of in[0..n) (out[n] = total); d_sums: scratch
+// of one word per 16Ki entries
+int vgk_scan_u32_u64(const uint32_t *in, int64_t n, uint64_t *out, unsigned long long *d_sums, vg_stream_t s) {
+    cudaStream_t st = (cudaStream_t)s;
+    const int64_t chunks = (n + kScanChunk - 1) / kScanChunk;
+    if (chunks == 0) {
+        cudaMemsetAsync(out, 0, 8, st);
+        return check(cudaGetLastError(), "scan");
+    }
+    scan_sums_kernel<<<(int)chunks, kThreads, 0, st>>>(in, n, d_sums);
+    scan_chunks_kernel<<<(int)chunks, kThreads, 0, st>>>(in, n, d_sums, chunks, out);
+    vg_launch_counter += 2;
+    return check(cudaGetLastError(), "scan");
 }
 
 // dense[b] = padded[b * stride]: the record ends after the partition pass

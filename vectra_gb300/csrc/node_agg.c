@@ -587,7 +587,11 @@ static PAgg *pagg_begin(VgAgg *A, Plan *P, VgAggLaunch *L, const VgDBatch *db) {
     return pg;
 }
 
-/* Step 2 for one batch: its rows become records of a new region. */
+/* Step 2 for one batch: its rows become records of a new region.  With at
+ * most VG_PAGG_CTA_BUCKETS buckets, each CTA of the partition kernel
+ * owns a range of every bucket, counted beforehand over exactly its rows,
+ * and hands positions out with shared-memory counters; otherwise the rows
+ * claim positions with global atomics on per-bucket cursors. */
 static void pagg_batch(PAgg *pg, Plan *P, VgAggLaunch *L, const VgDBatch *db, int64_t stream_pos, int64_t batch_idx) {
     if (pg->n_regions == VG_PAGG_MAX_REGIONS)
         vg_fail("partitioned aggregation: more than %d input batches", VG_PAGG_MAX_REGIONS);
@@ -597,15 +601,6 @@ static void pagg_batch(PAgg *pg, Plan *P, VgAggLaunch *L, const VgDBatch *db, in
     PRegion *R = &pg->reg[pg->n_regions++];
     R->off = (uint64_t *)vg_dmalloc((size_t)(nb + 1) * 8 + 256);
     R->cursor = (unsigned long long *)vg_dmalloc((size_t)nb * 8 + 256);
-    vg_check_rc(vgk_pagg_hist(kc, n, db->d_sel, pg->omin, pg->shift, nb, pg->cnt, vg_stream()),
-                "partitioned aggregation hist");
-    vg_check_rc(vgk_pagg_scan(pg->cnt, NULL, nb, R->off, pg->pcur, VG_PAGG_CURSOR_STRIDE, vg_stream()),
-                "partitioned aggregation scan");
-    uint64_t total = 0;
-    vg_d2h(&total, R->off + nb, 8);
-    vg_sync();
-    R->rec = (uint64_t *)vg_dmalloc((size_t)(total ? total : 1) * (size_t)pg->rw * 8 + 256);
-    pg->rows += total;
 
     for (int j = 0; j < P->pset.n; j++) L->pcols[j] = db->cols[P->pset.idx[j]];
     if (db->d_sel) {
@@ -631,26 +626,69 @@ static void pagg_batch(PAgg *pg, Plan *P, VgAggLaunch *L, const VgDBatch *db, in
     L->spill_cache_cap = 0;
     L->replay = NULL;
     L->replay_n = 0;
-    L->po.rec = R->rec;
-    L->po.cursor = pg->pcur;
-    L->po.end = R->off + 1;
     L->po.omin = pg->omin;
     L->po.shift = pg->shift;
     L->po.n_buckets = nb;
     L->po.rec_words = pg->rw;
     L->po.n_vals = pg->rw - 2;
     L->po.err = pg->err;
+    L->po.cursor = NULL;
+    L->po.cta_off = NULL;
+    L->po.start = R->off;
+    L->po.end = R->off + 1;
+
+    const int cta = nb <= VG_PAGG_CTA_BUCKETS && env_int("VGPU_PAGG_ATOMIC", 0) == 0;
+    uint64_t *cta_off = NULL;
+    if (cta) {
+        /* the kernel's geometry decides which rows each CTA counts */
+        L->po.cta_off = (const uint64_t *)R->off;   /* non-null: selects the per-CTA kernel */
+        int grid = 0;
+        int64_t tile = 0;
+        if (vgk_agg_jit_geometry(L, n, &grid, &tile) != 0) vg_fail("partitioned aggregation: %s", vgk_jit_error());
+        const int64_t cells = (int64_t)nb * grid;
+        uint32_t *m = (uint32_t *)vg_dmalloc((size_t)cells * 4 + 256);
+        cta_off = (uint64_t *)vg_dmalloc((size_t)(cells + 1) * 8 + 256);
+        unsigned long long *sums = (unsigned long long *)vg_dmalloc((size_t)(cells / 16384 + 2) * 8 + 256);
+        vg_check_rc(vgk_pagg_hist_cta(kc, n, db->d_sel, pg->omin, pg->shift, nb, grid, tile, m, vg_stream()),
+                    "partitioned aggregation hist");
+        vg_check_rc(vgk_scan_u32_u64(m, cells, cta_off, sums, vg_stream()), "partitioned aggregation scan");
+        /* bucket starts: the offsets of each bucket's first CTA (and the total) */
+        vg_check_rc(vgk_pagg_cursor_compact((const unsigned long long *)cta_off, grid, nb + 1,
+                                            (unsigned long long *)R->off, vg_stream()),
+                    "partitioned aggregation offsets");
+        vg_dfree(sums);
+        vg_dfree(m);
+        L->po.cta_off = cta_off;
+    } else {
+        vg_check_rc(vgk_pagg_hist(kc, n, db->d_sel, pg->omin, pg->shift, nb, pg->cnt, vg_stream()),
+                    "partitioned aggregation hist");
+        vg_check_rc(vgk_pagg_scan(pg->cnt, NULL, nb, R->off, pg->pcur, VG_PAGG_CURSOR_STRIDE, vg_stream()),
+                    "partitioned aggregation scan");
+        L->po.cursor = pg->pcur;
+    }
+    uint64_t total = 0;
+    vg_d2h(&total, R->off + nb, 8);
+    vg_sync();
+    R->rec = (uint64_t *)vg_dmalloc((size_t)(total ? total : 1) * (size_t)pg->rw * 8 + 256);
+    pg->rows += total;
+    L->po.rec = R->rec;
     if (n > 0) {
         const int rc = vgk_agg_launch_jit(L, n, vg_stream());
         if (rc <= 0) vg_fail("partitioned aggregation: %s", rc < 0 ? vgk_jit_error() : "plan not covered");
     }
     L->part = 0;
-    vg_check_rc(vgk_pagg_cursor_compact(pg->pcur, VG_PAGG_CURSOR_STRIDE, nb, R->cursor, vg_stream()),
-                "partitioned aggregation cursors");
+    /* record ends: the whole bucket (holes marked) or the cursors */
+    if (cta)
+        vg_check_rc(vgk_pagg_cursor_compact((const unsigned long long *)(R->off + 1), 1, nb, R->cursor, vg_stream()),
+                    "partitioned aggregation cursors");
+    else
+        vg_check_rc(vgk_pagg_cursor_compact(pg->pcur, VG_PAGG_CURSOR_STRIDE, nb, R->cursor, vg_stream()),
+                    "partitioned aggregation cursors");
     uint32_t err[2] = {0, 0};
     vg_d2h(&err[0], pg->err, 4);
     vg_d2h(&err[1], pg->na.gt.err, 4);
     vg_sync();
+    vg_dfree(cta_off);
     if (err[0] | err[1]) vg_fail("partitioned aggregation: partition kernel error (codes %u, %u)", err[0], err[1]);
 }
 
@@ -737,6 +775,8 @@ static void pagg_reduce_level(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggRed
         VgPaggReduce B2 = *B;
         B2.n_regions = 1;
         for (int r = 1; r < VG_PAGG_MAX_REGIONS; r++) { B2.rec[r] = NULL; B2.roff[r] = NULL; B2.rend[r] = NULL; }
+        B2.omin = hmm[0];
+        B2.shift = shift2;
         B2.rec[0] = rec2;
         B2.roff[0] = off2;
         B2.rend[0] = cur2;
@@ -764,6 +804,8 @@ static VecBatch *pagg_end(PAgg *pg, VgAgg *A, Plan *P, VgAggLaunch *L) {
     B.n_regions = pg->n_regions;
     B.rec_words = pg->rw;
     B.n_out = n_out;
+    B.omin = pg->omin;
+    B.shift = pg->shift;
     for (int r = 0; r < pg->n_regions; r++) {
         B.rec[r] = pg->reg[r].rec;
         B.roff[r] = pg->reg[r].off;

@@ -254,13 +254,26 @@ typedef struct {
     int32_t rec_words;
     int32_t n_vals;
     uint32_t *err;                /* VG_ERR_FULL: a bucket range was exceeded */
+    /* Per-CTA ranges (cta_off != NULL): CTA c of the launch owns records
+     * [cta_off[b * grid + c], cta_off[b * grid + c + 1]) of bucket b,
+     * counted beforehand over exactly the rows it processes, and hands
+     * them out with shared-memory counters instead of the global cursors;
+     * positions it leaves unused (rows a filter or inner join dropped)
+     * are written as holes.  start[b]: bucket b's first position. */
+    const uint64_t *cta_off;
+    const uint64_t *start;
 } VgPartOut;
+
+/* flags word of a partition record that is a hole (no row) */
+#define VG_PAGG_HOLE 0x8000000000000000ull
 
 #define VG_PAGG_MAX_REGIONS 64
 /* the partition pass's bucket cursors are VgPartOut.cursor[b * stride]: one
  * per 128-byte line, so cursor atomics of different buckets do not queue
  * on the same line */
 #define VG_PAGG_CURSOR_STRIDE 16
+/* most buckets whose per-CTA counters fit in the partition kernel's shared memory */
+#define VG_PAGG_CTA_BUCKETS 32768
 
 /* Second step of the partitioned aggregation: one CTA per bucket at a
  * time (bucket order from a ticket) aggregates the bucket's records in
@@ -272,6 +285,9 @@ typedef struct {
     int32_t n_buckets;
     int32_t rec_words;
     int32_t n_out;
+    uint64_t omin;                /* bucket b holds the order words [omin + (b << shift), +2^shift) */
+    int32_t shift;
+    int32_t pad_shift;
     const uint64_t *rec[VG_PAGG_MAX_REGIONS];
     const uint64_t *roff[VG_PAGG_MAX_REGIONS];
     const unsigned long long *rend[VG_PAGG_MAX_REGIONS];
@@ -496,6 +512,16 @@ int vgk_pagg_scan(const uint32_t *d_cnt, const VgPaggReduce *regions, int64_t nb
                   unsigned long long *d_cursor, int cursor_stride, vg_stream_t s);
 int vgk_pagg_cursor_compact(const unsigned long long *padded, int stride, int64_t nb, unsigned long long *dense,
                             vg_stream_t s);
+/* launch geometry of the fused kernel for L over n rows: grid and rows per
+ * CTA tile (CTA c processes tiles c, c + grid, ...) */
+int vgk_agg_jit_geometry(const VgAggLaunch *L, int64_t n, int *grid, int64_t *tile);
+/* counts of valid keys per (bucket, CTA) over the fused kernel's tiles:
+ * M[b * grid + c]; nb <= VG_PAGG_CTA_BUCKETS */
+int vgk_pagg_hist_cta(const VgCol *key, int64_t n, const int32_t *sel, uint64_t omin, int shift, int nb, int grid,
+                      int64_t tile, uint32_t *d_m, vg_stream_t s);
+/* out[0..n]: exclusive scan of n u32 counts (out[n] = total); d_sums:
+ * (n / 16384 + 1) words of scratch */
+int vgk_scan_u32_u64(const uint32_t *in, int64_t n, uint64_t *out, unsigned long long *d_sums, vg_stream_t s);
 int vgk_pagg_rec_minmax(const VgPaggReduce *R, int b, uint64_t rows, unsigned long long *d_mm, uint64_t *h_mm,
                         vg_stream_t s);
 int vgk_pagg_rec_split(const VgPaggReduce *R, int b, uint64_t rows, uint64_t omin, int shift, int nb, uint32_t *d_cnt,
