@@ -487,6 +487,9 @@ def workload_arm(args):
         run()
     torch.cuda.synchronize()
     pagg_runs = lib.vgpu_pagg_runs() - pagg_before
+    lib.vgpu_pagg_phase_ms.restype = C.c_double
+    lib.vgpu_pagg_phase_ms.argtypes = [C.c_int]
+    phase0 = [lib.vgpu_pagg_phase_ms(i) for i in range(6)]
     lib.vgpu_profile_reset()
     lib.vgpu_profile_enable(1)
     stream = torch.cuda.current_stream(dev)
@@ -513,6 +516,9 @@ def workload_arm(args):
             "agg_kernel_ms": agg_ms / max(1, args.steps * 1), "agg_launches": nl.value,
             "partitioned_path": bool(pagg_runs), "reduce_kernel_ms": reduce_ms / max(1, args.steps),
             "finish_kernel_ms": finish_ms / max(1, args.steps), "result_checked": True,
+            "partitioned_phases_ms": dict(zip(["sketch", "partition", "reduce", "compact", "host_buffers", "download"],
+                                              [round((lib.vgpu_pagg_phase_ms(i) - phase0[i]) / args.steps, 3)
+                                               for i in range(6)])) if pagg_runs else None,
             "timed": "the node C API producing the host result batch (malloc-owned columns), without "
                      "conversion to numpy"}
 

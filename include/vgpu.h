@@ -101,6 +101,10 @@ long        vgpu_warning_count(void);
  * the plan allows it, VGPU_PAGG_MIN_ROWS / VGPU_PAGG_MIN_GROUPS the
  * thresholds otherwise (4Mi rows, 256Ki estimated groups). */
 unsigned long long vgpu_pagg_runs(void);
+/* Host wall time (ms, summed since load) of the partitioned path's phases:
+ * 0 sketch, 1 partition pass, 2 bucket reducer, 3 compaction into the
+ * output columns, 4 waiting for the host result buffers, 5 copy to host. */
+double      vgpu_pagg_phase_ms(int phase);
 
 /* Optional kernel timing: CUDA events recorded on the launching stream
  * around each kernel class (VGPU_PROF_*), read back in milliseconds. */

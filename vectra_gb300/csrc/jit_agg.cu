@@ -283,10 +283,11 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
              "    const uint64_t d = ow < L.po.omin ? 0ull : ((ow - L.po.omin) >> L.po.shift);\n"
              "    const uint32_t b = d >= (uint64_t)L.po.n_buckets ? (uint32_t)(L.po.n_buckets - 1) : (uint32_t)d;\n";
         if (L.po.cta_off)
-            s += "    const unsigned long long pos = __ldg(L.po.start + b) + atomicAdd((uint32_t *)(sm + VGJ_OFF_PCUR) + b, 1u);\n";
+            s += "    const unsigned long long pos = atomicAdd((uint32_t *)(sm + VGJ_OFF_PCUR) + b, 1u);\n"
+                 "    return pos < L.po.total ? pos : ~0ull;\n";
         else
-            s += "    const unsigned long long pos = atomicAdd(L.po.cursor + (uint64_t)b * VG_PAGG_CURSOR_STRIDE, 1ull);\n";
-        s += "    (void)sm;\n    return pos < __ldg(L.po.end + b) ? pos : ~0ull;\n";
+            s += "    const unsigned long long pos = atomicAdd(L.po.cursor + (uint64_t)b * VG_PAGG_CURSOR_STRIDE, 1ull);\n"
+                 "    (void)sm;\n    return pos < __ldg(L.po.end + b) ? pos : ~0ull;\n";
     } else {
         s += "    (void)L; (void)sm; (void)key;\n    return ~0ull;\n";
     }

@@ -68,10 +68,11 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
     }
 #if VGJ_PART_CTA
     {
-        // this CTA's next position in each bucket, relative to the bucket's start
+        // this CTA's next position in each bucket (the region holds fewer
+        // than 2^32 records)
         uint32_t *pc = (uint32_t *)(sm + VGJ_OFF_PCUR);
         for (int i = threadIdx.x; i < L.po.n_buckets; i += blockDim.x)
-            pc[i] = (uint32_t)(L.po.cta_off[(int64_t)i * gridDim.x + blockIdx.x] - L.po.start[i]);
+            pc[i] = (uint32_t)L.po.cta_off[(int64_t)i * gridDim.x + blockIdx.x];
     }
 #endif
 #endif
@@ -334,7 +335,7 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
         const uint32_t *pc = (const uint32_t *)(sm + VGJ_OFF_PCUR);
         for (int i = threadIdx.x; i < L.po.n_buckets; i += blockDim.x) {
             const uint64_t e = L.po.cta_off[(int64_t)i * gridDim.x + blockIdx.x + 1];
-            for (uint64_t q = L.po.start[i] + pc[i]; q < e; q++) {
+            for (uint64_t q = pc[i]; q < e; q++) {
                 ulonglong2 *r = (ulonglong2 *)(L.po.rec + q * (uint64_t)L.po.rec_words);
                 r[0] = make_ulonglong2(0ull, VG_PAGG_HOLE);
             }

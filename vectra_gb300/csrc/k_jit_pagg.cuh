@@ -198,7 +198,15 @@ VG_DEV int find(char *sm, uint64_t key, int *s_ng, int *s_ovf, uint32_t *err) {
         if (v == kEmptyId) {
             const uint32_t prev = atomicCAS(hid + s, kEmptyId, kBusyId);
             if (prev == kEmptyId) {
-                const int id = atomicAdd(s_ng, 1);
+                // the lanes that claimed a slot here together take their
+                // ids with one counter update
+                const uint32_t m = __activemask();
+                const int lane = threadIdx.x & 31;
+                const int leader = __ffs(m) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(s_ng, __popc(m));
+                base = __shfl_sync(m, base, leader);
+                const int id = base + __popc(m & ((1u << lane) - 1u));
                 if (id >= G) {
                     *(volatile int *)s_ovf = 1;          // the slot stays busy; the bucket is abandoned
                     return -1;

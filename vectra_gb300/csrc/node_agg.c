@@ -25,6 +25,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #include "vg_host.h"
 
 typedef struct {
@@ -516,6 +517,22 @@ typedef struct {
     VgHostBufs *hb;                /* result columns, faulted in while the device works */
 } PAgg;
 
+/* Host wall time of the partitioned path's phases, summed since load
+ * (each phase ends in a device synchronisation, so its time includes its
+ * device work): 0 sketch and setup, 1 partition (hist, scan, partition
+ * kernel), 2 bucket reducer (and splits), 3 NA group and compaction into
+ * the output columns, 4 waiting for the host result buffers, 5 copying
+ * the result to the host. */
+static double g_pagg_ms[6];
+
+static double now_ms(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec * 1e3 + (double)ts.tv_nsec * 1e-6;
+}
+
+double vgpu_pagg_phase_ms(int phase) { return phase >= 0 && phase < 6 ? g_pagg_ms[phase] : 0.0; }
+
 static int env_int(const char *name, int dflt) {
     const char *e = getenv(name);
     return (e && *e) ? atoi(e) : dflt;
@@ -637,7 +654,9 @@ static void pagg_batch(PAgg *pg, Plan *P, VgAggLaunch *L, const VgDBatch *db, in
     L->po.start = R->off;
     L->po.end = R->off + 1;
 
-    const int cta = nb <= VG_PAGG_CTA_BUCKETS && env_int("VGPU_PAGG_ATOMIC", 0) == 0;
+    /* per-CTA ranges: every position below 2^32 (n rows or fewer records) */
+    const int cta = nb <= VG_PAGG_CTA_BUCKETS && (uint64_t)n < ((uint64_t)1 << 32) &&
+                    env_int("VGPU_PAGG_ATOMIC", 0) == 0;
     uint64_t *cta_off = NULL;
     if (cta) {
         /* the kernel's geometry decides which rows each CTA counts */
@@ -672,6 +691,7 @@ static void pagg_batch(PAgg *pg, Plan *P, VgAggLaunch *L, const VgDBatch *db, in
     R->rec = (uint64_t *)vg_dmalloc((size_t)(total ? total : 1) * (size_t)pg->rw * 8 + 256);
     pg->rows += total;
     L->po.rec = R->rec;
+    L->po.total = total;
     if (n > 0) {
         const int rc = vgk_agg_launch_jit(L, n, vg_stream());
         if (rc <= 0) vg_fail("partitioned aggregation: %s", rc < 0 ? vgk_jit_error() : "plan not covered");
@@ -840,7 +860,10 @@ static VecBatch *pagg_end(PAgg *pg, VgAgg *A, Plan *P, VgAggLaunch *L) {
 
     Leaves lv;
     memset(&lv, 0, sizeof(lv));
+    double t0 = now_ms();
     pagg_reduce_level(pg, L, P, &B, nb, stage_off, &lv, 0);
+    g_pagg_ms[2] += now_ms() - t0;
+    t0 = now_ms();
 
     /* the NA-key group */
     uint32_t na_n = 0;
@@ -891,7 +914,12 @@ static VecBatch *pagg_end(PAgg *pg, VgAgg *A, Plan *P, VgAggLaunch *L) {
     vg_check_rc(vgk_pagg_emit(lv.n, d_leaf, d_leaf + lv.n, n_groups, has_na, total, B.st_key, B.st_ok,
                               (const double *const *)B.st_out, n_out, kout, kval, aout, aval, vg_stream()),
                 "partitioned aggregation emit");
+    vg_sync();
+    g_pagg_ms[3] += now_ms() - t0;
+    t0 = now_ms();
     vg_host_bufs_wait(pg->hb);
+    g_pagg_ms[4] += now_ms() - t0;
+    t0 = now_ms();
     const size_t need = (size_t)n_groups * 8;
     res->columns[0] = vg_download_column_into(VEC_INT64, kout, kval, n_groups, vg_host_bufs_take(pg->hb, 0, need));
     res->col_names[0] = vg_xstrdup(ga->key_names[0]);
@@ -903,6 +931,7 @@ static VecBatch *pagg_end(PAgg *pg, VgAgg *A, Plan *P, VgAggLaunch *L) {
     uint32_t w = 0;
     vg_d2h(&w, warn, 4);
     vg_sync();
+    g_pagg_ms[5] += now_ms() - t0;
     vg_warn_count((long)w);
     vg_dfree(ob);
     vg_dfree(d_leaf);
@@ -1043,9 +1072,15 @@ static VecBatch *agg_next(VecNode *self) {
     PAgg *pg = NULL;
     while (vg_pull(P.src, need, 0, &db)) {
         int64_t n_logical = db.d_sel ? db.sel_n : db.n_rows;
-        if (batch_idx == 0) pg = pagg_begin(A, &P, L, &db);
+        if (batch_idx == 0) {
+            const double t0 = now_ms();
+            pg = pagg_begin(A, &P, L, &db);
+            if (pg) g_pagg_ms[0] += now_ms() - t0;
+        }
         if (pg) {
+            const double t0 = now_ms();
             pagg_batch(pg, &P, L, &db, stream_pos, batch_idx);
+            g_pagg_ms[1] += now_ms() - t0;
             vg_dbatch_release(&db);
             stream_pos += n_logical;
             batch_idx++;

@@ -262,6 +262,7 @@ typedef struct {
      * are written as holes.  start[b]: bucket b's first position. */
     const uint64_t *cta_off;
     const uint64_t *start;
+    uint64_t total;               /* records of the region (no position at or past it is written) */
 } VgPartOut;
 
 /* flags word of a partition record that is a hole (no row) */
