@@ -537,6 +537,35 @@ def query_set_arm(args, eng, lib, dev):
     lib.vgpu_queryset_prepare.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
     lib.vgpu_queryset_run.argtypes = [C.c_void_p]
     lib.vgpu_queryset_free.argtypes = [C.c_void_p]
+    lib.vgpu_queryset_tune.restype = C.c_int
+    lib.vgpu_queryset_tune.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    lib.vgpu_queryset_prepare_with.restype = C.c_int
+    lib.vgpu_queryset_prepare_with.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]
+    torch.cuda.synchronize()
+
+    def timed_set(params):
+        # median of `steps` runs of a set prepared with params (None: the recorded tuning)
+        p = C.c_void_p()
+        rc = (lib.vgpu_queryset_prepare(arr, n_inst, C.byref(p)) if params is None
+              else lib.vgpu_queryset_prepare_with(arr, n_inst, C.byref(params), C.byref(p)))
+        if rc != 0:
+            raise RuntimeError(lib.vgpu_last_error().decode())
+        for _ in range(args.warmup):
+            lib.vgpu_queryset_run(p)
+        ts = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            lib.vgpu_queryset_run(p)
+            ts.append(time.perf_counter() - t0)
+        lib.vgpu_queryset_free(p)
+        return statistics.median(ts)
+    # the autotuner: every candidate timed on this set, the fastest recorded for its shape
+    tuning = W.SetTuning()
+    t0 = time.perf_counter()
+    if lib.vgpu_queryset_tune(arr, n_inst, 2, C.byref(tuning)) != 0:
+        raise RuntimeError(lib.vgpu_last_error().decode())
+    tune_s = time.perf_counter() - t0
+    default_s = timed_set(W.SetTuning(threads=512, table_mult=2, chunk_rows=65536))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     plan = C.c_void_p()
@@ -591,7 +620,9 @@ def query_set_arm(args, eng, lib, dev):
                                    "values N(0,1)" % n_inst, "input_rows": rows},
             "plain_path_queries_per_s": 1.0 / plain_s, "plain_path_sample": len(plain),
             "speedup_vs_plain": (n_inst / set_s) * plain_s, "rows_per_s": rows / set_s,
-            "prepare_s": prep_s, "data": "synthetic (seeded numpy / torch generators, seed 0)",
+            "prepare_s": prep_s, "autotune": dict(tuning.as_dict(), seconds=round(tune_s, 3),
+                                                  default_ms=round(default_s * 1e3, 3)),
+            "data": "synthetic (seeded numpy / torch generators, seed 0)",
             "result_checked": "256 sampled instances against torch"}
 
 

@@ -169,6 +169,30 @@ int  vgpu_queryset_prepare(const VgpuSetQuery *queries, int n_queries, void **pl
  * small, repeated build keys) with vgpu_last_error set. */
 int  vgpu_queryset_run(void *plan);
 void vgpu_queryset_free(void *plan);
+/* Autotuning of a set's launch parameters: every candidate (threads per
+ * CTA 256 / 512 / 1024, rows per work item 16Ki / 64Ki / 256Ki, table load
+ * <= 1/2 or 1/4) is prepared and timed on the set itself (best of `reps`
+ * runs after a warm-up; outputs are rewritten), and the fastest is
+ * recorded for the set's shape (instance counts per kind, total and
+ * largest instance rows, mean group cardinality, each as a power of two).
+ * vgpu_queryset_prepare then uses the recorded parameters for any set of
+ * that shape.  VGPU_TUNE_FILE names a file that keeps the records across
+ * processes.  vgpu_queryset_tuning: 1 and the record for the set's shape,
+ * or 0 and the defaults. */
+typedef struct {
+    int32_t threads;            /* per CTA */
+    int32_t table_mult;         /* table capacity >= table_mult x keys */
+    int64_t chunk_rows;         /* rows per work item */
+    double  ms;                 /* measured time of one run (0: defaults) */
+    int32_t candidates;         /* configurations timed */
+    char    shape[60];
+} VgpuSetTuning;
+int  vgpu_queryset_tune(const VgpuSetQuery *queries, int n_queries, int reps, VgpuSetTuning *out);
+int  vgpu_queryset_tuning(const VgpuSetQuery *queries, int n_queries, VgpuSetTuning *out);
+/* vgpu_queryset_prepare with explicit launch parameters (threads,
+ * chunk_rows, table_mult of `params`; NULL: the defaults 512, 64Ki, 2). */
+int  vgpu_queryset_prepare_with(const VgpuSetQuery *queries, int n_queries, const VgpuSetTuning *params,
+                                void **plan);
 
 /* ---- serving loop over resident tables (no reference counterpart) ---- */
 /* A server keeps tables resident (device pointers the caller keeps alive)

@@ -7,8 +7,8 @@
 //          (exact double sums: correctly rounded, as the node path)
 //   JOIN   inner_join(probe, build, key) over unique build keys: the
 //          (probe row, build row) pairs in probe row order
-// Instances are cut into work items of at most kChunk rows; persistent
-// CTAs (one per SM) take items from atomic counters:
+// Instances are cut into work items of at most `chunk` rows; persistent
+// CTAs take items from atomic counters:
 //   phase 0  empty every instance's table
 //   phase 1  group chunks aggregate into their instance's table; join
 //            build chunks insert their keys
@@ -17,11 +17,19 @@
 //   phase 3  join probe chunks write their pairs at the offset the
 //            instance's earlier chunks leave (probe order)
 // Every instance's table lives in one scratch block sized at prepare time;
-// small tables stay in L2 while their instance runs.
+// small tables stay in L2 while their instance runs.  Threads per CTA,
+// rows per work item and the tables' load factor are chosen per set shape
+// by vgpu_queryset_tune (measured on the set) and recorded.
 
 #include <algorithm>
+#include <chrono>
+#include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
 #include <vector>
 #include "k_set_dev.cuh"
 
@@ -29,8 +37,13 @@
 
 namespace {
 
-constexpr int kSetThreads = 512;
-constexpr int64_t kChunk = 65536;
+// Launch parameters of a query set; the defaults, or what
+// vgpu_queryset_tune measured fastest for sets of the same shape.
+struct Cfg {
+    int threads = 512;            // per CTA: 256, 512 or 1024
+    int64_t chunk = 65536;        // rows per work item (each instance's fan-out)
+    int cap_mult = 2;             // table capacity >= cap_mult x keys (load <= 1/cap_mult)
+};
 
 int ck(cudaError_t e, const char *what) { return check(e, what); }
 
@@ -59,11 +72,13 @@ struct Plan {
     cudaGraphExec_t exec;
     cudaStream_t stream;
     int grid;
+    Cfg cfg;
 };
 
 // ---------------------------------------------------------------------
 // phase 0: empty the tables
 // ---------------------------------------------------------------------
+template <int kSetThreads>
 __global__ void __launch_bounds__(kSetThreads) set_init_kernel(const Inst *inst, int n_inst) {
     for (int i = blockIdx.x; i < n_inst; i += gridDim.x) {
         const Inst &I = inst[i];
@@ -94,6 +109,7 @@ __global__ void __launch_bounds__(kSetThreads) set_init_kernel(const Inst *inst,
 // ---------------------------------------------------------------------
 // phase 1: aggregate / build
 // ---------------------------------------------------------------------
+template <int kSetThreads>
 __global__ void __launch_bounds__(kSetThreads) set_phase1_kernel(const Inst *inst, const Item *items, int n_items,
                                                                 uint32_t *ctr) {
     __shared__ int item;
@@ -132,6 +148,7 @@ __global__ void __launch_bounds__(kSetThreads) set_phase1_kernel(const Inst *ins
 // ---------------------------------------------------------------------
 // phase 2: group results / join match counts
 // ---------------------------------------------------------------------
+template <int kSetThreads>
 __global__ void __launch_bounds__(kSetThreads) set_phase2_kernel(const Inst *inst, const Item *items, int n_items,
                                                                 int64_t *chunk_cnt, uint32_t *ctr) {
     __shared__ int item;
@@ -177,6 +194,7 @@ __global__ void __launch_bounds__(kSetThreads) set_phase2_kernel(const Inst *ins
 // ---------------------------------------------------------------------
 // phase 3: join pairs in probe order
 // ---------------------------------------------------------------------
+template <int kSetThreads>
 __global__ void __launch_bounds__(kSetThreads) set_phase3_kernel(const Inst *inst, const Item *items, int n_items,
                                                                 const int64_t *chunk_cnt, uint32_t *ctr) {
     __shared__ int item;
@@ -221,6 +239,15 @@ __global__ void __launch_bounds__(kSetThreads) set_phase3_kernel(const Inst *ins
     }
 }
 
+// the four phases of a run, as captured into the set's graph
+template <int T>
+void capture_phases(Plan *P, int n, cudaStream_t st) {
+    set_init_kernel<T><<<P->grid, T, 0, st>>>(P->d_inst, n);
+    set_phase1_kernel<T><<<P->grid, T, 0, st>>>(P->d_inst, P->d_items1, P->n1, P->d_ctr);
+    set_phase2_kernel<T><<<P->grid, T, 0, st>>>(P->d_inst, P->d_items2, P->n2, P->d_chunk_cnt, P->d_ctr);
+    set_phase3_kernel<T><<<P->grid, T, 0, st>>>(P->d_inst, P->d_items3, P->n3, P->d_chunk_cnt, P->d_ctr);
+}
+
 int64_t pow2_at_least(int64_t x) {
     int64_t c = 64;
     while (c < x) c <<= 1;
@@ -234,7 +261,8 @@ extern "C" {
 void vg_set_error(const char *fmt, ...);
 void vgpu_queryset_free(void *plan);
 
-static int queryset_prepare(const VgpuSetQuery *qs, int n, void **plan_out) {
+static int queryset_prepare(const VgpuSetQuery *qs, int n, const Cfg &cfg, void **plan_out) {
+    const int64_t kChunk = cfg.chunk;
     *plan_out = nullptr;
     if (n <= 0 || !qs) { snprintf(g_err, sizeof(g_err), "vgpu_queryset_prepare: no queries"); return -1; }
     Plan *P = new Plan();
@@ -255,7 +283,7 @@ static int queryset_prepare(const VgpuSetQuery *qs, int n, void **plan_out) {
                 delete P;
                 return -1;
             }
-            I.cap = pow2_at_least(2 * (q.max_groups < q.n ? q.max_groups : (q.n > 0 ? q.n : 1)));
+            I.cap = pow2_at_least(cfg.cap_mult * (q.max_groups < q.n ? q.max_groups : (q.n > 0 ? q.n : 1)));
             bytes += (size_t)(I.cap + 1) * sizeof(GSlot);
             for (int64_t lo = 0, c = 0; lo < q.n; lo += kChunk, c++)
                 it1.push_back(Item{i, (int32_t)c, lo, lo + kChunk < q.n ? lo + kChunk : q.n});
@@ -268,7 +296,7 @@ static int queryset_prepare(const VgpuSetQuery *qs, int n, void **plan_out) {
                 delete P;
                 return -1;
             }
-            I.cap = pow2_at_least(2 * (q.n_build > 0 ? q.n_build : 1));
+            I.cap = pow2_at_least(cfg.cap_mult * (q.n_build > 0 ? q.n_build : 1));
             bytes += (size_t)(I.cap + 1) * sizeof(JSlot);
             for (int64_t lo = 0, c = 0; lo < q.n_build; lo += kChunk, c++)
                 it1.push_back(Item{i, (int32_t)c, lo, lo + kChunk < q.n_build ? lo + kChunk : q.n_build});
@@ -325,13 +353,13 @@ static int queryset_prepare(const VgpuSetQuery *qs, int n, void **plan_out) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    P->grid = sms > 0 ? sms * (2048 / kSetThreads) : 64;
+    P->grid = sms > 0 ? sms * (2048 / cfg.threads) : 64;
+    P->cfg = cfg;
     if (ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "batch capture")) { vgpu_queryset_free(P); return -1; }
     cudaMemsetAsync(P->d_ctr, 0, 32, st);
-    set_init_kernel<<<P->grid, kSetThreads, 0, st>>>(P->d_inst, n);
-    set_phase1_kernel<<<P->grid, kSetThreads, 0, st>>>(P->d_inst, P->d_items1, P->n1, P->d_ctr);
-    set_phase2_kernel<<<P->grid, kSetThreads, 0, st>>>(P->d_inst, P->d_items2, P->n2, P->d_chunk_cnt, P->d_ctr);
-    set_phase3_kernel<<<P->grid, kSetThreads, 0, st>>>(P->d_inst, P->d_items3, P->n3, P->d_chunk_cnt, P->d_ctr);
+    if (cfg.threads == 256) capture_phases<256>(P, n, st);
+    else if (cfg.threads == 1024) capture_phases<1024>(P, n, st);
+    else capture_phases<512>(P, n, st);
     cudaError_t e = cudaStreamEndCapture(st, &P->graph);
     if (ck(e, "batch capture end") || ck(cudaGraphInstantiate(&P->exec, P->graph, 0), "batch graph")) {
         vgpu_queryset_free(P);
@@ -364,11 +392,203 @@ void vgpu_queryset_free(void *plan) {
     delete P;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------
+// autotuning: launch parameters measured per query-set shape
+// ---------------------------------------------------------------------
+namespace {
+
+struct Tuned {
+    Cfg cfg;
+    double ms;
+    int candidates;
+};
+
+std::mutex g_tune_mu;
+std::map<std::string, Tuned> g_tuned;
+bool g_tune_loaded = false;
+
+int lg2(double x) { return x < 1.0 ? 0 : (int)std::floor(std::log2(x)); }
+
+// Shape of a set: how many group and join instances, total and largest
+// instance rows, mean group cardinality -- each as a power of two.
+std::string shape_of(const VgpuSetQuery *qs, int n) {
+    int64_t ng = 0, nj = 0, rows = 0, maxr = 0;
+    double card = 0.0;
+    for (int i = 0; i < n; i++) {
+        const VgpuSetQuery &q = qs[i];
+        const int64_t r = q.n + (q.kind == VGPU_SET_JOIN ? q.n_build : 0);
+        rows += r;
+        maxr = r > maxr ? r : maxr;
+        if (q.kind == VGPU_SET_GROUP) {
+            ng++;
+            card += (double)(q.max_groups < q.n ? q.max_groups : (q.n > 0 ? q.n : 1));
+        } else {
+            nj++;
+        }
+    }
+    char buf[96];
+    snprintf(buf, sizeof(buf), "g%d.j%d.r%d.m%d.c%d", lg2((double)ng), lg2((double)nj), lg2((double)rows),
+             lg2((double)maxr), ng ? lg2(card / (double)ng) : 0);
+    return buf;
+}
+
+// Recorded tunings persist in the file named by VGPU_TUNE_FILE (one line
+// per measurement: shape threads chunk_rows table_mult ms candidates;
+// the last line of a shape wins).
+void load_tunings() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char *path = getenv("VGPU_TUNE_FILE");
+    if (!path || !*path) return;
+    FILE *f = fopen(path, "r");
+    if (!f) return;
+    char shape[96];
+    Tuned t;
+    long long chunk = 0;
+    while (fscanf(f, "%95s %d %lld %d %lf %d", shape, &t.cfg.threads, &chunk, &t.cfg.cap_mult, &t.ms, &t.candidates) ==
+           6) {
+        t.cfg.chunk = chunk;
+        if ((t.cfg.threads == 256 || t.cfg.threads == 512 || t.cfg.threads == 1024) && chunk >= 1024 &&
+            (t.cfg.cap_mult == 2 || t.cfg.cap_mult == 4))
+            g_tuned[shape] = t;
+    }
+    fclose(f);
+}
+
+void save_tuning(const std::string &shape, const Tuned &t) {
+    const char *path = getenv("VGPU_TUNE_FILE");
+    if (!path || !*path) return;
+    FILE *f = fopen(path, "a");
+    if (!f) return;
+    fprintf(f, "%s %d %lld %d %.6f %d\n", shape.c_str(), t.cfg.threads, (long long)t.cfg.chunk, t.cfg.cap_mult, t.ms,
+            t.candidates);
+    fclose(f);
+}
+
+Cfg config_for(const VgpuSetQuery *qs, int n, bool *tuned) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    load_tunings();
+    auto it = g_tuned.find(shape_of(qs, n));
+    *tuned = it != g_tuned.end();
+    return *tuned ? it->second.cfg : Cfg();
+}
+
+void fill(VgpuSetTuning *out, const std::string &shape, const Cfg &c, double ms, int candidates) {
+    if (!out) return;
+    memset(out, 0, sizeof(*out));
+    out->threads = c.threads;
+    out->table_mult = c.cap_mult;
+    out->chunk_rows = c.chunk;
+    out->ms = ms;
+    out->candidates = candidates;
+    snprintf(out->shape, sizeof(out->shape), "%s", shape.c_str());
+}
+
+// one run of a prepared plan, in milliseconds of wall time (the run waits)
+double time_run(void *plan) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (queryset_run(plan) != 0) return -1.0;
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+extern "C" {
+
 int vgpu_queryset_prepare(const VgpuSetQuery *qs, int n, void **plan) {
     g_err[0] = 0;
-    const int rc = queryset_prepare(qs, n, plan);
+    bool tuned = false;
+    const Cfg cfg = (qs && n > 0) ? config_for(qs, n, &tuned) : Cfg();
+    const int rc = queryset_prepare(qs, n, cfg, plan);
     if (rc) vg_set_error("%s", g_err);
     return rc;
+}
+
+int vgpu_queryset_prepare_with(const VgpuSetQuery *qs, int n, const VgpuSetTuning *params, void **plan) {
+    g_err[0] = 0;
+    Cfg cfg;
+    if (params) {
+        if ((params->threads != 256 && params->threads != 512 && params->threads != 1024) ||
+            params->chunk_rows < 1024 || (params->table_mult != 2 && params->table_mult != 4)) {
+            vg_set_error("vgpu_queryset_prepare_with: threads 256/512/1024, chunk_rows >= 1024, table_mult 2 or 4");
+            return -1;
+        }
+        cfg.threads = params->threads;
+        cfg.chunk = params->chunk_rows;
+        cfg.cap_mult = params->table_mult;
+    }
+    const int rc = queryset_prepare(qs, n, cfg, plan);
+    if (rc) vg_set_error("%s", g_err);
+    return rc;
+}
+
+int vgpu_queryset_tuning(const VgpuSetQuery *qs, int n, VgpuSetTuning *out) {
+    if (!qs || n <= 0) return 0;
+    const std::string shape = shape_of(qs, n);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    load_tunings();
+    auto it = g_tuned.find(shape);
+    if (it == g_tuned.end()) {
+        fill(out, shape, Cfg(), 0.0, 0);
+        return 0;
+    }
+    fill(out, shape, it->second.cfg, it->second.ms, it->second.candidates);
+    return 1;
+}
+
+// Times every candidate configuration on the set itself (one warm-up run
+// and the best of `reps` timed runs each; the queries' outputs are simply
+// rewritten) and records the fastest for the set's shape.
+int vgpu_queryset_tune(const VgpuSetQuery *qs, int n, int reps, VgpuSetTuning *out) {
+    g_err[0] = 0;
+    if (!qs || n <= 0) {
+        vg_set_error("vgpu_queryset_tune: no queries");
+        return -1;
+    }
+    if (reps < 1) reps = 1;
+    const int threads[] = {256, 512, 1024};
+    const int64_t chunks[] = {16384, 65536, 262144};
+    const int mults[] = {2, 4};
+    Tuned best;
+    best.ms = -1.0;
+    best.candidates = 0;
+    for (int t : threads)
+        for (int64_t c : chunks)
+            for (int m : mults) {
+                Cfg cfg;
+                cfg.threads = t;
+                cfg.chunk = c;
+                cfg.cap_mult = m;
+                void *plan = nullptr;
+                if (queryset_prepare(qs, n, cfg, &plan) != 0) continue;
+                double ms = time_run(plan);        // warm-up (and a check that it runs)
+                for (int r = 0; r < reps && ms >= 0.0; r++) {
+                    const double x = time_run(plan);
+                    ms = (r == 0 || x < ms) ? x : ms;
+                }
+                vgpu_queryset_free(plan);
+                if (ms < 0.0) continue;
+                best.candidates++;
+                if (best.ms < 0.0 || ms < best.ms) {
+                    best.cfg = cfg;
+                    best.ms = ms;
+                }
+            }
+    if (best.ms < 0.0) {
+        vg_set_error("vgpu_queryset_tune: no configuration ran (%s)", g_err);
+        return -1;
+    }
+    const std::string shape = shape_of(qs, n);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        load_tunings();
+        g_tuned[shape] = best;
+        save_tuning(shape, best);
+    }
+    fill(out, shape, best.cfg, best.ms, best.candidates);
+    return 0;
 }
 
 int vgpu_queryset_run(void *plan) {

@@ -181,6 +181,16 @@ class SetQuery(C.Structure):
                 ("out_build", C.c_void_p), ("out_rows", C.c_void_p)]
 
 
+class SetTuning(C.Structure):
+    """Mirror of VgpuSetTuning (include/vgpu.h)."""
+    _fields_ = [("threads", C.c_int32), ("table_mult", C.c_int32), ("chunk_rows", C.c_int64), ("ms", C.c_double),
+                ("candidates", C.c_int32), ("shape", C.c_char * 60)]
+
+    def as_dict(self):
+        return {"threads": self.threads, "table_mult": self.table_mult, "chunk_rows": self.chunk_rows,
+                "ms": round(self.ms, 4), "candidates": self.candidates, "shape": self.shape.decode()}
+
+
 def gen_query_set(torch, n_inst, seed, device, median_rows=20_000, sigma=1.5, cap_rows=5_000_000,
                   max_card=100_000):
     """n_inst instances: rows ~ LogNormal(ln median_rows, sigma) capped,
