@@ -501,6 +501,23 @@ def workload_arm(args):
     torch.cuda.synchronize()
     lib.vgpu_profile_enable(0)
     ms = e0.elapsed_time(e1) / args.steps
+    # where the host time of one query goes: plan construction, next_batch
+    # (the whole aggregation and the copy of its result), freeing the result
+    host = None
+    if args.workload == "high_card":
+        from vectra_gb300.plan import Tbl
+        t0 = time.perf_counter()
+        q = (Tbl(eng, W.device_source(lib, cols, n)[0]).group_by("key")
+             .summarise(temp_dir="tmp", s=("sum", "x"), m=("mean", "x"), lo=("min", "y"), hi=("max", "y"), n=("n",)))
+        node = q._take()
+        t1 = time.perf_counter()
+        b = eng.next_batch(node)
+        t2 = time.perf_counter()
+        eng.free_batch(b)
+        t3 = time.perf_counter()
+        eng.free_node(node)
+        host = {"plan_ms": round((t1 - t0) * 1e3, 3), "next_batch_ms": round((t2 - t1) * 1e3, 3),
+                "free_result_ms": round((t3 - t2) * 1e3, 3)}
     nl = C.c_ulonglong(0)
     agg_ms = lib.vgpu_profile_ms(0, C.byref(nl))
     n5 = C.c_ulonglong(0)
@@ -514,7 +531,8 @@ def workload_arm(args):
             "algorithmic_bytes": algo, "hbm_gbs_whole_query": algo / (ms * 1e-3) / 1e9,
             "frac_of_hbm_peak": algo / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
             "agg_kernel_ms": agg_ms / max(1, args.steps * 1), "agg_launches": nl.value,
-            "partitioned_path": bool(pagg_runs), "reduce_kernel_ms": reduce_ms / max(1, args.steps),
+            "partitioned_path": bool(pagg_runs), "host_split": host,
+            "reduce_kernel_ms": reduce_ms / max(1, args.steps),
             "finish_kernel_ms": finish_ms / max(1, args.steps), "result_checked": True,
             "partitioned_phases_ms": dict(zip(["sketch", "partition", "reduce", "compact", "host_buffers", "download"],
                                               [round((lib.vgpu_pagg_phase_ms(i) - phase0[i]) / args.steps, 3)

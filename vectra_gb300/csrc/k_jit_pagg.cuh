@@ -7,8 +7,8 @@
 // are contiguous key ranges, ascending.  Here one CTA takes one bucket at a
 // time, in bucket order from a ticket:
 //   1. every record's key is looked up in a shared-memory hash table that
-//      hands out dense group ids (the group's accumulators are initialised
-//      by the thread that claims the key), and the record's values update
+//      hands out dense group ids (all G groups' accumulators are
+//      initialised when the bucket starts), and the record's values update
 //      that group's accumulators with shared-memory atomics, in the same
 //      representation as the fused kernel's cache (exact double sums as
 //      32-bit digits in a window; a value outside the window goes to a
@@ -175,10 +175,9 @@ VG_DEV double finish(const char *sm, int g, const double *fs, const double *fc, 
     return vg_i2f(v);
 }
 
-// Group id of key (claiming one, and initialising its accumulators, if
-// the key is new); -1 when the CTA holds G groups already (the bucket
-// overflows) or a bounded wait expired (err set).
-VG_DEV int find(char *sm, uint64_t key, int *s_ng, int *s_ovf, uint32_t *err);
+// Group id of key; -1 when the CTA holds G groups already (the bucket
+// overflows).
+VG_DEV int find(char *sm, uint64_t key, int *s_ng, int *s_ovf, uint32_t *dead);
 
 }  // namespace vgp
 
@@ -189,48 +188,46 @@ VG_DEV uint32_t vgp_finish(const char *sm, int g, const VgPaggReduce &B, uint64_
 
 namespace vgp {
 
-VG_DEV int find(char *sm, uint64_t key, int *s_ng, int *s_ovf, uint32_t *err) {
+// Nobody waits: a thread that finds no entry for its key takes a private
+// group id first (with the other lanes of its warp that reach that point,
+// one counter update; every id's accumulators were initialised when the
+// bucket started), writes the group's key, and only then publishes the id
+// into an empty slot with one CAS.  A thread
+// that loses the CAS to the same key marks its private id dead (skipped
+// when the groups are ordered) and uses the winner's; one that loses it to
+// another key keeps its initialised id for the next empty slot.
+VG_DEV int find(char *sm, uint64_t key, int *s_ng, int *s_ovf, uint32_t *dead) {
     uint32_t *hid = (uint32_t *)(sm + VGP_OFF_HID);
     uint64_t *gk = (uint64_t *)(sm + VGP_OFF_GKEY);
     uint32_t s = (uint32_t)vg_mix64(key) & (uint32_t)(S - 1);
+    int mine = -1;
     for (int probe = 0; probe < S; probe++) {
         uint32_t v = *(volatile uint32_t *)(hid + s);
         if (v == kEmptyId) {
-            const uint32_t prev = atomicCAS(hid + s, kEmptyId, kBusyId);
-            if (prev == kEmptyId) {
-                // the lanes that claimed a slot here together take their
-                // ids with one counter update
+            if (mine < 0) {
                 const uint32_t m = __activemask();
                 const int lane = threadIdx.x & 31;
                 const int leader = __ffs(m) - 1;
                 int base = 0;
                 if (lane == leader) base = atomicAdd(s_ng, __popc(m));
                 base = __shfl_sync(m, base, leader);
-                const int id = base + __popc(m & ((1u << lane) - 1u));
-                if (id >= G) {
-                    *(volatile int *)s_ovf = 1;          // the slot stays busy; the bucket is abandoned
+                mine = base + __popc(m & ((1u << lane) - 1u));
+                if (mine >= G) {
+                    *(volatile int *)s_ovf = 1;
                     return -1;
                 }
-                gk[id] = key;
-                vgp_init(sm, id);
+                gk[mine] = key;                           // (its accumulators start initialised)
                 __threadfence_block();
-                atomicExch(hid + s, (uint32_t)id);
-                return id;
             }
+            const uint32_t prev = atomicCAS(hid + s, kEmptyId, (uint32_t)mine);
+            if (prev == kEmptyId) return mine;
             v = prev;
         }
-        int spins = 0;
-        while (v == kBusyId) {
-            if (*(volatile int *)s_ovf) return -1;
-            if (++spins > VG_SPIN_LIMIT) {
-                atomicOr(err, VG_ERR_WAIT);
-                *(volatile int *)s_ovf = 1;
-                return -1;
-            }
-            v = *(volatile uint32_t *)(hid + s);
-        }
         __threadfence_block();
-        if (*(volatile uint64_t *)(gk + v) == key) return (int)v;
+        if (*(volatile uint64_t *)(gk + v) == key) {
+            if (mine >= 0) atomicOr(dead + (mine >> 5), 1u << (mine & 31));
+            return (int)v;
+        }
         s = (s + 1) & (uint32_t)(S - 1);
     }
     *(volatile int *)s_ovf = 1;
@@ -242,8 +239,9 @@ VG_DEV int find(char *sm, uint64_t key, int *s_ng, int *s_ovf, uint32_t *err) {
 extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const __grid_constant__ VgPaggReduce B) {
     using namespace vgp;
     extern __shared__ __align__(16) char sm[];
-    __shared__ int s_bucket, s_ng, s_ovf, s_crowded;
+    __shared__ int s_bucket, s_ng, s_ovf, s_crowded, s_live;
     __shared__ uint32_t s_wsum[32];
+    __shared__ uint32_t s_dead[(G + 31) / 32];        // group ids lost to a racing insert of the same key
     uint32_t *hid = (uint32_t *)(sm + VGP_OFF_HID);
     const uint64_t *gk = (const uint64_t *)(sm + VGP_OFF_GKEY);
     for (;;) {
@@ -253,6 +251,8 @@ extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const _
             s_ovf = 0;
         }
         for (int i = threadIdx.x; i < S; i += blockDim.x) hid[i] = kEmptyId;
+        for (int i = threadIdx.x; i < (G + 31) / 32; i += blockDim.x) s_dead[i] = 0;
+        for (int g = threadIdx.x; g < G; g += blockDim.x) vgp_init(sm, g);   // every group's accumulators, coalesced
         __syncthreads();
         const int b = s_bucket;
         if (b >= B.n_buckets) break;
@@ -282,12 +282,12 @@ extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const _
                     }
                 }
                 if (!(w0[1] & VG_PAGG_HOLE)) {                 // holes: positions no row took
-                    const int g0 = find(sm, w0[0], &s_ng, &s_ovf, B.err);
+                    const int g0 = find(sm, w0[0], &s_ng, &s_ovf, s_dead);
                     if (g0 < 0) break;
                     vgp_acc(sm, g0, w0, B, sbase + (uint64_t)g0);
                 }
                 if (two && !(w1[1] & VG_PAGG_HOLE)) {
-                    const int g1 = find(sm, w1[0], &s_ng, &s_ovf, B.err);
+                    const int g1 = find(sm, w1[0], &s_ng, &s_ovf, s_dead);
                     if (g1 < 0) break;
                     vgp_acc(sm, g1, w1, B, sbase + (uint64_t)g1);
                 }
@@ -306,7 +306,7 @@ extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const _
         //    the top bits of each key's offset in the bucket's key range,
         //    insertion sort within a bin; a bitonic sort if some bin is
         //    crowded (keys outside the range the buckets were cut for)
-        const int n = s_ng;
+        const int n_ids = s_ng;                           // ids handed out (<= G: no overflow)
         uint32_t *ord = hid;
         uint32_t *cnt = hid + G;                          // kBins counters after the ids
         const uint64_t lo = B.omin + ((uint64_t)b << B.shift);
@@ -316,13 +316,28 @@ extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const _
             const uint64_t d = ow < lo ? 0ull : ((ow - lo) >> sh);
             return d >= (uint64_t)kBins ? kBins - 1 : (int)d;
         };
+        auto live = [&](int g) { return !((s_dead[g >> 5] >> (g & 31)) & 1u); };
         for (int i = threadIdx.x; i < kBins; i += blockDim.x) cnt[i] = 0;
-        if (threadIdx.x == 0) s_crowded = 0;
+        if (threadIdx.x == 0) {
+            s_crowded = 0;
+            s_live = 0;
+        }
         __syncthreads();
-        for (int g = threadIdx.x; g < n; g += blockDim.x) atomicAdd(cnt + bin_of((uint32_t)g), 1u);
+        {
+            unsigned c = 0;
+            for (int g = threadIdx.x; g < n_ids; g += blockDim.x)
+                if (live(g)) {
+                    atomicAdd(cnt + bin_of((uint32_t)g), 1u);
+                    c++;
+                }
+            c = __reduce_add_sync(0xFFFFFFFFu, c);
+            if ((threadIdx.x & 31) == 0 && c) atomicAdd(&s_live, (int)c);
+        }
         __syncthreads();
+        const int n = s_live;
         block_exclusive_scan(cnt, kBins, s_wsum);
-        for (int g = threadIdx.x; g < n; g += blockDim.x) ord[atomicAdd(cnt + bin_of((uint32_t)g), 1u)] = (uint32_t)g;
+        for (int g = threadIdx.x; g < n_ids; g += blockDim.x)
+            if (live(g)) ord[atomicAdd(cnt + bin_of((uint32_t)g), 1u)] = (uint32_t)g;
         __syncthreads();
         for (int i = threadIdx.x; i < kBins; i += blockDim.x) {
             const int e = (int)cnt[i], st = i ? (int)cnt[i - 1] : 0;
@@ -344,9 +359,10 @@ extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const _
         }
         __syncthreads();
         if (s_crowded) {
+            // the live ids are ord[0..n) already (bin order); sort them outright
             int P2 = 1;
             while (P2 < n) P2 <<= 1;
-            for (int i = threadIdx.x; i < P2; i += blockDim.x) ord[i] = i < n ? (uint32_t)i : kEmptyId;
+            for (int i = n + threadIdx.x; i < P2; i += blockDim.x) ord[i] = kEmptyId;
             __syncthreads();
             for (int size = 2; size <= P2; size <<= 1) {
                 for (int stride = size >> 1; stride > 0; stride >>= 1) {

@@ -599,7 +599,7 @@ static PAgg *pagg_begin(VgAgg *A, Plan *P, VgAggLaunch *L, const VgDBatch *db) {
      * number of groups: their fresh pages are faulted in by background
      * threads during the device passes */
     const double est = d * 1.04 + 4096.0;
-    if (est * 8.0 >= (double)(64 << 20) && est < 4e9)
+    if (est * 8.0 >= (double)(4 << 20) && est < 4e9)
         pg->hb = vg_host_bufs_begin(1 + A->ga.n_aggs, (size_t)est * 8);
     return pg;
 }

@@ -361,7 +361,7 @@ static void *touch_pages(void *arg) {
 
 static void prefault(void *p, size_t n) {
     enum { kMaxThreads = 8 };
-    if (n < ((size_t)64 << 20)) return;
+    if (n < ((size_t)4 << 20)) return;
     long cpus = sysconf(_SC_NPROCESSORS_ONLN);
     int nt = cpus >= 2 * kMaxThreads ? kMaxThreads : (int)(cpus > 1 ? cpus / 2 : 1);
     if (nt < 2) return;
