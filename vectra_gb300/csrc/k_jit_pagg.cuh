@@ -246,7 +246,7 @@ extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const _
     const uint64_t *gk = (const uint64_t *)(sm + VGP_OFF_GKEY);
     for (;;) {
         if (threadIdx.x == 0) {
-            s_bucket = (int)atomicAdd(B.ticket, 1u);
+            s_bucket = B.bucket_base + (int)atomicAdd(B.ticket, 1u);
             s_ng = 0;
             s_ovf = 0;
         }
@@ -255,7 +255,7 @@ extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const _
         for (int g = threadIdx.x; g < G; g += blockDim.x) vgp_init(sm, g);   // every group's accumulators, coalesced
         __syncthreads();
         const int b = s_bucket;
-        if (b >= B.n_buckets) break;
+        if (b >= B.bucket_base + B.n_buckets) break;
         const uint64_t sbase = B.stage_off[b];
         // 1. records -> groups (two records per thread in flight)
         for (int r = 0; r < B.n_regions; r++) {

@@ -8,8 +8,9 @@
 //   scan     bucket offsets and cursors;
 //   refine   a bucket with more groups than one reducer CTA holds is split
 //            by its own key range into 256 sub-buckets (records copied);
-//   emit     the staged group results of every bucket, in bucket order,
-//            compacted into the output columns with validity bitmaps.
+//   emit     the staged group results of a run of buckets, in bucket
+//            order, compacted into output columns (validity bits OR-ed in at
+//            the run's first output row).
 //
 // The first step proper (rows -> records) is the run-time specialised
 // fused kernel in partition mode (jit_agg.cu), the second (records ->
@@ -341,6 +342,7 @@ struct EmitArgs {
     int32_t has_na;
     int32_t n_out;
     uint64_t na_stage;
+    uint64_t out_base;            // validity bit of output row j: out_base + j (OR-ed into zeroed words)
     const uint64_t *st_key;
     const uint32_t *st_ok;
     const double *st_out[VG_MAX_OUTS];
@@ -370,14 +372,20 @@ __global__ void __launch_bounds__(256) emit_kernel(const __grid_constant__ EmitA
             src = A.na_stage;
         }
         if (in) A.key_out[j] = na ? 0ull : A.st_key[src];
-        const uint32_t km = __ballot_sync(0xFFFFFFFFu, in && !na);
-        if (lane == 0) A.key_valid[j >> 5] = km;
+        // a warp's 32 validity bits land at bit out_base + j0 (j0 = j - lane)
+        const uint64_t bit0 = A.out_base + (uint64_t)(j - lane);
+        auto put = [&](uint32_t *v, uint32_t m) {
+            if (lane != 0 || !m) return;
+            const uint64_t w = ((uint64_t)m) << (bit0 & 31);
+            atomicOr(v + (bit0 >> 5), (uint32_t)w);
+            if (w >> 32) atomicOr(v + (bit0 >> 5) + 1, (uint32_t)(w >> 32));
+        };
+        put(A.key_valid, __ballot_sync(0xFFFFFFFFu, in && !na));
         const uint32_t okb = in ? A.st_ok[src] : 0u;
         for (int o = 0; o < A.n_out; o++) {
             const bool ok = (okb >> o) & 1u;
             if (in) A.out[o][j] = ok ? A.st_out[o][src] : 0.0;
-            const uint32_t m = __ballot_sync(0xFFFFFFFFu, in && ok);
-            if (lane == 0) A.out_valid[o][j >> 5] = m;
+            put(A.out_valid[o], __ballot_sync(0xFFFFFFFFu, in && ok));
         }
     }
 }
@@ -563,7 +571,7 @@ int vgk_pagg_rec_split(const VgPaggReduce *R, int b, uint64_t rows, uint64_t omi
 int vgk_pagg_emit(int64_t n_leaves, const uint64_t *d_leaf_stage, const uint64_t *d_leaf_out, int64_t n_groups,
                   int has_na, uint64_t na_stage, const uint64_t *st_key, const uint32_t *st_ok,
                   const double *const *st_out, int n_out, uint64_t *key_out, uint32_t *key_valid, double **out,
-                  uint32_t **out_valid, vg_stream_t s) {
+                  uint32_t **out_valid, uint64_t out_base, vg_stream_t s) {
     if (n_groups <= 0) return 0;
     if (n_out > VG_MAX_OUTS) {
         snprintf(g_err, sizeof(g_err), "pagg emit: too many outputs");
@@ -578,6 +586,7 @@ int vgk_pagg_emit(int64_t n_leaves, const uint64_t *d_leaf_stage, const uint64_t
     A.has_na = has_na;
     A.n_out = n_out;
     A.na_stage = na_stage;
+    A.out_base = out_base;
     A.st_key = st_key;
     A.st_ok = st_ok;
     A.key_out = key_out;

@@ -515,6 +515,7 @@ typedef struct {
     uint32_t *counters;            /* spill counters of the partition launch (never used) */
     uint64_t rows;                 /* records written (upper bound) */
     VgHostBufs *hb;                /* result columns, faulted in while the device works */
+    size_t hb_bytes;               /* bytes of each */
 } PAgg;
 
 /* Host wall time of the partitioned path's phases, summed since load
@@ -600,7 +601,10 @@ static PAgg *pagg_begin(VgAgg *A, Plan *P, VgAggLaunch *L, const VgDBatch *db) {
      * threads during the device passes */
     const double est = d * 1.04 + 4096.0;
     if (est * 8.0 >= (double)(4 << 20) && est < 4e9)
-        pg->hb = vg_host_bufs_begin(1 + A->ga.n_aggs, (size_t)est * 8);
+    {
+        pg->hb_bytes = (size_t)est * 8;
+        pg->hb = vg_host_bufs_begin(1 + A->ga.n_aggs, pg->hb_bytes);
+    }
     return pg;
 }
 
@@ -730,44 +734,53 @@ static void leaves_push(Leaves *lv, uint64_t stage, uint64_t gc) {
     lv->n++;
 }
 
-/* Runs the reducer over the buckets of R (staging positions stage_off) and
- * appends the leaves in key order, splitting overflowing buckets. */
-static void pagg_reduce_level(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggReduce *B, int nb,
-                              const uint64_t *d_stage_off, Leaves *lv, int depth) {
-    uint32_t *gc = (uint32_t *)vg_dmalloc((size_t)nb * 8 + 256);
-    uint32_t *ovf = gc + nb;
-    unsigned int *ticket = (unsigned int *)vg_dmalloc(256);
+/* The reducer over buckets [b0, b0 + n) of B (a level of nb buckets;
+ * gc: 2 nb words of device scratch, groups then overflow flags). */
+static void pagg_reduce_launch(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggReduce *B, const uint64_t *d_stage_off,
+                               uint32_t *gc, int nb, unsigned int *ticket, int b0, int n) {
     vg_dmemset(ticket, 0, 4);
-    B->n_buckets = nb;
+    B->bucket_base = b0;
+    B->n_buckets = n;
     B->stage_off = d_stage_off;
     B->gc = gc;
-    B->ovf = ovf;
+    B->ovf = gc + nb;
     B->ticket = ticket;
     if (vgk_pagg_reduce(L, P->fin, P->n_out, pg->G, B, vg_stream()) != 0)
         vg_fail("partitioned aggregation reduce: %s", vgk_jit_error());
-    uint32_t *h = (uint32_t *)vg_xcalloc((size_t)nb * 2, 4);
-    uint64_t *hs = (uint64_t *)vg_xcalloc((size_t)nb, 8);
+}
+
+static void pagg_reduce_level(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggReduce *B, int nb,
+                              const uint64_t *d_stage_off, Leaves *lv, int depth);
+
+/* After the launch over [b0, b0 + n): the leaves of those buckets in key
+ * order; a bucket with more groups than a CTA holds is split by its own
+ * key range into up to 256 sub-buckets, reduced in turn (recursively). */
+static void pagg_reduce_collect(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggReduce *B,
+                                const uint64_t *d_stage_off, const uint32_t *gc, int nb, int b0, int n, Leaves *lv,
+                                int depth) {
+    uint32_t *h = (uint32_t *)vg_xcalloc((size_t)n * 2 + 1, 4);
+    uint64_t *hs = (uint64_t *)vg_xcalloc((size_t)n + 1, 8);
     uint32_t err = 0;
-    vg_d2h(h, gc, (size_t)nb * 8);
-    vg_d2h(hs, d_stage_off, (size_t)nb * 8);
+    vg_d2h(h, gc + b0, (size_t)n * 4);
+    vg_d2h(h + n, gc + nb + b0, (size_t)n * 4);
+    vg_d2h(hs, d_stage_off + b0, (size_t)n * 8);
     vg_d2h(&err, B->err, 4);
     vg_sync();
     if (err) vg_fail("partitioned aggregation: reduce kernel error (code %u)", err);
-    vg_dfree(ticket);
-    for (int b = 0; b < nb; b++) {
-        if (!h[nb + b]) {
-            leaves_push(lv, hs[b], h[b]);
+    for (int i = 0; i < n; i++) {
+        const int b = b0 + i;
+        if (!h[n + i]) {
+            leaves_push(lv, hs[i], h[i]);
             continue;
         }
-        /* more groups than a CTA holds: split this bucket by its key range */
         if (depth > 16) vg_fail("partitioned aggregation: bucket split did not converge");
         uint64_t rows = 0;
         for (int r = 0; r < B->n_regions; r++) {
-            uint64_t a = 0, e = 0;
-            vg_d2h(&a, B->roff[r] + b, 8);
-            vg_d2h(&e, B->rend[r] + b, 8);
+            uint64_t ra = 0, re = 0;
+            vg_d2h(&ra, B->roff[r] + b, 8);
+            vg_d2h(&re, B->rend[r] + b, 8);
             vg_sync();
-            rows += e - a;
+            rows += re - ra;
         }
         unsigned long long *mm = (unsigned long long *)vg_dmalloc(256);
         uint64_t hmm[3];
@@ -789,7 +802,7 @@ static void pagg_reduce_level(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggRed
         vg_d2h(&err, pg->err, 4);
         vg_sync();
         if (err) vg_fail("partitioned aggregation: split kernel error (code %u)", err);
-        for (int i = 0; i < nb2; i++) hoff[i] += hs[b];
+        for (int j = 0; j < nb2; j++) hoff[j] += hs[i];
         uint64_t *st2 = (uint64_t *)vg_dmalloc((size_t)nb2 * 8 + 256);
         vg_h2d(st2, hoff, (size_t)nb2 * 8);
         VgPaggReduce B2 = *B;
@@ -811,7 +824,38 @@ static void pagg_reduce_level(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggRed
     }
     free(h);
     free(hs);
+}
+
+/* Every bucket of a level, in one launch. */
+static void pagg_reduce_level(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggReduce *B, int nb,
+                              const uint64_t *d_stage_off, Leaves *lv, int depth) {
+    uint32_t *gc = (uint32_t *)vg_dmalloc((size_t)nb * 8 + 256);
+    unsigned int *ticket = (unsigned int *)vg_dmalloc(256);
+    pagg_reduce_launch(pg, L, P, B, d_stage_off, gc, nb, ticket, 0, nb);
+    pagg_reduce_collect(pg, L, P, B, d_stage_off, gc, nb, 0, nb, lv, depth);
+    vg_dfree(ticket);
     vg_dfree(gc);
+}
+
+/* Staging positions and output rows of the leaves [l0, l1) on the device:
+ * n + 1 staging positions, then n + 1 output rows relative to the first
+ * leaf's; *rows: their groups. */
+static uint64_t *leaf_arrays(const Leaves *lv, int64_t l0, int64_t l1, int64_t *rows) {
+    const int64_t n = l1 - l0;
+    uint64_t *h = (uint64_t *)vg_xcalloc((size_t)(2 * n + 2), 8);
+    int64_t run = 0;
+    for (int64_t i = 0; i < n; i++) {
+        h[i] = lv->stage[l0 + i];
+        h[n + 1 + i] = (uint64_t)run;
+        run += (int64_t)lv->gc[l0 + i];
+    }
+    h[2 * n + 1] = (uint64_t)run;
+    uint64_t *d = (uint64_t *)vg_dmalloc((size_t)(2 * n + 2) * 8 + 256);
+    vg_h2d(d, h, (size_t)(2 * n + 2) * 8);
+    vg_sync();
+    free(h);
+    *rows = run;
+    return d;
 }
 
 /* Steps 3 and 4: the result batch. */
@@ -860,12 +904,89 @@ static VecBatch *pagg_end(PAgg *pg, VgAgg *A, Plan *P, VgAggLaunch *L) {
 
     Leaves lv;
     memset(&lv, 0, sizeof(lv));
+    const int n_cols = 1 + n_out;
+    int64_t n_groups = 0;
+    VecBatch *res = NULL;
+    void *hcol[VG_MAX_OUTS + 1];
+    memset(hcol, 0, sizeof(hcol));
+    /* output validity: one bitmap per column for every possible row; each
+     * emit ORs its bits in from its first output row */
+    const size_t vwords = (size_t)((cap + 31) / 32) + 2;
+    uint32_t *dval = (uint32_t *)vg_dmalloc((size_t)n_cols * a256(vwords * 4) + 256);
+    vg_dmemset(dval, 0, (size_t)n_cols * a256(vwords * 4));
+    uint32_t *vcol[VG_MAX_OUTS + 1];
+    for (int c = 0; c < n_cols; c++) vcol[c] = (uint32_t *)((char *)dval + (size_t)c * a256(vwords * 4));
+
+    /* The buckets in W runs.  Run w's groups are emitted into a device
+     * buffer and copied into the host result columns on the copy stream
+     * while run w + 1 is reduced.  The host columns were faulted in during
+     * the earlier passes, sized from the distinct-key estimate (grown if the
+     * count turns out larger). */
+    const int W = (pg->hb && nb >= 2048) ? 8 : 1;
+    uint64_t *hso = (uint64_t *)vg_xcalloc((size_t)nb + 1, 8);
+    vg_d2h(hso, stage_off, (size_t)(nb + 1) * 8);
+    vg_sync();
+    uint64_t wmax = 1;
+    for (int w = 0; w < W; w++) {
+        const int b0 = (int)((int64_t)nb * w / W), b1 = (int)((int64_t)nb * (w + 1) / W);
+        if (hso[b1] - hso[b0] > wmax) wmax = hso[b1] - hso[b0];
+    }
+    double *wbuf = (double *)vg_dmalloc((size_t)2 * n_cols * a256(wmax * 8) + 256);
+    size_t hcap = 0;
+    if (W > 1) {
+        vg_host_bufs_wait(pg->hb);
+        for (int c = 0; c < n_cols; c++) hcol[c] = vg_host_bufs_take(pg->hb, c, 0);
+        hcap = pg->hb_bytes / 8;
+    }
+    uint32_t *gc = (uint32_t *)vg_dmalloc((size_t)nb * 8 + 256);
+    unsigned int *tickets = (unsigned int *)vg_dmalloc((size_t)W * 4 + 256);
     double t0 = now_ms();
-    pagg_reduce_level(pg, L, P, &B, nb, stage_off, &lv, 0);
-    g_pagg_ms[2] += now_ms() - t0;
+    double t_emit = 0.0, t_copy = 0.0;
+    pagg_reduce_launch(pg, L, P, &B, stage_off, gc, nb, tickets, 0, (int)((int64_t)nb / W));
+    for (int w = 0; w < W; w++) {
+        const int b0 = (int)((int64_t)nb * w / W), b1 = (int)((int64_t)nb * (w + 1) / W);
+        const int64_t l0 = lv.n;
+        pagg_reduce_collect(pg, L, P, &B, stage_off, gc, nb, b0, b1 - b0, &lv, 0);
+        if (W == 1) break;
+        const double te = now_ms();
+        int64_t rows = 0;
+        uint64_t *d_leaf = leaf_arrays(&lv, l0, lv.n, &rows);
+        double *wb[VG_MAX_OUTS + 1];
+        for (int c = 0; c < n_cols; c++)
+            wb[c] = (double *)((char *)wbuf + (size_t)((w & 1) * n_cols + c) * a256(wmax * 8));
+        vg_check_rc(vgk_pagg_emit(lv.n - l0, d_leaf, d_leaf + (lv.n - l0) + 1, rows, 0, 0, B.st_key, B.st_ok,
+                                  (const double *const *)B.st_out, n_out, (uint64_t *)wb[0], vcol[0], wb + 1, vcol + 1,
+                                  (uint64_t)n_groups, vg_stream()),
+                    "partitioned aggregation emit");
+        vg_copy_after_main();                         /* the copies below wait for this emit only */
+        if (w + 1 < W) {
+            const int c0 = b1, c1 = (int)((int64_t)nb * (w + 2) / W);
+            pagg_reduce_launch(pg, L, P, &B, stage_off, gc, nb, tickets + w + 1, c0, c1 - c0);
+        }
+        t_emit += now_ms() - te;
+        const double tc = now_ms();
+        if ((size_t)(n_groups + rows) > hcap) {       /* more groups than estimated: grow the host columns */
+            size_t ncap = (size_t)(n_groups + rows) * 5 / 4 + 4096;
+            for (int c = 0; c < n_cols; c++) {
+                void *q = realloc(hcol[c], ncap * 8);
+                if (!q) vg_fail("out of host memory for the result");
+                hcol[c] = q;
+            }
+            hcap = ncap;
+        }
+        for (int c = 0; c < n_cols; c++)
+            vg_d2h_copy((char *)hcol[c] + (size_t)n_groups * 8, wb[c], (size_t)rows * 8);
+        vg_copy_sync();
+        vg_dfree(d_leaf);
+        t_copy += now_ms() - tc;
+        n_groups += rows;
+    }
+    g_pagg_ms[2] += now_ms() - t0 - t_emit - t_copy;
+    g_pagg_ms[3] += t_emit;
+    g_pagg_ms[5] += t_copy;
     t0 = now_ms();
 
-    /* the NA-key group */
+    /* the NA-key group, last */
     uint32_t na_n = 0;
     vg_d2h(&na_n, pg->na.gt.n_used, 4);
     vg_sync();
@@ -884,61 +1005,81 @@ static VecBatch *pagg_end(PAgg *pg, VgAgg *A, Plan *P, VgAggLaunch *L) {
                     "NA group");
         has_na = 1;
     }
-
-    /* leaf offsets in the output */
-    int64_t ng = 0;
-    uint64_t *hout = (uint64_t *)vg_xcalloc((size_t)lv.n + 1, 8);
-    for (int64_t i = 0; i < lv.n; i++) {
-        hout[i] = (uint64_t)ng;
-        ng += (int64_t)lv.gc[i];
+    if (W == 1) {
+        /* one run: every group (and the NA group) emitted at once */
+        int64_t rows = 0;
+        uint64_t *d_leaf = leaf_arrays(&lv, 0, lv.n, &rows);
+        const int64_t ng = rows + has_na;
+        size_t per = a256((size_t)ng * 8 + 8);
+        char *ob = (char *)vg_dmalloc(per * (size_t)n_cols + 256);
+        double *oc[VG_MAX_OUTS + 1];
+        for (int c = 0; c < n_cols; c++) oc[c] = (double *)(ob + per * (size_t)c);
+        vg_check_rc(vgk_pagg_emit(lv.n, d_leaf, d_leaf + lv.n + 1, ng, has_na, total, B.st_key, B.st_ok,
+                                  (const double *const *)B.st_out, n_out, (uint64_t *)oc[0], vcol[0], oc + 1, vcol + 1,
+                                  0, vg_stream()),
+                    "partitioned aggregation emit");
+        vg_sync();
+        g_pagg_ms[3] += now_ms() - t0;
+        t0 = now_ms();
+        vg_host_bufs_wait(pg->hb);
+        g_pagg_ms[4] += now_ms() - t0;
+        t0 = now_ms();
+        n_groups = ng;
+        res = vg_batch_alloc(n_cols, n_groups);
+        const size_t need = (size_t)n_groups * 8;
+        for (int c = 0; c < n_cols; c++) {
+            void *dst = vg_host_bufs_take(pg->hb, c, need);
+            if (!dst) dst = vg_xcalloc(need ? need : 1, 1);
+            vg_d2h(dst, oc[c], need);
+            res->columns[c] = vg_host_column(c == 0 ? VEC_INT64 : VEC_DOUBLE, n_groups, dst, vcol[c]);
+        }
+        vg_sync();
+        vg_dfree(d_leaf);
+        vg_dfree(ob);
+    } else {
+        if (has_na) {
+            /* one more run: the NA group alone */
+            double *wb[VG_MAX_OUTS + 1];
+            for (int c = 0; c < n_cols; c++) wb[c] = (double *)((char *)wbuf + (size_t)c * a256(wmax * 8));
+            uint64_t *d_leaf = (uint64_t *)vg_dmalloc(256);
+            vg_dmemset(d_leaf, 0, 16);
+            vg_check_rc(vgk_pagg_emit(0, d_leaf, d_leaf, 1, 1, total, B.st_key, B.st_ok,
+                                      (const double *const *)B.st_out, n_out, (uint64_t *)wb[0], vcol[0], wb + 1,
+                                      vcol + 1, (uint64_t)n_groups, vg_stream()),
+                        "partitioned aggregation emit");
+            if ((size_t)(n_groups + 1) > hcap) {
+                for (int c = 0; c < n_cols; c++) {
+                    void *q = realloc(hcol[c], (size_t)(n_groups + 1) * 8);
+                    if (!q) vg_fail("out of host memory for the result");
+                    hcol[c] = q;
+                }
+            }
+            for (int c = 0; c < n_cols; c++) vg_d2h((char *)hcol[c] + (size_t)n_groups * 8, wb[c], 8);
+            vg_sync();
+            vg_dfree(d_leaf);
+            n_groups += 1;
+        }
+        res = vg_batch_alloc(n_cols, n_groups);
+        for (int c = 0; c < n_cols; c++) {
+            res->columns[c] = vg_host_column(c == 0 ? VEC_INT64 : VEC_DOUBLE, n_groups, hcol[c], vcol[c]);
+            hcol[c] = NULL;
+        }
     }
-    hout[lv.n] = (uint64_t)ng;
-    const int64_t n_groups = ng + has_na;
-    uint64_t *d_leaf = (uint64_t *)vg_dmalloc((size_t)(2 * lv.n + 1) * 8 + 256);
-    if (lv.n) vg_h2d(d_leaf, lv.stage, (size_t)lv.n * 8);
-    vg_h2d(d_leaf + lv.n, hout, (size_t)(lv.n + 1) * 8);
-
-    int n_cols = ga->n_keys + n_out;
-    VecBatch *res = vg_batch_alloc(n_cols, n_groups);
-    size_t wb = (size_t)((n_groups + 31) / 32) * 4;
-    size_t per = a256((size_t)n_groups * 8 + 8) + a256(wb + 8);
-    char *ob = (char *)vg_dmalloc(per * (size_t)n_cols + 256);
-    uint64_t *kout = (uint64_t *)ob;
-    uint32_t *kval = (uint32_t *)((char *)kout + a256((size_t)n_groups * 8 + 8));
-    double *aout[VG_MAX_OUTS];
-    uint32_t *aval[VG_MAX_OUTS];
-    for (int j = 0; j < n_out; j++) {
-        aout[j] = (double *)(ob + per * (size_t)(1 + j));
-        aval[j] = (uint32_t *)((char *)aout[j] + a256((size_t)n_groups * 8 + 8));
-    }
-    vg_check_rc(vgk_pagg_emit(lv.n, d_leaf, d_leaf + lv.n, n_groups, has_na, total, B.st_key, B.st_ok,
-                              (const double *const *)B.st_out, n_out, kout, kval, aout, aval, vg_stream()),
-                "partitioned aggregation emit");
-    vg_sync();
-    g_pagg_ms[3] += now_ms() - t0;
-    t0 = now_ms();
-    vg_host_bufs_wait(pg->hb);
-    g_pagg_ms[4] += now_ms() - t0;
-    t0 = now_ms();
-    const size_t need = (size_t)n_groups * 8;
-    res->columns[0] = vg_download_column_into(VEC_INT64, kout, kval, n_groups, vg_host_bufs_take(pg->hb, 0, need));
     res->col_names[0] = vg_xstrdup(ga->key_names[0]);
-    for (int j = 0; j < n_out; j++) {
-        res->columns[1 + j] =
-            vg_download_column_into(VEC_DOUBLE, aout[j], aval[j], n_groups, vg_host_bufs_take(pg->hb, 1 + j, need));
-        res->col_names[1 + j] = vg_xstrdup(ga->agg_specs[j].output_name);
-    }
+    for (int j = 0; j < n_out; j++) res->col_names[1 + j] = vg_xstrdup(ga->agg_specs[j].output_name);
     uint32_t w = 0;
     vg_d2h(&w, warn, 4);
     vg_sync();
     g_pagg_ms[5] += now_ms() - t0;
     vg_warn_count((long)w);
-    vg_dfree(ob);
-    vg_dfree(d_leaf);
+    vg_dfree(tickets);
+    vg_dfree(gc);
+    vg_dfree(wbuf);
+    vg_dfree(dval);
+    free(hso);
     vg_dfree(warn);
     vg_dfree(blk);
     vg_dfree(stage_off);
-    free(hout);
     free(lv.stage);
     free(lv.gc);
     return res;

@@ -169,6 +169,56 @@ void vg_d2h(void *dst, const void *src, size_t bytes) {
     if (e != cudaSuccess) vg_fail("device to host copy failed: %s", cudaGetErrorString(e));
 }
 
+/* A second stream for result copies that overlap device work on the main
+ * stream: vg_copy_after_main() makes it wait for everything queued on the
+ * main stream so far; vg_d2h_copy() copies on it (into pageable memory the
+ * call returns when the copy is done). */
+static cudaStream_t g_copy_stream = NULL;
+
+static cudaStream_t copy_stream(void) {
+    if (!g_copy_stream) {
+        cudaError_t e = cudaStreamCreateWithFlags(&g_copy_stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) vg_fail("copy stream: %s", cudaGetErrorString(e));
+    }
+    return g_copy_stream;
+}
+
+void vg_copy_after_main(void) {
+    cudaEvent_t ev;
+    cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ev, (cudaStream_t)vg_stream());
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(copy_stream(), ev, 0);
+    if (e != cudaSuccess) vg_fail("copy stream ordering: %s", cudaGetErrorString(e));
+    cudaEventDestroy(ev);
+}
+
+void vg_d2h_copy(void *dst, const void *src, size_t bytes) {
+    if (!bytes) return;
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, copy_stream());
+    if (e != cudaSuccess) vg_fail("device to host copy failed: %s", cudaGetErrorString(e));
+}
+
+void vg_copy_sync(void) {
+    if (!g_copy_stream) return;
+    cudaError_t e = cudaStreamSynchronize(g_copy_stream);
+    if (e != cudaSuccess) vg_fail("copy stream: %s", cudaGetErrorString(e));
+}
+
+/* A host column over values already on the host (malloc-owned, taken
+ * over) with its validity copied from the device bitmap d_valid. */
+VecArray vg_host_column(int type, int64_t n, void *values, const uint32_t *d_valid) {
+    VecArray a;
+    memset(&a, 0, sizeof(a));
+    a.type = (VecType)type;
+    a.length = n;
+    a.owns_data = 1;
+    a.validity = (uint8_t *)vg_xcalloc((size_t)vg_vbytes(n), 1);
+    if (type == VEC_BOOL) a.buf.bln = (uint8_t *)values;
+    else a.buf.i64 = (int64_t *)values;
+    if (n > 0) vg_d2h(a.validity, d_valid, (size_t)vg_vbytes(n));
+    return a;
+}
+
 void vg_dmemset(void *dst, int v, size_t bytes) {
     if (!bytes) return;
     cudaError_t e = cudaMemsetAsync(dst, v, bytes, (cudaStream_t)vg_stream());

@@ -283,9 +283,11 @@ typedef struct {
  * [roff[r][b], rend[r][b]). */
 typedef struct {
     int32_t n_regions;
-    int32_t n_buckets;
+    int32_t n_buckets;            /* buckets [bucket_base, bucket_base + n_buckets) */
     int32_t rec_words;
     int32_t n_out;
+    int32_t bucket_base;
+    int32_t pad_base;
     uint64_t omin;                /* bucket b holds the order words [omin + (b << shift), +2^shift) */
     int32_t shift;
     int32_t pad_shift;
@@ -531,7 +533,7 @@ int vgk_pagg_rec_split(const VgPaggReduce *R, int b, uint64_t rows, uint64_t omi
 int vgk_pagg_emit(int64_t n_leaves, const uint64_t *d_leaf_stage, const uint64_t *d_leaf_out, int64_t n_groups,
                   int has_na, uint64_t na_stage, const uint64_t *st_key, const uint32_t *st_ok,
                   const double *const *st_out, int n_out, uint64_t *key_out, uint32_t *key_valid, double **out,
-                  uint32_t **out_valid, vg_stream_t s);
+                  uint32_t **out_valid, uint64_t out_base, vg_stream_t s);
 /* the results of one group-table slot written to staging position pos */
 int vgk_group_stage(const VgGroupTable *gt, const VgFinish *fin, int n_out, int64_t slot, uint64_t *st_key,
                     uint32_t *st_ok, double *const *st_out, uint64_t pos, uint32_t *d_warn, vg_stream_t s);
