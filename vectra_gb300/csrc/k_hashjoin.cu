@@ -288,9 +288,9 @@ __global__ void jt_insert_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, in
 // (4 bytes per key: small enough to stay in L2) with the validity bits of
 // its two payload values in bits 29 and 30, and reports min, max and count
 // of the valid values of int64 payload columns (mm, 3 words per column).
-// If a key repeats, one of its rows survives; pass 2 finds that out.  Pass
-// 3 writes every payload entry in key order (coalesced), gathering the
-// payload values by row.
+// If a key repeats, one of its rows survives; pass 2 finds that out while
+// the surviving rows write their keys' entries (reading their payload values
+// in row order), and the entries of keys no row has are cleared last.
 constexpr int32_t kRowBits = 29;                       // build rows < 2^29
 constexpr uint32_t kRowMask = (1u << kRowBits) - 1u;
 
@@ -357,35 +357,48 @@ __global__ void jt_rows_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int3
     }
 }
 
-// Pass 2: a row whose key records another row shares its key with it
-// (counters[3] = 1: duplicates, the payload does not apply).
-__global__ void jt_rows_verify_kernel(const uint32_t *rowof, int64_t n, const int32_t *rslot, uint32_t *counters) {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool dup = false;
-    if (r < n) {
-        const int32_t d = rslot[r];
-        if (d >= 0) dup = (__ldg(rowof + d) & kRowMask) != (uint32_t)r;
+// Pass 2 (as verify + gather in one): each row that its key's entry names
+// writes the entry, reading its payload values where they are (coalesced);
+// a row whose key names another row reports a repeated key.  Entries of
+// keys no row has are written by jt_pay_absent_kernel.
+__global__ void jt_pay_scatter_kernel(VgJoinTable jt, const uint32_t *rowof, const int32_t *rslot, int64_t n,
+                                      PayArgs P, uint32_t *counters) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t r0 = (int64_t)blockIdx.x * blockDim.x; r0 < n; r0 += stride) {
+        const int64_t r = r0 + threadIdx.x;
+        bool dup = false;
+        if (r < n) {
+            const int32_t d = rslot[r];
+            if (d >= 0) {
+                const uint32_t v = __ldg(rowof + d);
+                if ((v & kRowMask) != (uint32_t)r) {
+                    dup = true;
+                } else {
+                    const uint32_t meta = 1u | (((v >> kRowBits) & 3u) << 1);
+                    const ulonglong2 a = make_ulonglong2((uint64_t)jt.dmin + (uint64_t)d,
+                                                         (unsigned long long)(uint32_t)r |
+                                                             ((unsigned long long)meta << 32));
+                    ulonglong2 b = make_ulonglong2(0ull, 0ull);
+                    if (P.n_cols > 0) b.x = vg_load_bits(P.c0, r);
+                    if (P.n_cols > 1) b.y = vg_load_bits(P.c1, r);
+                    ulonglong2 *o = (ulonglong2 *)(P.pay + d);
+                    o[0] = a;
+                    o[1] = b;
+                }
+            }
+        }
+        if (__any_sync(0xFFFFFFFFu, dup) && (threadIdx.x & 31) == 0) atomicOr(counters + 3, 1u);
     }
-    if (__any_sync(0xFFFFFFFFu, dup) && (threadIdx.x & 31) == 0) atomicOr(counters + 3, 1u);
 }
 
-// Pass 3: the payload entries in key order.
-__global__ void jt_pay_gather_kernel(VgJoinTable jt, const uint32_t *rowof, PayArgs P) {
+// The entries of keys no build row has (and the extra entry at cap): absent.
+__global__ void jt_pay_absent_kernel(VgJoinTable jt, const uint32_t *rowof, PayArgs P) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d <= jt.cap; d += stride) {
-        const uint32_t v = d < jt.cap ? __ldg(rowof + d) : 0xFFFFFFFFu;
-        ulonglong2 a = make_ulonglong2(0ull, 0ull), b = make_ulonglong2(0ull, 0ull);
-        if (v != 0xFFFFFFFFu) {
-            const int64_t r = v & kRowMask;
-            const uint32_t meta = 1u | (((v >> kRowBits) & 3u) << 1);
-            a = make_ulonglong2((uint64_t)jt.dmin + (uint64_t)d, (unsigned long long)(uint32_t)r |
-                                                                  ((unsigned long long)meta << 32));
-            if (P.n_cols > 0) b.x = vg_load_bits(P.c0, r);
-            if (P.n_cols > 1) b.y = vg_load_bits(P.c1, r);
-        }
+        if (d < jt.cap && __ldg(rowof + d) != 0xFFFFFFFFu) continue;
         ulonglong2 *o = (ulonglong2 *)(P.pay + d);
-        o[0] = a;
-        o[1] = b;
+        o[0] = make_ulonglong2(0ull, 0ull);
+        o[1] = make_ulonglong2(0ull, 0ull);
     }
 }
 
@@ -614,22 +627,23 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
     if (P.pay && n_build >= ((int64_t)1 << kRowBits)) P.pay = nullptr;   // too many rows for rowof: no payload
     if (P.pay) {
         // direct table with a payload copy: rows record themselves per key,
-        // a check pass looks for repeated keys, then the payload is written
-        // in key order; the slot table is derived later, only if something
-        // reads it (vgk_join_slots_from_payload)
+        // then each recorded row writes its key's entry with its payload
+        // values (a row whose key records another row reports a repeated
+        // key) and the entries of absent keys are cleared; the slot table is
+        // derived later, only if something reads it
+        // (vgk_join_slots_from_payload)
         uint32_t *rowof = (uint32_t *)p;
         jt_init_kernel<<<1, 32, 0, st>>>(*jt, counters, nullptr, 0, mm);
         vg_launch_counter++;
         if (check(cudaMemsetAsync(rowof, 0xFF, (size_t)jt->cap * 4, st), "join build")) return -1;
         vg_prof_begin(VG_PROF_JOIN_BUILD, st);
         if (n_build > 0) {
-            const unsigned g = (unsigned)((n_build + 255) / 256);
             jt_rows_direct_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(*jt, K, n_build, rslot, counters, P,
                                                                            rowof, mm);
-            jt_rows_verify_kernel<<<g, 256, 0, st>>>(rowof, n_build, rslot, counters);
+            jt_pay_scatter_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(*jt, rowof, rslot, n_build, P, counters);
             vg_launch_counter += 2;
         }
-        jt_pay_gather_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, rowof, P);
+        jt_pay_absent_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, rowof, P);
         vg_launch_counter++;
         vg_prof_end(VG_PROF_JOIN_BUILD, st);
         uint32_t hc[4] = {0, 0, 0, 0};

@@ -335,7 +335,9 @@ static int cache_slots_for(const VgAggLaunch *L) {
 static int run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_logical) {
     int sms = vgk_num_sms();
     /* spill space for this launch */
-    int64_t need_rows = n_logical + 65536;
+    /* a dense cache holds every group: nothing misses it, so rows never
+     * spill (a spill would be reported, not lost) */
+    int64_t need_rows = L->dense ? 65536 : n_logical + 65536;
     if (!S->counters) S->counters = (uint32_t *)vg_dmalloc(256);
     if (g_spill_rows_cap < need_rows) {
         vg_dfree(g_spill_rows);
@@ -1233,7 +1235,7 @@ static VecBatch *agg_next(VecNode *self) {
         int settled = 0;
         for (int64_t off = 0, n = 0; off < n_logical; off += n) {
             n = n_logical - off;
-            if (!settled && n > kChunk) n = kChunk;
+            if (!settled && n > kChunk && !L->dense) n = kChunk;   /* dense: the table cannot grow */
             if (db.d_sel) {
                 for (int j = 0; j < P.pset.n; j++) L->pcols[j] = db.cols[P.pset.idx[j]];
                 L->n_rows = db.n_rows;
