@@ -302,12 +302,21 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
         for (int v = 0; v < nv; v++) fmt(s, "    const InVal v%d = %s;\n", v, value(*vals[v]).c_str());
         s += "    uint64_t fl = 0;\n";
         for (int v = 0; v < nv; v++) fmt(s, "    if (v%d.ok) fl |= %lluull;\n", v, 1ull << v);
-        fmt(s, "    ulonglong2 *r = (ulonglong2 *)(L.po.rec + pos * %dull);\n", rw);
-        s += "    r[0] = make_ulonglong2(key, fl);\n";
-        for (int v = 0; v < nv; v += 2) {
-            if (v + 1 < nv) fmt(s, "    r[%d] = make_ulonglong2(v%d.bits, v%d.bits);\n", 1 + v / 2, v, v + 1);
-            else fmt(s, "    r[%d] = make_ulonglong2(v%d.bits, 0ull);\n", 1 + v / 2, v);
-        }
+        // the record's words: 32-byte stores when records are a multiple of
+        // 4 words (so every record starts 32-byte aligned), else 16-byte ones
+        std::vector<std::string> w;
+        w.push_back("key");
+        w.push_back("fl");
+        for (int v = 0; v < nv; v++) w.push_back("v" + std::to_string(v) + ".bits");
+        while ((int)w.size() < rw) w.push_back("0ull");
+        fmt(s, "    uint64_t *r = L.po.rec + pos * %dull;\n", rw);
+        int i = 0;
+        if (rw % 4 == 0)
+            for (; i + 4 <= rw; i += 4)
+                fmt(s, "    vg_st256(r + %d, %s, %s, %s, %s);\n", i, w[i].c_str(), w[i + 1].c_str(), w[i + 2].c_str(),
+                    w[i + 3].c_str());
+        for (; i < rw; i += 2)
+            fmt(s, "    *(ulonglong2 *)(r + %d) = make_ulonglong2(%s, %s);\n", i, w[i].c_str(), w[i + 1].c_str());
     }
     s += "    (void)L; (void)pos; (void)key; (void)X; (void)j;\n}\n";
 

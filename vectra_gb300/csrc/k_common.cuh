@@ -39,6 +39,15 @@ VG_DEV uint32_t vg_ld_acquire(const uint32_t *p) {
     return v;
 }
 
+// 32-byte (256-bit) global store / streaming load of four 64-bit words;
+// the address is 32-byte aligned (sm_100 family).
+VG_DEV void vg_st256(void *p, uint64_t a, uint64_t b, uint64_t c, uint64_t d) {
+    asm volatile("st.global.v4.b64 [%0], {%1, %2, %3, %4};" ::"l"(p), "l"(a), "l"(b), "l"(c), "l"(d) : "memory");
+}
+VG_DEV void vg_ld256_cs(const void *p, uint64_t &a, uint64_t &b, uint64_t &c, uint64_t &d) {
+    asm volatile("ld.global.cs.v4.b64 {%0, %1, %2, %3}, [%4];" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
+}
+
 VG_DEV bool vg_valid(const VgCol &c, int64_t r) {
     r += c.voff;
     return c.valid == nullptr || ((__ldg(c.valid + (r >> 5)) >> (r & 31)) & 1u);

@@ -175,6 +175,23 @@ VG_DEV double finish(const char *sm, int g, const double *fs, const double *fc, 
     return vg_i2f(v);
 }
 
+// Record p (RW words): 32-byte streaming loads when records are a
+// multiple of 4 words (every record 32-byte aligned), else 16-byte ones.
+VG_DEV void load_record(const ulonglong2 *rec, uint64_t p, uint64_t (&w)[RW]) {
+    const uint64_t *q = (const uint64_t *)rec + p * RW;
+    int i = 0;
+    if (RW % 4 == 0) {
+#pragma unroll
+        for (; i + 4 <= RW; i += 4) vg_ld256_cs(q + i, w[i], w[i + 1], w[i + 2], w[i + 3]);
+    }
+#pragma unroll
+    for (; i < RW; i += 2) {
+        const ulonglong2 a = __ldcs((const ulonglong2 *)(q + i));
+        w[i] = a.x;
+        w[i + 1] = a.y;
+    }
+}
+
 // Group id of key; -1 when the CTA holds G groups already (the bucket
 // overflows).
 VG_DEV int find(char *sm, uint64_t key, int *s_ng, int *s_ovf, uint32_t *dead);
@@ -267,20 +284,8 @@ extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const _
                 if (*(volatile int *)&s_ovf) break;
                 uint64_t w0[RW], w1[RW];
                 const bool two = p + 1 < hi;
-#pragma unroll
-                for (int i = 0; i < RW / 2; i++) {
-                    const ulonglong2 a = __ldcs(rec + (p * RW) / 2 + i);
-                    w0[2 * i] = a.x;
-                    w0[2 * i + 1] = a.y;
-                }
-                if (two) {
-#pragma unroll
-                    for (int i = 0; i < RW / 2; i++) {
-                        const ulonglong2 a = __ldcs(rec + ((p + 1) * RW) / 2 + i);
-                        w1[2 * i] = a.x;
-                        w1[2 * i + 1] = a.y;
-                    }
-                }
+                load_record(rec, p, w0);
+                if (two) load_record(rec, p + 1, w1);
                 if (!(w0[1] & VG_PAGG_HOLE)) {                 // holes: positions no row took
                     const int g0 = find(sm, w0[0], &s_ng, &s_ovf, s_dead);
                     if (g0 < 0) break;

@@ -695,6 +695,8 @@ static void pagg_batch(PAgg *pg, Plan *P, VgAggLaunch *L, const VgDBatch *db, in
     vg_d2h(&total, R->off + nb, 8);
     vg_sync();
     R->rec = (uint64_t *)vg_dmalloc((size_t)(total ? total : 1) * (size_t)pg->rw * 8 + 256);
+    if ((uintptr_t)R->rec & 31)       /* records are written and read as aligned 32-byte words */
+        vg_fail("partitioned aggregation: record area not 32-byte aligned");
     pg->rows += total;
     L->po.rec = R->rec;
     L->po.total = total;
@@ -797,6 +799,7 @@ static void pagg_reduce_collect(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggR
         uint64_t *off2 = (uint64_t *)vg_dmalloc((size_t)(nb2 + 1) * 8 + 256);
         unsigned long long *cur2 = (unsigned long long *)vg_dmalloc((size_t)nb2 * 8 + 256);
         uint64_t *rec2 = (uint64_t *)vg_dmalloc((size_t)(rows ? rows : 1) * (size_t)pg->rw * 8 + 256);
+        if ((uintptr_t)rec2 & 31) vg_fail("partitioned aggregation: record area not 32-byte aligned");
         vg_check_rc(vgk_pagg_rec_split(B, b, rows, hmm[0], shift2, nb2, cnt2, off2, cur2, rec2, pg->err, vg_stream()),
                     "partitioned aggregation split");
         uint64_t *hoff = (uint64_t *)vg_xcalloc((size_t)nb2 + 1, 8);
