@@ -489,7 +489,7 @@ def workload_arm(args):
     pagg_runs = lib.vgpu_pagg_runs() - pagg_before
     lib.vgpu_pagg_phase_ms.restype = C.c_double
     lib.vgpu_pagg_phase_ms.argtypes = [C.c_int]
-    phase0 = [lib.vgpu_pagg_phase_ms(i) for i in range(6)]
+    phase0 = [lib.vgpu_pagg_phase_ms(i) for i in range(7)]
     lib.vgpu_profile_reset()
     lib.vgpu_profile_enable(1)
     stream = torch.cuda.current_stream(dev)
@@ -501,6 +501,7 @@ def workload_arm(args):
     torch.cuda.synchronize()
     lib.vgpu_profile_enable(0)
     ms = e0.elapsed_time(e1) / args.steps
+    phases = [round((lib.vgpu_pagg_phase_ms(i) - phase0[i]) / args.steps, 3) for i in range(7)]
     # where the host time of one query goes: plan construction, next_batch
     # (the whole aggregation and the copy of its result), freeing the result
     host = None
@@ -534,9 +535,8 @@ def workload_arm(args):
             "partitioned_path": bool(pagg_runs), "host_split": host,
             "reduce_kernel_ms": reduce_ms / max(1, args.steps),
             "finish_kernel_ms": finish_ms / max(1, args.steps), "result_checked": True,
-            "partitioned_phases_ms": dict(zip(["sketch", "partition", "reduce", "compact", "host_buffers", "download"],
-                                              [round((lib.vgpu_pagg_phase_ms(i) - phase0[i]) / args.steps, 3)
-                                               for i in range(6)])) if pagg_runs else None,
+            "partitioned_phases_ms": dict(zip(["sketch", "partition", "reduce", "compact", "host_buffers", "download",
+                                               "aggregation"], phases)) if pagg_runs else None,
             "timed": "the node C API producing the host result batch (malloc-owned columns), without "
                      "conversion to numpy"}
 

@@ -103,7 +103,8 @@ long        vgpu_warning_count(void);
 unsigned long long vgpu_pagg_runs(void);
 /* Host wall time (ms, summed since load) of the partitioned path's phases:
  * 0 sketch, 1 partition pass, 2 bucket reducer, 3 compaction into the
- * output columns, 4 waiting for the host result buffers, 5 copy to host. */
+ * output columns, 4 waiting for the host result buffers, 5 copy to host,
+ * 6 the whole next_batch call of the aggregation. */
 double      vgpu_pagg_phase_ms(int phase);
 
 /* Optional kernel timing: CUDA events recorded on the launching stream

@@ -525,8 +525,8 @@ typedef struct {
  * device work): 0 sketch and setup, 1 partition (hist, scan, partition
  * kernel), 2 bucket reducer (and splits), 3 NA group and compaction into
  * the output columns, 4 waiting for the host result buffers, 5 copying
- * the result to the host. */
-static double g_pagg_ms[6];
+ * the result to the host; 6 the whole aggregation (its next_batch call). */
+static double g_pagg_ms[7];
 
 static double now_ms(void) {
     struct timespec ts;
@@ -534,7 +534,7 @@ static double now_ms(void) {
     return (double)ts.tv_sec * 1e3 + (double)ts.tv_nsec * 1e-6;
 }
 
-double vgpu_pagg_phase_ms(int phase) { return phase >= 0 && phase < 6 ? g_pagg_ms[phase] : 0.0; }
+double vgpu_pagg_phase_ms(int phase) { return phase >= 0 && phase < 7 ? g_pagg_ms[phase] : 0.0; }
 
 static int env_int(const char *name, int dflt) {
     const char *e = getenv(name);
@@ -939,7 +939,8 @@ static VecBatch *pagg_end(PAgg *pg, VgAgg *A, Plan *P, VgAggLaunch *L) {
     double *wbuf = (double *)vg_dmalloc((size_t)2 * n_cols * a256(wmax * 8) + 256);
     size_t hcap = 0;
     if (W > 1) {
-        vg_host_bufs_wait(pg->hb);
+        /* the columns are taken now and filled from the front; each run's
+         * copy waits only for the pages it writes */
         for (int c = 0; c < n_cols; c++) hcol[c] = vg_host_bufs_take(pg->hb, c, 0);
         hcap = pg->hb_bytes / 8;
     }
@@ -969,8 +970,13 @@ static VecBatch *pagg_end(PAgg *pg, VgAgg *A, Plan *P, VgAggLaunch *L) {
             pagg_reduce_launch(pg, L, P, &B, stage_off, gc, nb, tickets + w + 1, c0, c1 - c0);
         }
         t_emit += now_ms() - te;
-        const double tc = now_ms();
-        if ((size_t)(n_groups + rows) > hcap) {       /* more groups than estimated: grow the host columns */
+        double tc = now_ms();
+        if ((size_t)(n_groups + rows) <= hcap) {
+            vg_host_bufs_wait_upto(pg->hb, (size_t)(n_groups + rows) * 8);
+            g_pagg_ms[4] += now_ms() - tc;
+            tc = now_ms();
+        } else {                                     /* more groups than estimated: grow the host columns */
+            vg_host_bufs_wait(pg->hb);
             size_t ncap = (size_t)(n_groups + rows) * 5 / 4 + 4096;
             for (int c = 0; c < n_cols; c++) {
                 void *q = realloc(hcol[c], ncap * 8);
@@ -986,6 +992,7 @@ static VecBatch *pagg_end(PAgg *pg, VgAgg *A, Plan *P, VgAggLaunch *L) {
         t_copy += now_ms() - tc;
         n_groups += rows;
     }
+    vg_host_bufs_wait(pg->hb);        /* every page touched: the threads are done with the buffers */
     g_pagg_ms[2] += now_ms() - t0 - t_emit - t_copy;
     g_pagg_ms[3] += t_emit;
     g_pagg_ms[5] += t_copy;
@@ -1113,6 +1120,7 @@ static VecBatch *agg_next(VecNode *self) {
     VgAgg *A = (VgAgg *)self;
     if (A->ga.done) return NULL;
     A->ga.done = 1;
+    const double t_start = now_ms();
     Plan P;
     plan_build(A, &P);
     /* columns to move to the device for each source batch */
@@ -1260,12 +1268,14 @@ static VecBatch *agg_next(VecNode *self) {
     }
     VecBatch *res = pg ? pagg_end(pg, A, &P, L) : emit_result(A, &P, &T);
     if (pg) g_pagg_runs++;
+    const int was_pagg = pg != NULL;
     pagg_free(pg);
     vg_dfree(T.block);
     vg_dfree(S.cache);
     vg_dfree(S.counters);
     free(L);
     free(need);
+    if (was_pagg) g_pagg_ms[6] += now_ms() - t_start;
     return res;
 }
 

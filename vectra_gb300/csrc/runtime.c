@@ -9,6 +9,8 @@
 #include <stdlib.h>
 #include <string.h>
 #include <pthread.h>
+#include <stdatomic.h>
+#include <time.h>
 #include <unistd.h>
 #include <cuda_runtime_api.h>
 
@@ -439,26 +441,33 @@ static void prefault(void *p, size_t n) {
 
 /* Host buffers faulted in by background threads while the device works
  * (a result whose size is estimated before it is computed). */
-typedef struct {
-    VgHostBufs *h;
-    size_t lo, hi;             /* the thread's share of every buffer */
-} Slice;
-
+/* The buffers are faulted in chunk by chunk in ascending offset (chunk k:
+ * bytes [k C, (k + 1) C) of every buffer), chunks handed out to the threads
+ * by a counter, so a consumer that fills the buffers from the front can
+ * start on the first chunks while the threads are still on later ones. */
 struct VgHostBufs {
     int n, nt;
-    size_t bytes;
-    void **buf;
+    size_t bytes, chunk, n_chunks;
+    void **buf;                    /* the buffers not taken yet */
+    void **tbuf;                   /* every buffer, as the threads see them */
     pthread_t th[8];
-    Slice sl[8];
     int started;
+    atomic_size_t next;
+    atomic_uchar *done;            /* per chunk */
 };
 
-static void *touch_slices(void *arg) {
-    Slice *t = (Slice *)arg;
+static void *touch_chunks(void *arg) {
+    VgHostBufs *h = (VgHostBufs *)arg;
     long pg = sysconf(_SC_PAGESIZE);
     size_t step = pg > 4096 ? (size_t)pg : 4096;
-    for (int b = 0; b < t->h->n; b++)
-        for (size_t o = t->lo; o < t->hi; o += step) ((volatile char *)t->h->buf[b])[o] = 0;
+    for (;;) {
+        const size_t k = atomic_fetch_add(&h->next, 1);
+        if (k >= h->n_chunks) break;
+        const size_t lo = k * h->chunk, hi = lo + h->chunk < h->bytes ? lo + h->chunk : h->bytes;
+        for (int b = 0; b < h->n; b++)
+            for (size_t o = lo; o < hi; o += step) ((volatile char *)h->tbuf[b])[o] = 0;
+        atomic_store(&h->done[k], 1);
+    }
     return NULL;
 }
 
@@ -467,29 +476,42 @@ VgHostBufs *vg_host_bufs_begin(int n, size_t bytes) {
     h->n = n;
     h->bytes = bytes;
     h->buf = (void **)vg_xcalloc((size_t)n, sizeof(void *));
+    h->tbuf = (void **)vg_xcalloc((size_t)n, sizeof(void *));
     for (int b = 0; b < n; b++) {
         h->buf[b] = malloc(bytes ? bytes : 1);
         if (!h->buf[b]) {
             for (int c = 0; c < b; c++) free(h->buf[c]);
             free(h->buf);
+            free(h->tbuf);
             free(h);
             return NULL;
         }
+        h->tbuf[b] = h->buf[b];
     }
+    h->chunk = (size_t)16 << 20;
+    h->n_chunks = (bytes + h->chunk - 1) / h->chunk;
+    h->done = (atomic_uchar *)vg_xcalloc(h->n_chunks ? h->n_chunks : 1, sizeof(atomic_uchar));
+    for (size_t k = 0; k < h->n_chunks; k++) atomic_init(&h->done[k], 0);
+    atomic_init(&h->next, 0);
     long cpus = sysconf(_SC_NPROCESSORS_ONLN);
     h->nt = cpus >= 16 ? 8 : (int)(cpus > 1 ? cpus / 2 : 1);
-    size_t chunk = (bytes + (size_t)h->nt - 1) / (size_t)h->nt;
-    chunk = (chunk + 65535) & ~(size_t)65535;
-    for (int i = 0; i < h->nt; i++) {
-        size_t lo = (size_t)i * chunk, hi = lo + chunk < bytes ? lo + chunk : bytes;
-        if (lo >= bytes) break;
-        h->sl[i].h = h;
-        h->sl[i].lo = lo;
-        h->sl[i].hi = hi;
-        if (pthread_create(&h->th[i], NULL, touch_slices, &h->sl[i]) == 0) h->started |= 1 << i;
-        else touch_slices(&h->sl[i]);
-    }
+    for (int i = 0; i < h->nt; i++)
+        if (pthread_create(&h->th[i], NULL, touch_chunks, h) == 0) h->started |= 1 << i;
+    if (!h->started) touch_chunks(h);
     return h;
+}
+
+/* Waits until the first `upto` bytes of every buffer are faulted in (the
+ * threads always progress: each chunk is finished by the thread that took
+ * it). */
+void vg_host_bufs_wait_upto(VgHostBufs *h, size_t upto) {
+    if (!h) return;
+    const size_t kmax = upto >= h->bytes ? h->n_chunks : (upto + h->chunk - 1) / h->chunk;
+    for (size_t k = 0; k < kmax; k++)
+        while (!atomic_load(&h->done[k])) {
+            struct timespec ts = {0, 20000};
+            nanosleep(&ts, NULL);
+        }
 }
 
 /* Waits for the touching threads; the buffers stay with h until taken. */
@@ -512,6 +534,8 @@ void vg_host_bufs_free(VgHostBufs *h) {
     vg_host_bufs_wait(h);
     for (int b = 0; b < h->n; b++) free(h->buf[b]);
     free(h->buf);
+    free(h->tbuf);
+    free((void *)h->done);
     free(h);
 }
 

@@ -72,6 +72,7 @@ void vg_copy_sync(void);
 typedef struct VgHostBufs VgHostBufs;
 VgHostBufs *vg_host_bufs_begin(int n, size_t bytes);
 void vg_host_bufs_wait(VgHostBufs *h);
+void vg_host_bufs_wait_upto(VgHostBufs *h, size_t bytes);   /* the first `bytes` of every buffer */
 void *vg_host_bufs_take(VgHostBufs *h, int b, size_t need);   /* NULL: too small or taken */
 void vg_host_bufs_free(VgHostBufs *h);
 
