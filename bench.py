@@ -271,9 +271,19 @@ def gpu_arm(args, rank, world):
             torch.distributed.barrier()
         return ms / k, wall / k, lib.vgpu_kernel_launches() - l0
 
+    lib.vgpu_agg_phase_ms.restype = C.c_double
+    lib.vgpu_agg_phase_ms.argtypes = [C.c_int]
     with ClockSampler(dev.index) as clk:
+        ph0 = [lib.vgpu_agg_phase_ms(i) for i in range(5)]
         ms_step, wall_step, launches = timed(dev_step, args.steps, args.warmup)
+        ph1 = [lib.vgpu_agg_phase_ms(i) for i in range(5)]
     clocks = clk.summary()
+    # host time of the aggregation's next_batch call per query (planning with
+    # the join build, launches and their synchronisations, result), counted
+    # over the warm-up and timed steps
+    n_q = args.steps + args.warmup
+    agg_phases = dict(zip(["plan_and_join_build", "join_build", "aggregate", "result", "next_batch"],
+                          [round((b - a) / n_q, 4) for a, b in zip(ph0, ph1)]))
     n_l = C.c_ulonglong(0)
     agg_ms = lib.vgpu_profile_ms(0, C.byref(n_l))
     agg_launches = max(1, n_l.value)
@@ -336,6 +346,7 @@ def gpu_arm(args, rank, world):
                      "peak_kind": peak_kind, "algorithmic_bytes_per_step": kernel_b,
                      "kernel_ms_per_step": kernel_ms, "kernel_launches_per_step": agg_launches / args.steps,
                      "traffic": profile_traffic()},
+        "host_phases_ms": agg_phases,
         "join_build_ms": build_ms / max(1, build_n.value),
         "e2e": {"value": rows * world / (e2e_ms * 1e-3), "unit": "rows/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -490,6 +501,9 @@ def workload_arm(args):
     lib.vgpu_pagg_phase_ms.restype = C.c_double
     lib.vgpu_pagg_phase_ms.argtypes = [C.c_int]
     phase0 = [lib.vgpu_pagg_phase_ms(i) for i in range(7)]
+    lib.vgpu_agg_phase_ms.restype = C.c_double
+    lib.vgpu_agg_phase_ms.argtypes = [C.c_int]
+    aph0 = [lib.vgpu_agg_phase_ms(i) for i in range(5)]
     lib.vgpu_profile_reset()
     lib.vgpu_profile_enable(1)
     stream = torch.cuda.current_stream(dev)
@@ -502,6 +516,7 @@ def workload_arm(args):
     lib.vgpu_profile_enable(0)
     ms = e0.elapsed_time(e1) / args.steps
     phases = [round((lib.vgpu_pagg_phase_ms(i) - phase0[i]) / args.steps, 3) for i in range(7)]
+    aphases = [round((lib.vgpu_agg_phase_ms(i) - aph0[i]) / args.steps, 4) for i in range(5)]
     # where the host time of one query goes: plan construction, next_batch
     # (the whole aggregation and the copy of its result), freeing the result
     host = None
@@ -537,6 +552,8 @@ def workload_arm(args):
             "finish_kernel_ms": finish_ms / max(1, args.steps), "result_checked": True,
             "partitioned_phases_ms": dict(zip(["sketch", "partition", "reduce", "compact", "host_buffers", "download",
                                                "aggregation"], phases)) if pagg_runs else None,
+            "host_phases_ms": None if pagg_runs else dict(zip(["plan_and_join_build", "join_build", "aggregate",
+                                                                "result", "next_batch"], aphases)),
             "timed": "the node C API producing the host result batch (malloc-owned columns), without "
                      "conversion to numpy"}
 

@@ -106,6 +106,11 @@ unsigned long long vgpu_pagg_runs(void);
  * output columns, 4 waiting for the host result buffers, 5 copy to host,
  * 6 the whole next_batch call of the aggregation. */
 double      vgpu_pagg_phase_ms(int phase);
+/* The same for the hash-table aggregation path: 0 planning before the
+ * first batch (join build included), 1 the join build alone, 2 the
+ * aggregation launches and their synchronisations, 3 the result
+ * (compaction, order, finish, copy to host), 4 the whole next_batch call. */
+double      vgpu_agg_phase_ms(int phase);
 
 /* Optional kernel timing: CUDA events recorded on the launching stream
  * around each kernel class (VGPU_PROF_*), read back in milliseconds. */

@@ -528,6 +528,15 @@ typedef struct {
  * the result to the host; 6 the whole aggregation (its next_batch call). */
 static double g_pagg_ms[7];
 
+/* Host wall time of the hash-table aggregation path, summed since load:
+ * 0 planning before the first batch (join build included), 1 the join
+ * build alone, 2 the aggregation launches and their synchronisations, 3
+ * the result (compaction, order, finish, copy to host), 4 the whole
+ * next_batch call. */
+static double g_agg_ms[5];
+
+double vgpu_agg_phase_ms(int phase) { return phase >= 0 && phase < 5 ? g_agg_ms[phase] : 0.0; }
+
 static double now_ms(void) {
     struct timespec ts;
     clock_gettime(CLOCK_MONOTONIC, &ts);
@@ -1142,7 +1151,9 @@ static VecBatch *agg_next(VecNode *self) {
         /* up to two build columns travel in a payload copy of the join
          * table (one sector per probe row in the specialised kernel) */
         const VgJPay *pay = NULL;
+        const double tb = now_ms();
         B = vg_join_build_payload(P.join, P.bset.idx, P.bset.n, &pay);
+        g_agg_ms[1] += now_ms() - tb;
         L->jpay = pay;
         L->jpay_n = pay ? P.bset.n : 0;
         L->has_join = 1;
@@ -1224,6 +1235,8 @@ static VecBatch *agg_next(VecNode *self) {
     VgDBatch db;
     int64_t batch_idx = 0, stream_pos = 0;
     PAgg *pg = NULL;
+    double t_loop = now_ms();
+    g_agg_ms[0] += t_loop - t_start;
     while (vg_pull(P.src, need, 0, &db)) {
         int64_t n_logical = db.d_sel ? db.sel_n : db.n_rows;
         if (batch_idx == 0) {
@@ -1266,7 +1279,10 @@ static VecBatch *agg_next(VecNode *self) {
         stream_pos += n_logical;
         batch_idx++;
     }
+    const double t_emit = now_ms();
+    if (!pg) g_agg_ms[2] += t_emit - t_loop;
     VecBatch *res = pg ? pagg_end(pg, A, &P, L) : emit_result(A, &P, &T);
+    if (!pg) g_agg_ms[3] += now_ms() - t_emit;
     if (pg) g_pagg_runs++;
     const int was_pagg = pg != NULL;
     pagg_free(pg);
@@ -1276,6 +1292,7 @@ static VecBatch *agg_next(VecNode *self) {
     free(L);
     free(need);
     if (was_pagg) g_pagg_ms[6] += now_ms() - t_start;
+    else g_agg_ms[4] += now_ms() - t_start;
     return res;
 }
 
