@@ -539,27 +539,6 @@ void vg_host_bufs_free(VgHostBufs *h) {
     free(h);
 }
 
-/* A column downloaded into dst (malloc-owned, at least value bytes of n
- * rows), or into a fresh allocation when dst is NULL. */
-VecArray vg_download_column_into(int type, const void *d_data, const uint32_t *d_valid, int64_t n, void *dst) {
-    if (!dst) return vg_download_column(type, d_data, d_valid, n);
-    VecArray a;
-    memset(&a, 0, sizeof(a));
-    a.type = (VecType)type;
-    a.length = n;
-    a.owns_data = 1;
-    a.validity = (uint8_t *)vg_xcalloc((size_t)vg_vbytes(n), 1);
-    size_t vb = value_bytes(type, n);
-    if (type == VEC_BOOL) a.buf.bln = (uint8_t *)dst;
-    else a.buf.i64 = (int64_t *)dst;
-    if (n > 0) {
-        vg_d2h(dst, d_data, vb);
-        if (d_valid) vg_d2h(a.validity, d_valid, (size_t)vg_vbytes(n));
-        else memset(a.validity, 0xFF, (size_t)vg_vbytes(n));
-    }
-    return a;
-}
-
 VecArray vg_download_column(int type, const void *d_data, const uint32_t *d_valid, int64_t n) {
     VecArray a;
     memset(&a, 0, sizeof(a));

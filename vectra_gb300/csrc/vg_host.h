@@ -63,7 +63,6 @@ void vg_dbatch_release(VgDBatch *b);
 
 /* Device column -> newly malloc'd host VecArray of n values. */
 VecArray vg_download_column(int type, const void *d_data, const uint32_t *d_valid, int64_t n);
-VecArray vg_download_column_into(int type, const void *d_data, const uint32_t *d_valid, int64_t n, void *dst);
 VecArray vg_host_column(int type, int64_t n, void *values, const uint32_t *d_valid);
 void vg_copy_after_main(void);
 void vg_d2h_copy(void *dst, const void *src, size_t bytes);
