@@ -57,9 +57,12 @@ struct Req {
     Table probe;                   // source / probe table
     Table build;                   // semi / anti build side
     double threshold;
-    GSlot *acc;                    // filter: one accumulator slot
+    long long *facc;               // filter: the sum as VG_LACC_WORDS 32-bit digits in 64-bit words ...
+    uint32_t *fflags;              // ... and its NaN / infinity bits
     GSlot *gt;                     // group: table (cap + 2 slots: marker key, NA key)
     int64_t cap;
+    int32_t direct;                // group over a dense key range: slot = key - probe.kmin (cap = krange)
+    int32_t pad_direct;
     int64_t max_groups;
     long long *out_key;
     uint8_t *out_key_valid;
@@ -104,16 +107,10 @@ __global__ void __launch_bounds__(kSrvThreads) srv_init_kernel(const Req *req, i
                 g.fc = 0.0;
             }
         }
+        if (R.facc)
+            for (int w = threadIdx.x; w < VG_LACC_WORDS; w += blockDim.x) R.facc[w] = 0;
         if (threadIdx.x == 0) {
-            if (R.acc) {
-                R.acc->key = 0;
-                R.acc->cnt = 0;
-                R.acc->base = kBaseUnset;
-                R.acc->flags = 0;
-                for (int w = 0; w < kWin; w++) R.acc->win[w] = 0;
-                R.acc->fs = 0.0;
-                R.acc->fc = 0.0;
-            }
+            if (R.fflags) *R.fflags = 0;
             *R.rows = 0;
             if (R.kept) *R.kept = 0;
         }
@@ -136,14 +133,58 @@ __global__ void __launch_bounds__(kSrvThreads) srv_phase1_kernel(const Req *req,
         const Table &T = R.probe;
         unsigned c = 0;
         if (R.kind == VGPU_SERVE_FILTER_SUM) {
+            // One exact sum for the whole request: every thread adds its
+            // values' 32-bit digits into a six-digit window of its own (in
+            // registers, anchored at its first value); a value outside it,
+            // and each window at the end of the item, go into the CTA's
+            // full-range digit words in shared memory; the CTA's words are
+            // added to the request's once per item.  No atomics on one
+            // address from every row.
+            long long *cw = (long long *)dsm;                // VG_LACC_WORDS words
+            uint32_t *cfl = (uint32_t *)(cw + VG_LACC_WORDS);
+            for (int w = threadIdx.x; w < VG_LACC_WORDS; w += blockDim.x) cw[w] = 0;
+            if (threadIdx.x == 0) *cfl = 0;
+            __syncthreads();
+            int64_t win[kWin];
+#pragma unroll
+            for (int w = 0; w < kWin; w++) win[w] = 0;
+            int base = -1;
+            uint32_t special = 0;
             for (int64_t r = W.lo + threadIdx.x; r < W.hi; r += blockDim.x) {
                 if (!bit(T.val_valid, r)) continue;
                 const uint64_t b = (uint64_t)__ldg(T.val + r);
                 const double x = vg_bits_to_f64(b);
                 if (!(x > R.threshold)) continue;
                 c++;
-                g_add(*R.acc, b);
+                const VgDigits d = vg_split_double(b);
+                if (d.special) { special |= d.special; continue; }
+                if (d.lo < 0) continue;
+                if (base < 0) {
+                    base = d.lo - 2;
+                    if (base < 0) base = 0;
+                    if (base > VG_LACC_WORDS - kWin) base = VG_LACC_WORDS - kWin;
+                }
+                const int rel = d.lo - base;
+                if (rel >= 0 && rel + 3 <= kWin) {
+#pragma unroll
+                    for (int w = 0; w < kWin; w++)
+                        win[w] += w == rel ? d.d0 : w == rel + 1 ? d.d1 : w == rel + 2 ? d.d2 : 0;
+                } else {
+                    atomicAdd((unsigned long long *)(cw + d.lo), (unsigned long long)d.d0);
+                    atomicAdd((unsigned long long *)(cw + d.lo + 1), (unsigned long long)d.d1);
+                    if (d.lo + 2 < VG_LACC_WORDS) atomicAdd((unsigned long long *)(cw + d.lo + 2), (unsigned long long)d.d2);
+                }
             }
+            if (base >= 0) {
+#pragma unroll
+                for (int w = 0; w < kWin; w++)
+                    if (win[w]) atomicAdd((unsigned long long *)(cw + base + w), (unsigned long long)win[w]);
+            }
+            if (special) atomicOr(cfl, special);
+            __syncthreads();
+            for (int w = threadIdx.x; w < VG_LACC_WORDS; w += blockDim.x)
+                if (cw[w]) atomicAdd((unsigned long long *)(R.facc + w), (unsigned long long)cw[w]);
+            if (threadIdx.x == 0 && *cfl) atomicOr(R.fflags, *cfl);
         } else if (R.kind == VGPU_SERVE_GROUP_SUM) {
             // hot keys aggregate in the CTA's cache, the rest go straight to
             // the request's table; the cache is merged at the end of the item
@@ -160,7 +201,7 @@ __global__ void __launch_bounds__(kSrvThreads) srv_phase1_kernel(const Req *req,
                     atomicAdd(&gc.cnt[cs], 1u);
                     if (!vv || gc_sum(gc, cs, v)) continue;
                 }
-                const int64_t s = kv ? g_slot(R.gt, R.cap, k) : R.cap + 1;
+                const int64_t s = !kv ? R.cap + 1 : R.direct ? (int64_t)(k - (uint64_t)T.kmin) : g_slot(R.gt, R.cap, k);
                 if (s < 0) { atomicOr(ctr + 4, VG_ERR_FULL); continue; }
                 if (cs < 0) atomicAdd(&R.gt[s].cnt, 1ull);
                 if (vv) g_add(R.gt[s], v);
@@ -168,7 +209,7 @@ __global__ void __launch_bounds__(kSrvThreads) srv_phase1_kernel(const Req *req,
             __syncthreads();
             for (int i = threadIdx.x; i < kGC; i += blockDim.x) {
                 if (gc.state[i] != 2u) continue;
-                const int64_t s = g_slot(R.gt, R.cap, gc.key[i]);
+                const int64_t s = R.direct ? (int64_t)(gc.key[i] - (uint64_t)T.kmin) : g_slot(R.gt, R.cap, gc.key[i]);
                 if (s < 0) { atomicOr(ctr + 4, VG_ERR_FULL); continue; }
                 gc_merge(gc, i, R.gt[s]);
             }
@@ -209,7 +250,7 @@ __global__ void __launch_bounds__(kSrvThreads) srv_phase2_kernel(const Req *req,
         const WItem W = items[it];
         const Req &R = req[W.req];
         if (R.kind == VGPU_SERVE_FILTER_SUM) {
-            if (threadIdx.x == 0) R.out_sum[0] = g_sum(*R.acc);
+            if (threadIdx.x == 0) R.out_sum[0] = vg_digits_to_double((const int64_t *)R.facc, VG_LACC_WORDS, *R.fflags);
         } else if (R.kind == VGPU_SERVE_GROUP_SUM) {
             for (int64_t s = W.lo + threadIdx.x; s < W.hi; s += blockDim.x) {
                 const GSlot &g = R.gt[s];
@@ -217,7 +258,7 @@ __global__ void __launch_bounds__(kSrvThreads) srv_phase2_kernel(const Req *req,
                 const unsigned long long o = atomicAdd(R.rows, 1ull);
                 if ((int64_t)o >= R.max_groups) { atomicOr(ctr + 4, VG_ERR_FULL); continue; }
                 const bool na = s == R.cap + 1;
-                R.out_key[o] = na ? 0 : (long long)g.key;
+                R.out_key[o] = na ? 0 : R.direct ? (long long)(R.probe.kmin + s) : (long long)g.key;
                 R.out_key_valid[o] = na ? 0 : 1;
                 R.out_sum[o] = g_sum(g);
                 R.out_n[o] = (long long)g.cnt;
@@ -406,10 +447,17 @@ int ensure_keyset(Server *S, Table &T) {
 
 // bytes a request holds while admitted (outputs and scratch)
 // group table bytes of a request (scratch, released when it finishes)
+// group table slots: the key range itself when the keys are dense (no
+// hashing), else a power of two at least twice the distinct keys
+int64_t group_cap(const Table &T) {
+    if (T.kbits && T.krange <= 2 * (T.distinct + 1) + 1024) return T.krange;
+    return pow2_ge(2 * (T.distinct + 1));
+}
+
 int64_t scratch_estimate(Server *S, const VgpuServeQuery &q) {
     if (q.kind != VGPU_SERVE_GROUP_SUM) return 0;
     const Table &T = S->tables[(size_t)q.table];
-    return (pow2_ge(2 * (T.distinct + 1)) + 2) * (int64_t)sizeof(GSlot);
+    return (group_cap(T) + 2) * (int64_t)sizeof(GSlot);
 }
 
 int64_t estimate(Server *S, const VgpuServeQuery &q) {
@@ -418,7 +466,7 @@ int64_t estimate(Server *S, const VgpuServeQuery &q) {
     case VGPU_SERVE_FILTER_SUM: return 4096;
     case VGPU_SERVE_GROUP_SUM: {
         const int64_t g = T.distinct + 1;          // distinct keys + the NA group
-        return (pow2_ge(2 * g) + 2) * (int64_t)sizeof(GSlot) + g * (8 + 1 + 8 + 8) + 4096;
+        return (group_cap(T) + 2) * (int64_t)sizeof(GSlot) + g * (8 + 1 + 8 + 8) + 4096;
     }
     default:
         return T.n * 4 + ((T.n + kChunk - 1) / kChunk + 1) * 8 + 4096;
@@ -489,14 +537,15 @@ int launch(Server *S) {
             // outputs and scratch of the request, one allocation on the wave's stream
             size_t bytes = 256 * 2;
             if (D.kind == VGPU_SERVE_GROUP_SUM) {
-                D.cap = pow2_ge(2 * (T.distinct + 1));
+                D.cap = group_cap(T);
+                D.direct = D.cap == T.krange && T.kbits ? 1 : 0;
                 D.max_groups = T.distinct + 1;
                 bytes += (size_t)D.max_groups * 25 + 1024;
                 if (cudaMallocAsync(&R.scratch, (size_t)(D.cap + 2) * sizeof(GSlot), W->stream) != cudaSuccess)
                     return srv_fail(S, "server: %s", "device allocation failed");
                 D.gt = (GSlot *)R.scratch;
             } else if (D.kind == VGPU_SERVE_FILTER_SUM) {
-                bytes += sizeof(GSlot) + 256;
+                bytes += VG_LACC_WORDS * 8 + 256;
             } else {
                 D.build = S->tables[(size_t)R.q.build_table];
                 bytes += (size_t)T.n * 4 + 256;
@@ -519,7 +568,8 @@ int launch(Server *S) {
                 for (int64_t lo = 0; lo < D.cap + 2; lo += kChunk)
                     it2.push_back(WItem{(int32_t)i, 0, lo, lo + kChunk < D.cap + 2 ? lo + kChunk : D.cap + 2});
             } else if (D.kind == VGPU_SERVE_FILTER_SUM) {
-                D.acc = (GSlot *)p;
+                D.facc = (long long *)p;
+                D.fflags = (uint32_t *)(p + VG_LACC_WORDS * 8);
                 for (int64_t lo = 0; lo < T.n; lo += kChunk)
                     it1.push_back(WItem{(int32_t)i, 0, lo, lo + kChunk < T.n ? lo + kChunk : T.n});
                 it2.push_back(WItem{(int32_t)i, 0, 0, 0});
