@@ -150,8 +150,12 @@ VG_DEV void gc_reset(GCache &c) {
 // when the key is not cached
 VG_DEV int gc_find(GCache &c, uint64_t k) {
     int s = (int)(bhash(k) & (uint64_t)(kGC - 1));
-    const bool may_insert = *(volatile int *)&c.used < (kGC * 3) / 4;
-    for (int p = 0; p < 8; p++) {
+    // keys are cached while the cache is at most half full, so that a key
+    // that is not cached (most keys of a high-cardinality table) is known to
+    // be absent after a few probes: a linear probe at load 1/2 ends at an
+    // empty slot after 2.5 probes on average
+    const bool may_insert = *(volatile int *)&c.used < kGC / 2;
+    for (int p = 0; p < (may_insert ? 8 : 4); p++) {
         uint32_t st = *(volatile uint32_t *)&c.state[s];
         if (st == 0) {
             if (!may_insert) return -1;
