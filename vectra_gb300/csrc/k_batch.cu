@@ -163,10 +163,18 @@ __global__ void __launch_bounds__(kSetThreads) set_phase2_kernel(const Inst *ins
         if (I.q.kind == VGPU_SET_GROUP) {
             // slots [lo, hi) of the table (items cover cap + 1 slots)
             const GSlot *t = (const GSlot *)I.table;
-            for (int64_t s = W.lo + threadIdx.x; s < W.hi; s += blockDim.x) {
+            const int lane = threadIdx.x & 31;
+            // output rows taken per warp (one counter update per 32 slots)
+            for (int64_t s0 = W.lo; s0 < W.hi; s0 += blockDim.x) {
+                const int64_t s = s0 + threadIdx.x;
+                const bool has = s < W.hi && t[s].cnt != 0;
+                const unsigned m = __ballot_sync(0xFFFFFFFFu, has);
+                unsigned long long ob = 0;
+                if (lane == 0 && m) ob = atomicAdd((unsigned long long *)I.q.out_rows, (unsigned long long)__popc(m));
+                ob = __shfl_sync(0xFFFFFFFFu, ob, 0);
+                if (!has) continue;
                 const GSlot &g = t[s];
-                if (g.cnt == 0) continue;
-                const unsigned long long o = atomicAdd((unsigned long long *)I.q.out_rows, 1ull);
+                const unsigned long long o = ob + (unsigned long long)__popc(m & ((1u << lane) - 1u));
                 if ((int64_t)o >= I.q.max_groups) { atomicOr(ctr + 4, VG_ERR_FULL); continue; }
                 const double sum = g_sum(g);
                 I.q.out_key[o] = (int64_t)g.key;

@@ -252,10 +252,18 @@ __global__ void __launch_bounds__(kSrvThreads) srv_phase2_kernel(const Req *req,
         if (R.kind == VGPU_SERVE_FILTER_SUM) {
             if (threadIdx.x == 0) R.out_sum[0] = vg_digits_to_double((const int64_t *)R.facc, VG_LACC_WORDS, *R.fflags);
         } else if (R.kind == VGPU_SERVE_GROUP_SUM) {
-            for (int64_t s = W.lo + threadIdx.x; s < W.hi; s += blockDim.x) {
+            // output rows taken per warp (one counter update per 32 slots,
+            // not one per group)
+            for (int64_t s0 = W.lo; s0 < W.hi; s0 += blockDim.x) {
+                const int64_t s = s0 + threadIdx.x;
+                const bool has = s < W.hi && R.gt[s].cnt != 0;
+                const unsigned m = __ballot_sync(0xFFFFFFFFu, has);
+                unsigned long long ob = 0;
+                if (lane == 0 && m) ob = atomicAdd(R.rows, (unsigned long long)__popc(m));
+                ob = __shfl_sync(0xFFFFFFFFu, ob, 0);
+                if (!has) continue;
                 const GSlot &g = R.gt[s];
-                if (g.cnt == 0) continue;
-                const unsigned long long o = atomicAdd(R.rows, 1ull);
+                const unsigned long long o = ob + (unsigned long long)__popc(m & ((1u << lane) - 1u));
                 if ((int64_t)o >= R.max_groups) { atomicOr(ctr + 4, VG_ERR_FULL); continue; }
                 const bool na = s == R.cap + 1;
                 R.out_key[o] = na ? 0 : R.direct ? (long long)(R.probe.kmin + s) : (long long)g.key;

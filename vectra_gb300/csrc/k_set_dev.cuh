@@ -93,7 +93,7 @@ VG_DEV long long j_find(const JSlot *t, int64_t cap, uint64_t k) {
 }
 
 // exact sum of a group slot, rounded once
-VG_DEV double g_sum(const GSlot &g) {
+__device__ __noinline__ double g_sum_wide(const GSlot &g) {
     int64_t w[VG_LACC_WORDS];
     for (int i = 0; i < VG_LACC_WORDS; i++) w[i] = 0;
     if (g.base != kBaseUnset)
@@ -110,6 +110,19 @@ VG_DEV double g_sum(const GSlot &g) {
         }
     }
     return vg_digits_to_double(w, VG_LACC_WORDS, special);
+}
+
+// The correctly rounded sum of a slot: its window alone is rounded on
+// registers (vg_window6_to_double); a slot that used the compensated pair
+// or saw a NaN / infinity takes the general digit rounding.
+static_assert(kWin == 6, "the register rounding takes a six-digit window");
+VG_DEV double g_sum(const GSlot &g) {
+    if (g.fs != 0.0 || g.fc != 0.0 || (g.flags & (4u | 8u | 16u))) return g_sum_wide(g);
+    if (g.base == kBaseUnset) return 0.0;
+    int64_t w[6];
+#pragma unroll
+    for (int i = 0; i < 6; i++) w[i] = g.win[i];
+    return vg_window6_to_double(w, g.base);
 }
 
 }  // namespace
