@@ -406,16 +406,36 @@ __global__ void minmax_init_kernel(long long *out) {
     out[2] = 0;
 }
 
+// Each thread takes kMinmaxU rows per step (blockDim apart: coalesced) and
+// issues their loads before it uses them, so that enough bytes are in
+// flight to keep HBM busy.
+constexpr int kMinmaxU = 4;
+
 __global__ void minmax_i64_kernel(VgCol c, int64_t n, long long *out) {
     long long lo = 0x7FFFFFFFFFFFFFFFll, hi = (long long)0x8000000000000000ull, cnt = 0;
     const long long *v = (const long long *)c.data;
-    int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-        if (!vg_valid(c, r)) continue;
-        long long x = v[r];
-        lo = x < lo ? x : lo;
-        hi = x > hi ? x : hi;
-        cnt++;
+    const int64_t step = (int64_t)gridDim.x * blockDim.x * kMinmaxU;
+    for (int64_t r0 = (int64_t)blockIdx.x * blockDim.x * kMinmaxU + threadIdx.x; r0 < n; r0 += step) {
+        long long x[kMinmaxU];
+        uint32_t w[kMinmaxU];
+#pragma unroll
+        for (int u = 0; u < kMinmaxU; u++) {
+            const int64_t r = r0 + (int64_t)u * blockDim.x;
+            x[u] = 0;
+            w[u] = 0;
+            if (r < n) {
+                x[u] = __ldg(v + r);
+                w[u] = c.valid ? __ldg(c.valid + ((r + c.voff) >> 5)) : 0xFFFFFFFFu;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kMinmaxU; u++) {
+            const int64_t r = r0 + (int64_t)u * blockDim.x;
+            if (r >= n || !((w[u] >> ((r + c.voff) & 31)) & 1u)) continue;
+            lo = x[u] < lo ? x[u] : lo;
+            hi = x[u] > hi ? x[u] : hi;
+            cnt++;
+        }
     }
     for (int o = 16; o > 0; o >>= 1) {
         long long l2 = __shfl_xor_sync(0xFFFFFFFFu, lo, o);
@@ -569,7 +589,10 @@ int vgk_gather_into(const VgCol *col, const int32_t *d_idx, int64_t n, void *d_o
 int vgk_col_minmax_i64(const VgCol *col, int64_t n, int64_t *d_out, int64_t *h_out, vg_stream_t s) {
     cudaStream_t st = (cudaStream_t)s;
     { minmax_init_kernel<<<1, 1, 0, st>>>((long long *)d_out); vg_launch_counter++; }
-    if (n > 0) { minmax_i64_kernel<<<grid_for(n, 256), 256, 0, st>>>(*col, n, (long long *)d_out); vg_launch_counter++; }
+    if (n > 0) {
+        minmax_i64_kernel<<<grid_for((n + kMinmaxU - 1) / kMinmaxU, 256), 256, 0, st>>>(*col, n, (long long *)d_out);
+        vg_launch_counter++;
+    }
     if (check(cudaMemcpyAsync(h_out, d_out, 24, cudaMemcpyDeviceToHost, st), "column min/max")) return -1;
     return check(cudaStreamSynchronize(st), "column min/max");
 }

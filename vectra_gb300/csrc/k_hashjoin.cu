@@ -274,9 +274,8 @@ __global__ void jt_insert_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, in
                     p1 = vg_load_bits(P.c1, r);
                     if (vg_valid(P.c1, r)) meta |= 4u;
                 }
-                ulonglong2 *o = (ulonglong2 *)(P.pay + d);
-                o[0] = make_ulonglong2(k[0], (unsigned long long)(uint32_t)r | ((unsigned long long)meta << 32));
-                o[1] = make_ulonglong2(p0, p1);
+                vg_st256(P.pay + d, k[0], (unsigned long long)(uint32_t)r | ((unsigned long long)meta << 32), p0,
+                         p1);
             }
         }
     }
@@ -291,38 +290,89 @@ __global__ void jt_insert_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, in
 // If a key repeats, one of its rows survives; pass 2 finds that out while
 // the surviving rows write their keys' entries (reading their payload values
 // in row order), and the entries of keys no row has are cleared last.
+//
+// Each thread takes kBuildU rows per step (blockDim apart, so every load
+// stays coalesced) and issues all their loads before it uses any: a row's
+// work is a short chain of dependent loads, and one row per step leaves too
+// few bytes in flight to keep HBM busy.  The step loop runs on the block's
+// first row so that every thread of a warp takes the same number of steps.
+// A direct table has a single key (node_join.c builds one only then).
 constexpr int32_t kRowBits = 29;                       // build rows < 2^29
 constexpr uint32_t kRowMask = (1u << kRowBits) - 1u;
+constexpr int kBuildU = 4;
+static_assert(sizeof(VgJPay) == 32, "one 32-byte store per payload entry");
+
+// validity word of row r (all ones for a column without a bitmap), and the
+// bit of row r in it
+VG_DEV uint32_t valid_word(const VgCol &c, int64_t r) {
+    return c.valid ? __ldg(c.valid + ((r + c.voff) >> 5)) : 0xFFFFFFFFu;
+}
+VG_DEV bool valid_bit(const VgCol &c, int64_t r, uint32_t w) { return (w >> ((r + c.voff) & 31)) & 1u; }
+
+// key_words for a single key from its preloaded bits and validity word
+VG_DEV bool key_word_from(const KeyArgs &K, int64_t r, uint64_t b, uint32_t vw, uint64_t *k) {
+    if (!valid_bit(K.cols[0], r, vw)) return false;
+    if (K.conv[0]) b = vg_f64_to_bits(vg_i2f((int64_t)b));
+    if (K.types[0] == VEC_DOUBLE && vg_is_nan_bits(b)) return false;
+    k[0] = vg_norm_key(b, K.types[0]);
+    return true;
+}
 
 __global__ void jt_rows_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int32_t *rslot, uint32_t *counters,
                                       PayArgs P, uint32_t *rowof, long long *mm) {
-    // per-thread min / max / count over a grid-stride range, then one
-    // combine per block (the statistic words are single addresses)
+    // per-thread min / max / count, then one combine per block (the
+    // statistic words are single addresses)
     long long lo[2] = {0x7FFFFFFFFFFFFFFFll, 0x7FFFFFFFFFFFFFFFll};
     long long hi[2] = {(long long)0x8000000000000000ull, (long long)0x8000000000000000ull};
     unsigned long long cnt[2] = {0, 0};
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-        uint64_t k[VG_MAX_KEYS];
-        int64_t d = -1;
-        if (key_words(K, r, k)) {
-            d = jt_direct_slot(jt, k[0]);
-            if (d < 0) atomicOr(counters + 2, VG_ERR_FULL);
-        }
-        uint32_t vb = 0;                               // validity of the payload values
-        if (P.n_cols > 0 && vg_valid(P.c0, r)) vb |= 1u;
-        if (P.n_cols > 1 && vg_valid(P.c1, r)) vb |= 2u;
-        if (d >= 0) rowof[d] = (uint32_t)r | (vb << kRowBits);
-        rslot[r] = (int32_t)d;
+    const int64_t step = (int64_t)gridDim.x * blockDim.x * kBuildU;
+    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x * kBuildU; b0 < n; b0 += step) {
+        uint64_t kb[kBuildU], pb[2][kBuildU];
+        uint32_t kv[kBuildU], pv[2][kBuildU];
 #pragma unroll
-        for (int c = 0; c < 2; c++) {
-            if (c >= P.n_cols || !((vb >> c) & 1u)) continue;
-            const VgCol &col = c == 0 ? P.c0 : P.c1;
-            if (col.type != VEC_INT64) continue;
-            const long long x = (long long)vg_load_bits(col, r);
-            lo[c] = x < lo[c] ? x : lo[c];
-            hi[c] = x > hi[c] ? x : hi[c];
-            cnt[c]++;
+        for (int u = 0; u < kBuildU; u++) {
+            const int64_t r = b0 + (int64_t)u * blockDim.x + threadIdx.x;
+            kb[u] = 0;
+            kv[u] = 0;
+            pb[0][u] = pb[1][u] = 0;
+            pv[0][u] = pv[1][u] = 0;
+            if (r < n) {
+                kb[u] = vg_load_bits(K.cols[0], r);
+                kv[u] = valid_word(K.cols[0], r);
+#pragma unroll
+                for (int c = 0; c < 2; c++) {
+                    if (c >= P.n_cols) continue;
+                    const VgCol &col = c == 0 ? P.c0 : P.c1;
+                    pv[c][u] = valid_word(col, r);
+                    if (col.type == VEC_INT64) pb[c][u] = vg_load_bits(col, r);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kBuildU; u++) {
+            const int64_t r = b0 + (int64_t)u * blockDim.x + threadIdx.x;
+            if (r >= n) break;
+            uint64_t k[VG_MAX_KEYS];
+            int64_t d = -1;
+            if (key_word_from(K, r, kb[u], kv[u], k)) {
+                d = jt_direct_slot(jt, k[0]);
+                if (d < 0) atomicOr(counters + 2, VG_ERR_FULL);
+            }
+            uint32_t vb = 0;                           // validity of the payload values
+            if (P.n_cols > 0 && valid_bit(P.c0, r, pv[0][u])) vb |= 1u;
+            if (P.n_cols > 1 && valid_bit(P.c1, r, pv[1][u])) vb |= 2u;
+            if (d >= 0) rowof[d] = (uint32_t)r | (vb << kRowBits);
+            rslot[r] = (int32_t)d;
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                if (c >= P.n_cols || !((vb >> c) & 1u)) continue;
+                const VgCol &col = c == 0 ? P.c0 : P.c1;
+                if (col.type != VEC_INT64) continue;
+                const long long x = (long long)pb[c][u];
+                lo[c] = x < lo[c] ? x : lo[c];
+                hi[c] = x > hi[c] ? x : hi[c];
+                cnt[c]++;
+            }
         }
     }
     __shared__ long long s_lo[2], s_hi[2];
@@ -358,34 +408,42 @@ __global__ void jt_rows_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int3
 }
 
 // Pass 2 (as verify + gather in one): each row that its key's entry names
-// writes the entry, reading its payload values where they are (coalesced);
-// a row whose key names another row reports a repeated key.  Entries of
-// keys no row has are written by jt_pay_absent_kernel.
+// writes the entry (one 32-byte store; the payload copy is 32-byte aligned),
+// its payload values read where they are (coalesced); a row whose key names
+// another row reports a repeated key.  Entries of keys no row has are
+// written by jt_pay_absent_kernel.
 __global__ void jt_pay_scatter_kernel(VgJoinTable jt, const uint32_t *rowof, const int32_t *rslot, int64_t n,
                                       PayArgs P, uint32_t *counters) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t r0 = (int64_t)blockIdx.x * blockDim.x; r0 < n; r0 += stride) {
-        const int64_t r = r0 + threadIdx.x;
-        bool dup = false;
-        if (r < n) {
-            const int32_t d = rslot[r];
-            if (d >= 0) {
-                const uint32_t v = __ldg(rowof + d);
-                if ((v & kRowMask) != (uint32_t)r) {
-                    dup = true;
-                } else {
-                    const uint32_t meta = 1u | (((v >> kRowBits) & 3u) << 1);
-                    const ulonglong2 a = make_ulonglong2((uint64_t)jt.dmin + (uint64_t)d,
-                                                         (unsigned long long)(uint32_t)r |
-                                                             ((unsigned long long)meta << 32));
-                    ulonglong2 b = make_ulonglong2(0ull, 0ull);
-                    if (P.n_cols > 0) b.x = vg_load_bits(P.c0, r);
-                    if (P.n_cols > 1) b.y = vg_load_bits(P.c1, r);
-                    ulonglong2 *o = (ulonglong2 *)(P.pay + d);
-                    o[0] = a;
-                    o[1] = b;
-                }
+    const int64_t step = (int64_t)gridDim.x * blockDim.x * kBuildU;
+    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x * kBuildU; b0 < n; b0 += step) {
+        int32_t d[kBuildU];
+        uint64_t p0[kBuildU], p1[kBuildU];
+#pragma unroll
+        for (int u = 0; u < kBuildU; u++) {
+            const int64_t r = b0 + (int64_t)u * blockDim.x + threadIdx.x;
+            d[u] = -1;
+            p0[u] = p1[u] = 0;
+            if (r < n) {
+                d[u] = rslot[r];
+                if (P.n_cols > 0) p0[u] = vg_load_bits(P.c0, r);
+                if (P.n_cols > 1) p1[u] = vg_load_bits(P.c1, r);
             }
+        }
+        uint32_t v[kBuildU];
+#pragma unroll
+        for (int u = 0; u < kBuildU; u++) v[u] = d[u] >= 0 ? __ldg(rowof + d[u]) : 0u;
+        bool dup = false;
+#pragma unroll
+        for (int u = 0; u < kBuildU; u++) {
+            const int64_t r = b0 + (int64_t)u * blockDim.x + threadIdx.x;
+            if (d[u] < 0) continue;
+            if ((v[u] & kRowMask) != (uint32_t)r) {
+                dup = true;
+                continue;
+            }
+            const uint32_t meta = 1u | (((v[u] >> kRowBits) & 3u) << 1);
+            vg_st256(P.pay + d[u], (uint64_t)jt.dmin + (uint64_t)d[u],
+                     (unsigned long long)(uint32_t)r | ((unsigned long long)meta << 32), p0[u], p1[u]);
         }
         if (__any_sync(0xFFFFFFFFu, dup) && (threadIdx.x & 31) == 0) atomicOr(counters + 3, 1u);
     }
@@ -393,12 +451,19 @@ __global__ void jt_pay_scatter_kernel(VgJoinTable jt, const uint32_t *rowof, con
 
 // The entries of keys no build row has (and the extra entry at cap): absent.
 __global__ void jt_pay_absent_kernel(VgJoinTable jt, const uint32_t *rowof, PayArgs P) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d <= jt.cap; d += stride) {
-        if (d < jt.cap && __ldg(rowof + d) != 0xFFFFFFFFu) continue;
-        ulonglong2 *o = (ulonglong2 *)(P.pay + d);
-        o[0] = make_ulonglong2(0ull, 0ull);
-        o[1] = make_ulonglong2(0ull, 0ull);
+    const int64_t step = (int64_t)gridDim.x * blockDim.x * kBuildU;
+    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x * kBuildU; b0 <= jt.cap; b0 += step) {
+        uint32_t v[kBuildU];
+#pragma unroll
+        for (int u = 0; u < kBuildU; u++) {
+            const int64_t d = b0 + (int64_t)u * blockDim.x + threadIdx.x;
+            v[u] = d < jt.cap ? __ldg(rowof + d) : 0xFFFFFFFFu;
+        }
+#pragma unroll
+        for (int u = 0; u < kBuildU; u++) {
+            const int64_t d = b0 + (int64_t)u * blockDim.x + threadIdx.x;
+            if (d <= jt.cap && v[u] == 0xFFFFFFFFu) vg_st256(P.pay + d, 0ull, 0ull, 0ull, 0ull);
+        }
     }
 }
 
@@ -617,7 +682,7 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
     }
     PayArgs P;
     memset(&P, 0, sizeof(P));
-    if (pay && jt->direct && jt->slots && n_pay >= 0 && n_pay <= 2) {
+    if (pay && jt->direct && jt->slots && n_keys == 1 && n_pay >= 0 && n_pay <= 2) {
         P.pay = pay;
         P.n_cols = n_pay;
         if (n_pay > 0) P.c0 = pay_cols[0];
@@ -625,6 +690,10 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
     }
     if (slots_ready) *slots_ready = 1;
     if (P.pay && n_build >= ((int64_t)1 << kRowBits)) P.pay = nullptr;   // too many rows for rowof: no payload
+    if (P.pay && ((uintptr_t)P.pay & 31u)) {
+        snprintf(g_err, sizeof(g_err), "join build: payload copy not 32-byte aligned");
+        return -1;
+    }
     if (P.pay) {
         // direct table with a payload copy: rows record themselves per key,
         // then each recorded row writes its key's entry with its payload
@@ -638,12 +707,12 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         if (check(cudaMemsetAsync(rowof, 0xFF, (size_t)jt->cap * 4, st), "join build")) return -1;
         vg_prof_begin(VG_PROF_JOIN_BUILD, st);
         if (n_build > 0) {
-            jt_rows_direct_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(*jt, K, n_build, rslot, counters, P,
-                                                                           rowof, mm);
-            jt_pay_scatter_kernel<<<grid_for(n_build, 256), 256, 0, st>>>(*jt, rowof, rslot, n_build, P, counters);
+            const int gb = grid_for((n_build + kBuildU - 1) / kBuildU, 256);
+            jt_rows_direct_kernel<<<gb, 256, 0, st>>>(*jt, K, n_build, rslot, counters, P, rowof, mm);
+            jt_pay_scatter_kernel<<<gb, 256, 0, st>>>(*jt, rowof, rslot, n_build, P, counters);
             vg_launch_counter += 2;
         }
-        jt_pay_absent_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, rowof, P);
+        jt_pay_absent_kernel<<<grid_for((jt->cap + kBuildU) / kBuildU, 256), 256, 0, st>>>(*jt, rowof, P);
         vg_launch_counter++;
         vg_prof_end(VG_PROF_JOIN_BUILD, st);
         uint32_t hc[4] = {0, 0, 0, 0};
