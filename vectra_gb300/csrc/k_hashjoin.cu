@@ -715,11 +715,14 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         jt_pay_absent_kernel<<<grid_for((jt->cap + kBuildU) / kBuildU, 256), 256, 0, st>>>(*jt, rowof, P);
         vg_launch_counter++;
         vg_prof_end(VG_PROF_JOIN_BUILD, st);
-        uint32_t hc[4] = {0, 0, 0, 0};
-        long long hm[6];
-        cudaMemcpyAsync(hc, counters, 16, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(hm, mm, 48, cudaMemcpyDeviceToHost, st);
+        // counters and the payload min / max words are adjacent (256 bytes
+        // apart): one read-back
+        long long hbuf[32 + 6];
+        if (check(cudaMemcpyAsync(hbuf, counters, 256 + 48, cudaMemcpyDeviceToHost, st), "join build")) return -1;
         if (check(cudaStreamSynchronize(st), "join build")) return -1;
+        uint32_t hc[4];
+        memcpy(hc, hbuf, sizeof(hc));
+        const long long *hm = hbuf + 32;
         if (hc[2]) {
             snprintf(g_err, sizeof(g_err), "join build: key outside the direct range (code %u)", hc[2]);
             return -1;

@@ -364,11 +364,13 @@ static int run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_logi
         L->replay = NULL;
         L->replay_n = 0;
         vg_check_rc(vgk_agg_launch(L, vg_stream()), "group-agg");
-        uint32_t c[2] = {0, 0}, err = 0, used = 0;
-        vg_d2h(c, S->counters, 8);
-        vg_d2h(&err, T->gt.err, 4);
-        vg_d2h(&used, T->gt.n_used, 4);
+        /* spill counters, error word and groups used: three copies, one wait */
+        uint32_t *hw = (uint32_t *)vg_pinned_scratch(16);
+        vg_d2h(hw, S->counters, 8);
+        vg_d2h(hw + 2, T->gt.err, 4);
+        vg_d2h(hw + 3, T->gt.n_used, 4);
         vg_sync();
+        uint32_t c[2] = {hw[0], hw[1]}, err = hw[2], used = hw[3];
         if (err & (VG_ERR_WAIT | VG_ERR_PROG)) vg_fail("group-agg kernel error (code %u)", err);
         if (err & (VG_ERR_FULL | VG_ERR_SPILL))
             vg_fail("group-agg: spill capacity exceeded (%u rows, %u entries)", c[0], c[1]);
@@ -415,6 +417,9 @@ static int run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_logi
     }
 }
 
+/* results up to this size are read back in one page-locked copy */
+#define kSmallResultBytes ((size_t)8 << 20)
+
 static VecBatch *emit_result(VgAgg *A, Plan *P, Table *T) {
     GroupAggNode *ga = &A->ga;
     uint32_t n = 0;
@@ -449,9 +454,21 @@ static VecBatch *emit_result(VgAgg *A, Plan *P, Table *T) {
     vg_dmemset(d_warn, 0, 4);
     vg_check_rc(vgk_group_finish(&T->gt, P->n_keys, P->key_type, d_slots, ng, P->fin, ga->n_aggs, kout, kval,
                                  aout, aval, d_warn, vg_stream()), "group finish");
+    /* a small result comes back in one copy of the whole output block
+     * (page-locked, one wait); a large one column by column */
+    const size_t out_bytes = per * (size_t)n_out + 4;
+    const char *hb = NULL;
+    if (out_bytes <= kSmallResultBytes) {
+        char *pin = (char *)vg_pinned_scratch(out_bytes);
+        vg_d2h(pin, blk, out_bytes);
+        vg_sync();
+        hb = pin;
+    }
     for (int k = 0; k < ga->n_keys; k++) {
         int t = P->key_type[k];
-        VecArray arr = vg_download_column(VEC_INT64, kout[k], kval[k], ng);
+        VecArray arr = hb ? vg_column_from_host(VEC_INT64, hb + per * (size_t)k,
+                                                hb + per * (size_t)k + a256((size_t)ng * 8 + 8), ng)
+                          : vg_download_column(VEC_INT64, kout[k], kval[k], ng);
         if (t == VEC_BOOL) {
             vg_sync();
             uint8_t *bv = (uint8_t *)vg_xcalloc((size_t)ng + 1, 1);
@@ -464,12 +481,18 @@ static VecBatch *emit_result(VgAgg *A, Plan *P, Table *T) {
         res->col_names[k] = vg_xstrdup(ga->key_names[k]);
     }
     for (int a = 0; a < ga->n_aggs; a++) {
-        res->columns[ga->n_keys + a] = vg_download_column(VEC_DOUBLE, aout[a], aval[a], ng);
+        const size_t o = per * (size_t)(ga->n_keys + a);
+        res->columns[ga->n_keys + a] = hb ? vg_column_from_host(VEC_DOUBLE, hb + o, hb + o + a256((size_t)ng * 8 + 8), ng)
+                                          : vg_download_column(VEC_DOUBLE, aout[a], aval[a], ng);
         res->col_names[ga->n_keys + a] = vg_xstrdup(ga->agg_specs[a].output_name);
     }
     uint32_t warn = 0;
-    vg_d2h(&warn, d_warn, 4);
-    vg_sync();
+    if (hb) {
+        memcpy(&warn, hb + per * (size_t)n_out, 4);
+    } else {
+        vg_d2h(&warn, d_warn, 4);
+        vg_sync();
+    }
     vg_warn_count((long)warn);
     vg_dfree(blk);
     vg_dfree(d_slots);

@@ -232,6 +232,28 @@ void vg_sync(void) {
     if (e != cudaSuccess) vg_fail("device execution failed: %s", cudaGetErrorString(e));
 }
 
+static void *g_pin = NULL;
+static size_t g_pin_bytes = 0;
+
+void *vg_pinned_scratch(size_t bytes) {
+    if (bytes <= g_pin_bytes) return g_pin;
+    size_t nb = 65536;
+    while (nb < bytes) nb <<= 1;
+    if (g_pin) {
+        vg_sync();                      /* no copy into the old buffer is in flight */
+        cudaFreeHost(g_pin);
+        g_pin = NULL;
+        g_pin_bytes = 0;
+    }
+    cudaError_t e = cudaMallocHost(&g_pin, nb);
+    if (e != cudaSuccess) {
+        g_pin = NULL;
+        vg_fail("page-locked allocation of %zu bytes failed: %s", nb, cudaGetErrorString(e));
+    }
+    g_pin_bytes = nb;
+    return g_pin;
+}
+
 /* ------------------------------------------------------------------ */
 /* host memory, batches, schemas                                       */
 /* ------------------------------------------------------------------ */
@@ -537,6 +559,25 @@ void vg_host_bufs_free(VgHostBufs *h) {
     free(h->tbuf);
     free((void *)h->done);
     free(h);
+}
+
+VecArray vg_column_from_host(int type, const void *values, const void *valid, int64_t n) {
+    VecArray a;
+    memset(&a, 0, sizeof(a));
+    a.type = (VecType)type;
+    a.length = n;
+    a.owns_data = 1;
+    a.validity = (uint8_t *)vg_xcalloc((size_t)vg_vbytes(n), 1);
+    size_t vb = value_bytes(type, n);
+    void *dst = vg_xcalloc(vb ? vb : 1, 1);
+    if (type == VEC_BOOL) a.buf.bln = (uint8_t *)dst;
+    else a.buf.i64 = (int64_t *)dst;
+    if (n > 0) {
+        memcpy(dst, values, vb);
+        if (valid) memcpy(a.validity, valid, (size_t)vg_vbytes(n));
+        else memset(a.validity, 0xFF, (size_t)vg_vbytes(n));
+    }
+    return a;
 }
 
 VecArray vg_download_column(int type, const void *d_data, const uint32_t *d_valid, int64_t n) {

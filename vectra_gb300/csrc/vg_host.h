@@ -28,6 +28,11 @@ void vg_h2d(void *dst, const void *src, size_t bytes);
 void vg_d2h(void *dst, const void *src, size_t bytes);
 void vg_dmemset(void *dst, int v, size_t bytes);
 void vg_sync(void);
+/* A page-locked host buffer of at least `bytes` for small read-backs:
+ * copies into it do not wait, so several go out before one vg_sync().
+ * Kept for the process; a larger request replaces it (after a sync), so
+ * a caller reads what it copied before asking again. */
+void *vg_pinned_scratch(size_t bytes);
 
 /* ---- host batches ---- */
 void *vg_xmalloc(size_t n);
@@ -64,6 +69,9 @@ void vg_dbatch_release(VgDBatch *b);
 /* Device column -> newly malloc'd host VecArray of n values. */
 VecArray vg_download_column(int type, const void *d_data, const uint32_t *d_valid, int64_t n);
 VecArray vg_host_column(int type, int64_t n, void *values, const uint32_t *d_valid);
+/* Newly malloc'd host VecArray of n values copied from host memory (values
+ * of value_bytes(type, n), validity as the device's 32-bit words). */
+VecArray vg_column_from_host(int type, const void *values, const void *valid, int64_t n);
 void vg_copy_after_main(void);
 void vg_d2h_copy(void *dst, const void *src, size_t bytes);
 void vg_copy_sync(void);
