@@ -292,6 +292,23 @@ def ja_dense_keys(E, temp_dir):     # join + aggregate keyed on a small-range bu
     return out
 
 
+def ja_payload_edges(E, temp_dir):  # join + aggregate: NA build keys, a bool build column, NA payload values
+    rng = np.random.default_rng(23)
+    nf, nd = 6000, 333
+    ids = rng.permutation(nd) + 1
+    fact = {"key": (rng.integers(1, nd + 20, nf), rng.random(nf) > 0.02),
+            "value": (rng.normal(0, 5, nf), rng.random(nf) > 0.03)}
+    dim = {"id": (ids, rng.random(nd) > 0.07),
+           "flag": (rng.integers(0, 2, nd).astype(np.uint8), rng.random(nd) > 0.1),
+           "weight": (rng.random(nd), rng.random(nd) > 0.05)}
+    out = []
+    for kind in ("left_join", "inner_join"):
+        out += (getattr(tbl(E, fact, batch_rows=1500), kind)(tbl(E, dim, batch_rows=100), {"key": "id"})
+                .group_by("flag").summarise(temp_dir=temp_dir, s=("sum", col("value") * col("weight")),
+                                            sr=("sum", col("value") * col("weight"), True), n=("n",)).batches())
+    return out
+
+
 # ---------------------------------------------------------------------------
 # seeded random cases
 # ---------------------------------------------------------------------------
@@ -334,7 +351,7 @@ FILTER_CASES = [f_simple, f_equality, f_and_or_not, f_na_dropped, f_is_na, f_kle
                 f_empty, f_general_expr, f_int_vs_double_literal]
 GROUP_CASES = [g_basic, g_na_key, g_multi_key, g_na_semantics, g_int_sum_double, g_resize_200,
                g_filter_then_group, g_ungrouped, g_nested_expr, g_bool_and_double_keys, ja_join_agg,
-               ja_dense_keys, ja_join_agg_sparse, ja_dup_build_keys]
+               ja_dense_keys, ja_join_agg_sparse, ja_dup_build_keys, ja_payload_edges]
 JOIN_CASES = [j_inner_left_semi_anti, j_duplicates, j_na_keys, j_suffix, j_coerce, j_streaming,
               j_after_filter, j_full]
 
