@@ -273,8 +273,7 @@ static int queryset_prepare(const VgpuSetQuery *qs, int n, const Cfg &cfg, void 
     const int64_t kChunk = cfg.chunk;
     *plan_out = nullptr;
     if (n <= 0 || !qs) { snprintf(g_err, sizeof(g_err), "vgpu_queryset_prepare: no queries"); return -1; }
-    Plan *P = new Plan();
-    memset(P, 0, sizeof(*P));
+    Plan *P = new Plan();      // value-initialised: every pointer and count zero
     P->n_inst = n;
     std::vector<Inst> inst((size_t)n);
     std::vector<Item> it1, it2, it3;
