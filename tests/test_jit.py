@@ -8,10 +8,10 @@ import re
 import pytest
 
 
-@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4, 5, 6, 7],
+@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4, 5, 6, 7, 8],
                          ids=["join_direct_payload", "filter_sel_mean", "two_keys_all_accs", "inner_join_gather",
                               "join_hashed_payload", "partition_cta_ranges", "partition_filter_holes",
-                              "partition_global_cursors"])
+                              "partition_global_cursors", "filter_queued_mean"])
 def test_generated_kernel_compiles(shape):
     import vectra_gb300
     lib = vectra_gb300.load()

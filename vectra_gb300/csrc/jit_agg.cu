@@ -203,6 +203,9 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
             L.join_kind, L.jkey_col[0], L.jkey_conv[0], L.jt.key_types[0], L.jt.direct ? 1 : 0);
     fmt(s, "#define VGJ_NK %d\n#define VGJ_DENSE %d\n#define VGJ_TRACK %d\n#define VGJ_PART %d\n", L.n_keys,
         L.dense ? 1 : 0, L.track_first ? 1 : 0, L.part ? 1 : 0);
+    // rows that pass a filter queued per warp (few of a step's rows pass)
+    fmt(s, "#define VGJ_COMPACT %d\n",
+        (L.pred.n_terms > 0 && !L.has_join && !L.part && !L.sel && !L.track_first && !L.dense) ? 1 : 0);
     // per-CTA record ranges; holes when a filter or an inner join drops rows
     fmt(s, "#define VGJ_PART_CTA %d\n#define VGJ_PART_HOLES %d\n#define VGJ_OFF_PCUR %lluu\n",
         (L.part && L.po.cta_off) ? 1 : 0,
@@ -884,9 +887,11 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
         L.jpay_n = 2;
         L.jt.direct = shape == 0;   // shape 4: hashed table, linear-probing chain
         L.jt.dmin = 1;
-    } else if (shape == 1) {
+    } else if (shape == 1 || shape == 8) {
+        // filter -> group_by -> sum, n: 1 behind a selection vector, 8 over
+        // whole batches (passing rows queued per warp)
         static int32_t sel[4];
-        L.sel = sel;
+        L.sel = shape == 1 ? sel : nullptr;
         L.n_pcols = 3;
         L.pcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
         L.pcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};

@@ -16,6 +16,13 @@
 // Partition mode (VGJ_PART, hooks vgj_reserve / vgj_write): rows with a valid key are
 // written as records into their key-range bucket instead; the cache then
 // holds the NA-key group alone, one slot per warp.
+// Queued mode (VGJ_COMPACT: a filter, no join, no partition, no selection
+// vector, no first-seen order): when few of a warp's rows pass the filter,
+// their row numbers join a per-warp queue (one slot per lane) instead of
+// being aggregated in place, where one or two live lanes would run the
+// whole update path; a full queue is aggregated by all 32 lanes, each
+// reloading its row.  A step in which more than 32 of the warp's rows pass
+// is aggregated in place as usual.
 
 #pragma once
 
@@ -97,10 +104,51 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
         }
     }
 #endif
+#if VGJ_COMPACT
+    // the warp's queue: lane i holds slot i, qn slots are used (warp-uniform)
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t qn = 0;
+    int64_t qrow = 0;
+    // aggregates the first nq queued rows, one per lane (the hashed-cache
+    // update of the in-place path below, for one row)
+    auto flush_queue = [&](uint32_t nq) {
+        if (lane >= nq) return;
+        Rows Q;
+        int64_t qp[R];
+#pragma unroll
+        for (int j = 0; j < R; j++) qp[j] = qrow;
+        vgj_load_probe(L, Q, qrow, 1, false, qp, 1u);
+        Keys k;
+#pragma unroll
+        for (int i = 0; i < VG_MAX_KEYS; i++) k.w[i] = 0;
+        uint32_t nm = 0;
+        vgj_keys(Q, 0, k, nm);
+        int err = 0;
+        const int found =
+            cache_find<S, VGJ_NK>(sm, VGJ_OFF_STATE, VGJ_OFF_NM, VGJ_OFF_KEYS, &cache_used, k, nm, kt, &err);
+        if (err) atomicOr(L.gt.err, VG_ERR_WAIT);
+        const uint32_t fail = found < 0 ? 0u : vgj_cache_update(sm, found, Q, 0);
+        if (found >= 0 && !fail) return;
+        const int64_t g = gt_find_insert(L.gt, k, VGJ_NK, kt, nm, hash_k(k, VGJ_NK, nm));
+        if (g < 0) {
+            if (found < 0) spill_row(L, qrow, 0, -1);
+            else vgj_spill(L, qrow, fail);
+            return;
+        }
+        vgj_global_update(L, g, Q, 0, found < 0 ? 0xFFFFFFFFu : fail);
+    };
+#endif
     for (int64_t base = (int64_t)blockIdx.x * tile; base < n_rows; base += step) {
         const int64_t r0 = base + (int64_t)R * threadIdx.x;
+#if VGJ_COMPACT
+        // every lane takes every step (the queue below is warp-collective);
+        // lanes past the end have no rows
+        const bool in_range = r0 < n_rows;
+#else
         if (r0 >= n_rows) continue;
-        const int nv = (int)(n_rows - r0 < R ? n_rows - r0 : R);
+        const bool in_range = true;
+#endif
+        const int nv = in_range ? (int)(n_rows - r0 < R ? n_rows - r0 : R) : 0;
         const uint32_t all = (1u << nv) - 1u;
         int64_t phys[R];
 #pragma unroll
@@ -130,6 +178,52 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
         uint32_t live = all;
 #if VGJ_PRED
         live &= vgj_pred(L, X);
+#endif
+#if VGJ_COMPACT
+        {
+            // the step's passing rows, numbered across the warp in lane order
+            const uint32_t cnt = (uint32_t)__popc(live);
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= (uint32_t)o) incl += v;
+            }
+            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            if (total == 0u) continue;
+            if (total <= 32u) {
+                // slot s takes the step's row k = (s - qn) mod 32: slots
+                // qn..31 first, then, after the queue is aggregated, the
+                // slots from 0 on
+                const uint32_t k = (lane - qn) & 31u;
+                uint32_t pos = 0;                   // owner: the lanes whose rows end at or before k
+#pragma unroll
+                for (uint32_t w = 16; w; w >>= 1) {
+                    const uint32_t v = __shfl_sync(0xFFFFFFFFu, incl, pos + w - 1);
+                    if (v <= k) pos += w;
+                }
+                const uint32_t o_excl = __shfl_sync(0xFFFFFFFFu, incl - cnt, pos);
+                const uint32_t o_live = __shfl_sync(0xFFFFFFFFu, live, pos);
+                const int64_t o_r0 = __shfl_sync(0xFFFFFFFFu, r0, pos);
+                const bool has = k < total;
+                uint32_t m = o_live;                // the (k - o_excl)-th live row of the owner
+                const uint32_t t = k - o_excl;
+#pragma unroll
+                for (uint32_t i = 0; i + 1 < (uint32_t)R; i++)
+                    if (i < t) m &= m - 1u;
+                const int64_t row = o_r0 + (int64_t)(__ffs(m) - 1);
+                if (has && lane >= qn) qrow = row;
+                if (qn + total >= 32u) {
+                    flush_queue(32u);
+                    const uint32_t before = qn;
+                    qn = qn + total - 32u;
+                    if (has && lane < before) qrow = row;
+                } else {
+                    qn += total;
+                }
+                continue;
+            }
+        }
 #endif
         uint32_t matched = 0;
 #if VGJ_JOIN
@@ -328,6 +422,9 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
         }
     }
 
+#if VGJ_COMPACT
+    flush_queue(qn);
+#endif
     __syncthreads();
 #if VGJ_PART_CTA && VGJ_PART_HOLES
     {
