@@ -12,6 +12,12 @@
 //
 // Host code only (no kernels of its own); the headers NVRTC needs are
 // embedded at build time (vg_jit_headers.inc, written by build.py).
+//
+// The generated hooks restate, per plan: the predicate's comparisons after
+// type promotion and its Kleene logic (vec_cmp / vec_bool_binary,
+// src/scalar_ops.c:70-203), projected arithmetic (vec_arith,
+// src/scalar_ops.c:11-66) and each accumulator's update (agg_accum_feed,
+// src/agg_ops.c:93-158).
 
 #include <cstdarg>
 #include <cstdio>

@@ -1,4 +1,6 @@
 // k_common.cuh -- device helpers shared by libvgpu's kernels (sm_103a).
+// Validity follows the reference's bit-packed layout, bit i set = row i
+// valid (VecArray.validity, src/types.h:47), read as 32-bit words.
 #pragma once
 
 #ifdef __CUDACC_RTC__

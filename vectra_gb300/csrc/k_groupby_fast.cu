@@ -13,6 +13,10 @@
 //    shared-memory pointers live in registers;
 //  * a group key with a small known range (a build-side attribute) indexes
 //    the shared cache directly instead of hashing into it.
+// Semantics are those of the reference's hash aggregation loop
+// (hash_agg_next_batch, src/group_agg.c:155-281) with its accumulators
+// (agg_accum_feed, src/agg_ops.c:93-158), behind a single-key join probe
+// (join_probe_one, src/join.c:262-480) where the plan has one.
 
 #include "k_groupby_dev.cuh"
 

@@ -16,6 +16,9 @@
 // Partition mode (VGJ_PART, hooks vgj_reserve / vgj_write): rows with a valid key are
 // written as records into their key-range bucket instead; the cache then
 // holds the NA-key group alone, one slot per warp.
+// Semantics restated: hash_agg_next_batch (src/group_agg.c:155-281) with
+// agg_accum_feed (src/agg_ops.c:93-158), behind join_probe_one
+// (src/join.c:262-480; NA keys never match, src/join.c:77-113).
 // Queued mode (VGJ_COMPACT: a filter, no join, no partition, no selection
 // vector, no first-seen order): when few of a warp's rows pass the filter,
 // their row numbers join a per-warp queue (one slot per lane) instead of

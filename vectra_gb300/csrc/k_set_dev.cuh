@@ -1,7 +1,10 @@
 // k_set_dev.cuh -- device building blocks shared by the query-set and the
 // serving kernels (k_batch.cu, k_serve.cu): per-query group tables with
 // exact double sums and per-query join / key-set tables, in global memory
-// (small ones stay in L2 while their query runs).
+// (small ones stay in L2 while their query runs).  Each query keeps the
+// node path's semantics: groups and accumulators as in hash_agg_next_batch
+// (src/group_agg.c:155-281) and agg_accum_feed (src/agg_ops.c:93-158),
+// inner-join matches as in join_probe_one (src/join.c:262-480).
 #pragma once
 #include "k_groupby_dev.cuh"
 

@@ -1,5 +1,8 @@
 // k_sort.cu -- device-wide building blocks: a stable LSD radix sort of
 // (64-bit key, 32-bit value) pairs and exclusive prefix sums (sm_103a).
+// The group order built on them is the reference's sorted path's:
+// ascending key, NA last (compare_value, src/sort.c:32-38;
+// sorted_agg_next_batch, src/group_agg.c:466-585).
 
 #include <cstdio>
 #include <cstring>

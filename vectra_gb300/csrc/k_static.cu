@@ -5,6 +5,7 @@
 // selected-row total and an error word) out of this file-scope array
 // instead of allocating it.  Its address is looked up once per device with
 // cudaGetSymbolAddress and cached; that first lookup is the only set-up.
+// The selection it computes is filter_next_batch's (src/filter.c:13-64).
 
 #include <cstdio>
 #include "vgpu_internal.h"

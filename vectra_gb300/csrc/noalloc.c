@@ -5,7 +5,8 @@
  *
  * Nothing here allocates: no device allocation of any kind and no host
  * heap (the predicate compiles into structs on the stack; the column views
- * are on the stack).  No counterpart in the reference engine.
+ * are on the stack).  No counterpart in the reference engine; the
+ * selection is filter_next_batch's (src/filter.c:13-64).
  */
 #include <string.h>
 
