@@ -216,6 +216,22 @@ def profile_traffic():
     return None
 
 
+def max_over_ranks(torch, ms, device):
+    """The slowest rank's time: every rank passes its own and gets the
+    maximum (all ranks then leave together).  The job's time per step is the
+    slowest replica's."""
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.barrier()
+    return float(t.item())
+
+
+def whole_job_rate(rows_per_rank, world, ms_per_step):
+    """Rows per second of the whole job: every replica processes its own
+    rows_per_rank in each step, and a step lasts as long as the slowest."""
+    return rows_per_rank * world / (ms_per_step * 1e-3)
+
+
 def gpu_arm(args, rank, world):
     import torch
     import vectra_gb300
@@ -265,10 +281,7 @@ def gpu_arm(args, rank, world):
         lib.vgpu_profile_enable(0)
         ms = e0.elapsed_time(e1)
         if world > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
-            torch.distributed.barrier()
+            ms = max_over_ranks(torch, ms, dev)
         return ms / k, wall / k, lib.vgpu_kernel_launches() - l0
 
     lib.vgpu_agg_phase_ms.restype = C.c_double
@@ -332,7 +345,7 @@ def gpu_arm(args, rank, world):
     # (the join build reads the third, id)
     kernel_b = fact_b + dim_b * 2 // 3
     achieved = kernel_b / (kernel_ms * 1e-3) / 1e9
-    value = rows * world / (ms_step * 1e-3)
+    value = whole_job_rate(rows, world, ms_step)
     line = {
         "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -348,10 +361,10 @@ def gpu_arm(args, rank, world):
                      "traffic": profile_traffic()},
         "host_phases_ms": agg_phases,
         "join_build_ms": build_ms / max(1, build_n.value),
-        "e2e": {"value": rows * world / (e2e_ms * 1e-3), "unit": "rows/s", "ms_per_step": e2e_ms,
+        "e2e": {"value": whole_job_rate(rows, world, e2e_ms), "unit": "rows/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "node C API, page-locked host columns read in place by the kernels (VGPU_SRC_MAPPED)"},
-        "e2e_copy": {"value": rows * world / (copy_ms * 1e-3), "unit": "rows/s", "ms_per_step": copy_ms,
+        "e2e_copy": {"value": whole_job_rate(rows, world, copy_ms), "unit": "rows/s", "ms_per_step": copy_ms,
                      "path": "node C API, page-locked host columns staged by async copies, 16M-row fact batches"},
         "gpu_launches": launches,
         "clocks": clocks,
