@@ -448,9 +448,58 @@ def cpu_baseline(torch=None, repeats=1):
             "seconds": best}
 
 
+def cpu_workload_sample(name, torch, scale=1):
+    """One run of the CPU restatement of the reference path (the oracle port,
+    single-threaded like the reference engine) on a bounded sample of a
+    workload, same generators and distributions as the GPU run (torch on the
+    CPU: a different random stream), further divided by scale.  Returns
+    (input rows, seconds, sample)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from engines import OracleEngine
+    import vectra_gb300.workloads as W
+    E = OracleEngine()
+    cpu = torch.device("cpu")
+
+    def host(cols):
+        return {k: (v.numpy(), None if m is None else m.numpy()) for k, (v, m) in cols.items()}
+
+    if name == "filter_group":
+        n = 10_000_000 // scale
+        cols = host(W.gen_filter_group(torch, n, 0, cpu))
+        t0 = time.perf_counter()
+        W.run_filter_group(E, E.make_source(cols, 100_000), temp_dir=E.tmp)
+        return n, time.perf_counter() - t0, "%d rows (the whole workload at scale 1) in 100k-row batches" % n
+    if name == "high_card":
+        n, distinct = 200_000_000 // (SAMPLE_DIV * scale), 50_000_000 // (SAMPLE_DIV * scale)
+        cols, _ = W.gen_high_card(torch, n, distinct, 0, cpu)
+        cols = host(cols)
+        t0 = time.perf_counter()
+        W.run_high_card(E, E.make_source(cols, 100_000), temp_dir=E.tmp)
+        return n, time.perf_counter() - t0, ("1/%d-scale: %d rows over %d distinct keys in 100k-row batches, "
+                                             "sort path (spilled runs)" % (SAMPLE_DIV * scale, n, distinct))
+    raise ValueError("no CPU sample for workload %r" % name)
+
+
+def workload_reference_arm(args):
+    import torch
+    for _ in range(args.warmup):
+        cpu_workload_sample(args.workload, torch, args.scale)
+    runs = [cpu_workload_sample(args.workload, torch, args.scale) for _ in range(max(1, args.steps))]
+    secs = statistics.median([r[1] for r in runs])
+    v = runs[0][0] / secs
+    return {"impl": "reference", "metric": "rows/s (input rows per second, whole query)", "value": v,
+            "unit": "rows/s", "n_gpus": 1, "steps": len(runs), "warmup": args.warmup, "ms_per_step": 1e3 * secs,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64+f64",
+            "data": "synthetic (torch CPU generator, seed 0)", "config": {"workload": args.workload},
+            "cpu_baseline": {"value": v, "unit": "rows/s", "cores": 1, "kind": "port", "sample": runs[0][2]},
+            "e2e": {"value": v, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def reference_arm(args, rank, world):
     if rank != 0:
         return None
+    if args.workload in ("filter_group", "high_card"):
+        return workload_reference_arm(args)
     for _ in range(args.warmup):
         cpu_baseline()
     vals = []

@@ -1,0 +1,22 @@
+"""bench.py --impl reference on the other workloads: the CPU restatement of
+the reference path (single-threaded, like the reference engine) timed on a
+sample of the filter + group-by and high-cardinality workloads, here at a
+very small scale."""
+import argparse
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("workload", ["filter_group", "high_card"])
+def test_cpu_reference_sample_of_a_workload(workload):
+    sys.path.insert(0, ROOT)
+    import bench
+    args = argparse.Namespace(workload=workload, steps=1, warmup=0, scale=1000)
+    line = bench.reference_arm(args, 0, 1)
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] == 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0

@@ -52,3 +52,4 @@ def test_whole_job_rate_counts_every_replica():
     assert one == rows / 2.0e-3
     # two replicas, the slower at 2.5 ms: twice the rows over the slower time
     assert bench.whole_job_rate(rows, 2, 2.5) == 2 * rows / 2.5e-3
+
