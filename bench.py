@@ -477,6 +477,28 @@ def cpu_workload_sample(name, torch, scale=1):
         W.run_high_card(E, E.make_source(cols, 100_000), temp_dir=E.tmp)
         return n, time.perf_counter() - t0, ("1/%d-scale: %d rows over %d distinct keys in 100k-row batches, "
                                              "sort path (spilled runs)" % (SAMPLE_DIV * scale, n, distinct))
+    if name == "query_set":
+        # the queries the GPU plain path samples: 128 of the 4096 instances,
+        # one after another through the node API
+        from vectra_gb300.plan import tbl
+        n_inst = 4096 // scale
+        qs = W.gen_query_set(torch, n_inst, 0, cpu)
+        rng = np.random.default_rng(2)                     # the GPU arm's draws: checked sample, then plain sample
+        rng.choice(n_inst, size=min(256, n_inst), replace=False)
+        pick = rng.choice(n_inst, size=min(128, n_inst), replace=False)
+        off = np.concatenate([[0], np.cumsum(qs["rows"])])
+        boff = np.concatenate([[0], np.cumsum(qs["bcard"])])
+        key, value, bkey = qs["key"].numpy(), qs["value"].numpy(), qs["bkey"].numpy()
+        t0 = time.perf_counter()
+        for i in pick:
+            k = key[off[i]:off[i + 1]]
+            if qs["kind"][i] == W.SET_GROUP:
+                (tbl(E, {"key": k, "value": value[off[i]:off[i + 1]]}).group_by("key")
+                 .summarise(temp_dir=None, s=("sum", "value"), m=("mean", "value"), n=("n",)).batches())
+            else:
+                tbl(E, {"key": k}).inner_join(tbl(E, {"key": bkey[boff[i]:boff[i + 1]]}), "key").batches()
+        return len(pick), time.perf_counter() - t0, ("%d of the %d instances, one query after another "
+                                                      "(hash-path group-by, inner join)" % (len(pick), n_inst))
     raise ValueError("no CPU sample for workload %r" % name)
 
 
@@ -487,18 +509,22 @@ def workload_reference_arm(args):
     runs = [cpu_workload_sample(args.workload, torch, args.scale) for _ in range(max(1, args.steps))]
     secs = statistics.median([r[1] for r in runs])
     v = runs[0][0] / secs
-    return {"impl": "reference", "metric": "rows/s (input rows per second, whole query)", "value": v,
-            "unit": "rows/s", "n_gpus": 1, "steps": len(runs), "warmup": args.warmup, "ms_per_step": 1e3 * secs,
+    if args.workload == "query_set":
+        metric, unit = "queries/s (query set of small group-by / inner-join instances)", "queries/s"
+    else:
+        metric, unit = "rows/s (input rows per second, whole query)", "rows/s"
+    return {"impl": "reference", "metric": metric, "value": v,
+            "unit": unit, "n_gpus": 1, "steps": len(runs), "warmup": args.warmup, "ms_per_step": 1e3 * secs,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64+f64",
             "data": "synthetic (torch CPU generator, seed 0)", "config": {"workload": args.workload},
-            "cpu_baseline": {"value": v, "unit": "rows/s", "cores": 1, "kind": "port", "sample": runs[0][2]},
-            "e2e": {"value": v, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "cpu_baseline": {"value": v, "unit": unit, "cores": 1, "kind": "port", "sample": runs[0][2]},
+            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def reference_arm(args, rank, world):
     if rank != 0:
         return None
-    if args.workload in ("filter_group", "high_card"):
+    if args.workload in ("filter_group", "high_card", "query_set"):
         return workload_reference_arm(args)
     for _ in range(args.warmup):
         cpu_baseline()

@@ -1,7 +1,7 @@
 """bench.py --impl reference on the other workloads: the CPU restatement of
 the reference path (single-threaded, like the reference engine) timed on a
-sample of the filter + group-by and high-cardinality workloads, here at a
-very small scale."""
+sample of the filter + group-by, high-cardinality and query-set workloads,
+here at a very small scale."""
 import argparse
 import os
 import sys
@@ -11,7 +11,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-@pytest.mark.parametrize("workload", ["filter_group", "high_card"])
+@pytest.mark.parametrize("workload", ["filter_group", "high_card", "query_set"])
 def test_cpu_reference_sample_of_a_workload(workload):
     sys.path.insert(0, ROOT)
     import bench
