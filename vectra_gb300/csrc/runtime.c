@@ -53,11 +53,14 @@ void vg_set_error(const char *fmt, ...) {
     va_end(ap);
 }
 
+static void sync_before_error(void);
+
 void vg_fail(const char *fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
     vsnprintf(g_msg, sizeof(g_msg), fmt, ap);
     va_end(ap);
+    sync_before_error();
     vectra_error("%s", g_msg);
     abort();   /* vectra_error does not return */
 }
@@ -116,6 +119,13 @@ int vgpu_init(int device) {
     }
     g_inited = 1;
     return 0;
+}
+
+/* Before an error leaves the library, the failed call's kernels and copies
+ * on the library's stream end (a device that has faulted answers at once
+ * with its error, which is ignored here: the message is already set). */
+static void sync_before_error(void) {
+    if (g_inited) (void)cudaStreamSynchronize(g_use_user ? g_user_stream : g_own_stream);
 }
 
 void vg_ensure_init(void) {
