@@ -50,3 +50,21 @@ def test_partition_reducer_compiles(shape):
     assert 0 < regs.value <= 64, log
     kernel = re.search(r"Function properties for vg_jit_pagg\s*\n.*?(\d+) bytes spill stores", log)
     assert kernel and int(kernel.group(1)) <= 256, log
+
+
+@pytest.mark.parametrize("shape,queued", [(8, 1), (1, 0), (9, 0), (10, 0), (6, 0), (0, 0)],
+                         ids=["filter_whole_batches", "filter_sel", "filter_first_seen_order", "filter_join",
+                              "filter_partition", "no_filter"])
+def test_queue_only_behind_a_filter(shape, queued, tmp_path, monkeypatch):
+    """Passing rows are queued per warp only for a filter over whole batches
+    with no join, no partition mode and no first-seen order."""
+    import vectra_gb300
+    dump = tmp_path / "src.cu"
+    monkeypatch.setenv("VGPU_JIT_DUMP", str(dump))
+    lib = vectra_gb300.load()
+    lib.vgk_jit_error.restype = C.c_char_p
+    regs = C.c_int(-1)
+    assert lib.vgpu_jit_selftest(shape, C.byref(regs)) == 0, lib.vgk_jit_error().decode()
+    src = dump.read_text() if dump.exists() else ""
+    assert src, "the compiled source was not written (already compiled in this process?)"
+    assert ("#define VGJ_COMPACT %d\n" % queued) in src

@@ -378,11 +378,20 @@ int nvrtc_cubin(const std::string &src, std::vector<char> &cubin, int *spill, st
 int compile_plan(const VgAggLaunch &L, int S, bool vec, std::vector<char> &cubin, Shape &used,
                  std::string *log_out) {
     Shape sh = plan_shape(L);
+    std::string src;
     for (;;) {
         int spill = 0;
-        if (nvrtc_cubin(gen_source(L, S, vec, sh), cubin, &spill, log_out) != 0) return -1;
+        src = gen_source(L, S, vec, sh);
+        if (nvrtc_cubin(src, cubin, &spill, log_out) != 0) return -1;
         if (spill == 0 || sh.threads <= 256) break;
         sh.threads /= 2;
+    }
+    // VGPU_JIT_DUMP=<file>: append the source of each plan compiled
+    if (const char *dump = getenv("VGPU_JIT_DUMP")) {
+        if (FILE *f = fopen(dump, "a")) {
+            fputs(src.c_str(), f);
+            fclose(f);
+        }
     }
     used = sh;
     return 0;
@@ -467,15 +476,6 @@ JitKernel *plan_kernel(const VgAggLaunch *L, int S, bool vec) {
     if (it == g_cache.end()) {
         JitKernel k;
         std::vector<char> cubin;
-        // VGPU_JIT_DUMP=<file>: append each newly compiled plan's source
-        const char *dump = getenv("VGPU_JIT_DUMP");
-        if (dump) {
-            FILE *f = fopen(dump, "a");
-            if (f) {
-                fputs(src.c_str(), f);
-                fclose(f);
-            }
-        }
         if (compile_plan(*L, S, vec, cubin, k.shape, nullptr) != 0) return nullptr;
         if (load_kernel(cubin, k) != 0) return nullptr;
         it = g_cache.emplace(src, k).first;
@@ -865,7 +865,7 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
     memset(&L, 0, sizeof(L));
     static double dummy[4];
     L.cache_slots = 1024;
-    if (shape == 0 || shape == 4) {
+    if (shape == 0 || shape == 4 || shape == 10) {
         L.n_pcols = 2;
         L.pcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
         L.pcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};
@@ -891,13 +891,19 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
         L.dense_n = 256;
         L.jpay = (const VgJPay *)dummy;
         L.jpay_n = 2;
-        L.jt.direct = shape == 0;   // shape 4: hashed table, linear-probing chain
+        L.jt.direct = shape != 4;   // shape 4: hashed table, linear-probing chain
         L.jt.dmin = 1;
-    } else if (shape == 1 || shape == 8) {
+        if (shape == 10) {          // a filter on the probe side in front of the join
+            L.pred.n_terms = 1;
+            L.pred.term[0] = VgTerm{1, VG_TERM_RANGE, VG_DOM_DOUBLE, 0, 0, 0};
+        }
+    } else if (shape == 1 || shape == 8 || shape == 9) {
         // filter -> group_by -> sum, n: 1 behind a selection vector, 8 over
-        // whole batches (passing rows queued per warp)
+        // whole batches (passing rows queued per warp), 9 the same in
+        // first-seen group order
         static int32_t sel[4];
         L.sel = shape == 1 ? sel : nullptr;
+        L.track_first = shape == 9;
         L.n_pcols = 3;
         L.pcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
         L.pcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};
