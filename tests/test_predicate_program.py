@@ -6,7 +6,9 @@ compiled, the program is run row by row as the filter kernel runs it
 an integer division by zero, IEEE double arithmetic with fmod, a NaN
 comparing equal, R's three-valued AND / OR), and the rows it keeps must be
 exactly the rows the CPU oracle's filter keeps (src/expr.c:91-281,
-src/scalar_ops.c:11-203)."""
+src/scalar_ops.c:11-203).  Likewise the values the fused kernels compute
+(vg_compile_value: one operand, or two with one arithmetic operator, after
+the reference's type promotion) against the oracle's projection."""
 import ctypes as C
 import struct
 
@@ -193,3 +195,98 @@ def test_programs_keep_the_oracles_rows(seed, oracle):
                 keep.append(r)
         assert keep == want, repr(e.kw)
     assert ran > 60
+
+
+# ---------------------------------------------------------------------------
+# values the fused kernels compute (aggregate inputs, keys): vg_compile_value
+# ---------------------------------------------------------------------------
+
+SIDE_PROBE, SIDE_BUILD, SIDE_LIT, SIDE_NA = 0, 1, 2, 3
+
+
+class Operand(C.Structure):
+    _fields_ = [("side", C.c_int32), ("col", C.c_int32), ("type", C.c_int32), ("pad", C.c_int32),
+                ("lit", C.c_int64)]
+
+
+class Value(C.Structure):
+    _fields_ = [("op", C.c_int32), ("type", C.c_int32), ("a", Operand), ("b", Operand)]
+
+
+def operand(o, cols, r, want):
+    """The operand's (payload, valid) for row r, coerced to type `want`."""
+    if o.side == SIDE_NA:
+        return 0, False
+    if o.side == SIDE_LIT:
+        x, ok, ty = o.lit & M64, True, o.type
+    else:
+        v, valid, ty = cols[o.col]
+        x = f2b(float(v[r])) if ty == abi.VEC_DOUBLE else int(v[r]) & M64
+        ok = bool(valid[r])
+    if want == abi.VEC_DOUBLE and ty != abi.VEC_DOUBLE:
+        x = f2b(float(s64(x)))
+    return x, ok
+
+
+def value_of(val, cols, r):
+    a, oka = operand(val.a, cols, r, val.type)
+    if val.op == 0:
+        return a, oka
+    b, okb = operand(val.b, cols, r, val.type)
+    if not (oka and okb):
+        return 0, False
+    if val.type == abi.VEC_DOUBLE:
+        return f2b(arith_f64(b2f(a), b2f(b), chr(val.op))), True
+    v, ok = arith_i64(s64(a), s64(b), chr(val.op))
+    return v & M64, ok
+
+
+def random_operand(rng):
+    k = rng.random()
+    if k < 0.3: return col("i")
+    if k < 0.6: return col("d")
+    if k < 0.7: return col("b")
+    if k < 0.75: return lit(None)
+    return lit(int(rng.integers(-3, 4))) if rng.random() < 0.5 else lit(float(rng.choice([0.0, -0.0, 2.5, 1e300])))
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_values_match_the_oracles_projection(seed, oracle):
+    import vectra_gb300
+    lib = vectra_gb300.load()
+    lib.vg_compile_value.argtypes = [C.c_void_p, MAPFN, C.c_void_p, C.c_int, C.POINTER(Value)]
+    lib.vg_compile_value.restype = C.c_int
+    rng = np.random.default_rng(50 + seed)
+    t = random_table(rng, 200)
+    names = ["i", "d", "b"]
+    types = [abi.VEC_INT64, abi.VEC_DOUBLE, abi.VEC_BOOL]
+
+    def colmap(ctx, name, ty):
+        k = names.index(name.decode())
+        ty[0] = types[k]
+        return k
+    cmap = MAPFN(colmap)
+    cols = [(t[n][0], t[n][1], ty) for n, ty in zip(names, types)]
+    done = 0
+    for _ in range(60):
+        a, b = random_operand(rng), random_operand(rng)
+        op = ["+", "-", "*", "/", "%"][int(rng.integers(0, 5))]
+        e = {"+": a + b, "-": a - b, "*": a * b, "/": a / b, "%": a % b}[op]
+        v = Value()
+        if lib.vg_compile_value(C.cast(e.to_c(list(zip(names, types))), C.c_void_p), cmap, None, SIDE_PROBE,
+                                C.byref(v)) <= 0:
+            continue
+        done += 1
+        got = tbl(oracle, {k: t[k] for k in names}).mutate(v=e).collect()["v"]
+        for r in range(200):
+            x, ok = value_of(v, cols, r)
+            assert ok == bool(got[1][r]), (repr(e.kw), r)
+            if not ok:
+                continue
+            want = float(got[0][r]) if v.type == abi.VEC_DOUBLE else int(got[0][r])
+            if v.type == abi.VEC_DOUBLE:
+                y = b2f(x)
+                assert (y != y and want != want) or f2b(y) == f2b(want), (repr(e.kw), r, y, want)
+            else:
+                assert s64(x) == want, (repr(e.kw), r, s64(x), want)
+    assert done > 40
