@@ -10,7 +10,9 @@
  * src/group_agg.c and src/join.c hands every plan the R front end and the
  * optimizer build to the GPU.  The nodes they return keep the reference's
  * struct prefixes and `kind` strings (include/vectra_abi.h), which the
- * optimizer and explain() read through casts.
+ * optimizer and explain() read through casts.  Construction touches no
+ * device (the library initialises on the first next_batch), so the
+ * optimizer can rewrite a plan of libvgpu nodes on any host.
  *
  * Batches crossing the boundary are host memory owned by the receiver and
  * released with free(), as in the reference.  Columns stay resident on the
@@ -66,8 +68,15 @@ JoinNode *join_node_create(VecNode *left, VecNode *right, JoinKind kind,
                                 cudaHostRegister memory; over NVLink-C2C on
                                 Grace systems) -- no staging copy            */
 
-/* A table as a source node, emitting batches of batch_rows rows (a multiple
- * of 32).  data[c]: n_rows int64 / double values or bool bytes;
+/* The largest batch a table source emits: row ids inside a batch are
+ * int32, as the reference's selection vectors are (src/types.h:70-85). */
+#define VGPU_MAX_BATCH_ROWS ((int64_t)2147483647)
+
+/* A table as a source node, emitting batches of batch_rows rows (any count
+ * from 1 to VGPU_MAX_BATCH_ROWS; 0 or less = the whole table, clamped to
+ * VGPU_MAX_BATCH_ROWS; a larger value fails with NULL and vgpu_last_error).
+ * Its kind string is "VgpuTableSource", not "ScanNode": the reference
+ * optimizer reads a .vtr file header through every "ScanNode".  data[c]: n_rows int64 / double values or bool bytes;
  * validity[c]: the reference bitmap (bit i%8 of byte i/8), NULL = all
  * valid.  With VGPU_SRC_DEVICE both are device pointers and libvgpu nodes
  * read the batches in place; any other consumer gets host copies.  With
@@ -266,14 +275,20 @@ int     vgpu_copy_to_host(void *dst_host, const void *src_device, int64_t bytes)
  * else the legacy default stream, and synchronises that stream before it
  * returns.  Returns 0, or -1 with vgpu_last_error set: more than
  * VGPU_STATIC_MAX_ROWS rows, more than 24 columns, a string column or an
- * unsupported predicate.
+ * unsupported predicate.  If the library's own stream belongs to another
+ * device than the current one (vgpu_init chose a device, the caller has
+ * since switched), the call runs on the current device's legacy default
+ * stream instead.
  *
  * Working space is one fixed device array of 1 MiB + 64 KiB compiled into
  * libvgpu; nothing in it needs to be zero beforehand (each call writes
  * what it reads).  Because that array is shared, calls must not overlap:
  * two calls at once, from two threads or on two streams, race on it.  The
  * first call on each device looks up the array's address
- * (cudaGetSymbolAddress) -- make one call before capturing a stream. */
+ * (cudaGetSymbolAddress), and its first launches load the filter kernels'
+ * module (CUDA loads modules lazily by default), which takes a little
+ * device memory once: make one call on each device as a warm-up before a
+ * memory budget is fixed or a stream is captured. */
 #define VGPU_STATIC_MAX_ROWS 8388608LL
 int vgpu_filter_select_static(int n_cols, const char *const *names,
                               const int *types, const void *const *d_data,

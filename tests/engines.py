@@ -19,7 +19,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 PORT_LIB = os.path.join(ORACLE_DIR, "liboracle_port.so")
 REF_LIB = os.path.join(ORACLE_DIR, "_ref", "libvectra_ref.so")
-REF_SRC = "/root/reference/src"
+# the reference checkout's C sources (build recipe input; absent on machines without it)
+REF_SRC = os.environ.get("VECTRA_REF_SRC", "/root/reference/src")
 
 _port = None
 _ref = None
@@ -52,7 +53,7 @@ def ref_available():
     if os.path.exists(REF_LIB):
         return True
     if os.path.isdir(REF_SRC):
-        r = subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref"], capture_output=True)
+        r = subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref", "REF=" + REF_SRC], capture_output=True)
         return r.returncode == 0 and os.path.exists(REF_LIB)
     return False
 

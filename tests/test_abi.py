@@ -62,3 +62,29 @@ def test_ctypes_mirror_matches_header():
     assert C.sizeof(abi.AggSpec) == int(sizes["AggSpec"])
     assert C.sizeof(abi.JoinKey) == int(sizes["JoinKey"])
     assert C.sizeof(abi.ProjEntry) == int(sizes["ProjEntry"])
+
+
+def test_table_source_batch_bounds_and_kind():
+    """batch_rows above the int32 row-id range is rejected; the default
+    (whole table) is clamped to it; the node's kind is not "ScanNode" (the
+    reference optimizer reads a .vtr header through every ScanNode).  Host
+    work only: no device is touched."""
+    import numpy as np
+    import vectra_gb300
+    from vectra_gb300 import abi
+    lib = vectra_gb300.load()
+    f = lib.vgpu_table_source_create
+    f.restype = C.c_void_p
+    f.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int]
+    vals = np.arange(100, dtype=np.int64)
+    names = (C.c_char_p * 1)(b"k")
+    types = (C.c_int * 1)(abi.VEC_INT64)
+    data = (C.c_void_p * 1)(vals.ctypes.data)
+    assert f(1, names, types, data, None, 100, 2 ** 31, 0) is None
+    assert b"batch_rows 2147483648 is above the largest batch" in lib.vgpu_last_error()
+    for br in (0, 7, 2 ** 31 - 1):
+        p = f(1, names, types, data, None, 100, br, 0)
+        assert p
+        node = C.cast(p, C.POINTER(abi.VecNode)).contents
+        assert node.kind == b"VgpuTableSource"
+        node.free_node(C.cast(p, C.POINTER(abi.VecNode)))

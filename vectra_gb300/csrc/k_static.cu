@@ -10,7 +10,7 @@
 #include <cstdio>
 #include "vgpu_internal.h"
 
-#define VG_STATIC_SCRATCH_BYTES ((size_t)1 << 20) + ((size_t)1 << 16)   // 1 MiB + 64 KiB
+constexpr size_t VG_STATIC_SCRATCH_BYTES = ((size_t)1 << 20) + ((size_t)1 << 16);   // 1 MiB + 64 KiB
 
 namespace {
 

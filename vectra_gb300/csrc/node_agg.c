@@ -1335,7 +1335,6 @@ static void agg_free(VecNode *self) {
 
 GroupAggNode *group_agg_node_create(VecNode *child, int n_keys, char **key_names, int n_aggs,
                                     AggSpec *agg_specs, const char *temp_dir) {
-    vg_ensure_init();
     if (n_keys > VG_MAX_KEYS) vg_fail("GPU group-agg supports at most %d key columns", VG_MAX_KEYS);
     if (n_aggs > VG_MAX_OUTS) vg_fail("GPU group-agg supports at most %d aggregates", VG_MAX_OUTS);
     const VecSchema *cs = &child->output_schema;

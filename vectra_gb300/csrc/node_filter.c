@@ -126,7 +126,6 @@ static void filter_free(VecNode *self) {
 }
 
 FilterNode *filter_node_create(VecNode *child, VecExpr *predicate) {
-    vg_ensure_init();
     VgFilter *f = (VgFilter *)vg_xcalloc(1, sizeof(VgFilter));
     f->fn.child = child;
     f->fn.predicate = predicate;

@@ -428,7 +428,6 @@ static const char *type_name(int t) {
 JoinNode *join_node_create(VecNode *left, VecNode *right, JoinKind kind, int n_keys, JoinKey *keys,
                            const char *suffix_x, const char *suffix_y) {
     static const char *kind_names[] = {"inner_join", "left_join", "full_join", "semi_join", "anti_join"};
-    vg_ensure_init();
     const VecSchema *ls = &left->output_schema, *rs = &right->output_schema;
     if (n_keys < 1 || n_keys > VG_MAX_KEYS) vg_fail("GPU join supports 1 to %d key columns", VG_MAX_KEYS);
     for (int k = 0; k < n_keys; k++) {

@@ -167,7 +167,6 @@ static void project_free(VecNode *self) {
 }
 
 ProjectNode *project_node_create(VecNode *child, int n_entries, ProjEntry *entries) {
-    vg_ensure_init();
     VgProject *p = (VgProject *)vg_xcalloc(1, sizeof(VgProject));
     p->pn.child = child;
     p->pn.n_entries = n_entries;

@@ -86,6 +86,7 @@ void vg_check_rc(int rc, const char *what) {
 /* ------------------------------------------------------------------ */
 
 static int g_inited = 0;
+static int g_device = 0;
 static cudaStream_t g_own_stream = NULL;
 static cudaStream_t g_user_stream = NULL;
 static int g_use_user = 0;
@@ -117,6 +118,7 @@ int vgpu_init(int device) {
         uint64_t thr = UINT64_MAX;
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
     }
+    g_device = device;
     g_inited = 1;
     return 0;
 }
@@ -146,10 +148,17 @@ vg_stream_t vg_stream(void) {
 
 /* The stream for work that must not initialise the library (the
  * allocation-free entry point): the caller's stream if one was set, else
- * the library's own once it exists, else the legacy default stream. */
+ * the library's own once it exists and belongs to the current device, else
+ * the legacy default stream (of whichever device is current). */
 vg_stream_t vg_stream_noinit(void) {
     if (g_use_user) return (vg_stream_t)g_user_stream;
-    return g_inited ? (vg_stream_t)g_own_stream : (vg_stream_t)0;
+    if (!g_inited) return (vg_stream_t)0;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev != g_device) {
+        cudaGetLastError();
+        return (vg_stream_t)0;
+    }
+    return (vg_stream_t)g_own_stream;
 }
 
 int vgpu_synchronize(void) {

@@ -158,8 +158,16 @@ static void source_free(VecNode *self) {
 VecNode *vgpu_table_source_create(int n_cols, const char *const *names, const int *types,
                                   const void *const *data, const uint8_t *const *validity,
                                   int64_t n_rows, int64_t batch_rows, int flags) {
-    if (batch_rows <= 0) batch_rows = n_rows > 0 ? n_rows : 1;
+    /* selection vectors and filter row ids are int32 (src/types.h:70-85), so
+     * a batch holds at most INT32_MAX rows; the default (whole table in one
+     * batch) is clamped to that */
+    if (batch_rows <= 0) batch_rows = n_rows > 0 ? (n_rows > VGPU_MAX_BATCH_ROWS ? VGPU_MAX_BATCH_ROWS : n_rows) : 1;
     if (n_cols <= 0 || n_rows < 0) { vg_set_error("table source: bad shape"); return NULL; }
+    if (batch_rows > VGPU_MAX_BATCH_ROWS) {
+        vg_set_error("table source: batch_rows %lld is above the largest batch, %lld rows", (long long)batch_rows,
+                     (long long)VGPU_MAX_BATCH_ROWS);
+        return NULL;
+    }
     for (int c = 0; c < n_cols; c++) {
         if (types[c] != VEC_INT64 && types[c] != VEC_DOUBLE && types[c] != VEC_BOOL) {
             vg_set_error("table source: column '%s' has a type the GPU path does not support", names[c]);
@@ -217,6 +225,10 @@ VecNode *vgpu_table_source_create(int n_cols, const char *const *names, const in
     free(ts);
     s->base.next_batch = source_next;
     s->base.free_node = source_free;
-    s->base.kind = "ScanNode";
+    /* not "ScanNode": the reference optimizer casts nodes of that kind to its
+     * ScanNode struct and reads the .vtr file header through it
+     * (src/optimize.c:38-41, 90-91, 360-363); an unknown kind stops its
+     * propagation there (src/optimize.c:343) */
+    s->base.kind = "VgpuTableSource";
     return &s->base;
 }
