@@ -135,11 +135,11 @@ def source_from_ptrs(lib, cols, n_rows, batch_rows, flags):
     return p
 
 
-def run_query(eng, fact_src, dim_src, temp_dir="tmp"):
+def run_query(eng, fact_src, dim_src, temp_dir="tmp", na_rm=False):
     from vectra_gb300.plan import Tbl, col
     out = (Tbl(eng, fact_src).left_join(Tbl(eng, dim_src), {"key": "id"})
            .group_by("category")
-           .summarise(temp_dir=temp_dir, s=("sum", col("value") * col("weight")), n=("n",))
+           .summarise(temp_dir=temp_dir, s=("sum", col("value") * col("weight"), na_rm), n=("n",))
            .collect())
     return out
 
@@ -259,6 +259,11 @@ def gpu_arm(args, rank, world):
     # must equal an independent (torch, FP64) evaluation to 1e-12
     out = dev_step()
     check_full(torch, out, fact, dim)
+    # the na.rm variant at full size: every group's sum against its exactly
+    # rounded value, beside the reference's naive row-order sum
+    fp64_err = check_full_na_rm(torch, run_query(eng, source_from_ptrs(lib, fcols, N_FACT, N_FACT, 2),
+                                                 source_from_ptrs(lib, dcols, N_DIM, N_DIM, 2), na_rm=True),
+                                fact, dim)
 
     def timed(step, k, w):
         for _ in range(w):
@@ -368,6 +373,7 @@ def gpu_arm(args, rank, world):
                      "path": "node C API, page-locked host columns staged by async copies, 16M-row fact batches"},
         "gpu_launches": launches,
         "clocks": clocks,
+        "fp64_sum_check": fp64_err,
     }
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(torch, repeats=1)
@@ -396,6 +402,62 @@ def check_full(torch, out, fact, dim):
     if sm.any():
         rel = np.abs(sv[sm] - s[sm]) / np.abs(s[sm])
         assert rel.max() <= 1e-12, rel.max()
+
+
+def exact_group_sums(torch, groups, x, n_groups):
+    """Exactly rounded sum of x per group (x finite).  Each summand is
+    m * 2^(e - 1075) with a 53-bit integer m; its two halves (27 and 26 bits)
+    are added as int64 per (group, exponent) -- exact, since a cell holds
+    fewer than 2^36 summands -- and the cells are combined with Python
+    integers and rounded once (Fraction -> float rounds to nearest even)."""
+    from fractions import Fraction
+    bits = x.view(torch.int64)
+    e = (bits >> 52) & 0x7FF
+    m = (bits & ((1 << 52) - 1)) | ((e > 0).to(torch.int64) << 52)
+    neg = bits < 0
+    hi = torch.where(neg, -(m >> 26), m >> 26)
+    lo = torch.where(neg, -(m & ((1 << 26) - 1)), m & ((1 << 26) - 1))
+    cell = groups * 2048 + e
+    sh = torch.zeros(n_groups * 2048, dtype=torch.int64, device=x.device).index_add_(0, cell, hi)
+    sl = torch.zeros(n_groups * 2048, dtype=torch.int64, device=x.device).index_add_(0, cell, lo)
+    sh, sl = sh.view(n_groups, 2048).cpu().numpy(), sl.view(n_groups, 2048).cpu().numpy()
+    out = []
+    for g in range(n_groups):
+        tot = 0
+        for ex in np.nonzero(sh[g] | sl[g])[0]:
+            tot += ((int(sh[g, ex]) << 26) + int(sl[g, ex])) << (max(int(ex), 1) - 1)
+        out.append(float(Fraction(tot, 1 << 1074)))
+    return np.array(out)
+
+
+def check_full_na_rm(torch, out, fact, dim):
+    """sum(value * weight, na.rm = TRUE) at full size: n() exactly, every
+    sum non-NA, and the largest relative error of the GPU's sums and of the
+    reference's naive row-order sums against the exactly rounded sums."""
+    keys, _ = fact["key"]
+    vals, valid = fact["value"]
+    ids = dim["id"][0]
+    pos = torch.empty(N_DIM + 1, dtype=torch.int64, device=ids.device)
+    pos[ids] = torch.arange(N_DIM, device=ids.device)
+    p = pos[keys]
+    cat = dim["category"][0][p]
+    prod = vals * dim["weight"][0][p]            # one rounding per product, as the projection
+    n = torch.bincount(cat, minlength=N_CAT).cpu().numpy()
+    exact = exact_group_sums(torch, cat[valid], prod[valid], N_CAT)
+    # the reference adds each group's products in row order (np.add.at is
+    # unbuffered and runs in index order)
+    naive = np.zeros(N_CAT)
+    np.add.at(naive, cat[valid].cpu().numpy(), prod[valid].cpu().numpy())
+    assert list(out["category"][0]) == list(range(N_CAT)), "groups not in key order"
+    assert np.array_equal(out["n"][0], n.astype(np.float64)), "n() mismatch"
+    sv, sm = out["s"]
+    assert sm.all(), "na.rm sums must all be present"
+    gpu_err = float(np.max(np.abs(sv - exact) / np.abs(exact)))
+    ref_err = float(np.max(np.abs(naive - exact) / np.abs(exact)))
+    assert gpu_err <= 1e-12, gpu_err
+    return {"query": "sum(value * weight, na.rm = TRUE), full size", "groups": N_CAT,
+            "max_rel_err_gpu_vs_exact": gpu_err, "max_rel_err_reference_naive_vs_exact": ref_err,
+            "gpu_bit_exact_groups": int(np.sum(sv == exact))}
 
 
 def same_result(a, b):
