@@ -27,6 +27,7 @@
 #include "vg_rtc_types.h"   /* run-time compiled device code: no libc headers */
 #else
 #include <stdint.h>
+#include <stdio.h>
 #include <stddef.h>
 #endif
 
@@ -234,6 +235,55 @@ typedef struct {
     ProjEntry  *entries;
 } ProjectNode;
 #endif
+
+#ifndef __CUDACC_RTC__   /* host-only: the file handle holds a FILE * */
+#ifndef VECTRA_VTR1_H
+#define VECTRA_VTR1_H
+/* .vtr file handle (src/vtr1.h): read by the optimizer's pruning and
+ * pushdown through ScanNode->file (src/optimize.c:38-41, 360-363). */
+typedef struct {
+    uint16_t  version;
+    VecSchema schema;
+    uint32_t  n_rowgroups;
+} Vtr1Header;
+
+/* per-column per-row-group min / max (version 3) */
+typedef struct {
+    uint8_t has_stats;
+    union {
+        struct { int64_t min, max; } i64;
+        struct { double min, max; } dbl;
+        struct { uint8_t min, max; } bln;
+    };
+} Vtr1ColStat;
+
+typedef struct {
+    int64_t      file_offset;
+    int64_t      n_rows;
+    Vtr1ColStat *col_stats;     /* n_cols entries; NULL before version 3 */
+} Vtr1RowGroup;
+
+typedef struct {
+    FILE         *fp;
+    Vtr1Header    header;
+    Vtr1RowGroup *rowgroups;
+} Vtr1File;
+#endif
+
+#ifndef VECTRA_SCAN_H
+#define VECTRA_SCAN_H
+/* Read by the optimizer (src/optimize.c:38-77 prunes col_mask and the
+ * output schema; 356-371 attaches a FilterNode's predicate, borrowed). */
+typedef struct {
+    VecNode    base;
+    Vtr1File  *file;
+    int       *col_mask;        /* file columns read */
+    uint32_t   next_rg;
+    VecExpr   *predicate;       /* pushed-down predicate, NULL = none */
+    int        pred_borrowed;   /* 1: owned by the filter node */
+} ScanNode;
+#endif
+#endif /* __CUDACC_RTC__ */
 
 #ifdef __cplusplus
 }

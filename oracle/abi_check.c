@@ -18,6 +18,8 @@
 #include "join.h"
 #include "filter.h"
 #include "project.h"
+#include "vtr1.h"
+#include "scan.h"
 typedef JoinNode JoinPrefixT;
 #else
 #include "vectra_abi.h"
@@ -55,6 +57,13 @@ int main(void) {
     S(ProjEntry); O(ProjEntry, output_name); O(ProjEntry, expr);
     S(ProjectNode); O(ProjectNode, child); O(ProjectNode, n_entries);
     O(ProjectNode, entries);
+    S(Vtr1Header); O(Vtr1Header, version); O(Vtr1Header, schema); O(Vtr1Header, n_rowgroups);
+    S(Vtr1ColStat); O(Vtr1ColStat, has_stats); O(Vtr1ColStat, i64.min); O(Vtr1ColStat, i64.max);
+    O(Vtr1ColStat, dbl.min); O(Vtr1ColStat, dbl.max); O(Vtr1ColStat, bln.min); O(Vtr1ColStat, bln.max);
+    S(Vtr1RowGroup); O(Vtr1RowGroup, file_offset); O(Vtr1RowGroup, n_rows); O(Vtr1RowGroup, col_stats);
+    S(Vtr1File); O(Vtr1File, fp); O(Vtr1File, header); O(Vtr1File, rowgroups);
+    S(ScanNode); O(ScanNode, file); O(ScanNode, col_mask); O(ScanNode, next_rg);
+    O(ScanNode, predicate); O(ScanNode, pred_borrowed);
     printf("enum VEC_STRING %d EXPR_GREPL %d AGG_MAX %d JOIN_ANTI %d\n",
            (int)VEC_STRING, (int)EXPR_GREPL, (int)AGG_MAX, (int)JOIN_ANTI);
     return 0;
