@@ -58,6 +58,16 @@ JoinNode *join_node_create(VecNode *left, VecNode *right, JoinKind kind,
                            int n_keys, JoinKey *keys,
                            const char *suffix_x, const char *suffix_y);
 
+/* replaces src/scan.h:22 (ScanNode *scan_node_create): a .vtr scan with
+ * the reference's ScanNode prefix and kind, so the optimizer prunes its
+ * columns and pushes a filter's predicate into it as before; row groups the
+ * predicate's min / max statistics rule out are skipped (src/scan.c:12-105).
+ * libvgpu nodes above it read each row group straight into page-locked
+ * staging and copy it to the device asynchronously; other consumers get
+ * malloc-owned batches as from src/vtr1.c:306-392.  col_indices: NULL = all
+ * columns. */
+ScanNode *scan_node_create(const char *path, int *col_indices, int n_selected);
+
 /* ---- data sources (no reference counterpart beyond ScanNode's role) -- */
 
 #define VGPU_SRC_COPY    0   /* copy the host columns at creation          */
@@ -142,6 +152,7 @@ ProjectNode  *vgpu_guard_project(VecNode *child, int n, ProjEntry *entries);
 GroupAggNode *vgpu_guard_group_agg(VecNode *child, int n_keys, char **key_names,
                                    int n_aggs, AggSpec *specs,
                                    const char *temp_dir);
+ScanNode     *vgpu_guard_scan(const char *path, int *col_indices, int n_selected);
 JoinNode     *vgpu_guard_join(VecNode *left, VecNode *right, JoinKind kind,
                               int n_keys, JoinKey *keys, const char *suffix_x,
                               const char *suffix_y);

@@ -23,6 +23,7 @@
 #include "group_agg.h"
 #include "join.h"
 #include "project.h"
+#include "scan.h"
 
 static jmp_buf *g_jmp = NULL;
 static char g_msg[1024];
@@ -84,6 +85,13 @@ JoinNode *vref_guard_join(VecNode *l, VecNode *r, JoinKind kind, int n_keys,
     JoinNode *j = join_node_create(l, r, kind, n_keys, keys, sx, sy);
     GUARD_END
     return j;
+}
+
+ScanNode *vref_guard_scan(const char *path, int *col_indices, int n_selected) {
+    GUARD_BEGIN
+    ScanNode *r = scan_node_create(path, col_indices, n_selected);
+    GUARD_END
+    return r;
 }
 
 ProjectNode *vref_guard_project(VecNode *child, int n, ProjEntry *entries) {

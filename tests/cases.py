@@ -384,3 +384,29 @@ def same_batches(a, b, rtol=0.0, tol_cols=()):
             else:
                 eq = (va == vb) | (np.isnan(va) & np.isnan(vb) if va.dtype == np.float64 else False)
                 assert np.all(eq), (bi, name, va[~eq], vb[~eq])
+
+
+def vtr_weather_table():
+    """The table of tests/golden/ref_weather.vtr (written there by the
+    reference's own writer, 7 row groups of 600 rows, the last 234):
+    station int64 U{0..99}; temperature double N(20, 10) with 2% NA and
+    every even row group below 25; year int64 U{2000..2025}; flag bool with
+    5% NA; city string with 3% NA."""
+    rng = np.random.default_rng(77)
+    n = 6 * 600 + 234
+    station = rng.integers(0, 100, n).astype(np.int64)
+    temp = rng.normal(20.0, 10.0, n)
+    g = np.arange(n) // 600
+    temp = np.where(g % 2 == 0, np.minimum(temp, 24.0), temp)
+    tv = rng.random(n) >= 0.02
+    temp[~tv] = 0.0
+    year = rng.integers(2000, 2026, n).astype(np.int64)
+    flag = rng.random(n) < 0.4
+    fv = rng.random(n) >= 0.05
+    flag[~fv] = False
+    cities = np.array(["oslo", "lima", "quito", "", "kyiv", "perth"], dtype=object)
+    city = list(cities[rng.integers(0, len(cities), n)])
+    cv = rng.random(n) >= 0.03
+    city = [c if ok else "" for c, ok in zip(city, cv)]
+    return {"station": station, "temperature": (temp, tv), "year": year, "flag": (flag, fv),
+            "city": (city, cv)}

@@ -118,6 +118,7 @@ class RefEngine(Engine):
         super().__init__(lib, "vref_guard_filter", "vref_guard_project", "vref_guard_group_agg",
                          "vref_guard_join", "vref_guard_next_batch", "vec_batch_free", "vref_last_error")
         self.tmp = tempfile.mkdtemp(prefix="vgpu_ref_")
+        self.scan_fn = "vref_guard_scan"
 
     def make_source(self, table, batch_rows=None, sel_mode=0, **_):
         return make_oracle_source(table, batch_rows, sel_mode)

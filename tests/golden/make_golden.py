@@ -2,6 +2,8 @@
 (oracle/_ref/libvectra_ref.so, compiled from the reference's C sources) for
 every parity case in tests/cases.py.  tests/test_golden.py checks the CPU
 oracle against these fixtures wherever the reference checkout is absent.
+Also tests/golden/ref_weather.vtr: cases.vtr_weather_table() written by the
+reference's own .vtr writer (read by the scan tests).
 
     python tests/golden/make_golden.py
 """
@@ -33,7 +35,59 @@ def all_cases():
                 lambda E, n=n, b=batch, m=mode: cases.r_group(E, n + 1, n, b, 1, None if m == "hash" else E.tmp))
 
 
+def write_vtr_ref(path, table, batch_rows):
+    """Writes `table` with the reference's own .vtr writer
+    (vtr1_write_header / vtr1_write_rowgroup, src/vtr1.c:39-153)."""
+    import ctypes as C
+    from engines import ref_lib
+    from vectra_gb300 import abi, vtr
+    R = ref_lib()
+    libc = C.CDLL(None)
+    libc.fopen.restype, libc.fopen.argtypes = C.c_void_p, [C.c_char_p, C.c_char_p]
+    libc.fclose.argtypes = [C.c_void_p]
+    R.vtr1_write_header.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
+    R.vtr1_write_rowgroup.argtypes = [C.c_void_p, C.c_void_p]
+    names = list(table)
+    cols = [vtr._col(table[n]) for n in names]
+    n = len(cols[0][1])
+    keep = []
+    cnames = (C.c_char_p * len(names))(*[x.encode() for x in names])
+    ctypes_ = (C.c_int * len(names))(*[t for _, _, t in cols])
+    schema = abi.VecSchema(len(names), cnames, ctypes_, None)
+    groups = [(lo, min(n, lo + batch_rows)) for lo in range(0, n, batch_rows)] if n else []
+    fp = libc.fopen(path.encode(), b"wb")
+    R.vtr1_write_header(fp, C.byref(schema), len(groups))
+    for lo, hi in groups:
+        arrs = (abi.VecArray * len(names))()
+        for c, (vals, mask, t) in enumerate(cols):
+            a = arrs[c]
+            a.type, a.length, a.owns_data = t, hi - lo, 1
+            bits = np.packbits(mask[lo:hi], bitorder="little")
+            bits = np.concatenate([bits, np.zeros(1, np.uint8)])
+            keep.append(bits)
+            a.validity = bits.ctypes.data_as(C.POINTER(C.c_uint8))
+            if t == abi.VEC_STRING:
+                enc = [str(s).encode() for s in vals[lo:hi]]
+                offs = np.zeros(len(enc) + 1, np.int64)
+                offs[1:] = np.cumsum([len(e) for e in enc])
+                data = C.create_string_buffer(b"".join(enc) or b"\0")
+                keep += [offs, data]
+                a.buf.str.offsets = offs.ctypes.data_as(C.POINTER(C.c_int64))
+                a.buf.str.data = C.cast(data, C.c_char_p)
+                a.buf.str.data_len = int(offs[-1])
+            else:
+                v = np.ascontiguousarray(vals[lo:hi], dtype=np.uint8 if t == abi.VEC_BOOL else None)
+                keep.append(v)
+                a.buf.i64 = v.ctypes.data_as(C.POINTER(C.c_int64))
+        b = abi.VecBatch(hi - lo, len(names), cnames, arrs, None, 0)
+        keep.append(arrs)
+        R.vtr1_write_rowgroup(fp, C.byref(b))
+    libc.fclose(fp)
+    return len(groups)
+
+
 def main():
+    write_vtr_ref(os.path.join(HERE, "ref_weather.vtr"), cases.vtr_weather_table(), 600)
     R = RefEngine()
     arrays, manifest = {}, {}
     for name, fn in all_cases():

@@ -16,7 +16,10 @@ vec_optimize (src/optimize.c), over the plans:
   statistics rule the predicate out (src/scan.c:12-105);
 - a join of two scans (src/optimize.c:313-333): both sides stay whole;
 - a filter over libvgpu's table source: its kind is not "ScanNode", so the
-  optimizer neither casts it to a ScanNode nor pushes anything into it.
+  optimizer neither casts it to a ScanNode nor pushes anything into it;
+- the first plan again over libvgpu's own scan node (its scan_node_create,
+  the drop-in for src/scan.c): the optimizer prunes and pushes into it
+  through the same struct fields, and it skips the same row groups.
 
 Nothing here touches a device: node construction is host work only, and the
 plans are freed without being run.  The reference objects come from
@@ -38,6 +41,7 @@ HOST = r"""
 #include <stdlib.h>
 #include <string.h>
 #include <stdarg.h>
+#include <dlfcn.h>
 
 #include "types.h"
 #include "array.h"
@@ -116,8 +120,37 @@ static void write_weather(const char *path, int n_rg, int64_t n) {
     fclose(fp);
 }
 
+/* filter -> group_agg over a scan made by `mk`: pushdown, pruning and the
+ * row groups the scan then returns */
+static void filter_agg_plan(ScanNode *(*mk)(const char *, int *, int), const char *path, const char *tmp) {
+    ScanNode *sn = mk(path, NULL, 0);
+    CHECK(strcmp(sn->base.kind, "ScanNode") == 0 && sn->base.output_schema.n_cols == 4);
+    CHECK(sn->file->header.version == 3 && sn->file->header.n_rowgroups == 6);
+    VecExpr *pred = and_(cmp(colref("temperature"), '>', ' ', lit_d(30.0)),
+                         cmp(colref("year"), '>', '=', lit_d(2020.0)));
+    FilterNode *fn = filter_node_create(&sn->base, pred);
+    char **keys = malloc(sizeof(char *));
+    keys[0] = dup("station");
+    AggSpec *specs = calloc(2, sizeof(AggSpec));
+    specs[0].kind = AGG_MEAN; specs[0].input_col = dup("temperature"); specs[0].output_name = dup("avg");
+    specs[1].kind = AGG_COUNT_STAR; specs[1].input_col = NULL; specs[1].output_name = dup("n");
+    GroupAggNode *ga = group_agg_node_create(&fn->base, 1, keys, 2, specs, tmp);
+    vec_optimize(&ga->base);
+    CHECK(sn->predicate == pred && sn->pred_borrowed == 1 && fn->predicate == pred);
+    CHECK(sn->col_mask[0] == 1 && sn->col_mask[1] == 1 && sn->col_mask[2] == 1 && sn->col_mask[3] == 0);
+    CHECK(sn->base.output_schema.n_cols == 3 && fn->base.output_schema.n_cols == 3);
+    int n_batches = 0;
+    for (VecBatch *b; (b = sn->base.next_batch(&sn->base)) != NULL; n_batches++) {
+        CHECK(b->n_cols == 3 && b->n_rows == 1000);
+        CHECK(strcmp(b->col_names[2], "year") == 0);
+        vec_batch_free(b);
+    }
+    CHECK(n_batches == 3);
+    ga->base.free_node(&ga->base);
+}
+
 int main(int argc, char **argv) {
-    if (argc < 2) return 2;
+    if (argc < 3) return 2;
     char path[4096], path2[4096];
     snprintf(path, sizeof(path), "%s/weather.vtr", argv[1]);
     snprintf(path2, sizeof(path2), "%s/dim.vtr", argv[1]);
@@ -192,6 +225,18 @@ int main(int argc, char **argv) {
     CHECK(f2->predicate == p2 && f2->base.output_schema.n_cols == 2);
     f2->base.free_node(&f2->base);
 
+    /* the same plan over libvgpu's own scan node (scan_node_create from
+     * libvgpu.so, looked up by name: the reference's scan.o, linked into this
+     * program, defines the same symbol) */
+    void *h = dlopen(argv[2], RTLD_NOW | RTLD_LOCAL);
+    CHECK(h != NULL);
+    if (h) {
+        ScanNode *(*vg_scan)(const char *, int *, int) = (ScanNode * (*)(const char *, int *, int))dlsym(h, "scan_node_create");
+        CHECK(vg_scan != NULL && vg_scan != scan_node_create);
+        if (vg_scan && vg_scan != scan_node_create) filter_agg_plan(vg_scan, path, argv[1]);
+    }
+    filter_agg_plan(scan_node_create, path, argv[1]);
+
     remove(path);
     remove(path2);
     if (fails) return 1;
@@ -218,13 +263,14 @@ def test_libvgpu_nodes_under_the_reference_optimizer(tmp_path):
     libdir = os.path.join(ROOT, "vectra_gb300")
     r = subprocess.run([gcc, "-std=gnu11", "-O1", "-o", str(exe), str(src), *objs,
                         "-I", REF_SRC, "-I", os.path.join(ORACLE_DIR, "rshim"),
-                        os.path.join(libdir, "libvgpu.so"), "-Wl,-rpath," + libdir, "-lm"],
+                        os.path.join(libdir, "libvgpu.so"), "-Wl,-rpath," + libdir, "-lm", "-ldl"],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     nm = subprocess.run(["nm", str(exe)], capture_output=True, text=True, check=True).stdout
     # the node constructors come from libvgpu, not from the reference's objects
     for sym in ("filter_node_create", "group_agg_node_create", "join_node_create"):
         assert any(l.split()[-1] == sym and " U " in l for l in nm.splitlines()), sym
-    out = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=120)
+    out = subprocess.run([str(exe), str(tmp_path), os.path.join(libdir, "libvgpu.so")], capture_output=True,
+                         text=True, timeout=120)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "plans ok" in out.stdout

@@ -381,6 +381,7 @@ static size_t valid_bytes_dev(int64_t n) { return (size_t)((n + 31) / 32) * 4; }
 int vg_pull(VecNode *child, const uint8_t *need, int keep_host, VgDBatch *out) {
     memset(out, 0, sizeof(*out));
     if (vg_is_table_source(child) && !keep_host) return vg_source_pull(child, need, out);
+    if (vg_is_vtr_scan(child) && !keep_host) return vg_scan_pull(child, need, out);
     VecBatch *b = child->next_batch(child);
     if (!b) return 0;
     int64_t n = b->n_rows;
@@ -651,6 +652,12 @@ GroupAggNode *vgpu_guard_group_agg(VecNode *child, int n_keys, char **key_names,
                                    AggSpec *specs, const char *temp_dir) {
     GUARD_BEGIN(GroupAggNode *)
     GroupAggNode *r = group_agg_node_create(child, n_keys, key_names, n_aggs, specs, temp_dir);
+    GUARD_END
+    return r;
+}
+ScanNode *vgpu_guard_scan(const char *path, int *col_indices, int n_selected) {
+    GUARD_BEGIN(ScanNode *)
+    ScanNode *r = scan_node_create(path, col_indices, n_selected);
     GUARD_END
     return r;
 }

@@ -1,0 +1,461 @@
+/*
+ * scan_vtr.c -- the .vtr scan node (replaces src/scan.c; reads the format of
+ * src/vtr1.c:39-392 with code of its own).
+ *
+ * scan_node_create returns a node whose struct prefix is the reference's
+ * ScanNode {base, file, col_mask, next_rg, predicate, pred_borrowed} and
+ * whose file handle starts with Vtr1File {fp, header, rowgroups}, with the
+ * kind "ScanNode": the optimizer prunes col_mask and the output schema and
+ * attaches a FilterNode's predicate through those fields
+ * (src/optimize.c:38-77, 356-371), exactly as on the reference's node.
+ *
+ * Two ways out of the node:
+ *  - next_batch (any consumer): the next row group that the pushed-down
+ *    predicate does not rule out, as a malloc-owned batch of the selected
+ *    columns, as vtr1_read_rowgroup returns it (src/vtr1.c:306-392);
+ *  - vg_scan_pull (libvgpu nodes): the same row group's needed columns read
+ *    with pread straight into a page-locked staging block laid out like the
+ *    device block, then one asynchronous copy to the device.  Two staging
+ *    blocks alternate: the file read of the next row group overlaps the copy
+ *    and the kernels of this one, and a block is reused only after the
+ *    event recorded behind its copy has completed.
+ *
+ * Row-group pruning restates predicate_might_match (src/scan.c:12-105):
+ * AND / OR of `column <op> numeric literal` terms against the row group's
+ * v3 min / max statistics (valid values only), anything else may match.
+ */
+#define _GNU_SOURCE
+#include <fcntl.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+#include <cuda_runtime_api.h>
+
+#include "vg_host.h"
+
+typedef struct {
+    Vtr1File f;                 /* reference prefix */
+    int fd;                     /* pread handle (same file) */
+    int n_cols;
+    int64_t *valid_off;         /* [rg * n_cols + c]: file offset of the validity bitmap */
+    int64_t *str_len;           /* [rg * n_cols + c]: string data bytes (string columns) */
+} VgVtrFile;
+
+typedef struct {
+    ScanNode sn;                /* reference prefix */
+    int64_t rows_out;           /* rows emitted so far (stream position) */
+    void *stage[2];             /* page-locked staging blocks */
+    size_t stage_bytes[2];
+    cudaEvent_t ev[2];          /* recorded behind each block's copy */
+    int ev_live[2];
+    int cur;
+} VgScan;
+
+static VecBatch *scan_next(VecNode *self);
+static void scan_free(VecNode *self);
+
+int vg_is_vtr_scan(const VecNode *n) { return n && n->next_batch == scan_next; }
+
+/* ---- file ---------------------------------------------------------- */
+
+static void rd(FILE *fp, void *p, size_t n, const char *what) {
+    if (n && fread(p, 1, n, fp) != n) vg_fail("unexpected end of file reading %s", what);
+}
+
+static void pread_all(int fd, void *dst, size_t n, int64_t off) {
+    char *p = (char *)dst;
+    while (n > 0) {
+        ssize_t r = pread(fd, p, n, (off_t)off);
+        if (r <= 0) vg_fail("unexpected end of file reading column data");
+        p += r;
+        n -= (size_t)r;
+        off += r;
+    }
+}
+
+static int64_t data_bytes(int type, int64_t n) {
+    return type == VEC_BOOL ? n : 8 * n;
+}
+
+static void vtr_close(VgVtrFile *v) {
+    if (!v) return;
+    if (v->f.fp) fclose(v->f.fp);
+    if (v->fd >= 0) close(v->fd);
+    vg_schema_free(&v->f.header.schema);
+    if (v->f.rowgroups) {
+        for (uint32_t g = 0; g < v->f.header.n_rowgroups; g++) free(v->f.rowgroups[g].col_stats);
+        free(v->f.rowgroups);
+    }
+    free(v->valid_off);
+    free(v->str_len);
+    free(v);
+}
+
+/* Header (magic "VTR1", version 1-3, columns with their names, types and,
+ * from version 2, annotations), then the row-group index: each group's
+ * offset, row count, v3 statistics and the offsets of its columns. */
+static VgVtrFile *vtr_open(const char *path) {
+    FILE *fp = fopen(path, "rb");
+    if (!fp) vg_fail("cannot open file: %s", path);
+    char magic[4];
+    if (fread(magic, 1, 4, fp) != 4 || memcmp(magic, "VTR1", 4) != 0) {
+        fclose(fp);
+        vg_fail("not a valid .vtr file (bad magic): %s", path);
+    }
+    VgVtrFile *v = (VgVtrFile *)vg_xcalloc(1, sizeof(VgVtrFile));
+    v->f.fp = fp;
+    v->fd = -1;
+    uint16_t ver = 0, nc = 0;
+    rd(fp, &ver, 2, "the version");
+    if (ver < 1 || ver > 3) {
+        vtr_close(v);
+        vg_fail("unsupported .vtr version: %u", (unsigned)ver);
+    }
+    v->f.header.version = ver;
+    rd(fp, &nc, 2, "the column count");
+    char **names = (char **)vg_xcalloc(nc ? nc : 1, sizeof(char *));
+    char **ann = (char **)vg_xcalloc(nc ? nc : 1, sizeof(char *));
+    VecType *types = (VecType *)vg_xcalloc(nc ? nc : 1, sizeof(VecType));
+    for (int c = 0; c < nc; c++) {
+        uint16_t len = 0;
+        rd(fp, &len, 2, "a column name");
+        names[c] = (char *)vg_xmalloc((size_t)len + 1);
+        rd(fp, names[c], len, "a column name");
+        names[c][len] = 0;
+        uint8_t t = 0;
+        rd(fp, &t, 1, "a column type");
+        types[c] = (VecType)t;
+        if (ver >= 2) {
+            uint16_t al = 0;
+            rd(fp, &al, 2, "an annotation");
+            if (al) {
+                ann[c] = (char *)vg_xmalloc((size_t)al + 1);
+                rd(fp, ann[c], al, "an annotation");
+                ann[c][al] = 0;
+            }
+        }
+    }
+    v->f.header.schema = vg_schema_make(nc, names, types);
+    for (int c = 0; c < nc; c++) {
+        v->f.header.schema.col_annotations[c] = ann[c];
+        free(names[c]);
+    }
+    free(names);
+    free(ann);
+    free(types);
+    v->n_cols = nc;
+    uint32_t nrg = 0;
+    rd(fp, &nrg, 4, "the row-group count");
+    v->f.header.n_rowgroups = nrg;
+    v->f.rowgroups = (Vtr1RowGroup *)vg_xcalloc(nrg ? nrg : 1, sizeof(Vtr1RowGroup));
+    v->valid_off = (int64_t *)vg_xcalloc((size_t)(nrg ? nrg : 1) * (nc ? nc : 1), sizeof(int64_t));
+    v->str_len = (int64_t *)vg_xcalloc((size_t)(nrg ? nrg : 1) * (nc ? nc : 1), sizeof(int64_t));
+    int64_t pos = ftell(fp);
+    for (uint32_t g = 0; g < nrg; g++) {
+        Vtr1RowGroup *rg = &v->f.rowgroups[g];
+        rg->file_offset = pos;
+        if (fseek(fp, (long)pos, SEEK_SET) != 0) vg_fail("unexpected end of file");
+        uint64_t n = 0;
+        rd(fp, &n, 8, "a row count");
+        rg->n_rows = (int64_t)n;
+        pos += 8;
+        if (ver >= 3) {
+            rg->col_stats = (Vtr1ColStat *)vg_xcalloc(nc ? nc : 1, sizeof(Vtr1ColStat));
+            for (int c = 0; c < nc; c++) {
+                uint8_t has = 0;
+                uint64_t a = 0, b = 0;
+                rd(fp, &has, 1, "statistics");
+                rd(fp, &a, 8, "statistics");
+                rd(fp, &b, 8, "statistics");
+                Vtr1ColStat *st = &rg->col_stats[c];
+                st->has_stats = has;
+                if (!has) continue;
+                if (v->f.header.schema.col_types[c] == VEC_BOOL) {
+                    st->bln.min = (uint8_t)a;
+                    st->bln.max = (uint8_t)b;
+                } else {
+                    memcpy(&st->i64.min, &a, 8);   /* int64 and double share the bytes */
+                    memcpy(&st->i64.max, &b, 8);
+                }
+            }
+            pos += 17 * (int64_t)nc;
+        }
+        for (int c = 0; c < nc; c++) {
+            const int t = v->f.header.schema.col_types[c];
+            v->valid_off[(size_t)g * nc + c] = pos;
+            pos += vg_vbytes((int64_t)n);
+            if (t == VEC_STRING) {
+                pos += 8 * ((int64_t)n + 1);
+                uint64_t dl = 0;
+                if (fseek(fp, (long)pos, SEEK_SET) != 0) vg_fail("unexpected end of file");
+                rd(fp, &dl, 8, "string data length");
+                v->str_len[(size_t)g * nc + c] = (int64_t)dl;
+                pos += 8 + (int64_t)dl;
+            } else {
+                pos += data_bytes(t, (int64_t)n);
+            }
+        }
+    }
+    v->fd = open(path, O_RDONLY | O_CLOEXEC);
+    if (v->fd < 0) {
+        vtr_close(v);
+        vg_fail("cannot open file: %s", path);
+    }
+    return v;
+}
+
+/* ---- pruning (src/scan.c:12-105) ------------------------------------ */
+
+static int might_match(const VecExpr *p, const Vtr1ColStat *stats, const VecSchema *s) {
+    if (!p || !stats) return 1;
+    if (p->kind == EXPR_BOOL && p->op == '&') return might_match(p->left, stats, s) && might_match(p->right, stats, s);
+    if (p->kind == EXPR_BOOL && p->op == '|') return might_match(p->left, stats, s) || might_match(p->right, stats, s);
+    if (p->kind != EXPR_CMP) return 1;
+    const VecExpr *c = NULL, *l = NULL;
+    int col_left = 0;
+    const int lit_r = p->right->kind == EXPR_LIT_INT64 || p->right->kind == EXPR_LIT_DOUBLE;
+    const int lit_l = p->left->kind == EXPR_LIT_INT64 || p->left->kind == EXPR_LIT_DOUBLE;
+    if (p->left->kind == EXPR_COL_REF && lit_r) {
+        c = p->left;
+        l = p->right;
+        col_left = 1;
+    } else if (p->right->kind == EXPR_COL_REF && lit_l) {
+        c = p->right;
+        l = p->left;
+    } else {
+        return 1;
+    }
+    const int ci = vg_schema_find(s, c->col_name);
+    if (ci < 0 || !stats[ci].has_stats) return 1;
+    const double lit = l->kind == EXPR_LIT_DOUBLE ? l->lit_dbl : (double)l->lit_i64;
+    double lo, hi;
+    if (s->col_types[ci] == VEC_INT64) {
+        lo = (double)stats[ci].i64.min;
+        hi = (double)stats[ci].i64.max;
+    } else if (s->col_types[ci] == VEC_DOUBLE) {
+        lo = stats[ci].dbl.min;
+        hi = stats[ci].dbl.max;
+    } else {
+        return 1;
+    }
+    char op = p->op;
+    const char op2 = p->op2;
+    /* `literal op column`: < and > swap sides (the second character stays) */
+    if (!col_left) op = op == '<' ? '>' : op == '>' ? '<' : op;
+    if (op == '>' && op2 == ' ') return hi > lit;
+    if (op == '>' && op2 == '=') return hi >= lit;
+    if (op == '<' && op2 == ' ') return lo < lit;
+    if (op == '<' && op2 == '=') return lo <= lit;
+    if (op == '=' && op2 == '=') return lo <= lit && hi >= lit;
+    if (op == '!' && op2 == '=') return !(lo == lit && hi == lit);
+    return 1;
+}
+
+/* the next row group the pushed-down predicate does not rule out, or -1 */
+static int64_t next_group(VgScan *s) {
+    VgVtrFile *v = (VgVtrFile *)s->sn.file;
+    while (s->sn.next_rg < v->f.header.n_rowgroups) {
+        const uint32_t g = s->sn.next_rg++;
+        if (s->sn.predicate && v->f.header.version >= 3 &&
+            !might_match(s->sn.predicate, v->f.rowgroups[g].col_stats, &v->f.header.schema))
+            continue;
+        return g;
+    }
+    return -1;
+}
+
+/* ---- host batches (src/vtr1.c:306-392) ------------------------------- */
+
+static VecBatch *scan_next(VecNode *self) {
+    VgScan *s = (VgScan *)self;
+    VgVtrFile *v = (VgVtrFile *)s->sn.file;
+    const int64_t g = next_group(s);
+    if (g < 0) return NULL;
+    const int64_t n = v->f.rowgroups[g].n_rows;
+    int n_sel = 0;
+    for (int c = 0; c < v->n_cols; c++) n_sel += s->sn.col_mask[c] != 0;
+    VecBatch *b = vg_batch_alloc(n_sel, n);
+    int o = 0;
+    for (int c = 0; c < v->n_cols; c++) {
+        if (!s->sn.col_mask[c]) continue;
+        const int t = v->f.header.schema.col_types[c];
+        VecArray a;
+        memset(&a, 0, sizeof(a));
+        a.type = (VecType)t;
+        a.length = n;
+        a.owns_data = 1;
+        a.validity = (uint8_t *)vg_xcalloc((size_t)(vg_vbytes(n) ? vg_vbytes(n) : 1), 1);
+        int64_t off = v->valid_off[(size_t)g * v->n_cols + c];
+        pread_all(v->fd, a.validity, (size_t)vg_vbytes(n), off);
+        off += vg_vbytes(n);
+        if (t == VEC_STRING) {
+            a.buf.str.offsets = (int64_t *)vg_xcalloc((size_t)n + 1, 8);
+            pread_all(v->fd, a.buf.str.offsets, 8 * ((size_t)n + 1), off);
+            const int64_t dl = v->str_len[(size_t)g * v->n_cols + c];
+            a.buf.str.data_len = dl;
+            a.buf.str.data = dl ? (char *)vg_xmalloc((size_t)dl) : NULL;
+            pread_all(v->fd, a.buf.str.data, (size_t)dl, off + 8 * (n + 1) + 8);
+        } else {
+            void *d = vg_xcalloc((size_t)(n ? data_bytes(t, n) : 1), 1);
+            pread_all(v->fd, d, (size_t)data_bytes(t, n), off);
+            if (t == VEC_BOOL) a.buf.bln = (uint8_t *)d;
+            else a.buf.i64 = (int64_t *)d;
+        }
+        b->columns[o] = a;
+        b->col_names[o] = vg_xstrdup(v->f.header.schema.col_names[c]);
+        o++;
+    }
+    s->rows_out += n;
+    return b;
+}
+
+/* ---- device batches -------------------------------------------------- */
+
+static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static void *stage_block(VgScan *s, size_t bytes) {
+    const int i = s->cur;
+    if (s->ev_live[i]) {
+        cudaError_t e = cudaEventSynchronize(s->ev[i]);
+        if (e != cudaSuccess) vg_fail("scan: staging copy failed: %s", cudaGetErrorString(e));
+    }
+    if (s->stage_bytes[i] < bytes) {
+        if (s->stage[i]) cudaFreeHost(s->stage[i]);
+        s->stage[i] = NULL;
+        size_t want = bytes + bytes / 4;
+        if (cudaHostAlloc(&s->stage[i], want, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            s->stage_bytes[i] = 0;
+            vg_fail("scan: page-locked staging block of %zu bytes could not be allocated", want);
+        }
+        s->stage_bytes[i] = want;
+    }
+    return s->stage[i];
+}
+
+int vg_scan_pull(VecNode *node, const uint8_t *need, VgDBatch *out) {
+    VgScan *s = (VgScan *)node;
+    VgVtrFile *v = (VgVtrFile *)s->sn.file;
+    memset(out, 0, sizeof(*out));
+    const int64_t g = next_group(s);
+    if (g < 0) return 0;
+    const int64_t n = v->f.rowgroups[g].n_rows;
+    int n_sel = 0;
+    for (int c = 0; c < v->n_cols; c++) n_sel += s->sn.col_mask[c] != 0;
+    out->n_rows = n;
+    out->n_cols = n_sel;
+    out->row_base = s->rows_out;
+    out->cols = (VgCol *)vg_xcalloc((size_t)(n_sel ? n_sel : 1), sizeof(VgCol));
+    const size_t vwords = (size_t)((n + 31) / 32) * 4;
+    size_t total = 0;
+    int o = 0;
+    for (int c = 0; c < v->n_cols; c++) {
+        if (!s->sn.col_mask[c]) continue;
+        const int t = v->f.header.schema.col_types[c];
+        if (!need || need[o]) {
+            if (t == VEC_STRING)
+                vg_fail("string column '%s' is not supported by the GPU path", v->f.header.schema.col_names[c]);
+            total += a256((size_t)data_bytes(t, n)) + a256(vwords);
+        }
+        o++;
+    }
+    s->rows_out += n;
+    if (total == 0) return 1;
+    char *h = (char *)stage_block(s, total);
+    char *d = (char *)vg_dmalloc(total);
+    out->block = d;
+    size_t off = 0;
+    o = 0;
+    for (int c = 0; c < v->n_cols; c++) {
+        if (!s->sn.col_mask[c]) continue;
+        const int t = v->f.header.schema.col_types[c];
+        out->cols[o].type = t;
+        if (!need || need[o]) {
+            const int64_t fo = v->valid_off[(size_t)g * v->n_cols + c];
+            const size_t db = (size_t)data_bytes(t, n);
+            pread_all(v->fd, h + off, db, fo + vg_vbytes(n));
+            out->cols[o].data = d + off;
+            off += a256(db);
+            if (vg_vbytes(n) & 3)   /* the last 32-bit word's bytes past the bitmap read as 0 */
+                memset(h + off + ((size_t)vg_vbytes(n) & ~(size_t)3), 0, 4);
+            pread_all(v->fd, h + off, (size_t)vg_vbytes(n), fo);
+            out->cols[o].valid = (const uint32_t *)(d + off);
+            out->cols[o].voff = 0;
+            off += a256(vwords);
+        }
+        o++;
+    }
+    cudaStream_t st = (cudaStream_t)vg_stream();
+    cudaError_t e = cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !s->ev_live[s->cur]) {
+        e = cudaEventCreateWithFlags(&s->ev[s->cur], cudaEventDisableTiming);
+        if (e == cudaSuccess) s->ev_live[s->cur] = 1;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[s->cur], st);
+    if (e != cudaSuccess) {
+        vg_dbatch_release(out);
+        vg_fail("scan: copy of a row group to the device failed: %s", cudaGetErrorString(e));
+    }
+    s->cur ^= 1;
+    return 1;
+}
+
+/* ---- node ------------------------------------------------------------ */
+
+static void scan_free(VecNode *self) {
+    VgScan *s = (VgScan *)self;
+    for (int i = 0; i < 2; i++) {
+        if (s->ev_live[i]) {
+            cudaEventSynchronize(s->ev[i]);
+            cudaEventDestroy(s->ev[i]);
+        }
+        if (s->stage[i]) cudaFreeHost(s->stage[i]);
+    }
+    if (s->sn.predicate && !s->sn.pred_borrowed) vg_expr_free(s->sn.predicate);
+    vtr_close((VgVtrFile *)s->sn.file);
+    free(s->sn.col_mask);
+    vg_schema_free(&s->sn.base.output_schema);
+    free(s);
+}
+
+ScanNode *scan_node_create(const char *path, int *col_indices, int n_selected) {
+    VgVtrFile *v = vtr_open(path);
+    VgScan *s = (VgScan *)vg_xcalloc(1, sizeof(VgScan));
+    s->sn.file = &v->f;
+    const VecSchema *fs = &v->f.header.schema;
+    s->sn.col_mask = (int *)vg_xcalloc((size_t)(fs->n_cols ? fs->n_cols : 1), sizeof(int));
+    if (!col_indices) {
+        for (int c = 0; c < fs->n_cols; c++) s->sn.col_mask[c] = 1;
+        s->sn.base.output_schema = vg_schema_copy(fs);
+    } else {
+        for (int i = 0; i < n_selected; i++) {
+            if (col_indices[i] < 0 || col_indices[i] >= fs->n_cols) {
+                const int bad = col_indices[i];
+                vtr_close(v);
+                free(s->sn.col_mask);
+                free(s);
+                vg_fail("column index out of range: %d", bad);
+            }
+            s->sn.col_mask[col_indices[i]] = 1;
+        }
+        int k = 0;
+        for (int c = 0; c < fs->n_cols; c++) k += s->sn.col_mask[c];
+        char **names = (char **)vg_xcalloc((size_t)(k ? k : 1), sizeof(char *));
+        VecType *types = (VecType *)vg_xcalloc((size_t)(k ? k : 1), sizeof(VecType));
+        int j = 0;
+        for (int c = 0; c < fs->n_cols; c++) {
+            if (!s->sn.col_mask[c]) continue;
+            names[j] = fs->col_names[c];
+            types[j] = fs->col_types[c];
+            j++;
+        }
+        s->sn.base.output_schema = vg_schema_make(k, names, types);
+        free(names);
+        free(types);
+    }
+    s->sn.base.next_batch = scan_next;
+    s->sn.base.free_node = scan_free;
+    s->sn.base.kind = "ScanNode";
+    return &s->sn;
+}

@@ -83,6 +83,10 @@ void vg_host_bufs_wait_upto(VgHostBufs *h, size_t bytes);   /* the first `bytes`
 void *vg_host_bufs_take(VgHostBufs *h, int b, size_t need);   /* NULL: too small or taken */
 void vg_host_bufs_free(VgHostBufs *h);
 
+/* ---- .vtr scan (scan_vtr.c) ---- */
+int vg_is_vtr_scan(const VecNode *n);
+int vg_scan_pull(VecNode *n, const uint8_t *need, VgDBatch *out);
+
 /* ---- table source (source.c) ---- */
 int vg_is_table_source(const VecNode *n);
 int vg_source_pull(VecNode *n, const uint8_t *need, VgDBatch *out);

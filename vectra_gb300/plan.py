@@ -184,6 +184,14 @@ class Engine:
 
     # subclasses provide make_source(table, batch_rows, **opts) -> node pointer
 
+    def make_scan(self, path, cols=None, scan_fn=None):
+        """A .vtr scan node (scan_node_create through the library's guard);
+        cols: file column indices, None = all."""
+        f = getattr(self.lib, scan_fn or self.scan_fn)
+        f.restype, f.argtypes = C.c_void_p, [C.c_char_p, C.c_void_p, C.c_int]
+        idx = (C.c_int * len(cols))(*cols) if cols else None
+        return self.check(f(path.encode(), idx, len(cols) if cols else 0), "scan")
+
     def filter(self, node, expr_ptr):
         return self.check(self._filter(node, C.cast(expr_ptr, C.c_void_p)), "filter")
 
@@ -254,6 +262,7 @@ class GpuEngine(Engine):
         super().__init__(lib, "vgpu_guard_filter", "vgpu_guard_project", "vgpu_guard_group_agg",
                          "vgpu_guard_join", "vgpu_guard_next_batch", "vgpu_batch_free",
                          "vgpu_last_error")
+        self.scan_fn = "vgpu_guard_scan"
         lib.vgpu_table_source_create.restype = C.c_void_p
         lib.vgpu_table_source_create.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                                  C.c_void_p, C.c_int64, C.c_int64, C.c_int]
@@ -304,6 +313,11 @@ class GpuEngine(Engine):
 
 def tbl(engine, table, batch_rows=None, **opts):
     return Tbl(engine, engine.make_source(table, batch_rows, **opts))
+
+
+def scan(engine, path, cols=None):
+    """tbl(path) over a .vtr file: the engine's scan node."""
+    return Tbl(engine, engine.make_scan(path, cols))
 
 
 class Tbl:
