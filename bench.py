@@ -311,7 +311,7 @@ def gpu_arm(args, rank, world):
     if args.no_e2e:
         line = {"metric": METRIC, "ms_per_step": ms_step, "kernel_ms": agg_ms / args.steps,
                 "kernel_launches_per_step": agg_launches / args.steps,
-                "join_build_ms": build_ms / max(1, build_n.value), "scale": args.scale, "gpu_launches": launches}
+                "join_build_ms": build_ms / args.steps, "scale": args.scale, "gpu_launches": launches}
         return line
     # e2e: page-locked host copies of the same columns
     hf = {k: (v.cpu().pin_memory(), m.cpu().pin_memory()) for k, (v, m) in fcols.items()}
@@ -365,7 +365,7 @@ def gpu_arm(args, rank, world):
                      "kernel_ms_per_step": kernel_ms, "kernel_launches_per_step": agg_launches / args.steps,
                      "traffic": profile_traffic()},
         "host_phases_ms": agg_phases,
-        "join_build_ms": build_ms / max(1, build_n.value),
+        "join_build_ms": build_ms / args.steps,
         "e2e": {"value": whole_job_rate(rows, world, e2e_ms), "unit": "rows/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "node C API, page-locked host columns read in place by the kernels (VGPU_SRC_MAPPED)"},

@@ -38,7 +38,8 @@ namespace {
 // Launch shape: rows per thread, threads per CTA, CTAs per SM the register
 // budget is set for, and whether the next rows' loads are issued before the
 // current rows are processed.  VGPU_JIT_SHAPE="rows,threads,ctas[,pipe]"
-// overrides it (tuning runs).
+// overrides it (tuning runs), and is compiled as given even if registers
+// spill.
 struct Shape { int rows = 2, threads = 1024, ctas = 1, pipe = 1; };
 
 const Shape &shape() {
@@ -58,9 +59,24 @@ const Shape &shape() {
 // The shape a plan is compiled for: partition mode keeps four rows per
 // thread in flight (each row's record position is a global atomic whose
 // latency the other rows' hide).
+// A dense group key read from a direct join's payload copy (the join +
+// aggregate of a fact table against a dimension) runs two CTAs of 768
+// threads per SM: 48 warps instead of 32 hide more of the payload reads'
+// latency, worth the few registers spilled at that budget (measured on the
+// 100M x 10M join + aggregate: 0.85 ms against 0.95 ms at 1024 x 1).
+bool occupancy_shape(const VgAggLaunch &L) {
+    return !getenv("VGPU_JIT_SHAPE") && L.has_join && L.jpay && L.dense && L.jt.direct && !L.part && !L.sel;
+}
+
 Shape plan_shape(const VgAggLaunch &L) {
     Shape sh = shape();
     if (L.part && !getenv("VGPU_JIT_SHAPE")) sh.rows = 4;
+    if (occupancy_shape(L)) {
+        sh.rows = 2;
+        sh.threads = 768;
+        sh.ctas = 2;
+        sh.pipe = 0;
+    }
     return sh;
 }
 
@@ -207,6 +223,13 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
         fmt(s, "#define VGJ_JKIND %d\n#define VGJ_JCOL %d\n#define VGJ_JCONV %d\n#define VGJ_JKT %d\n"
                "#define VGJ_JDIRECT %d\n",
             L.join_kind, L.jkey_col[0], L.jkey_conv[0], L.jt.key_types[0], L.jt.direct ? 1 : 0);
+    // compact payload entries (VgJPay16): which column is narrowed, and its type
+    {
+        const int p16 = (L.has_join && L.jpay && L.jpay16 && L.jt.direct) ? 1 : 0;
+        const int nar = p16 ? L.jpay_narrow : -1;
+        fmt(s, "#define VGJ_PAY16 %d\n#define VGJ_PAY_NARROW %d\n#define VGJ_PAY_NARROW_T %d\n", p16, nar,
+            nar >= 0 ? L.bcols[nar].type : 0);
+    }
     fmt(s, "#define VGJ_NK %d\n#define VGJ_DENSE %d\n#define VGJ_TRACK %d\n#define VGJ_PART %d\n", L.n_keys,
         L.dense ? 1 : 0, L.track_first ? 1 : 0, L.part ? 1 : 0);
     // rows that pass a filter queued per warp (few of a step's rows pass)
@@ -383,7 +406,14 @@ int compile_plan(const VgAggLaunch &L, int S, bool vec, std::vector<char> &cubin
         int spill = 0;
         src = gen_source(L, S, vec, sh);
         if (nvrtc_cubin(src, cubin, &spill, log_out) != 0) return -1;
-        if (spill == 0 || sh.threads <= 256) break;
+        if (spill == 0 || sh.threads <= 256 || getenv("VGPU_JIT_SHAPE")) break;   // an explicit shape is kept
+        if (sh.ctas == 2 && sh.threads == 768) {
+            // the two-CTA shape: a few spilled words are fine, more fall
+            // back to one CTA of 1024 threads
+            if (spill <= 64) break;
+            sh = Shape();
+            continue;
+        }
         sh.threads /= 2;
     }
     // VGPU_JIT_DUMP=<file>: append the source of each plan compiled
@@ -865,7 +895,7 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
     memset(&L, 0, sizeof(L));
     static double dummy[4];
     L.cache_slots = 1024;
-    if (shape == 0 || shape == 4 || shape == 10) {
+    if (shape == 0 || shape == 4 || shape == 10 || shape == 11) {
         L.n_pcols = 2;
         L.pcols[0] = VgCol{VEC_INT64, 0, dummy, nullptr};
         L.pcols[1] = VgCol{VEC_DOUBLE, 0, dummy, nullptr};
@@ -893,6 +923,10 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
         L.jpay_n = 2;
         L.jt.direct = shape != 4;   // shape 4: hashed table, linear-probing chain
         L.jt.dmin = 1;
+        if (shape == 11) {          // compact payload entries, the group key narrowed
+            L.jpay16 = 1;
+            L.jpay_narrow = 0;
+        }
         if (shape == 10) {          // a filter on the probe side in front of the join
             L.pred.n_terms = 1;
             L.pred.term[0] = VgTerm{1, VG_TERM_RANGE, VG_DOM_DOUBLE, 0, 0, 0};

@@ -17,6 +17,7 @@
 //    batch (src/join.c:438-450).  SEMI/ANTI emit a selection vector.
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include "k_common.cuh"
 
@@ -91,7 +92,25 @@ struct PayArgs {
     VgCol c0, c1;
     int n_cols;
     VgJPay *pay;             // NULL: none requested
+    int narrow;              // the column a VgJPay16 entry narrows (int64 / bool), -1: none
+    ulonglong2 *payrow;      // pass 1: each build row's would-be compact entry, in row order (or NULL)
 };
+
+// Whether the payload fits VgJPay16 entries (decided on the host from the
+// statistics of pass 1): one column, or two of which `narrow` is a bool
+// column or an int64 column whose valid values span less than 2^32 (none
+// valid: stored as 0).  *mn: the narrowed column's minimum.
+inline bool pay16_fits(int n_cols, int narrow, int narrow_type, const long long *mm, long long *mn) {
+    *mn = 0;
+    if (n_cols == 1) return true;
+    if (n_cols != 2 || narrow < 0) return false;
+    if (narrow_type == VEC_BOOL) return true;
+    if (narrow_type != VEC_INT64) return false;
+    if (mm[3 * narrow + 2] == 0) return true;
+    if ((unsigned long long)mm[3 * narrow + 1] - (unsigned long long)mm[3 * narrow] > 0xFFFFFFFFull) return false;
+    *mn = mm[3 * narrow];
+    return true;
+}
 
 // Empties the table (init_slots) and / or zeroes the payload copy; resets
 // the counters and the payload min / max words.
@@ -285,11 +304,15 @@ __global__ void jt_insert_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, in
 // Direct tables with a payload copy, built without random writes to the
 // large tables.  Pass 1: every build row records itself in rowof[key - min]
 // (4 bytes per key: small enough to stay in L2) with the validity bits of
-// its two payload values in bits 29 and 30, and reports min, max and count
-// of the valid values of int64 payload columns (mm, 3 words per column).
-// If a key repeats, one of its rows survives; pass 2 finds that out while
-// the surviving rows write their keys' entries (reading their payload values
-// in row order), and the entries of keys no row has are cleared last.
+// its two payload values in bits 29 and 30, reports a key that repeats (an
+// exchange that finds another row), and reports min, max and count of the
+// valid values of int64 payload columns (mm, 3 words per column); for a
+// payload that may take compact entries it also writes each row's would-be
+// entry in row order.  Pass 2, once the host has read those statistics:
+// compact entries are gathered by slot (coalesced writes,
+// jt_pay16_gather_kernel); otherwise each recorded row writes its key's full
+// entry (reading its payload values in row order) and the entries of keys
+// no row has are cleared last.
 //
 // Each thread takes kBuildU rows per step (blockDim apart, so every load
 // stays coalesced) and issues all their loads before it uses any: a row's
@@ -344,7 +367,7 @@ __global__ void jt_rows_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int3
                     if (c >= P.n_cols) continue;
                     const VgCol &col = c == 0 ? P.c0 : P.c1;
                     pv[c][u] = valid_word(col, r);
-                    if (col.type == VEC_INT64) pb[c][u] = vg_load_bits(col, r);
+                    if (col.type == VEC_INT64 || P.payrow) pb[c][u] = vg_load_bits(col, r);
                 }
             }
         }
@@ -361,8 +384,18 @@ __global__ void jt_rows_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int3
             uint32_t vb = 0;                           // validity of the payload values
             if (P.n_cols > 0 && valid_bit(P.c0, r, pv[0][u])) vb |= 1u;
             if (P.n_cols > 1 && valid_bit(P.c1, r, pv[1][u])) vb |= 2u;
-            if (d >= 0) rowof[d] = (uint32_t)r | (vb << kRowBits);
+            // a repeated key finds another row here: reported (the payload
+            // copy then does not apply)
+            if (d >= 0 && atomicExch(rowof + d, (uint32_t)r | (vb << kRowBits)) != 0xFFFFFFFFu)
+                atomicOr(counters + 3, 1u);
             rslot[r] = (int32_t)d;
+            if (P.payrow) {
+                // the kept column whole, the narrowed one's low 32 bits (its
+                // minimum is known only at the end of this pass)
+                const uint64_t a = P.n_cols == 1 ? pb[0][u] : (P.narrow == 0 ? pb[1][u] : pb[0][u]);
+                const uint64_t nv = P.narrow == 0 ? pb[0][u] : pb[1][u];
+                P.payrow[r] = make_ulonglong2(a, P.n_cols == 1 ? 0ull : (unsigned long long)(uint32_t)nv);
+            }
 #pragma unroll
             for (int c = 0; c < 2; c++) {
                 if (c >= P.n_cols || !((vb >> c) & 1u)) continue;
@@ -464,6 +497,25 @@ __global__ void jt_pay_absent_kernel(VgJoinTable jt, const uint32_t *rowof, PayA
             const int64_t d = b0 + (int64_t)u * blockDim.x + threadIdx.x;
             if (d <= jt.cap && v[u] == 0xFFFFFFFFu) vg_st256(P.pay + d, 0ull, 0ull, 0ull, 0ull);
         }
+    }
+}
+
+// Compact entries by slot (coalesced writes): slot d takes the row its key
+// recorded in pass 1 and that row's would-be entry, with the narrowed
+// column rebased on its minimum; slots no row has are cleared.
+__global__ void jt_pay16_gather_kernel(VgJoinTable jt, const uint32_t *rowof, const ulonglong2 *payrow, int n_cols,
+                                       long long nmin, VgJPay16 *pay) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d <= jt.cap; d += stride) {
+        const uint32_t v = d < jt.cap ? __ldg(rowof + d) : 0xFFFFFFFFu;
+        ulonglong2 e = make_ulonglong2(0ull, 0ull);
+        if (v != 0xFFFFFFFFu) {
+            const ulonglong2 q = __ldg(payrow + (v & kRowMask));
+            const uint32_t meta = 1u | (((v >> kRowBits) & 3u) << 1);
+            const uint32_t b = n_cols == 1 ? 0u : (uint32_t)q.y - (uint32_t)(unsigned long long)nmin;
+            e = make_ulonglong2(q.x, (unsigned long long)b | ((unsigned long long)meta << 32));
+        }
+        *((ulonglong2 *)pay + d) = e;
     }
 }
 
@@ -649,7 +701,8 @@ size_t vgk_join_build_scratch_bytes(int64_t n_build) {
     // words, and the row of each key of a direct table (whose range is
     // below max(2 n, 65536), node_join.c)
     const size_t rowof = a256((size_t)((2 * n > 65536 ? 2 * n : 65536) + 64) * 4);
-    return a256((size_t)n * 4) + a256((size_t)n * 8) + vgk_sort_pairs_scratch(n) + 256 + 256 + rowof;
+    return a256((size_t)n * 4) + a256((size_t)n * 8) + vgk_sort_pairs_scratch(n) + 256 + 256 + rowof +
+           a256((size_t)n * 16);   // pass 1's row-order compact entries
 }
 
 // jt->cap, state, keys, start, count, rows (n_build entries) are allocated by
@@ -657,7 +710,9 @@ size_t vgk_join_build_scratch_bytes(int64_t n_build) {
 int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t *key_conv,
                    int64_t n_build, void *d_scratch, size_t scratch_bytes, int64_t *h_distinct,
                    int64_t *h_maxdup, const VgCol *pay_cols, int n_pay, VgJPay *pay, int64_t *h_pay_mm,
-                   int *slots_ready, vg_stream_t s) {
+                   int *h_pay_layout, int64_t *h_pay_min, int *slots_ready, vg_stream_t s) {
+    if (h_pay_layout) *h_pay_layout = -2;
+    if (h_pay_min) *h_pay_min = 0;
     cudaStream_t st = (cudaStream_t)s;
     if (scratch_bytes < vgk_join_build_scratch_bytes(n_build)) {
         snprintf(g_err, sizeof(g_err), "join build scratch too small");
@@ -687,6 +742,13 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         P.n_cols = n_pay;
         if (n_pay > 0) P.c0 = pay_cols[0];
         if (n_pay > 1) P.c1 = pay_cols[1];
+        // the column a compact entry would narrow: a bool or int64 one (the
+        // second if both qualify)
+        P.narrow = -1;
+        if (n_pay == 2) {
+            if (P.c1.type == VEC_INT64 || P.c1.type == VEC_BOOL) P.narrow = 1;
+            else if (P.c0.type == VEC_INT64 || P.c0.type == VEC_BOOL) P.narrow = 0;
+        }
     }
     if (slots_ready) *slots_ready = 1;
     if (P.pay && n_build >= ((int64_t)1 << kRowBits)) P.pay = nullptr;   // too many rows for rowof: no payload
@@ -702,6 +764,13 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         // derived later, only if something reads it
         // (vgk_join_slots_from_payload)
         uint32_t *rowof = (uint32_t *)p;
+        p += a256((size_t)((2 * n > 65536 ? 2 * n : 65536) + 64) * 4);
+        // a payload that can take compact entries (one column, or a bool /
+        // int64 one to narrow) also gets each row's would-be entry in row
+        // order in pass 1, to be gathered by slot once the narrowed column's
+        // range is known
+        const bool cand16 = h_pay_layout && !getenv("VGPU_PAY32") && (n_pay == 1 || P.narrow >= 0);
+        P.payrow = cand16 ? (ulonglong2 *)p : nullptr;
         jt_init_kernel<<<1, 32, 0, st>>>(*jt, counters, nullptr, 0, mm);
         vg_launch_counter++;
         if (check(cudaMemsetAsync(rowof, 0xFF, (size_t)jt->cap * 4, st), "join build")) return -1;
@@ -709,11 +778,8 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         if (n_build > 0) {
             const int gb = grid_for((n_build + kBuildU - 1) / kBuildU, 256);
             jt_rows_direct_kernel<<<gb, 256, 0, st>>>(*jt, K, n_build, rslot, counters, P, rowof, mm);
-            jt_pay_scatter_kernel<<<gb, 256, 0, st>>>(*jt, rowof, rslot, n_build, P, counters);
-            vg_launch_counter += 2;
+            vg_launch_counter++;
         }
-        jt_pay_absent_kernel<<<grid_for((jt->cap + kBuildU) / kBuildU, 256), 256, 0, st>>>(*jt, rowof, P);
-        vg_launch_counter++;
         vg_prof_end(VG_PROF_JOIN_BUILD, st);
         // counters and the payload min / max words are adjacent (256 bytes
         // apart): one read-back
@@ -729,7 +795,29 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         }
         if (h_pay_mm)
             for (int i = 0; i < 6; i++) h_pay_mm[i] = hm[i];
+        long long nmin = 0;
+        const bool fits16 = cand16 && !hc[3] &&
+                            pay16_fits(P.n_cols, P.narrow, P.narrow == 1 ? P.c1.type : P.c0.type, hm, &nmin);
         if (!hc[3]) {
+            vg_prof_begin(VG_PROF_JOIN_BUILD, st);
+            if (fits16) {
+                jt_pay16_gather_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, rowof, P.payrow, P.n_cols,
+                                                                                    nmin, (VgJPay16 *)P.pay);
+                vg_launch_counter++;
+                *h_pay_layout = P.n_cols == 1 ? -1 : P.narrow;
+                if (h_pay_min) *h_pay_min = nmin;
+            } else {
+                // full entries: each recorded row writes its key's entry
+                if (n_build > 0) {
+                    const int gb = grid_for((n_build + kBuildU - 1) / kBuildU, 256);
+                    jt_pay_scatter_kernel<<<gb, 256, 0, st>>>(*jt, rowof, rslot, n_build, P, counters);
+                    vg_launch_counter++;
+                }
+                jt_pay_absent_kernel<<<grid_for((jt->cap + kBuildU) / kBuildU, 256), 256, 0, st>>>(*jt, rowof, P);
+                vg_launch_counter++;
+            }
+            vg_prof_end(VG_PROF_JOIN_BUILD, st);
+            if (check(cudaGetLastError(), "join build")) return -1;
             *h_distinct = -1;      // not counted on this path
             *h_maxdup = 1;
             jt->rows = nullptr;
@@ -877,6 +965,29 @@ int vgk_join_payload(const VgJoinTable *jt, const VgCol *key, const VgCol *cols,
                                                              n_cols > 1 ? cols[1] : none, n_cols, pay);
       vg_launch_counter++; }
     return check(cudaGetLastError(), "join payload");
+}
+
+int vgk_join_slots_from_keys(const VgJoinTable *jt, const VgCol *key, int32_t key_conv, int64_t n_build,
+                             void *d_scratch, vg_stream_t s) {
+    cudaStream_t st = (cudaStream_t)s;
+    KeyArgs K;
+    memset(&K, 0, sizeof(K));
+    K.n_keys = 1;
+    K.cols[0] = *key;
+    K.conv[0] = key_conv;
+    K.types[0] = jt->key_types[0];
+    PayArgs P;
+    memset(&P, 0, sizeof(P));
+    const int64_t n = n_build > 0 ? n_build : 1;
+    int32_t *rslot = (int32_t *)d_scratch;
+    uint32_t *counters = (uint32_t *)((char *)d_scratch + (((size_t)n * 4 + 127) & ~(size_t)127));
+    jt_init_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, counters, nullptr, 1, nullptr);
+    vg_launch_counter++;
+    if (n_build > 0) {
+        jt_insert_direct_kernel<<<(unsigned)((n_build + 255) / 256), 256, 0, st>>>(*jt, K, n_build, rslot, counters, P);
+        vg_launch_counter++;
+    }
+    return check(cudaGetLastError(), "join slots");
 }
 
 int vgk_join_slots_from_payload(const VgJoinTable *jt, const VgJPay *pay, vg_stream_t s) {

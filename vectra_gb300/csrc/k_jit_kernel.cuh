@@ -256,7 +256,36 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
 #endif
                 need |= 1u << j;
             }
-#if VGJ_PAY
+#if VGJ_PAY && VGJ_PAY16
+            // compact payload copy of a direct table: one 16-byte entry per
+            // probe, {kept column, narrowed column, validity}
+            ulonglong2 ea[R];
+#pragma unroll
+            for (int j = 0; j < R; j++)
+                if ((need >> j) & 1u) ea[j] = __ldg((const ulonglong2 *)L.jpay + slot[j]);
+#pragma unroll
+            for (int i = 0; i < kNB; i++) X.bok[i] = 0;
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                if (!((need >> j) & 1u)) continue;
+                const uint32_t meta = (uint32_t)(ea[j].y >> 32);
+                if (!(meta & 1u)) continue;
+                matched |= 1u << j;
+                brow[j] = 0;
+                if (VGJ_PAY_NARROW < 0) {
+                    X.b[0][j] = ea[j].x;
+                    X.bok[0] |= ((meta >> 1) & 1u) << j;
+                } else {
+                    constexpr int kN = VGJ_PAY_NARROW < 0 ? 0 : VGJ_PAY_NARROW;
+                    constexpr int kK = kNB > 1 ? 1 - kN : 0;
+                    const uint32_t b = (uint32_t)ea[j].y;
+                    X.b[kK][j] = ea[j].x;
+                    X.b[kN][j] = VGJ_PAY_NARROW_T == VEC_BOOL ? (uint64_t)b : (uint64_t)L.jpay_min + (uint64_t)b;
+                    X.bok[0] |= ((meta >> 1) & 1u) << j;
+                    if (kNB > 1) X.bok[kNB > 1 ? 1 : 0] |= ((meta >> 2) & 1u) << j;
+                }
+            }
+#elif VGJ_PAY
             // payload copy: key, build row, validity and up to two build
             // columns in one 32-byte sector per probe
             ulonglong2 ea[R], eb[R];

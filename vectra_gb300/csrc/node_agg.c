@@ -1179,6 +1179,9 @@ static VecBatch *agg_next(VecNode *self) {
         g_agg_ms[1] += now_ms() - tb;
         L->jpay = pay;
         L->jpay_n = pay ? P.bset.n : 0;
+        L->jpay16 = pay && B->pay_layout != -2;
+        L->jpay_narrow = pay ? (B->pay_layout >= 0 ? B->pay_layout : -1) : -1;
+        L->jpay_min = pay ? B->pay_min : 0;
         L->has_join = 1;
         L->join_kind = vg_join_kind(P.join);
         L->n_jkeys = B->n_keys;

@@ -203,8 +203,10 @@ static void join_build(VgJoin *j) {
     size_t sb = vgk_join_build_scratch_bytes(total);
     void *scratch = vg_dmalloc(sb);
     int64_t distinct = 0, maxdup = 0;
+    j->B.pay_layout = -2;
     int rc = vgk_join_build(jt, kc, nk, j->conv_build, total, scratch, sb, &distinct, &maxdup, pc,
-                            j->pay ? j->pay_n : 0, j->pay, j->B.pay_mm, &j->slots_ready, vg_stream());
+                            j->pay ? j->pay_n : 0, j->pay, j->B.pay_mm, &j->B.pay_layout, &j->B.pay_min,
+                            &j->slots_ready, vg_stream());
     if (j->pay) {
         j->B.pay_n = j->pay_n;
         for (int q = 0; q < j->pay_n; q++) j->B.pay_col[q] = j->pay_col[q];
@@ -245,7 +247,18 @@ void vg_join_ensure_slots(VecNode *n) {
     VgJoin *j = (VgJoin *)n;
     join_build(j);
     if (j->slots_ready) return;
-    vg_check_rc(vgk_join_slots_from_payload(&j->B.jt, j->pay, vg_stream()), "join slots");
+    if (j->B.pay_layout == -2) {
+        vg_check_rc(vgk_join_slots_from_payload(&j->B.jt, j->pay, vg_stream()), "join slots");
+    } else {
+        /* compact entries hold neither keys nor build rows: the slots come
+         * from the key column */
+        void *scratch = vg_dmalloc((size_t)(j->B.jt.n_build > 0 ? j->B.jt.n_build : 1) * 4 + 256);
+        const VgCol kc = j->B.bcols[j->jn.keys[0].right_col];
+        const int rc = vgk_join_slots_from_keys(&j->B.jt, &kc, j->conv_build[0], j->B.jt.n_build, scratch,
+                                                vg_stream());
+        vg_dfree(scratch);
+        vg_check_rc(rc, "join slots");
+    }
     j->slots_ready = 1;
 }
 

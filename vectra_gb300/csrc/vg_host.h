@@ -149,6 +149,10 @@ typedef struct {
     int32_t pay_col[2];
     int pay_mm_ok;
     int64_t pay_mm[6];
+    /* the payload copy's entries: -2 VgJPay; -1 VgJPay16 of one column;
+     * 0 / 1 VgJPay16 narrowing that payload column (minimum pay_min) */
+    int pay_layout;
+    int64_t pay_min;
 } VgJoinBuilt;
 const VgJoinBuilt *vg_join_build_now(VecNode *n);
 /* builds with a payload copy of right columns cols[0..n_cols) (n_cols <= 2);

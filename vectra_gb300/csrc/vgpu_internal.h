@@ -204,6 +204,19 @@ typedef struct {
     uint64_t p[2];
 } VgJPay;
 
+/* The compact form of the payload copy of a direct-addressed table (the
+ * slot is key - min, so no key; the fused aggregation reads no build row):
+ * 16 bytes per slot.  `a` holds the one payload column that is not
+ * narrowed (any type); `b` the narrowed one: an int64 column whose valid
+ * values span less than 2^32 as (value - its minimum), a bool column as its
+ * byte.  meta as in VgJPay.  Used when the payload is one column, or two of
+ * which one narrows. */
+typedef struct {
+    uint64_t a;
+    uint32_t b;
+    uint32_t meta;
+} VgJPay16;
+
 /* Join hash table over the build side (keys unique per slot; rows of a key
  * listed in ascending build-row order in rows[start .. start+count)). */
 /* Single-key join slot: one 16-byte sector per probe.  key == VG_JEMPTY
@@ -360,6 +373,11 @@ typedef struct {
      * (read by the run-time specialised kernel). */
     const VgJPay *jpay;
     int32_t   jpay_n;
+    /* 1: jpay holds VgJPay16 entries; jpay_narrow: the payload column kept in
+     * VgJPay16.b (-1: none, one payload column), jpay_min its minimum */
+    int32_t   jpay16;
+    int32_t   jpay_narrow;
+    int64_t   jpay_min;
     /* 1: partitioned aggregation's first step (run-time specialised kernel
      * only): rows with a valid key become records (po); NA-key rows update
      * the group table gt, which holds the NA group alone. */
@@ -435,18 +453,26 @@ size_t vgk_order_scratch_bytes(int64_t n_groups);
 /* join */
 int64_t vgk_join_cap(int64_t n_build);
 size_t vgk_join_build_scratch_bytes(int64_t n_build);
-/* pay (optional, (cap + 1) entries): filled with the payload copy of
- * pay_cols[0..n_pay) when every key is unique (in the insert pass itself
- * for direct tables, which then also report min, max and count of the
- * valid values of int64 payload columns in h_pay_mm[3 c .. 3 c + 2], and
- * leave the slot table unfilled: *slots_ready == 0) */
+/* pay (optional, (cap + 1) 32-byte entries of room): filled with the
+ * payload copy of pay_cols[0..n_pay) when every key is unique (for direct
+ * tables in passes of their own, which then also report min, max and count
+ * of the valid values of int64 payload columns in h_pay_mm[3 c .. 3 c + 2],
+ * and leave the slot table unfilled: *slots_ready == 0).  Direct tables
+ * write VgJPay16 entries when the payload fits them: *h_pay_layout = -1
+ * (one payload column) or the index of the narrowed column (its minimum in
+ * *h_pay_min); -2: VgJPay entries. */
 int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t *key_conv,
                    int64_t n_build, void *d_scratch, size_t scratch_bytes, int64_t *h_distinct,
                    int64_t *h_maxdup, const VgCol *pay_cols, int n_pay, VgJPay *pay, int64_t *h_pay_mm,
-                   int *slots_ready, vg_stream_t s);
+                   int *h_pay_layout, int64_t *h_pay_min, int *slots_ready, vg_stream_t s);
 /* fills the slot table of a unique-key direct table from its payload copy
- * (a build that returned *slots_ready == 0) */
+ * (a build that returned *slots_ready == 0 with VgJPay entries) */
 int vgk_join_slots_from_payload(const VgJoinTable *jt, const VgJPay *pay, vg_stream_t s);
+/* the same from the key column itself (a build that wrote VgJPay16 entries,
+ * which hold neither keys nor build rows); d_scratch: n_build * 4 + 256
+ * bytes */
+int vgk_join_slots_from_keys(const VgJoinTable *jt, const VgCol *key, int32_t key_conv, int64_t n_build,
+                             void *d_scratch, vg_stream_t s);
 size_t vgk_join_probe_scratch_bytes(int64_t n_logical);
 int vgk_join_probe_count(const VgJoinTable *jt, const VgCol *pkeys, int n_keys, const int32_t *key_conv,
                          int64_t n_rows, const int32_t *d_sel, int64_t sel_n, int kind,
