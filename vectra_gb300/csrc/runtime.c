@@ -378,6 +378,51 @@ static size_t value_bytes(int type, int64_t n) {
 }
 static size_t valid_bytes_dev(int64_t n) { return (size_t)((n + 31) / 32) * 4; }
 
+/* Two page-locked staging blocks for batches of foreign children (host
+ * batches the caller frees): a batch's needed columns are copied into one
+ * block laid out like its device block, then moved by one asynchronous copy;
+ * the host batch is freed at once and the block is reused only after the
+ * event behind its copy has completed, so copy and kernels overlap the
+ * child's production of the next batch. */
+static void *g_stage[2];
+static size_t g_stage_bytes[2];
+static cudaEvent_t g_stage_ev[2];
+static int g_stage_ev_live[2];
+static int g_stage_cur;
+
+static char *stage_take(size_t bytes) {
+    const int i = g_stage_cur;
+    if (g_stage_ev_live[i]) {
+        cudaError_t e = cudaEventSynchronize(g_stage_ev[i]);
+        if (e != cudaSuccess) vg_fail("staging copy failed: %s", cudaGetErrorString(e));
+    }
+    if (g_stage_bytes[i] < bytes) {
+        if (g_stage[i]) cudaFreeHost(g_stage[i]);
+        g_stage[i] = NULL;
+        g_stage_bytes[i] = 0;
+        size_t want = bytes + bytes / 4;
+        if (cudaHostAlloc(&g_stage[i], want, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            vg_fail("page-locked staging block of %zu bytes could not be allocated", want);
+        }
+        g_stage_bytes[i] = want;
+    }
+    return (char *)g_stage[i];
+}
+
+static void stage_send(void *dst, const void *src, size_t bytes) {
+    const int i = g_stage_cur;
+    cudaStream_t st = (cudaStream_t)vg_stream();
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !g_stage_ev_live[i]) {
+        e = cudaEventCreateWithFlags(&g_stage_ev[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) g_stage_ev_live[i] = 1;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(g_stage_ev[i], st);
+    if (e != cudaSuccess) vg_fail("staged copy to the device failed: %s", cudaGetErrorString(e));
+    g_stage_cur ^= 1;
+}
+
 int vg_pull(VecNode *child, const uint8_t *need, int keep_host, VgDBatch *out) {
     memset(out, 0, sizeof(*out));
     if (vg_is_table_source(child) && !keep_host) return vg_source_pull(child, need, out);
@@ -398,6 +443,36 @@ int vg_pull(VecNode *child, const uint8_t *need, int keep_host, VgDBatch *out) {
     if (b->sel) total += a256((size_t)b->sel_n * 4);
     char *blk = total ? (char *)vg_dmalloc(total) : NULL;
     out->block = blk;
+    if (!keep_host && total) {
+        /* staged: the batch's bytes into a page-locked block laid out like
+         * the device block, one copy, the host batch freed at once */
+        char *h = stage_take(total);
+        size_t o = 0;
+        for (int c = 0; c < b->n_cols; c++) {
+            VecArray *a = &b->columns[c];
+            out->cols[c].type = a->type;
+            if (!need || !need[c]) continue;
+            const size_t vb = value_bytes(a->type, n);
+            if (vb) memcpy(h + o, a->type == VEC_BOOL ? (void *)a->buf.bln : (void *)a->buf.i64, vb);
+            out->cols[c].data = blk + o;
+            o += a256(vb);
+            if (a->validity) {
+                const size_t wb = valid_bytes_dev(n);
+                memset(h + o + (wb >= 4 ? wb - 4 : 0), 0, wb >= 4 ? 4 : wb);
+                memcpy(h + o, a->validity, (size_t)vg_vbytes(n));
+                out->cols[c].valid = (const uint32_t *)(blk + o);
+            }
+            o += a256(valid_bytes_dev(n));
+        }
+        if (b->sel) {
+            memcpy(h + o, b->sel, (size_t)b->sel_n * 4);
+            out->d_sel = (const int32_t *)(blk + o);
+            out->sel_n = b->sel_n;
+        }
+        stage_send(blk, h, total);
+        vg_batch_free(b);
+        return 1;
+    }
     size_t off = 0;
     for (int c = 0; c < b->n_cols; c++) {
         VecArray *a = &b->columns[c];
