@@ -143,6 +143,19 @@ void   vgpu_profile_enable(int on);
 void   vgpu_profile_reset(void);
 double vgpu_profile_ms(int kernel_class, unsigned long long *launches);
 
+/* ---- diagnostics (no reference counterpart) ---------------------------- */
+/* Bytes the device's default memory pool (where libvgpu allocates) has
+ * handed out and not taken back, or -1: a failed call leaves it where it
+ * was before the call. */
+long long vgpu_device_bytes_in_use(void);
+/* Fault injection: the n-th device allocation from now on fails (0: none);
+ * also read once from the environment, VGPU_FAIL_ALLOC=n. */
+void      vgpu_debug_fail_alloc(long n);
+/* Runs the device's bounded wait on a word nothing changes for `limit`
+ * polls: returns -1 with vgpu_last_error describing the expired wait (the
+ * device stays usable), as any wait of a libvgpu kernel that runs out does. */
+int       vgpu_wait_selftest(long long limit);
+
 /* ---- guarded entry points for callers without an R error handler ----- */
 /* Each returns NULL (and sets vgpu_last_error) where the unguarded call
  * would raise vectra_error. */
@@ -261,6 +274,11 @@ int     vgpu_server_poll(void *server);          /* requests not yet done, or -1
 int     vgpu_server_done(void *server, int64_t id);
 int     vgpu_server_result(void *server, int64_t id, VgpuServeResult *result);
 void    vgpu_server_release(void *server, int64_t id);
+/* Withdraws a request still waiting for admission (submitted, not yet
+ * admitted by a poll): 0, its id is then unknown to the server; -1 if it
+ * is unknown or already admitted (release it once done).  A request whose
+ * estimate alone exceeds the budget is refused at submit (-1). */
+int     vgpu_server_cancel(void *server, int64_t id);
 /* Builds a table's key set now (it is built at the first request that
  * needs it otherwise): 0 or -1. */
 int     vgpu_server_warm(void *server, int table);

@@ -425,5 +425,21 @@ VG_DEV double vg_window6_to_double(const int64_t (&w)[6], int base) {
 
 #define VG_SPIN_LIMIT (1 << 22)
 
+// Waits while the word at w holds `busy` (a slot another thread is still
+// filling), starting from the value `v` already read, for at most `limit`
+// polls with a short sleep between them.  Returns the value that ended the
+// wait, or `busy` when the limit ran out: the caller then records
+// VG_ERR_WAIT in its launch's error word and gives up, so the host sees an
+// error status instead of a kernel that never ends.
+VG_DEV uint32_t vg_wait_while(const uint32_t *w, uint32_t busy, uint32_t v, long long limit) {
+    long long spins = 0;
+    while (v == busy) {
+        if (++spins > limit) return busy;
+        __nanosleep(32);
+        v = vg_ld_acquire(w);
+    }
+    return v;
+}
+
 
 

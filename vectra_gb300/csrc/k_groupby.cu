@@ -480,7 +480,31 @@ int grid_for(int64_t n, int threads) {
 
 }  // namespace
 
+// One thread waits, through the table's own bounded wait, on a word that
+// nothing will change; the expired wait is reported in the error word.
+__global__ void wait_selftest_kernel(const uint32_t *busy_word, long long limit, uint32_t *err) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const uint32_t v = vg_wait_while(busy_word, 1u, vg_ld_acquire(busy_word), limit);
+    if (v == 1u) atomicOr(err, VG_ERR_WAIT);
+}
+
 extern "C" {
+
+// Runs wait_selftest_kernel: 0 and the error word read back in *code, or -1.
+int vgk_wait_selftest(long long limit, uint32_t *code, vg_stream_t s) {
+    cudaStream_t st = (cudaStream_t)s;
+    uint32_t *d = nullptr;
+    if (check(cudaMallocAsync((void **)&d, 256, st), "wait self-test")) return -1;
+    uint32_t h[2] = {1u, 0u};
+    if (check(cudaMemcpyAsync(d, h, 8, cudaMemcpyHostToDevice, st), "wait self-test")) return -1;
+    wait_selftest_kernel<<<1, 32, 0, st>>>(d, limit, d + 1);
+    vg_launch_counter++;
+    cudaMemcpyAsync(h, d, 8, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    if (check(cudaStreamSynchronize(st), "wait self-test")) return -1;
+    *code = h[1];
+    return 0;
+}
 
 const char *vgk_agg_last_error(void) { return g_err; }
 

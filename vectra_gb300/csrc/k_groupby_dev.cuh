@@ -362,12 +362,8 @@ VG_DEV int64_t gt_find_insert(const VgGroupTable &gt, const Keys &k, int nk, con
             }
             st = vg_ld_acquire(gt.state + slot);
         }
-        int spins = 0;
-        while (st == 1u) {
-            if (++spins > VG_SPIN_LIMIT) { atomicOr(gt.err, VG_ERR_WAIT); return -1; }
-            __nanosleep(32);
-            st = vg_ld_acquire(gt.state + slot);
-        }
+        st = vg_wait_while(gt.state + slot, 1u, st, VG_SPIN_LIMIT);
+        if (st == 1u) { atomicOr(gt.err, VG_ERR_WAIT); return -1; }
         uint32_t tnm = *(volatile uint32_t *)(gt.nullmask + slot);
         if (keys_eq(gt.keys, gt.cap, slot, k, nk, kt, tnm, nm)) return slot;
         slot = (slot + 1) & mask;

@@ -704,8 +704,15 @@ int64_t vgpu_server_submit(void *srv, const VgpuServeQuery *q) {
     }
     Request R;
     R.q = *q;
-    R.id = S->next_id++;
     R.bytes = estimate(S, *q);
+    if (R.bytes > S->budget) {
+        // admission is by estimated bytes: a request that alone exceeds the
+        // budget could never be admitted without breaking it
+        vg_set_error("vgpu_server_submit: the request needs an estimated %lld bytes, more than the server's "
+                     "budget of %lld", (long long)R.bytes, (long long)S->budget);
+        return -1;
+    }
+    R.id = S->next_id++;
     R.scratch_bytes = scratch_estimate(S, *q);
     R.scratch = nullptr;
     R.state = 0;
@@ -760,6 +767,31 @@ int vgpu_server_result(void *srv, int64_t id, VgpuServeResult *out) {
         out->rows = (int64_t)R.h_rows;
         out->sel = R.dev.out_sel;
     }
+    return 0;
+}
+
+int vgpu_server_cancel(void *srv, int64_t id) {
+    Server *S = (Server *)srv;
+    if (!S) {
+        vg_set_error("vgpu_server_cancel: no server");
+        return -1;
+    }
+    auto it = S->reqs.find(id);
+    if (it == S->reqs.end()) {
+        vg_set_error("vgpu_server_cancel: no request %lld", (long long)id);
+        return -1;
+    }
+    if (it->second.state != 0) {
+        vg_set_error("vgpu_server_cancel: request %lld is already admitted (release it once it is done)",
+                     (long long)id);
+        return -1;
+    }
+    for (auto q = S->queue.begin(); q != S->queue.end(); ++q)
+        if (*q == id) {
+            S->queue.erase(q);
+            break;
+        }
+    S->reqs.erase(it);
     return 0;
 }
 

@@ -341,7 +341,7 @@ static int run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_logi
     if (!S->counters) S->counters = (uint32_t *)vg_dmalloc(256);
     if (g_spill_rows_cap < need_rows) {
         vg_dfree(g_spill_rows);
-        g_spill_rows = (int64_t *)vg_dmalloc((size_t)need_rows * 16);
+        g_spill_rows = (int64_t *)vg_dmalloc_kept((size_t)need_rows * 16);   /* reused by later calls */
         g_spill_rows_cap = need_rows;
     }
     S->rows = g_spill_rows;
@@ -1148,7 +1148,7 @@ static void pagg_free(PAgg *pg) {
     free(pg);
 }
 
-static VecBatch *agg_next(VecNode *self) {
+static VecBatch *agg_next_body(VecNode *self) {
     VgAgg *A = (VgAgg *)self;
     if (A->ga.done) return NULL;
     A->ga.done = 1;
@@ -1320,6 +1320,14 @@ static VecBatch *agg_next(VecNode *self) {
     if (was_pagg) g_pagg_ms[6] += now_ms() - t_start;
     else g_agg_ms[4] += now_ms() - t_start;
     return res;
+}
+
+/* one node API call: its temporary device memory is released if it fails */
+static VecBatch *agg_next(VecNode *self) {
+    vg_scope_enter();
+    VecBatch *b = agg_next_body(self);
+    vg_scope_leave();
+    return b;
 }
 
 static void agg_free(VecNode *self) {

@@ -77,7 +77,7 @@ const VgPred *vg_filter_cnf(VecNode *n, VecNode **child_out, const VgColSet **se
     return f->compiled == 1 ? &f->pred : NULL;
 }
 
-static VecBatch *filter_next(VecNode *self) {
+static VecBatch *filter_next_body(VecNode *self) {
     VgFilter *f = (VgFilter *)self;
     compile_filter(f);
     if (f->compiled == 3) vg_fail("%s", f->err);
@@ -114,6 +114,14 @@ static VecBatch *filter_next(VecNode *self) {
         vg_dbatch_release(&db);   /* empty after filtering: drop and pull the next */
     }
     return NULL;
+}
+
+/* one node API call: its temporary device memory is released if it fails */
+static VecBatch *filter_next(VecNode *self) {
+    vg_scope_enter();
+    VecBatch *b = filter_next_body(self);
+    vg_scope_leave();
+    return b;
 }
 
 static void filter_free(VecNode *self) {

@@ -112,6 +112,7 @@ static void join_build(VgJoin *j) {
         }
         j->kept = bs[0];
         j->has_kept = 1;
+        vg_dkeep(j->kept.block);   /* the node owns it now */
         nb = 0;
     }
     /* otherwise a dense device copy of the logical rows (one gather per batch) */
@@ -119,7 +120,7 @@ static void join_build(VgJoin *j) {
     size_t bytes = 0;
     for (int c = 0; c < nr && !j->has_kept; c++)
         if (need[c]) bytes += a256((size_t)total * elem(rs->col_types[c]) + 8) + a256(wbytes);
-    char *blk = j->has_kept ? NULL : (char *)vg_dmalloc(bytes ? bytes : 256);
+    char *blk = j->has_kept ? NULL : (char *)vg_dmalloc_kept(bytes ? bytes : 256);
     j->build_block = blk;
     size_t off = 0;
     for (int c = 0; c < nr && !j->has_kept; c++) {
@@ -172,7 +173,7 @@ static void join_build(VgJoin *j) {
     size_t rows_b = a256((size_t)(total > 0 ? total : 1) * 4);
     size_t tb = (nk == 1) ? a256((size_t)(tcap + 1) * sizeof(VgJSlot)) + rows_b + 256
                           : a256((size_t)tcap * 4) * 3 + a256((size_t)tcap * 8 * (size_t)nk) + rows_b + 256;
-    char *t = (char *)vg_dmalloc(tb);
+    char *t = (char *)vg_dmalloc_kept(tb);
     j->table_block = t;
     VgJoinTable *jt = &j->B.jt;
     memset(jt, 0, sizeof(*jt));
@@ -198,7 +199,7 @@ static void join_build(VgJoin *j) {
     memset(pc, 0, sizeof(pc));
     if (j->pay_n > 0 && nk == 1) {
         for (int q = 0; q < j->pay_n; q++) pc[q] = j->B.bcols[j->pay_col[q]];
-        j->pay = (VgJPay *)vg_dmalloc((size_t)(tcap + 1) * sizeof(VgJPay));
+        j->pay = (VgJPay *)vg_dmalloc_kept((size_t)(tcap + 1) * sizeof(VgJPay));
     }
     size_t sb = vgk_join_build_scratch_bytes(total);
     void *scratch = vg_dmalloc(sb);
@@ -216,7 +217,7 @@ static void join_build(VgJoin *j) {
     vg_check_rc(rc, "join build");
     if (j->jn.kind == JOIN_FULL) {
         size_t mb = (size_t)((total + 31) / 32) * 4 + 8;
-        j->d_matched = (uint32_t *)vg_dmalloc(mb);
+        j->d_matched = (uint32_t *)vg_dmalloc_kept(mb);
         vg_dmemset(j->d_matched, 0, mb);
     }
     j->built = 1;
@@ -342,7 +343,7 @@ static VecBatch *probe_one(VgJoin *j) {
 
 static VecBatch *finalize_one(VgJoin *j) {
     if (!j->d_unmatched) {
-        j->d_unmatched = (int32_t *)vg_dmalloc((size_t)(j->n_build > 0 ? j->n_build : 1) * 4);
+        j->d_unmatched = (int32_t *)vg_dmalloc_kept((size_t)(j->n_build > 0 ? j->n_build : 1) * 4);
         size_t sb = vgk_join_probe_scratch_bytes(j->n_build);
         void *scratch = vg_dmalloc(sb);
         int rc = vgk_join_unmatched_build(j->d_matched, j->n_build, j->d_unmatched, &j->n_unmatched, scratch, sb,
@@ -394,7 +395,7 @@ static VecBatch *finalize_one(VgJoin *j) {
     return out;
 }
 
-static VecBatch *join_next(VecNode *self) {
+static VecBatch *join_next_body(VecNode *self) {
     VgJoin *j = (VgJoin *)self;
     if (j->state == 0) { join_build(j); j->state = 1; }
     if (j->state == 1) {
@@ -408,6 +409,14 @@ static VecBatch *join_next(VecNode *self) {
         j->state = 3;
     }
     return NULL;
+}
+
+/* one node API call: its temporary device memory is released if it fails */
+static VecBatch *join_next(VecNode *self) {
+    vg_scope_enter();
+    VecBatch *b = join_next_body(self);
+    vg_scope_leave();
+    return b;
 }
 
 static void join_free(VecNode *self) {

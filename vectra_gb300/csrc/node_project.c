@@ -73,7 +73,7 @@ static int map_compact(void *ctx, const char *name, int *type) {
     return c->n++;
 }
 
-static VecBatch *project_next(VecNode *self) {
+static VecBatch *project_next_body(VecNode *self) {
     VgProject *p = (VgProject *)self;
     const VecSchema *cs = &p->pn.child->output_schema;
     int nc = cs->n_cols, ne = p->pn.n_entries;
@@ -152,6 +152,14 @@ static VecBatch *project_next(VecNode *self) {
     vg_dbatch_release(&db);
     free(w.names); free(w.cols); free(w.need);
     return out;
+}
+
+/* one node API call: its temporary device memory is released if it fails */
+static VecBatch *project_next(VecNode *self) {
+    vg_scope_enter();
+    VecBatch *b = project_next_body(self);
+    vg_scope_leave();
+    return b;
 }
 
 static void project_free(VecNode *self) {

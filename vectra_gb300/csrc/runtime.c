@@ -55,12 +55,15 @@ void vg_set_error(const char *fmt, ...) {
 
 static void sync_before_error(void);
 
+static void release_scope(void);
+
 void vg_fail(const char *fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
     vsnprintf(g_msg, sizeof(g_msg), fmt, ap);
     va_end(ap);
     sync_before_error();
+    release_scope();
     vectra_error("%s", g_msg);
     abort();   /* vectra_error does not return */
 }
@@ -166,16 +169,131 @@ int vgpu_synchronize(void) {
     return cudaStreamSynchronize((cudaStream_t)vg_stream()) == cudaSuccess ? 0 : -1;
 }
 
-void *vg_dmalloc(size_t bytes) {
+/* ---- the per-call scope of temporary device memory --------------------
+ * Every device allocation made inside a node API call (next_batch of a
+ * libvgpu node, entered through vg_scope_enter / vg_scope_leave) is
+ * recorded until it is freed.  A call that fails releases what is still
+ * recorded -- after the stream has synchronised, before vectra_error -- so
+ * a failed query leaves no device memory behind; state a node keeps
+ * across calls (join tables, kept batches) is allocated with
+ * vg_dmalloc_kept and released by the node's free_node.  The reference's
+ * contract: release device and pinned memory, then raise
+ * (src/error.c:4-11). */
+static void **g_tmp = NULL;
+static size_t g_tmp_n = 0, g_tmp_cap = 0;
+static int g_scope_depth = 0;
+static long g_alloc_seq = 0;          /* device allocations so far (fault injection) */
+static long g_fail_at = -1;           /* VGPU_FAIL_ALLOC: the allocation that fails */
+
+void vg_scope_enter(void) { g_scope_depth++; }
+
+void vg_scope_leave(void) {
+    if (--g_scope_depth <= 0) {
+        g_scope_depth = 0;
+        g_tmp_n = 0;
+    }
+}
+
+static void tmp_add(void *p) {
+    if (g_scope_depth <= 0 || !p) return;
+    if (g_tmp_n == g_tmp_cap) {
+        size_t nc = g_tmp_cap ? 2 * g_tmp_cap : 64;
+        void **q = (void **)realloc(g_tmp, nc * sizeof(void *));
+        if (!q) return;   /* not recorded: at worst not released on an error */
+        g_tmp = q;
+        g_tmp_cap = nc;
+    }
+    g_tmp[g_tmp_n++] = p;
+}
+
+static void tmp_remove(void *p) {
+    for (size_t i = g_tmp_n; i-- > 0;) {
+        if (g_tmp[i] == p) {
+            g_tmp[i] = g_tmp[--g_tmp_n];
+            return;
+        }
+    }
+}
+
+/* after the stream has synchronised: the failed call's temporaries */
+static void release_scope(void) {
+    if (g_inited)
+        for (size_t i = 0; i < g_tmp_n; i++) cudaFreeAsync(g_tmp[i], g_use_user ? g_user_stream : g_own_stream);
+    g_tmp_n = 0;
+    g_scope_depth = 0;
+}
+
+static void *dmalloc_raw(size_t bytes) {
     void *p = NULL;
     if (bytes == 0) bytes = 256;
-    cudaError_t e = cudaMallocAsync(&p, bytes, (cudaStream_t)vg_stream());
+    if (g_fail_at == -1) {
+        const char *e = getenv("VGPU_FAIL_ALLOC");
+        g_fail_at = e ? atol(e) : 0;
+    }
+    cudaError_t e = (g_fail_at > 0 && ++g_alloc_seq == g_fail_at)
+                        ? cudaErrorMemoryAllocation
+                        : cudaMallocAsync(&p, bytes, (cudaStream_t)vg_stream());
     if (e != cudaSuccess) vg_fail("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
     return p;
 }
 
+void *vg_dmalloc(size_t bytes) {
+    void *p = dmalloc_raw(bytes);
+    tmp_add(p);
+    return p;
+}
+
+void *vg_dmalloc_kept(size_t bytes) { return dmalloc_raw(bytes); }
+
+void vg_dkeep(void *p) {
+    if (p) tmp_remove(p);
+}
+
 void vg_dfree(void *p) {
-    if (p) cudaFreeAsync(p, (cudaStream_t)vg_stream());
+    if (!p) return;
+    tmp_remove(p);
+    cudaFreeAsync(p, (cudaStream_t)vg_stream());
+}
+
+/* Fault injection for tests: the n-th device allocation from now fails
+ * (0: none). */
+void vgpu_debug_fail_alloc(long n) {
+    g_alloc_seq = 0;
+    g_fail_at = n > 0 ? n : 0;
+}
+
+int vgk_wait_selftest(long long limit, uint32_t *code, vg_stream_t s);
+
+/* The device's bounded wait run out on purpose: a kernel polls, through the
+ * group table's own wait, a word that nothing changes, for `limit` polls;
+ * the expired wait comes back as an error (-1, vgpu_last_error), the device
+ * stays usable.  0 would mean the wait ended, which it cannot. */
+int vgpu_wait_selftest(long long limit) {
+    vg_ensure_init();
+    uint32_t code = 0;
+    if (vgk_wait_selftest(limit, &code, vg_stream()) != 0) {
+        vg_set_error("wait self-test: %s", vgk_agg_last_error());
+        return -1;
+    }
+    if (code & VG_ERR_WAIT) {
+        vg_set_error("a bounded wait on the device expired after %lld polls (error code %u)", limit, code);
+        return -1;
+    }
+    return 0;
+}
+
+/* Bytes the device's default memory pool has handed out and not taken
+ * back (the pool libvgpu allocates from), or -1. */
+long long vgpu_device_bytes_in_use(void) {
+    int dev = 0;
+    cudaMemPool_t pool;
+    unsigned long long v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess ||
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &v) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return (long long)v;
 }
 
 void vg_h2d(void *dst, const void *src, size_t bytes) {

@@ -22,8 +22,14 @@ void vg_check_rc(int rc, const char *what);
 void vg_ensure_init(void);
 vg_stream_t vg_stream(void);
 vg_stream_t vg_stream_noinit(void);
-void *vg_dmalloc(size_t bytes);          /* stream-ordered, fails loudly */
+void *vg_dmalloc(size_t bytes);          /* stream-ordered, fails loudly; a temporary of the current call */
+void *vg_dmalloc_kept(size_t bytes);     /* the same, for state a node keeps across calls */
+void vg_dkeep(void *p);                  /* a temporary becomes state a node keeps */
 void vg_dfree(void *p);
+/* The node API call scope: temporaries still allocated when a call fails
+ * are released before the error is raised. */
+void vg_scope_enter(void);
+void vg_scope_leave(void);
 void vg_h2d(void *dst, const void *src, size_t bytes);
 void vg_d2h(void *dst, const void *src, size_t bytes);
 void vg_dmemset(void *dst, int v, size_t bytes);
