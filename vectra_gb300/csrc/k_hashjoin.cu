@@ -96,11 +96,12 @@ struct PayArgs {
     ulonglong2 *payrow;      // pass 1: each build row's would-be compact entry, in row order (or NULL)
 };
 
-// Whether the payload fits VgJPay16 entries (decided on the host from the
-// statistics of pass 1): one column, or two of which `narrow` is a bool
+// Whether the payload fits VgJPay16 entries (decided from the statistics of
+// pass 1, the same way on the device and on the host): one column, or two of which `narrow` is a bool
 // column or an int64 column whose valid values span less than 2^32 (none
 // valid: stored as 0).  *mn: the narrowed column's minimum.
-inline bool pay16_fits(int n_cols, int narrow, int narrow_type, const long long *mm, long long *mn) {
+__host__ __device__ inline bool pay16_fits(int n_cols, int narrow, int narrow_type, const long long *mm,
+                                           long long *mn) {
     *mn = 0;
     if (n_cols == 1) return true;
     if (n_cols != 2 || narrow < 0) return false;
@@ -138,7 +139,7 @@ __global__ void jt_init_kernel(VgJoinTable jt, uint32_t *counters, VgJPay *pay, 
             jt.count[i] = 0;
         }
     }
-    if (blockIdx.x == 0 && threadIdx.x < 4) counters[threadIdx.x] = 0;
+    if (blockIdx.x == 0 && threadIdx.x < 8) counters[threadIdx.x] = 0;
 }
 
 // single key: claim a slot with one CAS on its key word (direct tables:
@@ -304,15 +305,15 @@ __global__ void jt_insert_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, in
 // Direct tables with a payload copy, built without random writes to the
 // large tables.  Pass 1: every build row records itself in rowof[key - min]
 // (4 bytes per key: small enough to stay in L2) with the validity bits of
-// its two payload values in bits 29 and 30, reports a key that repeats (an
-// exchange that finds another row), and reports min, max and count of the
-// valid values of int64 payload columns (mm, 3 words per column); for a
-// payload that may take compact entries it also writes each row's would-be
-// entry in row order.  Pass 2, once the host has read those statistics:
-// compact entries are gathered by slot (coalesced writes,
-// jt_pay16_gather_kernel); otherwise each recorded row writes its key's full
-// entry (reading its payload values in row order) and the entries of keys
-// no row has are cleared last.
+// its two payload values in bits 29 and 30, counts the rows it recorded, and
+// reports min, max and count of the valid values of int64 payload columns
+// (mm, 3 words per column); for a payload that may take compact entries it
+// also writes each row's would-be entry in row order.  Pass 2 counts the
+// slots some row holds (fewer than rows recorded: a key repeats) and, if
+// the payload fits compact entries, gathers them by slot (coalesced writes,
+// jt_pay16_gather_kernel).  Otherwise, once the host has read the counts,
+// each recorded row writes its key's full entry (reading its payload values
+// in row order) and the entries of keys no row has are cleared last.
 //
 // Each thread takes kBuildU rows per step (blockDim apart, so every load
 // stays coalesced) and issues all their loads before it uses any: a row's
@@ -348,6 +349,7 @@ __global__ void jt_rows_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int3
     long long lo[2] = {0x7FFFFFFFFFFFFFFFll, 0x7FFFFFFFFFFFFFFFll};
     long long hi[2] = {(long long)0x8000000000000000ull, (long long)0x8000000000000000ull};
     unsigned long long cnt[2] = {0, 0};
+    unsigned long long recorded = 0;
     const int64_t step = (int64_t)gridDim.x * blockDim.x * kBuildU;
     for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x * kBuildU; b0 < n; b0 += step) {
         uint64_t kb[kBuildU], pb[2][kBuildU];
@@ -384,10 +386,12 @@ __global__ void jt_rows_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int3
             uint32_t vb = 0;                           // validity of the payload values
             if (P.n_cols > 0 && valid_bit(P.c0, r, pv[0][u])) vb |= 1u;
             if (P.n_cols > 1 && valid_bit(P.c1, r, pv[1][u])) vb |= 2u;
-            // a repeated key finds another row here: reported (the payload
-            // copy then does not apply)
-            if (d >= 0 && atomicExch(rowof + d, (uint32_t)r | (vb << kRowBits)) != 0xFFFFFFFFu)
-                atomicOr(counters + 3, 1u);
+            // rows with a key in range record themselves (counted: fewer
+            // keys present than rows recorded means a key repeats)
+            if (d >= 0) {
+                rowof[d] = (uint32_t)r | (vb << kRowBits);
+                recorded++;
+            }
             rslot[r] = (int32_t)d;
             if (P.payrow) {
                 // the kept column whole, the narrowed one's low 32 bits (its
@@ -431,6 +435,8 @@ __global__ void jt_rows_direct_kernel(VgJoinTable jt, KeyArgs K, int64_t n, int3
             atomicAdd(s_cnt + c, cnt[c]);
         }
     }
+    for (int o = 16; o > 0; o >>= 1) recorded += __shfl_xor_sync(0xFFFFFFFFu, recorded, o);
+    if ((threadIdx.x & 31) == 0 && recorded) atomicAdd((unsigned long long *)(counters + 4), recorded);
     __syncthreads();
     if (threadIdx.x < 2 && threadIdx.x < P.n_cols && s_cnt[threadIdx.x]) {
         const int c = threadIdx.x;
@@ -503,11 +509,19 @@ __global__ void jt_pay_absent_kernel(VgJoinTable jt, const uint32_t *rowof, PayA
 // Compact entries by slot (coalesced writes): slot d takes the row its key
 // recorded in pass 1 and that row's would-be entry, with the narrowed
 // column rebased on its minimum; slots no row has are cleared.
+// Also counts the slots some row recorded (counters[6]); with a payload
+// that does not fit compact entries (statistics of pass 1) it only counts.
 __global__ void jt_pay16_gather_kernel(VgJoinTable jt, const uint32_t *rowof, const ulonglong2 *payrow, int n_cols,
-                                       long long nmin, VgJPay16 *pay) {
+                                       int narrow, int narrow_type, const long long *mm, VgJPay16 *pay,
+                                       uint32_t *counters) {
+    long long nmin = 0;
+    const bool fits = payrow && pay16_fits(n_cols, narrow, narrow_type, mm, &nmin);
+    unsigned long long present = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d <= jt.cap; d += stride) {
         const uint32_t v = d < jt.cap ? __ldg(rowof + d) : 0xFFFFFFFFu;
+        present += v != 0xFFFFFFFFu;
+        if (!fits) continue;
         ulonglong2 e = make_ulonglong2(0ull, 0ull);
         if (v != 0xFFFFFFFFu) {
             const ulonglong2 q = __ldg(payrow + (v & kRowMask));
@@ -517,6 +531,8 @@ __global__ void jt_pay16_gather_kernel(VgJoinTable jt, const uint32_t *rowof, co
         }
         *((ulonglong2 *)pay + d) = e;
     }
+    for (int o = 16; o > 0; o >>= 1) present += __shfl_xor_sync(0xFFFFFFFFu, present, o);
+    if ((threadIdx.x & 31) == 0 && present) atomicAdd((unsigned long long *)(counters + 6), present);
 }
 
 // The slot table of a unique-key direct table from its payload copy, for
@@ -775,18 +791,24 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         vg_launch_counter++;
         if (check(cudaMemsetAsync(rowof, 0xFF, (size_t)jt->cap * 4, st), "join build")) return -1;
         vg_prof_begin(VG_PROF_JOIN_BUILD, st);
+        const int ntype = P.narrow == 1 ? P.c1.type : P.c0.type;
         if (n_build > 0) {
             const int gb = grid_for((n_build + kBuildU - 1) / kBuildU, 256);
             jt_rows_direct_kernel<<<gb, 256, 0, st>>>(*jt, K, n_build, rslot, counters, P, rowof, mm);
             vg_launch_counter++;
         }
+        // compact entries gathered by slot if the payload fits them (decided
+        // on the device), and the slots present counted either way
+        jt_pay16_gather_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, rowof, P.payrow, P.n_cols, P.narrow,
+                                                                            ntype, mm, (VgJPay16 *)P.pay, counters);
+        vg_launch_counter++;
         vg_prof_end(VG_PROF_JOIN_BUILD, st);
         // counters and the payload min / max words are adjacent (256 bytes
         // apart): one read-back
         long long hbuf[32 + 6];
         if (check(cudaMemcpyAsync(hbuf, counters, 256 + 48, cudaMemcpyDeviceToHost, st), "join build")) return -1;
         if (check(cudaStreamSynchronize(st), "join build")) return -1;
-        uint32_t hc[4];
+        uint32_t hc[8];
         memcpy(hc, hbuf, sizeof(hc));
         const long long *hm = hbuf + 32;
         if (hc[2]) {
@@ -795,19 +817,19 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
         }
         if (h_pay_mm)
             for (int i = 0; i < 6; i++) h_pay_mm[i] = hm[i];
+        unsigned long long recorded = 0, present = 0;
+        memcpy(&recorded, hc + 4, 8);
+        memcpy(&present, hc + 6, 8);
+        const bool repeated = present < recorded;
         long long nmin = 0;
-        const bool fits16 = cand16 && !hc[3] &&
-                            pay16_fits(P.n_cols, P.narrow, P.narrow == 1 ? P.c1.type : P.c0.type, hm, &nmin);
-        if (!hc[3]) {
-            vg_prof_begin(VG_PROF_JOIN_BUILD, st);
+        const bool fits16 = cand16 && pay16_fits(P.n_cols, P.narrow, ntype, hm, &nmin);
+        if (!repeated) {
             if (fits16) {
-                jt_pay16_gather_kernel<<<grid_for(jt->cap + 1, 256), 256, 0, st>>>(*jt, rowof, P.payrow, P.n_cols,
-                                                                                    nmin, (VgJPay16 *)P.pay);
-                vg_launch_counter++;
                 *h_pay_layout = P.n_cols == 1 ? -1 : P.narrow;
                 if (h_pay_min) *h_pay_min = nmin;
             } else {
                 // full entries: each recorded row writes its key's entry
+                vg_prof_begin(VG_PROF_JOIN_BUILD, st);
                 if (n_build > 0) {
                     const int gb = grid_for((n_build + kBuildU - 1) / kBuildU, 256);
                     jt_pay_scatter_kernel<<<gb, 256, 0, st>>>(*jt, rowof, rslot, n_build, P, counters);
@@ -815,8 +837,8 @@ int vgk_join_build(VgJoinTable *jt, const VgCol *keys, int n_keys, const int32_t
                 }
                 jt_pay_absent_kernel<<<grid_for((jt->cap + kBuildU) / kBuildU, 256), 256, 0, st>>>(*jt, rowof, P);
                 vg_launch_counter++;
+                vg_prof_end(VG_PROF_JOIN_BUILD, st);
             }
-            vg_prof_end(VG_PROF_JOIN_BUILD, st);
             if (check(cudaGetLastError(), "join build")) return -1;
             *h_distinct = -1;      // not counted on this path
             *h_maxdup = 1;
