@@ -236,6 +236,31 @@ typedef struct {
 } ProjectNode;
 #endif
 
+#ifndef VECTRA_SORT_H
+#define VECTRA_SORT_H
+/* src/sort.h:6-26: read by the optimizer, which re-points col_index after
+ * pruning the child (src/optimize.c:141-178). */
+typedef struct {
+    int   col_index;
+    int   descending;   /* 1 = DESC, 0 = ASC */
+} SortKey;
+
+typedef struct {
+    VecNode   base;
+    VecNode  *child;
+    int       n_keys;
+    SortKey  *keys;
+    int       phase;
+    int64_t   mem_budget;
+    char     *temp_dir;
+    int       n_runs;
+    int       runs_cap;
+    char    **run_paths;
+    VecBatch *mem_result;
+    void     *merge;
+} SortNode;
+#endif
+
 #ifndef __CUDACC_RTC__   /* host-only: the file handle holds a FILE * */
 #ifndef VECTRA_VTR1_H
 #define VECTRA_VTR1_H

@@ -68,6 +68,16 @@ JoinNode *join_node_create(VecNode *left, VecNode *right, JoinKind kind,
  * columns. */
 ScanNode *scan_node_create(const char *path, int *col_indices, int n_selected);
 
+/* replaces src/sort.h:31-32 (SortNode *sort_node_create): arrange() on the
+ * GPU.  The node keeps the reference's SortNode prefix and kind, reads its
+ * keys (col_index, descending) only when it runs, and returns every row of
+ * the child stably sorted -- NA last ascending, first descending, ties in
+ * input order (src/sort.c:32-116) -- as one batch (an empty one for no
+ * rows), then NULL.  temp_dir is kept for the struct's sake: nothing is
+ * spilled, the rows stay in device memory.  String columns are an error.
+ * Takes ownership of keys. */
+SortNode *sort_node_create(VecNode *child, int n_keys, SortKey *keys, const char *temp_dir);
+
 /* ---- data sources (no reference counterpart beyond ScanNode's role) -- */
 
 #define VGPU_SRC_COPY    0   /* copy the host columns at creation          */
@@ -166,6 +176,7 @@ GroupAggNode *vgpu_guard_group_agg(VecNode *child, int n_keys, char **key_names,
                                    int n_aggs, AggSpec *specs,
                                    const char *temp_dir);
 ScanNode     *vgpu_guard_scan(const char *path, int *col_indices, int n_selected);
+SortNode     *vgpu_guard_sort(VecNode *child, int n_keys, SortKey *keys, const char *temp_dir);
 JoinNode     *vgpu_guard_join(VecNode *left, VecNode *right, JoinKind kind,
                               int n_keys, JoinKey *keys, const char *suffix_x,
                               const char *suffix_y);

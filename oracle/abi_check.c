@@ -20,6 +20,7 @@
 #include "project.h"
 #include "vtr1.h"
 #include "scan.h"
+#include "sort.h"
 typedef JoinNode JoinPrefixT;
 #else
 #include "vectra_abi.h"
@@ -64,6 +65,10 @@ int main(void) {
     S(Vtr1File); O(Vtr1File, fp); O(Vtr1File, header); O(Vtr1File, rowgroups);
     S(ScanNode); O(ScanNode, file); O(ScanNode, col_mask); O(ScanNode, next_rg);
     O(ScanNode, predicate); O(ScanNode, pred_borrowed);
+    S(SortKey); O(SortKey, col_index); O(SortKey, descending);
+    S(SortNode); O(SortNode, child); O(SortNode, n_keys); O(SortNode, keys); O(SortNode, phase);
+    O(SortNode, mem_budget); O(SortNode, temp_dir); O(SortNode, n_runs); O(SortNode, runs_cap);
+    O(SortNode, run_paths); O(SortNode, mem_result); O(SortNode, merge);
     printf("enum VEC_STRING %d EXPR_GREPL %d AGG_MAX %d JOIN_ANTI %d\n",
            (int)VEC_STRING, (int)EXPR_GREPL, (int)AGG_MAX, (int)JOIN_ANTI);
     return 0;

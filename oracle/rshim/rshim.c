@@ -24,6 +24,7 @@
 #include "join.h"
 #include "project.h"
 #include "scan.h"
+#include "sort.h"
 
 static jmp_buf *g_jmp = NULL;
 static char g_msg[1024];
@@ -85,6 +86,13 @@ JoinNode *vref_guard_join(VecNode *l, VecNode *r, JoinKind kind, int n_keys,
     JoinNode *j = join_node_create(l, r, kind, n_keys, keys, sx, sy);
     GUARD_END
     return j;
+}
+
+SortNode *vref_guard_sort(VecNode *child, int n_keys, SortKey *keys, const char *temp_dir) {
+    GUARD_BEGIN
+    SortNode *r = sort_node_create(child, n_keys, keys, temp_dir);
+    GUARD_END
+    return r;
 }
 
 ScanNode *vref_guard_scan(const char *path, int *col_indices, int n_selected) {

@@ -1400,6 +1400,136 @@ VecNode *orc_group_agg_node_create(VecNode *child, int n_keys, char **key_names,
 }
 
 /* ------------------------------------------------------------------ */
+/* sort node (src/sort.c, the in-memory path)                           */
+/* ------------------------------------------------------------------ */
+
+/* compare_value (src/sort.c:32-71): NA last ascending, first descending
+ * (its sign is not flipped), values compared by < and >, so NaN is equal to
+ * everything and -0 to +0; descending flips the value comparison. */
+static int sort_cmp_value(const VecArray *a, int64_t ra, int64_t rb, int desc) {
+    int va = is_valid(a, ra), vb = is_valid(a, rb);
+    if (!va && !vb) return 0;
+    if (!va) return desc ? -1 : 1;
+    if (!vb) return desc ? 1 : -1;
+    int c = 0;
+    switch (a->type) {
+    case VEC_DOUBLE: {
+        double x = a->buf.dbl[ra], y = a->buf.dbl[rb];
+        c = x < y ? -1 : x > y ? 1 : 0;
+        break;
+    }
+    case VEC_INT64: {
+        int64_t x = a->buf.i64[ra], y = a->buf.i64[rb];
+        c = x < y ? -1 : x > y ? 1 : 0;
+        break;
+    }
+    case VEC_BOOL: c = (int)a->buf.bln[ra] - (int)a->buf.bln[rb]; break;
+    case VEC_STRING: {
+        int64_t sa = a->buf.str.offsets[ra], la = a->buf.str.offsets[ra + 1] - sa;
+        int64_t sb = a->buf.str.offsets[rb], lb = a->buf.str.offsets[rb + 1] - sb;
+        c = memcmp(a->buf.str.data + sa, a->buf.str.data + sb, (size_t)(la < lb ? la : lb));
+        if (c == 0) c = la < lb ? -1 : la > lb ? 1 : 0;
+        break;
+    }
+    }
+    return desc ? -c : c;
+}
+
+typedef struct { VecArray *cols; const SortKey *keys; int nk; } OSortCtx;
+
+static int sort_cmp_rows(const OSortCtx *c, int64_t x, int64_t y) {
+    for (int k = 0; k < c->nk; k++) {
+        int r = sort_cmp_value(&c->cols[c->keys[k].col_index], x, y, c->keys[k].descending);
+        if (r) return r;
+    }
+    return 0;
+}
+
+/* stable top-down merge sort (src/sort.c:97-116) */
+static void sort_msort(int64_t *idx, int64_t *tmp, int64_t n, const OSortCtx *c) {
+    if (n <= 1) return;
+    int64_t m = n / 2;
+    sort_msort(idx, tmp, m, c);
+    sort_msort(idx + m, tmp, n - m, c);
+    int64_t i = 0, j = m, k = 0;
+    while (i < m && j < n) tmp[k++] = sort_cmp_rows(c, idx[i], idx[j]) <= 0 ? idx[i++] : idx[j++];
+    while (i < m) tmp[k++] = idx[i++];
+    while (j < n) tmp[k++] = idx[j++];
+    memcpy(idx, tmp, (size_t)n * 8);
+}
+
+typedef struct {
+    SortNode sn;              /* the reference's prefix */
+} OSort;
+
+/* every logical row of the child, then one stably sorted batch (an empty
+ * input gives one batch of no rows, src/sort.c:488-504) */
+static VecBatch *sort_next(VecNode *self) {
+    OSort *o = (OSort *)self;
+    if (o->sn.phase) return NULL;
+    o->sn.phase = 1;
+    const VecSchema *cs = &o->sn.base.output_schema;
+    int nc = cs->n_cols;
+    Bld *all = (Bld *)xcalloc((size_t)(nc ? nc : 1), sizeof(Bld));
+    for (int c = 0; c < nc; c++) all[c] = bld_init(cs->col_types[c]);
+    VecBatch *b;
+    while ((b = o->sn.child->next_batch(o->sn.child)) != NULL) {
+        int64_t nl = logical_rows(b);
+        for (int c = 0; c < nc; c++) bld_reserve(&all[c], nl);
+        for (int64_t li = 0; li < nl; li++) {
+            int64_t r = phys_row(b, li);
+            for (int c = 0; c < nc; c++) bld_append_one(&all[c], &b->columns[c], r);
+        }
+        orc_batch_free(b);
+    }
+    int64_t n = nc ? all[0].len : 0;
+    VecArray *cols = (VecArray *)xcalloc((size_t)(nc ? nc : 1), sizeof(VecArray));
+    for (int c = 0; c < nc; c++) cols[c] = bld_finish(&all[c]);
+    free(all);
+    int64_t *idx = (int64_t *)xmalloc((size_t)(n ? n : 1) * 8), *tmp = (int64_t *)xmalloc((size_t)(n ? n : 1) * 8);
+    for (int64_t i = 0; i < n; i++) idx[i] = i;
+    OSortCtx sc = {cols, o->sn.keys, o->sn.n_keys};
+    sort_msort(idx, tmp, n, &sc);
+    free(tmp);
+    VecBatch *res = batch_alloc(nc, n);
+    for (int c = 0; c < nc; c++) {
+        Bld ob = bld_init(cs->col_types[c]);
+        bld_reserve(&ob, n);
+        for (int64_t i = 0; i < n; i++) bld_append_one(&ob, &cols[c], idx[i]);
+        res->columns[c] = bld_finish(&ob);
+        res->col_names[c] = xstrdup(cs->col_names[c]);
+        arr_free(&cols[c]);
+    }
+    free(cols);
+    free(idx);
+    return res;
+}
+
+static void sort_free(VecNode *self) {
+    OSort *o = (OSort *)self;
+    o->sn.child->free_node(o->sn.child);
+    free(o->sn.keys);
+    free(o->sn.temp_dir);
+    schema_free(&self->output_schema);
+    free(o);
+}
+
+VecNode *orc_sort_node_create(VecNode *child, int n_keys, SortKey *keys, const char *temp_dir) {
+    OSort *o = (OSort *)xcalloc(1, sizeof(OSort));
+    o->sn.child = child;
+    o->sn.n_keys = n_keys;
+    o->sn.keys = keys;
+    o->sn.mem_budget = 1024LL * 1024 * 1024;
+    o->sn.temp_dir = temp_dir ? xstrdup(temp_dir) : NULL;
+    const VecSchema *cs = &child->output_schema;
+    o->sn.base.output_schema = schema_make(cs->n_cols, cs->col_names, cs->col_types);
+    o->sn.base.next_batch = sort_next;
+    o->sn.base.free_node = sort_free;
+    o->sn.base.kind = "SortNode";
+    return &o->sn.base;
+}
+
+/* ------------------------------------------------------------------ */
 /* hash join (src/join.c)                                              */
 /* ------------------------------------------------------------------ */
 
@@ -1768,6 +1898,12 @@ VecNode *orc_guard_group_agg(VecNode *child, int n_keys, char **key_names,
                              int n_aggs, AggSpec *specs, const char *temp_dir) {
     GUARD_BEGIN
     VecNode *r = orc_group_agg_node_create(child, n_keys, key_names, n_aggs, specs, temp_dir);
+    GUARD_END
+    return r;
+}
+VecNode *orc_guard_sort(VecNode *child, int n_keys, SortKey *keys, const char *temp_dir) {
+    GUARD_BEGIN
+    VecNode *r = orc_sort_node_create(child, n_keys, keys, temp_dir);
     GUARD_END
     return r;
 }

@@ -53,6 +53,10 @@ VecNode *orc_project_node_create(VecNode *child, int n_entries,
 VecNode *orc_group_agg_node_create(VecNode *child, int n_keys,
                                    char **key_names, int n_aggs,
                                    AggSpec *agg_specs, const char *temp_dir);
+/* arrange(): every logical row, stably sorted by the keys, as one batch
+ * (the in-memory path of src/sort.c). */
+VecNode *orc_sort_node_create(VecNode *child, int n_keys, SortKey *keys, const char *temp_dir);
+VecNode *orc_guard_sort(VecNode *child, int n_keys, SortKey *keys, const char *temp_dir);
 VecNode *orc_join_node_create(VecNode *left, VecNode *right, JoinKind kind,
                               int n_keys, JoinKey *keys,
                               const char *suffix_x, const char *suffix_y);

@@ -410,3 +410,58 @@ def vtr_weather_table():
     city = [c if ok else "" for c, ok in zip(city, cv)]
     return {"station": station, "temperature": (temp, tv), "year": year, "flag": (flag, fv),
             "city": (city, cv)}
+
+
+# --- arrange (SortNode, src/sort.c; tests/testthat/test-verbs.R:174-222) ---
+
+def s_ascending(E):          # test-verbs.R:176-183
+    return tbl(E, T(x=[3.0, 1.0, 2.0])).arrange("x").batches()
+
+
+def s_descending(E):         # test-verbs.R:185-192
+    return tbl(E, T(x=[3.0, 1.0, 2.0])).arrange(("x", True)).batches()
+
+
+def s_multi(E):              # test-verbs.R:194-203 (the grouping key as int64)
+    return tbl(E, T(g=[1, 2, 1, 2], x=[2.0, 1.0, 1.0, 2.0])).arrange("g", "x").batches()
+
+
+def s_na_last(E):            # test-verbs.R:205-213
+    return tbl(E, T(x=[2.0, None, 1.0, 3.0])).arrange("x").batches()
+
+
+def s_na_desc(E):            # NA before the values when descending (src/sort.c:38-40)
+    return tbl(E, T(x=[2.0, None, 1.0, None, 3.0], i=[1, 2, 3, 4, 5])).arrange(("x", True)).batches()
+
+
+def s_ties_stable(E):        # equal keys keep their input order (src/sort.c:97-116)
+    return tbl(E, T(k=[2, 1, 2, 1, 2, 1, None, 2], i=[1, 2, 3, 4, 5, 6, 7, 8]), batch_rows=3).arrange("k").batches()
+
+
+def s_signed_zero_bool(E):   # -0 equals +0; bool keys; int64 extremes
+    b = (np.array([True, False, False, True, False]), np.array([True, True, False, True, True]))
+    return tbl(E, T(z=[0.0, -0.0, -1.5, 0.0, -0.0], b=b,
+                    w=[-(2 ** 63), 2 ** 63 - 1, 0, -1, 1])).arrange(("b", True), "z", ("w", True)).batches()
+
+
+def s_empty(E):              # no rows: one empty batch
+    return tbl(E, T(x=[1.0, 2.0])).filter(col("x") > 5.0).arrange("x").batches()
+
+
+def s_after_filter(E):       # a selection vector below the sort
+    rng = np.random.default_rng(11)
+    n = 3000
+    t = {"k": (rng.integers(0, 40, n), rng.random(n) > 0.1), "v": (np.round(rng.normal(0, 2, n), 1), rng.random(n) > 0.1),
+         "i": np.arange(n)}
+    return tbl(E, t, batch_rows=500).filter(col("v") > -1.0).arrange(("k", True), "v").batches()
+
+
+def r_sort(E, seed, n, batch_rows):
+    rng = np.random.default_rng(seed)
+    t = {"a": (rng.integers(0, 50, n), rng.random(n) > 0.05), "b": (np.round(rng.normal(0, 3, n), 2), rng.random(n) > 0.05),
+         "c": (rng.random(n) < 0.5, rng.random(n) > 0.1), "d": rng.integers(-(2 ** 62), 2 ** 62, n), "i": np.arange(n)}
+    return tbl(E, t, batch_rows=batch_rows).arrange(("c", True), "a", ("b", True), "d").batches()
+
+
+SORT_CASES = [s_ascending, s_descending, s_multi, s_na_last, s_na_desc, s_ties_stable, s_signed_zero_bool, s_empty,
+              s_after_filter]

@@ -107,6 +107,7 @@ class OracleEngine(Engine):
         super().__init__(lib, "orc_guard_filter", "orc_guard_project", "orc_guard_group_agg",
                          "orc_guard_join", "orc_guard_next_batch", "orc_batch_free", "orc_last_error")
         self.tmp = tempfile.mkdtemp(prefix="vgpu_oracle_")
+        self.sort_fn = "orc_guard_sort"
 
     def make_source(self, table, batch_rows=None, sel_mode=0, **_):
         return make_oracle_source(table, batch_rows, sel_mode)
@@ -119,6 +120,7 @@ class RefEngine(Engine):
                          "vref_guard_join", "vref_guard_next_batch", "vec_batch_free", "vref_last_error")
         self.tmp = tempfile.mkdtemp(prefix="vgpu_ref_")
         self.scan_fn = "vref_guard_scan"
+        self.sort_fn = "vref_guard_sort"
 
     def make_source(self, table, batch_rows=None, sel_mode=0, **_):
         return make_oracle_source(table, batch_rows, sel_mode)

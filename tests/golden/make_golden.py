@@ -22,7 +22,7 @@ from engines import RefEngine  # noqa: E402
 
 
 def all_cases():
-    for f in cases.FILTER_CASES + cases.JOIN_CASES:
+    for f in cases.FILTER_CASES + cases.JOIN_CASES + cases.SORT_CASES:
         yield f.__name__, (lambda E, f=f: f(E))
     for f in cases.GROUP_CASES:
         for mode in ("sorted", "hash"):
@@ -33,6 +33,7 @@ def all_cases():
         for mode in ("sorted", "hash"):
             yield "r_group[%d,%d,%s]" % (n, batch, mode), (
                 lambda E, n=n, b=batch, m=mode: cases.r_group(E, n + 1, n, b, 1, None if m == "hash" else E.tmp))
+        yield "r_sort[%d,%d]" % (n, batch), (lambda E, n=n, b=batch: cases.r_sort(E, n + 2, n, b))
 
 
 def write_vtr_ref(path, table, batch_rows):

@@ -8,7 +8,7 @@ import pytest
 import cases
 
 
-@pytest.mark.parametrize("case", cases.FILTER_CASES + cases.JOIN_CASES, ids=lambda f: f.__name__)
+@pytest.mark.parametrize("case", cases.FILTER_CASES + cases.JOIN_CASES + cases.SORT_CASES, ids=lambda f: f.__name__)
 def test_filter_join_cases(case, oracle, ref):
     cases.same_batches(case(oracle), case(ref))
 
@@ -61,3 +61,8 @@ def test_join_chain_quirk(oracle, ref):
     finally:
         port_lib().orc_set_join_quirk(1)
     assert len(c[0]["k"][0]) == 6
+
+
+@pytest.mark.parametrize("n,batch", cases.RAGGED)
+def test_random_sort(n, batch, oracle, ref):
+    cases.same_batches(cases.r_sort(oracle, n + 2, n, batch), cases.r_sort(ref, n + 2, n, batch))

@@ -165,3 +165,8 @@ def batch_to_numpy(bp, logical=True):
             vals, valid = vals[sel], valid[sel]
         out[name] = (vals, valid)
     return out, sel
+
+
+class SortKey(C.Structure):
+    """src/sort.h:6-9"""
+    _fields_ = [("col_index", C.c_int), ("descending", C.c_int)]

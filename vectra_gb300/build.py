@@ -29,7 +29,7 @@ JIT_HEADERS = [("vg_rtc_types.h", CSRC), ("vectra_abi.h", INCLUDE), ("vgpu_inter
                ("k_common.cuh", CSRC), ("k_groupby_dev.cuh", CSRC), ("k_jit_lib.cuh", CSRC),
                ("k_jit_kernel.cuh", CSRC), ("k_jit_pagg.cuh", CSRC)]
 C_SOURCES = ["runtime.c", "compile.c", "source.c", "node_filter.c",
-             "node_project.c", "node_agg.c", "node_join.c", "noalloc.c", "scan_vtr.c"]
+             "node_project.c", "node_agg.c", "node_join.c", "noalloc.c", "scan_vtr.c", "node_sort.c"]
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -174,11 +174,125 @@ tile_scan_kernel(const int32_t *in, int64_t n, const int64_t *tile_base, int64_t
     }
 }
 
+// ---- arrange(): the permutation of a stable multi-key sort ----
+
+// The order word of a valid value (its order is the reference's value
+// comparison, src/sort.c:32-71): int64 with the sign bit flipped; a double
+// as its order-preserving bit image with -0 taken as +0 (equal, so ties
+// keep their input order); a bool's byte.  Descending: the word inverted.
+__device__ __forceinline__ uint64_t sort_word(const VgCol &c, int64_t r, int desc) {
+    uint64_t w;
+    if (c.type == VEC_BOOL) {
+        w = (uint64_t)__ldg((const uint8_t *)c.data + r);
+    } else {
+        uint64_t b = vg_load_bits(c, r);
+        if (c.type == VEC_DOUBLE) {
+            if (b == 0x8000000000000000ull) b = 0;
+            w = (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+        } else {
+            w = b ^ 0x8000000000000000ull;
+        }
+    }
+    return desc ? ~w : w;
+}
+
+// words[i] = the order word of row perm[i] (0 for NA); stats[0] |= the bits
+// in which valid words differ from the first row's, stats[1] += NA rows
+__global__ void sort_words_kernel(VgCol c, const int32_t *perm, int64_t n, int desc, uint64_t *words,
+                                  unsigned long long *stats) {
+    const int64_t r0 = __ldg(perm);
+    const uint64_t wref = vg_valid(c, r0) ? sort_word(c, r0, desc) : 0ull;
+    unsigned long long diff = 0, na = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int64_t r = __ldg(perm + i);
+        uint64_t w = 0;
+        if (vg_valid(c, r)) {
+            w = sort_word(c, r, desc);
+            diff |= w ^ wref;
+        } else {
+            na++;
+        }
+        words[i] = w;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        diff |= __shfl_xor_sync(0xFFFFFFFFu, diff, o);
+        na += __shfl_xor_sync(0xFFFFFFFFu, na, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (diff) atomicOr(stats, diff);
+        if (na) atomicAdd(stats + 1, na);
+    }
+}
+
+// NA placement of row perm[i]: ascending puts NA after every value (flag
+// 1), descending before them (flag 0 for NA), src/sort.c:38-40
+__global__ void sort_naflag_kernel(VgCol c, const int32_t *perm, int64_t n, int desc, uint64_t *flags) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const bool v = vg_valid(c, __ldg(perm + i));
+        flags[i] = desc ? (v ? 1ull : 0ull) : (v ? 0ull : 1ull);
+    }
+}
+
+__global__ void iota_kernel(int32_t *perm, int64_t n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) perm[i] = (int32_t)i;
+}
+
 }  // namespace
 
 extern "C" {
 
 const char *vgk_sort_last_error(void) { return g_err; }
+
+size_t vgk_sort_rows_scratch(int64_t n) {
+    const int64_t m = n > 0 ? n : 1;
+    return a256((size_t)m * 8) + vgk_sort_pairs_scratch(m) + 256;
+}
+
+// perm (n int32 entries) := the stable order of rows 0..n-1 by the keys
+// (cols[key_col[k]], descending desc[k]), the first key most significant:
+// least significant key first, each key a radix sort of its order words
+// over the bits in which they differ, then, if the key has NA rows, a
+// one-bit pass that moves them after (ascending) or before (descending)
+// the values.  Every pass is stable, as the reference's merge sort is
+// (src/sort.c:97-116).
+int vgk_sort_rows(const VgCol *cols, const int *key_col, const int *desc, int n_keys, int32_t *perm, int64_t n,
+                  void *scratch, size_t scratch_bytes, vg_stream_t s) {
+    cudaStream_t st = (cudaStream_t)s;
+    if (n <= 0) return 0;
+    if (scratch_bytes < vgk_sort_rows_scratch(n)) {
+        snprintf(g_err, sizeof(g_err), "sort scratch too small");
+        return -1;
+    }
+    char *p = (char *)scratch;
+    uint64_t *words = (uint64_t *)p; p += a256((size_t)n * 8);
+    void *pair_scratch = p; p += vgk_sort_pairs_scratch(n);
+    unsigned long long *stats = (unsigned long long *)p;
+    const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    iota_kernel<<<grid, 256, 0, st>>>(perm, n);
+    vg_launch_counter++;
+    for (int k = n_keys - 1; k >= 0; k--) {
+        const VgCol &c = cols[key_col[k]];
+        if (check(cudaMemsetAsync(stats, 0, 16, st), "sort")) return -1;
+        sort_words_kernel<<<grid, 256, 0, st>>>(c, perm, n, desc[k], words, stats);
+        vg_launch_counter++;
+        unsigned long long h[2];
+        if (check(cudaMemcpyAsync(h, stats, 16, cudaMemcpyDeviceToHost, st), "sort")) return -1;
+        if (check(cudaStreamSynchronize(st), "sort")) return -1;
+        int bits = 0;
+        while (bits < 64 && (h[0] >> bits)) bits++;
+        if (bits > 0 && vgk_sort_pairs(words, perm, n, bits, pair_scratch, vgk_sort_pairs_scratch(n), s) != 0)
+            return -1;
+        if (h[1] > 0) {
+            sort_naflag_kernel<<<grid, 256, 0, st>>>(c, perm, n, desc[k], words);
+            vg_launch_counter++;
+            if (vgk_sort_pairs(words, perm, n, 1, pair_scratch, vgk_sort_pairs_scratch(n), s) != 0) return -1;
+        }
+    }
+    return check(cudaGetLastError(), "sort");
+}
 
 size_t vgk_sort_pairs_scratch(int64_t n) {
     int64_t tiles = (n + kRadixTile - 1) / kRadixTile;

@@ -848,6 +848,12 @@ GroupAggNode *vgpu_guard_group_agg(VecNode *child, int n_keys, char **key_names,
     GUARD_END
     return r;
 }
+SortNode *vgpu_guard_sort(VecNode *child, int n_keys, SortKey *keys, const char *temp_dir) {
+    GUARD_BEGIN(SortNode *)
+    SortNode *r = sort_node_create(child, n_keys, keys, temp_dir);
+    GUARD_END
+    return r;
+}
 ScanNode *vgpu_guard_scan(const char *path, int *col_indices, int n_selected) {
     GUARD_BEGIN(ScanNode *)
     ScanNode *r = scan_node_create(path, col_indices, n_selected);

@@ -489,6 +489,10 @@ size_t vgk_sort_pairs_scratch(int64_t n);
 int vgk_sort_pairs(uint64_t *keys, int32_t *vals, int64_t n, int key_bits, void *scratch,
                    size_t scratch_bytes, vg_stream_t s);
 const char *vgk_sort_last_error(void);
+/* the stable order of rows 0..n-1 by several keys (arrange) into perm */
+size_t vgk_sort_rows_scratch(int64_t n);
+int vgk_sort_rows(const VgCol *cols, const int *key_col, const int *desc, int n_keys, int32_t *perm, int64_t n,
+                  void *scratch, size_t scratch_bytes, vg_stream_t s);
 size_t vgk_scan_scratch(int64_t n);
 int vgk_exclusive_scan(const int32_t *in, int64_t n, int64_t *out, int64_t *d_total, void *scratch,
                        size_t scratch_bytes, vg_stream_t s);

@@ -184,6 +184,14 @@ class Engine:
 
     # subclasses provide make_source(table, batch_rows, **opts) -> node pointer
 
+    def sort(self, node, keys, temp_dir):
+        """A sort node (arrange): keys = [(column index, descending)]."""
+        f = getattr(self.lib, self.sort_fn)
+        f.restype, f.argtypes = C.c_void_p, [C.c_void_p, C.c_int, C.c_void_p, C.c_char_p]
+        ka = c_array(abi.SortKey, [abi.SortKey(c, 1 if d else 0) for c, d in keys])
+        td = temp_dir.encode() if temp_dir is not None else None
+        return self.check(f(node, len(keys), C.cast(ka, C.c_void_p), td), "sort")
+
     def make_scan(self, path, cols=None, scan_fn=None):
         """A .vtr scan node (scan_node_create through the library's guard);
         cols: file column indices, None = all."""
@@ -263,6 +271,7 @@ class GpuEngine(Engine):
                          "vgpu_guard_join", "vgpu_guard_next_batch", "vgpu_batch_free",
                          "vgpu_last_error")
         self.scan_fn = "vgpu_guard_scan"
+        self.sort_fn = "vgpu_guard_sort"
         lib.vgpu_table_source_create.restype = C.c_void_p
         lib.vgpu_table_source_create.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                                  C.c_void_p, C.c_int64, C.c_int64, C.c_int]
@@ -339,6 +348,15 @@ class Tbl:
     def filter(self, expr):
         schema = self.schema
         return Tbl(self.engine, self.engine.filter(self._take(), expr.to_c(schema)))
+
+    def arrange(self, *keys, temp_dir="<tempdir>"):
+        """arrange(): keys are column names, or (name, True) for descending."""
+        schema = [n for n, _ in self.schema]
+        ks = []
+        for k in keys:
+            name, desc = (k, False) if isinstance(k, str) else k
+            ks.append((schema.index(name), bool(desc)))
+        return Tbl(self.engine, self.engine.sort(self._take(), ks, temp_dir))
 
     def select(self, *names):
         entries = [ProjEntry(c_strdup(n), None) for n in names]
