@@ -47,9 +47,12 @@ def test_sort_over_scan(tmp_path):
 
 
 def test_string_columns_are_an_error():
-    from vectra_gb300.plan import EngineError, tbl
+    """A child with a string column (here the oracle's own source node, as a
+    reference scan would deliver it): an explicit error, no fallback."""
+    from vectra_gb300.plan import EngineError, Tbl
     G = _gpu()
     t = cases.T(x=[2.0, 1.0])
     t["s"] = (["b", "a"], np.array([True, True]))
-    with pytest.raises(EngineError, match="string column"):
-        tbl(G, t).arrange("x").batches()
+    src = OracleEngine().make_source(t)
+    with pytest.raises(EngineError, match="string column 's'"):
+        Tbl(G, src).arrange("x").batches()
