@@ -1035,9 +1035,9 @@ def nested_workloads(args):
 
 def vtr_path_arm(args, eng, lib, fcols_host, dcols_host, want):
     """The headline query as R runs it: both tables read from .vtr files (in
-    the page cache) by scan_node_create in 100,000-row row groups, each row
-    group read into page-locked staging and copied to the device
-    asynchronously while the previous one is aggregated."""
+    the page cache) by scan_node_create in 100,000-row row groups, read
+    ahead by the scan's reader threads into page-locked staging and copied
+    to the device asynchronously while earlier groups are aggregated."""
     import tempfile
     from vectra_gb300 import vtr
     from vectra_gb300.plan import Tbl, col, scan
@@ -1076,8 +1076,8 @@ def vtr_path_arm(args, eng, lib, fcols_host, dcols_host, want):
     return {"value": (N_FACT + N_DIM) / (ms * 1e-3), "unit": "rows/s", "ms_per_step": ms,
             "file_bytes_per_step": file_bytes,
             "path": ".vtr files in the page cache (written once, %.1f s) through scan_node_create, the drop-in "
-                    "ScanNode: 100k-row groups read into page-locked staging, asynchronous copies, node C API "
-                    "above; wall clock per query" % write_s}
+                    "ScanNode: 100k-row groups read ahead by its reader threads into page-locked staging, "
+                    "asynchronous copies, node C API above; wall clock per query" % write_s}
 
 
 def main():

@@ -313,6 +313,7 @@ typedef struct {
     uint32_t *counters;       /* [0] rows, [1] cache entries */
     char *cache;
     int64_t rows_cap, cache_cap;
+    int deferred;             /* launches not yet checked (dense cache) */
 } Spill;
 
 /* The spill list is sized for a whole launch and kept between queries (the
@@ -352,8 +353,13 @@ static int run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_logi
         S->cache = (char *)vg_dmalloc(vgk_agg_cache_bytes(L, cc) + 256);
         S->cache_cap = cc;
     }
+    /* a dense cache holds every group and the table cannot outgrow its
+     * first allocation: nothing spills, so a stream of batches is checked
+     * once, after its last launch (check_deferred), and the host does not
+     * wait for each batch's kernel before pulling the next batch */
+    const int deferred = L->dense != 0;
     for (;;) {
-        vg_dmemset(S->counters, 0, 8);
+        if (!deferred || !S->deferred) vg_dmemset(S->counters, 0, 8);
         L->gt = T->gt;
         L->spill_rows = S->rows;
         L->spill_rows_n = S->counters;
@@ -364,6 +370,10 @@ static int run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_logi
         L->replay = NULL;
         L->replay_n = 0;
         vg_check_rc(vgk_agg_launch(L, vg_stream()), "group-agg");
+        if (deferred) {
+            S->deferred = 1;
+            return 0;
+        }
         /* spill counters, error word and groups used: three copies, one wait */
         uint32_t *hw = (uint32_t *)vg_pinned_scratch(16);
         vg_d2h(hw, S->counters, 8);
@@ -415,6 +425,20 @@ static int run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_logi
         if (err) vg_fail("group-agg: table still full after growing (code %u)", err);
         return 1;
     }
+}
+
+/* the status of deferred launches (dense cache): an error, or rows that
+ * left the cache (which a dense cache cannot lose), fails the call */
+static void check_deferred(Table *T, Spill *S) {
+    uint32_t *hw = (uint32_t *)vg_pinned_scratch(16);
+    vg_d2h(hw, S->counters, 8);
+    vg_d2h(hw + 2, T->gt.err, 4);
+    vg_sync();
+    S->deferred = 0;
+    const uint32_t err = hw[2];
+    if (err & (VG_ERR_WAIT | VG_ERR_PROG)) vg_fail("group-agg kernel error (code %u)", err);
+    if ((err & (VG_ERR_FULL | VG_ERR_SPILL)) || hw[0] || hw[1])
+        vg_fail("group-agg: rows left a dense group cache (%u rows, %u entries, code %u)", hw[0], hw[1], err);
 }
 
 /* results up to this size are read back in one page-locked copy */
@@ -1305,6 +1329,7 @@ static VecBatch *agg_next_body(VecNode *self) {
         stream_pos += n_logical;
         batch_idx++;
     }
+    if (S.deferred) check_deferred(&T, &S);
     const double t_emit = now_ms();
     if (!pg) g_agg_ms[2] += t_emit - t_loop;
     VecBatch *res = pg ? pagg_end(pg, A, &P, L) : emit_result(A, &P, &T);

@@ -15,17 +15,23 @@
  *    columns, as vtr1_read_rowgroup returns it (src/vtr1.c:306-392);
  *  - vg_scan_pull (libvgpu nodes): the same row group's needed columns read
  *    with pread straight into a page-locked staging block laid out like the
- *    device block, then one asynchronous copy to the device.  Two staging
- *    blocks alternate: the file read of the next row group overlaps the copy
- *    and the kernels of this one, and a block is reused only after the
- *    event recorded behind its copy has completed.
+ *    device block, then one asynchronous copy to the device.  A pool of
+ *    reader threads reads the next row groups ahead, each into a staging
+ *    block of its own (a ring of up to 32), while the caller hands the
+ *    groups that are ready to the device in file order; a block is reused
+ *    only after the event recorded behind its copy has completed.  The
+ *    readers only read the file: every CUDA call and every error report
+ *    stays on the calling thread.  VGPU_SCAN_THREADS sets the number of
+ *    readers (0: the caller reads each group itself, with two blocks).
  *
  * Row-group pruning restates predicate_might_match (src/scan.c:12-105):
  * AND / OR of `column <op> numeric literal` terms against the row group's
  * v3 min / max statistics (valid values only), anything else may match.
  */
 #define _GNU_SOURCE
+#include <errno.h>
 #include <fcntl.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -42,14 +48,38 @@ typedef struct {
     int64_t *str_len;           /* [rg * n_cols + c]: string data bytes (string columns) */
 } VgVtrFile;
 
+enum { PF_FREE = 0, PF_QUEUED, PF_READY, PF_FAILED };
+#define VG_SCAN_RING 32
+#define VG_SCAN_MAX_READERS 16
+
+/* one row group read ahead into a page-locked staging block */
+typedef struct {
+    int64_t g;                  /* row group */
+    int state;                  /* PF_*, under the pool's mutex */
+    int err;                    /* errno of a failed read (0: short file) */
+    char *h;                    /* page-locked staging block */
+    size_t cap;
+    cudaEvent_t ev;             /* recorded behind the block's copy */
+    int ev_live;
+    int copy_pending;
+} VgPre;
+
 typedef struct {
     ScanNode sn;                /* reference prefix */
     int64_t rows_out;           /* rows emitted so far (stream position) */
-    void *stage[2];             /* page-locked staging blocks */
-    size_t stage_bytes[2];
-    cudaEvent_t ev[2];          /* recorded behind each block's copy */
-    int ev_live[2];
-    int cur;
+    /* read-ahead (device path) */
+    int pf_on;
+    uint8_t *pf_need;           /* per output column: read for the device */
+    uint32_t pf_rg;             /* next row group to consider for reading ahead */
+    int n_slots, head, count;   /* ring: slots head .. head+count-1 hold groups in file order */
+    VgPre slot[VG_SCAN_RING];
+    int n_readers;
+    pthread_t th[VG_SCAN_MAX_READERS];
+    pthread_mutex_t mu;
+    pthread_cond_t cv_task, cv_done;
+    int q[VG_SCAN_RING];        /* slots waiting for a reader */
+    int q_head, q_n;
+    int stop;
 } VgScan;
 
 static VecBatch *scan_next(VecNode *self);
@@ -267,9 +297,12 @@ static int64_t next_group(VgScan *s) {
 
 /* ---- host batches (src/vtr1.c:306-392) ------------------------------- */
 
+static void reset_ahead(VgScan *s);
+
 static VecBatch *scan_next(VecNode *self) {
     VgScan *s = (VgScan *)self;
     VgVtrFile *v = (VgVtrFile *)s->sn.file;
+    if (s->pf_on) reset_ahead(s);    /* groups read ahead for the device are read again here */
     const int64_t g = next_group(s);
     if (g < 0) return NULL;
     const int64_t n = v->f.rowgroups[g].n_rows;
@@ -314,72 +347,275 @@ static VecBatch *scan_next(VecNode *self) {
 
 static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-static void *stage_block(VgScan *s, size_t bytes) {
-    const int i = s->cur;
-    if (s->ev_live[i]) {
-        cudaError_t e = cudaEventSynchronize(s->ev[i]);
-        if (e != cudaSuccess) vg_fail("scan: staging copy failed: %s", cudaGetErrorString(e));
+/* pread of n bytes at off without reporting: 0, or the errno of a failed
+ * read (-1: the file ends early) */
+static int pread_quiet(int fd, void *dst, size_t n, int64_t off) {
+    char *p = (char *)dst;
+    while (n > 0) {
+        ssize_t r = pread(fd, p, n, (off_t)off);
+        if (r < 0 && errno == EINTR) continue;
+        if (r <= 0) return r < 0 ? errno : -1;
+        p += r;
+        n -= (size_t)r;
+        off += r;
     }
-    if (s->stage_bytes[i] < bytes) {
-        if (s->stage[i]) cudaFreeHost(s->stage[i]);
-        s->stage[i] = NULL;
-        size_t want = bytes + bytes / 4;
-        if (cudaHostAlloc(&s->stage[i], want, cudaHostAllocDefault) != cudaSuccess) {
-            cudaGetLastError();
-            s->stage_bytes[i] = 0;
-            vg_fail("scan: page-locked staging block of %zu bytes could not be allocated", want);
-        }
-        s->stage_bytes[i] = want;
-    }
-    return s->stage[i];
+    return 0;
 }
 
-int vg_scan_pull(VecNode *node, const uint8_t *need, VgDBatch *out) {
-    VgScan *s = (VgScan *)node;
-    VgVtrFile *v = (VgVtrFile *)s->sn.file;
-    memset(out, 0, sizeof(*out));
-    const int64_t g = next_group(s);
-    if (g < 0) return 0;
+/* bytes of row group g's staging / device block for the needed columns:
+ * per column its data, then its validity words, each 256-byte aligned */
+static size_t group_bytes(const VgScan *s, int64_t g, const uint8_t *need) {
+    const VgVtrFile *v = (const VgVtrFile *)s->sn.file;
     const int64_t n = v->f.rowgroups[g].n_rows;
-    int n_sel = 0;
-    for (int c = 0; c < v->n_cols; c++) n_sel += s->sn.col_mask[c] != 0;
-    out->n_rows = n;
-    out->n_cols = n_sel;
-    out->row_base = s->rows_out;
-    out->cols = (VgCol *)vg_xcalloc((size_t)(n_sel ? n_sel : 1), sizeof(VgCol));
     const size_t vwords = (size_t)((n + 31) / 32) * 4;
     size_t total = 0;
     int o = 0;
     for (int c = 0; c < v->n_cols; c++) {
         if (!s->sn.col_mask[c]) continue;
         const int t = v->f.header.schema.col_types[c];
-        if (!need || need[o]) {
-            if (t == VEC_STRING)
-                vg_fail("string column '%s' is not supported by the GPU path", v->f.header.schema.col_names[c]);
-            total += a256((size_t)data_bytes(t, n)) + a256(vwords);
+        if (need[o]) total += a256((size_t)data_bytes(t, n)) + a256(vwords);
+        o++;
+    }
+    return total;
+}
+
+/* reads row group g's needed columns into h in the device block's layout;
+ * 0 or an error as pread_quiet */
+static int read_group(const VgScan *s, int64_t g, const uint8_t *need, char *h) {
+    const VgVtrFile *v = (const VgVtrFile *)s->sn.file;
+    const int64_t n = v->f.rowgroups[g].n_rows;
+    const size_t vwords = (size_t)((n + 31) / 32) * 4;
+    size_t off = 0;
+    int o = 0;
+    for (int c = 0; c < v->n_cols; c++) {
+        if (!s->sn.col_mask[c]) continue;
+        const int t = v->f.header.schema.col_types[c];
+        if (need[o]) {
+            const int64_t fo = v->valid_off[(size_t)g * v->n_cols + c];
+            const size_t db = (size_t)data_bytes(t, n);
+            int e = pread_quiet(v->fd, h + off, db, fo + vg_vbytes(n));
+            if (e) return e;
+            off += a256(db);
+            if (vg_vbytes(n) & 3)   /* the last 32-bit word's bytes past the bitmap read as 0 */
+                memset(h + off + ((size_t)vg_vbytes(n) & ~(size_t)3), 0, 4);
+            e = pread_quiet(v->fd, h + off, (size_t)vg_vbytes(n), fo);
+            if (e) return e;
+            off += a256(vwords);
         }
         o++;
     }
+    return 0;
+}
+
+static void *reader_main(void *arg) {
+    VgScan *s = (VgScan *)arg;
+    pthread_mutex_lock(&s->mu);
+    for (;;) {
+        while (!s->stop && s->q_n == 0) pthread_cond_wait(&s->cv_task, &s->mu);
+        if (s->stop) break;
+        const int i = s->q[s->q_head];
+        s->q_head = (s->q_head + 1) % VG_SCAN_RING;
+        s->q_n--;
+        VgPre *p = &s->slot[i];
+        const int64_t g = p->g;
+        char *h = p->h;
+        pthread_mutex_unlock(&s->mu);
+        const int e = read_group(s, g, s->pf_need, h);
+        pthread_mutex_lock(&s->mu);
+        p->err = e;
+        p->state = e ? PF_FAILED : PF_READY;
+        pthread_cond_broadcast(&s->cv_done);
+    }
+    pthread_mutex_unlock(&s->mu);
+    return NULL;
+}
+
+/* the next row group after pf_rg that the pushed-down predicate does not
+ * rule out (advancing pf_rg), or -1 */
+static int64_t next_ahead(VgScan *s) {
+    VgVtrFile *v = (VgVtrFile *)s->sn.file;
+    while (s->pf_rg < v->f.header.n_rowgroups) {
+        const uint32_t g = s->pf_rg++;
+        if (s->sn.predicate && v->f.header.version >= 3 &&
+            !might_match(s->sn.predicate, v->f.rowgroups[g].col_stats, &v->f.header.schema))
+            continue;
+        return g;
+    }
+    return -1;
+}
+
+/* waits for every queued read (the caller holds no lock) */
+static void drain_reads(VgScan *s) {
+    if (s->n_readers == 0) return;
+    pthread_mutex_lock(&s->mu);
+    for (int k = 0; k < s->count; k++) {
+        VgPre *p = &s->slot[(s->head + k) % s->n_slots];
+        while (p->state == PF_QUEUED) pthread_cond_wait(&s->cv_done, &s->mu);
+    }
+    pthread_mutex_unlock(&s->mu);
+}
+
+/* forgets the groups read ahead (the next pull starts from the delivered
+ * position again) */
+static void reset_ahead(VgScan *s) {
+    drain_reads(s);
+    for (int k = 0; k < s->count; k++) s->slot[(s->head + k) % s->n_slots].state = PF_FREE;
+    s->head = 0;
+    s->count = 0;
+    s->pf_rg = s->sn.next_rg;
+}
+
+static void start_readers(VgScan *s) {
+    int nr = 8;
+    const long cpus = sysconf(_SC_NPROCESSORS_ONLN);
+    if (cpus > 0 && cpus < nr) nr = (int)cpus;
+    const char *env = getenv("VGPU_SCAN_THREADS");
+    if (env) nr = atoi(env);
+    if (nr < 0) nr = 0;
+    if (nr > VG_SCAN_MAX_READERS) nr = VG_SCAN_MAX_READERS;
+    s->n_slots = nr == 0 ? 2 : (2 * nr < VG_SCAN_RING ? 2 * nr : VG_SCAN_RING);
+    if (pthread_mutex_init(&s->mu, NULL) != 0 || pthread_cond_init(&s->cv_task, NULL) != 0 ||
+        pthread_cond_init(&s->cv_done, NULL) != 0)
+        vg_fail("scan: reader pool could not be set up");
+    s->n_readers = 0;
+    for (int i = 0; i < nr; i++) {
+        if (pthread_create(&s->th[i], NULL, reader_main, s) != 0) break;
+        s->n_readers++;
+    }
+    if (nr > 0 && s->n_readers == 0) s->n_slots = 2;   /* no thread could start: read on the caller */
+}
+
+/* fills the ring with the next row groups and queues their reads */
+static void fill_ahead(VgScan *s) {
+    while (s->count < s->n_slots) {
+        const int i = (s->head + s->count) % s->n_slots;
+        VgPre *p = &s->slot[i];
+        if (p->copy_pending) {
+            /* the block's previous copy must have read it; while other
+             * groups are queued, a copy still running ends the filling
+             * instead of a wait */
+            cudaError_t e = cudaEventQuery(p->ev);
+            if (e == cudaErrorNotReady) {
+                if (s->count > 0) return;
+                e = cudaEventSynchronize(p->ev);
+            }
+            if (e != cudaSuccess) vg_fail("scan: staging copy failed: %s", cudaGetErrorString(e));
+            p->copy_pending = 0;
+        }
+        const int64_t g = next_ahead(s);
+        if (g < 0) return;
+        const size_t bytes = group_bytes(s, g, s->pf_need);
+        if (p->cap < bytes) {
+            if (p->h) cudaFreeHost(p->h);
+            p->h = NULL;
+            p->cap = 0;
+            const size_t want = bytes + bytes / 4;
+            if (cudaHostAlloc((void **)&p->h, want, cudaHostAllocDefault) != cudaSuccess) {
+                cudaGetLastError();
+                p->h = NULL;
+                s->pf_rg--;          /* this group is not taken */
+                vg_fail("scan: page-locked staging block of %zu bytes could not be allocated", want);
+            }
+            p->cap = want;
+        }
+        p->g = g;
+        p->err = 0;
+        s->count++;
+        if (s->n_readers == 0) {
+            p->state = PF_READY;     /* read when it is taken */
+            continue;
+        }
+        pthread_mutex_lock(&s->mu);
+        p->state = PF_QUEUED;
+        s->q[(s->q_head + s->q_n) % VG_SCAN_RING] = i;
+        s->q_n++;
+        pthread_cond_signal(&s->cv_task);
+        pthread_mutex_unlock(&s->mu);
+    }
+}
+
+int vg_scan_pull(VecNode *node, const uint8_t *need, VgDBatch *out) {
+    VgScan *s = (VgScan *)node;
+    VgVtrFile *v = (VgVtrFile *)s->sn.file;
+    memset(out, 0, sizeof(*out));
+    int n_sel = 0;
+    for (int c = 0; c < v->n_cols; c++) n_sel += s->sn.col_mask[c] != 0;
+    /* the columns this consumer needs (strings cannot go to the device) */
+    uint8_t *nd = (uint8_t *)vg_xcalloc((size_t)(n_sel ? n_sel : 1), 1);
+    int o = 0;
+    for (int c = 0; c < v->n_cols; c++) {
+        if (!s->sn.col_mask[c]) continue;
+        nd[o] = (uint8_t)(!need || need[o]);
+        if (nd[o] && v->f.header.schema.col_types[c] == VEC_STRING) {
+            free(nd);
+            vg_fail("string column '%s' is not supported by the GPU path", v->f.header.schema.col_names[c]);
+        }
+        o++;
+    }
+    if (!s->pf_on) {
+        start_readers(s);
+        s->pf_on = 1;
+        s->pf_need = nd;
+        s->pf_rg = s->sn.next_rg;
+    } else if (memcmp(nd, s->pf_need, (size_t)(n_sel ? n_sel : 1)) != 0) {
+        reset_ahead(s);              /* another set of columns: read again from here */
+        free(s->pf_need);
+        s->pf_need = nd;
+    } else {
+        free(nd);
+    }
+    fill_ahead(s);
+    if (s->count == 0) return 0;
+    VgPre *p = &s->slot[s->head];
+    if (s->n_readers > 0) {
+        pthread_mutex_lock(&s->mu);
+        while (p->state == PF_QUEUED) pthread_cond_wait(&s->cv_done, &s->mu);
+        pthread_mutex_unlock(&s->mu);
+    } else {
+        p->err = read_group(s, p->g, s->pf_need, p->h);
+        if (p->err) p->state = PF_FAILED;
+    }
+    const int64_t g = p->g;
+    s->head = (s->head + 1) % s->n_slots;
+    s->count--;
+    s->sn.next_rg = (uint32_t)g + 1;
+    if (p->state == PF_FAILED) {
+        const int e = p->err;
+        p->state = PF_FREE;
+        reset_ahead(s);
+        if (e > 0) vg_fail("scan: reading column data failed: %s", strerror(e));
+        vg_fail("unexpected end of file reading column data");
+    }
+    p->state = PF_FREE;
+
+    const int64_t n = v->f.rowgroups[g].n_rows;
+    out->n_rows = n;
+    out->n_cols = n_sel;
+    out->row_base = s->rows_out;
+    out->cols = (VgCol *)vg_xcalloc((size_t)(n_sel ? n_sel : 1), sizeof(VgCol));
     s->rows_out += n;
-    if (total == 0) return 1;
-    char *h = (char *)stage_block(s, total);
+    const size_t total = group_bytes(s, g, s->pf_need);
+    o = 0;
+    for (int c = 0; c < v->n_cols; c++) {
+        if (!s->sn.col_mask[c]) continue;
+        out->cols[o].type = v->f.header.schema.col_types[c];
+        o++;
+    }
+    if (total == 0) {
+        fill_ahead(s);
+        return 1;
+    }
     char *d = (char *)vg_dmalloc(total);
     out->block = d;
+    const size_t vwords = (size_t)((n + 31) / 32) * 4;
     size_t off = 0;
     o = 0;
     for (int c = 0; c < v->n_cols; c++) {
         if (!s->sn.col_mask[c]) continue;
         const int t = v->f.header.schema.col_types[c];
-        out->cols[o].type = t;
-        if (!need || need[o]) {
-            const int64_t fo = v->valid_off[(size_t)g * v->n_cols + c];
-            const size_t db = (size_t)data_bytes(t, n);
-            pread_all(v->fd, h + off, db, fo + vg_vbytes(n));
+        if (s->pf_need[o]) {
             out->cols[o].data = d + off;
-            off += a256(db);
-            if (vg_vbytes(n) & 3)   /* the last 32-bit word's bytes past the bitmap read as 0 */
-                memset(h + off + ((size_t)vg_vbytes(n) & ~(size_t)3), 0, 4);
-            pread_all(v->fd, h + off, (size_t)vg_vbytes(n), fo);
+            off += a256((size_t)data_bytes(t, n));
             out->cols[o].valid = (const uint32_t *)(d + off);
             out->cols[o].voff = 0;
             off += a256(vwords);
@@ -387,17 +623,18 @@ int vg_scan_pull(VecNode *node, const uint8_t *need, VgDBatch *out) {
         o++;
     }
     cudaStream_t st = (cudaStream_t)vg_stream();
-    cudaError_t e = cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && !s->ev_live[s->cur]) {
-        e = cudaEventCreateWithFlags(&s->ev[s->cur], cudaEventDisableTiming);
-        if (e == cudaSuccess) s->ev_live[s->cur] = 1;
+    cudaError_t e = cudaMemcpyAsync(d, p->h, total, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !p->ev_live) {
+        e = cudaEventCreateWithFlags(&p->ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) p->ev_live = 1;
     }
-    if (e == cudaSuccess) e = cudaEventRecord(s->ev[s->cur], st);
+    if (e == cudaSuccess) e = cudaEventRecord(p->ev, st);
     if (e != cudaSuccess) {
         vg_dbatch_release(out);
         vg_fail("scan: copy of a row group to the device failed: %s", cudaGetErrorString(e));
     }
-    s->cur ^= 1;
+    p->copy_pending = 1;
+    fill_ahead(s);                   /* keep the readers busy while this group is used */
     return 1;
 }
 
@@ -405,12 +642,26 @@ int vg_scan_pull(VecNode *node, const uint8_t *need, VgDBatch *out) {
 
 static void scan_free(VecNode *self) {
     VgScan *s = (VgScan *)self;
-    for (int i = 0; i < 2; i++) {
-        if (s->ev_live[i]) {
-            cudaEventSynchronize(s->ev[i]);
-            cudaEventDestroy(s->ev[i]);
+    if (s->pf_on) {
+        if (s->n_readers > 0) {
+            pthread_mutex_lock(&s->mu);
+            s->stop = 1;
+            pthread_cond_broadcast(&s->cv_task);
+            pthread_mutex_unlock(&s->mu);
+            for (int i = 0; i < s->n_readers; i++) pthread_join(s->th[i], NULL);
         }
-        if (s->stage[i]) cudaFreeHost(s->stage[i]);
+        pthread_mutex_destroy(&s->mu);
+        pthread_cond_destroy(&s->cv_task);
+        pthread_cond_destroy(&s->cv_done);
+        for (int i = 0; i < VG_SCAN_RING; i++) {
+            VgPre *p = &s->slot[i];
+            if (p->ev_live) {
+                cudaEventSynchronize(p->ev);
+                cudaEventDestroy(p->ev);
+            }
+            if (p->h) cudaFreeHost(p->h);
+        }
+        free(s->pf_need);
     }
     if (s->sn.predicate && !s->sn.pred_borrowed) vg_expr_free(s->sn.predicate);
     vtr_close((VgVtrFile *)s->sn.file);
