@@ -280,17 +280,26 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
     s += "    (void)X; (void)j; (void)k; (void)nm;\n}\n";
 
     // cache updates
-    s += "VG_DEV uint32_t vgj_cache_update(char *sm, int slot, const Rows &X, int j) {\n    uint32_t fail = 0;\n";
+    s += "VG_DEV uint32_t vgj_cache_update(char *sm, int slot, const Rows &X, int j, VgjBases &wb) {\n"
+         "    uint32_t fail = 0;\n";
     for (int a = 0; a < L.n_accs; a++) {
         const VgAccSpec &A = L.acc[a];
         const int count = (L.skip_count_mask >> a) & 1u ? 0 : 1;
         std::string v = A.cls == VG_ACC_COUNT_ALL ? std::string("InVal{0ull, true}") : value(A.in);
-        fmt(s, "    if (!cache_acc<%d, %d, %d, %lluu, %lluu, %lluu, %lluu, %lluu, %d>(sm, slot, %s)) fail |= %uu;\n",
-            A.cls, A.na_rm ? 1 : 0, count, (unsigned long long)c.cnt[a], (unsigned long long)c.val[a],
+        fmt(s, "    if (!cache_acc_k<%d, %d, %d, %d, %lluu, %lluu, %lluu, %lluu, %lluu, %d>(sm, slot, %s, wb)) "
+               "fail |= %uu;\n",
+            a, A.cls, A.na_rm ? 1 : 0, count, (unsigned long long)c.cnt[a], (unsigned long long)c.val[a],
             (unsigned long long)c.flags[a], (unsigned long long)c.base[a], (unsigned long long)c.win[a], S,
             v.c_str(), 1u << a);
     }
-    s += "    (void)sm; (void)slot; (void)X; (void)j;\n    return fail;\n}\n";
+    s += "    (void)sm; (void)slot; (void)X; (void)j; (void)wb;\n    return fail;\n}\n";
+
+    // the CTA's window bases into a live slot's base words (kernel tail)
+    s += "VG_DEV void vgj_fix_bases(char *sm, int slot) {\n";
+    for (int a = 0; a < L.n_accs; a++)
+        if (L.acc[a].cls == VG_ACC_SUM_F64)
+            fmt(s, "    ((int32_t *)(sm + %lluu))[slot] = vgj_cta_base[%d];\n", (unsigned long long)c.base[a], a);
+    s += "    (void)sm; (void)slot;\n}\n";
 
     // global-table updates of the accumulators in `which`
     s += "VG_DEV void vgj_global_update(const VgAggLaunch &L, int64_t g, const Rows &X, int j, uint32_t which) {\n";

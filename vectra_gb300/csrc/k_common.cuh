@@ -243,6 +243,17 @@ struct VgDigits32 {
     uint32_t zero;
 };
 
+// High word of (hi:lo) << s, s in [0, 31] (a funnel shift on the device).
+__host__ __device__ inline uint32_t vg_fshl32(uint32_t lo, uint32_t hi, uint32_t s) {
+#ifdef __CUDA_ARCH__
+    return __funnelshift_l(lo, hi, s);
+#else
+    return s ? (hi << s) | (lo >> (32 - s)) : hi;
+#endif
+}
+
+// Straight-line apart from the special case: the digits of a zero come out
+// as 0 at word 0 (and zero is set).
 __host__ __device__ inline VgDigits32 vg_split_double32(uint64_t bits) {
     VgDigits32 r;
     const uint32_t hi = (uint32_t)(bits >> 32), lo = (uint32_t)bits;
@@ -250,22 +261,23 @@ __host__ __device__ inline VgDigits32 vg_split_double32(uint64_t bits) {
     const uint32_t fh = hi & 0xFFFFFu;
     r.neg = hi >> 31;
     r.special = 0;
-    r.zero = 0;
-    r.word = 0;
-    r.d0 = r.d1 = r.d2 = 0;
     if (e == 0x7FFu) {
         r.special = (fh | lo) ? 4u : (r.neg ? 16u : 8u);
+        r.zero = 0;
+        r.word = 0;
+        r.d0 = r.d1 = r.d2 = 0;
         return r;
     }
-    const uint32_t mh = fh | (e ? 0x100000u : 0u);
-    if ((mh | lo) == 0) { r.zero = 1; return r; }
-    const uint32_t sh = e ? e - 1 : 0;
+    const uint32_t nz = e != 0u;
+    const uint32_t mh = fh | (nz << 20);
+    r.zero = (mh | lo) == 0u;
+    const uint32_t sh = e - nz;            // subnormals share the exponent of the smallest normals
     const uint32_t off = sh & 31u;
     r.word = (int)(sh >> 5);
     // (mh:lo) << off spread over three 32-bit digits
     r.d0 = lo << off;
-    r.d1 = off ? (mh << off) | (lo >> (32 - off)) : mh;
-    r.d2 = off ? mh >> (32 - off) : 0u;
+    r.d1 = vg_fshl32(lo, mh, off);
+    r.d2 = vg_fshl32(mh, 0u, off);
     return r;
 }
 

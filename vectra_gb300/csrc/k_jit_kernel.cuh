@@ -54,6 +54,10 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
         make_lay(L, S, cl);
         cache_used = 0;
     }
+    if (threadIdx.x < VG_MAX_ACCS) vgj_cta_base[threadIdx.x] = kBaseUnset;
+    VgjBases wb;
+#pragma unroll
+    for (int a = 0; a < VG_MAX_ACCS; a++) wb.b[a] = kBaseUnset;
     __syncthreads();
     for (int i = threadIdx.x; i < S; i += blockDim.x) init_slot(L, sm, cl, S, i);
 #if VGJ_DENSE
@@ -130,7 +134,7 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
         const int found =
             cache_find<S, VGJ_NK>(sm, VGJ_OFF_STATE, VGJ_OFF_NM, VGJ_OFF_KEYS, &cache_used, k, nm, kt, &err);
         if (err) atomicOr(L.gt.err, VG_ERR_WAIT);
-        const uint32_t fail = found < 0 ? 0u : vgj_cache_update(sm, found, Q, 0);
+        const uint32_t fail = found < 0 ? 0u : vgj_cache_update(sm, found, Q, 0, wb);
         if (found >= 0 && !fail) return;
         const int64_t g = gt_find_insert(L.gt, k, VGJ_NK, kt, nm, hash_k(k, VGJ_NK, nm));
         if (g < 0) {
@@ -426,7 +430,7 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
 #if VGJ_TRACK
             atomicMin((unsigned long long *)(sm + VGJ_OFF_FIRST) + found, (unsigned long long)vgj_order(L, r0 + j, matched, j));
 #endif
-            failm[j] = vgj_cache_update(sm, found, X, j);
+            failm[j] = vgj_cache_update(sm, found, X, j, wb);
             if (failm[j]) rare |= 1u << j;
         }
         if (rare | miss) {
@@ -476,6 +480,7 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
     __syncthreads();
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
         if (st[i] != 2u) continue;
+        vgj_fix_bases(sm, i);
         if (!merge_entry(L, sm, cl, S, i)) spill_entry(L, sm, cl, S, i, sl);
     }
 }

@@ -168,15 +168,20 @@ VG_DEV uint32_t term_mask(const VgAggLaunch &L, const Rows &X) {
 }
 
 // A double into a cache slot's digit window (same representation as
-// cwin_add, in 32-bit arithmetic): each digit magnitude is added to (or,
-// for a negative summand, subtracted from) the low word of its (lo, hi)
-// pair; the carries / borrows, rare, are applied to the high words after.
-// False: outside the window.
+// cwin_add, in 32-bit arithmetic): each digit, negated for a negative
+// summand, is added to the low word of its (lo, hi) pair as an unsigned
+// 32-bit add; the high word then takes the add's carry, less one for a
+// negated nonzero digit (so a borrow comes out as -1, no carry and no
+// borrow as 0).  Written without branches apart from the rare ones (a
+// special value, the slot's first value, a value outside the window): the
+// adjustments are predicated atomics.  False: outside the window.
 template <int S>
 VG_DEV bool cache_sum_f64(char *sm, uint32_t OBASE, uint32_t OWIN, uint32_t *flags, int slot, uint64_t bits) {
     const VgDigits32 d = vg_split_double32(bits);
-    if (d.special) { set_flags(flags, d.special); return true; }
-    if (d.zero) return true;
+    if (d.special | d.zero) {
+        if (d.special) set_flags(flags, d.special);
+        return true;
+    }
     int32_t *bp = (int32_t *)(sm + OBASE) + slot;
     int b = *(volatile int *)bp;
     if (b == kBaseUnset) {
@@ -187,26 +192,73 @@ VG_DEV bool cache_sum_f64(char *sm, uint32_t OBASE, uint32_t OWIN, uint32_t *fla
         b = (prev == kBaseUnset) ? want : prev;
     }
     const int rel = d.word - b;
-    if (rel < 0 || rel + (d.d2 ? 3 : 2) > kWin) return false;
+    // the value's digits take words rel .. rel+1 (+2 if d2 is nonzero)
+    if ((unsigned)rel > (unsigned)(kWin - 2 - (d.d2 != 0u))) return false;
     uint32_t *wl = (uint32_t *)(sm + OWIN) + slot + rel * S;
     int32_t *wh = (int32_t *)(sm + OWIN + 4 * S * kWin) + slot + rel * S;
-    // adding 2^32 - d to a low word subtracts d from it
-    const uint32_t a0 = d.neg ? 0u - d.d0 : d.d0;
-    const uint32_t a1 = d.neg ? 0u - d.d1 : d.d1;
-    const uint32_t a2 = d.neg ? 0u - d.d2 : d.d2;
+    const uint32_t m = 0u - d.neg;
+    const uint32_t a0 = (d.d0 ^ m) + d.neg, a1 = (d.d1 ^ m) + d.neg, a2 = (d.d2 ^ m) + d.neg;
     const uint32_t o0 = atomicAdd(wl, a0);
     const uint32_t o1 = atomicAdd(wl + S, a1);
-    const uint32_t o2 = a2 ? atomicAdd(wl + 2 * S, a2) : 0u;
-    // carry out of an add: the sum wrapped; borrow of a subtract: old < d
-    const bool c0 = d.neg ? (o0 < d.d0) : (o0 + a0 < o0);
-    const bool c1 = d.neg ? (o1 < d.d1) : (o1 + a1 < o1);
-    const bool c2 = d.neg ? (o2 < d.d2) : (o2 + a2 < o2);
-    if (c0 | c1 | c2) {
-        const int32_t adj = d.neg ? -1 : 1;
-        if (c0) atomicAdd(wh, adj);
-        if (c1) atomicAdd(wh + S, adj);
-        if (c2 && a2) atomicAdd(wh + 2 * S, adj);
+    uint32_t o2 = 0u;
+    if (a2) o2 = atomicAdd(wl + 2 * S, a2);
+    const int j0 = (int)(o0 + a0 < o0) - (int)(d.neg & (d.d0 != 0u));
+    const int j1 = (int)(o1 + a1 < o1) - (int)(d.neg & (d.d1 != 0u));
+    const int j2 = (int)(o2 + a2 < o2) - (int)(d.neg & (d.d2 != 0u));
+    if (j0) atomicAdd(wh, j0);
+    if (j1) atomicAdd(wh + S, j1);
+    if (j2) atomicAdd(wh + 2 * S, j2);
+    return true;
+}
+
+// The fused kernel's cache places every double sum of one accumulator on
+// one digit window per CTA (not one per group): its base word is fixed by
+// the first value the CTA adds (two words below it, as a group's own base
+// would be) and held in a register by each thread, so a row's update reads
+// no base from shared memory.  The kernel tail writes the CTA base into
+// every live slot's base word before the slots are merged.  Values outside
+// the window take the global table, as they do for a group's own window.
+__shared__ int vgj_cta_base[VG_MAX_ACCS];
+
+struct VgjBases {
+    int b[VG_MAX_ACCS];
+};
+
+template <int S>
+VG_DEV bool cache_sum_f64_cta(char *sm, uint32_t OWIN, uint32_t *flags, int slot, uint64_t bits, int &wb,
+                              int *cta_base) {
+    const VgDigits32 d = vg_split_double32(bits);
+    if (d.special | d.zero) {
+        if (d.special) set_flags(flags, d.special);
+        return true;
     }
+    if (wb == kBaseUnset) {
+        int b = *(volatile int *)cta_base;
+        if (b == kBaseUnset) {
+            int want = d.word - 2;
+            if (want < 0) want = 0;
+            if (want > VG_LACC_WORDS - kWin) want = VG_LACC_WORDS - kWin;
+            const int prev = atomicCAS(cta_base, kBaseUnset, want);
+            b = (prev == kBaseUnset) ? want : prev;
+        }
+        wb = b;
+    }
+    const int rel = d.word - wb;
+    if ((unsigned)rel > (unsigned)(kWin - 2 - (d.d2 != 0u))) return false;
+    uint32_t *wl = (uint32_t *)(sm + OWIN) + slot + rel * S;
+    int32_t *wh = (int32_t *)(sm + OWIN + 4 * S * kWin) + slot + rel * S;
+    const uint32_t m = 0u - d.neg;
+    const uint32_t a0 = (d.d0 ^ m) + d.neg, a1 = (d.d1 ^ m) + d.neg, a2 = (d.d2 ^ m) + d.neg;
+    const uint32_t o0 = atomicAdd(wl, a0);
+    const uint32_t o1 = atomicAdd(wl + S, a1);
+    uint32_t o2 = 0u;
+    if (a2) o2 = atomicAdd(wl + 2 * S, a2);
+    const int j0 = (int)(o0 + a0 < o0) - (int)(d.neg & (d.d0 != 0u));
+    const int j1 = (int)(o1 + a1 < o1) - (int)(d.neg & (d.d1 != 0u));
+    const int j2 = (int)(o2 + a2 < o2) - (int)(d.neg & (d.d2 != 0u));
+    if (j0) atomicAdd(wh, j0);
+    if (j1) atomicAdd(wh + S, j1);
+    if (j2) atomicAdd(wh + 2 * S, j2);
     return true;
 }
 
@@ -254,6 +306,23 @@ VG_DEV bool cache_acc(char *sm, int slot, InVal x) {
         return true;
     }
     return true;   // VG_ACC_NA_ONLY
+}
+
+// cache_acc for the fused kernel's cache: double sums on the CTA's window
+// (A = the accumulator's index), everything else as cache_acc.
+template <int A, int CLS, int NA_RM, int COUNT, uint32_t OCNT, uint32_t OVAL, uint32_t OFLAGS, uint32_t OBASE,
+          uint32_t OWIN, int S>
+VG_DEV bool cache_acc_k(char *sm, int slot, InVal x, VgjBases &wb) {
+    if (CLS != VG_ACC_SUM_F64) return cache_acc<CLS, NA_RM, COUNT, OCNT, OVAL, OFLAGS, OBASE, OWIN, S>(sm, slot, x);
+    uint32_t *cnt = (uint32_t *)(sm + OCNT) + slot;
+    uint32_t *flags = (uint32_t *)(sm + OFLAGS) + slot;
+    if (!x.ok) {
+        if (!NA_RM) set_flags(flags, 1u);
+        return true;
+    }
+    if (!cache_sum_f64_cta<S>(sm, OWIN, flags, slot, x.bits, wb.b[A], &vgj_cta_base[A])) return false;
+    if (COUNT) atomicAdd(cnt, 1u);
+    return true;
 }
 
 // Finds or claims the cache slot of a key (open addressing, bounded
