@@ -85,6 +85,7 @@ char g_jit_err[2048];
 struct JitKernel {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t kernel = nullptr;
+    cudaKernel_t replay = nullptr;   // vg_jit_replay, in modules that defer rows
     int smem_set = 0;
     Shape shape;             // the launch shape it was compiled for
 };
@@ -204,6 +205,9 @@ int vgk_agg_jit_source(const VgAggLaunch *L, int S, char *out, size_t out_bytes)
 
 namespace {
 
+// A dense cache (it never misses) defers its rows for the global table.
+bool defer_ok(const VgAggLaunch &L) { return L.dense && !L.part && L.defer_bits && L.defer_n; }
+
 std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
     VgAggLaunch T = L;
     T.cache_slots = S;
@@ -232,6 +236,13 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
     }
     fmt(s, "#define VGJ_NK %d\n#define VGJ_DENSE %d\n#define VGJ_TRACK %d\n#define VGJ_PART %d\n", L.n_keys,
         L.dense ? 1 : 0, L.track_first ? 1 : 0, L.part ? 1 : 0);
+    // a dense cache's rows for the global table, deferred to the replay kernel
+    {
+        uint32_t f64 = 0;
+        for (int a = 0; a < L.n_accs; a++)
+            if (L.acc[a].cls == VG_ACC_SUM_F64) f64 |= 1u << a;
+        fmt(s, "#define VGJ_DEFER %d\n#define VGJ_F64_MASK %uu\n", defer_ok(L) ? 1 : 0, f64);
+    }
     // rows that pass a filter queued per warp (few of a step's rows pass)
     fmt(s, "#define VGJ_COMPACT %d\n",
         (L.pred.n_terms > 0 && !L.has_join && !L.part && !L.sel && !L.track_first && !L.dense) ? 1 : 0);
@@ -517,6 +528,14 @@ JitKernel *plan_kernel(const VgAggLaunch *L, int S, bool vec) {
         std::vector<char> cubin;
         if (compile_plan(*L, S, vec, cubin, k.shape, nullptr) != 0) return nullptr;
         if (load_kernel(cubin, k) != 0) return nullptr;
+        if (defer_ok(*L)) {
+            cudaError_t e = cudaLibraryGetKernel(&k.replay, k.lib, "vg_jit_replay");
+            if (e != cudaSuccess) {
+                snprintf(g_jit_err, sizeof(g_jit_err), "cudaLibraryGetKernel(vg_jit_replay): %s",
+                         cudaGetErrorString(e));
+                return nullptr;
+            }
+        }
         it = g_cache.emplace(src, k).first;
     }
     return &it->second;
@@ -568,6 +587,11 @@ int vgk_agg_launch_jit(const VgAggLaunch *L, int64_t n_logical, vg_stream_t s) {
     vg_prof_begin(VG_PROF_AGG, st);
     cudaError_t e = cudaLaunchKernel((const void *)jk->kernel, dim3(grid), dim3(sh.threads), args, (size_t)smem, st);
     vg_launch_counter++;
+    // the rows this launch deferred (a dense cache): applied right after it
+    if (e == cudaSuccess && jk->replay) {
+        e = cudaLaunchKernel((const void *)jk->replay, dim3(2 * vgk_num_sms()), dim3(256), args, 0, st);
+        vg_launch_counter++;
+    }
     vg_prof_end(VG_PROF_AGG, st);
     if (e != cudaSuccess) {
         snprintf(g_jit_err, sizeof(g_jit_err), "jit agg launch: %s", cudaGetErrorString(e));
@@ -932,6 +956,10 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
         L.jpay_n = 2;
         L.jt.direct = shape != 4;   // shape 4: hashed table, linear-probing chain
         L.jt.dmin = 1;
+        static uint32_t defer_dummy[4];
+        L.defer_bits = defer_dummy;     // the dense cache defers rows to the replay kernel
+        L.defer_n = defer_dummy + 2;
+        L.defer_words = 1;
         if (shape == 11) {          // compact payload entries, the group key narrowed
             L.jpay16 = 1;
             L.jpay_narrow = 0;

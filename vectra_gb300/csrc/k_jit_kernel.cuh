@@ -43,6 +43,216 @@ VG_DEV uint64_t vgj_order(const VgAggLaunch &L, int64_t li, uint32_t matched, in
 #endif
 }
 
+#if VGJ_JOIN
+// The join probe of the rows in `live` (R rows of X): their slot reads are
+// issued together, then their payload entries (or build rows) are read.
+// Returns the rows that matched; for an inner join, live loses the rest.
+VG_DEV uint32_t vgj_join_probe(const VgAggLaunch &L, Rows &X, uint32_t &live) {
+    uint32_t matched = 0;
+    int64_t brow[R];
+        {
+            uint64_t kw[R];
+            int64_t slot[R];
+            uint32_t need = 0;
+            const int64_t mask = L.jt.cap - 1;
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                brow[j] = -1;
+                kw[j] = 0;
+                slot[j] = 0;
+                if (!((live >> j) & 1u)) continue;
+                if (!((X.pok[VGJ_JCOL] >> j) & 1u)) continue;           // NA never matches
+                uint64_t b = X.p[VGJ_JCOL][j];
+                if (VGJ_JCONV) b = vg_f64_to_bits(vg_i2f((int64_t)b));
+                if (VGJ_JKT == VEC_DOUBLE && vg_is_nan_bits(b)) continue;
+                kw[j] = vg_norm_key(b, VGJ_JKT);
+#if VGJ_JDIRECT
+                slot[j] = jt_direct_slot(L.jt, kw[j]);
+                if (slot[j] < 0) continue;                           // outside the key range: no match
+#else
+                slot[j] = kw[j] == VG_JEMPTY ? L.jt.cap : (int64_t)(vg_jhash(&kw[j], 1) & (uint64_t)mask);
+#endif
+                need |= 1u << j;
+            }
+#if VGJ_PAY && VGJ_PAY16
+            // compact payload copy of a direct table: one 16-byte entry per
+            // probe, {kept column, narrowed column, validity}
+            ulonglong2 ea[R];
+#pragma unroll
+            for (int j = 0; j < R; j++)
+                if ((need >> j) & 1u) ea[j] = __ldg((const ulonglong2 *)L.jpay + slot[j]);
+#pragma unroll
+            for (int i = 0; i < kNB; i++) X.bok[i] = 0;
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                if (!((need >> j) & 1u)) continue;
+                const uint32_t meta = (uint32_t)(ea[j].y >> 32);
+                if (!(meta & 1u)) continue;
+                matched |= 1u << j;
+                brow[j] = 0;
+                if (VGJ_PAY_NARROW < 0) {
+                    X.b[0][j] = ea[j].x;
+                    X.bok[0] |= ((meta >> 1) & 1u) << j;
+                } else {
+                    constexpr int kN = VGJ_PAY_NARROW < 0 ? 0 : VGJ_PAY_NARROW;
+                    constexpr int kK = kNB > 1 ? 1 - kN : 0;
+                    const uint32_t b = (uint32_t)ea[j].y;
+                    X.b[kK][j] = ea[j].x;
+                    X.b[kN][j] = VGJ_PAY_NARROW_T == VEC_BOOL ? (uint64_t)b : (uint64_t)L.jpay_min + (uint64_t)b;
+                    X.bok[0] |= ((meta >> 1) & 1u) << j;
+                    if (kNB > 1) X.bok[kNB > 1 ? 1 : 0] |= ((meta >> 2) & 1u) << j;
+                }
+            }
+#elif VGJ_PAY
+            // payload copy: key, build row, validity and up to two build
+            // columns in one 32-byte sector per probe
+            ulonglong2 ea[R], eb[R];
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                if (!((need >> j) & 1u)) continue;
+                const VgJPay *q = L.jpay + slot[j];
+                ea[j] = __ldg((const ulonglong2 *)q);
+                eb[j] = __ldg((const ulonglong2 *)q + 1);
+            }
+#pragma unroll
+            for (int i = 0; i < kNB; i++) X.bok[i] = 0;
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                if (!((need >> j) & 1u)) continue;
+                bool hit;
+                if (VGJ_JDIRECT || kw[j] == VG_JEMPTY) {
+                    hit = ((ea[j].y >> 32) & 1u) != 0;
+                } else {
+                    hit = false;
+                    int64_t s = slot[j];
+                    for (int64_t probe = 0; probe < L.jt.cap; probe++) {
+                        if (ea[j].x == kw[j]) { hit = true; break; }
+                        if (ea[j].x == VG_JEMPTY) break;
+                        s = (s + 1) & mask;
+                        const VgJPay *q = L.jpay + s;
+                        ea[j] = __ldg((const ulonglong2 *)q);
+                        eb[j] = __ldg((const ulonglong2 *)q + 1);
+                    }
+                }
+                if (hit) {
+                    const uint32_t meta = (uint32_t)(ea[j].y >> 32);
+                    brow[j] = (int64_t)(int32_t)(uint32_t)ea[j].y;
+                    matched |= 1u << j;
+                    X.b[0][j] = eb[j].x;
+                    X.bok[0] |= ((meta >> 1) & 1u) << j;
+                    if (kNB > 1) {
+                        X.b[kNB > 1 ? 1 : 0][j] = eb[j].y;
+                        X.bok[kNB > 1 ? 1 : 0] |= ((meta >> 2) & 1u) << j;
+                    }
+                }
+            }
+#else
+            VgJSlot e[R];
+#pragma unroll
+            for (int j = 0; j < R; j++)
+                if ((need >> j) & 1u) e[j] = jt_slot(L.jt.slots + slot[j]);
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                if (!((need >> j) & 1u)) continue;
+                if (VGJ_JDIRECT || kw[j] == VG_JEMPTY) {
+                    if (e[j].count > 0) { brow[j] = e[j].start; matched |= 1u << j; }
+                    continue;
+                }
+                int64_t s = slot[j];
+                for (int64_t probe = 0; probe < L.jt.cap; probe++) {
+                    if (e[j].key == kw[j]) { brow[j] = e[j].start; matched |= 1u << j; break; }
+                    if (e[j].key == VG_JEMPTY) break;
+                    s = (s + 1) & mask;
+                    e[j] = jt_slot(L.jt.slots + s);
+                }
+            }
+#endif
+            (void)mask;
+            if (VGJ_JKIND != JOIN_LEFT) live &= matched;
+        }
+#if !VGJ_PAY
+        vgj_load_build(L, X, brow, live & matched);
+#else
+        (void)brow;
+#endif
+    return matched;
+}
+#endif
+
+#if VGJ_DEFER
+// Dense cache: a row whose double sums fell outside the CTA's digit window
+// is marked (one bit per row and double-sum accumulator) instead of
+// updating the global table in the row loop, so the loop carries no
+// global-table code and keeps its registers; the replay kernel below,
+// launched after this one, applies the marks.
+VG_DEV void vgj_defer_row(const VgAggLaunch &L, int64_t li, uint32_t which) {
+    uint32_t n = 0;
+    int f = 0;
+#pragma unroll
+    for (int a = 0; a < VG_MAX_ACCS; a++) {
+        if (!((VGJ_F64_MASK >> a) & 1u)) continue;
+        if ((which >> a) & 1u) {
+            atomicOr(L.defer_bits + (int64_t)f * L.defer_words + (li >> 5), 1u << (int)(li & 31));
+            n++;
+        }
+        f++;
+    }
+    atomicAdd(L.defer_n, n);
+}
+
+// Applies and clears the marks of the launch before it (same plan, same
+// rows): each marked row is read again from device memory and its marked
+// accumulators update the global table.  Returns at once when there are
+// none.
+extern "C" __global__ void __launch_bounds__(256)
+vg_jit_replay(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
+    using namespace vgj;
+    (void)n_rows;
+    if (*(volatile const uint32_t *)L.defer_n == 0u) return;
+    const KeyTypes kt = key_types(L);
+    int f = 0;
+#pragma unroll
+    for (int a = 0; a < VG_MAX_ACCS; a++) {
+        if (!((VGJ_F64_MASK >> a) & 1u)) continue;
+        uint32_t *bits = L.defer_bits + (int64_t)f * L.defer_words;
+        f++;
+        for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < L.defer_words;
+             w += (int64_t)gridDim.x * blockDim.x) {
+            uint32_t m = bits[w];
+            if (!m) continue;
+            bits[w] = 0u;
+            while (m) {
+                const int b = __ffs(m) - 1;
+                m &= m - 1u;
+                const int64_t li = w * 32 + b;
+                Rows X;
+                int64_t phys[R];
+#pragma unroll
+                for (int j = 0; j < R; j++) phys[j] = 0;
+#if VGJ_SEL
+                phys[0] = (int64_t)__ldg(L.sel + li);
+#else
+                phys[0] = li;
+#endif
+                vgj_load_probe(L, X, li, 1, false, phys, 1u);
+#if VGJ_JOIN
+                uint32_t live = 1u;
+                (void)vgj_join_probe(L, X, live);
+#endif
+                Keys k;
+#pragma unroll
+                for (int i = 0; i < VG_MAX_KEYS; i++) k.w[i] = 0;
+                uint32_t nm = 0;
+                vgj_keys(X, 0, k, nm);
+                const int64_t g = gt_find_insert(L.gt, k, VGJ_NK, kt, nm, hash_k(k, VGJ_NK, nm));
+                if (g < 0) vgj_spill(L, li, 1u << a);
+                else vgj_global_update(L, g, X, 0, 1u << a);
+            }
+        }
+    }
+}
+#endif
+
 extern "C" __global__ void __launch_bounds__(VGJ_THREADS, VGJ_MINB)
 vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
     using namespace vgj;
@@ -234,133 +444,7 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
 #endif
         uint32_t matched = 0;
 #if VGJ_JOIN
-        // join probe: the R rows' slot reads are issued together
-        int64_t brow[R];
-        {
-            uint64_t kw[R];
-            int64_t slot[R];
-            uint32_t need = 0;
-            const int64_t mask = L.jt.cap - 1;
-#pragma unroll
-            for (int j = 0; j < R; j++) {
-                brow[j] = -1;
-                kw[j] = 0;
-                slot[j] = 0;
-                if (!((live >> j) & 1u)) continue;
-                if (!((X.pok[VGJ_JCOL] >> j) & 1u)) continue;           // NA never matches
-                uint64_t b = X.p[VGJ_JCOL][j];
-                if (VGJ_JCONV) b = vg_f64_to_bits(vg_i2f((int64_t)b));
-                if (VGJ_JKT == VEC_DOUBLE && vg_is_nan_bits(b)) continue;
-                kw[j] = vg_norm_key(b, VGJ_JKT);
-#if VGJ_JDIRECT
-                slot[j] = jt_direct_slot(L.jt, kw[j]);
-                if (slot[j] < 0) continue;                           // outside the key range: no match
-#else
-                slot[j] = kw[j] == VG_JEMPTY ? L.jt.cap : (int64_t)(vg_jhash(&kw[j], 1) & (uint64_t)mask);
-#endif
-                need |= 1u << j;
-            }
-#if VGJ_PAY && VGJ_PAY16
-            // compact payload copy of a direct table: one 16-byte entry per
-            // probe, {kept column, narrowed column, validity}
-            ulonglong2 ea[R];
-#pragma unroll
-            for (int j = 0; j < R; j++)
-                if ((need >> j) & 1u) ea[j] = __ldg((const ulonglong2 *)L.jpay + slot[j]);
-#pragma unroll
-            for (int i = 0; i < kNB; i++) X.bok[i] = 0;
-#pragma unroll
-            for (int j = 0; j < R; j++) {
-                if (!((need >> j) & 1u)) continue;
-                const uint32_t meta = (uint32_t)(ea[j].y >> 32);
-                if (!(meta & 1u)) continue;
-                matched |= 1u << j;
-                brow[j] = 0;
-                if (VGJ_PAY_NARROW < 0) {
-                    X.b[0][j] = ea[j].x;
-                    X.bok[0] |= ((meta >> 1) & 1u) << j;
-                } else {
-                    constexpr int kN = VGJ_PAY_NARROW < 0 ? 0 : VGJ_PAY_NARROW;
-                    constexpr int kK = kNB > 1 ? 1 - kN : 0;
-                    const uint32_t b = (uint32_t)ea[j].y;
-                    X.b[kK][j] = ea[j].x;
-                    X.b[kN][j] = VGJ_PAY_NARROW_T == VEC_BOOL ? (uint64_t)b : (uint64_t)L.jpay_min + (uint64_t)b;
-                    X.bok[0] |= ((meta >> 1) & 1u) << j;
-                    if (kNB > 1) X.bok[kNB > 1 ? 1 : 0] |= ((meta >> 2) & 1u) << j;
-                }
-            }
-#elif VGJ_PAY
-            // payload copy: key, build row, validity and up to two build
-            // columns in one 32-byte sector per probe
-            ulonglong2 ea[R], eb[R];
-#pragma unroll
-            for (int j = 0; j < R; j++) {
-                if (!((need >> j) & 1u)) continue;
-                const VgJPay *q = L.jpay + slot[j];
-                ea[j] = __ldg((const ulonglong2 *)q);
-                eb[j] = __ldg((const ulonglong2 *)q + 1);
-            }
-#pragma unroll
-            for (int i = 0; i < kNB; i++) X.bok[i] = 0;
-#pragma unroll
-            for (int j = 0; j < R; j++) {
-                if (!((need >> j) & 1u)) continue;
-                bool hit;
-                if (VGJ_JDIRECT || kw[j] == VG_JEMPTY) {
-                    hit = ((ea[j].y >> 32) & 1u) != 0;
-                } else {
-                    hit = false;
-                    int64_t s = slot[j];
-                    for (int64_t probe = 0; probe < L.jt.cap; probe++) {
-                        if (ea[j].x == kw[j]) { hit = true; break; }
-                        if (ea[j].x == VG_JEMPTY) break;
-                        s = (s + 1) & mask;
-                        const VgJPay *q = L.jpay + s;
-                        ea[j] = __ldg((const ulonglong2 *)q);
-                        eb[j] = __ldg((const ulonglong2 *)q + 1);
-                    }
-                }
-                if (hit) {
-                    const uint32_t meta = (uint32_t)(ea[j].y >> 32);
-                    brow[j] = (int64_t)(int32_t)(uint32_t)ea[j].y;
-                    matched |= 1u << j;
-                    X.b[0][j] = eb[j].x;
-                    X.bok[0] |= ((meta >> 1) & 1u) << j;
-                    if (kNB > 1) {
-                        X.b[kNB > 1 ? 1 : 0][j] = eb[j].y;
-                        X.bok[kNB > 1 ? 1 : 0] |= ((meta >> 2) & 1u) << j;
-                    }
-                }
-            }
-#else
-            VgJSlot e[R];
-#pragma unroll
-            for (int j = 0; j < R; j++)
-                if ((need >> j) & 1u) e[j] = jt_slot(L.jt.slots + slot[j]);
-#pragma unroll
-            for (int j = 0; j < R; j++) {
-                if (!((need >> j) & 1u)) continue;
-                if (VGJ_JDIRECT || kw[j] == VG_JEMPTY) {
-                    if (e[j].count > 0) { brow[j] = e[j].start; matched |= 1u << j; }
-                    continue;
-                }
-                int64_t s = slot[j];
-                for (int64_t probe = 0; probe < L.jt.cap; probe++) {
-                    if (e[j].key == kw[j]) { brow[j] = e[j].start; matched |= 1u << j; break; }
-                    if (e[j].key == VG_JEMPTY) break;
-                    s = (s + 1) & mask;
-                    e[j] = jt_slot(L.jt.slots + s);
-                }
-            }
-#endif
-            (void)mask;
-            if (VGJ_JKIND != JOIN_LEFT) live &= matched;
-        }
-#if !VGJ_PAY
-        vgj_load_build(L, X, brow, live & matched);
-#else
-        (void)brow;
-#endif
+        matched = vgj_join_probe(L, X, live);
 #endif
 #if VGJ_PART
         // Partition mode: the rows with a valid key claim their record
@@ -433,6 +517,15 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
             failm[j] = vgj_cache_update(sm, found, X, j, wb);
             if (failm[j]) rare |= 1u << j;
         }
+#if VGJ_DEFER
+        // rows for the global table are marked for the replay (a dense cache never misses)
+        (void)miss;
+        if (rare) {
+#pragma unroll
+            for (int j = 0; j < R; j++)
+                if ((rare >> j) & 1u) vgj_defer_row(L, r0 + j, failm[j]);
+        }
+#else
         if (rare | miss) {
 #pragma unroll
             for (int j = 0; j < R; j++) {
@@ -456,7 +549,9 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
                 vgj_global_update(L, g, X, j, m ? 0xFFFFFFFFu : failm[j]);
             }
         }
+#endif
     }
+
 
 #if VGJ_COMPACT
     flush_queue(qn);

@@ -333,8 +333,38 @@ static int cache_slots_for(const VgAggLaunch *L) {
 }
 
 /* one launch over n_logical rows (+ growth and replay); 1 if the table grew */
+/* The dense cache's deferred-row marks (see VgAggLaunch.defer_bits): a
+ * count word, then one bit per row and double-sum accumulator; kept and
+ * reused by later calls, cleared before every launch. */
+static void *g_defer;
+static size_t g_defer_cap;
+
+static void defer_prepare(VgAggLaunch *L, int64_t n_logical) {
+    L->defer_bits = NULL;
+    L->defer_n = NULL;
+    L->defer_words = 0;
+    if (!L->dense || L->part) return;
+    int nf = 0;
+    for (int a = 0; a < L->n_accs; a++) nf += L->acc[a].cls == VG_ACC_SUM_F64;
+    if (nf == 0) return;
+    const int64_t words = (n_logical + 31) / 32;
+    const size_t bytes = 256 + (size_t)nf * (size_t)words * 4;
+    if (g_defer_cap < bytes) {
+        vg_dfree(g_defer);
+        g_defer = NULL;
+        g_defer_cap = 0;
+        g_defer = vg_dmalloc_kept(bytes);
+        g_defer_cap = bytes;
+    }
+    vg_dmemset(g_defer, 0, bytes);
+    L->defer_n = (uint32_t *)g_defer;
+    L->defer_bits = (uint32_t *)((char *)g_defer + 256);
+    L->defer_words = words;
+}
+
 static int run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_logical) {
     int sms = vgk_num_sms();
+    defer_prepare(L, n_logical);
     /* spill space for this launch */
     /* a dense cache holds every group: nothing misses it, so rows never
      * spill (a spill would be reported, not lost) */

@@ -383,6 +383,15 @@ typedef struct {
      * the group table gt, which holds the NA group alone. */
     int32_t   part;
     VgPartOut po;
+    /* Dense cache, run-time specialised kernel: rows whose double sums fall
+     * outside the CTA's digit window are deferred instead of updating the
+     * global table in the row loop: bit li of word array f (one array of
+     * defer_words words per double-sum accumulator, in accumulator order)
+     * marks row li for accumulator f, defer_n counts the marks, and the
+     * replay kernel that follows each launch applies them and clears them. */
+    uint32_t *defer_bits;
+    int64_t   defer_words;
+    uint32_t *defer_n;
 } VgAggLaunch;
 
 /* ------------------------------------------------------------------ */
