@@ -332,6 +332,25 @@ def gpu_arm(args, rank, world):
         ds = source_from_ptrs(lib, hd, N_DIM, N_DIM, 1)
         return run_query(eng, fs, ds)
 
+    # the host link's rate for these bytes: every page-locked input column
+    # copied to the device by asynchronous copies, CUDA events around them
+    dst = {k: (torch.empty_like(v, device=dev), torch.empty_like(m, device=dev))
+           for k, (v, m) in list(hf.items()) + [("d_" + k, c) for k, c in hd.items()]}
+    srcs = list(hf.values()) + list(hd.values())
+    link = []
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for (v, m), (dv, dm) in zip(srcs, dst.values()):
+            dv.copy_(v, non_blocking=True)
+            dm.copy_(m, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        link.append(e0.elapsed_time(e1))
+    del dst
+    link_bytes = sum(v.numel() * v.element_size() + m.numel() for v, m in srcs)
+    host_link_gbs = link_bytes / (min(link) * 1e-3) / 1e9
     out2 = host_step()
     same_result(out, out2)
     same_result(out, copy_step())
@@ -369,7 +388,9 @@ def gpu_arm(args, rank, world):
         "join_build_ms": build_ms / args.steps,
         "e2e": {"value": whole_job_rate(rows, world, e2e_ms), "unit": "rows/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "path": "node C API, page-locked host columns read in place by the kernels (VGPU_SRC_MAPPED)"},
+                "path": "node C API, page-locked host columns read in place by the kernels (VGPU_SRC_MAPPED)",
+                "host_link_h2d_gbs": host_link_gbs,
+                "frac_of_host_link": (h2d / (e2e_ms * 1e-3) / 1e9) / host_link_gbs},
         "e2e_copy": {"value": whole_job_rate(rows, world, copy_ms), "unit": "rows/s", "ms_per_step": copy_ms,
                      "path": "node C API, page-locked host columns staged by async copies, 16M-row fact batches"},
         "e2e_r_path": r_path,
