@@ -236,6 +236,16 @@ std::string gen_source(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
     }
     fmt(s, "#define VGJ_NK %d\n#define VGJ_DENSE %d\n#define VGJ_TRACK %d\n#define VGJ_PART %d\n", L.n_keys,
         L.dense ? 1 : 0, L.track_first ? 1 : 0, L.part ? 1 : 0);
+    // a dense cache with an n() accumulator: a slot is live when its count
+    // is nonzero (no per-row state store)
+    {
+        int live_acc = -1;
+        if (L.dense && !L.part)
+            for (int a = 0; a < L.n_accs && live_acc < 0; a++)
+                if (L.acc[a].cls == VG_ACC_COUNT_ALL) live_acc = a;
+        fmt(s, "#define VGJ_LIVE_BY_CNT %d\n#define VGJ_LIVE_CNT %lluu\n", live_acc >= 0 ? 1 : 0,
+            live_acc >= 0 ? (unsigned long long)c.cnt[live_acc] : 0ull);
+    }
     // a dense cache's rows for the global table, deferred to the replay kernel
     {
         uint32_t f64 = 0;

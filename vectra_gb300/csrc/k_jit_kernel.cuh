@@ -498,7 +498,9 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
 #elif VGJ_DENSE
             (void)cache_used;
             found = nm ? L.dense_n : (int)((int64_t)k.w[0] - L.dense_min);
+#if !VGJ_LIVE_BY_CNT
             st[found] = 2u;                           // every touch marks the slot live (same value)
+#endif
 #else
             {
                 int err = 0;
@@ -574,7 +576,12 @@ vg_jit_agg(const __grid_constant__ VgAggLaunch L, int64_t n_rows) {
     if (threadIdx.x == 0) make_lay(L, (uint64_t)L.spill_cache_cap, sl);
     __syncthreads();
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
+#if VGJ_DENSE && VGJ_LIVE_BY_CNT
+        // every row counts in n(): a slot some row touched has a nonzero count
+        if (((const uint32_t *)(sm + VGJ_LIVE_CNT))[i] == 0u) continue;
+#else
         if (st[i] != 2u) continue;
+#endif
         vgj_fix_bases(sm, i);
         if (!merge_entry(L, sm, cl, S, i)) spill_entry(L, sm, cl, S, i, sl);
     }
