@@ -700,6 +700,7 @@ def workload_arm(args):
     lib.vgpu_profile_ms.argtypes = [C.c_int, C.POINTER(C.c_ulonglong)]
     if args.workload == "query_set":
         return query_set_arm(args, eng, lib, dev)
+    fanout = None
     if args.workload == "filter_group":
         n = 10_000_000 // args.scale
         cols = W.gen_filter_group(torch, n, 0, dev)
@@ -714,7 +715,27 @@ def workload_arm(args):
         n, distinct = 200_000_000 // args.scale, 50_000_000 // args.scale
         cols, raw = W.gen_high_card(torch, n, distinct, 0, dev)
         run = lambda numpy=False: W.run_high_card(eng, W.device_source(lib, cols, n)[0], numpy=numpy)
+        # the fan-out is tuned on the first three queries (untimed; the
+        # first is also the checked one) and the fastest kept
+        import tempfile
+        os.environ.setdefault("VGPU_TUNE_FILE", os.path.join(tempfile.mkdtemp(prefix="vgpu_tune_"), "tune.txt"))
+        lib.vgpu_pagg_tune.argtypes = [C.c_int]
+        lib.vgpu_pagg_tuned.restype = C.c_int
+        lib.vgpu_pagg_tuned.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_double)]
+        shape, tms = C.create_string_buffer(96), C.c_double(0)
+        lib.vgpu_pagg_tune(1)
         out = run(True)
+        cands = [(lib.vgpu_pagg_tuned(shape, 96, C.byref(tms)), tms.value)]
+        for _ in range(2):
+            run()
+            cands.append((lib.vgpu_pagg_tuned(shape, 96, C.byref(tms)), tms.value))
+        lib.vgpu_pagg_tune(0)
+        run()
+        kept = lib.vgpu_pagg_tuned(shape, 96, C.byref(tms))
+        fanout = {"shape_class": shape.value.decode(), "doublings_kept": kept,
+                  "candidates_ms": {"x%d" % (1 << k): round(v, 3) for k, v in cands},
+                  "what": "bucket count = the key sketch's count x 1, 2, 4; device time of the partition and "
+                          "reducer launches of one query each; the fastest kept and recorded (VGPU_TUNE_FILE)"}
         groups = W.check_high_card(torch, out, cols, raw, distinct)
         del raw
         algo = W.high_card_bytes(n, groups)
@@ -786,7 +807,7 @@ def workload_arm(args):
             "algorithmic_bytes": algo, "hbm_gbs_whole_query": algo / (ms * 1e-3) / 1e9,
             "frac_of_hbm_peak": algo / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind, "roofline": roofline,
             "agg_kernel_ms": agg_ms / max(1, args.steps * 1), "agg_launches": nl.value,
-            "partitioned_path": bool(pagg_runs), "host_split": host,
+            "partitioned_path": bool(pagg_runs), "host_split": host, "fanout": fanout,
             "reduce_kernel_ms": reduce_ms / max(1, args.steps),
             "finish_kernel_ms": finish_ms / max(1, args.steps), "result_checked": True,
             "partitioned_phases_ms": dict(zip(["sketch", "partition", "reduce", "compact", "host_buffers", "download",

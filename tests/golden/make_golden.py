@@ -74,7 +74,7 @@ def write_vtr_ref(path, table, batch_rows):
                 data = C.create_string_buffer(b"".join(enc) or b"\0")
                 keep += [offs, data]
                 a.buf.str.offsets = offs.ctypes.data_as(C.POINTER(C.c_int64))
-                a.buf.str.data = C.cast(data, C.c_char_p)
+                a.buf.str.data = C.cast(data, C.c_void_p)
                 a.buf.str.data_len = int(offs[-1])
             else:
                 v = np.ascontiguousarray(vals[lo:hi], dtype=np.uint8 if t == abi.VEC_BOOL else None)

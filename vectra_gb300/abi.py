@@ -24,7 +24,9 @@ NP_OF = {VEC_INT64: np.int64, VEC_DOUBLE: np.float64, VEC_BOOL: np.uint8}
 
 
 class StrBuf(C.Structure):
-    _fields_ = [("offsets", C.POINTER(C.c_int64)), ("data", C.c_char_p), ("data_len", C.c_int64)]
+    # data is not NUL-terminated: a plain pointer (a c_char_p field would be
+    # read up to a NUL, past the end of the buffer)
+    _fields_ = [("offsets", C.POINTER(C.c_int64)), ("data", C.c_void_p), ("data_len", C.c_int64)]
 
 
 class ArrBuf(C.Union):
@@ -150,7 +152,7 @@ def batch_to_numpy(bp, logical=True):
         name = b.col_names[c].decode()
         if a.type == VEC_STRING:
             offs = np.ctypeslib.as_array(a.buf.str.offsets, shape=(n + 1,)).copy() if n else np.zeros(1, np.int64)
-            data = C.string_at(C.cast(a.buf.str.data, C.c_void_p), int(offs[-1])) if offs[-1] else b""
+            data = C.string_at(a.buf.str.data, int(offs[-1])) if offs[-1] else b""
             vals = np.array([data[offs[i]:offs[i + 1]].decode() for i in range(n)], dtype=object)
         elif n == 0:
             vals = np.zeros(0, NP_OF[a.type])

@@ -26,6 +26,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#include <cuda_runtime_api.h>
 #include "vg_host.h"
 
 typedef struct {
@@ -595,6 +596,9 @@ typedef struct {
     uint64_t rows;                 /* records written (upper bound) */
     VgHostBufs *hb;                /* result columns, faulted in while the device works */
     size_t hb_bytes;               /* bytes of each */
+    struct PTune *tune;            /* fan-out being tuned by this query, or NULL */
+    cudaEvent_t *tev;              /* pairs around its partition and reducer launches */
+    int ntev, tev_cap;
 } PAgg;
 
 /* Host wall time of the partitioned path's phases, summed since load
@@ -637,6 +641,133 @@ static int bitlen64(uint64_t x) {
  * first batch.  VGPU_PAGG=0 never, =1 always when the plan allows it
  * (tests); otherwise when the batch has at least VGPU_PAGG_MIN_ROWS
  * logical rows and an estimated VGPU_PAGG_MIN_GROUPS distinct keys. */
+/* ---- fan-out of the partitioned path, tuned per shape class ---------
+ *
+ * The bucket count follows the key sketch: the fewest powers of two that
+ * keep each bucket's groups at 3/4 of a reducer CTA's capacity.  Tuning
+ * (vgpu_pagg_tune(1) or VGPU_PAGG_TUNE=1) times that count, twice it and
+ * four times it -- one per query, on the first queries of a shape class
+ * (rows of the first batch, estimated groups, record words, accumulators:
+ * powers of two) -- by the device time of the partition and reducer
+ * launches, and keeps the fastest; fewer buckets than the sketch's count
+ * overflow the reducer's capacity and are not tried.  The choice is
+ * appended to the file named by VGPU_TUNE_FILE (the query sets' tuning
+ * file; a line "pagg.<shape> 0 <doublings> 0 <ms> <candidates>") and read
+ * back by later processes. */
+#define PT_CANDS 3
+typedef struct PTune {
+    char shape[96];
+    int recorded, shift, next;
+    double ms[PT_CANDS];
+} PTune;
+static PTune g_pt[64];
+static int g_pt_n, g_pt_loaded, g_pt_armed = -1;
+static int g_pt_last_shift = -1;
+static double g_pt_last_ms;
+static char g_pt_last_shape[96];
+
+void vgpu_pagg_tune(int on) { g_pt_armed = on ? 1 : 0; }
+
+/* The last fan-out decision: the shape class, the doublings over the
+ * sketch's bucket count (-1: none yet) and its measured milliseconds. */
+int vgpu_pagg_tuned(char *shape, int shape_bytes, double *ms) {
+    if (shape && shape_bytes > 0) snprintf(shape, (size_t)shape_bytes, "%s", g_pt_last_shape);
+    if (ms) *ms = g_pt_last_ms;
+    return g_pt_last_shift;
+}
+
+static PTune *pt_find(const char *shape, int create) {
+    for (int i = 0; i < g_pt_n; i++)
+        if (strcmp(g_pt[i].shape, shape) == 0) return &g_pt[i];
+    if (!create || g_pt_n == (int)(sizeof(g_pt) / sizeof(g_pt[0]))) return NULL;
+    PTune *t = &g_pt[g_pt_n++];
+    memset(t, 0, sizeof(*t));
+    snprintf(t->shape, sizeof(t->shape), "%s", shape);
+    return t;
+}
+
+static void pt_load(void) {
+    if (g_pt_loaded) return;
+    g_pt_loaded = 1;
+    const char *path = getenv("VGPU_TUNE_FILE");
+    if (!path || !*path) return;
+    FILE *f = fopen(path, "r");
+    if (!f) return;
+    char shape[96];
+    int threads = 0, mult = 0, cands = 0;
+    long long chunk = 0;
+    double ms = 0;
+    while (fscanf(f, "%95s %d %lld %d %lf %d", shape, &threads, &chunk, &mult, &ms, &cands) == 6) {
+        if (strncmp(shape, "pagg.", 5) != 0 || chunk < 0 || chunk >= PT_CANDS) continue;
+        PTune *t = pt_find(shape, 1);
+        if (!t) break;
+        t->recorded = 1;           /* the last line of a shape wins */
+        t->shift = (int)chunk;
+    }
+    fclose(f);
+}
+
+static void pt_save(const PTune *t, double ms) {
+    const char *path = getenv("VGPU_TUNE_FILE");
+    if (!path || !*path) return;
+    FILE *f = fopen(path, "a");
+    if (!f) return;
+    fprintf(f, "%s 0 %d 0 %.6f %d\n", t->shape, t->shift, ms, PT_CANDS);
+    fclose(f);
+}
+
+static int lg2d(double x) {
+    int b = 0;
+    while (x >= 2.0 && b < 62) { x /= 2.0; b++; }
+    return b;
+}
+
+static void pt_mark(PAgg *pg) {
+    if (!pg->tune) return;
+    if (pg->ntev == pg->tev_cap) {
+        pg->tev_cap = pg->tev_cap ? 2 * pg->tev_cap : 32;
+        cudaEvent_t *e = (cudaEvent_t *)realloc(pg->tev, (size_t)pg->tev_cap * sizeof(cudaEvent_t));
+        if (!e) vg_fail("host allocation failed");
+        pg->tev = e;
+    }
+    cudaEvent_t *e = &pg->tev[pg->ntev];
+    if (cudaEventCreate(e) != cudaSuccess || cudaEventRecord(*e, (cudaStream_t)vg_stream()) != cudaSuccess) {
+        cudaGetLastError();
+        vg_fail("partitioned aggregation: timing event");
+    }
+    pg->ntev++;
+}
+
+/* after the query's last launch: its time for the candidate it ran */
+static void pt_finish(PAgg *pg) {
+    if (!pg->tune) return;
+    vg_sync();
+    double ms = 0.0;
+    for (int i = 0; i + 1 < pg->ntev; i += 2) {
+        float m = 0.f;
+        if (cudaEventElapsedTime(&m, pg->tev[i], pg->tev[i + 1]) == cudaSuccess) ms += m;
+    }
+    PTune *t = pg->tune;
+    t->ms[t->next] = ms;
+    g_pt_last_shift = t->next;
+    g_pt_last_ms = ms;
+    if (++t->next == PT_CANDS) {
+        int best = 0;
+        for (int c = 1; c < PT_CANDS; c++)
+            if (t->ms[c] < t->ms[best]) best = c;
+        t->shift = best;
+        t->recorded = 1;
+        pt_save(t, t->ms[best]);
+    }
+}
+
+static void pt_free(PAgg *pg) {
+    for (int i = 0; i < pg->ntev; i++) cudaEventDestroy(pg->tev[i]);
+    free(pg->tev);
+    pg->tev = NULL;
+    pg->ntev = 0;
+}
+
 static PAgg *pagg_begin(VgAgg *A, Plan *P, VgAggLaunch *L, const VgDBatch *db) {
     const int mode = env_int("VGPU_PAGG", -1);
     if (mode == 0 || !A->sorted || P->n_keys != 1 || P->key[0].op != 0 || P->key[0].a.side != VG_SIDE_PROBE ||
@@ -667,7 +798,28 @@ static PAgg *pagg_begin(VgAgg *A, Plan *P, VgAggLaunch *L, const VgDBatch *db) {
     const double want = d / (0.75 * (double)pg->G);
     int nb = 2;
     while ((double)nb < want && nb < (1 << 20)) nb <<= 1;
-    if (env_int("VGPU_PAGG_BUCKETS", 0) > 1) nb = env_int("VGPU_PAGG_BUCKETS", 0);
+    if (env_int("VGPU_PAGG_BUCKETS", 0) > 1) {
+        nb = env_int("VGPU_PAGG_BUCKETS", 0);
+    } else {
+        /* the recorded (or, while tuning, the next) fan-out of this shape class */
+        char shape[96];
+        snprintf(shape, sizeof(shape), "pagg.r%d.d%d.w%d.a%d", lg2d((double)n), lg2d(d), pg->rw, P->n_accs);
+        if (g_pt_armed < 0) g_pt_armed = env_int("VGPU_PAGG_TUNE", 0) != 0;
+        pt_load();
+        PTune *t = pt_find(shape, g_pt_armed);
+        int doublings = 0;
+        if (t && t->recorded) doublings = t->shift;
+        else if (t) {
+            doublings = t->next;
+            pg->tune = t;
+        }
+        snprintf(g_pt_last_shape, sizeof(g_pt_last_shape), "%s", shape);
+        if (t && t->recorded) {
+            g_pt_last_shift = doublings;
+            g_pt_last_ms = t->ms[doublings];
+        }
+        for (int k = 0; k < doublings && nb < (1 << 20); k++) nb <<= 1;
+    }
     pg->omin = hmm[2] ? hmm[0] : 0;
     const int bits = hmm[2] ? bitlen64(hmm[1] - hmm[0]) : 0;
     int lb = 0;
@@ -787,8 +939,10 @@ static void pagg_batch(PAgg *pg, Plan *P, VgAggLaunch *L, const VgDBatch *db, in
     L->po.rec = R->rec;
     L->po.total = total;
     if (n > 0) {
+        pt_mark(pg);
         const int rc = vgk_agg_launch_jit(L, n, vg_stream());
         if (rc <= 0) vg_fail("partitioned aggregation: %s", rc < 0 ? vgk_jit_error() : "plan not covered");
+        pt_mark(pg);
     }
     L->part = 0;
     /* record ends: the whole bucket (holes marked) or the cursors */
@@ -835,8 +989,10 @@ static void pagg_reduce_launch(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggRe
     B->gc = gc;
     B->ovf = gc + nb;
     B->ticket = ticket;
+    pt_mark(pg);
     if (vgk_pagg_reduce(L, P->fin, P->n_out, pg->G, B, vg_stream()) != 0)
         vg_fail("partitioned aggregation reduce: %s", vgk_jit_error());
+    pt_mark(pg);
 }
 
 static void pagg_reduce_level(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggReduce *B, int nb,
@@ -1188,6 +1344,7 @@ unsigned long long vgpu_pagg_runs(void) { return g_pagg_runs; }
 
 static void pagg_free(PAgg *pg) {
     if (!pg) return;
+    pt_free(pg);
     for (int r = 0; r < pg->n_regions; r++) {
         vg_dfree(pg->reg[r].rec);
         vg_dfree(pg->reg[r].off);
@@ -1363,6 +1520,7 @@ static VecBatch *agg_next_body(VecNode *self) {
     const double t_emit = now_ms();
     if (!pg) g_agg_ms[2] += t_emit - t_loop;
     VecBatch *res = pg ? pagg_end(pg, A, &P, L) : emit_result(A, &P, &T);
+    if (pg) pt_finish(pg);
     if (!pg) g_agg_ms[3] += now_ms() - t_emit;
     if (pg) g_pagg_runs++;
     const int was_pagg = pg != NULL;
