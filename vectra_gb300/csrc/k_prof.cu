@@ -58,6 +58,20 @@ void vgpu_profile_reset(void) {
     for (int i = 0; i < VG_PROF_CLASSES; i++) { g_ms[i] = 0; g_n[i] = 0; }
 }
 
+// profiling on for a while (the partitioned path's fan-out tuning times
+// its launches with it): the previous state, to restore
+int vg_prof_force_on(void) {
+    resolve();
+    const int prev = g_on ? 1 : 0;
+    g_on = true;
+    return prev;
+}
+
+void vg_prof_restore(int prev) {
+    resolve();
+    g_on = prev != 0;
+}
+
 // total milliseconds and launches of a kernel class since the last reset
 double vgpu_profile_ms(int cls, unsigned long long *launches) {
     resolve();

@@ -26,7 +26,6 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
-#include <cuda_runtime_api.h>
 #include "vg_host.h"
 
 typedef struct {
@@ -597,8 +596,8 @@ typedef struct {
     VgHostBufs *hb;                /* result columns, faulted in while the device works */
     size_t hb_bytes;               /* bytes of each */
     struct PTune *tune;            /* fan-out being tuned by this query, or NULL */
-    cudaEvent_t *tev;              /* pairs around its partition and reducer launches */
-    int ntev, tev_cap;
+    int prof_prev;                 /* kernel timing state before the tuning query */
+    double prof_base;              /* partition + reducer milliseconds before it */
 } PAgg;
 
 /* Host wall time of the partitioned path's phases, summed since load
@@ -722,32 +721,24 @@ static int lg2d(double x) {
     return b;
 }
 
-static void pt_mark(PAgg *pg) {
-    if (!pg->tune) return;
-    if (pg->ntev == pg->tev_cap) {
-        pg->tev_cap = pg->tev_cap ? 2 * pg->tev_cap : 32;
-        cudaEvent_t *e = (cudaEvent_t *)realloc(pg->tev, (size_t)pg->tev_cap * sizeof(cudaEvent_t));
-        if (!e) vg_fail("host allocation failed");
-        pg->tev = e;
-    }
-    cudaEvent_t *e = &pg->tev[pg->ntev];
-    if (cudaEventCreate(e) != cudaSuccess || cudaEventRecord(*e, (cudaStream_t)vg_stream()) != cudaSuccess) {
-        cudaGetLastError();
-        vg_fail("partitioned aggregation: timing event");
-    }
-    pg->ntev++;
+/* the partition and reducer launches' device time so far (events around
+ * each launch, recorded after its kernel is compiled) */
+static double pt_kernel_ms(void) {
+    return vgpu_profile_ms(VG_PROF_CLASS_AGG, NULL) + vgpu_profile_ms(VG_PROF_CLASS_PAGG, NULL);
+}
+
+static void pt_start(PAgg *pg) {
+    pg->prof_prev = vg_prof_force_on();
+    pg->prof_base = pt_kernel_ms();
 }
 
 /* after the query's last launch: its time for the candidate it ran */
 static void pt_finish(PAgg *pg) {
     if (!pg->tune) return;
-    vg_sync();
-    double ms = 0.0;
-    for (int i = 0; i + 1 < pg->ntev; i += 2) {
-        float m = 0.f;
-        if (cudaEventElapsedTime(&m, pg->tev[i], pg->tev[i + 1]) == cudaSuccess) ms += m;
-    }
+    const double ms = pt_kernel_ms() - pg->prof_base;
+    vg_prof_restore(pg->prof_prev);
     PTune *t = pg->tune;
+    pg->tune = NULL;
     t->ms[t->next] = ms;
     g_pt_last_shift = t->next;
     g_pt_last_ms = ms;
@@ -761,11 +752,10 @@ static void pt_finish(PAgg *pg) {
     }
 }
 
+/* a tuning query that failed: its candidate is tried again next time */
 static void pt_free(PAgg *pg) {
-    for (int i = 0; i < pg->ntev; i++) cudaEventDestroy(pg->tev[i]);
-    free(pg->tev);
-    pg->tev = NULL;
-    pg->ntev = 0;
+    if (pg->tune) vg_prof_restore(pg->prof_prev);
+    pg->tune = NULL;
 }
 
 static PAgg *pagg_begin(VgAgg *A, Plan *P, VgAggLaunch *L, const VgDBatch *db) {
@@ -812,6 +802,7 @@ static PAgg *pagg_begin(VgAgg *A, Plan *P, VgAggLaunch *L, const VgDBatch *db) {
         else if (t) {
             doublings = t->next;
             pg->tune = t;
+            pt_start(pg);
         }
         snprintf(g_pt_last_shape, sizeof(g_pt_last_shape), "%s", shape);
         if (t && t->recorded) {
@@ -939,10 +930,8 @@ static void pagg_batch(PAgg *pg, Plan *P, VgAggLaunch *L, const VgDBatch *db, in
     L->po.rec = R->rec;
     L->po.total = total;
     if (n > 0) {
-        pt_mark(pg);
         const int rc = vgk_agg_launch_jit(L, n, vg_stream());
         if (rc <= 0) vg_fail("partitioned aggregation: %s", rc < 0 ? vgk_jit_error() : "plan not covered");
-        pt_mark(pg);
     }
     L->part = 0;
     /* record ends: the whole bucket (holes marked) or the cursors */
@@ -989,10 +978,8 @@ static void pagg_reduce_launch(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggRe
     B->gc = gc;
     B->ovf = gc + nb;
     B->ticket = ticket;
-    pt_mark(pg);
     if (vgk_pagg_reduce(L, P->fin, P->n_out, pg->G, B, vg_stream()) != 0)
         vg_fail("partitioned aggregation reduce: %s", vgk_jit_error());
-    pt_mark(pg);
 }
 
 static void pagg_reduce_level(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggReduce *B, int nb,

@@ -82,6 +82,14 @@ void vg_copy_after_main(void);
 void vg_d2h_copy(void *dst, const void *src, size_t bytes);
 void vg_copy_sync(void);
 /* n host buffers of `bytes` each, faulted in by background threads */
+/* kernel timing (k_prof.cu): classes 0 the aggregation kernel, 5 the
+ * partitioned path's bucket reducer */
+int vg_prof_force_on(void);
+void vg_prof_restore(int prev);
+double vgpu_profile_ms(int cls, unsigned long long *launches);
+#define VG_PROF_CLASS_AGG 0
+#define VG_PROF_CLASS_PAGG 5
+
 typedef struct VgHostBufs VgHostBufs;
 VgHostBufs *vg_host_bufs_begin(int n, size_t bytes);
 void vg_host_bufs_wait(VgHostBufs *h);
