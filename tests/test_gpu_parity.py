@@ -136,6 +136,47 @@ def test_join_agg_exact(G):
         assert out["s"][0][g] == exact_sum_products(fv[m], ww[m])
 
 
+def test_join_agg_exact_wide_range(G):
+    """The same plan with values spread over 600 decimal orders: most rows
+    fall outside their CTA's digit window, are marked for the replay kernel
+    and reach the global table there.  Every sum is still the exactly
+    rounded sum of the rounded products, every mean that sum over the
+    valid rows, every n() exact -- with and without na.rm."""
+    from vectra_gb300.plan import tbl, col
+    rng = np.random.default_rng(17)
+    nf, nd = 300_000, 7000
+    ids = rng.permutation(nd) + 1
+    fk = rng.integers(1, nd + 1, nf)
+    fv = rng.normal(0, 1, nf) * 10.0 ** rng.integers(-300, 300, nf)
+    cat = rng.integers(0, 12, nd)
+    w = rng.uniform(0.5, 2.0, nd)
+    pos = np.empty(nd + 1, np.int64)
+    pos[ids] = np.arange(nd)
+    c = cat[pos[fk]]
+    ww = w[pos[fk]]
+    fvv = ~((c < 6) & (rng.random(nf) < 0.02))        # NA values in half of the groups
+    fv[~fvv] = 0.0
+    fact = {"key": fk, "value": (fv, fvv)}
+    dim = {"id": ids, "category": cat, "weight": w}
+    for na_rm in (True, False):
+        out = (tbl(G, fact, batch_rows=1 << 17)
+               .left_join(tbl(G, dim), {"key": "id"})
+               .group_by("category").summarise(temp_dir="tmp", s=("sum", col("value") * col("weight"), na_rm),
+                                               m=("mean", col("value") * col("weight"), na_rm),
+                                               n=("n",)).collect())
+        for g in range(12):
+            m = c == g
+            assert out["category"][0][g] == g
+            assert out["n"][0][g] == m.sum()
+            ok = m & fvv
+            if not na_rm and (m & ~fvv).any():
+                assert not out["s"][1][g] and not out["m"][1][g]
+                continue
+            want = exact_sum_products(fv[ok], ww[ok])
+            assert out["s"][0][g] == want, (g, out["s"][0][g], want)
+            assert out["m"][0][g] == want / ok.sum()
+
+
 def test_specialised_kernel_ran(G):
     """The group cases above ran through the run-time specialised kernel."""
     import vectra_gb300
