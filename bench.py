@@ -715,27 +715,28 @@ def workload_arm(args):
         n, distinct = 200_000_000 // args.scale, 50_000_000 // args.scale
         cols, raw = W.gen_high_card(torch, n, distinct, 0, dev)
         run = lambda numpy=False: W.run_high_card(eng, W.device_source(lib, cols, n)[0], numpy=numpy)
-        # the fan-out is tuned on the first three queries (untimed; the
-        # first is also the checked one) and the fastest kept
+        # the fan-out and reducer shape are tuned on the first five queries
+        # (untimed; the first is also the checked one) and the fastest kept
         import tempfile
         os.environ.setdefault("VGPU_TUNE_FILE", os.path.join(tempfile.mkdtemp(prefix="vgpu_tune_"), "tune.txt"))
         lib.vgpu_pagg_tune.argtypes = [C.c_int]
         lib.vgpu_pagg_tuned.restype = C.c_int
-        lib.vgpu_pagg_tuned.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_double)]
-        shape, tms = C.create_string_buffer(96), C.c_double(0)
+        lib.vgpu_pagg_tuned.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        shape, tctas, tms = C.create_string_buffer(96), C.c_int(0), C.c_double(0)
         lib.vgpu_pagg_tune(1)
         out = run(True)
-        cands = [(lib.vgpu_pagg_tuned(shape, 96, C.byref(tms)), tms.value)]
-        for _ in range(2):
+        cands = [(lib.vgpu_pagg_tuned(shape, 96, C.byref(tctas), C.byref(tms)), tctas.value, tms.value)]
+        for _ in range(4):
             run()
-            cands.append((lib.vgpu_pagg_tuned(shape, 96, C.byref(tms)), tms.value))
+            cands.append((lib.vgpu_pagg_tuned(shape, 96, C.byref(tctas), C.byref(tms)), tctas.value, tms.value))
         lib.vgpu_pagg_tune(0)
         run()
-        kept = lib.vgpu_pagg_tuned(shape, 96, C.byref(tms))
-        fanout = {"shape_class": shape.value.decode(), "doublings_kept": kept,
-                  "candidates_ms": {"x%d" % (1 << k): round(v, 3) for k, v in cands},
-                  "what": "bucket count = the key sketch's count x 1, 2, 4; device time of the partition and "
-                          "reducer launches of one query each; the fastest kept and recorded (VGPU_TUNE_FILE)"}
+        kept = lib.vgpu_pagg_tuned(shape, 96, C.byref(tctas), C.byref(tms))
+        fanout = {"shape_class": shape.value.decode(), "kept": {"doublings": kept, "reducer_ctas_per_sm": tctas.value},
+                  "candidates_ms": {"x%d/%dcta" % (1 << k, c): round(v, 3) for k, c, v in cands},
+                  "what": "bucket count = the key sketch's count x 1, 2, 4 with one reducer CTA of 1024 threads "
+                          "per SM, x 1, 2 with two of 512 (half the groups each); device time of the partition "
+                          "and reducer launches of one query each; the fastest kept and recorded (VGPU_TUNE_FILE)"}
         groups = W.check_high_card(torch, out, cols, raw, distinct)
         del raw
         algo = W.high_card_bytes(n, groups)

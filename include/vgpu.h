@@ -130,19 +130,21 @@ long        vgpu_warning_count(void);
  * the plan allows it, VGPU_PAGG_MIN_ROWS / VGPU_PAGG_MIN_GROUPS the
  * thresholds otherwise (4Mi rows, 256Ki estimated groups). */
 unsigned long long vgpu_pagg_runs(void);
-/* Fan-out (bucket count) of the partitioned path, tuned per shape class
- * (rows of the first batch, estimated groups, record words, accumulators,
- * each as a power of two).  With tuning on (vgpu_pagg_tune(1), or
- * VGPU_PAGG_TUNE=1), the first queries of a shape class without a record
- * run the sketch's bucket count, twice it and four times it, one per
- * query (each a complete, correct query), timed by the device time of
- * their partition and reducer launches; the fastest is kept for the rest
- * of the process and appended to the file named by VGPU_TUNE_FILE, from
- * which later processes read it.  vgpu_pagg_tuned: the last decision --
- * the doublings over the sketch's count (-1: none yet), its shape class
- * and its measured milliseconds. */
+/* Fan-out (bucket count) and reducer shape of the partitioned path, tuned
+ * per shape class (rows of the first batch, estimated groups, record
+ * words, accumulators, each as a power of two).  With tuning on
+ * (vgpu_pagg_tune(1), or VGPU_PAGG_TUNE=1), the first five queries of a
+ * shape class without a record run, one per query (each a complete,
+ * correct query): the sketch's bucket count x1, x2, x4 with one reducer
+ * CTA of 1024 threads per SM, then x1 and x2 with two CTAs of 512 threads
+ * per SM (each holding half the groups); they are timed by the device
+ * time of their partition and reducer launches, the fastest is kept for
+ * the rest of the process and appended to the file named by
+ * VGPU_TUNE_FILE, from which later processes read it.  vgpu_pagg_tuned:
+ * the last decision -- its doublings over the sketch's count (-1: none
+ * yet), shape class, reducer CTAs per SM and measured milliseconds. */
 void        vgpu_pagg_tune(int on);
-int         vgpu_pagg_tuned(char *shape, int shape_bytes, double *ms);
+int         vgpu_pagg_tuned(char *shape, int shape_bytes, int *ctas, double *ms);
 /* Host wall time (ms, summed since load) of the partitioned path's phases:
  * 0 sketch, 1 partition pass, 2 bucket reducer, 3 compaction into the
  * output columns, 4 waiting for the host result buffers, 5 copy to host,

@@ -200,30 +200,32 @@ def test_window_rounding_matches_general(G):
 
 
 def test_fanout_tuning(G, oracle, force, tmp_path):
-    """Tuning on: the first three queries of a new shape class run the
-    sketch's bucket count, twice it and four times it -- each result equal
-    to the oracle's -- the fastest is appended to the tuning file and the
-    fourth query runs it."""
+    """Tuning on: the first five queries of a new shape class run the
+    sketch's bucket count x1, x2, x4 with one reducer CTA per SM and x1, x2
+    with two -- each result equal to the oracle's -- the fastest is
+    appended to the tuning file and the sixth query runs it."""
     tune = tmp_path / "tune.txt"
     force.setenv("VGPU_TUNE_FILE", str(tune))
     lib = G.lib
     lib.vgpu_pagg_tuned.restype = C.c_int
-    lib.vgpu_pagg_tuned.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_double)]
+    lib.vgpu_pagg_tuned.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     lib.vgpu_pagg_tune.argtypes = [C.c_int]
     t = high_card_table(11, 300_007, 90_001)
     want = five_aggs(oracle, t, oracle.tmp)
     shape = C.create_string_buffer(96)
+    ctas = C.c_int(0)
     ms = C.c_double(0)
     lib.vgpu_pagg_tune(1)
     try:
         seen = []
-        for i in range(4):
+        for i in range(6):
             cases.same_batches(five_aggs(G, t, oracle.tmp), want, rtol=RTOL, tol_cols=FP_COLS)
-            seen.append(lib.vgpu_pagg_tuned(shape, 96, C.byref(ms)))
+            d = lib.vgpu_pagg_tuned(shape, 96, C.byref(ctas), C.byref(ms))
+            seen.append((d, ctas.value))
             assert ms.value > 0.0
-        assert seen[:3] == [0, 1, 2], seen
+        assert seen[:5] == [(0, 1), (1, 1), (2, 1), (0, 2), (1, 2)], seen
         lines = [ln.split() for ln in tune.read_text().splitlines() if ln.startswith("pagg.")]
         assert len(lines) == 1 and lines[0][0] == shape.value.decode(), lines
-        assert int(lines[0][2]) == seen[3] and lines[0][5] == "3", lines
+        assert (int(lines[0][2]), int(lines[0][1])) == seen[5] and lines[0][5] == "5", (lines, seen)
     finally:
         lib.vgpu_pagg_tune(0)

@@ -660,7 +660,8 @@ constexpr uint64_t kPaggSmem = 226 * 1024;   // dynamic shared memory of one red
 
 int hash_slots(int G) { return next_pow2(2 * G); }
 
-std::string gen_pagg_source(const VgAggLaunch &L, const VgFinish *fin, int n_out, int G, int threads) {
+std::string gen_pagg_source(const VgAggLaunch &L, const VgFinish *fin, int n_out, int G, int threads,
+                            int minb = 1) {
     const int S = hash_slots(G);
     const PLay c = pagg_lay(L, G, S);
     int acc_val[VG_MAX_ACCS];
@@ -670,7 +671,8 @@ std::string gen_pagg_source(const VgAggLaunch &L, const VgFinish *fin, int n_out
     std::string s;
     s += "// generated by jit_agg.cu (partitioned aggregation, bucket reducer)\n";
     s += "#define VGJ_R 2\n#define VGJ_NPC 1\n#define VGJ_NBC 1\n#include \"k_jit_lib.cuh\"\n";
-    fmt(s, "#define VGP_G %d\n#define VGP_S %d\n#define VGP_RW %d\n#define VGP_THREADS %d\n", G, S, rw, threads);
+    fmt(s, "#define VGP_G %d\n#define VGP_S %d\n#define VGP_RW %d\n#define VGP_THREADS %d\n#define VGP_MINB %d\n", G,
+        S, rw, threads, minb);
     fmt(s, "#define VGP_OFF_HID %lluu\n#define VGP_OFF_GKEY %lluu\n", (unsigned long long)c.hid,
         (unsigned long long)c.gkey);
     s += "#include \"k_jit_pagg.cuh\"\n";
@@ -746,13 +748,17 @@ std::string gen_pagg_source(const VgAggLaunch &L, const VgFinish *fin, int n_out
 extern "C" {
 
 // Groups one reducer CTA holds for this plan (0: the plan does not fit).
-int vgk_pagg_groups(const VgAggLaunch *L) {
+int vgk_pagg_groups_for(const VgAggLaunch *L, int ctas) {
+    // each CTA on an SM also holds about 1 KiB of the SM's shared memory
+    const uint64_t limit = ctas <= 1 ? kPaggSmem : kPaggSmem / (uint64_t)ctas - 1024;
     for (int G = 4096; G >= 256; G -= 256) {
         const PLay c = pagg_lay(*L, G, hash_slots(G));
-        if (c.total <= kPaggSmem) return G;
+        if (c.total <= limit) return G;
     }
     return 0;
 }
+
+int vgk_pagg_groups(const VgAggLaunch *L) { return vgk_pagg_groups_for(L, 1); }
 
 // Record words of the plan's partition records.
 int vgk_pagg_record_words(const VgAggLaunch *L) {
@@ -771,14 +777,15 @@ int vgk_pagg_source(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G,
 
 // Compiles (cached) and launches the bucket reducer: one CTA per SM.
 // 0 on success, -1 with vgk_jit_error() set.
-int vgk_pagg_reduce(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, const VgPaggReduce *B,
+int vgk_pagg_reduce(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, int ctas, const VgPaggReduce *B,
                     vg_stream_t s) {
     if (getenv("VGPU_NO_JIT")) {
         snprintf(g_jit_err, sizeof(g_jit_err), "partitioned aggregation needs the run-time compiler");
         return -1;
     }
-    int threads = 1024;
-    std::string src = gen_pagg_source(*L, fin, n_out, G, threads);
+    if (ctas != 2) ctas = 1;
+    int threads = 1024 / ctas;
+    std::string src = gen_pagg_source(*L, fin, n_out, G, threads, ctas);
     JitKernel *jk;
     {
         std::lock_guard<std::mutex> lock(g_mu);
@@ -790,8 +797,9 @@ int vgk_pagg_reduce(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G,
             if (nvrtc_cubin(src, cubin, &spill, nullptr) != 0) return -1;
             if (spill > 256) {
                 // fewer threads, more registers each
-                threads = 512;
-                if (nvrtc_cubin(gen_pagg_source(*L, fin, n_out, G, threads), cubin, &spill, nullptr) != 0) return -1;
+                threads /= 2;
+                if (nvrtc_cubin(gen_pagg_source(*L, fin, n_out, G, threads, ctas), cubin, &spill, nullptr) != 0)
+                    return -1;
             }
             k.shape.threads = threads;
             if (load_kernel(cubin, k, "vg_jit_pagg") != 0) return -1;
@@ -809,8 +817,8 @@ int vgk_pagg_reduce(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G,
         }
         jk->smem_set = smem;
     }
-    const int sms = vgk_num_sms();
-    const int grid = B->n_buckets < sms ? (B->n_buckets < 1 ? 1 : B->n_buckets) : sms;
+    const int cap = vgk_num_sms() * ctas;
+    const int grid = B->n_buckets < cap ? (B->n_buckets < 1 ? 1 : B->n_buckets) : cap;
     cudaStream_t st = (cudaStream_t)s;
     VgPaggReduce T = *B;
     void *args[] = {(void *)&T};
@@ -827,11 +835,12 @@ int vgk_pagg_reduce(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G,
 }
 
 // Compiles the reducer without launching it (no device needed).
-int vgk_pagg_compile_only(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, int *regs_out) {
+int vgk_pagg_compile_only(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, int threads,
+                          int *regs_out) {
     std::vector<char> cubin;
     int spill = 0;
     std::string log;
-    const int rc = nvrtc_cubin(gen_pagg_source(*L, fin, n_out, G, 1024), cubin, &spill, &log);
+    const int rc = nvrtc_cubin(gen_pagg_source(*L, fin, n_out, G, threads, 1024 / threads), cubin, &spill, &log);
     snprintf(g_jit_err, sizeof(g_jit_err), "%s%.1800s", rc == 0 ? "" : "NVRTC failed:\n", log.c_str());
     if (regs_out) {
         const char *p = strstr(log.c_str(), "Used ");
@@ -1070,6 +1079,9 @@ extern "C" int vgpu_pagg_selftest(int shape, int *regs) {
     VgFinish fin[VG_MAX_OUTS];
     int n_out = 0;
     memset(fin, 0, sizeof(fin));
+    // shapes 2 and 3: the plans of 0 and 1 for two reducer CTAs per SM
+    const int ctas = shape >= 2 ? 2 : 1;
+    if (shape >= 2) shape -= 2;
     if (shape == 0) {
         pagg_plan(L, 0);
         const int kinds[5] = {AGG_SUM, AGG_MEAN, AGG_MIN, AGG_MAX, AGG_COUNT_STAR};
@@ -1090,12 +1102,12 @@ extern "C" int vgpu_pagg_selftest(int shape, int *regs) {
         snprintf(g_jit_err, sizeof(g_jit_err), "no such self-test shape %d", shape);
         return -1;
     }
-    const int G = vgk_pagg_groups(&L);
+    const int G = vgk_pagg_groups_for(&L, ctas);
     if (G <= 0) {
         snprintf(g_jit_err, sizeof(g_jit_err), "plan does not fit the reducer");
         return -1;
     }
-    return vgk_pagg_compile_only(&L, fin, n_out, G, regs);
+    return vgk_pagg_compile_only(&L, fin, n_out, G, 1024 / ctas, regs);
 }
 
 // Host check of the 32-bit digit split against the 64-bit one on n bit

@@ -23,7 +23,8 @@
 //
 // Included by the NVRTC source that jit_agg.cu generates, which defines
 // before inclusion VGP_G (groups per CTA), VGP_S (hash slots), VGP_RW (record words),
-// VGP_THREADS and the layout offsets VGP_OFF_HID / VGP_OFF_GKEY, and after
+// VGP_THREADS, VGP_MINB (CTAs per SM) and the layout offsets VGP_OFF_HID /
+// VGP_OFF_GKEY, and after
 // it the hooks vgp_init, vgp_acc and vgp_finish.
 
 #pragma once
@@ -253,7 +254,7 @@ VG_DEV int find(char *sm, uint64_t key, int *s_ng, int *s_ovf, uint32_t *dead) {
 
 }  // namespace vgp
 
-extern "C" __global__ void __launch_bounds__(VGP_THREADS, 1) vg_jit_pagg(const __grid_constant__ VgPaggReduce B) {
+extern "C" __global__ void __launch_bounds__(VGP_THREADS, VGP_MINB) vg_jit_pagg(const __grid_constant__ VgPaggReduce B) {
     using namespace vgp;
     extern __shared__ __align__(16) char sm[];
     __shared__ int s_bucket, s_ng, s_ovf, s_crowded, s_live;

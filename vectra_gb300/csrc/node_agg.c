@@ -581,6 +581,7 @@ typedef struct {
 
 typedef struct {
     int G;                         /* groups per reducer CTA */
+    int ctas;                      /* reducer CTAs per SM (1 or 2) */
     int rw;                        /* record words */
     int nb;                        /* buckets */
     int shift;
@@ -640,39 +641,47 @@ static int bitlen64(uint64_t x) {
  * first batch.  VGPU_PAGG=0 never, =1 always when the plan allows it
  * (tests); otherwise when the batch has at least VGPU_PAGG_MIN_ROWS
  * logical rows and an estimated VGPU_PAGG_MIN_GROUPS distinct keys. */
-/* ---- fan-out of the partitioned path, tuned per shape class ---------
+/* ---- fan-out and reducer shape of the partitioned path, tuned per shape
+ * class --------------------------------------------------------------
  *
  * The bucket count follows the key sketch: the fewest powers of two that
- * keep each bucket's groups at 3/4 of a reducer CTA's capacity.  Tuning
- * (vgpu_pagg_tune(1) or VGPU_PAGG_TUNE=1) times that count, twice it and
- * four times it -- one per query, on the first queries of a shape class
- * (rows of the first batch, estimated groups, record words, accumulators:
- * powers of two) -- by the device time of the partition and reducer
- * launches, and keeps the fastest; fewer buckets than the sketch's count
- * overflow the reducer's capacity and are not tried.  The choice is
- * appended to the file named by VGPU_TUNE_FILE (the query sets' tuning
- * file; a line "pagg.<shape> 0 <doublings> 0 <ms> <candidates>") and read
- * back by later processes. */
-#define PT_CANDS 3
+ * keep each bucket's groups at 3/4 of a reducer CTA's capacity, one
+ * reducer CTA of 1024 threads per SM.  Tuning (vgpu_pagg_tune(1) or
+ * VGPU_PAGG_TUNE=1) tries, one per query on the first queries of a shape
+ * class (rows of the first batch, estimated groups, record words,
+ * accumulators: powers of two), that count x1, x2 and x4 with one reducer
+ * CTA per SM, and x1 and x2 with two reducer CTAs of 512 threads per SM
+ * (each holding half the groups, so the count itself doubles) -- timed by
+ * the device time of their partition and reducer launches -- and keeps the
+ * fastest.  Fewer buckets than the sketch's count overflow the reducer's
+ * capacity and are not tried.  The choice is appended to the file named by
+ * VGPU_TUNE_FILE (the query sets' tuning file; a line
+ * "pagg.<shape> <reducer CTAs per SM> <doublings> 0 <ms> <candidates>")
+ * and read back by later processes. */
+#define PT_CANDS 5
+static const int kPtDoublings[PT_CANDS] = {0, 1, 2, 0, 1};
+static const int kPtCtas[PT_CANDS] = {1, 1, 1, 2, 2};
 typedef struct PTune {
     char shape[96];
-    int recorded, shift, next;
+    int recorded, cand, next;
     double ms[PT_CANDS];
 } PTune;
 static PTune g_pt[64];
 static int g_pt_n, g_pt_loaded, g_pt_armed = -1;
-static int g_pt_last_shift = -1;
+static int g_pt_last = -1;
 static double g_pt_last_ms;
 static char g_pt_last_shape[96];
 
 void vgpu_pagg_tune(int on) { g_pt_armed = on ? 1 : 0; }
 
-/* The last fan-out decision: the shape class, the doublings over the
- * sketch's bucket count (-1: none yet) and its measured milliseconds. */
-int vgpu_pagg_tuned(char *shape, int shape_bytes, double *ms) {
+/* The last decision: the shape class, the reducer CTAs per SM, the
+ * measured milliseconds; returns the doublings over the sketch's bucket
+ * count (-1: none yet). */
+int vgpu_pagg_tuned(char *shape, int shape_bytes, int *ctas, double *ms) {
     if (shape && shape_bytes > 0) snprintf(shape, (size_t)shape_bytes, "%s", g_pt_last_shape);
     if (ms) *ms = g_pt_last_ms;
-    return g_pt_last_shift;
+    if (ctas) *ctas = g_pt_last >= 0 ? kPtCtas[g_pt_last] : 0;
+    return g_pt_last >= 0 ? kPtDoublings[g_pt_last] : -1;
 }
 
 static PTune *pt_find(const char *shape, int create) {
@@ -697,11 +706,16 @@ static void pt_load(void) {
     long long chunk = 0;
     double ms = 0;
     while (fscanf(f, "%95s %d %lld %d %lf %d", shape, &threads, &chunk, &mult, &ms, &cands) == 6) {
-        if (strncmp(shape, "pagg.", 5) != 0 || chunk < 0 || chunk >= PT_CANDS) continue;
+        if (strncmp(shape, "pagg.", 5) != 0) continue;
+        int c = -1;
+        for (int k = 0; k < PT_CANDS; k++)
+            if (kPtCtas[k] == threads && kPtDoublings[k] == chunk) c = k;
+        if (c < 0) continue;
         PTune *t = pt_find(shape, 1);
         if (!t) break;
         t->recorded = 1;           /* the last line of a shape wins */
-        t->shift = (int)chunk;
+        t->cand = c;
+        t->ms[c] = ms;
     }
     fclose(f);
 }
@@ -711,7 +725,7 @@ static void pt_save(const PTune *t, double ms) {
     if (!path || !*path) return;
     FILE *f = fopen(path, "a");
     if (!f) return;
-    fprintf(f, "%s 0 %d 0 %.6f %d\n", t->shape, t->shift, ms, PT_CANDS);
+    fprintf(f, "%s %d %d 0 %.6f %d\n", t->shape, kPtCtas[t->cand], kPtDoublings[t->cand], ms, PT_CANDS);
     fclose(f);
 }
 
@@ -740,13 +754,13 @@ static void pt_finish(PAgg *pg) {
     PTune *t = pg->tune;
     pg->tune = NULL;
     t->ms[t->next] = ms;
-    g_pt_last_shift = t->next;
+    g_pt_last = t->next;
     g_pt_last_ms = ms;
     if (++t->next == PT_CANDS) {
         int best = 0;
         for (int c = 1; c < PT_CANDS; c++)
             if (t->ms[c] < t->ms[best]) best = c;
-        t->shift = best;
+        t->cand = best;
         t->recorded = 1;
         pt_save(t, t->ms[best]);
     }
@@ -781,36 +795,48 @@ static PAgg *pagg_begin(VgAgg *A, Plan *P, VgAggLaunch *L, const VgDBatch *db) {
     PAgg *pg = (PAgg *)vg_xcalloc(1, sizeof(PAgg));
     pg->G = env_int("VGPU_PAGG_G", G);          /* a smaller G exercises the bucket split (tests) */
     if (pg->G < 1 || pg->G > G) pg->G = G;
+    pg->ctas = 1;
     L->part = 1;
     pg->rw = vgk_pagg_record_words(L);
     L->part = 0;
-    /* buckets: about 3/4 of G groups each */
-    const double want = d / (0.75 * (double)pg->G);
-    int nb = 2;
-    while ((double)nb < want && nb < (1 << 20)) nb <<= 1;
-    if (env_int("VGPU_PAGG_BUCKETS", 0) > 1) {
-        nb = env_int("VGPU_PAGG_BUCKETS", 0);
-    } else {
-        /* the recorded (or, while tuning, the next) fan-out of this shape class */
+    /* the recorded (or, while tuning, the next) fan-out and reducer shape
+     * of this shape class, unless a test forces the buckets or G */
+    const int forced = env_int("VGPU_PAGG_BUCKETS", 0) > 1 || env_int("VGPU_PAGG_G", 0) > 0;
+    int doublings = 0;
+    if (!forced) {
         char shape[96];
         snprintf(shape, sizeof(shape), "pagg.r%d.d%d.w%d.a%d", lg2d((double)n), lg2d(d), pg->rw, P->n_accs);
         if (g_pt_armed < 0) g_pt_armed = env_int("VGPU_PAGG_TUNE", 0) != 0;
         pt_load();
         PTune *t = pt_find(shape, g_pt_armed);
-        int doublings = 0;
-        if (t && t->recorded) doublings = t->shift;
-        else if (t) {
-            doublings = t->next;
+        int c = 0;
+        if (t && t->recorded) {
+            c = t->cand;
+            g_pt_last = c;
+            g_pt_last_ms = t->ms[c];
+        } else if (t) {
+            c = t->next;
             pg->tune = t;
             pt_start(pg);
         }
         snprintf(g_pt_last_shape, sizeof(g_pt_last_shape), "%s", shape);
-        if (t && t->recorded) {
-            g_pt_last_shift = doublings;
-            g_pt_last_ms = t->ms[doublings];
+        doublings = kPtDoublings[c];
+        if (kPtCtas[c] == 2) {
+            L->part = 1;
+            const int G2 = vgk_pagg_groups_for(L, 2);
+            L->part = 0;
+            if (G2 > 0) {
+                pg->ctas = 2;
+                pg->G = G2;
+            }
         }
-        for (int k = 0; k < doublings && nb < (1 << 20); k++) nb <<= 1;
     }
+    /* buckets: about 3/4 of G groups each */
+    const double want = d / (0.75 * (double)pg->G);
+    int nb = 2;
+    while ((double)nb < want && nb < (1 << 20)) nb <<= 1;
+    if (env_int("VGPU_PAGG_BUCKETS", 0) > 1) nb = env_int("VGPU_PAGG_BUCKETS", 0);
+    for (int k = 0; k < doublings && nb < (1 << 20); k++) nb <<= 1;
     pg->omin = hmm[2] ? hmm[0] : 0;
     const int bits = hmm[2] ? bitlen64(hmm[1] - hmm[0]) : 0;
     int lb = 0;
@@ -978,7 +1004,7 @@ static void pagg_reduce_launch(PAgg *pg, VgAggLaunch *L, const Plan *P, VgPaggRe
     B->gc = gc;
     B->ovf = gc + nb;
     B->ticket = ticket;
-    if (vgk_pagg_reduce(L, P->fin, P->n_out, pg->G, B, vg_stream()) != 0)
+    if (vgk_pagg_reduce(L, P->fin, P->n_out, pg->G, pg->ctas, B, vg_stream()) != 0)
         vg_fail("partitioned aggregation reduce: %s", vgk_jit_error());
 }
 

@@ -536,10 +536,14 @@ unsigned long long vgk_jit_compiles(void);
 
 /* partitioned aggregation (k_pagg.cu, jit_agg.cu) */
 int vgk_pagg_groups(const VgAggLaunch *L);          /* groups per reducer CTA, 0 = does not fit */
+/* the same with `ctas` reducer CTAs sharing one SM's shared memory */
+int vgk_pagg_groups_for(const VgAggLaunch *L, int ctas);
 int vgk_pagg_record_words(const VgAggLaunch *L);
 int vgk_pagg_source(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, char *out, size_t out_bytes);
-int vgk_pagg_compile_only(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, int *regs_out);
-int vgk_pagg_reduce(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, const VgPaggReduce *B,
+int vgk_pagg_compile_only(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, int threads,
+                          int *regs_out);
+/* ctas: reducer CTAs per SM (1: 1024 threads; 2: 512 threads each, G sized for half the shared memory) */
+int vgk_pagg_reduce(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, int ctas, const VgPaggReduce *B,
                     vg_stream_t s);
 const char *vgk_pagg_last_error(void);
 /* distinct-key estimate and the order-word range (min, max, valid count)
