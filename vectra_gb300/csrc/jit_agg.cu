@@ -783,7 +783,7 @@ int vgk_pagg_reduce(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G,
         snprintf(g_jit_err, sizeof(g_jit_err), "partitioned aggregation needs the run-time compiler");
         return -1;
     }
-    if (ctas != 2) ctas = 1;
+    if (ctas != 2 && ctas != 4) ctas = 1;
     int threads = 1024 / ctas;
     std::string src = gen_pagg_source(*L, fin, n_out, G, threads, ctas);
     JitKernel *jk;
@@ -1079,9 +1079,10 @@ extern "C" int vgpu_pagg_selftest(int shape, int *regs) {
     VgFinish fin[VG_MAX_OUTS];
     int n_out = 0;
     memset(fin, 0, sizeof(fin));
-    // shapes 2 and 3: the plans of 0 and 1 for two reducer CTAs per SM
-    const int ctas = shape >= 2 ? 2 : 1;
-    if (shape >= 2) shape -= 2;
+    // shapes 2 and 3: the plans of 0 and 1 for two reducer CTAs per SM;
+    // 4 and 5 for four
+    const int ctas = shape >= 4 ? 4 : shape >= 2 ? 2 : 1;
+    shape %= 2;
     if (shape == 0) {
         pagg_plan(L, 0);
         const int kinds[5] = {AGG_SUM, AGG_MEAN, AGG_MIN, AGG_MAX, AGG_COUNT_STAR};

@@ -581,7 +581,7 @@ typedef struct {
 
 typedef struct {
     int G;                         /* groups per reducer CTA */
-    int ctas;                      /* reducer CTAs per SM (1 or 2) */
+    int ctas;                      /* reducer CTAs per SM (1, 2 or 4) */
     int rw;                        /* record words */
     int nb;                        /* buckets */
     int shift;
@@ -650,17 +650,18 @@ static int bitlen64(uint64_t x) {
  * VGPU_PAGG_TUNE=1) tries, one per query on the first queries of a shape
  * class (rows of the first batch, estimated groups, record words,
  * accumulators: powers of two), that count x1, x2 and x4 with one reducer
- * CTA per SM, and x1 and x2 with two reducer CTAs of 512 threads per SM
- * (each holding half the groups, so the count itself doubles) -- timed by
+ * CTA per SM, x1 and x2 with two reducer CTAs of 512 threads per SM (each
+ * holding half the groups, so the count itself doubles), and x1 with four
+ * of 256 threads (a quarter of the groups each) -- timed by
  * the device time of their partition and reducer launches -- and keeps the
  * fastest.  Fewer buckets than the sketch's count overflow the reducer's
  * capacity and are not tried.  The choice is appended to the file named by
  * VGPU_TUNE_FILE (the query sets' tuning file; a line
  * "pagg.<shape> <reducer CTAs per SM> <doublings> 0 <ms> <candidates>")
  * and read back by later processes. */
-#define PT_CANDS 5
-static const int kPtDoublings[PT_CANDS] = {0, 1, 2, 0, 1};
-static const int kPtCtas[PT_CANDS] = {1, 1, 1, 2, 2};
+#define PT_CANDS 6
+static const int kPtDoublings[PT_CANDS] = {0, 1, 2, 0, 1, 0};
+static const int kPtCtas[PT_CANDS] = {1, 1, 1, 2, 2, 4};
 typedef struct PTune {
     char shape[96];
     int recorded, cand, next;
@@ -821,13 +822,13 @@ static PAgg *pagg_begin(VgAgg *A, Plan *P, VgAggLaunch *L, const VgDBatch *db) {
         }
         snprintf(g_pt_last_shape, sizeof(g_pt_last_shape), "%s", shape);
         doublings = kPtDoublings[c];
-        if (kPtCtas[c] == 2) {
+        if (kPtCtas[c] > 1) {
             L->part = 1;
-            const int G2 = vgk_pagg_groups_for(L, 2);
+            const int Gc = vgk_pagg_groups_for(L, kPtCtas[c]);
             L->part = 0;
-            if (G2 > 0) {
-                pg->ctas = 2;
-                pg->G = G2;
+            if (Gc > 0) {
+                pg->ctas = kPtCtas[c];
+                pg->G = Gc;
             }
         }
     }
