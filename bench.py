@@ -715,7 +715,7 @@ def workload_arm(args):
         n, distinct = 200_000_000 // args.scale, 50_000_000 // args.scale
         cols, raw = W.gen_high_card(torch, n, distinct, 0, dev)
         run = lambda numpy=False: W.run_high_card(eng, W.device_source(lib, cols, n)[0], numpy=numpy)
-        # the fan-out and reducer shape are tuned on the first six queries
+        # the fan-out and reducer shape are tuned on the first seven queries
         # (untimed; the first is also the checked one) and the fastest kept
         import tempfile
         os.environ.setdefault("VGPU_TUNE_FILE", os.path.join(tempfile.mkdtemp(prefix="vgpu_tune_"), "tune.txt"))
@@ -726,7 +726,7 @@ def workload_arm(args):
         lib.vgpu_pagg_tune(1)
         out = run(True)
         cands = [(lib.vgpu_pagg_tuned(shape, 96, C.byref(tctas), C.byref(tms)), tctas.value, tms.value)]
-        for _ in range(5):
+        for _ in range(6):
             run()
             cands.append((lib.vgpu_pagg_tuned(shape, 96, C.byref(tctas), C.byref(tms)), tctas.value, tms.value))
         lib.vgpu_pagg_tune(0)
@@ -735,7 +735,8 @@ def workload_arm(args):
         fanout = {"shape_class": shape.value.decode(), "kept": {"doublings": kept, "reducer_ctas_per_sm": tctas.value},
                   "candidates_ms": {"x%d/%dcta" % (1 << k, c): round(v, 3) for k, c, v in cands},
                   "what": "bucket count = the key sketch's count x 1, 2, 4 with one reducer CTA of 1024 threads "
-                          "per SM, x 1, 2 with two of 512 (half the groups each), x 1 with four of 256; device "
+                          "per SM, x 1, 2 with two of 512 (half the groups each), x 1 with four of 256 and eight of "
+                          "128; device "
                           "time of the partition "
                           "and reducer launches of one query each; the fastest kept and recorded (VGPU_TUNE_FILE)"}
         groups = W.check_high_card(torch, out, cols, raw, distinct)

@@ -133,12 +133,13 @@ unsigned long long vgpu_pagg_runs(void);
 /* Fan-out (bucket count) and reducer shape of the partitioned path, tuned
  * per shape class (rows of the first batch, estimated groups, record
  * words, accumulators, each as a power of two).  With tuning on
- * (vgpu_pagg_tune(1), or VGPU_PAGG_TUNE=1), the first six queries of a
+ * (vgpu_pagg_tune(1), or VGPU_PAGG_TUNE=1), the first seven queries of a
  * shape class without a record run, one per query (each a complete,
  * correct query): the sketch's bucket count x1, x2, x4 with one reducer
  * CTA of 1024 threads per SM, x1 and x2 with two CTAs of 512 threads per
- * SM (each holding half the groups), x1 with four of 256 threads (a
- * quarter each); they are timed by the device
+ * SM (each holding half the groups), x1 with four of 256 threads and x1
+ * with eight of 128 (a quarter / an eighth each); they are timed by the
+ * device
  * time of their partition and reducer launches, the fastest is kept for
  * the rest of the process and appended to the file named by
  * VGPU_TUNE_FILE, from which later processes read it.  vgpu_pagg_tuned:

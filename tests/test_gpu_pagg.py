@@ -200,10 +200,11 @@ def test_window_rounding_matches_general(G):
 
 
 def test_fanout_tuning(G, oracle, force, tmp_path):
-    """Tuning on: the first six queries of a new shape class run the
+    """Tuning on: the first seven queries of a new shape class run the
     sketch's bucket count x1, x2, x4 with one reducer CTA per SM, x1, x2
-    with two and x1 with four -- each result equal to the oracle's -- the
-    fastest is appended to the tuning file and the seventh query runs it."""
+    with two, x1 with four and x1 with eight -- each result equal to the
+    oracle's -- the fastest is appended to the tuning file and the eighth
+    query runs it."""
     tune = tmp_path / "tune.txt"
     force.setenv("VGPU_TUNE_FILE", str(tune))
     lib = G.lib
@@ -218,14 +219,14 @@ def test_fanout_tuning(G, oracle, force, tmp_path):
     lib.vgpu_pagg_tune(1)
     try:
         seen = []
-        for i in range(7):
+        for i in range(8):
             cases.same_batches(five_aggs(G, t, oracle.tmp), want, rtol=RTOL, tol_cols=FP_COLS)
             d = lib.vgpu_pagg_tuned(shape, 96, C.byref(ctas), C.byref(ms))
             seen.append((d, ctas.value))
             assert ms.value > 0.0
-        assert seen[:6] == [(0, 1), (1, 1), (2, 1), (0, 2), (1, 2), (0, 4)], seen
+        assert seen[:7] == [(0, 1), (1, 1), (2, 1), (0, 2), (1, 2), (0, 4), (0, 8)], seen
         lines = [ln.split() for ln in tune.read_text().splitlines() if ln.startswith("pagg.")]
         assert len(lines) == 1 and lines[0][0] == shape.value.decode(), lines
-        assert (int(lines[0][2]), int(lines[0][1])) == seen[6] and lines[0][5] == "6", (lines, seen)
+        assert (int(lines[0][2]), int(lines[0][1])) == seen[7] and lines[0][5] == "7", (lines, seen)
     finally:
         lib.vgpu_pagg_tune(0)

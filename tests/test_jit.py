@@ -37,13 +37,15 @@ def test_digit_split_32bit_matches_64bit():
     assert lib.vgk_digits_selftest(C.c_longlong(4_000_000), C.c_ulonglong(0x9E3779B97F4A7C15)) == 0
 
 
-@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4, 5],
+@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4, 5, 6, 7],
                          ids=["high_card_5_aggs", "every_acc_class", "high_card_5_aggs_two_ctas",
-                              "every_acc_class_two_ctas", "high_card_5_aggs_four_ctas", "every_acc_class_four_ctas"])
+                              "every_acc_class_two_ctas", "high_card_5_aggs_four_ctas", "every_acc_class_four_ctas",
+                              "high_card_5_aggs_eight_ctas", "every_acc_class_eight_ctas"])
 def test_partition_reducer_compiles(shape):
     """The partitioned aggregation's bucket reducer for representative
     plans: compiles for one CTA of 1024 threads per SM, or two of 512 /
-    four of 256 with that share of the groups each, within 64 registers (the exact-sum finish keeps
+    four of 256 / eight of 128 with that share of the groups each, within
+    64 registers (the exact-sum finish keeps
     its 66-digit array on the stack; the per-record path does not spill
     more than a few words)."""
     import vectra_gb300

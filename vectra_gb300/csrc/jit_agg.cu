@@ -783,7 +783,7 @@ int vgk_pagg_reduce(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G,
         snprintf(g_jit_err, sizeof(g_jit_err), "partitioned aggregation needs the run-time compiler");
         return -1;
     }
-    if (ctas != 2 && ctas != 4) ctas = 1;
+    if (ctas != 2 && ctas != 4 && ctas != 8) ctas = 1;
     int threads = 1024 / ctas;
     std::string src = gen_pagg_source(*L, fin, n_out, G, threads, ctas);
     JitKernel *jk;
@@ -1080,8 +1080,8 @@ extern "C" int vgpu_pagg_selftest(int shape, int *regs) {
     int n_out = 0;
     memset(fin, 0, sizeof(fin));
     // shapes 2 and 3: the plans of 0 and 1 for two reducer CTAs per SM;
-    // 4 and 5 for four
-    const int ctas = shape >= 4 ? 4 : shape >= 2 ? 2 : 1;
+    // 4 and 5 for four, 6 and 7 for eight
+    const int ctas = shape >= 6 ? 8 : shape >= 4 ? 4 : shape >= 2 ? 2 : 1;
     shape %= 2;
     if (shape == 0) {
         pagg_plan(L, 0);

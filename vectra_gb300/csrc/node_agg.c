@@ -581,7 +581,7 @@ typedef struct {
 
 typedef struct {
     int G;                         /* groups per reducer CTA */
-    int ctas;                      /* reducer CTAs per SM (1, 2 or 4) */
+    int ctas;                      /* reducer CTAs per SM (1, 2, 4 or 8) */
     int rw;                        /* record words */
     int nb;                        /* buckets */
     int shift;
@@ -652,16 +652,17 @@ static int bitlen64(uint64_t x) {
  * accumulators: powers of two), that count x1, x2 and x4 with one reducer
  * CTA per SM, x1 and x2 with two reducer CTAs of 512 threads per SM (each
  * holding half the groups, so the count itself doubles), and x1 with four
- * of 256 threads (a quarter of the groups each) -- timed by
+ * of 256 threads or eight of 128 (a quarter or an eighth of the groups
+ * each) -- timed by
  * the device time of their partition and reducer launches -- and keeps the
  * fastest.  Fewer buckets than the sketch's count overflow the reducer's
  * capacity and are not tried.  The choice is appended to the file named by
  * VGPU_TUNE_FILE (the query sets' tuning file; a line
  * "pagg.<shape> <reducer CTAs per SM> <doublings> 0 <ms> <candidates>")
  * and read back by later processes. */
-#define PT_CANDS 6
-static const int kPtDoublings[PT_CANDS] = {0, 1, 2, 0, 1, 0};
-static const int kPtCtas[PT_CANDS] = {1, 1, 1, 2, 2, 4};
+#define PT_CANDS 7
+static const int kPtDoublings[PT_CANDS] = {0, 1, 2, 0, 1, 0, 0};
+static const int kPtCtas[PT_CANDS] = {1, 1, 1, 2, 2, 4, 8};
 typedef struct PTune {
     char shape[96];
     int recorded, cand, next;

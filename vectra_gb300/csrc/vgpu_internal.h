@@ -542,8 +542,8 @@ int vgk_pagg_record_words(const VgAggLaunch *L);
 int vgk_pagg_source(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, char *out, size_t out_bytes);
 int vgk_pagg_compile_only(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, int threads,
                           int *regs_out);
-/* ctas: reducer CTAs per SM (1: 1024 threads; 2 or 4: 512 or 256 threads each, G sized for that share
- * of the shared memory) */
+/* ctas: reducer CTAs per SM (1: 1024 threads; 2, 4 or 8: 512, 256 or 128 threads each, G sized for
+ * that share of the shared memory) */
 int vgk_pagg_reduce(const VgAggLaunch *L, const VgFinish *fin, int n_out, int G, int ctas, const VgPaggReduce *B,
                     vg_stream_t s);
 const char *vgk_pagg_last_error(void);
