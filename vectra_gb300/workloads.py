@@ -28,8 +28,17 @@ def _validity(torch, mask):
     return (m.view(-1, 8) * w).sum(dim=1, dtype=torch.uint8)
 
 
-def device_source(lib, cols, n_rows, batch_rows=None):
-    """A VGPU_SRC_DEVICE table source over {name: (values, valid_mask or None)}."""
+def pack_columns(torch, cols):
+    """{name: (values, valid_mask or None)} with each mask packed once into
+    the validity bitmap the table source reads (for device_source(...,
+    packed=True): the queries then start from device-resident columns and
+    bitmaps, as a host keeps them)."""
+    return {k: (v, _validity(torch, m) if m is not None else None) for k, (v, m) in cols.items()}
+
+
+def device_source(lib, cols, n_rows, batch_rows=None, packed=False):
+    """A VGPU_SRC_DEVICE table source over {name: (values, valid_mask or
+    None)}, or over already packed bitmaps (packed=True, pack_columns)."""
     names = list(cols)
     keep = []
     data = (C.c_void_p * len(names))()
@@ -40,8 +49,11 @@ def device_source(lib, cols, n_rows, batch_rows=None):
         data[i] = v.data_ptr()
         types[i] = 1 if v.dtype.is_floating_point else 0
         if m is not None:
-            import torch
-            bits = _validity(torch, m)
+            if packed:
+                bits = m
+            else:
+                import torch
+                bits = _validity(torch, m)
             keep.append(bits)
             val[i] = bits.data_ptr()
         else:
