@@ -155,7 +155,10 @@ double      vgpu_pagg_phase_ms(int phase);
 /* The same for the hash-table aggregation path: 0 planning before the
  * first batch (join build included), 1 the join build alone, 2 the
  * aggregation launches and their synchronisations, 3 the result
- * (compaction, order, finish, copy to host), 4 the whole next_batch call. */
+ * (compaction, order, finish, copy to host), 4 the whole next_batch call.
+ * The launches over a dense group cache are not waited for batch by batch:
+ * their status is read back with the result's first read-back, so the
+ * wait for them counts in 3. */
 double      vgpu_agg_phase_ms(int phase);
 
 /* Optional kernel timing: CUDA events recorded on the launching stream

@@ -457,14 +457,20 @@ static int run_batch(Plan *P, Table *T, VgAggLaunch *L, Spill *S, int64_t n_logi
     }
 }
 
-/* the status of deferred launches (dense cache): an error, or rows that
- * left the cache (which a dense cache cannot lose), fails the call */
-static void check_deferred(Table *T, Spill *S) {
-    uint32_t *hw = (uint32_t *)vg_pinned_scratch(16);
+/* The status of deferred launches (dense cache): queued for the host
+ * behind them (no wait here); check_deferred reads it once the stream has
+ * synchronised -- the result's first read-back waits for it. */
+static uint32_t *queue_deferred_status(Table *T, Spill *S) {
+    uint32_t *hw = vg_pinned_status();
     vg_d2h(hw, S->counters, 8);
     vg_d2h(hw + 2, T->gt.err, 4);
-    vg_sync();
     S->deferred = 0;
+    return hw;
+}
+
+/* an error, or rows that left the cache (which a dense cache cannot lose),
+ * fails the call */
+static void check_deferred(const uint32_t *hw) {
     const uint32_t err = hw[2];
     if (err & (VG_ERR_WAIT | VG_ERR_PROG)) vg_fail("group-agg kernel error (code %u)", err);
     if ((err & (VG_ERR_FULL | VG_ERR_SPILL)) || hw[0] || hw[1])
@@ -474,11 +480,12 @@ static void check_deferred(Table *T, Spill *S) {
 /* results up to this size are read back in one page-locked copy */
 #define kSmallResultBytes ((size_t)8 << 20)
 
-static VecBatch *emit_result(VgAgg *A, Plan *P, Table *T) {
+static VecBatch *emit_result(VgAgg *A, Plan *P, Table *T, const uint32_t *deferred) {
     GroupAggNode *ga = &A->ga;
     uint32_t n = 0;
     int32_t *d_slots = (int32_t *)vg_dmalloc((size_t)T->gt.cap * 4 + 16);
     vg_check_rc(vgk_group_table_compact(&T->gt, d_slots, &n, vg_stream()), "group compact");
+    if (deferred) check_deferred(deferred);     /* read back behind the launches, before the count */
     int64_t ng = n;
     if (ng > 1 && ga->n_keys > 0) {
         size_t sb = vgk_order_scratch_bytes(ng);
@@ -613,7 +620,8 @@ static double g_pagg_ms[7];
  * 0 planning before the first batch (join build included), 1 the join
  * build alone, 2 the aggregation launches and their synchronisations, 3
  * the result (compaction, order, finish, copy to host), 4 the whole
- * next_batch call. */
+ * next_batch call.  A dense cache's launches are waited for in 3 (their
+ * status comes back with the result's first read-back). */
 static double g_agg_ms[5];
 
 double vgpu_agg_phase_ms(int phase) { return phase >= 0 && phase < 5 ? g_agg_ms[phase] : 0.0; }
@@ -1531,10 +1539,10 @@ static VecBatch *agg_next_body(VecNode *self) {
         stream_pos += n_logical;
         batch_idx++;
     }
-    if (S.deferred) check_deferred(&T, &S);
+    const uint32_t *deferred = S.deferred ? queue_deferred_status(&T, &S) : NULL;
     const double t_emit = now_ms();
     if (!pg) g_agg_ms[2] += t_emit - t_loop;
-    VecBatch *res = pg ? pagg_end(pg, A, &P, L) : emit_result(A, &P, &T);
+    VecBatch *res = pg ? pagg_end(pg, A, &P, L) : emit_result(A, &P, &T, deferred);
     if (pg) pt_finish(pg);
     if (!pg) g_agg_ms[3] += now_ms() - t_emit;
     if (pg) g_pagg_runs++;

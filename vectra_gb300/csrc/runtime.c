@@ -372,6 +372,20 @@ void vg_sync(void) {
 static void *g_pin = NULL;
 static size_t g_pin_bytes = 0;
 
+/* 256 page-locked bytes of status words, apart from the scratch above (a
+ * status copy can stay in flight while the scratch is regrown) */
+static void *g_stat_pin = NULL;
+uint32_t *vg_pinned_status(void) {
+    if (!g_stat_pin) {
+        cudaError_t e = cudaMallocHost(&g_stat_pin, 256);
+        if (e != cudaSuccess) {
+            g_stat_pin = NULL;
+            vg_fail("page-locked allocation of 256 bytes failed: %s", cudaGetErrorString(e));
+        }
+    }
+    return (uint32_t *)g_stat_pin;
+}
+
 void *vg_pinned_scratch(size_t bytes) {
     if (bytes <= g_pin_bytes) return g_pin;
     size_t nb = 65536;

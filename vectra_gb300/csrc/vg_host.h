@@ -39,6 +39,7 @@ void vg_sync(void);
  * Kept for the process; a larger request replaces it (after a sync), so
  * a caller reads what it copied before asking again. */
 void *vg_pinned_scratch(size_t bytes);
+uint32_t *vg_pinned_status(void);
 
 /* ---- host batches ---- */
 void *vg_xmalloc(size_t n);
