@@ -62,8 +62,9 @@ const Shape &shape() {
 // A dense group key read from a direct join's payload copy (the join +
 // aggregate of a fact table against a dimension) runs two CTAs of 768
 // threads per SM: 48 warps instead of 32 hide more of the payload reads'
-// latency, worth the few registers spilled at that budget (measured on the
-// 100M x 10M join + aggregate: 0.85 ms against 0.95 ms at 1024 x 1).
+// latency (measured on the 100M x 10M join + aggregate: 0.85 ms against
+// 0.95 ms at 1024 x 1, when the 40-register budget still spilled a few
+// words; with the rare rows deferred to the replay kernel it spills none).
 bool occupancy_shape(const VgAggLaunch &L) {
     return !getenv("VGPU_JIT_SHAPE") && L.has_join && L.jpay && L.dense && L.jt.direct && !L.part && !L.sel;
 }
