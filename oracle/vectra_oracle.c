@@ -687,12 +687,83 @@ static VecArray eval(const VecExpr *e, const VecBatch *b) {
         arr_free(&x);
         return o;
     }
-    case EXPR_LIT_STRING:
-    case EXPR_NCHAR:
-    case EXPR_SUBSTR:
-    case EXPR_GREPL:
-        orc_error("oracle: string expressions are outside the restated path");
-        break;
+    case EXPR_LIT_STRING: {   /* the literal repeated per row (src/expr.c:64-77) */
+        const char *lit = e->lit_str ? e->lit_str : "";
+        const int64_t l = (int64_t)strlen(lit);
+        VecArray o = arr_alloc(VEC_STRING, n);
+        set_all_valid(&o);
+        o.buf.str.data = (char *)xmalloc((size_t)(l * n > 0 ? l * n : 1));
+        o.buf.str.data_len = l * n;
+        for (int64_t i = 0; i < n; i++) {
+            o.buf.str.offsets[i] = i * l;
+            memcpy(o.buf.str.data + i * l, lit, (size_t)l);
+        }
+        o.buf.str.offsets[n] = l * n;
+        return o;
+    }
+    case EXPR_NCHAR: {        /* byte length (src/expr.c:153-170) */
+        VecArray x = eval(e->operand, b);
+        if (x.type != VEC_STRING) { arr_free(&x); orc_error("nchar: argument must be string"); }
+        VecArray o = arr_alloc(VEC_INT64, x.length);
+        for (int64_t i = 0; i < x.length; i++) {
+            if (!is_valid(&x, i)) continue;
+            set_valid(&o, i);
+            o.buf.i64[i] = x.buf.str.offsets[i + 1] - x.buf.str.offsets[i];
+        }
+        arr_free(&x);
+        return o;
+    }
+    case EXPR_SUBSTR: {       /* 1-based, inclusive stop (src/expr.c:172-235) */
+        VecArray x = eval(e->operand, b);
+        VecArray a0 = eval(e->left, b), a1 = eval(e->right, b);
+        if (x.type != VEC_STRING) {
+            arr_free(&x); arr_free(&a0); arr_free(&a1);
+            orc_error("substr: first argument must be string");
+        }
+        /* start and stop as int64: doubles truncated toward zero */
+        VecArray st = arr_coerce(&a0, a0.type == VEC_DOUBLE ? VEC_DOUBLE : VEC_INT64);
+        VecArray sp = arr_coerce(&a1, a1.type == VEC_DOUBLE ? VEC_DOUBLE : VEC_INT64);
+        const int64_t m = x.length;
+        VecArray o = arr_alloc(VEC_STRING, m);
+        int64_t cap = x.buf.str.data_len > 0 ? x.buf.str.data_len : 1, at = 0;
+        o.buf.str.data = (char *)xmalloc((size_t)cap);
+        for (int64_t i = 0; i < m; i++) {
+            o.buf.str.offsets[i] = at;
+            if (!is_valid(&x, i) || !is_valid(&st, i) || !is_valid(&sp, i)) continue;
+            set_valid(&o, i);
+            const int64_t so = x.buf.str.offsets[i], sl = x.buf.str.offsets[i + 1] - so;
+            int64_t from = (st.type == VEC_DOUBLE ? (int64_t)st.buf.dbl[i] : st.buf.i64[i]) - 1;
+            int64_t to = sp.type == VEC_DOUBLE ? (int64_t)sp.buf.dbl[i] : sp.buf.i64[i];
+            if (from < 0) from = 0;
+            if (to > sl) to = sl;
+            if (to > from) {
+                memcpy(o.buf.str.data + at, x.buf.str.data + so + from, (size_t)(to - from));
+                at += to - from;
+            }
+        }
+        o.buf.str.offsets[m] = at;
+        o.buf.str.data_len = at;
+        arr_free(&x); arr_free(&a0); arr_free(&a1); arr_free(&st); arr_free(&sp);
+        return o;
+    }
+    case EXPR_GREPL: {        /* fixed substring search (src/expr.c:237-268) */
+        VecArray x = eval(e->operand, b);
+        if (x.type != VEC_STRING) { arr_free(&x); orc_error("grepl: argument must be string"); }
+        const char *pat = e->lit_str ? e->lit_str : "";
+        const int64_t pl = (int64_t)strlen(pat);
+        VecArray o = arr_alloc(VEC_BOOL, x.length);
+        for (int64_t i = 0; i < x.length; i++) {
+            if (!is_valid(&x, i)) continue;
+            set_valid(&o, i);
+            const char *sv = x.buf.str.data + x.buf.str.offsets[i];
+            const int64_t sl = x.buf.str.offsets[i + 1] - x.buf.str.offsets[i];
+            int hit = 0;
+            for (int64_t j = 0; !hit && j + pl <= sl; j++) hit = memcmp(sv + j, pat, (size_t)pl) == 0;
+            o.buf.bln[i] = (uint8_t)hit;
+        }
+        arr_free(&x);
+        return o;
+    }
     case EXPR_IF_ELSE:
     case EXPR_CAST:
         orc_error("if_else/cast not yet implemented");

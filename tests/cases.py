@@ -10,7 +10,7 @@ sizes and selection vectors.
 """
 import numpy as np
 
-from vectra_gb300.plan import tbl, col, lit, is_na
+from vectra_gb300.plan import tbl, col, lit, is_na, nchar, substr, grepl
 
 NA = None
 
@@ -18,6 +18,8 @@ NA = None
 def vals(x, dtype=None):
     """(values, valid) from a list with None as NA."""
     valid = np.array([v is not None for v in x], dtype=bool)
+    if dtype is None and any(isinstance(v, str) for v in x):
+        return np.array(["" if v is None else v for v in x], dtype=object), valid
     if dtype is None:
         dtype = np.float64 if any(isinstance(v, float) for v in x) else np.int64
     fill = [0 if v is None else v for v in x]
@@ -345,6 +347,126 @@ def r_join(E, seed, n, batch_rows, kind, spread=1):
     r = {"k": (rng.integers(0, 80, 70) * spread, rng.random(70) > 0.05), "y": rng.normal(0, 1, 70),
          "z": rng.integers(0, 5, 70)}
     return getattr(tbl(E, l, batch_rows=batch_rows), kind)(tbl(E, r, batch_rows=32), "k").batches()
+
+
+# --- strings (test-optimize.R:95-148, test-groupby.R:1-150) ---
+
+def sf_nchar(E):                    # test-optimize.R:98-116
+    t = T(s=["abc", NA, "de", "f", "hello", "", "h\u00e9"])
+    return tbl(E, t).mutate(n=nchar(col("s"))).batches()
+
+
+def sf_substr(E):                   # test-optimize.R:118-126
+    t = T(s=["hello", "world", NA, "ab", ""])
+    return tbl(E, t).mutate(sub=substr(col("s"), 1, 3)).batches()
+
+
+def sf_grepl(E):                    # test-optimize.R:128-148
+    t = T(s=["apple", "banana", "grape", "pineapple", NA, "abc", "abcdef", "", "ap"])
+    a = tbl(E, t).filter(grepl("app", col("s"))).batches()
+    b = tbl(E, t).filter(grepl("abc", col("s"))).batches()
+    c = tbl(E, t).filter(grepl("", col("s"))).batches()          # an empty pattern matches
+    return a + b + c
+
+
+def sf_compare_literal(E):          # memcmp, then the shorter first; bytes above 127 unsigned
+    w = ["b", "a", "ab", "abc", "", NA, "B", "\u00e9", "ba", "abd", "b", "aa"]
+    t = T(s=w, i=list(range(len(w))))
+    out = []
+    for op in ("==", "!=", "<", "<=", ">", ">="):
+        out += tbl(E, t).filter(col("s")._cmp(op, "ab")).batches()
+        out += tbl(E, t).filter(lit("b")._cmp(op, col("s"))).batches()
+    return out
+
+
+def sf_compare_columns(E):
+    t = T(a=["x", "ab", NA, "abc", "", "zz", "q"], b=["x", "abc", "q", NA, "a", "z", "q"])
+    return (tbl(E, t).filter(col("a") < col("b")).batches() + tbl(E, t).filter(col("a").eq(col("b"))).batches()
+            + tbl(E, t).filter(~(col("a") >= col("b")) | is_na(col("b"))).batches())
+
+
+def sf_substr_bounds(E):            # start below 1, stop past the end or before start, double bounds
+    t = T(s=["hello", "world", "a", "", NA, "abcdef"], st=[0, 2, 1, 1, 1, -4], sp=[10, 4, 0, 3, 2, 3],
+          x=[2.7, 1.2, -3.5, 1.0, 1.0, 3.99])
+    return tbl(E, t).mutate(a=substr(col("s"), col("st"), col("sp")), b=substr(col("s"), col("x"), 3.9),
+                            c=substr(col("s"), 2, 2), n=nchar(substr(col("s"), 2, 100))).batches()
+
+
+def sf_substr_filter(E):
+    t = T(s=["hello", "help", "shell", "he", NA, "yellow", "ell"])
+    return tbl(E, t).filter(substr(col("s"), 2, 4).eq("ell")).batches()
+
+
+def sf_nchar_filter(E):
+    t = T(s=["abc", "", NA, "hello", "ab"], v=[1, 2, 3, 4, 5])
+    return (tbl(E, t).filter((nchar(col("s")) > 2) | is_na(col("s"))).batches()
+            + tbl(E, t).filter(nchar(col("s")).eq(col("v"))).batches())
+
+
+def sf_passthrough(E):              # string columns carried through filter and select
+    t = T(s=["a", NA, "bb", "ccc", ""], x=[1.0, 2.0, 3.0, 4.0, 5.0], u=["p", "q", NA, "r", "s"])
+    return (tbl(E, t).filter(col("x") > 1.5).select("u", "x", "s").batches()
+            + tbl(E, t).filter(col("u").ne("q")).mutate(y=col("x") * 2.0).batches())
+
+
+def sg_string_key(E, temp_dir):     # test-groupby.R:1-60: first-seen order, NA key group
+    t = T(g=["a", "b", "a", "b", "a", NA, "", NA, "ab"], x=[1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0, 8.0, 9.0])
+    return tbl(E, t).group_by("g").summarise(temp_dir=temp_dir, n=("n",), s=("sum", "x"), m=("mean", "x"),
+                                            lo=("min", "x"), hi=("max", "x")).batches()
+
+
+def sg_string_and_int_keys(E, temp_dir):   # test-groupby.R:61-72 with a string key
+    t = T(a=["x", "x", "y", "y", "x", NA, "y"], b=[1, 2, 1, 1, 1, 2, NA], v=[10, 20, 30, 40, 50, 60, 70])
+    return tbl(E, t).group_by("a", "b").summarise(temp_dir=temp_dir, s=("sum", "v"), n=("n",)).batches()
+
+
+def sg_string_arena_resizes(E, temp_dir):  # test-groupby.R:101-131: many keys, ragged batches
+    rng = np.random.default_rng(55)
+    n, d = 6000, 900
+    base = ["k%04d" % i + "x" * (i % 37) for i in range(d)]
+    pick = rng.integers(0, d, n)
+    g = [base[i] for i in pick]
+    gv = rng.random(n) > 0.03
+    t = {"g": (g, gv), "x": rng.normal(0, 1, n), "i": rng.integers(-50, 50, n)}
+    return (tbl(E, t, batch_rows=700).filter(col("i") > -40).group_by("g")
+            .summarise(temp_dir=temp_dir, s=("sum", "x"), si=("sum", "i"), n=("n",)).batches())
+
+
+def sg_filter_on_string(E, temp_dir):      # a string predicate below a string key
+    t = T(g=["apple", "pear", "apple", "fig", NA, "pear", "fig"], x=[1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0])
+    return (tbl(E, t).filter(grepl("p", col("g")) | is_na(col("g"))).group_by("g")
+            .summarise(temp_dir=temp_dir, s=("sum", "x"), n=("n",)).batches())
+
+
+def random_strings(rng, n, d, maxlen=24):
+    """n strings drawn from d distinct ones with shared prefixes, empty
+    strings and bytes above 127."""
+    alphabet = list("ab\u00e9z") + ["aa", "\u00ff"]
+    pool = []
+    for i in range(d):
+        k = int(rng.integers(0, maxlen))
+        pool.append("".join(alphabet[j] for j in rng.integers(0, len(alphabet), k)))
+    return np.array([pool[i] for i in rng.integers(0, d, n)], dtype=object)
+
+
+def r_string_filter(E, seed, n, batch_rows, sel_mode):
+    rng = np.random.default_rng(seed)
+    t = {"s": (random_strings(rng, n, 60), rng.random(n) > 0.05), "x": rng.normal(0, 1, n)}
+    pred = ((col("s") > "ab") & (nchar(col("s")) <= 9)) | grepl("\u00e9z", col("s")) | substr(col("s"), 2, 3).eq("aa")
+    return tbl(E, t, batch_rows=batch_rows, sel_mode=sel_mode).filter(pred).batches()
+
+
+def r_string_group(E, seed, n, batch_rows, sel_mode, temp_dir):
+    rng = np.random.default_rng(seed)
+    t = {"s": (random_strings(rng, n, max(n // 7, 3)), rng.random(n) > 0.04), "x": rng.normal(0, 1, n),
+         "k": rng.integers(0, 3, n)}
+    return (tbl(E, t, batch_rows=batch_rows, sel_mode=sel_mode).filter(col("x") > -1.5)
+            .group_by("s", "k").summarise(temp_dir=temp_dir, n=("n",), s1=("sum", "x"), c=("count", "x")).batches())
+
+
+STRING_FILTER_CASES = [sf_nchar, sf_substr, sf_grepl, sf_compare_literal, sf_compare_columns, sf_substr_bounds,
+                       sf_substr_filter, sf_nchar_filter, sf_passthrough]
+STRING_GROUP_CASES = [sg_string_key, sg_string_and_int_keys, sg_string_arena_resizes, sg_filter_on_string]
 
 
 FILTER_CASES = [f_simple, f_equality, f_and_or_not, f_na_dropped, f_is_na, f_kleene, f_double_filter,

@@ -77,7 +77,7 @@ def make_oracle_source(table, batch_rows=None, sel_mode=0):
     val = (C.c_void_p * len(names))()
     for i, (t, d, v) in enumerate(zip(types, datas, valids)):
         if t == abi.VEC_STRING:
-            enc = [("" if s is None else str(s)).encode() for s in d]
+            enc = [("" if s is None else str(s)).encode("utf-8", "surrogateescape") for s in d]
             offs = np.zeros(len(enc) + 1, np.int64)
             offs[1:] = np.cumsum([len(e) for e in enc])
             blob = np.frombuffer(b"".join(enc) + b"\0", dtype=np.uint8).copy()
@@ -137,6 +137,11 @@ def exact_sum_products(a, b):
     return port_lib().orc_exact_sum_products(a.ctypes.data, b.ctypes.data, len(a))
 
 
+def _has_strings(table):
+    from vectra_gb300.plan import _table_types
+    return abi.VEC_STRING in _table_types(table)[1]
+
+
 def gpu_engine():
     """libvgpu, fed by its own table source, or -- for batches that carry a
     selection vector (sel_mode=1) -- by the oracle's source node, which is
@@ -146,7 +151,9 @@ def gpu_engine():
 
     class GpuTestEngine(GpuEngine):
         def make_source(self, table, batch_rows=None, sel_mode=0, **opts):
-            if sel_mode:
+            # string columns come as the reference's scan delivers them:
+            # host batches of a foreign source node
+            if sel_mode or _has_strings(table):
                 return make_oracle_source(table, batch_rows, sel_mode)
             return super().make_source(table, batch_rows, **opts)
 

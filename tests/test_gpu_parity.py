@@ -187,13 +187,14 @@ def test_specialised_kernel_ran(G):
 
 
 def test_unsupported_is_an_error(G):
-    """No silent CPU fallback: string keys are rejected explicitly."""
-    from vectra_gb300.plan import tbl, EngineError
+    """No silent CPU fallback: a sum over a string column is rejected
+    explicitly."""
+    from vectra_gb300.plan import EngineError
     from engines import make_oracle_source
     from vectra_gb300.plan import Tbl
     src = make_oracle_source({"s": np.array(["a", "b"], dtype=object), "x": np.array([1.0, 2.0])})
     with pytest.raises(EngineError):
-        Tbl(G, src).group_by("s").summarise(n=("n",)).batches()
+        Tbl(G, src).group_by("x").summarise(t=("sum", "s")).batches()
 
 
 def test_mapped_host_source(G, oracle):

@@ -66,3 +66,32 @@ def test_join_chain_quirk(oracle, ref):
 @pytest.mark.parametrize("n,batch", cases.RAGGED)
 def test_random_sort(n, batch, oracle, ref):
     cases.same_batches(cases.r_sort(oracle, n + 2, n, batch), cases.r_sort(ref, n + 2, n, batch))
+
+
+@pytest.mark.parametrize("case", cases.STRING_FILTER_CASES, ids=lambda f: f.__name__)
+def test_string_filter_cases(case, oracle, ref):
+    """String predicates and projections: nchar, substr, grepl, string
+    comparisons (src/expr.c:153-273, src/scalar_ops.c:78-107)."""
+    cases.same_batches(case(oracle), case(ref))
+
+
+@pytest.mark.parametrize("temp_dir", ["tmp", None], ids=["sorted", "hash"])
+@pytest.mark.parametrize("case", cases.STRING_GROUP_CASES, ids=lambda f: f.__name__)
+def test_string_group_cases(case, temp_dir, oracle, ref):
+    td = None if temp_dir is None else ref.tmp
+    cases.same_batches(case(oracle, td), case(ref, td))
+
+
+@pytest.mark.parametrize("n,batch", [(0, 32), (33, 32), (700, 64), (5000, 1024)])
+@pytest.mark.parametrize("sel_mode", [0, 1])
+def test_random_string_filter(n, batch, sel_mode, oracle, ref):
+    cases.same_batches(cases.r_string_filter(oracle, n + 5, n, batch, sel_mode),
+                       cases.r_string_filter(ref, n + 5, n, batch, sel_mode))
+
+
+@pytest.mark.parametrize("n,batch", [(33, 32), (3000, 256)])
+@pytest.mark.parametrize("temp_dir", ["tmp", None], ids=["sorted", "hash"])
+def test_random_string_group(n, batch, temp_dir, oracle, ref):
+    td = None if temp_dir is None else ref.tmp
+    cases.same_batches(cases.r_string_group(oracle, n + 9, n, batch, 1, td),
+                       cases.r_string_group(ref, n + 9, n, batch, 1, td))

@@ -20,7 +20,8 @@ from vectra_gb300.plan import col, is_na, lit, tbl
 
 MAX_INSNS = 48
 (COL_I64, COL_F64, COL_BOOL, LIT_I64, LIT_F64, LIT_BOOL, LIT_NA, I2F, ARITH_I64, ARITH_F64, CMP_I64, CMP_F64,
- AND, OR, NOT, IS_NA, NEG_I64, NEG_F64) = range(1, 19)
+ AND, OR, NOT, IS_NA, NEG_I64, NEG_F64, COL_STR, LIT_STR, CMP_STR, NCHAR, SUBSTR, GREPL, F2I) = range(1, 26)
+PROG_POOL = 512
 
 
 class Insn(C.Structure):
@@ -28,8 +29,8 @@ class Insn(C.Structure):
 
 
 class Prog(C.Structure):
-    _fields_ = [("n", C.c_int32), ("result_type", C.c_int32), ("max_depth", C.c_int32), ("pad", C.c_int32),
-                ("insn", Insn * MAX_INSNS)]
+    _fields_ = [("n", C.c_int32), ("result_type", C.c_int32), ("max_depth", C.c_int32), ("pool_n", C.c_int32),
+                ("insn", Insn * MAX_INSNS), ("pool", C.c_char * PROG_POOL)]
 
 
 MAPFN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_char_p, C.POINTER(C.c_int))
@@ -70,11 +71,42 @@ def cmp(c, code):
     return [c == 0, c != 0, c < 0, c <= 0, c > 0, c >= 0][code]
 
 
+def f2i(x):
+    """double -> int64 toward zero; NaN 0, out of range saturated."""
+    if x != x: return 0
+    if x >= 2.0 ** 63: return (1 << 63) - 1
+    if x < -2.0 ** 63: return -(1 << 63)
+    return int(x)
+
+
 def run(prog, cols, r):
     st = []
+    pool = bytes(prog.pool)
     for ins in prog.insn[:prog.n]:
         op = ins.op
-        if op in (COL_I64, COL_F64, COL_BOOL):
+        if op == COL_STR:                       # a string cell holds its bytes
+            v, valid, ty = cols[ins.a]
+            st.append([v[r].encode("utf-8", "surrogateescape"), bool(valid[r])])
+        elif op == LIT_STR:
+            st.append([pool[ins.imm:ins.imm + ins.a], True])
+        elif op == CMP_STR:                     # memcmp, then the shorter first: bytes order
+            b, a = st.pop(), st.pop()
+            ok = a[1] and b[1]
+            st.append([int(cmp((a[0] > b[0]) - (a[0] < b[0]), ins.a)) if ok else 0, ok])
+        elif op == NCHAR:
+            st[-1][0] = len(st[-1][0])
+        elif op == SUBSTR:
+            stop, start = st.pop(), st.pop()
+            s = st[-1]
+            ok = s[1] and start[1] and stop[1]
+            b0 = max(s64(start[0] - 1), 0)
+            e0 = min(s64(stop[0]), len(s[0]))
+            st[-1] = [s[0][b0:e0] if ok and e0 > b0 else b"", ok]
+        elif op == GREPL:
+            st[-1][0] = int(st[-1][1] and pool[ins.imm:ins.imm + ins.a] in st[-1][0])
+        elif op == F2I:
+            st[-1][0] = f2i(b2f(st[-1][0])) & M64
+        elif op in (COL_I64, COL_F64, COL_BOOL):
             v, valid, ty = cols[ins.a]
             x = f2b(float(v[r])) if ty == abi.VEC_DOUBLE else int(v[r]) & M64   # the column's 64-bit payload
             if op == COL_F64 and ty != abi.VEC_DOUBLE:
@@ -195,6 +227,75 @@ def test_programs_keep_the_oracles_rows(seed, oracle):
                 keep.append(r)
         assert keep == want, repr(e.kw)
     assert ran > 60
+
+
+def random_string_bool(rng, depth=0):
+    """Predicates over the string column s, the int64 column i and the
+    double column d: comparisons with literals and between expressions,
+    nchar, substr with column, literal and double bounds, grepl."""
+    from vectra_gb300.plan import grepl, nchar, substr
+    words = ["", "a", "ab", "abc", "b", "\u00e9", "ba", "zz"]
+
+    def sval(k=0):
+        r = rng.random()
+        if k > 1 or r < 0.5:
+            return col("s") if rng.random() < 0.8 else lit(words[int(rng.integers(0, len(words)))])
+        lo = [col("i"), lit(int(rng.integers(-2, 4))), col("d"), lit(float(rng.choice([0.5, 2.9, -1.5])))]
+        return substr(sval(k + 1), lo[int(rng.integers(0, 4))], lo[int(rng.integers(0, 4))])
+    r = rng.random()
+    if depth > 1 or r < 0.55:
+        k = rng.random()
+        if k < 0.45:
+            a, b = sval(), sval()
+            return [a.__lt__, a.__le__, a.__gt__, a.__ge__, a.eq, a.ne][int(rng.integers(0, 6))](b)
+        if k < 0.65:
+            return grepl(words[int(rng.integers(0, len(words)))], sval())
+        if k < 0.85:
+            return nchar(sval()) > lit(int(rng.integers(0, 4)))
+        return is_na(sval())
+    a, b = random_string_bool(rng, depth + 1), random_string_bool(rng, depth + 1)
+    e = (a | b) if rng.random() < 0.6 else (a & b)
+    return ~e if rng.random() < 0.3 else e
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_string_programs_keep_the_oracles_rows(seed, oracle):
+    """String instructions (column views, pool literals, comparison, nchar,
+    substr, grepl, double -> int64 bounds) as run_prog runs them, against
+    the oracle's filter."""
+    import vectra_gb300
+    lib = vectra_gb300.load()
+    lib.vg_compile_prog.argtypes = [C.c_void_p, MAPFN, C.c_void_p, C.POINTER(Prog)]
+    lib.vg_compile_prog.restype = C.c_int
+    rng = np.random.default_rng(70 + seed)
+    n = 250
+    words = ["", "a", "ab", "abc", "abcd", "b", "ba", "\u00e9t\u00e9", "zz", "azb", "bab"]
+    t = {"s": ([words[k] for k in rng.integers(0, len(words), n)], rng.random(n) > 0.1),
+         "i": (rng.integers(-1, 5, n).astype(np.int64), rng.random(n) > 0.1),
+         "d": (rng.choice([0.5, 1.0, 2.7, -3.2, 4.0], n), rng.random(n) > 0.1),
+         "rid": np.arange(n, dtype=np.int64)}
+    names = ["s", "i", "d"]
+    types = [abi.VEC_STRING, abi.VEC_INT64, abi.VEC_DOUBLE]
+
+    def colmap(ctx, name, ty):
+        k = names.index(name.decode())
+        ty[0] = types[k]
+        return k
+    cmap = MAPFN(colmap)
+    cols = [(t[nm][0], t[nm][1], ty) for nm, ty in zip(names, types)]
+    ran = 0
+    for _ in range(60):
+        e = random_string_bool(rng)
+        p = Prog()
+        if lib.vg_compile_prog(C.cast(e.to_c(list(zip(names, types))), C.c_void_p), cmap, None,
+                               C.byref(p)) != 0:
+            continue
+        ran += 1
+        got = tbl(oracle, t).filter(e).collect()
+        want = got["rid"][0].tolist() if got else []
+        keep = [r for r in range(n) if (lambda v: v[1] and v[0])(run(p, cols, r))]
+        assert keep == want, repr(e.kw)
+    assert ran > 50
 
 
 # ---------------------------------------------------------------------------

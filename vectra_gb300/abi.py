@@ -153,7 +153,8 @@ def batch_to_numpy(bp, logical=True):
         if a.type == VEC_STRING:
             offs = np.ctypeslib.as_array(a.buf.str.offsets, shape=(n + 1,)).copy() if n else np.zeros(1, np.int64)
             data = C.string_at(a.buf.str.data, int(offs[-1])) if offs[-1] else b""
-            vals = np.array([data[offs[i]:offs[i + 1]].decode() for i in range(n)], dtype=object)
+            vals = np.array([data[offs[i]:offs[i + 1]].decode("utf-8", "surrogateescape") for i in range(n)],
+                            dtype=object)
         elif n == 0:
             vals = np.zeros(0, NP_OF[a.type])
         elif a.type == VEC_BOOL:

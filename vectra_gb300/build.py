@@ -23,13 +23,14 @@ ARCHIVE = os.path.join(HERE, "libvgpu.a")
 
 CU_SOURCES = ["k_groupby_fastj.cu", "k_groupby_fast.cu", "k_groupby.cu", "jit_agg.cu", "k_filter.cu",
               "k_sort.cu", "k_hashjoin.cu", "k_prof.cu", "k_static.cu", "k_batch.cu", "k_serve.cu",
-              "k_pagg.cu"]
+              "k_pagg.cu", "k_strings.cu"]
 # headers the run-time compiler needs, embedded into jit_agg.cu's object
 JIT_HEADERS = [("vg_rtc_types.h", CSRC), ("vectra_abi.h", INCLUDE), ("vgpu_internal.h", CSRC),
                ("k_common.cuh", CSRC), ("k_groupby_dev.cuh", CSRC), ("k_jit_lib.cuh", CSRC),
                ("k_jit_kernel.cuh", CSRC), ("k_jit_pagg.cuh", CSRC)]
 C_SOURCES = ["runtime.c", "compile.c", "source.c", "node_filter.c",
-             "node_project.c", "node_agg.c", "node_join.c", "noalloc.c", "scan_vtr.c", "node_sort.c"]
+             "node_project.c", "node_agg.c", "node_join.c", "noalloc.c", "scan_vtr.c", "node_sort.c",
+             "strdict.c"]
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -102,8 +102,10 @@ static int type_of(const VecExpr *e, vg_colmap_fn map, void *ctx) {
         if (c == VEC_BOOL) c = VEC_INT64;
         return c;
     }
-    case EXPR_CMP: case EXPR_BOOL: case EXPR_IS_NA: return VEC_BOOL;
+    case EXPR_CMP: case EXPR_BOOL: case EXPR_IS_NA: case EXPR_GREPL: return VEC_BOOL;
     case EXPR_NEGATE: return type_of(e->operand, map, ctx);
+    case EXPR_NCHAR: return VEC_INT64;
+    case EXPR_SUBSTR: return VEC_STRING;
     default: return -1;
     }
 }
@@ -346,6 +348,38 @@ static int coerce_top(PC *pc, int from, int to) {
     return 0;                                                /* bool -> int64: payload is 0/1 */
 }
 
+/* a string literal's bytes into the program's pool: its offset, or -1 */
+static int64_t pool_add(PC *pc, const char *str, int *len) {
+    const size_t n = str ? strlen(str) : 0;
+    if ((size_t)pc->p->pool_n + n > VG_PROG_POOL)
+        return cerr("string literals too long for the GPU program%s", "");
+    memcpy(pc->p->pool + pc->p->pool_n, str ? str : "", n);
+    const int64_t off = pc->p->pool_n;
+    pc->p->pool_n += (int32_t)n;
+    *len = (int)n;
+    return off;
+}
+
+static int prog_rec(PC *pc, const VecExpr *e);
+
+/* an argument that must be a string (nchar, substr, grepl) */
+static int prog_string_arg(PC *pc, const VecExpr *e, const char *what) {
+    int t = prog_rec(pc, e);
+    if (t < 0) return -1;
+    if (t != VEC_STRING) return cerr("%s: argument must be string", what);
+    return 0;
+}
+
+/* substr's start / stop: int64 (a double is truncated toward zero, as the
+ * reference's (int64_t) cast does, src/expr.c:186-193) */
+static int prog_int_arg(PC *pc, const VecExpr *e) {
+    int t = prog_rec(pc, e);
+    if (t < 0) return -1;
+    if (t == VEC_STRING) return cerr("substr: start and stop must be numeric%s", "");
+    if (t == VEC_DOUBLE) return emit(pc, VI_F2I, 0, 0, 0);
+    return 0;
+}
+
 /* returns the type of the value pushed, or -1 */
 static int prog_rec(PC *pc, const VecExpr *e) {
     switch (e->kind) {
@@ -353,9 +387,36 @@ static int prog_rec(PC *pc, const VecExpr *e) {
         int ty = -1;
         int ci = pc->map(pc->ctx, e->col_name, &ty);
         if (ci < 0) return cerr("column not found: %s", e->col_name);
-        if (ty == VEC_STRING) return cerr("string column '%s' is not supported by the GPU path", e->col_name);
+        if (ty == VEC_STRING) {
+            if (emit(pc, VI_COL_STR, ci, 0, 1)) return -1;
+            return VEC_STRING;
+        }
         if (emit(pc, ty == VEC_DOUBLE ? VI_COL_F64 : ty == VEC_BOOL ? VI_COL_BOOL : VI_COL_I64, ci, 0, 1)) return -1;
         return ty;
+    }
+    case EXPR_LIT_STRING: {
+        int len = 0;
+        int64_t off = pool_add(pc, e->lit_str, &len);
+        if (off < 0) return -1;
+        if (emit(pc, VI_LIT_STR, len, off, 1)) return -1;
+        return VEC_STRING;
+    }
+    case EXPR_NCHAR:   /* bytes of the string (src/expr.c:153-170) */
+        if (prog_string_arg(pc, e->operand, "nchar")) return -1;
+        if (emit(pc, VI_NCHAR, 0, 0, 0)) return -1;
+        return VEC_INT64;
+    case EXPR_SUBSTR:  /* src/expr.c:172-235 */
+        if (prog_string_arg(pc, e->operand, "substr")) return -1;
+        if (prog_int_arg(pc, e->left) || prog_int_arg(pc, e->right)) return -1;
+        if (emit(pc, VI_SUBSTR, 0, 0, -2)) return -1;
+        return VEC_STRING;
+    case EXPR_GREPL: { /* fixed pattern (src/expr.c:237-268) */
+        if (prog_string_arg(pc, e->operand, "grepl")) return -1;
+        int len = 0;
+        int64_t off = pool_add(pc, e->lit_str, &len);
+        if (off < 0) return -1;
+        if (emit(pc, VI_GREPL, len, off, 0)) return -1;
+        return VEC_BOOL;
     }
     case EXPR_LIT_INT64:
         if (emit(pc, VI_LIT_I64, 0, e->lit_i64, 1)) return -1;
@@ -389,8 +450,15 @@ static int prog_rec(PC *pc, const VecExpr *e) {
     case EXPR_CMP: {
         int lt = type_of(e->left, pc->map, pc->ctx), rt = type_of(e->right, pc->map, pc->ctx);
         if (lt == -2 || rt == -2) return cerr("column not found%s", "");
+        if (lt == VEC_STRING && rt == VEC_STRING) {   /* src/scalar_ops.c:78-107 */
+            int code = cmp_code(e->op, e->op2);
+            if (code < 0) return cerr("unknown comparison%s", "");
+            if (prog_rec(pc, e->left) < 0 || prog_rec(pc, e->right) < 0) return -1;
+            if (emit(pc, VI_CMP_STR, code, 0, -1)) return -1;
+            return VEC_BOOL;
+        }
         if (lt == VEC_STRING || rt == VEC_STRING)
-            return cerr("string comparisons are not supported by the GPU path%s", "");
+            return cerr("cannot coerce string in arithmetic/comparison%s", "");
         int c = common_type(lt, rt);
         if (c == VEC_BOOL) c = VEC_INT64;
         int code = cmp_code(e->op, e->op2);
@@ -434,7 +502,7 @@ static int prog_rec(PC *pc, const VecExpr *e) {
     case EXPR_CAST:
         return cerr("if_else/cast not yet implemented%s", "");
     default:
-        return cerr("string expressions (nchar/substr/grepl/string literals) are not supported by the GPU path%s", "");
+        return cerr("unknown expression kind%s", "");
     }
 }
 

@@ -62,6 +62,21 @@ VG_DEV uint64_t vg_load_bits(const VgCol &c, int64_t r) {
     return (uint64_t)__ldg((const unsigned long long *)c.data + r);
 }
 
+// the first four bytes of a string, big-endian, zero-padded
+VG_DEV uint32_t vg_str_pre(const char *p, uint32_t len) {
+    uint32_t pre = 0;
+    for (uint32_t i = 0; i < 4; i++) pre = (pre << 8) | (i < len ? (uint32_t)(unsigned char)p[i] : 0u);
+    return pre;
+}
+
+VG_DEV VgStrView vg_str_view(const char *p, uint32_t len) {
+    VgStrView v;
+    v.len = len;
+    v.pre = vg_str_pre(p, len);
+    v.ptr = p;
+    return v;
+}
+
 VG_DEV double vg_bits_to_f64(uint64_t b) { return __longlong_as_double((long long)b); }
 VG_DEV uint64_t vg_f64_to_bits(double d) { return (uint64_t)__double_as_longlong(d); }
 

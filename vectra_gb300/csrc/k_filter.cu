@@ -51,7 +51,41 @@ VG_DEV bool pred_keep(const VgPred &P, const VgCol *cols, int64_t p) {
 // ---------------------------------------------------------------------
 // postfix program interpreter (one row per lane)
 // ---------------------------------------------------------------------
-struct Cell { uint64_t v; bool ok; };
+// A cell holds an int64, a double's bits or a bool as 0/1 in v; a string
+// as a pointer to its bytes in v and its length in len.
+struct Cell { uint64_t v; uint32_t len; bool ok; };
+
+// memcmp over the shorter length, then the shorter string first: the
+// reference's string order (src/scalar_ops.c:78-107)
+VG_DEV int str_cmp(const char *a, uint32_t la, const char *b, uint32_t lb) {
+    const uint32_t m = la < lb ? la : lb;
+    for (uint32_t i = 0; i < m; i++) {
+        const unsigned char x = (unsigned char)a[i], y = (unsigned char)b[i];
+        if (x != y) return x < y ? -1 : 1;
+    }
+    return (la > lb) - (la < lb);
+}
+
+// fixed-pattern search (src/expr.c:237-268): an empty pattern matches
+VG_DEV bool str_contains(const char *s, uint32_t ls, const char *pat, uint32_t lp) {
+    if (lp > ls) return false;
+    for (uint32_t j = 0; j + lp <= ls; j++) {
+        uint32_t k = 0;
+        while (k < lp && s[j + k] == pat[k]) k++;
+        if (k == lp) return true;
+    }
+    return false;
+}
+
+// double -> int64 toward zero, as C's cast does for values in range; C
+// leaves NaN and out-of-range values undefined, here NaN gives 0 and the
+// rest saturate
+VG_DEV int64_t f2i_trunc(double x) {
+    if (x != x) return 0;
+    if (x >= 9223372036854775808.0) return INT64_MAX;
+    if (x < -9223372036854775808.0) return INT64_MIN;
+    return (int64_t)x;
+}
 
 VG_DEV int cmp_code(int c, int code) {
     switch (code) {
@@ -191,12 +225,58 @@ VG_DEV Cell run_prog(const VgProg &P, const VgCol *cols, int64_t p, uint32_t *er
         case VI_NEG_F64:
             st[sp - 1].v ^= 0x8000000000000000ull;
             break;
+        case VI_COL_STR: {
+            const VgCol &c = cols[in.a];
+            const ulonglong2 w = __ldg((const ulonglong2 *)c.data + p);
+            st[sp].ok = vg_valid(c, p);
+            st[sp].v = w.y;
+            st[sp].len = (uint32_t)w.x;
+            sp++;
+            break;
+        }
+        case VI_LIT_STR:
+            st[sp].v = (uint64_t)(P.pool + in.imm);
+            st[sp].len = (uint32_t)in.a;
+            st[sp].ok = true;
+            sp++;
+            break;
+        case VI_CMP_STR: {
+            Cell b = st[--sp], a = st[sp - 1];
+            const bool ok = a.ok && b.ok;
+            const int c = ok ? str_cmp((const char *)a.v, a.len, (const char *)b.v, b.len) : 0;
+            st[sp - 1].v = (uint64_t)cmp_code(c, in.a); st[sp - 1].ok = ok;
+            break;
+        }
+        case VI_NCHAR:
+            st[sp - 1].v = (uint64_t)st[sp - 1].len;
+            break;
+        case VI_SUBSTR: {   // substr(s, start, stop), 1-based and inclusive (src/expr.c:172-235)
+            Cell stop = st[--sp], start = st[--sp];
+            Cell &s = st[sp - 1];
+            const bool ok = s.ok && start.ok && stop.ok;
+            int64_t b0 = (int64_t)((uint64_t)start.v - 1u);
+            if (b0 < 0) b0 = 0;
+            int64_t e0 = (int64_t)stop.v;
+            if (e0 > (int64_t)s.len) e0 = (int64_t)s.len;
+            const int64_t n = ok && e0 > b0 ? e0 - b0 : 0;
+            s.v = n > 0 ? s.v + (uint64_t)b0 : s.v;
+            s.len = (uint32_t)n;
+            s.ok = ok;
+            break;
+        }
+        case VI_GREPL:
+            st[sp - 1].v = st[sp - 1].ok && str_contains((const char *)st[sp - 1].v, st[sp - 1].len, P.pool + in.imm,
+                                                         (uint32_t)in.a) ? 1u : 0u;
+            break;
+        case VI_F2I:
+            st[sp - 1].v = (uint64_t)f2i_trunc(vg_bits_to_f64(st[sp - 1].v));
+            break;
         default:
             atomicOr(err, VG_ERR_PROG);
             st[0].ok = false;
             return st[0];
         }
-        if (sp < 1 || sp > 15) { atomicOr(err, VG_ERR_PROG); Cell z{0, false}; return z; }
+        if (sp < 1 || sp > 15) { atomicOr(err, VG_ERR_PROG); Cell z{0, 0, false}; return z; }
     }
     return st[sp - 1];
 }
@@ -303,11 +383,12 @@ __global__ void eval_kernel(const ProgArgs *ga, int64_t n_logical, const int32_t
     // iterate in whole warps so that the validity word is voted at once
     int64_t n_pad = (n_logical + 31) & ~31ll;
     for (int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; li < n_pad; li += stride) {
-        Cell c{0, false};
+        Cell c{0, 0, false};
         if (li < n_logical) {
             int64_t p = sel ? (int64_t)sel[li] : li;
             c = run_prog(ga->prog, ga->cols, p, err);
             if (out_type == VEC_BOOL) ((uint8_t *)out)[li] = (uint8_t)(c.ok ? (c.v ? 1 : 0) : 0);
+            else if (out_type == VEC_STRING) ((VgStrView *)out)[li] = vg_str_view((const char *)c.v, c.ok ? c.len : 0u);
             else ((uint64_t *)out)[li] = c.ok ? c.v : 0;
         }
         uint32_t m = __ballot_sync(0xFFFFFFFFu, c.ok && li < n_logical);
@@ -327,9 +408,12 @@ __global__ void gather_kernel(VgCol c, const int32_t *idx, int64_t n_out, int nu
             if (p >= 0) {
                 ok = vg_valid(c, p);
                 if (c.type == VEC_BOOL) ((uint8_t *)out)[j] = ok ? __ldg((const uint8_t *)c.data + p) : 0;
+                else if (c.type == VEC_STRING)
+                    ((ulonglong2 *)out)[j] = ok ? __ldg((const ulonglong2 *)c.data + p) : make_ulonglong2(0, 0);
                 else ((uint64_t *)out)[j] = ok ? vg_load_bits(c, p) : 0;
             } else {
                 if (c.type == VEC_BOOL) ((uint8_t *)out)[j] = 0;
+                else if (c.type == VEC_STRING) ((ulonglong2 *)out)[j] = make_ulonglong2(0, 0);
                 else ((uint64_t *)out)[j] = 0;
             }
         }
@@ -347,6 +431,8 @@ __global__ void gather_into_kernel(VgCol c, const int32_t *idx, int64_t n, void 
         bool ok = vg_valid(c, p);
         int64_t d = row0 + j;
         if (c.type == VEC_BOOL) ((uint8_t *)out)[d] = ok ? __ldg((const uint8_t *)c.data + p) : 0;
+        else if (c.type == VEC_STRING)
+            ((ulonglong2 *)out)[d] = ok ? __ldg((const ulonglong2 *)c.data + p) : make_ulonglong2(0, 0);
         else ((uint64_t *)out)[d] = ok ? vg_load_bits(c, p) : 0;
         if (ok) atomicOr(out_valid + (d >> 5), 1u << (d & 31));
     }

@@ -50,6 +50,13 @@ typedef struct {
     VgAccSpec acc[VG_MAX_ACCS];
     VgFinish fin[VG_MAX_OUTS];
     int fail;                 /* resolution failed: not fusable */
+    /* string group keys: grouped by their dictionary codes (strdict.c) */
+    int allow_str;            /* resolving a key: a string source column is allowed */
+    int n_str;
+    int str_key[VG_MAX_KEYS]; /* key k is a string column of the source */
+    int str_col[VG_MAX_KEYS]; /* that source column */
+    VgDict *dict[VG_MAX_KEYS];
+    int dict_owner[VG_MAX_KEYS];
 } Plan;
 
 typedef struct {
@@ -96,7 +103,7 @@ static int resolve_operand(Plan *P, VecNode *at, const char *name, VgOperand *o)
     o->side = VG_SIDE_PROBE;
     o->col = j;
     o->type = t;
-    return t != VEC_STRING;
+    return t != VEC_STRING || P->allow_str;
 }
 
 static int add_probe(Plan *P, VecNode *at, const char *name, int *type) {
@@ -172,7 +179,18 @@ static int plan_resolve(VgAgg *A, Plan *P) {
     GroupAggNode *ga = &A->ga;
     P->n_keys = ga->n_keys;
     for (int k = 0; k < ga->n_keys; k++) {
-        if (!resolve_value(P, ga->key_names[k], &P->key[k])) return 0;
+        P->allow_str = 1;
+        const int ok = resolve_value(P, ga->key_names[k], &P->key[k]);
+        P->allow_str = 0;
+        if (!ok) return 0;
+        if (P->key[k].type == VEC_STRING) {
+            /* a plain column of the source, grouped by its codes */
+            if (P->key[k].op != 0 || P->key[k].a.side != VG_SIDE_PROBE) return 0;
+            P->key[k].type = P->key[k].a.type = VEC_INT64;
+            P->str_key[k] = 1;
+            P->str_col[k] = P->pset.idx[P->key[k].a.col];
+            P->n_str++;
+        }
         P->key_type[k] = P->key[k].type;
     }
     P->n_accs = 0;
@@ -480,6 +498,47 @@ static void check_deferred(const uint32_t *hw) {
 /* results up to this size are read back in one page-locked copy */
 #define kSmallResultBytes ((size_t)8 << 20)
 
+/* ------------------------------------------------------------------ */
+/* string group keys                                                   */
+/* ------------------------------------------------------------------ */
+
+/* one dictionary per distinct string key column */
+static void str_dicts_begin(Plan *P) {
+    for (int k = 0; k < P->n_keys; k++) {
+        if (!P->str_key[k]) continue;
+        for (int k2 = 0; k2 < k; k2++)
+            if (P->str_key[k2] && P->str_col[k2] == P->str_col[k]) P->dict[k] = P->dict[k2];
+        if (!P->dict[k]) {
+            P->dict[k] = vg_dict_new();
+            P->dict_owner[k] = 1;
+        }
+    }
+}
+
+static void str_dicts_free(Plan *P) {
+    for (int k = 0; k < P->n_keys; k++)
+        if (P->dict_owner[k]) vg_dict_free(P->dict[k]);
+}
+
+/* Each string key column of the batch replaced by the int64 codes of its
+ * logical rows (validity unchanged); returns the device block of the
+ * codes, freed by the caller after the batch's launches. */
+static void *str_encode_batch(Plan *P, VgDBatch *db) {
+    const int64_t n = db->n_rows, n_logical = db->d_sel ? db->sel_n : db->n_rows;
+    const size_t per = a256((size_t)(n ? n : 1) * 8);
+    char *blk = (char *)vg_dmalloc(per * (size_t)P->n_keys);
+    for (int k = 0; k < P->n_keys; k++) {
+        if (!P->dict_owner[k]) continue;
+        VgCol *c = &db->cols[P->str_col[k]];
+        if (c->type != VEC_STRING) vg_fail("group_by: key column %d is not a string column", P->str_col[k]);
+        int64_t *codes = (int64_t *)(blk + per * (size_t)k);
+        vg_dict_encode(P->dict[k], c, db->d_sel, n_logical, 1, codes);
+        c->type = VEC_INT64;
+        c->data = codes;
+    }
+    return blk;
+}
+
 static VecBatch *emit_result(VgAgg *A, Plan *P, Table *T, const uint32_t *deferred) {
     GroupAggNode *ga = &A->ga;
     uint32_t n = 0;
@@ -487,6 +546,16 @@ static VecBatch *emit_result(VgAgg *A, Plan *P, Table *T, const uint32_t *deferr
     vg_check_rc(vgk_group_table_compact(&T->gt, d_slots, &n, vg_stream()), "group compact");
     if (deferred) check_deferred(deferred);     /* read back behind the launches, before the count */
     int64_t ng = n;
+    /* key order of string keys: each group's code becomes the rank of its
+     * string, then the groups sort as integer keys do */
+    int32_t *sperm[VG_MAX_KEYS] = {0};
+    int64_t *srank[VG_MAX_KEYS] = {0};
+    const int str_ranked = A->sorted && ng > 1;
+    for (int k = 0; str_ranked && k < P->n_keys; k++) {
+        if (!P->str_key[k]) continue;
+        vg_dict_order(P->dict[k], &sperm[k], &srank[k]);
+        vg_check_rc(vgk_group_keys_remap(&T->gt, k, d_slots, ng, srank[k], vg_stream()), "string key order");
+    }
     if (ng > 1 && ga->n_keys > 0) {
         size_t sb = vgk_order_scratch_bytes(ng);
         void *scratch = vg_dmalloc(sb);
@@ -526,6 +595,14 @@ static VecBatch *emit_result(VgAgg *A, Plan *P, Table *T, const uint32_t *deferr
         hb = pin;
     }
     for (int k = 0; k < ga->n_keys; k++) {
+        if (P->str_key[k]) {
+            res->columns[k] = vg_dict_strings(P->dict[k], (const int64_t *)kout[k], kval[k],
+                                              str_ranked ? sperm[k] : NULL, ng);
+            res->col_names[k] = vg_xstrdup(ga->key_names[k]);
+            vg_dfree(sperm[k]);
+            vg_dfree(srank[k]);
+            continue;
+        }
         int t = P->key_type[k];
         VecArray arr = hb ? vg_column_from_host(VEC_INT64, hb + per * (size_t)k,
                                                 hb + per * (size_t)k + a256((size_t)ng * 8 + 8), ng)
@@ -1497,9 +1574,11 @@ static VecBatch *agg_next_body(VecNode *self) {
     PAgg *pg = NULL;
     double t_loop = now_ms();
     g_agg_ms[0] += t_loop - t_start;
+    if (P.n_str) str_dicts_begin(&P);
     while (vg_pull(P.src, need, 0, &db)) {
         int64_t n_logical = db.d_sel ? db.sel_n : db.n_rows;
-        if (batch_idx == 0) {
+        void *codes = P.n_str ? str_encode_batch(&P, &db) : NULL;
+        if (batch_idx == 0 && !P.n_str) {
             const double t0 = now_ms();
             pg = pagg_begin(A, &P, L, &db);
             if (pg) g_pagg_ms[0] += now_ms() - t0;
@@ -1535,6 +1614,7 @@ static VecBatch *agg_next_body(VecNode *self) {
             L->li_base = off;
             settled = !run_batch(&P, &T, L, &S, n);
         }
+        vg_dfree(codes);
         vg_dbatch_release(&db);
         stream_pos += n_logical;
         batch_idx++;
@@ -1543,6 +1623,7 @@ static VecBatch *agg_next_body(VecNode *self) {
     const double t_emit = now_ms();
     if (!pg) g_agg_ms[2] += t_emit - t_loop;
     VecBatch *res = pg ? pagg_end(pg, A, &P, L) : emit_result(A, &P, &T, deferred);
+    str_dicts_free(&P);
     if (pg) pt_finish(pg);
     if (!pg) g_agg_ms[3] += now_ms() - t_emit;
     if (pg) g_pagg_runs++;
@@ -1588,8 +1669,6 @@ GroupAggNode *group_agg_node_create(VecNode *child, int n_keys, char **key_names
     for (int k = 0; k < n_keys; k++) {
         int idx = vg_schema_find(cs, key_names[k]);
         if (temp_dir && idx < 0) vg_fail("group_by: column not found: %s", key_names[k]);
-        if (idx >= 0 && cs->col_types[idx] == VEC_STRING)
-            vg_fail("string group keys are not supported by the GPU group-agg (%s)", key_names[k]);
     }
     VgAgg *A = (VgAgg *)vg_xcalloc(1, sizeof(VgAgg));
     A->ga.child = child;

@@ -80,7 +80,14 @@ const VgPred *vg_filter_cnf(VecNode *n, VecNode **child_out, const VgColSet **se
 static VecBatch *filter_next_body(VecNode *self) {
     VgFilter *f = (VgFilter *)self;
     compile_filter(f);
-    if (f->compiled == 3) vg_fail("%s", f->err);
+    if (f->compiled == 3) {
+        /* the reference evaluates the predicate on each batch: its errors
+         * come with the first batch, and an empty input has none */
+        VecBatch *b = f->fn.child->next_batch(f->fn.child);
+        if (!b) return NULL;
+        vg_batch_free(b);
+        vg_fail("%s", f->err);
+    }
     VgDBatch db;
     while (vg_pull(f->fn.child, f->need, 1, &db)) {
         VgCol cols[VG_MAX_COLS];

@@ -110,12 +110,14 @@ static VecBatch *project_next_body(VecNode *self) {
     int64_t n = db.d_sel ? db.sel_n : db.n_rows;
     /* dense copies of the needed child columns over the logical rows */
     size_t wb = (size_t)((n + 31) / 32) * 4;
-    size_t per = (((size_t)n * 8 + 255) & ~(size_t)255) + ((wb + 255) & ~(size_t)255);
+    /* room for the widest value: a string column is one 16-byte view per row */
+    const size_t vbytes = ((size_t)n * 16 + 255) & ~(size_t)255;
+    size_t per = vbytes + ((wb + 255) & ~(size_t)255);
     char *blk = (char *)vg_dmalloc(per * (size_t)(nc + ne) + 256);
     for (int c = 0; c < nc; c++) {
         if (!w.need[c]) { w.cols[c].data = NULL; continue; }
         char *dv = blk + per * (size_t)c;
-        uint32_t *dm = (uint32_t *)(dv + (((size_t)n * 8 + 255) & ~(size_t)255));
+        uint32_t *dm = (uint32_t *)(dv + vbytes);
         vg_check_rc(vgk_gather(&db.cols[c], db.d_sel, n, 0, dv, dm, vg_stream()), "project gather");
         w.cols[c].data = dv;
         w.cols[c].valid = dm;
@@ -139,13 +141,15 @@ static VecBatch *project_next_body(VecNode *self) {
             VgCol cols[VG_MAX_COLS];
             for (int j = 0; j < cm.n; j++) cols[j] = w.cols[cm.idx[j]];
             char *dv = blk + per * (size_t)k;
-            uint32_t *dm = (uint32_t *)(dv + (((size_t)n * 8 + 255) & ~(size_t)255));
+            uint32_t *dm = (uint32_t *)(dv + vbytes);
             vg_check_rc(vgk_eval_prog(cols, cm.n, &prog, n, NULL, n, dv, dm, vg_stream()), "project eval");
             w.cols[k].data = dv;
             w.cols[k].valid = dm;
             src = k++;
         }
-        out->columns[i] = vg_download_column(w.cols[src].type, w.cols[src].data, w.cols[src].valid, n);
+        out->columns[i] = w.cols[src].type == VEC_STRING
+                              ? vg_download_strings(&w.cols[src], NULL, n)
+                              : vg_download_column(w.cols[src].type, w.cols[src].data, w.cols[src].valid, n);
     }
     vg_sync();
     vg_dfree(blk);

@@ -81,6 +81,7 @@ void vg_check_rc(int rc, const char *what) {
     if (!m || !*m) m = vgk_sort_last_error();
     if (!m || !*m) m = vgk_pagg_last_error();
     if (!m || !*m) m = vgk_jit_error();
+    if (!m || !*m) m = vgk_str_last_error();
     vg_fail("%s failed: %s", what, (m && *m) ? m : "unknown device error");
 }
 
@@ -555,10 +556,50 @@ static void stage_send(void *dst, const void *src, size_t bytes) {
     g_stage_cur ^= 1;
 }
 
+/* bytes of a string column's characters in one batch (below 4 GiB: a
+ * device view holds a 32-bit length) */
+static size_t str_bytes(const VecArray *a, int64_t n) {
+    if (n <= 0) return 0;
+    const int64_t e = a->buf.str.offsets[n];
+    if (e < 0 || e > (int64_t)0xFFFFFFFFll)
+        vg_fail("string column: %lld bytes in one batch; the GPU path takes less than 4 GiB per batch", (long long)e);
+    return (size_t)e;
+}
+
+/* the device reads each row's bytes through its offsets: they must start
+ * at 0 or above and never decrease */
+static void check_offsets(const VecArray *a, int64_t n) {
+    const int64_t *o = a->buf.str.offsets;
+    if (n <= 0) return;
+    if (!o || o[0] < 0 || (o[n] > 0 && !a->buf.str.data)) vg_fail("string column: malformed offsets");
+    for (int64_t i = 0; i < n; i++) {
+        if (o[i + 1] < o[i]) vg_fail("string column: offsets decrease at row %lld", (long long)i);
+        if (o[i + 1] - o[i] > (int64_t)0x7FFFFFFF)
+            vg_fail("string column: a value of %lld bytes (the GPU path takes below 2 GiB)",
+                    (long long)(o[i + 1] - o[i]));
+    }
+}
+
+/* A needed column's part of the device block: values (for strings, one
+ * 16-byte view per row), validity words, and for strings the offsets and
+ * the characters, from which the views are made on the device. */
+static size_t col_dev_bytes(const VecArray *a, int64_t n) {
+    if (a->type == VEC_STRING)
+        return a256((size_t)n * 16) + a256(valid_bytes_dev(n)) + a256((size_t)(n + 1) * 8) + a256(str_bytes(a, n) + 1);
+    return a256(value_bytes(a->type, n)) + a256(valid_bytes_dev(n));
+}
+
+static int needs_string(const VecNode *child, const uint8_t *need) {
+    const VecSchema *s = &child->output_schema;
+    for (int c = 0; c < s->n_cols; c++)
+        if ((!need || need[c]) && s->col_types[c] == VEC_STRING) return 1;
+    return 0;
+}
+
 int vg_pull(VecNode *child, const uint8_t *need, int keep_host, VgDBatch *out) {
     memset(out, 0, sizeof(*out));
     if (vg_is_table_source(child) && !keep_host) return vg_source_pull(child, need, out);
-    if (vg_is_vtr_scan(child) && !keep_host) return vg_scan_pull(child, need, out);
+    if (vg_is_vtr_scan(child) && !keep_host && !needs_string(child, need)) return vg_scan_pull(child, need, out);
     VecBatch *b = child->next_batch(child);
     if (!b) return 0;
     int64_t n = b->n_rows;
@@ -568,75 +609,123 @@ int vg_pull(VecNode *child, const uint8_t *need, int keep_host, VgDBatch *out) {
     size_t total = 0;
     for (int c = 0; c < b->n_cols; c++) {
         if (!need || !need[c]) continue;
-        if (b->columns[c].type == VEC_STRING)
-            vg_fail("string column '%s' is not supported by the GPU path", b->col_names[c]);
-        total += a256(value_bytes(b->columns[c].type, n)) + a256(valid_bytes_dev(n));
+        total += col_dev_bytes(&b->columns[c], n);
     }
     if (b->sel) total += a256((size_t)b->sel_n * 4);
     char *blk = total ? (char *)vg_dmalloc(total) : NULL;
     out->block = blk;
-    if (!keep_host && total) {
-        /* staged: the batch's bytes into a page-locked block laid out like
-         * the device block, one copy, the host batch freed at once */
-        char *h = stage_take(total);
-        size_t o = 0;
-        for (int c = 0; c < b->n_cols; c++) {
-            VecArray *a = &b->columns[c];
-            out->cols[c].type = a->type;
-            if (!need || !need[c]) continue;
-            const size_t vb = value_bytes(a->type, n);
-            if (vb) memcpy(h + o, a->type == VEC_BOOL ? (void *)a->buf.bln : (void *)a->buf.i64, vb);
-            out->cols[c].data = blk + o;
-            o += a256(vb);
-            if (a->validity) {
-                const size_t wb = valid_bytes_dev(n);
-                memset(h + o + (wb >= 4 ? wb - 4 : 0), 0, wb >= 4 ? 4 : wb);
-                memcpy(h + o, a->validity, (size_t)vg_vbytes(n));
-                out->cols[c].valid = (const uint32_t *)(blk + o);
-            }
-            o += a256(valid_bytes_dev(n));
-        }
-        if (b->sel) {
-            memcpy(h + o, b->sel, (size_t)b->sel_n * 4);
-            out->d_sel = (const int32_t *)(blk + o);
-            out->sel_n = b->sel_n;
-        }
-        stage_send(blk, h, total);
-        vg_batch_free(b);
-        return 1;
-    }
-    size_t off = 0;
+    /* string columns: where their offsets and characters land, for the
+     * views made once the copies are queued */
+    int n_str = 0;
+    for (int c = 0; c < b->n_cols; c++) n_str += (!need || need[c]) && b->columns[c].type == VEC_STRING;
+    size_t *str_at = n_str ? (size_t *)vg_xcalloc((size_t)b->n_cols, sizeof(size_t)) : NULL;
+    char *h = (!keep_host && total) ? stage_take(total) : NULL;
+    size_t o = 0;
     for (int c = 0; c < b->n_cols; c++) {
         VecArray *a = &b->columns[c];
         out->cols[c].type = a->type;
         if (!need || !need[c]) continue;
-        char *dv = blk + off;
-        off += a256(value_bytes(a->type, n));
-        vg_h2d(dv, a->type == VEC_BOOL ? (void *)a->buf.bln : (void *)a->buf.i64, value_bytes(a->type, n));
-        out->cols[c].data = dv;
-        if (a->validity) {
-            char *dm = blk + off;
-            off += a256(valid_bytes_dev(n));
-            if (vg_vbytes(n) & 3) vg_dmemset(dm + (vg_vbytes(n) & ~(int64_t)3), 0, 4);
-            vg_h2d(dm, a->validity, (size_t)vg_vbytes(n));
-            out->cols[c].valid = (const uint32_t *)dm;
+        const size_t wb = valid_bytes_dev(n);
+        if (a->type == VEC_STRING) {
+            /* views, validity, offsets, characters */
+            out->cols[c].data = blk + o;
+            const size_t ov = o + a256((size_t)n * 16);
+            const size_t oo = ov + a256(wb);
+            const size_t oc = oo + a256((size_t)(n + 1) * 8);
+            const size_t nb = str_bytes(a, n);
+            check_offsets(a, n);
+            if (n > 0) {
+                if (h) {
+                    memcpy(h + oo, a->buf.str.offsets, (size_t)(n + 1) * 8);
+                    if (nb) memcpy(h + oc, a->buf.str.data, nb);
+                } else {
+                    vg_h2d(blk + oo, a->buf.str.offsets, (size_t)(n + 1) * 8);
+                    vg_h2d(blk + oc, a->buf.str.data, nb);
+                }
+            }
+            str_at[c] = o;
+            o = ov;
         } else {
-            off += a256(valid_bytes_dev(n));
+            const size_t vb = value_bytes(a->type, n);
+            void *src = a->type == VEC_BOOL ? (void *)a->buf.bln : (void *)a->buf.i64;
+            if (h) { if (vb) memcpy(h + o, src, vb); }
+            else vg_h2d(blk + o, src, vb);
+            out->cols[c].data = blk + o;
+            o += a256(vb);
         }
+        if (a->validity) {
+            if (h) {
+                memset(h + o + (wb >= 4 ? wb - 4 : 0), 0, wb >= 4 ? 4 : wb);
+                memcpy(h + o, a->validity, (size_t)vg_vbytes(n));
+            } else {
+                if (vg_vbytes(n) & 3) vg_dmemset(blk + o + (vg_vbytes(n) & ~(int64_t)3), 0, 4);
+                vg_h2d(blk + o, a->validity, (size_t)vg_vbytes(n));
+            }
+            out->cols[c].valid = (const uint32_t *)(blk + o);
+        }
+        o += a256(wb);
+        if (a->type == VEC_STRING) o += a256((size_t)(n + 1) * 8) + a256(str_bytes(a, n) + 1);
     }
     if (b->sel) {
-        int32_t *ds = (int32_t *)(blk + off);
-        vg_h2d(ds, b->sel, (size_t)b->sel_n * 4);
-        out->d_sel = ds;
+        if (h) memcpy(h + o, b->sel, (size_t)b->sel_n * 4);
+        else vg_h2d(blk + o, b->sel, (size_t)b->sel_n * 4);
+        out->d_sel = (const int32_t *)(blk + o);
         out->sel_n = b->sel_n;
     }
+    if (h) stage_send(blk, h, total);
+    for (int c = 0; n_str && c < b->n_cols; c++) {
+        if ((need && !need[c]) || b->columns[c].type != VEC_STRING) continue;
+        const size_t ov = str_at[c] + a256((size_t)n * 16);
+        const size_t oo = ov + a256(valid_bytes_dev(n));
+        const size_t oc = oo + a256((size_t)(n + 1) * 8);
+        vg_check_rc(vgk_str_views((const int64_t *)(blk + oo), blk + oc, n, (VgStrView *)(blk + str_at[c]),
+                                  vg_stream()), "string column upload");
+    }
+    free(str_at);
     if (keep_host) {
         out->host = b;
     } else {
-        vg_sync();
+        if (!h) vg_sync();
         vg_batch_free(b);
     }
     return 1;
+}
+
+/* A device string column (views) -> newly malloc'd host VecArray in the
+ * reference's layout, rows d_idx[j] (or j; a negative id gives NA). */
+VecArray vg_download_strings(const VgCol *c, const int32_t *d_idx, int64_t n) {
+    VecArray a;
+    memset(&a, 0, sizeof(a));
+    a.type = VEC_STRING;
+    a.length = n;
+    a.owns_data = 1;
+    a.validity = (uint8_t *)vg_xcalloc((size_t)vg_vbytes(n) + 1, 1);
+    a.buf.str.offsets = (int64_t *)vg_xcalloc((size_t)n + 1, 8);
+    if (n <= 0) {
+        a.buf.str.data = (char *)vg_xcalloc(1, 1);
+        return a;
+    }
+    const size_t sb = vgk_scan_scratch(n);
+    char *blk = (char *)vg_dmalloc(a256((size_t)n * 4) + a256((size_t)(n + 1) * 8) + a256(valid_bytes_dev(n)) + sb);
+    int32_t *len = (int32_t *)blk;
+    int64_t *offs = (int64_t *)(blk + a256((size_t)n * 4));
+    uint32_t *val = (uint32_t *)((char *)offs + a256((size_t)(n + 1) * 8));
+    void *scr = (char *)val + a256(valid_bytes_dev(n));
+    vg_check_rc(vgk_str_lengths(c, d_idx, n, len, val, vg_stream()), "string download");
+    vg_check_rc(vgk_exclusive_scan(len, n, offs, offs + n, scr, sb, vg_stream()), "string download");
+    vg_d2h(a.buf.str.offsets, offs, (size_t)(n + 1) * 8);
+    vg_d2h(a.validity, val, (size_t)vg_vbytes(n));
+    vg_sync();
+    const int64_t total = a.buf.str.offsets[n];
+    char *d_chars = (char *)vg_dmalloc((size_t)total + 1);
+    vg_check_rc(vgk_str_pack(c, d_idx, n, offs, d_chars, vg_stream()), "string download");
+    a.buf.str.data = (char *)vg_xmalloc((size_t)total + 1);
+    a.buf.str.data_len = total;
+    vg_d2h(a.buf.str.data, d_chars, (size_t)total);
+    vg_sync();
+    vg_dfree(d_chars);
+    vg_dfree(blk);
+    return a;
 }
 
 void vg_dbatch_release(VgDBatch *b) {

@@ -75,6 +75,8 @@ void vg_dbatch_release(VgDBatch *b);
 
 /* Device column -> newly malloc'd host VecArray of n values. */
 VecArray vg_download_column(int type, const void *d_data, const uint32_t *d_valid, int64_t n);
+/* Device string column (views) -> host VecArray of rows d_idx[j] (or j). */
+VecArray vg_download_strings(const VgCol *c, const int32_t *d_idx, int64_t n);
 VecArray vg_host_column(int type, int64_t n, void *values, const uint32_t *d_valid);
 /* Newly malloc'd host VecArray of n values copied from host memory (values
  * of value_bytes(type, n), validity as the device's 32-bit words). */
@@ -97,6 +99,20 @@ void vg_host_bufs_wait(VgHostBufs *h);
 void vg_host_bufs_wait_upto(VgHostBufs *h, size_t bytes);   /* the first `bytes` of every buffer */
 void *vg_host_bufs_take(VgHostBufs *h, int b, size_t need);   /* NULL: too small or taken */
 void vg_host_bufs_free(VgHostBufs *h);
+
+/* ---- string dictionaries (strdict.c) ---- */
+typedef struct VgDict VgDict;
+VgDict *vg_dict_new(void);
+void vg_dict_free(VgDict *D);
+/* d_codes[p] for the logical rows p of string column c (insert: new
+ * strings get the next codes; otherwise absent strings get -1) */
+void vg_dict_encode(VgDict *D, const VgCol *c, const int32_t *d_sel, int64_t n_logical, int insert,
+                    int64_t *d_codes);
+int64_t vg_dict_size(VgDict *D);
+const VgStrDict *vg_dict_device(VgDict *D);
+void vg_dict_order(VgDict *D, int32_t **d_perm, int64_t **d_rank);
+VecArray vg_dict_strings(VgDict *D, const int64_t *d_codes, const uint32_t *d_valid, const int32_t *d_perm,
+                         int64_t n);
 
 /* ---- .vtr scan (scan_vtr.c) ---- */
 int vg_is_vtr_scan(const VecNode *n);

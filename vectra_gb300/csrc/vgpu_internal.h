@@ -37,6 +37,17 @@ typedef struct {
     const uint32_t *valid;
 } VgCol;
 
+/* A string value on the device: its length, its first four bytes packed
+ * big-endian and zero-padded (two prefixes compare as the strings do, so
+ * most comparisons end there), and a pointer to its bytes.  A VEC_STRING
+ * column's data is one view per row; the bytes live in the batch's own
+ * device block (or a dictionary's arena). */
+typedef struct {
+    uint32_t len;
+    uint32_t pre;
+    const char *ptr;
+} VgStrView;
+
 #define VG_MAX_COLS   24
 #define VG_MAX_TERMS  12
 #define VG_MAX_KEYS   4
@@ -100,8 +111,17 @@ enum {
     VI_NOT,
     VI_IS_NA,
     VI_NEG_I64,
-    VI_NEG_F64
+    VI_NEG_F64,
+    /* strings: a string cell holds a pointer to its bytes and its length */
+    VI_COL_STR,       /* push column a (string views)      */
+    VI_LIT_STR,       /* push pool bytes [imm, imm + a)    */
+    VI_CMP_STR,       /* a = cmp code: memcmp, then length */
+    VI_NCHAR,         /* top: string -> int64 byte count   */
+    VI_SUBSTR,        /* (s, start, stop) -> substring     */
+    VI_GREPL,         /* top: string -> contains pool bytes [imm, imm + a) */
+    VI_F2I            /* top: double -> int64, toward zero */
 };
+#define VG_PROG_POOL 512   /* bytes of string literals per program */
 enum { VG_CMP_EQ = 0, VG_CMP_NE, VG_CMP_LT, VG_CMP_LE, VG_CMP_GT, VG_CMP_GE };
 
 typedef struct {
@@ -114,8 +134,9 @@ typedef struct {
     int32_t n;
     int32_t result_type;     /* VecType of the value left on the stack */
     int32_t max_depth;
-    int32_t pad;
+    int32_t pool_n;          /* bytes of pool in use */
     VgInsn insn[VG_MAX_INSNS];
+    char pool[VG_PROG_POOL]; /* string literals (no terminators) */
 } VgProg;
 
 /* ------------------------------------------------------------------ */
@@ -192,6 +213,28 @@ typedef struct {
     uint32_t *n_used;        /* number of occupied slots */
     uint32_t *err;           /* error word: nonzero = a bounded wait expired / table full */
 } VgGroupTable;
+
+/* A string dictionary: every distinct string gets the next int64 code and
+ * a copy of its bytes in the arena; slot[] is an open-addressing table of
+ * codes (0xFFFFFFFF empty, 0xFFFFFFFE being filled).  The host keeps
+ * room for every row of a launch before it (table at most half full). */
+#define VG_DICT_CODES  0     /* ctr[]: codes given out */
+#define VG_DICT_USED   1     /*        arena bytes used */
+#define VG_DICT_ROWS   2     /*        pre-pass: valid rows of the batch */
+#define VG_DICT_BYTES  3     /*        pre-pass: their bytes */
+#define VG_DICT_MAXLEN 4     /*        longest string seen */
+#define VG_DICT_CTRS   8
+typedef struct {
+    int64_t   cap;           /* slots, power of two */
+    uint32_t *slot;
+    int64_t   codes_cap;
+    uint64_t *c_hash;
+    int64_t  *c_off;
+    uint32_t *c_len;
+    char     *arena;
+    int64_t   arena_cap;
+    unsigned long long *ctr; /* VG_DICT_CTRS counters */
+} VgStrDict;
 
 /* Build-row payload inlined into a copy of a single-key join table's
  * slots (same capacity and slot positions): one 32-byte sector per probe
@@ -492,6 +535,35 @@ int vgk_join_probe_emit(const VgJoinTable *jt, int64_t n_rows, const int32_t *d_
 int vgk_join_unmatched_build(const uint32_t *d_matched, int64_t n_build, int32_t *d_out, int64_t *h_n,
                              void *d_scratch, size_t scratch_bytes, vg_stream_t s);
 const char *vgk_join_last_error(void);
+
+/* strings (k_strings.cu) */
+const char *vgk_str_last_error(void);
+/* views of n rows in the reference's layout (offsets n + 1, bytes) */
+int vgk_str_views(const int64_t *d_offs, const char *d_bytes, int64_t n, VgStrView *d_out, vg_stream_t s);
+/* lengths of rows d_idx[j] (or j; NA and negative ids: 0) and, d_valid
+ * given, the validity words of the packed column */
+int vgk_str_lengths(const VgCol *c, const int32_t *d_idx, int64_t n, int32_t *d_len, uint32_t *d_valid,
+                    vg_stream_t s);
+/* their bytes to d_out + d_offs[j] */
+int vgk_str_pack(const VgCol *c, const int32_t *d_idx, int64_t n, const int64_t *d_offs, char *d_out,
+                 vg_stream_t s);
+int vgk_dict_prepass(const VgCol *c, const int32_t *d_sel, int64_t n_logical, unsigned long long *d_ctr,
+                     vg_stream_t s);
+/* d_codes[p] of the logical rows p: the string's code (insert: new strings
+ * get codes; otherwise -1 for a string not present); NA rows: 0 */
+int vgk_dict_encode(const VgStrDict *d, const VgCol *c, const int32_t *d_sel, int64_t n_logical, int insert,
+                    int64_t *d_codes, uint32_t *d_err, vg_stream_t s);
+int vgk_dict_rehash(const VgStrDict *d, int64_t n_codes, uint32_t *d_err, vg_stream_t s);
+/* views of the strings of d_codes[j] (through d_map when given) */
+int vgk_dict_views(const VgStrDict *d, const int64_t *d_codes, const uint32_t *d_valid, const int32_t *d_map,
+                   int64_t n, VgStrView *d_out, vg_stream_t s);
+/* (n_chunks + 1) int64 columns of n_codes rows whose lexicographic order
+ * is the strings' order */
+int vgk_dict_chunks(const VgStrDict *d, int64_t n_codes, int n_chunks, int64_t *d_out, vg_stream_t s);
+int vgk_rank_of(const int32_t *d_perm, int64_t n, int64_t *d_rank, vg_stream_t s);
+/* key word k of the listed group-table slots replaced by d_rank[word] */
+int vgk_group_keys_remap(const VgGroupTable *gt, int k, const int32_t *d_slots, int64_t n, const int64_t *d_rank,
+                         vg_stream_t s);
 
 /* sort / scan building blocks */
 size_t vgk_sort_pairs_scratch(int64_t n);

@@ -90,8 +90,10 @@ class Expr:
         if k == abi.EXPR_ARITH:
             lt, rt = self.kw["left"].result_type(schema), self.kw["right"].result_type(schema)
             return abi.VEC_DOUBLE if abi.VEC_DOUBLE in (lt, rt) else abi.VEC_INT64
-        if k in (abi.EXPR_CMP, abi.EXPR_BOOL, abi.EXPR_IS_NA): return abi.VEC_BOOL
+        if k in (abi.EXPR_CMP, abi.EXPR_BOOL, abi.EXPR_IS_NA, abi.EXPR_GREPL): return abi.VEC_BOOL
         if k == abi.EXPR_NEGATE: return self.kw["operand"].result_type(schema)
+        if k == abi.EXPR_LIT_STRING or k == abi.EXPR_SUBSTR: return abi.VEC_STRING
+        if k == abi.EXPR_NCHAR: return abi.VEC_INT64
         return abi.VEC_DOUBLE
 
     def to_c(self, schema):
@@ -110,6 +112,8 @@ class Expr:
             x.lit_dbl = float(kw["value"])
         elif self.kind == abi.EXPR_LIT_BOOL:
             x.lit_bln = 1 if kw["value"] else 0
+        if "text" in kw:                       # string literal / grepl pattern
+            x.lit_str = c_strdup(kw["text"])
         if "op" in kw:
             op = kw["op"]
             x.op = op[0].encode()
@@ -127,6 +131,8 @@ def col(name):
 def lit(v, na_type=abi.VEC_DOUBLE):
     if v is None:
         return Expr(abi.EXPR_LIT_NA, type=na_type)
+    if isinstance(v, str):
+        return Expr(abi.EXPR_LIT_STRING, text=v)
     if isinstance(v, (bool, np.bool_)):
         return Expr(abi.EXPR_LIT_BOOL, value=bool(v))
     if isinstance(v, (int, np.integer)):
@@ -140,6 +146,21 @@ def wrap(v):
 
 def is_na(e):
     return Expr(abi.EXPR_IS_NA, operand=wrap(e))
+
+
+def nchar(e):
+    """nchar(x): bytes of a string (src/expr.c:153-170)."""
+    return Expr(abi.EXPR_NCHAR, operand=wrap(e))
+
+
+def substr(e, start, stop):
+    """substr(x, start, stop), 1-based, stop inclusive (src/expr.c:172-235)."""
+    return Expr(abi.EXPR_SUBSTR, operand=wrap(e), left=wrap(start), right=wrap(stop))
+
+
+def grepl(pattern, e):
+    """grepl(pattern, x, fixed = TRUE) (src/expr.c:237-268)."""
+    return Expr(abi.EXPR_GREPL, operand=wrap(e), text=pattern)
 
 
 # ---------------------------------------------------------------------------
