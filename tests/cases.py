@@ -464,6 +464,67 @@ def r_string_group(E, seed, n, batch_rows, sel_mode, temp_dir):
             .group_by("s", "k").summarise(temp_dir=temp_dir, n=("n",), s1=("sum", "x"), c=("count", "x")).batches())
 
 
+def sj_string_keys(E):              # test-joins.R:133-147
+    l = T(name=["alice", "bob"], x=[1.0, 2.0])
+    r = T(name=["bob", "carol"], y=[20.0, 30.0])
+    out = []
+    for kind in ("inner_join", "left_join", "semi_join", "anti_join", "full_join"):
+        out += getattr(tbl(E, l), kind)(tbl(E, r), "name").batches()
+    return out
+
+
+def sj_composite_string_key(E):     # test-joins.R:149-160
+    l = T(a=[1.0, 1.0, 2.0], b=["x", "y", "x"], v1=[10.0, 20.0, 30.0])
+    r = T(a=[1.0, 2.0], b=["x", "x"], v2=[100.0, 300.0])
+    return (tbl(E, l).inner_join(tbl(E, r), ["a", "b"]).batches()
+            + tbl(E, l).full_join(tbl(E, r), ["a", "b"]).batches())
+
+
+def sj_many_string_keys(E):         # test-joins.R:164-190: 200 keys, duplicates, string payloads
+    rng = np.random.default_rng(42)
+    keys = ["key_%d" % i for i in range(1, 201)]
+    l = {"id": np.array([k for k in keys for _ in range(3)], dtype=object), "x": rng.normal(0, 1, 600)}
+    r = {"id": np.array(keys[::2] + ["key_x%d" % i for i in range(20)], dtype=object),
+         "tag": np.array(["t%d" % (i % 7) for i in range(120)], dtype=object), "y": rng.normal(0, 1, 120)}
+    return (tbl(E, l, batch_rows=128).left_join(tbl(E, r, batch_rows=50), "id").batches()
+            + tbl(E, l, batch_rows=128).full_join(tbl(E, r, batch_rows=50), "id").batches())
+
+
+def sj_na_and_empty_string_keys(E):  # NA never matches; "" is a key like any other
+    l = T(k=["", NA, "a", "b", NA, ""], x=[1, 2, 3, 4, 5, 6])
+    r = T(k=[NA, "", "a", "a", "c"], y=["p", "q", NA, "s", "t"])
+    out = []
+    for kind in ("inner_join", "left_join", "semi_join", "anti_join", "full_join"):
+        out += getattr(tbl(E, l), kind)(tbl(E, r), "k").batches()
+    return out
+
+
+def r_string_join(E, seed, n, batch_rows, kind):
+    rng = np.random.default_rng(seed)
+    lk = random_strings(rng, n, 40, maxlen=6)
+    rk = random_strings(rng, 70, 50, maxlen=6)
+    l = {"k": (lk, rng.random(n) > 0.05), "x": rng.normal(0, 1, n), "s": (random_strings(rng, n, 9), rng.random(n) > 0.1)}
+    r = {"k": (rk, rng.random(70) > 0.05), "y": rng.normal(0, 1, 70), "t": (random_strings(rng, 70, 5), rng.random(70) > 0.1)}
+    return getattr(tbl(E, l, batch_rows=batch_rows), kind)(tbl(E, r, batch_rows=32), "k").batches()
+
+
+STRING_JOIN_CASES = [sj_string_keys, sj_composite_string_key, sj_many_string_keys, sj_na_and_empty_string_keys]
+
+
+def ss_string_keys(E):              # arrange by strings: NA last ascending, first descending
+    t = T(s=["b", NA, "a", "", "ab", "b", "\u00e9", "aa", NA, "B"], i=[1, 2, 3, 4, 5, 6, 7, 8, 9, 10],
+          u=["x", "y", NA, "z", "w", "v", "u", "t", "s", "r"])
+    return (tbl(E, t).arrange("s").batches() + tbl(E, t).arrange(("s", True)).batches()
+            + tbl(E, t).arrange("u", ("i", True)).batches())
+
+
+def r_string_sort(E, seed, n, batch_rows):
+    rng = np.random.default_rng(seed)
+    t = {"s": (random_strings(rng, n, max(n // 5, 2), maxlen=14), rng.random(n) > 0.05),
+         "k": rng.integers(0, 4, n), "x": rng.normal(0, 1, n), "p": (random_strings(rng, n, 50), rng.random(n) > 0.1)}
+    return tbl(E, t, batch_rows=batch_rows).arrange("k", ("s", True), "x").batches()
+
+
 STRING_FILTER_CASES = [sf_nchar, sf_substr, sf_grepl, sf_compare_literal, sf_compare_columns, sf_substr_bounds,
                        sf_substr_filter, sf_nchar_filter, sf_passthrough]
 STRING_GROUP_CASES = [sg_string_key, sg_string_and_int_keys, sg_string_arena_resizes, sg_filter_on_string]

@@ -12,6 +12,8 @@ from engines import OracleEngine
 
 pytestmark = pytest.mark.gpu
 
+NA_F = None
+
 
 def _gpu():
     import vectra_gb300
@@ -46,13 +48,11 @@ def test_sort_over_scan(tmp_path):
     cases.same_batches(got, want)
 
 
-def test_string_columns_are_an_error():
+def test_string_columns_are_carried():
     """A child with a string column (here the oracle's own source node, as a
-    reference scan would deliver it): an explicit error, no fallback."""
-    from vectra_gb300.plan import EngineError, Tbl
-    G = _gpu()
-    t = cases.T(x=[2.0, 1.0])
-    t["s"] = (["b", "a"], np.array([True, True]))
-    src = OracleEngine().make_source(t)
-    with pytest.raises(EngineError, match="string column 's'"):
-        Tbl(G, src).arrange("x").batches()
+    reference scan would deliver it): the strings travel in the sort's order."""
+    from vectra_gb300.plan import Tbl
+    G, O = _gpu(), OracleEngine()
+    t = cases.T(x=[2.0, 1.0, NA_F, 0.5])
+    t["s"] = (["b", "a", "c", "d"], np.array([True, True, False, True]))
+    cases.same_batches(Tbl(G, O.make_source(t)).arrange("x").batches(), Tbl(O, O.make_source(t)).arrange("x").batches())

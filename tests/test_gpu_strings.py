@@ -96,3 +96,71 @@ def test_string_aggregate_input_is_an_error(G):
     t = cases.T(g=[1, 2], s=["a", "b"])
     with pytest.raises(EngineError):
         tbl(G, t).group_by("g").summarise(m=("min", "s")).batches()
+
+
+@pytest.mark.parametrize("case", cases.STRING_JOIN_CASES, ids=lambda f: f.__name__)
+def test_string_join_cases(case, G, oracle):
+    """String join keys (one dictionary: build strings inserted, probe
+    strings looked up) and string columns carried on both sides."""
+    cases.same_batches(case(G), case(oracle))
+
+
+@pytest.mark.parametrize("kind", ["inner_join", "left_join", "semi_join", "anti_join", "full_join"])
+@pytest.mark.parametrize("n,batch", [(0, 32), (33, 32), (500, 64), (20_000, 4096)])
+def test_random_string_join(kind, n, batch, G, oracle):
+    cases.same_batches(cases.r_string_join(G, n + 3, n, batch, kind),
+                       cases.r_string_join(oracle, n + 3, n, batch, kind))
+
+
+@pytest.mark.parametrize("temp_dir", ["tmp", None], ids=["sorted", "hash"])
+def test_join_then_group_by_strings(temp_dir, G, oracle):
+    """group_by a build-side string column after a string-key join (the
+    aggregation consumes the join's batches), and group_by a probe-side
+    string column above an int64-key join (fused)."""
+    from vectra_gb300.plan import tbl
+    rng = np.random.default_rng(12)
+    n = 40_000
+    cats = np.array(["c%02d" % i for i in range(30)], dtype=object)
+    fact = {"name": (cases.random_strings(rng, n, 300, maxlen=8), rng.random(n) > 0.02), "v": rng.lognormal(0, 1, n),
+            "id": rng.integers(0, 500, n), "city": (cats[rng.integers(0, 30, n)], rng.random(n) > 0.05)}
+    names = cases.random_strings(rng, 250, 260, maxlen=8)
+    _, first = np.unique(names, return_index=True)
+    dim_s = {"name": names[np.sort(first)], "grp": cats[rng.integers(0, 30, len(first))]}
+    dim_i = {"id": np.arange(500), "w": rng.random(500)}
+    td = None if temp_dir is None else oracle.tmp
+
+    def q1(E):
+        return (tbl(E, fact, batch_rows=8192).inner_join(tbl(E, dim_s), "name").group_by("grp")
+                .summarise(temp_dir=td, s=("sum", "v"), n=("n",)).batches())
+
+    def q2(E):
+        return (tbl(E, fact, batch_rows=8192).left_join(tbl(E, dim_i), "id").group_by("city")
+                .summarise(temp_dir=td, s=("sum", "w", True), n=("n",)).batches())
+    cases.same_batches(q1(G), q1(oracle), rtol=1e-12, tol_cols=("s",))
+    cases.same_batches(q2(G), q2(oracle), rtol=1e-12, tol_cols=("s",))
+
+
+def test_string_sort_case(G, oracle):
+    """arrange() by string keys (dictionary ranks) with string columns
+    carried, in both directions."""
+    cases.same_batches(cases.ss_string_keys(G), cases.ss_string_keys(oracle))
+
+
+@pytest.mark.parametrize("n,batch", [(0, 32), (33, 32), (2000, 256), (300_000, 65_536)])
+def test_random_string_sort(n, batch, G, oracle):
+    cases.same_batches(cases.r_string_sort(G, n + 1, n, batch), cases.r_string_sort(oracle, n + 1, n, batch))
+
+
+def test_string_order_long_prefixes(G):
+    """60k distinct strings of 0-33 'p's and a number, sorted three times:
+    the dictionary's 8-byte order words past each string's end must be
+    zero (they once picked up an earlier byte of the string, so a string
+    could sort after a longer one it prefixes)."""
+    from vectra_gb300.plan import tbl
+    rng = np.random.default_rng(8)
+    pool = sorted({"%s%d" % ("p" * int(rng.integers(0, 34)), i) for i in range(60_000)})
+    want = sorted(pool, key=lambda s: s.encode())
+    t = {"g": np.array(pool, dtype=object), "i": np.arange(len(pool))}
+    for _ in range(3):
+        got = tbl(G, t, batch_rows=100_000).arrange("g").batches()[0]["g"][0]
+        assert list(got) == want

@@ -95,3 +95,24 @@ def test_random_string_group(n, batch, temp_dir, oracle, ref):
     td = None if temp_dir is None else ref.tmp
     cases.same_batches(cases.r_string_group(oracle, n + 9, n, batch, 1, td),
                        cases.r_string_group(ref, n + 9, n, batch, 1, td))
+
+
+@pytest.mark.parametrize("case", cases.STRING_JOIN_CASES, ids=lambda f: f.__name__)
+def test_string_join_cases(case, oracle, ref):
+    cases.same_batches(case(oracle), case(ref))
+
+
+@pytest.mark.parametrize("kind", ["inner_join", "left_join", "semi_join", "anti_join", "full_join"])
+@pytest.mark.parametrize("n,batch", [(0, 32), (33, 32), (500, 64)])
+def test_random_string_join(kind, n, batch, oracle, ref):
+    cases.same_batches(cases.r_string_join(oracle, n + 3, n, batch, kind),
+                       cases.r_string_join(ref, n + 3, n, batch, kind))
+
+
+def test_string_sort_case(oracle, ref):
+    cases.same_batches(cases.ss_string_keys(oracle), cases.ss_string_keys(ref))
+
+
+@pytest.mark.parametrize("n,batch", [(0, 32), (33, 32), (2000, 256)])
+def test_random_string_sort(n, batch, oracle, ref):
+    cases.same_batches(cases.r_string_sort(oracle, n + 1, n, batch), cases.r_string_sort(ref, n + 1, n, batch))

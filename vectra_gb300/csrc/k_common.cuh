@@ -64,8 +64,14 @@ VG_DEV uint64_t vg_load_bits(const VgCol &c, int64_t r) {
 
 // the first four bytes of a string, big-endian, zero-padded
 VG_DEV uint32_t vg_str_pre(const char *p, uint32_t len) {
+    if (len == 0) return 0;
+    const uint32_t last = len - 1;
     uint32_t pre = 0;
-    for (uint32_t i = 0; i < 4; i++) pre = (pre << 8) | (i < len ? (uint32_t)(unsigned char)p[i] : 0u);
+    for (uint32_t i = 0; i < 4; i++) {
+        // read at a clamped position inside the string, then mask
+        const uint32_t b = (uint32_t)(unsigned char)p[i < last ? i : last];
+        pre = (pre << 8) | (i < len ? b : 0u);
+    }
     return pre;
 }
 

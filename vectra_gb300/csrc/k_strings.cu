@@ -64,8 +64,17 @@ VG_DEV uint64_t str_hash(const char *p, uint32_t len) {
         h = (h ^ w) * 0xFF51AFD7ED558CCDull;
         h ^= h >> 32;
     }
+    // the tail: up to 7 bytes, each read at a clamped position inside the
+    // string and masked
     uint64_t w = 0;
-    for (uint32_t k = 0; i + k < len; k++) w |= (uint64_t)(unsigned char)p[i + k] << (8 * k);
+    if (i < len) {
+        const uint32_t last = len - 1;
+        for (uint32_t k = 0; k < 8; k++) {
+            const uint32_t at = i + k;
+            const uint64_t b = (uint64_t)(unsigned char)p[at < last ? at : last];
+            w |= (at < len ? b : 0ull) << (8 * k);
+        }
+    }
     h = (h ^ w) * 0xC4CEB9FE1A85EC53ull;
     h ^= h >> 29;
     h *= 0xFF51AFD7ED558CCDull;
@@ -269,13 +278,18 @@ __global__ void dict_views_kernel(VgStrDict d, const int64_t *codes, const uint3
 __global__ void dict_chunks_kernel(VgStrDict d, int64_t n_codes, int n_chunks, int64_t *out) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n_codes; c += stride) {
-        const char *s = d.arena + d.c_off[c];
+        const unsigned char *s = (const unsigned char *)d.arena + d.c_off[c];
         const uint32_t len = d.c_len[c];
+        const uint32_t last = len ? len - 1 : 0;
         for (int w = 0; w < n_chunks; w++) {
             uint64_t x = 0;
             for (int k = 0; k < 8; k++) {
+                // every byte is read (at a clamped position inside the
+                // string) and masked, rather than read conditionally
                 const uint32_t at = (uint32_t)w * 8u + (uint32_t)k;
-                x = (x << 8) | (at < len ? (uint64_t)(unsigned char)s[at] : 0ull);
+                const uint32_t b = len ? (uint32_t)s[at < last ? at : last] : 0u;
+                const uint32_t m = at < len ? 0xFFu : 0u;
+                x = (x << 8) | (uint64_t)(b & m);
             }
             out[(int64_t)w * n_codes + c] = (int64_t)(x ^ 0x8000000000000000ull);
         }
@@ -286,6 +300,17 @@ __global__ void dict_chunks_kernel(VgStrDict d, int64_t n_codes, int n_chunks, i
 __global__ void rank_kernel(const int32_t *perm, int64_t n, int64_t *rank) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) rank[perm[r]] = r;
+}
+
+// out[i] = table[codes[i]] where row i is valid (voff: bit offset of row 0)
+__global__ void map_codes_kernel(const int64_t *table, const int64_t *codes, const uint32_t *valid, int voff,
+                                 int64_t n, int64_t *out) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int64_t r = i + voff;
+        const bool ok = valid == nullptr || ((valid[r >> 5] >> (r & 31)) & 1u);
+        out[i] = ok ? table[codes[i]] : 0;
+    }
 }
 
 // key word k of the listed group-table slots: code -> rank (NA keys kept)
@@ -374,6 +399,14 @@ int vgk_rank_of(const int32_t *d_perm, int64_t n, int64_t *d_rank, vg_stream_t s
     rank_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)s>>>(d_perm, n, d_rank);
     vg_launch_counter++;
     return check(cudaGetLastError(), "string dictionary order");
+}
+
+int vgk_map_codes(const int64_t *d_table, const int64_t *d_codes, const uint32_t *d_valid, int voff, int64_t n,
+                  int64_t *d_out, vg_stream_t s) {
+    if (n <= 0) return 0;
+    map_codes_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)s>>>(d_table, d_codes, d_valid, voff, n, d_out);
+    vg_launch_counter++;
+    return check(cudaGetLastError(), "string order");
 }
 
 int vgk_group_keys_remap(const VgGroupTable *gt, int k, const int32_t *d_slots, int64_t n, const int64_t *d_rank,

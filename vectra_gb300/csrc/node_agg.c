@@ -230,7 +230,8 @@ static void plan_build(VgAgg *A, Plan *P) {
     memset(P, 0, sizeof(*P));
     VecNode *n = A->ga.child;
     if (vg_is_project(n)) { P->project = n; n = vg_project_child(n); }
-    if (vg_is_join(n) && (vg_join_kind(n) == JOIN_INNER || vg_join_kind(n) == JOIN_LEFT)) {
+    if (vg_is_join(n) && (vg_join_kind(n) == JOIN_INNER || vg_join_kind(n) == JOIN_LEFT) &&
+        !vg_join_has_string_keys(n)) {
         P->join = n;
         n = vg_join_left(n);
     }

@@ -43,6 +43,16 @@ typedef struct {
     int32_t *d_unmatched;
     int64_t n_unmatched, fin_cursor;
     int64_t batch_idx;
+    /* string keys: both sides' key strings as codes of one dictionary (the
+     * build side's inserted, the probe side's looked up: a string the build
+     * side does not hold gets -1 and matches nothing) */
+    VgDict *dict;
+    int str_key[VG_MAX_KEYS];
+    VgCol bkey_codes[VG_MAX_KEYS];
+    void *codes_block;
+    /* build batches kept whole: the build columns' string views point into them */
+    VgDBatch *bkeep;
+    int bkeep_n;
 } VgJoin;
 
 static VecBatch *join_next(VecNode *self);
@@ -69,7 +79,40 @@ static int common_type(int a, int b) {
 }
 
 static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
-static size_t elem(int t) { return t == VEC_BOOL ? 1 : 8; }
+static size_t elem(int t) { return t == VEC_BOOL ? 1 : t == VEC_STRING ? 16 : 8; }
+
+int vg_join_has_string_keys(VecNode *n) {
+    VgJoin *j = (VgJoin *)n;
+    for (int k = 0; k < j->jn.n_keys; k++)
+        if (j->str_key[k]) return 1;
+    return 0;
+}
+
+/* a host string column of n NA rows */
+static VecArray na_strings(int64_t n) {
+    VecArray a;
+    memset(&a, 0, sizeof(a));
+    a.type = VEC_STRING;
+    a.length = n;
+    a.owns_data = 1;
+    a.validity = (uint8_t *)vg_xcalloc((size_t)vg_vbytes(n) + 1, 1);
+    a.buf.str.offsets = (int64_t *)vg_xcalloc((size_t)n + 1, 8);
+    a.buf.str.data = (char *)vg_xcalloc(1, 1);
+    return a;
+}
+
+/* n rows of a device column gathered by idx (-1: NA) to the host; dv/dm
+ * hold 16 bytes and one validity bit per row */
+static VecArray gather_down(const VgCol *src, const int32_t *idx, int64_t n, char *dv, uint32_t *dm) {
+    vg_check_rc(vgk_gather(src, idx, n, 1, dv, dm, vg_stream()), "join gather");
+    if (src->type != VEC_STRING) return vg_download_column(src->type, dv, dm, n);
+    VgCol v;
+    memset(&v, 0, sizeof(v));
+    v.type = VEC_STRING;
+    v.data = dv;
+    v.valid = dm;
+    return vg_download_strings(&v, NULL, n);
+}
 
 /* BUILD: materialise the right side on the device, then the hash table
  * (and, when a fused aggregation asked for it, the payload copy of up to
@@ -80,12 +123,9 @@ static void join_build(VgJoin *j) {
     int nr = rs->n_cols;
     uint8_t *need = (uint8_t *)vg_xcalloc((size_t)(nr ? nr : 1), 1);
     for (int k = 0; k < j->jn.n_keys; k++) need[j->jn.keys[k].right_col] = 1;
-    for (int q = 0; q < j->r_nonkey_n; q++) {
-        int c = j->r_nonkey[q];
-        if (rs->col_types[c] == VEC_STRING)
-            vg_fail("string column '%s' is not supported by the GPU join", rs->col_names[c]);
-        need[c] = 1;
-    }
+    for (int q = 0; q < j->r_nonkey_n; q++) need[j->r_nonkey[q]] = 1;
+    int has_str = 0;
+    for (int c = 0; c < nr; c++) has_str |= need[c] && rs->col_types[c] == VEC_STRING;
     /* pull every batch, keeping them on the device until the total is known */
     int cap = 16, nb = 0;
     VgDBatch *bs = (VgDBatch *)vg_xcalloc((size_t)cap, sizeof(VgDBatch));
@@ -146,15 +186,40 @@ static void join_build(VgJoin *j) {
         j->B.bcols[c].data = dv;
         j->B.bcols[c].valid = dm;
     }
-    for (int b = 0; b < nb; b++) vg_dbatch_release(&bs[b]);
-    free(bs);
+    if (has_str && nb > 0) {
+        /* the gathered string views point into the batches' blocks */
+        for (int b = 0; b < nb; b++) vg_dkeep(bs[b].block);
+        j->bkeep = bs;
+        j->bkeep_n = nb;
+    } else {
+        for (int b = 0; b < nb; b++) vg_dbatch_release(&bs[b]);
+        free(bs);
+    }
     free(need);
+
+    /* string keys: the build key columns as dictionary codes */
+    int n_skeys = 0;
+    for (int k = 0; k < j->jn.n_keys; k++) n_skeys += j->str_key[k];
+    if (n_skeys) {
+        j->dict = vg_dict_new_kept();
+        const size_t per = a256((size_t)(total > 0 ? total : 1) * 8);
+        j->codes_block = vg_dmalloc_kept(per * (size_t)j->jn.n_keys);
+        for (int k = 0; k < j->jn.n_keys; k++) {
+            if (!j->str_key[k]) continue;
+            const VgCol *sc = &j->B.bcols[j->jn.keys[k].right_col];
+            int64_t *codes = (int64_t *)((char *)j->codes_block + per * (size_t)k);
+            vg_dict_encode(j->dict, sc, NULL, total, 1, codes);
+            j->bkey_codes[k] = *sc;
+            j->bkey_codes[k].type = VEC_INT64;
+            j->bkey_codes[k].data = codes;
+        }
+    }
 
     /* hash table, or a direct-addressed one when the only key is an int64
      * column whose values span at most twice the build rows (dense ids) */
     int nk = j->jn.n_keys;
     VgCol kc[VG_MAX_KEYS];
-    for (int k = 0; k < nk; k++) kc[k] = j->B.bcols[j->jn.keys[k].right_col];
+    for (int k = 0; k < nk; k++) kc[k] = j->str_key[k] ? j->bkey_codes[k] : j->B.bcols[j->jn.keys[k].right_col];
     int direct = 0;
     int64_t dmin = 0, drange = 0;
     if (nk == 1 && j->key_type[0] == VEC_INT64 && kc[0].type == VEC_INT64 && total > 0) {
@@ -254,7 +319,7 @@ void vg_join_ensure_slots(VecNode *n) {
         /* compact entries hold neither keys nor build rows: the slots come
          * from the key column */
         void *scratch = vg_dmalloc((size_t)(j->B.jt.n_build > 0 ? j->B.jt.n_build : 1) * 4 + 256);
-        const VgCol kc = j->B.bcols[j->jn.keys[0].right_col];
+        const VgCol kc = j->str_key[0] ? j->bkey_codes[0] : j->B.bcols[j->jn.keys[0].right_col];
         const int rc = vgk_join_slots_from_keys(&j->B.jt, &kc, j->conv_build[0], j->B.jt.n_build, scratch,
                                                 vg_stream());
         vg_dfree(scratch);
@@ -276,13 +341,8 @@ static VecBatch *probe_one(VgJoin *j) {
     int semi = (j->jn.kind == JOIN_SEMI || j->jn.kind == JOIN_ANTI);
     uint8_t *need = (uint8_t *)vg_xcalloc((size_t)(nl ? nl : 1), 1);
     for (int k = 0; k < nk; k++) need[j->jn.keys[k].left_col] = 1;
-    if (!semi) {
-        for (int c = 0; c < nl; c++) {
-            if (ls->col_types[c] == VEC_STRING)
-                vg_fail("string column '%s' is not supported by the GPU join", ls->col_names[c]);
-            need[c] = 1;
-        }
-    }
+    if (!semi)
+        for (int c = 0; c < nl; c++) need[c] = 1;
     for (;;) {
         VgDBatch db;
         if (!vg_pull(j->jn.left, need, semi, &db)) { free(need); return NULL; }
@@ -290,13 +350,26 @@ static VecBatch *probe_one(VgJoin *j) {
         int64_t n = db.d_sel ? db.sel_n : db.n_rows;
         VgCol pk[VG_MAX_KEYS];
         for (int k = 0; k < nk; k++) pk[k] = db.cols[j->jn.keys[k].left_col];
+        /* string keys: the probe strings' codes (looked up, not inserted) */
+        char *pcodes = NULL;
+        if (j->dict) {
+            const size_t per = a256((size_t)(db.n_rows > 0 ? db.n_rows : 1) * 8);
+            pcodes = (char *)vg_dmalloc(per * (size_t)nk);
+            for (int k = 0; k < nk; k++) {
+                if (!j->str_key[k]) continue;
+                int64_t *codes = (int64_t *)(pcodes + per * (size_t)k);
+                vg_dict_encode(j->dict, &pk[k], db.d_sel, n, 0, codes);
+                pk[k].type = VEC_INT64;
+                pk[k].data = codes;
+            }
+        }
         size_t sb = vgk_join_probe_scratch_bytes(n);
         void *scratch = vg_dmalloc(sb);
         int64_t total = 0;
         int rc = vgk_join_probe_count(&j->B.jt, pk, nk, j->B.conv, db.n_rows, db.d_sel, db.sel_n,
                                       j->jn.kind, scratch, sb, &total, vg_stream());
         if (rc) { vg_dfree(scratch); vg_dbatch_release(&db); vg_check_rc(rc, "join probe"); }
-        if (total == 0) { vg_dfree(scratch); vg_dbatch_release(&db); continue; }
+        if (total == 0) { vg_dfree(scratch); vg_dfree(pcodes); vg_dbatch_release(&db); continue; }
         int32_t *pairs = (int32_t *)vg_dmalloc((size_t)total * 8 + 16);
         int32_t *op = pairs, *ob = semi ? NULL : pairs + total;
         rc = vgk_join_probe_emit(&j->B.jt, db.n_rows, db.d_sel, db.sel_n, j->jn.kind, scratch, sb, op, ob,
@@ -318,23 +391,23 @@ static VecBatch *probe_one(VgJoin *j) {
             int oc = j->jn.base.output_schema.n_cols;
             out = vg_batch_alloc(oc, total);
             size_t wb = (size_t)((total + 31) / 32) * 4;
-            size_t per = a256((size_t)total * 8) + a256(wb);
+            size_t per = a256((size_t)total * 16) + a256(wb);
             char *blk = (char *)vg_dmalloc(per * (size_t)oc + 256);
             for (int c = 0; c < oc; c++) {
                 char *dv = blk + per * (size_t)c;
-                uint32_t *dm = (uint32_t *)(dv + a256((size_t)total * 8));
+                uint32_t *dm = (uint32_t *)(dv + a256((size_t)total * 16));
                 const VgCol *src;
                 const int32_t *idx;
                 if (c < nl) { src = &db.cols[c]; idx = op; }
                 else { src = &j->B.bcols[j->r_nonkey[c - nl]]; idx = ob; }
-                vg_check_rc(vgk_gather(src, idx, total, 1, dv, dm, vg_stream()), "join gather");
-                out->columns[c] = vg_download_column(src->type, dv, dm, total);
+                out->columns[c] = gather_down(src, idx, total, dv, dm);
                 out->col_names[c] = vg_xstrdup(j->jn.base.output_schema.col_names[c]);
             }
             vg_sync();
             vg_dfree(blk);
         }
         vg_dfree(pairs);
+        vg_dfree(pcodes);
         vg_dbatch_release(&db);
         free(need);
         return out;
@@ -361,16 +434,20 @@ static VecBatch *finalize_one(VgJoin *j) {
     int nl = ls->n_cols, oc = j->jn.base.output_schema.n_cols;
     VecBatch *out = vg_batch_alloc(oc, n);
     size_t wb = (size_t)((n + 31) / 32) * 4;
-    size_t per = a256((size_t)n * 8) + a256(wb);
+    size_t per = a256((size_t)n * 16) + a256(wb);
     char *blk = (char *)vg_dmalloc(per * (size_t)oc + 256);
     for (int c = 0; c < oc; c++) {
         char *dv = blk + per * (size_t)c;
-        uint32_t *dm = (uint32_t *)(dv + a256((size_t)n * 8));
+        uint32_t *dm = (uint32_t *)(dv + a256((size_t)n * 16));
         out->col_names[c] = vg_xstrdup(j->jn.base.output_schema.col_names[c]);
         if (c < nl) {
             int rk = -1;
             for (int k = 0; k < j->jn.n_keys; k++)
                 if (j->jn.keys[k].left_col == c) { rk = j->jn.keys[k].right_col; break; }
+            if (rk < 0 && ls->col_types[c] == VEC_STRING) {
+                out->columns[c] = na_strings(n);
+                continue;
+            }
             if (rk < 0) {   /* non-key left column: NA */
                 VecArray a;
                 memset(&a, 0, sizeof(a));
@@ -382,12 +459,14 @@ static VecBatch *finalize_one(VgJoin *j) {
                 out->columns[c] = a;
                 continue;
             }
+            if (j->B.bcols[rk].type == VEC_STRING) {
+                out->columns[c] = gather_down(&j->B.bcols[rk], idx, n, dv, dm);
+                continue;
+            }
             vg_check_rc(vgk_gather(&j->B.bcols[rk], idx, n, 0, dv, dm, vg_stream()), "join finalize gather");
             out->columns[c] = vg_download_column(ls->col_types[c], dv, dm, n);
         } else {
-            const VgCol *src = &j->B.bcols[j->r_nonkey[c - nl]];
-            vg_check_rc(vgk_gather(src, idx, n, 0, dv, dm, vg_stream()), "join finalize gather");
-            out->columns[c] = vg_download_column(src->type, dv, dm, n);
+            out->columns[c] = gather_down(&j->B.bcols[j->r_nonkey[c - nl]], idx, n, dv, dm);
         }
     }
     vg_sync();
@@ -434,6 +513,10 @@ static void join_free(VecNode *self) {
     vg_dfree(j->table_block);
     vg_dfree(j->d_matched);
     vg_dfree(j->d_unmatched);
+    vg_dict_free(j->dict);
+    vg_dfree(j->codes_block);
+    for (int b = 0; b < j->bkeep_n; b++) vg_dbatch_release(&j->bkeep[b]);
+    free(j->bkeep);
     vg_schema_free(&j->jn.base.output_schema);
     free(j);
 }
@@ -458,8 +541,6 @@ JoinNode *join_node_create(VecNode *left, VecNode *right, JoinKind kind, int n_k
             vg_fail("%s key type mismatch: x.%s (%s) vs y.%s (%s)", kind_names[kind],
                     ls->col_names[keys[k].left_col], type_name(lt), rs->col_names[keys[k].right_col],
                     type_name(rt));
-        if (lt == VEC_STRING)
-            vg_fail("string join keys are not supported by the GPU join (%s)", ls->col_names[keys[k].left_col]);
         if (kind == JOIN_FULL && lt != rt)
             vg_fail("full_join with key columns of different types (x.%s %s, y.%s %s) is not supported by the GPU join",
                     ls->col_names[keys[k].left_col], type_name(lt), rs->col_names[keys[k].right_col], type_name(rt));
@@ -477,6 +558,10 @@ JoinNode *join_node_create(VecNode *left, VecNode *right, JoinKind kind, int n_k
     for (int k = 0; k < n_keys; k++) {
         int lt = ls->col_types[keys[k].left_col], rt = rs->col_types[keys[k].right_col];
         int c = common_type(lt, rt);
+        if (lt == VEC_STRING) {   /* both strings: joined on dictionary codes */
+            j->str_key[k] = 1;
+            c = VEC_INT64;
+        }
         j->key_type[k] = c;
         j->conv_build[k] = (rt != c && c == VEC_DOUBLE);
         j->B.conv[k] = (lt != c && c == VEC_DOUBLE);

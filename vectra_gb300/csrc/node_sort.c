@@ -16,7 +16,11 @@
  * (src/sort.c:488-529), an empty batch included.  Where the reference
  * spills runs beyond its 1 GiB budget and merges them in 65,536-row
  * batches, this node keeps everything in HBM and still returns one batch.
- * String columns are an explicit error (no CPU fallback).
+ * A string key sorts by the rank of its string among the column's
+ * distinct strings (a device dictionary, ordered by memcmp with the
+ * shorter string first, the reference's string compare); string columns
+ * travel as device views into the child's batches, which stay resident
+ * until the output is copied out.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -28,7 +32,7 @@ typedef struct {
 } VgSort;
 
 static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
-static size_t elem(int type) { return type == VEC_BOOL ? 1 : 8; }
+static size_t elem(int type) { return type == VEC_BOOL ? 1 : type == VEC_STRING ? 16 : 8; }
 
 static VecBatch *sort_next_body(VecNode *self) {
     VgSort *S = (VgSort *)self;
@@ -37,9 +41,6 @@ static VecBatch *sort_next_body(VecNode *self) {
     VecNode *child = S->sn.child;
     const VecSchema *cs = &child->output_schema;
     const int nc = cs->n_cols;
-    for (int c = 0; c < nc; c++)
-        if (cs->col_types[c] == VEC_STRING)
-            vg_fail("string column '%s' is not supported by the GPU sort", cs->col_names[c]);
     for (int k = 0; k < S->sn.n_keys; k++)
         if (S->sn.keys[k].col_index < 0 || S->sn.keys[k].col_index >= nc)
             vg_fail("sort: key column %d out of range", S->sn.keys[k].col_index);
@@ -94,9 +95,6 @@ static VecBatch *sort_next_body(VecNode *self) {
         cols[c].valid = dm;
         cols[c].voff = 0;
     }
-    for (int b = 0; b < nb; b++) vg_dbatch_release(&bs[b]);
-    free(bs);
-
     /* the order, then every column gathered in it */
     VecBatch *out = vg_batch_alloc(nc, total);
     for (int c = 0; c < nc; c++) out->col_names[c] = vg_xstrdup(cs->col_names[c]);
@@ -104,22 +102,55 @@ static VecBatch *sort_next_body(VecNode *self) {
         const int nk = S->sn.n_keys;
         int *kc = (int *)vg_xcalloc((size_t)(nk ? nk : 1), sizeof(int));
         int *kd = (int *)vg_xcalloc((size_t)(nk ? nk : 1), sizeof(int));
+        /* sort columns: the columns themselves, then one rank column per string key */
+        VgCol *sc = (VgCol *)vg_xcalloc((size_t)(nc + nk + 1), sizeof(VgCol));
+        for (int c = 0; c < nc; c++) sc[c] = cols[c];
+        int n_sc = nc;
+        char *ranks = NULL;
         for (int k = 0; k < nk; k++) {
             kc[k] = S->sn.keys[k].col_index;
             kd[k] = S->sn.keys[k].descending != 0;
+            if (cols[kc[k]].type != VEC_STRING) continue;
+            if (!ranks) ranks = (char *)vg_dmalloc(a256((size_t)total * 8) * (size_t)(nk + 1) + 256);
+            int64_t *codes = (int64_t *)(ranks + a256((size_t)total * 8) * (size_t)nk);
+            int64_t *rk = (int64_t *)(ranks + a256((size_t)total * 8) * (size_t)k);
+            VgDict *D = vg_dict_new();
+            vg_dict_encode(D, &cols[kc[k]], NULL, total, 1, codes);
+            int32_t *dperm = NULL;
+            int64_t *drank = NULL;
+            vg_dict_order(D, &dperm, &drank);
+            vg_check_rc(vgk_map_codes(drank, codes, cols[kc[k]].valid, 0, total, rk, vg_stream()), "sort");
+            vg_dfree(dperm);
+            vg_dfree(drank);
+            vg_dict_free(D);
+            sc[n_sc].type = VEC_INT64;
+            sc[n_sc].data = rk;
+            sc[n_sc].valid = cols[kc[k]].valid;
+            kc[k] = n_sc++;
         }
         const size_t sb = vgk_sort_rows_scratch(total);
         char *work = (char *)vg_dmalloc(sb + (size_t)total * 4 + 256);
         int32_t *perm = (int32_t *)(work + sb);
-        vg_check_rc(vgk_sort_rows(cols, kc, kd, nk, perm, total, work, sb, vg_stream()), "sort");
+        vg_check_rc(vgk_sort_rows(sc, kc, kd, nk, perm, total, work, sb, vg_stream()), "sort");
+        vg_dfree(ranks);
+        free(sc);
         free(kc);
         free(kd);
-        const size_t ob = a256((size_t)total * 8 + 8) + a256(wbytes);
+        const size_t ob = a256((size_t)total * 16 + 8) + a256(wbytes);
         char *ob_blk = (char *)vg_dmalloc(ob);
         for (int c = 0; c < nc; c++) {
-            uint32_t *om = (uint32_t *)(ob_blk + a256((size_t)total * 8 + 8));
+            uint32_t *om = (uint32_t *)(ob_blk + a256((size_t)total * 16 + 8));
             vg_check_rc(vgk_gather(&cols[c], perm, total, 0, ob_blk, om, vg_stream()), "sort gather");
-            out->columns[c] = vg_download_column(cs->col_types[c], ob_blk, om, total);
+            if (cs->col_types[c] == VEC_STRING) {
+                VgCol v;
+                memset(&v, 0, sizeof(v));
+                v.type = VEC_STRING;
+                v.data = ob_blk;
+                v.valid = om;
+                out->columns[c] = vg_download_strings(&v, NULL, total);
+            } else {
+                out->columns[c] = vg_download_column(cs->col_types[c], ob_blk, om, total);
+            }
         }
         vg_sync();
         vg_dfree(ob_blk);
@@ -131,10 +162,17 @@ static VecBatch *sort_next_body(VecNode *self) {
             a.type = (VecType)cs->col_types[c];
             a.owns_data = 1;
             a.validity = (uint8_t *)vg_xcalloc(1, 1);
-            a.buf.i64 = (int64_t *)vg_xcalloc(1, 8);
+            if (a.type == VEC_STRING) {
+                a.buf.str.offsets = (int64_t *)vg_xcalloc(1, 8);
+                a.buf.str.data = (char *)vg_xcalloc(1, 1);
+            } else {
+                a.buf.i64 = (int64_t *)vg_xcalloc(1, 8);
+            }
             out->columns[c] = a;
         }
     }
+    for (int b = 0; b < nb; b++) vg_dbatch_release(&bs[b]);   /* string views point into them */
+    free(bs);
     vg_dfree(blk);
     free(cols);
     return out;

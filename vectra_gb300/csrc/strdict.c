@@ -25,17 +25,26 @@ struct VgDict {
     VgStrDict d;
     unsigned long long *d_ctr;       /* VG_DICT_CTRS counters, then the error word */
     unsigned long long h_ctr[VG_DICT_CTRS + 1];
+    int kept;                        /* outlives the node call that made it */
 };
 
 static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-VgDict *vg_dict_new(void) {
+static void *dalloc(VgDict *D, size_t bytes) { return D->kept ? vg_dmalloc_kept(bytes) : vg_dmalloc(bytes); }
+
+static VgDict *dict_new(int kept) {
     VgDict *D = (VgDict *)vg_xcalloc(1, sizeof(VgDict));
-    D->d_ctr = (unsigned long long *)vg_dmalloc((VG_DICT_CTRS + 1) * 8);
+    D->kept = kept;
+    D->d_ctr = (unsigned long long *)dalloc(D, (VG_DICT_CTRS + 1) * 8);
     vg_dmemset(D->d_ctr, 0, (VG_DICT_CTRS + 1) * 8);
     D->d.ctr = D->d_ctr;
     return D;
 }
+
+VgDict *vg_dict_new(void) { return dict_new(0); }
+
+/* for a node that keeps the dictionary across its calls (a join's keys) */
+VgDict *vg_dict_new_kept(void) { return dict_new(1); }
 
 void vg_dict_free(VgDict *D) {
     if (!D) return;
@@ -59,8 +68,8 @@ static void dict_read(VgDict *D) {
     if (err) vg_fail("string dictionary: table full (error %u)", err);
 }
 
-static void *grow(void *old, size_t used, size_t bytes) {
-    void *p = vg_dmalloc(bytes);
+static void *grow(VgDict *D, void *old, size_t used, size_t bytes) {
+    void *p = dalloc(D, bytes);
     if (old && used) {
         cudaMemcpyAsync(p, old, used, cudaMemcpyDeviceToDevice, (cudaStream_t)vg_stream());
     }
@@ -76,22 +85,22 @@ static void dict_reserve(VgDict *D, int64_t rows, int64_t bytes) {
     if (need > D->d.codes_cap) {
         int64_t cap = D->d.codes_cap ? 2 * D->d.codes_cap : 1024;
         while (cap < need) cap *= 2;
-        D->d.c_hash = (uint64_t *)grow(D->d.c_hash, (size_t)n * 8, a256((size_t)cap * 8));
-        D->d.c_off = (int64_t *)grow(D->d.c_off, (size_t)n * 8, a256((size_t)cap * 8));
-        D->d.c_len = (uint32_t *)grow(D->d.c_len, (size_t)n * 4, a256((size_t)cap * 4));
+        D->d.c_hash = (uint64_t *)grow(D, D->d.c_hash, (size_t)n * 8, a256((size_t)cap * 8));
+        D->d.c_off = (int64_t *)grow(D, D->d.c_off, (size_t)n * 8, a256((size_t)cap * 8));
+        D->d.c_len = (uint32_t *)grow(D, D->d.c_len, (size_t)n * 4, a256((size_t)cap * 4));
         D->d.codes_cap = cap;
     }
     if (used + bytes > D->d.arena_cap) {
         int64_t cap = D->d.arena_cap ? 2 * D->d.arena_cap : (int64_t)1 << 16;
         while (cap < used + bytes) cap *= 2;
-        D->d.arena = (char *)grow(D->d.arena, (size_t)used, a256((size_t)cap));
+        D->d.arena = (char *)grow(D, D->d.arena, (size_t)used, a256((size_t)cap));
         D->d.arena_cap = cap;
     }
     if (D->d.cap == 0 || 2 * need > D->d.cap) {
         int64_t cap = D->d.cap ? 2 * D->d.cap : 2048;
         while (cap < 2 * need) cap *= 2;
         vg_dfree(D->d.slot);
-        D->d.slot = (uint32_t *)vg_dmalloc(a256((size_t)cap * 4));
+        D->d.slot = (uint32_t *)dalloc(D, a256((size_t)cap * 4));
         D->d.cap = cap;
         vg_check_rc(vgk_dict_rehash(&D->d, n, err_word(D), vg_stream()), "string dictionary");
     }

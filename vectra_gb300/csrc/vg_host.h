@@ -103,6 +103,7 @@ void vg_host_bufs_free(VgHostBufs *h);
 /* ---- string dictionaries (strdict.c) ---- */
 typedef struct VgDict VgDict;
 VgDict *vg_dict_new(void);
+VgDict *vg_dict_new_kept(void);
 void vg_dict_free(VgDict *D);
 /* d_codes[p] for the logical rows p of string column c (insert: new
  * strings get the next codes; otherwise absent strings get -1) */
@@ -195,6 +196,7 @@ int vg_join_right_type(VecNode *n, int col);
 void vg_join_ensure_slots(VecNode *n);
 VecNode *vg_join_left(VecNode *n);
 int vg_join_kind(VecNode *n);
+int vg_join_has_string_keys(VecNode *n);
 /* resolves an output column name of the join: side 0 = left column index,
  * side 1 = right column index; returns 0 if not found */
 int vg_join_resolve(VecNode *n, const char *name, int *side, int *col);

@@ -561,6 +561,9 @@ int vgk_dict_views(const VgStrDict *d, const int64_t *d_codes, const uint32_t *d
  * is the strings' order */
 int vgk_dict_chunks(const VgStrDict *d, int64_t n_codes, int n_chunks, int64_t *d_out, vg_stream_t s);
 int vgk_rank_of(const int32_t *d_perm, int64_t n, int64_t *d_rank, vg_stream_t s);
+/* d_out[i] = d_table[d_codes[i]] where row i is valid (else 0) */
+int vgk_map_codes(const int64_t *d_table, const int64_t *d_codes, const uint32_t *d_valid, int voff, int64_t n,
+                  int64_t *d_out, vg_stream_t s);
 /* key word k of the listed group-table slots replaced by d_rank[word] */
 int vgk_group_keys_remap(const VgGroupTable *gt, int k, const int32_t *d_slots, int64_t n, const int64_t *d_rank,
                          vg_stream_t s);
