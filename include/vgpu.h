@@ -147,6 +147,12 @@ unsigned long long vgpu_pagg_runs(void);
  * yet), shape class, reducer CTAs per SM and measured milliseconds. */
 void        vgpu_pagg_tune(int on);
 int         vgpu_pagg_tuned(char *shape, int shape_bytes, int *ctas, double *ms);
+
+/* arrange() beyond device memory: sorted runs kept in host memory since
+ * load (returned) and key ranges merged back on the device (*ranges).  A
+ * sort spills when its input passes a share of the free device memory, or
+ * VGPU_SORT_RUN_ROWS rows when that is set. */
+long        vgpu_sort_spill_stats(long *ranges);
 /* Host wall time (ms, summed since load) of the partitioned path's phases:
  * 0 sketch, 1 partition pass, 2 bucket reducer, 3 compaction into the
  * output columns, 4 waiting for the host result buffers, 5 copy to host,

@@ -56,3 +56,59 @@ def test_string_columns_are_carried():
     t = cases.T(x=[2.0, 1.0, NA_F, 0.5])
     t["s"] = (["b", "a", "c", "d"], np.array([True, True, False, True]))
     cases.same_batches(Tbl(G, O.make_source(t)).arrange("x").batches(), Tbl(O, O.make_source(t)).arrange("x").batches())
+
+
+def _spill(budget, fn):
+    """fn() with the sort's run budget forced to `budget` rows; returns its
+    result and the runs / key ranges the spilled sorts took."""
+    import ctypes as C
+    import os
+    import vectra_gb300
+    lib = vectra_gb300.load()
+    lib.vgpu_sort_spill_stats.restype = C.c_long
+    lib.vgpu_sort_spill_stats.argtypes = [C.POINTER(C.c_long)]
+    r0 = C.c_long(0)
+    runs0 = lib.vgpu_sort_spill_stats(C.byref(r0))
+    os.environ["VGPU_SORT_RUN_ROWS"] = str(budget)
+    try:
+        out = fn()
+    finally:
+        del os.environ["VGPU_SORT_RUN_ROWS"]
+    r1 = C.c_long(0)
+    runs1 = lib.vgpu_sort_spill_stats(C.byref(r1))
+    return out, runs1 - runs0, r1.value - r0.value
+
+
+@pytest.mark.parametrize("n,batch,budget", [(200_000, 9_000, 20_000), (50_001, 1_000, 4_096), (7_000, 64, 1_000)])
+def test_sort_beyond_the_device_budget(n, batch, budget):
+    """Runs sorted into host memory and merged back by key range give the
+    in-memory order exactly (multi-key, NA, descending, ties in input
+    order)."""
+    got, runs, ranges = _spill(budget, lambda: cases.r_sort(_gpu(), n + 2, n, batch))
+    assert runs >= n // budget and ranges > 1
+    cases.same_batches(got, cases.r_sort(OracleEngine(), n + 2, n, batch))
+
+
+def test_sort_beyond_the_budget_skewed_keys():
+    """One key repeated on most rows (a key range larger than the budget is
+    copied in run order), plus strings and a selection vector below."""
+    from vectra_gb300.plan import col, tbl
+    rng = np.random.default_rng(21)
+    n = 60_000
+    k = np.where(rng.random(n) < 0.8, 7, rng.integers(0, 50, n))
+    t = {"k": (k, rng.random(n) > 0.01), "s": (cases.random_strings(rng, n, 400, maxlen=10), rng.random(n) > 0.05),
+         "i": np.arange(n), "x": rng.normal(0, 1, n)}
+
+    from engines import gpu_engine
+    G = gpu_engine()                 # strings come from a foreign source node
+
+    def q(E):
+        return tbl(E, t, batch_rows=2_500).filter(col("x") > -1.0).arrange("k", ("s", True)).batches()
+    got, runs, ranges = _spill(3_000, lambda: q(G))
+    assert runs > 5
+    cases.same_batches(got, q(OracleEngine()))
+
+    def q2(E):
+        return tbl(E, t, batch_rows=2_500).arrange(("k", True)).batches()
+    got2, _, _ = _spill(3_000, lambda: q2(G))
+    cases.same_batches(got2, q2(OracleEngine()))

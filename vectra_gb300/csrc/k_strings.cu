@@ -82,12 +82,13 @@ VG_DEV uint64_t str_hash(const char *p, uint32_t len) {
     return h;
 }
 
-// views over the reference's layout: row i is bytes [offs[i], offs[i+1])
-__global__ void views_kernel(const int64_t *offs, const char *bytes, int64_t n, VgStrView *out) {
+// views over the reference's layout: row i is bytes [offs[i], offs[i+1]),
+// bytes[0] being the byte at offset `base`
+__global__ void views_kernel(const int64_t *offs, int64_t base, const char *bytes, int64_t n, VgStrView *out) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const int64_t a = offs[i], b = offs[i + 1];
-        out[i] = vg_str_view(bytes + a, (uint32_t)(b - a));
+        out[i] = vg_str_view(bytes + (a - base), (uint32_t)(b - a));
     }
 }
 
@@ -330,9 +331,10 @@ extern "C" {
 
 const char *vgk_str_last_error(void) { return g_err; }
 
-int vgk_str_views(const int64_t *d_offs, const char *d_bytes, int64_t n, VgStrView *d_out, vg_stream_t s) {
+int vgk_str_views(const int64_t *d_offs, int64_t base, const char *d_bytes, int64_t n, VgStrView *d_out,
+                  vg_stream_t s) {
     if (n <= 0) return 0;
-    views_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)s>>>(d_offs, d_bytes, n, d_out);
+    views_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)s>>>(d_offs, base, d_bytes, n, d_out);
     vg_launch_counter++;
     return check(cudaGetLastError(), "string views");
 }

@@ -678,7 +678,7 @@ int vg_pull(VecNode *child, const uint8_t *need, int keep_host, VgDBatch *out) {
         const size_t ov = str_at[c] + a256((size_t)n * 16);
         const size_t oo = ov + a256(valid_bytes_dev(n));
         const size_t oc = oo + a256((size_t)(n + 1) * 8);
-        vg_check_rc(vgk_str_views((const int64_t *)(blk + oo), blk + oc, n, (VgStrView *)(blk + str_at[c]),
+        vg_check_rc(vgk_str_views((const int64_t *)(blk + oo), 0, blk + oc, n, (VgStrView *)(blk + str_at[c]),
                                   vg_stream()), "string column upload");
     }
     free(str_at);
@@ -689,6 +689,53 @@ int vg_pull(VecNode *child, const uint8_t *need, int keep_host, VgDBatch *out) {
         vg_batch_free(b);
     }
     return 1;
+}
+
+/* Rows [lo, lo + n) of a host column to the device, in one new block
+ * (*blk, freed by the caller): values, validity (the bytes holding those
+ * rows, so voff = lo % 8), and for strings offsets, characters and views. */
+VgCol vg_upload_slice(const VecArray *a, int64_t lo, int64_t n, void **blk) {
+    VgCol c;
+    memset(&c, 0, sizeof(c));
+    c.type = a->type;
+    const int64_t b0 = lo / 8, nvb = (lo % 8 + n + 7) / 8;
+    const size_t vb = a256((size_t)nvb + 8);
+    size_t bytes = vb;
+    int64_t s0 = 0, s1 = 0;
+    if (a->type == VEC_STRING) {
+        s0 = n > 0 ? a->buf.str.offsets[lo] : 0;
+        s1 = n > 0 ? a->buf.str.offsets[lo + n] : 0;
+        bytes += a256((size_t)n * 16) + a256((size_t)(n + 1) * 8) + a256((size_t)(s1 - s0) + 1);
+    } else {
+        bytes += a256(value_bytes(a->type, n) + 8);
+    }
+    char *p = (char *)vg_dmalloc(bytes);
+    *blk = p;
+    if (n <= 0) return c;
+    if (a->validity) {
+        vg_dmemset(p, 0, vb);
+        vg_h2d(p, a->validity + b0, (size_t)nvb);
+        c.valid = (const uint32_t *)p;
+        c.voff = (int32_t)(lo % 8);
+    }
+    char *q = p + vb;
+    if (a->type == VEC_STRING) {
+        VecArray sl = *a;
+        sl.buf.str.offsets = a->buf.str.offsets + lo;
+        check_offsets(&sl, n);
+        char *views = q, *offs = q + a256((size_t)n * 16), *chars = offs + a256((size_t)(n + 1) * 8);
+        vg_h2d(offs, a->buf.str.offsets + lo, (size_t)(n + 1) * 8);
+        vg_h2d(chars, a->buf.str.data + s0, (size_t)(s1 - s0));
+        vg_check_rc(vgk_str_views((const int64_t *)offs, s0, chars, n, (VgStrView *)views, vg_stream()),
+                    "string column upload");
+        c.data = views;
+    } else {
+        const size_t es = a->type == VEC_BOOL ? 1 : 8;
+        vg_h2d(q, (const char *)(a->type == VEC_BOOL ? (void *)a->buf.bln : (void *)a->buf.i64) + (size_t)lo * es,
+               (size_t)n * es);
+        c.data = q;
+    }
+    return c;
 }
 
 /* A device string column (views) -> newly malloc'd host VecArray in the

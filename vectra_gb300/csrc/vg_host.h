@@ -75,6 +75,8 @@ void vg_dbatch_release(VgDBatch *b);
 
 /* Device column -> newly malloc'd host VecArray of n values. */
 VecArray vg_download_column(int type, const void *d_data, const uint32_t *d_valid, int64_t n);
+/* Rows [lo, lo + n) of a host column on the device (one new block *blk). */
+VgCol vg_upload_slice(const VecArray *a, int64_t lo, int64_t n, void **blk);
 /* Device string column (views) -> host VecArray of rows d_idx[j] (or j). */
 VecArray vg_download_strings(const VgCol *c, const int32_t *d_idx, int64_t n);
 VecArray vg_host_column(int type, int64_t n, void *values, const uint32_t *d_valid);

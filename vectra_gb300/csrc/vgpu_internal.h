@@ -538,8 +538,10 @@ const char *vgk_join_last_error(void);
 
 /* strings (k_strings.cu) */
 const char *vgk_str_last_error(void);
-/* views of n rows in the reference's layout (offsets n + 1, bytes) */
-int vgk_str_views(const int64_t *d_offs, const char *d_bytes, int64_t n, VgStrView *d_out, vg_stream_t s);
+/* views of n rows in the reference's layout (offsets n + 1, bytes; the
+ * first byte of d_bytes is the one at offset base) */
+int vgk_str_views(const int64_t *d_offs, int64_t base, const char *d_bytes, int64_t n, VgStrView *d_out,
+                  vg_stream_t s);
 /* lengths of rows d_idx[j] (or j; NA and negative ids: 0) and, d_valid
  * given, the validity words of the packed column */
 int vgk_str_lengths(const VgCol *c, const int32_t *d_idx, int64_t n, int32_t *d_len, uint32_t *d_valid,
