@@ -640,6 +640,13 @@ def cpu_workload_sample(name, torch, scale=1):
                 tbl(E, {"key": k}).inner_join(tbl(E, {"key": bkey[boff[i]:boff[i + 1]]}), "key").batches()
         return len(pick), time.perf_counter() - t0, ("%d of the %d instances, one query after another "
                                                       "(hash-path group-by, inner join)" % (len(pick), n_inst))
+    if name == "strings":
+        from vectra_gb300.plan import tbl
+        m = 1_000_000 // scale
+        _, _, cv, temp, year, city = strings_table(m)
+        t0 = time.perf_counter()
+        strings_query(E, tbl(E, {"city": (city, cv), "temperature": temp, "year": year}, batch_rows=100_000))
+        return m, time.perf_counter() - t0, "the first %d rows of the string workload in 100k-row batches" % m
     raise ValueError("no CPU sample for workload %r" % name)
 
 
@@ -665,7 +672,7 @@ def workload_reference_arm(args):
 def reference_arm(args, rank, world):
     if rank != 0:
         return None
-    if args.workload in ("filter_group", "high_card", "query_set"):
+    if args.workload in ("filter_group", "high_card", "query_set", "strings"):
         return workload_reference_arm(args)
     # every host core runs its own copy of the sampled query (the engine is
     # single-threaded, so this is all the host threads it can use)
@@ -1044,18 +1051,22 @@ def nested_workloads(args):
     import copy
     import torch
     out = {}
-    for name in ("filter_group", "high_card", "query_set", "serve"):
+    for name in ("filter_group", "high_card", "query_set", "serve", "strings"):
         a = copy.copy(args)
         a.workload = name
         a.steps = max(3, min(args.steps, 10))
         a.warmup = 3
         t0 = time.perf_counter()
         try:
-            r = serve_arm(a) if name == "serve" else workload_arm(a)
+            r = serve_arm(a) if name == "serve" else strings_arm(a) if name == "strings" else workload_arm(a)
         except Exception as e:                       # recorded, the headline stands
             out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
             continue
         r["wall_s"] = round(time.perf_counter() - t0, 1)
+        if name == "strings":
+            out[name] = r
+            torch.cuda.empty_cache()
+            continue
         if name in ("filter_group", "high_card", "query_set"):
             rows, secs, sample = cpu_workload_sample(name, torch)
             unit = "queries/s" if name == "query_set" else "rows/s"
@@ -1080,6 +1091,99 @@ def nested_workloads(args):
         out[name] = r
         torch.cuda.empty_cache()
     return out
+
+
+def strings_table(n):
+    """The string workload's columns: city (1000 distinct names of 5-14
+    bytes, 2% NA), temperature N(20, 8), year U{2000..2025}."""
+    rng = np.random.default_rng(5)
+    syl = ["an", "ber", "cor", "dal", "el", "fi", "gor", "ha", "ist", "jo", "ka", "lu", "mo", "no", "or", "pe"]
+    names = np.array(["%s%s%s%d" % (syl[i % 16], syl[(i // 16) % 16], syl[(i // 256) % 16], i) for i in range(1000)],
+                     dtype=object)
+    idx = rng.integers(0, 1000, n)
+    cv = rng.random(n) > 0.02
+    temp = rng.normal(20.0, 8.0, n)
+    year = rng.integers(2000, 2026, n)
+    return names, idx, cv, temp, year, names[idx]
+
+
+def strings_query(E, src):
+    from vectra_gb300.plan import col, grepl
+    return (src.filter(grepl("an", col("city")) | (col("year") >= 2020)).group_by("city")
+            .summarise(temp_dir="tmp", avg=("mean", "temperature"), n=("n",)).collect())
+
+
+def strings_arm(args):
+    """String columns as R feeds them: a .vtr file (city: 1000 distinct
+    names of 5-14 bytes, 2% NA; temperature; year) in 100k-row groups read
+    by scan_node_create, then filter(grepl("an", city) | year >= 2020) |>
+    group_by(city) |> summarise(avg = mean(temperature), n = n()) in key
+    order: the string predicate runs in the filter program, the string key
+    through the device dictionary.  Wall clock per query (the file in the
+    page cache), result checked against numpy; the CPU restatement on a
+    1M-row sample beside it."""
+    import tempfile
+    import torch
+    import vectra_gb300
+    from vectra_gb300 import vtr
+    from vectra_gb300.plan import col, grepl, scan, tbl
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    eng = vectra_gb300.engine(dev.index)
+    n = 10_000_000 // args.scale
+    names, idx, cv, temp, year, city = strings_table(n)
+    d = tempfile.mkdtemp(prefix="vgpu_bench_")
+    path = os.path.join(d, "weather.vtr")
+    t0 = time.perf_counter()
+    vtr.write_vtr(path, {"city": (city, cv), "temperature": temp, "year": year}, 100_000)
+    write_s = time.perf_counter() - t0
+    file_bytes = os.path.getsize(path)
+
+    query = strings_query
+    out = query(eng, scan(eng, path))
+    # expected: Kleene OR (NA | TRUE is TRUE), groups in byte order, NA last
+    has_an = np.array(["an" in s for s in names])
+    keep = (cv & has_an[idx]) | (year >= 2020)
+    kv = keep & cv
+    cnt = np.bincount(idx[kv], minlength=1000)
+    sm = np.bincount(idx[kv], weights=temp[kv], minlength=1000)
+    order = sorted((i for i in range(1000) if cnt[i]), key=lambda i: names[i].encode())
+    na_n = int((keep & ~cv).sum())
+    g, gv = out["city"]
+    assert list(g[gv]) == [names[i] for i in order] and (not na_n or not gv[-1]), "string group keys differ"
+    assert np.array_equal(out["n"][0][:len(order)], cnt[order].astype(np.float64)), "counts differ"
+    want_avg = sm[order] / cnt[order]
+    assert np.allclose(out["avg"][0][:len(order)], want_avg, rtol=1e-12, atol=0), "means differ"
+    if na_n:
+        assert out["n"][0][-1] == na_n
+    times = []
+    for i in range(max(1, min(args.steps, 3)) + 1):
+        t0 = time.perf_counter()
+        query(eng, scan(eng, path))
+        if i:
+            times.append(time.perf_counter() - t0)
+    try:
+        os.remove(path)
+        os.rmdir(d)
+    except OSError:
+        pass
+    ms = statistics.median(times) * 1e3
+    m, cpu_s, _ = cpu_workload_sample("strings", torch, args.scale)
+    return {"metric": "rows/s (input rows per second, whole query, from the .vtr file)", "value": n / (ms * 1e-3),
+            "unit": "rows/s", "ms_per_step": ms, "steps": len(times), "higher_is_better": True,
+            "config": {"workload": "scan(weather.vtr) |> filter(grepl(\"an\", city) | year >= 2020) |> "
+                                   "group_by(city) |> summarise(avg = mean(temperature), n = n())",
+                       "rows": n, "groups": len(order) + (1 if na_n else 0), "distinct_city": 1000,
+                       "city_na": 0.02, "row_group_rows": 100_000},
+            "file_bytes": file_bytes, "file_gbs": file_bytes / (ms * 1e-3) / 1e9, "result_checked": True,
+            "data": "synthetic (seeded numpy generator, seed 5)",
+            "roofline": None,
+            "path": ".vtr file in the page cache (written once, %.1f s) through scan_node_create; the string "
+                    "column crosses the host link as offsets + bytes, so the query is bound by the scan and "
+                    "the link, not by HBM" % write_s,
+            "cpu_baseline": {"value": m / cpu_s, "unit": "rows/s", "cores": 1, "kind": "port",
+                             "sample": "the first %d rows through the CPU restatement (100k-row batches)" % m,
+                             "seconds": cpu_s}}
 
 
 def vtr_path_arm(args, eng, lib, fcols_host, dcols_host, want):
@@ -1141,7 +1245,8 @@ def main():
                     help="skip the other configurations nested under `workloads` in the headline line")
     ap.add_argument("--scale", type=int, default=1,
                     help="divide both table sizes (small cases for profiling only; not a bench line)")
-    ap.add_argument("--workload", default="join_agg", choices=["join_agg", "filter_group", "high_card", "query_set", "serve"],
+    ap.add_argument("--workload", default="join_agg",
+                    choices=["join_agg", "filter_group", "high_card", "query_set", "serve", "strings"],
                     help="join_agg: the headline line; the others measure the reference's other "
                          "configurations (checked, not the headline)")
     args = ap.parse_args()
@@ -1160,6 +1265,8 @@ def main():
         line = reference_arm(args, rank, world)
     elif args.workload == "serve":
         line = serve_arm(args) if rank == 0 else None
+    elif args.workload == "strings":
+        line = strings_arm(args) if rank == 0 else None
     elif args.workload != "join_agg":
         line = workload_arm(args) if rank == 0 else None
     else:
