@@ -147,6 +147,28 @@ def g_filter_then_group(E, temp_dir):   # test-groupby.R:133-149, test-filter.R:
             .summarise(temp_dir=temp_dir, s=("sum", "x"), n=("n",)).batches())
 
 
+def g_program_filter_then_group(E, temp_dir):   # a predicate that does not fold into ranges
+    rng = np.random.default_rng(31)
+    n = 3000
+    x = np.where(np.arange(n) // 500 == 2, -1.0, rng.normal(0, 3, n))   # rows 1000-1499: none pass
+    t = {"g": (rng.integers(0, 40, n), rng.random(n) > 0.05), "x": (x, rng.random(n) > 0.05),
+         "y": (rng.integers(-5, 5, n), rng.random(n) > 0.1)}
+    pred = ((col("x") * 2.0) > col("y")) | (is_na(col("y")) & (col("x") > 0.0))
+    return (tbl(E, t, batch_rows=500).filter(pred).group_by("g")
+            .summarise(temp_dir=temp_dir, s=("sum", "x", True), n=("n",), c=("count", "y")).batches())
+
+
+def g_program_filter_join_group(E, temp_dir):   # the same below a fused join
+    rng = np.random.default_rng(32)
+    n, d = 4000, 300
+    fact = {"k": (rng.integers(0, d + 20, n), rng.random(n) > 0.03), "v": rng.lognormal(0, 1, n),
+            "z": rng.integers(0, 10, n)}
+    dim = {"k": np.arange(d), "cat": rng.integers(0, 12, d), "w": rng.random(d)}
+    pred = (col("z") % 3).eq(0) | (col("v") > 2.5)
+    return (tbl(E, fact, batch_rows=700).filter(pred).left_join(tbl(E, dim, batch_rows=128), "k").group_by("cat")
+            .summarise(temp_dir=temp_dir, s=("sum", col("v") * col("w"), True), n=("n",)).batches())
+
+
 def g_ungrouped(E, temp_dir):       # summarise without group_by (hash path, one group)
     t = T(x=[1.0, 2.0, NA, 4.0])
     a = tbl(E, t).group_by().summarise(temp_dir=temp_dir, s=("sum", "x", True), n=("n",)).batches()
@@ -534,7 +556,8 @@ FILTER_CASES = [f_simple, f_equality, f_and_or_not, f_na_dropped, f_is_na, f_kle
                 f_empty, f_general_expr, f_int_vs_double_literal]
 GROUP_CASES = [g_basic, g_na_key, g_multi_key, g_na_semantics, g_int_sum_double, g_resize_200,
                g_filter_then_group, g_ungrouped, g_nested_expr, g_bool_and_double_keys, ja_join_agg,
-               ja_dense_keys, ja_join_agg_sparse, ja_dup_build_keys, ja_payload_edges]
+               ja_dense_keys, ja_join_agg_sparse, ja_dup_build_keys, ja_payload_edges,
+               g_program_filter_then_group, g_program_filter_join_group]
 JOIN_CASES = [j_inner_left_semi_anti, j_duplicates, j_na_keys, j_suffix, j_coerce, j_streaming,
               j_after_filter, j_full]
 

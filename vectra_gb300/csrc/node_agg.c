@@ -41,6 +41,8 @@ typedef struct {
     VecNode *src;             /* pulled batch by batch */
     VecNode *project, *join, *filter;
     const VgPred *pred;       /* over the filter child's columns (set fset) */
+    const VgProg *prog;       /* or a general program over them, run per batch */
+    int prog_col[VG_MAX_COLS];/* its columns as source columns */
     const VgColSet *fset;
     VgColSet pset;            /* kernel probe column table -> src column */
     VgColSet bset;            /* kernel build column table -> right column */
@@ -239,7 +241,9 @@ static void plan_build(VgAgg *A, Plan *P) {
         VecNode *fc;
         const VgColSet *fs;
         const VgPred *pr = vg_filter_cnf(n, &fc, &fs);
+        const VgProg *pg = pr ? NULL : vg_filter_program(n, &fc, &fs);
         if (pr) { P->filter = n; P->pred = pr; P->fset = fs; n = fc; }
+        else if (pg) { P->filter = n; P->prog = pg; P->fset = fs; n = fc; }
     }
     P->src = n;
     if (plan_resolve(A, P)) return;
@@ -519,6 +523,25 @@ static void str_dicts_begin(Plan *P) {
 static void str_dicts_free(Plan *P) {
     for (int k = 0; k < P->n_keys; k++)
         if (P->dict_owner[k]) vg_dict_free(P->dict[k]);
+}
+
+/* The filter program over the batch: its selection (composed with any
+ * the batch had) replaces the batch's, on the device.  Returns the device
+ * block holding it, freed by the caller after the batch's launches. */
+static void *filter_batch(Plan *P, VgDBatch *db) {
+    VgCol cols[VG_MAX_COLS];
+    const int nc = P->fset->n;
+    for (int j = 0; j < nc; j++) cols[j] = db->cols[P->prog_col[j]];
+    const int64_t n_in = db->d_sel ? db->sel_n : db->n_rows;
+    const size_t sb = vgk_filter_scratch_bytes(n_in);
+    char *blk = (char *)vg_dmalloc(sb + (size_t)(n_in > 0 ? n_in : 1) * 4 + 256);
+    int32_t *out = (int32_t *)(blk + sb);
+    int64_t cnt = 0;
+    vg_check_rc(vgk_filter_prog(cols, nc, P->prog, db->n_rows, db->d_sel, db->sel_n, out, &cnt, blk, sb, vg_stream()),
+                "filter");
+    db->d_sel = out;
+    db->sel_n = cnt;
+    return blk;
 }
 
 /* Each string key column of the batch replaced by the int64 codes of its
@@ -1511,6 +1534,13 @@ static VecBatch *agg_next_body(VecNode *self) {
         L->n_bcols = P.bset.n;
         for (int j = 0; j < P.bset.n; j++) L->bcols[j] = B->bcols[P.bset.idx[j]];
     }
+    /* a general filter program: its columns come with every batch, and its
+     * selection is made on the device before the batch's launches */
+    if (P.prog)
+        for (int j = 0; j < P.fset->n; j++) {
+            P.prog_col[j] = P.fset->idx[j];
+            need[P.fset->idx[j]] = 1;
+        }
     for (int j = 0; j < P.pset.n; j++) need[P.pset.idx[j]] = 1;
     L->n_pcols = P.pset.n;
     L->n_keys = P.n_keys;
@@ -1577,6 +1607,12 @@ static VecBatch *agg_next_body(VecNode *self) {
     g_agg_ms[0] += t_loop - t_start;
     if (P.n_str) str_dicts_begin(&P);
     while (vg_pull(P.src, need, 0, &db)) {
+        void *fsel = P.prog ? filter_batch(&P, &db) : NULL;
+        if (P.prog && db.sel_n == 0) {                /* no row passes: as if the batch were dropped */
+            vg_dfree(fsel);
+            vg_dbatch_release(&db);
+            continue;
+        }
         int64_t n_logical = db.d_sel ? db.sel_n : db.n_rows;
         void *codes = P.n_str ? str_encode_batch(&P, &db) : NULL;
         if (batch_idx == 0 && !P.n_str) {
@@ -1588,6 +1624,7 @@ static VecBatch *agg_next_body(VecNode *self) {
             const double t0 = now_ms();
             pagg_batch(pg, &P, L, &db, stream_pos, batch_idx);
             g_pagg_ms[1] += now_ms() - t0;
+            vg_dfree(fsel);
             vg_dbatch_release(&db);
             stream_pos += n_logical;
             batch_idx++;
@@ -1616,6 +1653,7 @@ static VecBatch *agg_next_body(VecNode *self) {
             settled = !run_batch(&P, &T, L, &S, n);
         }
         vg_dfree(codes);
+        vg_dfree(fsel);
         vg_dbatch_release(&db);
         stream_pos += n_logical;
         batch_idx++;

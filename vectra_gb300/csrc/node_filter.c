@@ -9,7 +9,9 @@
  *
  * A group-agg node directly above this node does not call next_batch: it
  * reads the compiled predicate (vg_filter_cnf) and evaluates it inside its
- * own kernel, so the selection vector never exists.
+ * own kernel, so the selection vector never exists; or, for a general
+ * program (vg_filter_program), runs this node's filter kernels on the
+ * batch it already holds on the device and keeps the selection there.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -65,6 +67,17 @@ static void compile_filter(VgFilter *f) {
         return;
     }
     f->compiled = 2;
+}
+
+/* The general program this filter compiled to (its columns index the
+ * child columns listed in *set), or NULL if it is a conjunction or does not
+ * compile. */
+const VgProg *vg_filter_program(VecNode *n, VecNode **child_out, const VgColSet **set) {
+    VgFilter *f = (VgFilter *)n;
+    compile_filter(f);
+    *child_out = f->fn.child;
+    *set = &f->set;
+    return f->compiled == 2 ? &f->prog : NULL;
 }
 
 /* The conjunction this filter compiled to (term columns index the child

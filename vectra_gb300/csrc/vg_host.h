@@ -162,6 +162,7 @@ int vg_is_join(const VecNode *n);
 
 /* filter internals used by fusion */
 const VgPred *vg_filter_cnf(VecNode *n, VecNode **child_out, const VgColSet **set);
+const VgProg *vg_filter_program(VecNode *n, VecNode **child_out, const VgColSet **set);
 /* project internals: the expression producing column `name`, or NULL if it
  * is a pass-through (then *pass_name is the child column name) */
 int vg_project_lookup(VecNode *n, const char *name, const VecExpr **expr, const char **pass_name);
