@@ -203,6 +203,7 @@ VG_DEV int64_t dict_code(const VgStrDict &d, const VgStrView &v, bool insert, ui
                     return 0;
                 }
                 for (uint32_t k = 0; k < v.len; k++) d.arena[off + k] = v.ptr[k];
+                atomicMax(d.ctr + VG_DICT_MAXLEN, (unsigned long long)v.len);
                 d.c_hash[code] = h;
                 d.c_off[code] = (int64_t)off;
                 d.c_len[code] = v.len;

@@ -556,7 +556,8 @@ static void *str_encode_batch(Plan *P, VgDBatch *db) {
         VgCol *c = &db->cols[P->str_col[k]];
         if (c->type != VEC_STRING) vg_fail("group_by: key column %d is not a string column", P->str_col[k]);
         int64_t *codes = (int64_t *)(blk + per * (size_t)k);
-        vg_dict_encode(P->dict[k], c, db->d_sel, n_logical, 1, codes);
+        vg_dict_encode(P->dict[k], c, db->d_sel, n_logical, 1, codes,
+                       db->str_chars ? db->str_chars[P->str_col[k]] : -1);
         c->type = VEC_INT64;
         c->data = codes;
     }
@@ -620,6 +621,7 @@ static VecBatch *emit_result(VgAgg *A, Plan *P, Table *T, const uint32_t *deferr
     }
     for (int k = 0; k < ga->n_keys; k++) {
         if (P->str_key[k]) {
+            if (!str_ranked) (void)vg_dict_size(P->dict[k]);    /* its error word, read back once */
             res->columns[k] = vg_dict_strings(P->dict[k], (const int64_t *)kout[k], kval[k],
                                               str_ranked ? sperm[k] : NULL, ng);
             res->col_names[k] = vg_xstrdup(ga->key_names[k]);

@@ -208,7 +208,7 @@ static void join_build(VgJoin *j) {
             if (!j->str_key[k]) continue;
             const VgCol *sc = &j->B.bcols[j->jn.keys[k].right_col];
             int64_t *codes = (int64_t *)((char *)j->codes_block + per * (size_t)k);
-            vg_dict_encode(j->dict, sc, NULL, total, 1, codes);
+            vg_dict_encode(j->dict, sc, NULL, total, 1, codes, -1);
             j->bkey_codes[k] = *sc;
             j->bkey_codes[k].type = VEC_INT64;
             j->bkey_codes[k].data = codes;
@@ -358,7 +358,7 @@ static VecBatch *probe_one(VgJoin *j) {
             for (int k = 0; k < nk; k++) {
                 if (!j->str_key[k]) continue;
                 int64_t *codes = (int64_t *)(pcodes + per * (size_t)k);
-                vg_dict_encode(j->dict, &pk[k], db.d_sel, n, 0, codes);
+                vg_dict_encode(j->dict, &pk[k], db.d_sel, n, 0, codes, -1);
                 pk[k].type = VEC_INT64;
                 pk[k].data = codes;
             }

@@ -109,7 +109,7 @@ static int32_t *order_rows(VgSort *S, const VgCol *cols, int nc, int64_t n, char
         int64_t *codes = (int64_t *)(ranks + a256((size_t)n * 8) * (size_t)nk);
         int64_t *rk = (int64_t *)(ranks + a256((size_t)n * 8) * (size_t)k);
         VgDict *D = vg_dict_new();
-        vg_dict_encode(D, &cols[kc[k]], NULL, n, 1, codes);
+        vg_dict_encode(D, &cols[kc[k]], NULL, n, 1, codes, -1);
         int32_t *dperm = NULL;
         int64_t *drank = NULL;
         vg_dict_order(D, &dperm, &drank);

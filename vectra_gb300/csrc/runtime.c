@@ -589,17 +589,10 @@ static size_t col_dev_bytes(const VecArray *a, int64_t n) {
     return a256(value_bytes(a->type, n)) + a256(valid_bytes_dev(n));
 }
 
-static int needs_string(const VecNode *child, const uint8_t *need) {
-    const VecSchema *s = &child->output_schema;
-    for (int c = 0; c < s->n_cols; c++)
-        if ((!need || need[c]) && s->col_types[c] == VEC_STRING) return 1;
-    return 0;
-}
-
 int vg_pull(VecNode *child, const uint8_t *need, int keep_host, VgDBatch *out) {
     memset(out, 0, sizeof(*out));
     if (vg_is_table_source(child) && !keep_host) return vg_source_pull(child, need, out);
-    if (vg_is_vtr_scan(child) && !keep_host && !needs_string(child, need)) return vg_scan_pull(child, need, out);
+    if (vg_is_vtr_scan(child) && !keep_host) return vg_scan_pull(child, need, out);
     VecBatch *b = child->next_batch(child);
     if (!b) return 0;
     int64_t n = b->n_rows;
@@ -644,6 +637,8 @@ int vg_pull(VecNode *child, const uint8_t *need, int keep_host, VgDBatch *out) {
                 }
             }
             str_at[c] = o;
+            if (!out->str_chars) out->str_chars = (int64_t *)vg_xcalloc((size_t)b->n_cols, sizeof(int64_t));
+            out->str_chars[c] = (int64_t)nb;
             o = ov;
         } else {
             const size_t vb = value_bytes(a->type, n);
@@ -779,6 +774,7 @@ void vg_dbatch_release(VgDBatch *b) {
     if (b->block) vg_dfree(b->block);
     if (b->host) vg_batch_free(b->host);
     free(b->cols);
+    free(b->str_chars);
     memset(b, 0, sizeof(*b));
 }
 

@@ -362,18 +362,27 @@ static int pread_quiet(int fd, void *dst, size_t n, int64_t off) {
     return 0;
 }
 
-/* bytes of row group g's staging / device block for the needed columns:
- * per column its data, then its validity words, each 256-byte aligned */
+/* A column's part of row group g's staging / device block: its values
+ * (for strings one 16-byte view per row, made on the device), its
+ * validity words, and for strings the file's offsets and characters. */
+static size_t col_bytes(const VgVtrFile *v, int64_t g, int c, int64_t n) {
+    const size_t vwords = (size_t)((n + 31) / 32) * 4;
+    const int t = v->f.header.schema.col_types[c];
+    if (t != VEC_STRING) return a256((size_t)data_bytes(t, n)) + a256(vwords);
+    const int64_t dl = v->str_len[(size_t)g * v->n_cols + c];
+    return a256((size_t)n * 16) + a256(vwords) + a256(8 * ((size_t)n + 1)) + a256((size_t)dl + 1);
+}
+
+/* bytes of row group g's staging / device block for the needed columns,
+ * each part 256-byte aligned */
 static size_t group_bytes(const VgScan *s, int64_t g, const uint8_t *need) {
     const VgVtrFile *v = (const VgVtrFile *)s->sn.file;
     const int64_t n = v->f.rowgroups[g].n_rows;
-    const size_t vwords = (size_t)((n + 31) / 32) * 4;
     size_t total = 0;
     int o = 0;
     for (int c = 0; c < v->n_cols; c++) {
         if (!s->sn.col_mask[c]) continue;
-        const int t = v->f.header.schema.col_types[c];
-        if (need[o]) total += a256((size_t)data_bytes(t, n)) + a256(vwords);
+        if (need[o]) total += col_bytes(v, g, c, n);
         o++;
     }
     return total;
@@ -390,7 +399,18 @@ static int read_group(const VgScan *s, int64_t g, const uint8_t *need, char *h) 
     for (int c = 0; c < v->n_cols; c++) {
         if (!s->sn.col_mask[c]) continue;
         const int t = v->f.header.schema.col_types[c];
-        if (need[o]) {
+        if (need[o] && t == VEC_STRING) {
+            /* views (made on the device), validity, offsets, characters */
+            const int64_t fo = v->valid_off[(size_t)g * v->n_cols + c];
+            const int64_t dl = v->str_len[(size_t)g * v->n_cols + c];
+            const size_t ov = off + a256((size_t)n * 16), oo = ov + a256(vwords), oc = oo + a256(8 * ((size_t)n + 1));
+            if (vg_vbytes(n) & 3) memset(h + ov + ((size_t)vg_vbytes(n) & ~(size_t)3), 0, 4);
+            int e = pread_quiet(v->fd, h + ov, (size_t)vg_vbytes(n), fo);
+            if (!e) e = pread_quiet(v->fd, h + oo, 8 * ((size_t)n + 1), fo + vg_vbytes(n));
+            if (!e) e = pread_quiet(v->fd, h + oc, (size_t)dl, fo + vg_vbytes(n) + 8 * (n + 1) + 8);
+            if (e) return e;
+            off += col_bytes(v, g, c, n);
+        } else if (need[o]) {
             const int64_t fo = v->valid_off[(size_t)g * v->n_cols + c];
             const size_t db = (size_t)data_bytes(t, n);
             int e = pread_quiet(v->fd, h + off, db, fo + vg_vbytes(n));
@@ -540,16 +560,12 @@ int vg_scan_pull(VecNode *node, const uint8_t *need, VgDBatch *out) {
     memset(out, 0, sizeof(*out));
     int n_sel = 0;
     for (int c = 0; c < v->n_cols; c++) n_sel += s->sn.col_mask[c] != 0;
-    /* the columns this consumer needs (strings cannot go to the device) */
+    /* the columns this consumer needs */
     uint8_t *nd = (uint8_t *)vg_xcalloc((size_t)(n_sel ? n_sel : 1), 1);
     int o = 0;
     for (int c = 0; c < v->n_cols; c++) {
         if (!s->sn.col_mask[c]) continue;
         nd[o] = (uint8_t)(!need || need[o]);
-        if (nd[o] && v->f.header.schema.col_types[c] == VEC_STRING) {
-            free(nd);
-            vg_fail("string column '%s' is not supported by the GPU path", v->f.header.schema.col_names[c]);
-        }
         o++;
     }
     if (!s->pf_on) {
@@ -614,11 +630,28 @@ int vg_scan_pull(VecNode *node, const uint8_t *need, VgDBatch *out) {
         if (!s->sn.col_mask[c]) continue;
         const int t = v->f.header.schema.col_types[c];
         if (s->pf_need[o]) {
+            const size_t cb = col_bytes(v, g, c, n);
             out->cols[o].data = d + off;
-            off += a256((size_t)data_bytes(t, n));
+            off += t == VEC_STRING ? a256((size_t)n * 16) : a256((size_t)data_bytes(t, n));
             out->cols[o].valid = (const uint32_t *)(d + off);
             out->cols[o].voff = 0;
-            off += a256(vwords);
+            if (t == VEC_STRING) {
+                if (!out->str_chars) out->str_chars = (int64_t *)vg_xcalloc((size_t)(n_sel ? n_sel : 1), sizeof(int64_t));
+                out->str_chars[o] = v->str_len[(size_t)g * v->n_cols + c];
+                /* the file's offsets drive the device's reads: they must
+                 * start at 0 or above, never decrease, stay within the
+                 * characters and give values below 2 GiB */
+                const int64_t *fo = (const int64_t *)(p->h + off + a256(vwords));
+                const int64_t dl = v->str_len[(size_t)g * v->n_cols + c];
+                int bad = n > 0 && (fo[0] < 0 || fo[n] > dl);
+                for (int64_t i = 0; i < n && !bad; i++)
+                    bad = fo[i + 1] < fo[i] || fo[i + 1] - fo[i] > (int64_t)0x7FFFFFFF;
+                if (bad) {
+                    vg_dbatch_release(out);
+                    vg_fail("scan: malformed string offsets in column '%s'", v->f.header.schema.col_names[c]);
+                }
+            }
+            off = (size_t)((char *)out->cols[o].data - d) + cb;
         }
         o++;
     }
@@ -634,6 +667,19 @@ int vg_scan_pull(VecNode *node, const uint8_t *need, VgDBatch *out) {
         vg_fail("scan: copy of a row group to the device failed: %s", cudaGetErrorString(e));
     }
     p->copy_pending = 1;
+    /* string columns: views over the copied offsets and characters */
+    o = 0;
+    for (int c = 0; c < v->n_cols; c++) {
+        if (!s->sn.col_mask[c]) continue;
+        if (s->pf_need[o] && v->f.header.schema.col_types[c] == VEC_STRING && n > 0) {
+            const char *views = (const char *)out->cols[o].data;
+            const char *offs = views + a256((size_t)n * 16) + a256(vwords);
+            const char *chars = offs + a256(8 * ((size_t)n + 1));
+            vg_check_rc(vgk_str_views((const int64_t *)offs, 0, chars, n, (VgStrView *)views, vg_stream()),
+                        "string column upload");
+        }
+        o++;
+    }
     fill_ahead(s);                   /* keep the readers busy while this group is used */
     return 1;
 }

@@ -26,6 +26,10 @@ struct VgDict {
     unsigned long long *d_ctr;       /* VG_DICT_CTRS counters, then the error word */
     unsigned long long h_ctr[VG_DICT_CTRS + 1];
     int kept;                        /* outlives the node call that made it */
+    /* upper bounds of the device's code and arena counters since they were
+     * last read: launches whose rows fit under the capacity by these need
+     * no read-back first */
+    int64_t ub_codes, ub_used;
 };
 
 static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -107,13 +111,29 @@ static void dict_reserve(VgDict *D, int64_t rows, int64_t bytes) {
 }
 
 void vg_dict_encode(VgDict *D, const VgCol *c, const int32_t *d_sel, int64_t n_logical, int insert,
-                    int64_t *d_codes) {
+                    int64_t *d_codes, int64_t chars_ub) {
     if (n_logical <= 0) return;
-    if (insert) {
+    if (insert && chars_ub >= 0) {
+        /* every row may be new: room for all of them by the bounds, read
+         * the counters back only when the bounds pass the capacity (then
+         * with room for several more batches like this one) */
+        if (D->d.cap == 0 || D->ub_codes + n_logical > D->d.codes_cap || 2 * (D->ub_codes + n_logical) > D->d.cap ||
+            D->ub_used + chars_ub > D->d.arena_cap) {
+            const int64_t f = n_logical <= ((int64_t)1 << 20) ? 8 : 2;
+            dict_read(D);
+            dict_reserve(D, f * n_logical, f * chars_ub);
+            D->ub_codes = (int64_t)D->h_ctr[VG_DICT_CODES];
+            D->ub_used = (int64_t)D->h_ctr[VG_DICT_USED];
+        }
+        D->ub_codes += n_logical;
+        D->ub_used += chars_ub;
+    } else if (insert) {
         vg_dmemset(D->d_ctr + VG_DICT_ROWS, 0, 16);
         vg_check_rc(vgk_dict_prepass(c, d_sel, n_logical, D->d_ctr, vg_stream()), "string dictionary");
         dict_read(D);
         dict_reserve(D, (int64_t)D->h_ctr[VG_DICT_ROWS], (int64_t)D->h_ctr[VG_DICT_BYTES]);
+        D->ub_codes = (int64_t)D->h_ctr[VG_DICT_CODES] + (int64_t)D->h_ctr[VG_DICT_ROWS];
+        D->ub_used = (int64_t)D->h_ctr[VG_DICT_USED] + (int64_t)D->h_ctr[VG_DICT_BYTES];
     } else if (D->d.cap == 0) {
         dict_reserve(D, 0, 0);
     }

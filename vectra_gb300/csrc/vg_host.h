@@ -65,6 +65,7 @@ typedef struct {
     void *block;               /* device allocation holding uploaded data */
     int64_t row_base;          /* stream position of physical row 0 */
     int in_host;               /* columns are page-locked host memory read in place */
+    int64_t *str_chars;        /* n_cols: bytes of characters of each string column (or NULL) */
 } VgDBatch;
 
 /* Pulls the next batch of `child` with the columns flagged in need[]
@@ -108,9 +109,12 @@ VgDict *vg_dict_new(void);
 VgDict *vg_dict_new_kept(void);
 void vg_dict_free(VgDict *D);
 /* d_codes[p] for the logical rows p of string column c (insert: new
- * strings get the next codes; otherwise absent strings get -1) */
+ * strings get the next codes; otherwise absent strings get -1).
+ * chars_ub: an upper bound of the characters of those rows when the
+ * caller knows one (then room is made without reading the device's
+ * counters back), else -1. */
 void vg_dict_encode(VgDict *D, const VgCol *c, const int32_t *d_sel, int64_t n_logical, int insert,
-                    int64_t *d_codes);
+                    int64_t *d_codes, int64_t chars_ub);
 int64_t vg_dict_size(VgDict *D);
 const VgStrDict *vg_dict_device(VgDict *D);
 void vg_dict_order(VgDict *D, int32_t **d_perm, int64_t **d_rank);
