@@ -454,6 +454,14 @@ def sg_string_arena_resizes(E, temp_dir):  # test-groupby.R:101-131: many keys, 
             .summarise(temp_dir=temp_dir, s=("sum", "x"), si=("sum", "i"), n=("n",)).batches())
 
 
+def sg_zero_bytes(E, temp_dir):    # keys that differ only past a zero byte, or only in length
+    t = T(g=["ab", "ab\x00", "ab\x00\x00", "ab", "a\x00b", "", "\x00", "ab\x00", NA, "\x00\x00"],
+          x=[1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0, 8.0, 9.0, 10.0])
+    a = tbl(E, t).group_by("g").summarise(temp_dir=temp_dir, s=("sum", "x"), n=("n",)).batches()
+    b = tbl(E, t).filter(col("g") > "ab").batches() + tbl(E, t).filter(nchar(col("g")) >= 3).batches()
+    return a + b
+
+
 def sg_filter_on_string(E, temp_dir):      # a string predicate below a string key
     t = T(g=["apple", "pear", "apple", "fig", NA, "pear", "fig"], x=[1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0])
     return (tbl(E, t).filter(grepl("p", col("g")) | is_na(col("g"))).group_by("g")
@@ -549,7 +557,8 @@ def r_string_sort(E, seed, n, batch_rows):
 
 STRING_FILTER_CASES = [sf_nchar, sf_substr, sf_grepl, sf_compare_literal, sf_compare_columns, sf_substr_bounds,
                        sf_substr_filter, sf_nchar_filter, sf_passthrough]
-STRING_GROUP_CASES = [sg_string_key, sg_string_and_int_keys, sg_string_arena_resizes, sg_filter_on_string]
+STRING_GROUP_CASES = [sg_string_key, sg_string_and_int_keys, sg_string_arena_resizes, sg_filter_on_string,
+                      sg_zero_bytes]
 
 
 FILTER_CASES = [f_simple, f_equality, f_and_or_not, f_na_dropped, f_is_na, f_kleene, f_double_filter,
