@@ -552,6 +552,29 @@ __global__ void minmax_i64_kernel(VgCol c, int64_t n, long long *out) {
     }
 }
 
+// Pass 1 for general programs, whose rows cost far more than a range
+// test: one warp per keep word (32 rows), so that a batch of any size
+// spreads over every SM; each word's count is added to its 256-word
+// block's count (zeroed before the launch), the layout pass 2 reads.
+__global__ void __launch_bounds__(kThreads)
+keep_words_prog_kernel(const ProgArgs *ga, int64_t n_logical, const int32_t *sel, uint32_t *words,
+                       uint32_t *block_counts, uint32_t *err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t wi = ((int64_t)blockIdx.x * kThreads + threadIdx.x) >> 5;
+    const int64_t li = wi * 32 + lane;
+    bool keep = false;
+    if (li < n_logical) {
+        const int64_t p = sel ? (int64_t)sel[li] : li;
+        const Cell c = run_prog(ga->prog, ga->cols, p, err);
+        keep = c.ok && c.v;
+    }
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, keep);
+    if (lane == 0 && wi * 32 < n_logical) {
+        words[wi] = m;
+        if (m) atomicAdd(block_counts + wi / kThreads, (uint32_t)__popc(m));
+    }
+}
+
 template <bool kUseProg>
 int run_filter(const void *args, size_t args_bytes, int64_t n_logical, const int32_t *d_sel_in,
                int32_t *d_sel_out, int64_t *h_count, void *d_scratch, size_t scratch_bytes,
@@ -566,9 +589,17 @@ int run_filter(const void *args, size_t args_bytes, int64_t n_logical, const int
     if (check(cudaMemcpyAsync(fs.args, args, args_bytes, cudaMemcpyHostToDevice, s), "filter args")) return -1;
     if (check(cudaMemsetAsync(fs.err, 0, 4, s), "filter err")) return -1;
     vg_prof_begin(VG_PROF_FILTER, s);
-    { keep_words_kernel<kUseProg><<<n_blocks, kThreads, 0, s>>>(
-        (const PredArgs *)fs.args, (const ProgArgs *)fs.args, n_logical, d_sel_in,
-        fs.words, fs.counts, fs.err); vg_launch_counter++; }
+    if (kUseProg) {
+        const int64_t n_words = (n_logical + 31) / 32;
+        if (check(cudaMemsetAsync(fs.counts, 0, (size_t)n_blocks * 4, s), "filter counts")) return -1;
+        { keep_words_prog_kernel<<<(unsigned)((n_words + kThreads / 32 - 1) / (kThreads / 32)), kThreads, 0, s>>>(
+            (const ProgArgs *)fs.args, n_logical, d_sel_in, fs.words, fs.counts, fs.err); vg_launch_counter++; }
+    } else {
+        keep_words_kernel<false><<<n_blocks, kThreads, 0, s>>>(
+            (const PredArgs *)fs.args, (const ProgArgs *)fs.args, n_logical, d_sel_in,
+            fs.words, fs.counts, fs.err);
+        vg_launch_counter++;
+    }
     { compact_kernel<<<n_blocks, kThreads, 0, s>>>(n_logical, d_sel_in, fs.words, fs.counts,
                                                  n_blocks, d_sel_out, fs.total); vg_launch_counter++; }
     vg_prof_end(VG_PROF_FILTER, s);
