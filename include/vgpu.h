@@ -37,7 +37,9 @@ extern "C" {
 
 /* ---- drop-in node constructors -------------------------------------- */
 
-/* replaces src/filter.h:14 (FilterNode *filter_node_create) */
+/* replaces src/filter.h:14 (FilterNode *filter_node_create).  Predicates
+ * over int64, double, bool and string columns (comparisons, Kleene logic,
+ * is.na, arithmetic, nchar, substr, grepl with a fixed pattern). */
 FilterNode *filter_node_create(VecNode *child, VecExpr *predicate);
 
 /* replaces src/project.h:23 (ProjectNode *project_node_create) */
@@ -53,7 +55,9 @@ GroupAggNode *group_agg_node_create(VecNode *child, int n_keys,
                                     char **key_names, int n_aggs,
                                     AggSpec *agg_specs, const char *temp_dir);
 
-/* replaces src/join.h:76-78 (JoinNode *join_node_create) */
+/* replaces src/join.h:76-78 (JoinNode *join_node_create).  Keys of any
+ * type, string keys included (compared byte for byte); string columns are
+ * carried on both sides. */
 JoinNode *join_node_create(VecNode *left, VecNode *right, JoinKind kind,
                            int n_keys, JoinKey *keys,
                            const char *suffix_x, const char *suffix_y);
@@ -72,10 +76,12 @@ ScanNode *scan_node_create(const char *path, int *col_indices, int n_selected);
  * GPU.  The node keeps the reference's SortNode prefix and kind, reads its
  * keys (col_index, descending) only when it runs, and returns every row of
  * the child stably sorted -- NA last ascending, first descending, ties in
- * input order (src/sort.c:32-116) -- as one batch (an empty one for no
- * rows), then NULL.  temp_dir is kept for the struct's sake: nothing is
- * spilled, the rows stay in device memory.  String columns are an error.
- * Takes ownership of keys. */
+ * input order (src/sort.c:32-116); strings in memcmp order, the shorter
+ * first -- as one batch (an empty one for no rows), then NULL.  An input
+ * larger than a third of the free device memory (or VGPU_SORT_RUN_ROWS
+ * rows) is sorted in runs kept in host memory and merged back on the
+ * device by key range; temp_dir is kept for the struct's sake (nothing is
+ * written to disk).  Takes ownership of keys. */
 SortNode *sort_node_create(VecNode *child, int n_keys, SortKey *keys, const char *temp_dir);
 
 /* ---- data sources (no reference counterpart beyond ScanNode's role) -- */
