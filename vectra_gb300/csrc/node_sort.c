@@ -225,15 +225,16 @@ static void emit_rows(const VgCol *cols, int nc, const int32_t *perm, int64_t n,
 /* rows per run: VGPU_SORT_RUN_ROWS, else about a third of the free device
  * memory over the bytes a row takes on the device while it is sorted */
 static int64_t run_budget(const VecSchema *cs, int n_keys) {
+    const int64_t most = 2147483647;     /* a device sort orders at most 2^31-1 rows */
     const char *e = getenv("VGPU_SORT_RUN_ROWS");
-    if (e && atoll(e) > 0) return atoll(e);
+    if (e && atoll(e) > 0) return atoll(e) < most ? atoll(e) : most;
     size_t fr = 0, tot = 0;
-    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess || fr == 0) return (int64_t)1 << 40;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess || fr == 0) return most;
     size_t row = 64 + 40 * (size_t)n_keys;
     for (int c = 0; c < cs->n_cols; c++)
         row += 3 * elem(cs->col_types[c]) + 1 + (cs->col_types[c] == VEC_STRING ? 64 : 0);
     const int64_t r = (int64_t)(fr / 3 / row);
-    return r > 1024 ? r : 1024;
+    return r < 1024 ? 1024 : r > most ? most : r;
 }
 
 /* the order word of a valid fixed-width value, as the device sort forms it */
