@@ -1,8 +1,9 @@
 """The CPU oracle against the reference engine compiled from its own
 sources on randomly drawn plans: sizes (empty, one row, warp and batch
 edges), batch sizes, selection vectors, hash and sorted group paths, every
-join kind on direct-range and scattered keys, and join -> group_by plans
-with NA and repeated build keys.  Bit-exact, except double sums and means
+join kind on direct-range and scattered keys, join -> group_by plans
+with NA and repeated build keys, and plans over string columns (filters,
+group keys, join keys, sorts).  Bit-exact, except double sums and means
 (relative 1e-12: the reference sums in row order).  Runs where the
 reference checkout exists, like test_oracle_vs_ref.py."""
 import numpy as np
@@ -72,3 +73,30 @@ def test_random_join_then_group(master, oracle, ref):
     for _ in range(50):
         q = _join_agg_case(rng)
         cases.same_batches(q(oracle), q(ref), rtol=1e-12, tol_cols=FP)
+
+
+def _string_case(rng):
+    """Random plans over string columns: string filters, string group keys
+    (both paths), string join keys of every kind, sorts by strings."""
+    seed = int(rng.integers(0, 1 << 30))
+    n = int(rng.choice([0, 1, 2, 31, 64, 333, 1000, 3000]))
+    batch = int(rng.choice([1, 7, 32, 100, 1024]))
+    kind = int(rng.integers(0, 4))
+    if kind == 0:
+        sm = int(rng.integers(0, 2))
+        return lambda E: cases.r_string_filter(E, seed, n, batch, sm)
+    if kind == 1:
+        sm, td = int(rng.integers(0, 2)), bool(rng.integers(0, 2))
+        return lambda E: cases.r_string_group(E, seed, n, batch, sm, E.tmp if td else None)
+    if kind == 2:
+        jk = ["inner_join", "left_join", "semi_join", "anti_join", "full_join"][int(rng.integers(0, 5))]
+        return lambda E: cases.r_string_join(E, seed, n, batch, jk)
+    return lambda E: cases.r_string_sort(E, seed, n, batch)
+
+
+@pytest.mark.parametrize("master", range(4))
+def test_random_string_plans(master, oracle, ref):
+    rng = np.random.default_rng(3000 + master)
+    for _ in range(40):
+        q = _string_case(rng)
+        cases.same_batches(q(oracle), q(ref), rtol=1e-12, tol_cols=FP + ("s1",))
