@@ -164,3 +164,17 @@ def test_string_order_long_prefixes(G):
     for _ in range(3):
         got = tbl(G, t, batch_rows=100_000).arrange("g").batches()[0]["g"][0]
         assert list(got) == want
+
+
+@pytest.mark.parametrize("master", range(3))
+def test_random_string_plans(master, G, oracle):
+    """Randomly drawn plans over string columns (the oracle's fuzzing
+    against the reference draws the same kinds): sizes at warp and batch
+    edges, selection vectors, both group paths, every join kind, sorts."""
+    import sys
+    sys.path.insert(0, __import__("os").path.dirname(__file__))
+    from test_oracle_fuzz import _string_case, FP
+    rng = np.random.default_rng(5000 + master)
+    for _ in range(25):
+        q = _string_case(rng)
+        cases.same_batches(q(G), q(oracle), rtol=1e-12, tol_cols=FP + ("s1",))

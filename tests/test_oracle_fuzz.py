@@ -87,7 +87,7 @@ def _string_case(rng):
         return lambda E: cases.r_string_filter(E, seed, n, batch, sm)
     if kind == 1:
         sm, td = int(rng.integers(0, 2)), bool(rng.integers(0, 2))
-        return lambda E: cases.r_string_group(E, seed, n, batch, sm, E.tmp if td else None)
+        return lambda E: cases.r_string_group(E, seed, n, batch, sm, getattr(E, "tmp", "tmp") if td else None)
     if kind == 2:
         jk = ["inner_join", "left_join", "semi_join", "anti_join", "full_join"][int(rng.integers(0, 5))]
         return lambda E: cases.r_string_join(E, seed, n, batch, jk)
