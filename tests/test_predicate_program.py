@@ -391,3 +391,41 @@ def test_values_match_the_oracles_projection(seed, oracle):
             else:
                 assert s64(x) == want, (repr(e.kw), r, s64(x), want)
     assert done > 40
+
+
+def test_string_program_limits_and_errors():
+    """String literals go into the program's 512-byte pool (one that does
+    not fit is an error, not a truncation); strings mixed with numbers in
+    arithmetic or comparisons are the reference's coercion error
+    (src/coerce.c:7-16)."""
+    import vectra_gb300
+    from vectra_gb300.plan import grepl, nchar, substr
+    lib = vectra_gb300.load()
+    lib.vg_compile_prog.argtypes = [C.c_void_p, MAPFN, C.c_void_p, C.POINTER(Prog)]
+    lib.vg_compile_prog.restype = C.c_int
+    lib.vg_compile_error.restype = C.c_char_p
+    names = ["s", "i"]
+    types = [abi.VEC_STRING, abi.VEC_INT64]
+
+    def colmap(ctx, name, ty):
+        k = names.index(name.decode())
+        ty[0] = types[k]
+        return k
+    cmap = MAPFN(colmap)
+    schema = list(zip(names, types))
+
+    def compile_(e):
+        p = Prog()
+        rc = lib.vg_compile_prog(C.cast(e.to_c(schema), C.c_void_p), cmap, None, C.byref(p))
+        return rc, p, lib.vg_compile_error().decode()
+    rc, p, _ = compile_(col("s").eq("x" * 300) | grepl("y" * 200, col("s")))
+    assert rc == 0 and p.pool_n == 500
+    rc, _, msg = compile_(col("s").eq("x" * 300) | grepl("y" * 300, col("s")))
+    assert rc != 0 and "too long" in msg
+    for bad in (col("s") > col("i"), (col("s") + 1) > 0, col("s").eq(1)):
+        rc, _, msg = compile_(bad)
+        assert rc != 0 and "coerce" in msg, msg
+    rc, _, msg = compile_(nchar(col("i")) > 1)
+    assert rc != 0 and "nchar" in msg
+    rc, _, msg = compile_(substr(col("s"), col("s"), 2).eq("a"))
+    assert rc != 0 and "substr" in msg
