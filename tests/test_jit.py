@@ -76,3 +76,16 @@ def test_queue_only_behind_a_filter(shape, queued, tmp_path, monkeypatch):
     src = dump.read_text() if dump.exists() else ""
     assert src, "the compiled source was not written (already compiled in this process?)"
     assert ("#define VGJ_COMPACT %d\n" % queued) in src
+
+
+@pytest.mark.parametrize("shape", range(12))
+def test_launch_signature_premise(shape):
+    """The specialised kernel is looked up by a launch signature that
+    reduces pointers to set / unset and clears per-batch numbers; on every
+    self-test plan, changing all of those fields leaves the signature and
+    the generated source unchanged (vgpu_jit_sigcheck)."""
+    import ctypes as C
+    import vectra_gb300
+    lib = vectra_gb300.load()
+    lib.vgpu_jit_sigcheck.restype = C.c_int
+    assert lib.vgpu_jit_sigcheck(shape) == 0

@@ -530,8 +530,90 @@ namespace {
 
 // The compiled kernel of plan L (cached by its source), or null
 // (vgk_jit_error()).
+// The code-generation signature of a launch: the launch with every
+// pointer reduced to whether it is set and the per-batch numbers that the
+// kernel reads at run time (row counts and bases, capacities, the direct
+// table's minimum, partition bounds) cleared, plus S, vec and the shape.
+// gen_source reads pointers only to test them for NULL and those numbers
+// only as kernel parameters, so launches with one signature share one
+// source; the source (tens of kilobytes of text) is then generated and
+// looked up once per signature instead of once per launch.
+template <typename T> void set_flag(T *&p) { p = p ? (T *)(uintptr_t)1 : nullptr; }
+template <typename T> void shift_ptr(T *&p, uintptr_t d) { if (p) p = (T *)((uintptr_t)p + d); }
+
+std::string launch_signature(const VgAggLaunch &L, int S, bool vec, const Shape &sh) {
+    VgAggLaunch T;
+    memcpy(&T, &L, sizeof(T));
+    T.n_rows = T.sel_n = T.row_base = 0;
+    set_flag(T.sel);
+    for (int i = 0; i < VG_MAX_COLS; i++) {
+        set_flag(T.pcols[i].data);
+        set_flag(T.pcols[i].valid);
+        set_flag(T.bcols[i].data);
+        set_flag(T.bcols[i].valid);
+    }
+    T.jt.cap = 0;
+    T.jt.dmin = 0;
+    T.jt.n_build = 0;
+    set_flag(T.jt.slots);
+    set_flag(T.jt.state);
+    set_flag(T.jt.keys);
+    set_flag(T.jt.start);
+    set_flag(T.jt.count);
+    set_flag(T.jt.rows);
+    set_flag(T.jt.err);
+    T.gt.cap = 0;
+    set_flag(T.gt.state);
+    set_flag(T.gt.nullmask);
+    set_flag(T.gt.keys);
+    set_flag(T.gt.first_row);
+    for (int a = 0; a < VG_MAX_ACCS; a++) {
+        set_flag(T.gt.cnt[a]);
+        set_flag(T.gt.val[a]);
+        set_flag(T.gt.flags[a]);
+        set_flag(T.gt.lacc[a]);
+    }
+    set_flag(T.gt.n_used);
+    set_flag(T.gt.err);
+    set_flag(T.spill_rows);
+    set_flag(T.spill_rows_n);
+    set_flag(T.spill_cache);
+    set_flag(T.spill_cache_n);
+    set_flag(T.replay);
+    T.spill_rows_cap = T.spill_cache_cap = T.replay_n = T.batch_idx = T.li_base = 0;
+    T.dense_min = 0;
+    set_flag(T.jpay);
+    T.jpay_min = 0;
+    set_flag(T.po.rec);
+    set_flag(T.po.cursor);
+    set_flag(T.po.end);
+    set_flag(T.po.err);
+    set_flag(T.po.cta_off);
+    set_flag(T.po.start);
+    T.po.omin = 0;
+    T.po.shift = 0;
+    T.po.n_buckets = 0;
+    T.po.total = 0;
+    set_flag(T.defer_bits);
+    set_flag(T.defer_n);
+    T.defer_words = 0;
+    std::string sig((const char *)&T, sizeof(T));
+    const int extra[6] = {S, vec ? 1 : 0, sh.rows, sh.threads, sh.ctas, sh.pipe};
+    sig.append((const char *)extra, sizeof(extra));
+    return sig;
+}
+
+std::unordered_map<std::string, JitKernel *> g_by_sig;
+
 JitKernel *plan_kernel(const VgAggLaunch *L, int S, bool vec) {
-    std::string src = gen_source(*L, S, vec, plan_shape(*L));
+    const Shape sh = plan_shape(*L);
+    const std::string sig = launch_signature(*L, S, vec, sh);
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        auto hit = g_by_sig.find(sig);
+        if (hit != g_by_sig.end()) return hit->second;
+    }
+    std::string src = gen_source(*L, S, vec, sh);
     std::lock_guard<std::mutex> lock(g_mu);
     auto it = g_cache.find(src);
     if (it == g_cache.end()) {
@@ -549,6 +631,7 @@ JitKernel *plan_kernel(const VgAggLaunch *L, int S, bool vec) {
         }
         it = g_cache.emplace(src, k).first;
     }
+    g_by_sig.emplace(sig, &it->second);     // elements of g_cache never move
     return &it->second;
 }
 
@@ -943,8 +1026,10 @@ void pagg_plan(VgAggLaunch &L, int variant) {
 
 }  // namespace
 
-extern "C" int vgpu_jit_selftest(int shape, int *regs) {
-    static VgAggLaunch L;
+namespace {
+
+// The launches of the self-test shapes (no device memory behind them).
+int selftest_plan(VgAggLaunch &L, int shape) {
     memset(&L, 0, sizeof(L));
     static double dummy[4];
     L.cache_slots = 1024;
@@ -1067,7 +1152,77 @@ extern "C" int vgpu_jit_selftest(int shape, int *regs) {
         snprintf(g_jit_err, sizeof(g_jit_err), "no such self-test shape %d", shape);
         return -1;
     }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" int vgpu_jit_selftest(int shape, int *regs) {
+    static VgAggLaunch L;
+    if (selftest_plan(L, shape) != 0) return -1;
     return vgk_agg_jit_compile_only(&L, regs);
+}
+
+// The launch signature's premise, checked on a self-test shape (no device
+// needed): every field the signature reduces -- pointers to set / unset,
+// per-batch numbers -- changed to other values leaves the signature and
+// the generated source unchanged.  Returns 0, or 1 on a mismatch.
+extern "C" int vgpu_jit_sigcheck(int shape) {
+    static VgAggLaunch L, M;
+    if (selftest_plan(L, shape) != 0) return -1;
+    const int S = vgk_agg_jit_slots(&L);
+    const bool vec = vec_ok(L);
+    const Shape sh = plan_shape(L);
+    const std::string sig = launch_signature(L, S, vec, sh), src = gen_source(L, S, vec, sh);
+    for (int v = 1; v <= 3; v++) {
+        memcpy(&M, &L, sizeof(M));
+        // another non-NULL value for every pointer that is set (256-byte
+        // aligned, as device allocations are), NULL ones left NULL
+        const uintptr_t other = (uintptr_t)4096 * (uintptr_t)(v * 7919);
+        auto move = [&](auto *&ptr) { shift_ptr(ptr, other); };
+        move(M.sel);
+        for (int i = 0; i < VG_MAX_COLS; i++) {
+            move(M.pcols[i].data);
+            move(M.pcols[i].valid);
+            move(M.bcols[i].data);
+            move(M.bcols[i].valid);
+        }
+        move(M.jt.slots); move(M.jt.state); move(M.jt.keys); move(M.jt.start); move(M.jt.count); move(M.jt.rows);
+        move(M.jt.err);
+        move(M.gt.state); move(M.gt.nullmask); move(M.gt.keys); move(M.gt.first_row); move(M.gt.n_used);
+        move(M.gt.err);
+        for (int a = 0; a < VG_MAX_ACCS; a++) {
+            move(M.gt.cnt[a]); move(M.gt.val[a]); move(M.gt.flags[a]); move(M.gt.lacc[a]);
+        }
+        move(M.spill_rows); move(M.spill_rows_n); move(M.spill_cache); move(M.spill_cache_n); move(M.jpay);
+        move(M.po.rec); move(M.po.cursor); move(M.po.end); move(M.po.err); move(M.po.cta_off); move(M.po.start);
+        move(M.defer_bits); move(M.defer_n);
+        M.n_rows = 1000003 * v;
+        M.sel_n = 77 * v;
+        M.row_base = 123456789ll * v;
+        M.batch_idx = 5 * v;
+        M.li_base = 4096 * v;
+        M.spill_rows_cap = 65536 * v;
+        M.spill_cache_cap = 1024 * v;
+        M.dense_min = -17 * v;
+        M.jpay_min = 3 * v;
+        M.jt.cap = 1 << (10 + v);
+        M.jt.dmin = 9 * v;
+        M.jt.n_build = 999 * v;
+        M.gt.cap = 1 << (12 + v);
+        M.po.omin = 11ull * (uint64_t)v;
+        M.po.shift = 3 + v;
+        M.po.n_buckets = 16 << v;
+        M.po.total = 1000ull * (uint64_t)v;
+        M.defer_words = 100 * v;
+        const int S2 = vgk_agg_jit_slots(&M);
+        const bool vec2 = vec_ok(M);
+        const Shape sh2 = plan_shape(M);
+        if (S2 != S || vec2 != vec) return 1;
+        if (launch_signature(M, S2, vec2, sh2) != sig) return 1;
+        if (gen_source(M, S2, vec2, sh2) != src) return 1;
+    }
+    return 0;
 }
 
 // Partitioned-aggregation reducer of representative plans (no device
