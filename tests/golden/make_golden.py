@@ -34,6 +34,36 @@ def all_cases():
             yield "r_group[%d,%d,%s]" % (n, batch, mode), (
                 lambda E, n=n, b=batch, m=mode: cases.r_group(E, n + 1, n, b, 1, None if m == "hash" else E.tmp))
         yield "r_sort[%d,%d]" % (n, batch), (lambda E, n=n, b=batch: cases.r_sort(E, n + 2, n, b))
+    # string columns (filters, joins, sorts, group keys on both paths)
+    for f in cases.STRING_FILTER_CASES + cases.STRING_JOIN_CASES + [cases.ss_string_keys]:
+        yield f.__name__, (lambda E, f=f: f(E))
+    for f in cases.STRING_GROUP_CASES:
+        for mode in ("sorted", "hash"):
+            yield "%s[%s]" % (f.__name__, mode), (lambda E, f=f, m=mode: f(E, None if m == "hash" else E.tmp))
+    for n, batch in [(33, 32), (700, 64)]:
+        yield "r_string_filter[%d,%d]" % (n, batch), (lambda E, n=n, b=batch: cases.r_string_filter(E, n, n, b, 1))
+        for mode in ("sorted", "hash"):
+            yield "r_string_group[%d,%d,%s]" % (n, batch, mode), (
+                lambda E, n=n, b=batch, m=mode: cases.r_string_group(E, n, n, b, 1, None if m == "hash" else E.tmp))
+        for kind in ("left_join", "full_join"):
+            yield "r_string_join[%d,%d,%s]" % (n, batch, kind), (
+                lambda E, n=n, b=batch, k=kind: cases.r_string_join(E, n, n, b, k))
+        yield "r_string_sort[%d,%d]" % (n, batch), (lambda E, n=n, b=batch: cases.r_string_sort(E, n, n, b))
+
+
+def pack_strings(v):
+    """A string column as (offsets int64, bytes uint8): object arrays do
+    not go into the fixture file."""
+    enc = [str(x).encode("utf-8", "surrogateescape") for x in v]
+    offs = np.zeros(len(enc) + 1, np.int64)
+    offs[1:] = np.cumsum([len(e) for e in enc])
+    return offs, np.frombuffer(b"".join(enc), dtype=np.uint8).copy()
+
+
+def unpack_strings(offs, data):
+    b = data.tobytes()
+    return np.array([b[offs[i]:offs[i + 1]].decode("utf-8", "surrogateescape") for i in range(len(offs) - 1)],
+                    dtype=object)
 
 
 def write_vtr_ref(path, table, batch_rows):
@@ -96,7 +126,12 @@ def main():
         manifest[name] = [list(b.keys()) for b in batches]
         for bi, b in enumerate(batches):
             for col, (v, m) in b.items():
-                arrays["%s|%d|%s|v" % (name, bi, col)] = v
+                if v.dtype == object:
+                    offs, data = pack_strings(v)
+                    arrays["%s|%d|%s|o" % (name, bi, col)] = offs
+                    arrays["%s|%d|%s|s" % (name, bi, col)] = data
+                else:
+                    arrays["%s|%d|%s|v" % (name, bi, col)] = v
                 arrays["%s|%d|%s|m" % (name, bi, col)] = m
     np.savez_compressed(os.path.join(HERE, "ref_cases.npz"), **arrays)
     with open(os.path.join(HERE, "ref_cases.json"), "w") as f:

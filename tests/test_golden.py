@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import cases
-from golden.make_golden import all_cases
+from golden.make_golden import all_cases, unpack_strings
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 NPZ = os.path.join(HERE, "golden", "ref_cases.npz")
@@ -23,7 +23,12 @@ def load_golden(name):
     z = np.load(NPZ, allow_pickle=False)
     out = []
     for bi, cols in enumerate(manifest[name]):
-        out.append({c: (z["%s|%d|%s|v" % (name, bi, c)], z["%s|%d|%s|m" % (name, bi, c)]) for c in cols})
+        b = {}
+        for c in cols:
+            key = "%s|%d|%s|" % (name, bi, c)
+            v = unpack_strings(z[key + "o"], z[key + "s"]) if key + "o" in z.files else z[key + "v"]
+            b[c] = (v, z[key + "m"])
+        out.append(b)
     return out
 
 
