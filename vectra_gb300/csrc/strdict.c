@@ -75,7 +75,8 @@ static void dict_read(VgDict *D) {
 static void *grow(VgDict *D, void *old, size_t used, size_t bytes) {
     void *p = dalloc(D, bytes);
     if (old && used) {
-        cudaMemcpyAsync(p, old, used, cudaMemcpyDeviceToDevice, (cudaStream_t)vg_stream());
+        const cudaError_t e = cudaMemcpyAsync(p, old, used, cudaMemcpyDeviceToDevice, (cudaStream_t)vg_stream());
+        if (e != cudaSuccess) vg_fail("string dictionary: growing copy failed: %s", cudaGetErrorString(e));
     }
     vg_dfree(old);
     return p;
